@@ -1,0 +1,392 @@
+"""Benchmark: FP64 Ax=b solves/s (dgetrf + dgetrs) on GB300, plus sub-benchmarks.
+
+Workload (one "step"): the plain-FP64 LU + solve configuration -- n=8192,
+column-major A with entries uniform[-1,1] and the diagonal shifted by +n/4,
+one right-hand side b = A x_true -- factorised with flens_gb300_dgetrf and
+solved with flens_gb300_dgetrs on the device, A restored from a pristine copy
+at the start of every step (inside the timed region).  A is 512 MiB, larger
+than L2, so no L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints ONE JSON line on rank 0.  value = solves/s (whole job), e2e = the same
+metric through the Fortran-ABI dgesv_ with pinned host buffers (host<->device
+copies inside the timed region), roofline = the dominant kernel against a
+measured FP64 peak, cpu_baseline = the oracle CPU path on a bounded sample.
+With --impl reference the reference's CPU implementation (oracle/_ref when it
+was built here, else the bitwise-identical C restatement) is timed on all host
+cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Ax=b solves/s at FP64 accuracy (dgetrf+dgetrs, n=8192, 1 rhs)"
+UNIT = "solves/s"
+NB = 64
+
+
+def lu_block_flops(n: int, nblocks: int | None = None) -> float:
+    """Flops of the blocked right-looking LU (block 64), per block step, summed
+    over the first nblocks steps: panel r*w^2 + trsm w^2(r-w) + update 2(r-w)^2 w."""
+    fl, b, j = 0.0, 0, 0
+    while j < n and (nblocks is None or b < nblocks):
+        r = n - j
+        w = min(NB, r)
+        fl += r * w * w + w * w * (r - w) + 2.0 * (r - w) * (r - w) * w
+        j += NB
+        b += 1
+    return fl
+
+
+# ------------------------------------------------------------- clocks --
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------ reference arm --
+def reference_arm(args, rank: int) -> None:
+    if rank != 0:
+        return
+    import oracle
+    n = args.n
+    threads = os.cpu_count() or 1
+    kind = "port"
+    # the C restatement is bitwise identical to the reference's own trf
+    # (pinned by tests/test_oracle_pin.py); oracle/_ref is only on machines
+    # that hold the FLENS sources, and has no partial-factorisation entry.
+    port = oracle.Port()
+    steps_blocks = 1
+    f_sample = lu_block_flops(n, steps_blocks)
+    f_total = lu_block_flops(n) + 2.0 * n * n
+    for _ in range(args.warmup):
+        port.time_dgetrf_steps(n, steps_blocks, threads, seed=7)
+    times = []
+    for s in range(args.steps):
+        t, _ = port.time_dgetrf_steps(n, steps_blocks, threads, seed=11 + s)
+        times.append(t)
+    # each thread factorised its own copy: `threads` samples per wall time
+    per_solve_s = statistics.mean(times) * f_total / f_sample
+    value = threads / per_solve_s
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * statistics.mean(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (splitmix64 uniform[-1,1] + n/4 diagonal, seeded)",
+        "config": {"workload": f"dgetrf+dgetrs n={n} 1 rhs FP64 column-major", "n": n,
+                   "nrhs": 1, "l2": "input 512 MiB > L2"},
+        "cpu_baseline": {
+            "value": value, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": (f"each step: {threads} threads each run the first {steps_blocks} block step "
+                       f"(panel+laswp+trsm+trailing gemm, nb=64) of the n={n} LU on its own copy; "
+                       f"scaled by flops {f_total:.3e}/{f_sample:.3e}")},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------ our arm --
+def make_inputs(torch, n, seed, dev):
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    A0 = torch.rand((n, n), generator=g, dtype=torch.float64, device=dev).mul_(2).sub_(1)
+    A0.diagonal().add_(n / 4.0)
+    A0 = A0.t()  # column-major view: stride(0) == 1
+    x_true = torch.rand((n, 1), generator=g, dtype=torch.float64, device=dev).mul_(2).sub_(1)
+    b0 = A0 @ x_true
+    return A0, x_true, b0
+
+
+def fp64_peak(torch, dev):
+    """cuBLAS FP64 GEMM throughput (TFLOP/s), best of 3 at 8192^3, as the
+    measured FP64 roofline for this GPU."""
+    n = 8192
+    a = torch.rand((n, n), dtype=torch.float64, device=dev)
+    b = torch.rand((n, n), dtype=torch.float64, device=dev)
+    c = a @ b
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        c = a @ b
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b, c
+    return best
+
+
+def gemm_subbench(torch, fg, dev, reps=10):
+    """Config 1: C = 1.5*A*B + 0.5*C, M=N=K=1024 FP64, through flens_gb300_dgemm.
+    L2 is flushed (a 256 MiB write) between timed repetitions."""
+    n = 1024
+    g = torch.Generator(device=dev)
+    g.manual_seed(3)
+    A = torch.rand((n, n), generator=g, dtype=torch.float64, device=dev).t()
+    B = torch.rand((n, n), generator=g, dtype=torch.float64, device=dev).t()
+    C0 = torch.rand((n, n), generator=g, dtype=torch.float64, device=dev).t()
+    C = fg.to_colmajor(C0.clone())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(3):
+        fg.dgemm_dev("N", "N", 1.5, A, B, 0.5, C)
+    torch.cuda.synchronize()
+    tot = 0.0
+    for _ in range(reps):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fg.dgemm_dev("N", "N", 1.5, A, B, 0.5, C)
+        e1.record()
+        e1.synchronize()
+        tot += e0.elapsed_time(e1)
+    ms = tot / reps
+    return {"workload": "dgemm 1024^3 alpha=1.5 beta=0.5 FP64", "ms": ms,
+            "tflops": 2.0 * n ** 3 / (ms * 1e-3) / 1e12, "l2": "flushed between reps"}
+
+
+def our_arm(args, rank: int, world: int) -> None:
+    import numpy as np
+    import torch
+    import flens_gb300 as fg
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    n = args.n
+    stream = torch.cuda.current_stream()
+    A0, x_true, b0 = make_inputs(torch, n, 20261203 + rank, dev)
+    A = fg.to_colmajor(A0.clone())
+    b = b0.clone()
+    ipiv = torch.zeros(n, dtype=torch.int32, device=dev)
+    info = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def step():
+        A.copy_(A0)
+        b.copy_(b0)
+        fg.dgetrf_dev(A, ipiv, info, stream)
+        fg.dgetrs_dev("N", A, ipiv, b, stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    fg.sync(stream)
+
+    # -- timed region
+    fg.timing_enable(True)
+    launches0 = fg.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = fg.launch_count() - launches0
+    ms_total = e0.elapsed_time(e1)
+    fam = fg.timing_read()
+    fg.timing_enable(False)
+    fg.sync(stream)
+    if dist:
+        t = torch.tensor([ms_total], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+
+    # -- accuracy of the last solve
+    inf = int(info.item())
+    piv = ipiv.cpu().numpy()
+    pivots_identity = bool(np.array_equal(piv, np.arange(1, n + 1)))
+    x = b
+    r = b0 - A0 @ x
+    eps = float(np.finfo(np.float64).eps)
+    anorm = A0.abs().sum(0).max().item()
+    berr_solve = (r.abs().max() / (anorm * x.abs().max() + b0.abs().max())).item()
+    fwd = ((x - x_true).abs().max() / x_true.abs().max()).item()
+
+    value = world * args.steps / (ms_total * 1e-3)
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (torch seeded uniform[-1,1] + n/4 diagonal; b = A x_true)",
+        "config": {"workload": f"dgetrf+dgetrs n={n} 1 rhs FP64 column-major",
+                   "n": n, "nrhs": 1, "nb": NB, "parallelism": f"replicas x{world}",
+                   "l2": "input 512 MiB > L2 (no flush)",
+                   "step": "A,b restored from pristine copies + dgetrf + dgetrs"},
+        "gpu_launches": launches,
+        "accuracy": {"info": inf, "pivots_identity": pivots_identity,
+                     "backward_error_normwise": berr_solve,
+                     "backward_error_over_n_eps": berr_solve / (n * eps),
+                     "forward_error_vs_x_true": fwd},
+        "clocks": clk.summary(),
+        "kernels": {k: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps,
+                        "tflops": (v["flops"] / (v["ms"] * 1e-3) / 1e12) if v["ms"] > 0 else None}
+                    for k, v in fam.items()},
+    }
+
+    if rank == 0:
+        # -- dominant kernel vs the measured FP64 peak
+        peak = None if args.quick else fp64_peak(torch, dev)
+        dom = max(fam.items(), key=lambda kv: kv[1]["ms"])[0] if fam else None
+        if dom:
+            d = fam[dom]
+            achieved = d["flops"] / (d["ms"] * 1e-3) / 1e12
+            traffic = None
+            tpath = os.path.join(ROOT, "profiles", "traffic.json")
+            if os.path.exists(tpath):
+                traffic = json.load(open(tpath)).get(f"{dom}@n={n}")
+            result["roofline"] = {
+                "kernel": dom, "bound": "tensor", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None,
+                "traffic": traffic,
+                "peak_source": "cuBLAS FP64 dgemm 8192^3 measured in this run (MEASURED_PEAKS.json "
+                               "has no FP64 entry; tcgen05 has no f64 kind)",
+                "share_of_step": d["ms"] / ms_total,
+                "algorithmic": "2*m*n*k flops per trailing-update/trsm GEMM launch"}
+        if not args.quick:
+            result["gemm_fp64_config1"] = gemm_subbench(torch, fg, dev)
+        # -- e2e through the Fortran ABI with pinned host buffers
+        if not args.no_e2e:
+            result["e2e"] = e2e_dgesv(torch, fg, A0, b0, args)
+        # -- CPU baseline (oracle C restatement, 1 thread, bounded sample)
+        if not args.no_cpu:
+            result["cpu_baseline"] = cpu_baseline(n)
+        print(json.dumps(result), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def e2e_dgesv(torch, fg, A0, b0, args):
+    import ctypes
+    import numpy as np
+    n = A0.shape[0]
+    hA0 = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+    hA0.copy_(A0.t())                     # row-major storage of A^T == column-major A
+    hb0 = b0.cpu()
+    hA = torch.empty_like(hA0, pin_memory=True)
+    hb = torch.empty((n,), dtype=torch.float64, pin_memory=True)
+    hpiv = torch.zeros(n, dtype=torch.int32, pin_memory=True)
+    L = fg.lib()
+    i = lambda v: ctypes.byref(ctypes.c_int(v))
+    dptr = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    iptr = ctypes.cast(hpiv.data_ptr(), ctypes.POINTER(ctypes.c_int))
+    info = ctypes.c_int(0)
+    times = []
+    for s in range(args.warmup + args.steps):
+        hA.copy_(hA0)
+        hb.copy_(hb0[:, 0])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        L.dgesv_(i(n), i(1), dptr(hA), i(n), iptr, dptr(hb), i(n), ctypes.byref(info))
+        t1 = time.perf_counter()
+        if s >= args.warmup:
+            times.append(t1 - t0)
+    x = hb.numpy()
+    ok = info.value == 0 and bool(np.all(np.isfinite(x)))
+    return {"value": len(times) / sum(times), "unit": UNIT,
+            "h2d_bytes_per_step": 8 * n * n + 8 * n,
+            "d2h_bytes_per_step": 8 * n * n + 8 * n + 4 * n,
+            "api": "dgesv_ (Fortran ABI, host pointers, pinned)", "ok": ok,
+            "ms_per_step": 1000.0 * sum(times) / len(times)}
+
+
+def cpu_baseline(n):
+    import oracle
+    port = oracle.Port()
+    nblocks = 2
+    t, f_sample = port.time_dgetrf_steps(n, nblocks, 1, seed=5)
+    f_total = lu_block_flops(n) + 2.0 * n * n
+    per_solve = t * f_total / f_sample
+    return {"value": 1.0 / per_solve, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": (f"first {nblocks} block steps (nb=64) of the n={n} LU on 1 thread, "
+                       f"{t:.1f} s, scaled by flops {f_total:.3e}/{f_sample:.3e}"),
+            "gflops": f_sample / t / 1e9}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--quick", action="store_true", help="skip peak and sub-benchmarks")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        reference_arm(args, rank)
+    else:
+        our_arm(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,272 @@
+"""flens_gb300 -- GB300-native dense GEMM / TRSM / LU behind FLENS's interfaces.
+
+The product is the C-ABI shared library ``libflens_gb300.so`` (CUDA for
+sm_103a, declared in ``include/flens_gb300.h``).  This module is a thin ctypes
+binding over that library, used by the tests and the benchmark and by Python
+callers:
+
+* ``lib()`` -- the loaded ``ctypes.CDLL`` (raises if the library is missing:
+  there is no CPU fallback).
+* Fortran-ABI wrappers on host numpy arrays (column-major): :func:`dgemm`,
+  :func:`dtrsm`, :func:`dgetrf`, :func:`dgetrs`, :func:`dgesv`.  They call the
+  exported ``dgemm_``, ``dtrsm_``, ... exactly as a Fortran or C caller would.
+* Device wrappers on torch CUDA tensors (column-major = ``tensor.t()`` of a
+  contiguous row-major tensor, or any tensor with stride(0)==1):
+  :func:`dgemm_dev`, :func:`dtrsm_dev`, :func:`dgetrf_dev`, :func:`dgetrs_dev`,
+  :func:`dgesv_dev`.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libflens_gb300.so")
+
+ERR_CUDA = -1001
+ERR_TIMEOUT = -1002
+ERR_NO_DEVICE = -1003
+ERR_ALLOC = -1004
+ERR_UNSUPPORTED = -1005
+ERR_NOT_CONVERGED = -1006
+
+_lib = None
+_ip = ctypes.POINTER(ctypes.c_int)
+_dp = ctypes.POINTER(ctypes.c_double)
+_c = ctypes.c_char
+_i = ctypes.c_int
+_d = ctypes.c_double
+_v = ctypes.c_void_p
+
+
+class FlensGB300Error(RuntimeError):
+    def __init__(self, code: int, where: str):
+        msg = lib().flens_gb300_last_error().decode(errors="replace")
+        super().__init__(f"{where} returned {code}: {msg}")
+        self.code = code
+
+
+def build_library() -> str:
+    """Compile libflens_gb300.so (nvcc, sm_103a); see flens_gb300/build.py."""
+    from . import build as _b
+    return _b.build()
+
+
+def lib() -> ctypes.CDLL:
+    """Load libflens_gb300.so (building it first if only the sources exist)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with "
+            "`python -c 'import __graft_entry__ as g; g.build()'` (nvcc for sm_103a)")
+    L = ctypes.CDLL(LIB_PATH, mode=ctypes.RTLD_GLOBAL)
+    cp = ctypes.c_char_p
+    L.dgemm_.argtypes = [cp, cp, _ip, _ip, _ip, _dp, _dp, _ip, _dp, _ip, _dp, _dp, _ip]
+    L.dgemm_.restype = None
+    L.dtrsm_.argtypes = [cp, cp, cp, cp, _ip, _ip, _dp, _dp, _ip, _dp, _ip]
+    L.dtrsm_.restype = None
+    L.dgetrf_.argtypes = [_ip, _ip, _dp, _ip, _ip, _ip]
+    L.dgetrf_.restype = None
+    L.dgetrs_.argtypes = [cp, _ip, _ip, _dp, _ip, _ip, _dp, _ip, _ip]
+    L.dgetrs_.restype = None
+    L.dgesv_.argtypes = [_ip, _ip, _dp, _ip, _ip, _dp, _ip, _ip]
+    L.dgesv_.restype = None
+    L.flens_gb300_dgemm.argtypes = [_c, _c, _i, _i, _i, _d, _v, _i, _v, _i, _d, _v, _i, _v]
+    L.flens_gb300_dtrsm.argtypes = [_c, _c, _c, _c, _i, _i, _d, _v, _i, _v, _i, _v]
+    L.flens_gb300_dgetrf.argtypes = [_i, _i, _v, _i, _v, _v, _v]
+    L.flens_gb300_dgetrs.argtypes = [_c, _i, _i, _v, _i, _v, _v, _i, _v]
+    L.flens_gb300_dgesv.argtypes = [_i, _i, _v, _i, _v, _v, _i, _v, _v]
+    L.flens_gb300_sync.argtypes = [_v]
+    for f in ("flens_gb300_dgemm", "flens_gb300_dtrsm", "flens_gb300_dgetrf",
+              "flens_gb300_dgetrs", "flens_gb300_dgesv", "flens_gb300_sync"):
+        getattr(L, f).restype = _i
+    L.flens_gb300_last_error.restype = ctypes.c_char_p
+    L.flens_gb300_last_error.argtypes = []
+    L.flens_gb300_xerbla_calls.restype = _i
+    L.flens_gb300_xerbla_info.restype = _i
+    L.flens_gb300_xerbla_name.restype = ctypes.c_char_p
+    L.flens_gb300_version.restype = _i
+    L.flens_gb300_launch_count.restype = ctypes.c_longlong
+    L.flens_gb300_launch_count.argtypes = []
+    L.flens_gb300_timing_enable.argtypes = [_i]
+    L.flens_gb300_timing_enable.restype = None
+    L.flens_gb300_timing_read.argtypes = [_i, _dp, ctypes.POINTER(ctypes.c_longlong), _dp, _dp]
+    L.flens_gb300_timing_read.restype = _i
+    L.flens_gb300_family_name.argtypes = [_i]
+    L.flens_gb300_family_name.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return lib().flens_gb300_last_error().decode(errors="replace")
+
+
+# ------------------------------------------------------ instrumentation ---
+N_FAMILIES = 8
+
+
+def launch_count() -> int:
+    """Kernel launches issued by the library since it was loaded."""
+    return int(lib().flens_gb300_launch_count())
+
+
+def timing_enable(on: bool = True) -> None:
+    """Per-launch CUDA-event timing on the launching stream (clears totals)."""
+    lib().flens_gb300_timing_enable(1 if on else 0)
+
+
+def timing_read() -> dict:
+    """{family: {ms, launches, flops, bytes}} since timing_enable (synchronises)."""
+    out = {}
+    for f in range(N_FAMILIES):
+        ms, fl, by = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        cnt = ctypes.c_longlong()
+        lib().flens_gb300_timing_read(f, ctypes.byref(ms), ctypes.byref(cnt), ctypes.byref(fl),
+                                      ctypes.byref(by))
+        if cnt.value:
+            name = lib().flens_gb300_family_name(f).decode()
+            out[name] = {"ms": ms.value, "launches": cnt.value, "flops": fl.value,
+                         "bytes": by.value}
+    return out
+
+
+# ---------------------------------------------------------- host (numpy) ---
+def _ref(v, t):
+    return ctypes.byref(t(v))
+
+
+def _fd(a: np.ndarray):
+    if a.dtype != np.float64 or not a.flags.f_contiguous:
+        raise ValueError("expected a Fortran-ordered float64 array")
+    return a.ctypes.data_as(_dp)
+
+
+def dgemm(transA: str, transB: str, alpha: float, A: np.ndarray, B: np.ndarray,
+          beta: float, C: np.ndarray) -> np.ndarray:
+    """C <- beta*C + alpha*op(A)*op(B) through dgemm_ (in place on C)."""
+    m, n = C.shape
+    k = A.shape[1] if transA.upper() == "N" else A.shape[0]
+    lib().dgemm_(transA.encode(), transB.encode(), _ref(m, _i), _ref(n, _i), _ref(k, _i),
+                 _ref(alpha, _d), _fd(A), _ref(max(1, A.shape[0]), _i), _fd(B),
+                 _ref(max(1, B.shape[0]), _i), _ref(beta, _d), _fd(C), _ref(max(1, m), _i))
+    return C
+
+
+def dtrsm(side: str, uplo: str, transA: str, diag: str, alpha: float, A: np.ndarray,
+          B: np.ndarray) -> np.ndarray:
+    m, n = B.shape
+    lib().dtrsm_(side.encode(), uplo.encode(), transA.encode(), diag.encode(),
+                 _ref(m, _i), _ref(n, _i), _ref(alpha, _d), _fd(A),
+                 _ref(max(1, A.shape[0]), _i), _fd(B), _ref(max(1, m), _i))
+    return B
+
+
+def dgetrf(A: np.ndarray):
+    """In-place LU through dgetrf_; returns (ipiv 1-based int32, info)."""
+    m, n = A.shape
+    piv = np.zeros(max(1, min(m, n)), dtype=np.int32)
+    info = ctypes.c_int(0)
+    lib().dgetrf_(_ref(m, _i), _ref(n, _i), _fd(A), _ref(max(1, m), _i),
+                  piv.ctypes.data_as(_ip), ctypes.byref(info))
+    return piv[: min(m, n)], info.value
+
+
+def dgetrs(trans: str, LU: np.ndarray, ipiv: np.ndarray, B: np.ndarray):
+    n = LU.shape[0]
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    info = ctypes.c_int(0)
+    lib().dgetrs_(trans.encode(), _ref(n, _i), _ref(B.shape[1], _i), _fd(LU),
+                  _ref(max(1, n), _i), ipiv.ctypes.data_as(_ip), _fd(B),
+                  _ref(max(1, n), _i), ctypes.byref(info))
+    return B, info.value
+
+
+def dgesv(A: np.ndarray, B: np.ndarray):
+    n = A.shape[0]
+    piv = np.zeros(max(1, n), dtype=np.int32)
+    info = ctypes.c_int(0)
+    lib().dgesv_(_ref(n, _i), _ref(B.shape[1], _i), _fd(A), _ref(max(1, n), _i),
+                 piv.ctypes.data_as(_ip), _fd(B), _ref(max(1, n), _i), ctypes.byref(info))
+    return piv[:n], info.value
+
+
+# -------------------------------------------------------- device (torch) ---
+def _colmajor(t):
+    """(pointer, rows, cols, ld) of a column-major CUDA float64 tensor."""
+    if t.dim() != 2 or t.stride(0) != 1:
+        raise ValueError("expected a 2-D column-major tensor (stride(0) == 1)")
+    return t.data_ptr(), t.shape[0], t.shape[1], max(1, t.stride(1), t.shape[0])
+
+
+def _stream(stream):
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def _check(code: int, where: str) -> None:
+    if code != 0:
+        raise FlensGB300Error(code, where)
+
+
+def colmajor_empty(m: int, n: int, dtype=None, device="cuda"):
+    """A column-major (m x n) tensor: storage of an (n x m) row-major one, transposed."""
+    import torch
+    return torch.empty((n, m), dtype=dtype or torch.float64, device=device).t()
+
+
+def to_colmajor(t):
+    return t.t().contiguous().t()
+
+
+def dgemm_dev(transA, transB, alpha, A, B, beta, C, stream=None):
+    pa, ra, ca, lda = _colmajor(A)
+    pb, rb, cb, ldb = _colmajor(B)
+    pc, m, n, ldc = _colmajor(C)
+    k = ca if transA.upper() == "N" else ra
+    _check(lib().flens_gb300_dgemm(transA.encode(), transB.encode(), m, n, k, alpha, pa, lda,
+                                   pb, ldb, beta, pc, ldc, _stream(stream)), "flens_gb300_dgemm")
+    return C
+
+
+def dtrsm_dev(side, uplo, transA, diag, alpha, A, B, stream=None):
+    pa, ra, ca, lda = _colmajor(A)
+    pb, m, n, ldb = _colmajor(B)
+    _check(lib().flens_gb300_dtrsm(side.encode(), uplo.encode(), transA.encode(), diag.encode(),
+                                   m, n, alpha, pa, lda, pb, ldb, _stream(stream)),
+           "flens_gb300_dtrsm")
+    return B
+
+
+def dgetrf_dev(A, ipiv, info, stream=None):
+    """In-place LU of a column-major CUDA tensor; ipiv/info are int32 CUDA tensors."""
+    pa, m, n, lda = _colmajor(A)
+    _check(lib().flens_gb300_dgetrf(m, n, pa, lda, ipiv.data_ptr(), info.data_ptr(),
+                                    _stream(stream)), "flens_gb300_dgetrf")
+    return A
+
+
+def dgetrs_dev(trans, LU, ipiv, B, stream=None):
+    pa, n, _, lda = _colmajor(LU)
+    pb, _, nrhs, ldb = _colmajor(B)
+    _check(lib().flens_gb300_dgetrs(trans.encode(), n, nrhs, pa, lda, ipiv.data_ptr(), pb, ldb,
+                                    _stream(stream)), "flens_gb300_dgetrs")
+    return B
+
+
+def dgesv_dev(A, ipiv, B, info, stream=None):
+    pa, n, _, lda = _colmajor(A)
+    pb, _, nrhs, ldb = _colmajor(B)
+    _check(lib().flens_gb300_dgesv(n, nrhs, pa, lda, ipiv.data_ptr(), pb, ldb, info.data_ptr(),
+                                   _stream(stream)), "flens_gb300_dgesv")
+    return B
+
+
+def sync(stream=None) -> None:
+    _check(lib().flens_gb300_sync(_stream(stream)), "flens_gb300_sync")

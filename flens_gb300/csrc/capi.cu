@@ -1,0 +1,437 @@
+// capi.cu -- the C ABI of the library.
+//
+// 1. Fortran-ABI drop-ins with the reference's argument checks and error
+//    convention (xerbla_, then return; LAPACK routines also set INFO):
+//      dgemm_   flens/blas/interface/blas/gemm.cc:120-230
+//      dtrsm_   flens/blas/interface/blas/trsm.cc:90-166
+//      dgetrf_  flens/lapack/interface/src/getrf.cc:10-45
+//      dgetrs_  flens/lapack/interface/src/getrs.cc:13-53
+//      dgesv_   flens/lapack/interface/src/gesv.cc:13-49
+//    They take HOST pointers (as the reference does), copy the operands to
+//    the device, run the GPU path and copy the results back before
+//    returning.  Device (or managed) pointers are also accepted and used in
+//    place.
+// 2. flens_gb300_* device-pointer entry points, asynchronous on a caller
+//    stream: the fast path for callers that keep matrices resident in HBM.
+#include "common.cuh"
+
+#include <ctype.h>
+#include <stdio.h>
+#include <string.h>
+#include <algorithm>
+
+using namespace fg;
+
+// ------------------------------------------------------------ xerbla ----
+// Weak default: callers (or a Fortran runtime) may provide their own.  Like
+// the Netlib routine it reports the routine name and the parameter position;
+// unlike it, it does not stop the program.
+static thread_local char g_xerbla_name[8];
+static thread_local int g_xerbla_info;
+static thread_local int g_xerbla_calls;
+
+extern "C" __attribute__((weak, visibility("default"))) void xerbla_(const char *name,
+                                                                    const int *info, int len) {
+    (void)len;
+    char buf[8] = {0};
+    for (int i = 0; i < 6 && name[i]; ++i) buf[i] = name[i];
+    fprintf(stderr, " ** On entry to %6s parameter number %2d had an illegal value\n", buf, *info);
+}
+
+static void report_xerbla(const char *name, int info) {
+    memset(g_xerbla_name, 0, sizeof g_xerbla_name);
+    for (int i = 0; i < 6 && name[i]; ++i) g_xerbla_name[i] = name[i];
+    g_xerbla_info = info;
+    ++g_xerbla_calls;
+    set_last_error("argument %d of %s had an illegal value", info, g_xerbla_name);
+    xerbla_(name, &info, 6);
+}
+
+FG_API int flens_gb300_xerbla_calls(void) { return g_xerbla_calls; }
+FG_API int flens_gb300_xerbla_info(void) { return g_xerbla_info; }
+FG_API const char *flens_gb300_xerbla_name(void) { return g_xerbla_name; }
+
+// --------------------------------------------------------- host staging --
+namespace {
+
+struct HostStage {
+    cudaStream_t stream = nullptr;
+    void *buf[4] = {nullptr, nullptr, nullptr, nullptr};
+    size_t bytes[4] = {0, 0, 0, 0};
+    ~HostStage() {
+        for (int i = 0; i < 4; ++i)
+            if (buf[i]) cudaFree(buf[i]);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+thread_local HostStage t_stage;
+
+int stage_stream(cudaStream_t *out) {
+    if (!t_stage.stream) FG_CUDA(cudaStreamCreateWithFlags(&t_stage.stream, cudaStreamNonBlocking));
+    *out = t_stage.stream;
+    return kOk;
+}
+
+int stage_buf(int slot, size_t bytes, void **out) {
+    if (t_stage.bytes[slot] < bytes) {
+        if (t_stage.buf[slot]) {
+            cudaStreamSynchronize(t_stage.stream);
+            cudaFree(t_stage.buf[slot]);
+            t_stage.buf[slot] = nullptr;
+            t_stage.bytes[slot] = 0;
+        }
+        FG_CUDA(cudaMalloc(&t_stage.buf[slot], bytes < 256 ? 256 : bytes));
+        t_stage.bytes[slot] = bytes;
+    }
+    *out = t_stage.buf[slot];
+    return kOk;
+}
+
+bool is_device_ptr(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// A host rows x cols column-major matrix with leading dimension ld, viewed on
+// the device: either the pointer itself (device/managed memory) or a staged
+// copy with leading dimension `rows`.
+struct DevView {
+    double *p = nullptr;
+    int ld = 1;
+    bool staged = false;
+};
+
+int view_in(int slot, const double *h, int rows, int cols, int ld, bool copy, cudaStream_t s,
+            DevView *v) {
+    if (is_device_ptr(h)) {
+        v->p = const_cast<double *>(h);
+        v->ld = ld;
+        v->staged = false;
+        return kOk;
+    }
+    const int dld = rows > 0 ? rows : 1;
+    void *d;
+    int st = stage_buf(slot, (size_t)dld * (cols > 0 ? cols : 1) * sizeof(double), &d);
+    if (st != kOk) return st;
+    v->p = (double *)d;
+    v->ld = dld;
+    v->staged = true;
+    if (copy && rows > 0 && cols > 0)
+        FG_CUDA(cudaMemcpy2DAsync(v->p, (size_t)dld * sizeof(double), h, (size_t)ld * sizeof(double),
+                                  (size_t)rows * sizeof(double), cols, cudaMemcpyHostToDevice, s));
+    return kOk;
+}
+
+int view_out(const DevView &v, double *h, int rows, int cols, int ld, cudaStream_t s) {
+    if (!v.staged || rows <= 0 || cols <= 0) return kOk;
+    FG_CUDA(cudaMemcpy2DAsync(h, (size_t)ld * sizeof(double), v.p, (size_t)v.ld * sizeof(double),
+                              (size_t)rows * sizeof(double), cols, cudaMemcpyDeviceToHost, s));
+    return kOk;
+}
+
+int finish(cudaStream_t s) {
+    FG_CUDA(cudaStreamSynchronize(s));
+    return check_device_status(s);
+}
+
+}  // namespace
+
+FG_API const char *flens_gb300_last_error(void);
+// --------------------------------------------------------------- dgemm_ --
+static int dgemm_host(char ta, char tb, int m, int n, int k, double alpha, const double *A,
+                      int ldA, const double *B, int ldB, double beta, double *C, int ldC) {
+    if (m == 0 || n == 0) return kOk;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    if (st != kOk) return st;
+    const bool nA = ta == 'N', nB = tb == 'N';
+    DevView a, b, c;
+    const bool need_ab = alpha != 0.0 && k > 0;
+    if (need_ab) {
+        if ((st = view_in(0, A, nA ? m : k, nA ? k : m, ldA, true, s, &a)) != kOk) return st;
+        if ((st = view_in(1, B, nB ? k : n, nB ? n : k, ldB, true, s, &b)) != kOk) return st;
+    }
+    if ((st = view_in(2, C, m, n, ldC, true, s, &c)) != kOk) return st;
+    if (need_ab)
+        st = dgemm_launch(ta, tb, m, n, k, alpha, a.p, a.ld, b.p, b.ld, beta, c.p, c.ld, s);
+    else
+        st = dgemm_launch(ta, tb, m, n, 0, alpha, nullptr, 1, nullptr, 1, beta, c.p, c.ld, s);
+    if (st != kOk) return st;
+    if ((st = view_out(c, C, m, n, ldC, s)) != kOk) return st;
+    return finish(s);
+}
+
+FG_API void dgemm_(const char *TRANSA, const char *TRANSB, const int *M, const int *N,
+                   const int *K, const double *ALPHA, const double *A, const int *LDA,
+                   const double *B, const int *LDB, const double *BETA, double *C,
+                   const int *LDC) {
+    const char ta = (char)toupper(*TRANSA), tb = (char)toupper(*TRANSB);
+    const int nRowA = (ta == 'N') ? *M : *K;
+    const int nRowB = (tb == 'N') ? *K : *N;
+    int info = 0;
+    if (ta != 'N' && ta != 'C' && ta != 'T') info = 1;
+    else if (tb != 'N' && tb != 'C' && tb != 'T') info = 2;
+    else if (*M < 0) info = 3;
+    else if (*N < 0) info = 4;
+    else if (*K < 0) info = 5;
+    else if (*LDA < std::max(1, nRowA)) info = 8;
+    else if (*LDB < std::max(1, nRowB)) info = 10;
+    else if (*LDC < std::max(1, *M)) info = 13;
+    if (info != 0) {
+        report_xerbla("DGEMM ", info);
+        return;
+    }
+    const int st = dgemm_host(ta == 'C' ? 'T' : ta, tb == 'C' ? 'T' : tb, *M, *N, *K, *ALPHA, A,
+                              *LDA, B, *LDB, *BETA, C, *LDC);
+    if (st != kOk) fprintf(stderr, "[flens_gb300] dgemm_ failed (%d): %s\n", st, flens_gb300_last_error());
+}
+
+// --------------------------------------------------------------- dtrsm_ --
+FG_API void dtrsm_(const char *SIDE, const char *UPLO, const char *TRANSA, const char *DIAG,
+                   const int *M, const int *N, const double *ALPHA, const double *A,
+                   const int *LDA, double *B, const int *LDB) {
+    const char side = (char)toupper(*SIDE), uplo = (char)toupper(*UPLO);
+    const char ta = (char)toupper(*TRANSA), diag = (char)toupper(*DIAG);
+    const int nRowA = (side == 'L') ? *M : *N;
+    int info = 0;
+    if (side != 'L' && side != 'R') info = 1;
+    else if (uplo != 'U' && uplo != 'L') info = 2;
+    else if (ta != 'N' && ta != 'T' && ta != 'C') info = 3;
+    else if (diag != 'U' && diag != 'N') info = 4;
+    else if (*M < 0) info = 5;
+    else if (*N < 0) info = 6;
+    else if (*LDA < std::max(1, nRowA)) info = 9;
+    else if (*LDB < std::max(1, *M)) info = 11;
+    if (info != 0) {
+        report_xerbla("DTRSM ", info);
+        return;
+    }
+    const int m = *M, n = *N;
+    if (m == 0 || n == 0) return;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    DevView a, b;
+    const int ka = side == 'L' ? m : n;
+    if (st == kOk) st = view_in(0, A, ka, ka, *LDA, true, s, &a);
+    if (st == kOk) st = view_in(1, B, m, n, *LDB, true, s, &b);
+    if (st == kOk)
+        st = dtrsm_launch(side, uplo, ta == 'C' ? 'T' : ta, diag, m, n, *ALPHA, a.p, a.ld, b.p, b.ld, s);
+    if (st == kOk) st = view_out(b, B, m, n, *LDB, s);
+    if (st == kOk) st = finish(s);
+    if (st != kOk) fprintf(stderr, "[flens_gb300] dtrsm_ failed (%d): %s\n", st, flens_gb300_last_error());
+}
+
+// ----------------------------------------------------------- LAPACK LU --
+namespace {
+
+// ipiv staging: device copy of an int vector
+int ipiv_dev(int slot, int *h, int len, bool copy_in, cudaStream_t s, int **d, bool *staged) {
+    if (is_device_ptr(h)) {
+        *d = h;
+        *staged = false;
+        return kOk;
+    }
+    void *p;
+    int st = stage_buf(slot, (size_t)(len > 0 ? len : 1) * sizeof(int), &p);
+    if (st != kOk) return st;
+    *d = (int *)p;
+    *staged = true;
+    if (copy_in && len > 0) FG_CUDA(cudaMemcpyAsync(*d, h, (size_t)len * sizeof(int), cudaMemcpyHostToDevice, s));
+    return kOk;
+}
+
+int getrf_host(int m, int n, double *A, int ldA, int *IPIV, int *INFO) {
+    *INFO = 0;
+    if (m == 0 || n == 0) return kOk;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    if (st != kOk) return st;
+    DevView a;
+    if ((st = view_in(0, A, m, n, ldA, true, s, &a)) != kOk) return st;
+    const int mn = std::min(m, n);
+    int *dpiv;
+    bool pstaged;
+    if ((st = ipiv_dev(3, IPIV, mn, false, s, &dpiv, &pstaged)) != kOk) return st;
+    Workspace *w = workspace_for(s, 0);
+    if (!w) return kErrAlloc;
+    if ((st = dgetrf_launch(m, n, a.p, a.ld, dpiv, w->info, s)) != kOk) return st;
+    if ((st = view_out(a, A, m, n, ldA, s)) != kOk) return st;
+    if (pstaged) FG_CUDA(cudaMemcpyAsync(IPIV, dpiv, (size_t)mn * sizeof(int), cudaMemcpyDeviceToHost, s));
+    FG_CUDA(cudaMemcpyAsync(INFO, w->info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return finish(s);
+}
+
+int getrs_host(char trans, int n, int nrhs, const double *A, int ldA, const int *IPIV, double *B,
+               int ldB) {
+    if (n == 0 || nrhs == 0) return kOk;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    if (st != kOk) return st;
+    DevView a, b;
+    if ((st = view_in(0, A, n, n, ldA, true, s, &a)) != kOk) return st;
+    if ((st = view_in(1, B, n, nrhs, ldB, true, s, &b)) != kOk) return st;
+    int *dpiv;
+    bool pstaged;
+    if ((st = ipiv_dev(3, const_cast<int *>(IPIV), n, true, s, &dpiv, &pstaged)) != kOk) return st;
+    if ((st = dgetrs_launch(trans, n, nrhs, a.p, a.ld, dpiv, b.p, b.ld, s)) != kOk) return st;
+    if ((st = view_out(b, B, n, nrhs, ldB, s)) != kOk) return st;
+    return finish(s);
+}
+
+int gesv_host(int n, int nrhs, double *A, int ldA, int *IPIV, double *B, int ldB, int *INFO) {
+    *INFO = 0;
+    if (n == 0) return kOk;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    if (st != kOk) return st;
+    DevView a, b;
+    if ((st = view_in(0, A, n, n, ldA, true, s, &a)) != kOk) return st;
+    if ((st = view_in(1, B, n, nrhs, ldB, true, s, &b)) != kOk) return st;
+    int *dpiv;
+    bool pstaged;
+    if ((st = ipiv_dev(3, IPIV, n, false, s, &dpiv, &pstaged)) != kOk) return st;
+    Workspace *w = workspace_for(s, 0);
+    if (!w) return kErrAlloc;
+    if ((st = dgetrf_launch(n, n, a.p, a.ld, dpiv, w->info, s)) != kOk) return st;
+    FG_CUDA(cudaMemcpyAsync(INFO, w->info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FG_CUDA(cudaStreamSynchronize(s));
+    // flens/lapack/ge/sv.tcc:70-75: solve only if the factorisation succeeded
+    if (*INFO == 0 && nrhs > 0) {
+        if ((st = dgetrs_launch('N', n, nrhs, a.p, a.ld, dpiv, b.p, b.ld, s)) != kOk) return st;
+        if ((st = view_out(b, B, n, nrhs, ldB, s)) != kOk) return st;
+    }
+    if ((st = view_out(a, A, n, n, ldA, s)) != kOk) return st;
+    if (pstaged) FG_CUDA(cudaMemcpyAsync(IPIV, dpiv, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s));
+    return finish(s);
+}
+
+}  // namespace
+
+FG_API void dgetrf_(const int *M, const int *N, double *A, const int *LDA, int *IPIV, int *INFO) {
+    *INFO = 0;
+    if (*M < 0) *INFO = -1;
+    else if (*N < 0) *INFO = -2;
+    else if (*LDA < std::max(1, *M)) *INFO = -4;
+    if (*INFO != 0) {
+        report_xerbla("DGETRF", -*INFO);
+        return;
+    }
+    const int st = getrf_host(*M, *N, A, *LDA, IPIV, INFO);
+    if (st != kOk) *INFO = st;
+}
+
+FG_API void dgetrs_(const char *TRANS, const int *N, const int *NRHS, const double *A,
+                    const int *LDA, const int *IPIV, double *B, const int *LDB, int *INFO) {
+    *INFO = 0;
+    if (*TRANS != 'N' && *TRANS != 'T' && *TRANS != 'C') *INFO = -1;
+    else if (*N < 0) *INFO = -2;
+    else if (*NRHS < 0) *INFO = -3;
+    else if (*LDA < std::max(1, *N)) *INFO = -5;
+    else if (*LDB < std::max(1, *N)) *INFO = -8;
+    if (*INFO != 0) {
+        report_xerbla("DGETRS", -*INFO);
+        return;
+    }
+    const int st = getrs_host(*TRANS == 'C' ? 'T' : *TRANS, *N, *NRHS, A, *LDA, IPIV, B, *LDB);
+    if (st != kOk) *INFO = st;
+}
+
+FG_API void dgesv_(const int *N, const int *NRHS, double *A, const int *LDA, int *IPIV, double *B,
+                   const int *LDB, int *INFO) {
+    *INFO = 0;
+    if (*N < 0) *INFO = -1;
+    else if (*NRHS < 0) *INFO = -2;
+    else if (*LDA < std::max(1, *N)) *INFO = -4;
+    else if (*LDB < std::max(1, *N)) *INFO = -7;
+    if (*INFO != 0) {
+        report_xerbla("DGESV ", -*INFO);
+        return;
+    }
+    int info = 0;
+    const int st = gesv_host(*N, *NRHS, A, *LDA, IPIV, B, *LDB, &info);
+    *INFO = (st != kOk) ? st : info;
+}
+
+// ------------------------------------------------ device-pointer API ----
+static inline cudaStream_t as_stream(void *s) { return (cudaStream_t)s; }
+
+FG_API int flens_gb300_dgemm(char transA, char transB, int m, int n, int k, double alpha,
+                             const double *A, int ldA, const double *B, int ldB, double beta,
+                             double *C, int ldC, void *stream) {
+    const char ta = (char)toupper(transA), tb = (char)toupper(transB);
+    if (ta != 'N' && ta != 'T' && ta != 'C') return -1;
+    if (tb != 'N' && tb != 'T' && tb != 'C') return -2;
+    if (m < 0) return -3;
+    if (n < 0) return -4;
+    if (k < 0) return -5;
+    if (ldA < std::max(1, ta == 'N' ? m : k)) return -8;
+    if (ldB < std::max(1, tb == 'N' ? k : n)) return -10;
+    if (ldC < std::max(1, m)) return -13;
+    return dgemm_launch(ta == 'C' ? 'T' : ta, tb == 'C' ? 'T' : tb, m, n, k, alpha, A, ldA, B,
+                        ldB, beta, C, ldC, as_stream(stream));
+}
+
+FG_API int flens_gb300_dtrsm(char side, char uplo, char transA, char diag, int m, int n,
+                             double alpha, const double *A, int ldA, double *B, int ldB,
+                             void *stream) {
+    side = (char)toupper(side);
+    uplo = (char)toupper(uplo);
+    transA = (char)toupper(transA);
+    diag = (char)toupper(diag);
+    if (side != 'L' && side != 'R') return -1;
+    if (uplo != 'U' && uplo != 'L') return -2;
+    if (transA != 'N' && transA != 'T' && transA != 'C') return -3;
+    if (diag != 'U' && diag != 'N') return -4;
+    if (m < 0) return -5;
+    if (n < 0) return -6;
+    if (ldA < std::max(1, side == 'L' ? m : n)) return -9;
+    if (ldB < std::max(1, m)) return -11;
+    return dtrsm_launch(side, uplo, transA == 'C' ? 'T' : transA, diag, m, n, alpha, A, ldA, B, ldB,
+                        as_stream(stream));
+}
+
+FG_API int flens_gb300_dgetrf(int m, int n, double *A, int ldA, int *ipiv, int *info, void *stream) {
+    if (m < 0) return -1;
+    if (n < 0) return -2;
+    if (ldA < std::max(1, m)) return -4;
+    return dgetrf_launch(m, n, A, ldA, ipiv, info, as_stream(stream));
+}
+
+FG_API int flens_gb300_dgetrs(char trans, int n, int nrhs, const double *A, int ldA,
+                              const int *ipiv, double *B, int ldB, void *stream) {
+    trans = (char)toupper(trans);
+    if (trans != 'N' && trans != 'T' && trans != 'C') return -1;
+    if (n < 0) return -2;
+    if (nrhs < 0) return -3;
+    if (ldA < std::max(1, n)) return -5;
+    if (ldB < std::max(1, n)) return -8;
+    return dgetrs_launch(trans == 'C' ? 'T' : trans, n, nrhs, A, ldA, ipiv, B, ldB, as_stream(stream));
+}
+
+FG_API int flens_gb300_dgesv(int n, int nrhs, double *A, int ldA, int *ipiv, double *B, int ldB,
+                             int *info, void *stream) {
+    if (n < 0) return -1;
+    if (nrhs < 0) return -2;
+    if (ldA < std::max(1, n)) return -4;
+    if (ldB < std::max(1, n)) return -7;
+    cudaStream_t s = as_stream(stream);
+    int st = dgetrf_launch(n, n, A, ldA, ipiv, info, s);
+    if (st != kOk) return st;
+    int h = 0;
+    FG_CUDA(cudaMemcpyAsync(&h, info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FG_CUDA(cudaStreamSynchronize(s));
+    if (h != 0) return kOk;    // INFO>0 reported through *info; no solve (sv.tcc:70-75)
+    return dgetrs_launch('N', n, nrhs, A, ldA, ipiv, B, ldB, s);
+}
+
+FG_API int flens_gb300_sync(void *stream) {
+    cudaStream_t s = as_stream(stream);
+    FG_CUDA(cudaStreamSynchronize(s));
+    return check_device_status(s);
+}
+
+FG_API int flens_gb300_version(void) { return 100; }

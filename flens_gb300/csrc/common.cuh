@@ -1,0 +1,178 @@
+// common.cuh -- shared helpers for the GB300 dense LU / GEMM library.
+//
+// Everything in this directory is compiled for sm_103a only
+// (-gencode arch=compute_103a,code=sm_103a).  Matrices are column-major with
+// leading dimensions in elements, as in FLENS's FullStorage<T, ColMajor>
+// (flens/storage/fullstorage/fullstorage.h:58-60) and the Fortran ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#define FG_API extern "C" __attribute__((visibility("default")))
+
+namespace fg {
+
+// ---------------------------------------------------------------- status --
+// Library status codes (returned by the flens_gb300_* entry points).  Values
+// below zero that are > -100 are LAPACK-style argument positions.
+enum Status : int {
+    kOk = 0,
+    kErrCuda = -1001,        // a CUDA runtime call failed
+    kErrTimeout = -1002,     // a bounded device-side wait gave up
+    kErrNoDevice = -1003,    // no usable CUDA device
+    kErrAlloc = -1004,       // device workspace allocation failed
+    kErrUnsupported = -1005, // size/shape outside what this build supports
+    kErrNotConverged = -1006 // iterative refinement did not reach tolerance
+};
+
+// Device-side status word bits (written by kernels, read by the host).
+enum DeviceStatus : int {
+    kDevOk = 0,
+    kDevBarrierTimeout = 1,
+    kDevMbarTimeout = 2,
+};
+
+void set_last_error(const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define FG_CUDA(call)                                                     \
+    do {                                                                  \
+        cudaError_t _e = (call);                                          \
+        if (_e != cudaSuccess) return ::fg::cuda_fail(_e, #call);         \
+    } while (0)
+
+inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
+inline size_t ceil_div(size_t a, size_t b) { return (a + b - 1) / b; }
+
+// Per-(device, stream) workspace: scratch buffers kernels need beyond their
+// inputs/outputs.  Grown on demand, never shrunk, freed at library unload.
+struct Workspace {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    void *buf = nullptr;         // general scratch
+    size_t bytes = 0;
+    int *status = nullptr;       // device status word (DeviceStatus bits)
+    int *info = nullptr;         // device INFO for host-pointer entry points
+};
+
+// Returns the workspace bound to `stream` on the current device with at least
+// `bytes` of scratch (nullptr on allocation failure; last error set).
+Workspace *workspace_for(cudaStream_t stream, size_t bytes);
+
+int num_sms();                 // SM count of the current device
+int device_id();               // current device ordinal
+
+// Tracing: FLENS_GB300_TRACE=1 prints one line per kernel family chosen.
+bool trace_enabled();
+void trace(const char *fmt, ...);
+
+// ------------------------------------------------- launch accounting --
+// Every kernel launch of the library is wrapped in a KTimer: it counts the
+// launch and, while timing is enabled (flens_gb300_timing_enable), records a
+// CUDA event pair around it on the launching stream together with the
+// launch's algorithmic flops and bytes.
+enum Family : int {
+    kFamGemm = 0,     // FP64 GEMM (trailing updates, trsm off-diagonal blocks)
+    kFamPanel = 1,    // LU panel (pivot search, swap, scale, rank-1)
+    kFamLaswp = 2,    // row interchanges
+    kFamTrsm = 3,     // triangular diagonal-block solves
+    kFamAux = 4,      // scaling, permutation helpers, conversions
+    kFamTcGemm = 5,   // tcgen05 low-precision GEMM
+    kFamRefine = 6,   // residual / refinement / Krylov helpers
+    kFamBatched = 7,  // batched LU
+    kFamCount = 8
+};
+
+struct KTimer {
+    KTimer(int family, cudaStream_t stream, double flops, double bytes);
+    ~KTimer();
+    int family;
+    cudaStream_t stream;
+    double flops, bytes;
+    cudaEvent_t e0;
+    bool on;
+};
+
+// ---------------------------------------------------------- device helpers --
+__device__ __forceinline__ double ld_cg(const double *p) { return __ldcg(p); }
+__device__ __forceinline__ int ld_cg(const int *p) { return __ldcg(p); }
+
+// Bounded spin limit for every device-side wait (~1-2 s at GB300 clocks with
+// the nanosleep back-off below).
+constexpr unsigned kSpinLimit = 1u << 24;
+
+// Grid-wide barrier for a cooperatively launched grid.  Every block must call
+// it the same number of times.  Returns false (and sets *status) if the wait
+// exceeded kSpinLimit; the caller must then return without further barriers.
+struct GridBarrierState {
+    unsigned int count;
+    unsigned int generation;
+};
+
+__device__ __forceinline__ bool grid_barrier(GridBarrierState *bar,
+                                             unsigned int nblocks,
+                                             int *status) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (nblocks == 1) return true;
+    if (threadIdx.x == 0) {
+        volatile unsigned int *vgen = &bar->generation;
+        const unsigned int gen = *vgen;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(&bar->count, 1u);
+        int ok = 1;
+        if (arrived == nblocks - 1) {
+            atomicExch(&bar->count, 0u);
+            __threadfence();
+            atomicAdd(&bar->generation, 1u);
+        } else {
+            unsigned int spins = 0;
+            while (*vgen == gen) {
+                if (++spins > kSpinLimit) {
+                    atomicOr(status, kDevBarrierTimeout);
+                    ok = 0;
+                    break;
+                }
+                if (spins > 64) __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+}  // namespace fg
+
+// ----------------------------------------------------- internal launchers --
+// (host functions shared between translation units; all asynchronous on
+// `stream`, returning a Status)
+namespace fg {
+
+int dgemm_launch(char transA, char transB, int m, int n, int k, double alpha,
+                 const double *A, int ldA, const double *B, int ldB,
+                 double beta, double *C, int ldC, cudaStream_t stream);
+
+int dtrsm_launch(char side, char upLo, char transA, char diag, int m, int n,
+                 double alpha, const double *A, int ldA, double *B, int ldB,
+                 cudaStream_t stream);
+
+int dscal_matrix_launch(int m, int n, double alpha, double *B, int ldB,
+                        cudaStream_t stream);
+
+int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info,
+                  cudaStream_t stream);
+
+int dgetrs_launch(char trans, int n, int nrhs, const double *A, int ldA,
+                  const int *ipiv, double *B, int ldB, cudaStream_t stream);
+
+int dlaswp_launch(int nrows, int ncols, double *A, int ldA, int k1, int k2,
+                  const int *ipiv, int inc, cudaStream_t stream);
+
+// Reads and clears the workspace status word for `stream` (synchronises).
+int check_device_status(cudaStream_t stream);
+
+}  // namespace fg

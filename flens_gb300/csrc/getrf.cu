@@ -1,0 +1,493 @@
+// getrf.cu -- blocked LU with partial pivoting (trf), its row interchanges
+// (laswp) and solves (trs), FP64, column-major, 1-based pivots.
+//
+// Replaces, for double:
+//   flens::lapack::trf  -> generic::trf_impl   flens/lapack/ge/trf.tcc:59-152
+//   tf2 (panel)         -> generic::tf2_impl   flens/lapack/ge/tf2.tcc:56-136
+//   laswp               -> generic::laswp_impl flens/lapack/la/laswp.tcc:54-93
+//   trs                 -> generic::trs_impl   flens/lapack/ge/trs.tcc:59-109
+//
+// Structure (one stream, all asynchronous):
+//   for each block column j (width jb <= 64, the reference's ilaenv GETRF
+//   block size, flens/lapack/la/ilaenv.tcc:93-99):
+//     panel_kernel      cooperative grid, one CTA per SM; the (m-j) x jb panel
+//                       lives in shared memory split by rows; per column one
+//                       bounded grid barrier exchanges per-CTA pivot
+//                       candidates (warp-shuffle argmax, first maximum wins)
+//                       and the candidate rows, then every CTA swaps, scales
+//                       and applies the rank-1 update to its own rows.  At the
+//                       end it turns the jb interchanges into a list of
+//                       (destination row, source row) moves.
+//     laswp_pairs_kernel applies those moves to every column outside the
+//                       panel, one warp per column (loads, then stores).
+//     dtrsm_launch      U12 = L11^-1 A12
+//     dgemm_launch      A22 -= A21 * U12
+//
+// Unlike the reference, the GPU path always uses the blocked algorithm (the
+// reference switches to tf2 when nb >= min(m,n), trf.tcc:87-91); the pivots and
+// factors are the same in exact arithmetic.
+#include "common.cuh"
+
+#include <float.h>
+#include <limits.h>
+
+namespace fg {
+namespace {
+
+constexpr int PANEL_THREADS = 256;
+constexpr int PANEL_NB = 64;           // max panel width
+constexpr int PANEL_GMAX = 256;        // max CTAs in a panel grid
+constexpr int PANEL_RMIN = 32;         // min rows per CTA
+constexpr size_t PANEL_SMEM_MAX = 200 * 1024;
+
+struct PanelScratch {
+    GridBarrierState *bar;
+    double *cand_val;   // [2][GMAX]
+    int *cand_idx;      // [2][GMAX]
+    double *cand_row;   // [2][GMAX][NB]
+    double *rowjj;      // [2][NB]
+    int *swap_cnt;      // [1]
+    int *swap_dst;      // [2*NB]
+    int *swap_src;      // [2*NB]
+};
+
+size_t panel_scratch_bytes() {
+    size_t b = 256;                                            // barrier
+    b += 2 * PANEL_GMAX * sizeof(double);
+    b += 2 * PANEL_GMAX * sizeof(int);
+    b += 2 * (size_t)PANEL_GMAX * PANEL_NB * sizeof(double);
+    b += 2 * PANEL_NB * sizeof(double);
+    b += 256 + 4 * PANEL_NB * sizeof(int);
+    return b + 1024;
+}
+
+PanelScratch carve_panel_scratch(void *base) {
+    char *p = (char *)base;
+    PanelScratch s;
+    s.bar = (GridBarrierState *)p;
+    p += 256;
+    s.cand_val = (double *)p;
+    p += 2 * PANEL_GMAX * sizeof(double);
+    s.cand_idx = (int *)p;
+    p += 2 * PANEL_GMAX * sizeof(int);
+    s.cand_row = (double *)p;
+    p += 2 * (size_t)PANEL_GMAX * PANEL_NB * sizeof(double);
+    s.rowjj = (double *)p;
+    p += 2 * PANEL_NB * sizeof(double);
+    s.swap_cnt = (int *)p;
+    p += 256;
+    s.swap_dst = (int *)p;
+    p += 2 * PANEL_NB * sizeof(int);
+    s.swap_src = (int *)p;
+    return s;
+}
+
+// (key, row) "better than": larger key; on equal keys the smaller row, which
+// is cxxblas iamax's first-maximum rule (cxxblas/level1/iamax.tcc:52-56).
+__device__ __forceinline__ bool better(double v1, int i1, double v2, int i2) {
+    return v1 > v2 || (v1 == v2 && i1 < i2);
+}
+
+// Block-wide argmax of (key, row).  All threads get the result.
+__device__ __forceinline__ void block_argmax(double &v, int &i, double *red_v, int *red_i) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const double ov = __shfl_down_sync(0xffffffffu, v, off);
+        const int oi = __shfl_down_sync(0xffffffffu, i, off);
+        if (better(ov, oi, v, i)) { v = ov; i = oi; }
+    }
+    if (lane == 0) { red_v[warp] = v; red_i[warp] = i; }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        v = lane < nw ? red_v[lane] : -3.0;
+        i = lane < nw ? red_i[lane] : INT_MAX;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const double ov = __shfl_down_sync(0xffffffffu, v, off);
+            const int oi = __shfl_down_sync(0xffffffffu, i, off);
+            if (better(ov, oi, v, i)) { v = ov; i = oi; }
+        }
+        if (lane == 0) { red_v[0] = v; red_i[0] = i; }
+    }
+    __syncthreads();
+    v = red_v[0];
+    i = red_i[0];
+    __syncthreads();
+}
+
+// Panel factorisation, tf2 semantics (flens/lapack/ge/tf2.tcc:56-136).
+// A points at the panel's top-left element A(j,j); the panel is mp x jb.
+// CTA b owns panel rows [b*R, min(mp,(b+1)*R)), kept in shared memory as
+// S[c*R + r].
+__global__ void __launch_bounds__(PANEL_THREADS)
+panel_kernel(double *__restrict__ A, int lda, int mp, int jb, int j0,
+             int *__restrict__ ipiv, int *__restrict__ info, int *__restrict__ status,
+             PanelScratch ps, int R) {
+    extern __shared__ double S[];
+    __shared__ double prow[PANEL_NB], orow[PANEL_NB];
+    __shared__ double red_v[32];
+    __shared__ int red_i[32];
+    __shared__ int s_gs;
+    __shared__ int s_list_row[2 * PANEL_NB], s_list_src[2 * PANEL_NB];
+
+    const int b = blockIdx.x, G = gridDim.x, tid = threadIdx.x;
+    const int rb = b * R;
+    const int re = min(mp, rb + R);
+    const int nr = max(0, re - rb);
+
+    for (int e = tid; e < nr * jb; e += PANEL_THREADS) {
+        const int r = e % nr, c = e / nr;
+        S[c * R + r] = A[(size_t)(rb + r) + (size_t)c * lda];
+    }
+    __syncthreads();
+
+    for (int jj = 0; jj < jb; ++jj) {
+        const int par = jj & 1;
+        // -- local pivot candidate among owned rows g >= jj (NaN never wins)
+        double bv = -2.0;
+        int bi = INT_MAX;
+        for (int r = tid; r < nr; r += PANEL_THREADS) {
+            const int g = rb + r;
+            if (g >= jj) {
+                const double a = fabs(S[jj * R + r]);
+                const double key = isnan(a) ? -1.0 : a;
+                if (better(key, g, bv, bi)) { bv = key; bi = g; }
+            }
+        }
+        block_argmax(bv, bi, red_v, red_i);
+        if (tid == 0) {
+            ps.cand_val[par * PANEL_GMAX + b] = bv;
+            ps.cand_idx[par * PANEL_GMAX + b] = bi;
+        }
+        if (bi != INT_MAX) {
+            for (int c = tid; c < jb; c += PANEL_THREADS)
+                ps.cand_row[((size_t)par * PANEL_GMAX + b) * PANEL_NB + c] = S[c * R + (bi - rb)];
+        }
+        if (jj >= rb && jj < re) {
+            for (int c = tid; c < jb; c += PANEL_THREADS)
+                ps.rowjj[par * PANEL_NB + c] = S[c * R + (jj - rb)];
+        }
+        if (!grid_barrier(ps.bar, G, status)) return;
+
+        // -- global pivot: best candidate over CTAs
+        double gv = -3.0;
+        int gi = INT_MAX;
+        for (int t = tid; t < G; t += PANEL_THREADS) {
+            const double v = ld_cg(&ps.cand_val[par * PANEL_GMAX + t]);
+            const int i = ld_cg(&ps.cand_idx[par * PANEL_GMAX + t]);
+            if (better(v, i, gv, gi)) { gv = v; gi = i; }
+        }
+        block_argmax(gv, gi, red_v, red_i);
+        if (tid == 0) {
+            // iamax starts from element jj: if it is NaN nothing compares
+            // greater and jj is the pivot (cxxblas/level1/iamax.tcc:50-57).
+            const double ajj = ld_cg(&ps.rowjj[par * PANEL_NB + jj]);
+            s_gs = isnan(ajj) ? jj : gi;
+        }
+        __syncthreads();
+        const int gs = s_gs;
+        const int wb = gs / R;
+        for (int c = tid; c < jb; c += PANEL_THREADS) {
+            const double o = ld_cg(&ps.rowjj[par * PANEL_NB + c]);
+            orow[c] = o;
+            prow[c] = (gs == jj) ? o : ld_cg(&ps.cand_row[((size_t)par * PANEL_GMAX + wb) * PANEL_NB + c]);
+        }
+        __syncthreads();
+        const double pv = prow[jj];
+        if (b == 0 && tid == 0) {
+            ipiv[j0 + jj] = j0 + gs + 1;
+            if (pv == 0.0 && *info == 0) *info = j0 + jj + 1;
+        }
+        if (pv != 0.0) {
+            if (gs != jj) {
+                if (jj >= rb && jj < re)
+                    for (int c = tid; c < jb; c += PANEL_THREADS) S[c * R + (jj - rb)] = prow[c];
+                if (gs >= rb && gs < re)
+                    for (int c = tid; c < jb; c += PANEL_THREADS) S[c * R + (gs - rb)] = orow[c];
+            }
+            __syncthreads();
+            if (fabs(pv) >= DBL_MIN) {
+                const double rinv = 1.0 / pv;
+                for (int r = tid; r < nr; r += PANEL_THREADS)
+                    if (rb + r > jj) S[jj * R + r] *= rinv;
+            } else {
+                for (int r = tid; r < nr; r += PANEL_THREADS)
+                    if (rb + r > jj) S[jj * R + r] /= pv;
+            }
+        }
+        __syncthreads();
+        // -- rank-1 update of the panel's trailing part (rows > jj, cols > jj)
+        if (jj + 1 < jb) {
+            const int nc = jb - jj - 1;
+            for (int e = tid; e < nr * nc; e += PANEL_THREADS) {
+                const int r = e % nr, c = jj + 1 + e / nr;
+                if (rb + r > jj) S[c * R + r] = fma(-prow[c], S[jj * R + r], S[c * R + r]);
+            }
+        }
+        __syncthreads();
+    }
+
+    for (int e = tid; e < nr * jb; e += PANEL_THREADS) {
+        const int r = e % nr, c = e / nr;
+        A[(size_t)(rb + r) + (size_t)c * lda] = S[c * R + r];
+    }
+
+    // -- block 0, warp 0: the jb interchanges as (dst, src) row moves.
+    if (b == 0 && tid < 32) {
+        const int lane = tid;
+        for (int i = lane; i < jb; i += 32) {
+            s_list_row[i] = j0 + i;
+            s_list_src[i] = j0 + i;
+        }
+        __syncwarp();
+        int cnt = jb;
+        for (int i = 0; i < jb; ++i) {
+            const int p = ipiv[j0 + i] - 1;       // written by this warp's lane 0 above
+            int pos;
+            if (p < j0 + jb) {
+                pos = p - j0;
+            } else {
+                int found = -1;
+                for (int base = jb; base < cnt; base += 32) {
+                    const int e = base + lane;
+                    const unsigned hit = __ballot_sync(0xffffffffu, e < cnt && s_list_row[e] == p);
+                    if (hit) { found = base + __ffs(hit) - 1; break; }
+                }
+                if (found < 0) {
+                    found = cnt;
+                    if (lane == 0) { s_list_row[cnt] = p; s_list_src[cnt] = p; }
+                    ++cnt;
+                }
+                pos = found;
+            }
+            __syncwarp();
+            if (lane == 0 && pos != i) {
+                const int t = s_list_src[i];
+                s_list_src[i] = s_list_src[pos];
+                s_list_src[pos] = t;
+            }
+            __syncwarp();
+        }
+        // compact to the moves that change something
+        if (lane == 0) {
+            int k = 0;
+            for (int e = 0; e < cnt; ++e) {
+                if (s_list_row[e] != s_list_src[e]) {
+                    ps.swap_dst[k] = s_list_row[e];
+                    ps.swap_src[k] = s_list_src[e];
+                    ++k;
+                }
+            }
+            *ps.swap_cnt = k;
+        }
+    }
+}
+
+// Apply the panel's row moves to columns [0, cSplit) and [cSplit+skip, ...),
+// ncols columns in total; one warp per column.
+__global__ void __launch_bounds__(256)
+laswp_pairs_kernel(double *__restrict__ A, int lda, int ncols, int cSplit, int skip,
+                   const int *__restrict__ cntp, const int *__restrict__ dst,
+                   const int *__restrict__ src) {
+    __shared__ int s_dst[2 * PANEL_NB], s_src[2 * PANEL_NB];
+    const int cnt = *cntp;
+    if (cnt == 0) return;
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+        s_dst[e] = dst[e];
+        s_src[e] = src[e];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (q >= ncols) return;
+    const int c = q < cSplit ? q : q + skip;
+    double *col = A + (size_t)c * lda;
+    double v[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const int e = lane + 32 * t;
+        if (e < cnt) v[t] = col[s_src[e]];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const int e = lane + 32 * t;
+        if (e < cnt) col[s_dst[e]] = v[t];
+    }
+}
+
+// ---- laswp with an arbitrary pivot range (used by trs) ----------------------
+// perm[r] = source row of row r after the interchanges i <-> piv(i) for
+// i = k1..k2 (inc > 0) or k2..k1 (inc < 0); one thread walks the pivots in
+// order (the interchanges do not commute), the permutation lives in shared
+// memory when it fits.
+__global__ void laswp_perm_kernel(int nrows, int k1, int k2, const int *__restrict__ ipiv,
+                                  int inc, int *__restrict__ perm_g, int use_smem) {
+    extern __shared__ int perm_s[];
+    int *perm = use_smem ? perm_s : perm_g;
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) perm[r] = r;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (inc > 0) {
+            for (int i = k1; i <= k2; ++i) {
+                const int p = ipiv[i - 1] - 1, a = i - 1;
+                if (p != a && p >= 0 && p < nrows) { const int t = perm[a]; perm[a] = perm[p]; perm[p] = t; }
+            }
+        } else {
+            for (int i = k2; i >= k1; --i) {
+                const int p = ipiv[i - 1] - 1, a = i - 1;
+                if (p != a && p >= 0 && p < nrows) { const int t = perm[a]; perm[a] = perm[p]; perm[p] = t; }
+            }
+        }
+    }
+    __syncthreads();
+    if (use_smem)
+        for (int r = threadIdx.x; r < nrows; r += blockDim.x) perm_g[r] = perm[r];
+}
+
+// tmp[:, c] = A[perm, c] for the first nrows rows
+__global__ void gather_rows_kernel(int nrows, int ncols, const double *__restrict__ A, int lda,
+                                   const int *__restrict__ perm, double *__restrict__ tmp) {
+    const size_t total = (size_t)nrows * ncols;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const size_t c = e / nrows, r = e % nrows;
+        tmp[e] = A[(size_t)perm[r] + c * lda];
+    }
+}
+
+__global__ void copy_back_kernel(int nrows, int ncols, const double *__restrict__ tmp,
+                                 double *__restrict__ A, int lda) {
+    const size_t total = (size_t)nrows * ncols;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const size_t c = e / nrows, r = e % nrows;
+        A[r + c * lda] = tmp[e];
+    }
+}
+
+bool g_panel_attr_set = false;
+
+}  // namespace
+
+int dlaswp_launch(int nrows, int ncols, double *A, int ldA, int k1, int k2, const int *ipiv,
+                  int inc, cudaStream_t stream) {
+    if (nrows <= 0 || ncols <= 0 || k2 < k1) return kOk;
+    const size_t permBytes = ((size_t)nrows * sizeof(int) + 255) / 256 * 256;
+    const size_t tmpBytes = (size_t)nrows * ncols * sizeof(double);
+    Workspace *w = workspace_for(stream, permBytes + tmpBytes);
+    if (!w) return kErrAlloc;
+    int *perm = (int *)w->buf;
+    double *tmp = (double *)((char *)w->buf + permBytes);
+    const int use_smem = (size_t)nrows * sizeof(int) <= 200 * 1024 ? 1 : 0;
+    if (use_smem) {
+        static bool attr = false;
+        if (!attr) {
+            FG_CUDA(cudaFuncSetAttribute(laswp_perm_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+            attr = true;
+        }
+    }
+    KTimer kt(kFamLaswp, stream, 0.0, 2.0 * (double)nrows * ncols * 16.0);
+    laswp_perm_kernel<<<1, 1024, use_smem ? (size_t)nrows * sizeof(int) : 0, stream>>>(
+        nrows, k1, k2, ipiv, inc, perm, use_smem);
+    FG_CUDA(cudaGetLastError());
+    const size_t total = (size_t)nrows * ncols;
+    int blocks = (int)ceil_div(total, (size_t)256);
+    if (blocks > num_sms() * 16) blocks = num_sms() * 16;
+    gather_rows_kernel<<<blocks, 256, 0, stream>>>(nrows, ncols, A, ldA, perm, tmp);
+    FG_CUDA(cudaGetLastError());
+    copy_back_kernel<<<blocks, 256, 0, stream>>>(nrows, ncols, tmp, A, ldA);
+    FG_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, cudaStream_t stream) {
+    FG_CUDA(cudaMemsetAsync(info, 0, sizeof(int), stream));
+    if (m == 0 || n == 0) return kOk;
+    const int mn = m < n ? m : n;
+    Workspace *w = workspace_for(stream, panel_scratch_bytes());
+    if (!w) return kErrAlloc;
+    PanelScratch ps = carve_panel_scratch(w->buf);
+    FG_CUDA(cudaMemsetAsync(ps.bar, 0, sizeof(GridBarrierState), stream));
+    if (!g_panel_attr_set) {
+        FG_CUDA(cudaFuncSetAttribute(panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)PANEL_SMEM_MAX));
+        g_panel_attr_set = true;
+    }
+    int sms = num_sms();
+    if (sms <= 0) {
+        set_last_error("no CUDA device");
+        return kErrNoDevice;
+    }
+    const int gcap = sms < PANEL_GMAX ? sms : PANEL_GMAX;
+    trace("dgetrf m=%d n=%d lda=%d panel grid<=%d", m, n, ldA, gcap);
+
+    for (int j = 0; j < mn;) {
+        const int mp = m - j;
+        int R = ceil_div(mp, gcap);
+        if (R < PANEL_RMIN) R = PANEL_RMIN;
+        // panel width: the reference's 64, narrowed only if a CTA's rows
+        // would not fit in shared memory (very tall matrices)
+        int nb = PANEL_NB;
+        while (nb > 1 && (size_t)R * nb * sizeof(double) > PANEL_SMEM_MAX) nb >>= 1;
+        if ((size_t)R * nb * sizeof(double) > PANEL_SMEM_MAX) {
+            set_last_error("dgetrf: m=%d too tall for the shared-memory panel", m);
+            return kErrUnsupported;
+        }
+        const int jb = (mn - j) < nb ? (mn - j) : nb;
+        const int G = ceil_div(mp, R);
+        double *Ap = A + j + (size_t)j * ldA;
+        int *status = w->status;
+        int j0 = j;
+        size_t smem = (size_t)R * jb * sizeof(double);
+        void *args[] = {&Ap, &ldA, (void *)&mp, (void *)&jb, &j0, &ipiv, &info, &status, &ps, &R};
+        {
+            KTimer ktp(kFamPanel, stream, (double)mp * jb * jb - (double)jb * jb * jb / 3.0,
+                       16.0 * (double)mp * jb);
+            FG_CUDA(cudaLaunchCooperativeKernel((const void *)panel_kernel, dim3(G),
+                                                dim3(PANEL_THREADS), args, smem, stream));
+        }
+        // interchanges on the columns outside the panel
+        const int ncols = n - jb;
+        if (ncols > 0) {
+            const int blocks = ceil_div(ncols, 256 / 32);
+            KTimer ktl(kFamLaswp, stream, 0.0, 0.0);
+            laswp_pairs_kernel<<<blocks, 256, 0, stream>>>(A, ldA, ncols, j, jb, ps.swap_cnt,
+                                                           ps.swap_dst, ps.swap_src);
+            FG_CUDA(cudaGetLastError());
+        }
+        if (j + jb < n) {
+            int st = dtrsm_launch('L', 'L', 'N', 'U', jb, n - j - jb, 1.0, Ap, ldA,
+                                  A + j + (size_t)(j + jb) * ldA, ldA, stream);
+            if (st != kOk) return st;
+            if (j + jb < m) {
+                st = dgemm_launch('N', 'N', m - j - jb, n - j - jb, jb, -1.0,
+                                  A + (j + jb) + (size_t)j * ldA, ldA,
+                                  A + j + (size_t)(j + jb) * ldA, ldA, 1.0,
+                                  A + (j + jb) + (size_t)(j + jb) * ldA, ldA, stream);
+                if (st != kOk) return st;
+            }
+        }
+        j += jb;
+    }
+    return kOk;
+}
+
+int dgetrs_launch(char trans, int n, int nrhs, const double *A, int ldA, const int *ipiv,
+                  double *B, int ldB, cudaStream_t stream) {
+    if (n == 0 || nrhs == 0) return kOk;
+    int st;
+    if (trans == 'N' || trans == 'n') {
+        if ((st = dlaswp_launch(n, nrhs, B, ldB, 1, n, ipiv, 1, stream)) != kOk) return st;
+        if ((st = dtrsm_launch('L', 'L', 'N', 'U', n, nrhs, 1.0, A, ldA, B, ldB, stream)) != kOk) return st;
+        return dtrsm_launch('L', 'U', 'N', 'N', n, nrhs, 1.0, A, ldA, B, ldB, stream);
+    }
+    if ((st = dtrsm_launch('L', 'U', 'T', 'N', n, nrhs, 1.0, A, ldA, B, ldB, stream)) != kOk) return st;
+    if ((st = dtrsm_launch('L', 'L', 'T', 'U', n, nrhs, 1.0, A, ldA, B, ldB, stream)) != kOk) return st;
+    return dlaswp_launch(n, nrhs, B, ldB, 1, n, ipiv, -1, stream);
+}
+
+}  // namespace fg

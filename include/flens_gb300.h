@@ -1,0 +1,127 @@
+/*
+ * flens_gb300.h -- C ABI of the GB300 dense GEMM / TRSM / LU library.
+ *
+ * Two groups of entry points:
+ *
+ *  1. Fortran-ABI drop-ins.  Same symbols, signatures, argument checks and
+ *     error convention as the reference's shims; HOST pointers (device or
+ *     managed pointers are also accepted), column-major, 1-based IPIV.
+ *     INTEGER is int and names carry one trailing underscore, as in
+ *     flens/lapack/interface/include/config.h:11,29-31 and
+ *     flens/blas/interface/blas/config.h:22-28.  Argument errors call
+ *     xerbla_(name, &pos, 6) and return (LAPACK routines also set INFO=-pos).
+ *     A CUDA failure sets INFO to a FLENS_GB300_ERR_* code (< -1000); the BLAS
+ *     routines, which have no INFO, print it and record it for
+ *     flens_gb300_last_error().
+ *
+ *  2. flens_gb300_* device-pointer entry points (extension; no counterpart in
+ *     the reference).  All pointers are device pointers, work is queued on
+ *     `stream` (a cudaStream_t, NULL = legacy default stream) and the call
+ *     returns without waiting unless stated.  Return value: 0 on success,
+ *     -pos for an illegal argument pos (1-based, LAPACK numbering), or a
+ *     FLENS_GB300_ERR_* code.
+ */
+#ifndef FLENS_GB300_H
+#define FLENS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FLENS_GB300_ERR_CUDA          (-1001)
+#define FLENS_GB300_ERR_TIMEOUT       (-1002)
+#define FLENS_GB300_ERR_NO_DEVICE     (-1003)
+#define FLENS_GB300_ERR_ALLOC         (-1004)
+#define FLENS_GB300_ERR_UNSUPPORTED   (-1005)
+#define FLENS_GB300_ERR_NOT_CONVERGED (-1006)
+
+/* ---------------------------------------------- Fortran-ABI drop-ins --- */
+
+/* C <- beta*C + alpha*op(A)*op(B).
+ * Replaces dgemm_ at flens/blas/interface/blas/gemm.cc:120-133 (checks :158-181,
+ * then blas::mm :226 -> cxxblas::gemm cxxblas/level3/gemm.tcc:176-190). */
+void dgemm_(const char *TRANSA, const char *TRANSB, const int *M, const int *N,
+            const int *K, const double *ALPHA, const double *A, const int *LDA,
+            const double *B, const int *LDB, const double *BETA, double *C,
+            const int *LDC);
+
+/* B <- alpha*op(A)^-1*B (SIDE='L') or alpha*B*op(A)^-1 (SIDE='R').
+ * Replaces dtrsm_ at flens/blas/interface/blas/trsm.cc:90-102 (checks
+ * :136-160, then blas::sm :166 -> cxxblas::trsm cxxblas/level3/trsm.tcc:70-82). */
+void dtrsm_(const char *SIDE, const char *UPLO, const char *TRANSA,
+            const char *DIAG, const int *M, const int *N, const double *ALPHA,
+            const double *A, const int *LDA, double *B, const int *LDB);
+
+/* A = P*L*U with partial pivoting; INFO>0: U(INFO,INFO) is exactly zero.
+ * Replaces dgetrf_ at flens/lapack/interface/src/getrf.cc:10-45
+ * (-> lapack::trf flens/lapack/ge/trf.tcc:187-261). */
+void dgetrf_(const int *M, const int *N, double *A, const int *LDA, int *IPIV,
+             int *INFO);
+
+/* Solve op(A)*X = B from dgetrf_'s factors.
+ * Replaces dgetrs_ at flens/lapack/interface/src/getrs.cc:13-53
+ * (-> lapack::trs flens/lapack/ge/trs.tcc:151-223). */
+void dgetrs_(const char *TRANS, const int *N, const int *NRHS, const double *A,
+             const int *LDA, const int *IPIV, double *B, const int *LDB,
+             int *INFO);
+
+/* Factor and solve A*X = B (no solve when INFO>0).
+ * Replaces dgesv_ at flens/lapack/interface/src/gesv.cc:13-49
+ * (-> lapack::sv flens/lapack/ge/sv.tcc:115-219). */
+void dgesv_(const int *N, const int *NRHS, double *A, const int *LDA, int *IPIV,
+            double *B, const int *LDB, int *INFO);
+
+/* Weak default error handler (prints, does not stop).  Link your own
+ * xerbla_ to override it, as with Netlib BLAS/LAPACK. */
+void xerbla_(const char *SRNAME, const int *INFO, int SRNAME_LEN);
+
+/* ---------------------------------------- device-pointer entry points --- */
+
+/* dgemm on device memory (same semantics as dgemm_: beta scaling first,
+ * alpha==0 returns without reading A or B).  Async on stream. */
+int flens_gb300_dgemm(char transA, char transB, int m, int n, int k,
+                      double alpha, const double *A, int ldA,
+                      const double *B, int ldB, double beta, double *C,
+                      int ldC, void *stream);
+
+/* dtrsm on device memory.  Async on stream. */
+int flens_gb300_dtrsm(char side, char uplo, char transA, char diag, int m,
+                      int n, double alpha, const double *A, int ldA,
+                      double *B, int ldB, void *stream);
+
+/* dgetrf on device memory: ipiv (min(m,n) ints, 1-based) and info (one int)
+ * are device pointers, written asynchronously.  Async on stream. */
+int flens_gb300_dgetrf(int m, int n, double *A, int ldA, int *ipiv, int *info,
+                       void *stream);
+
+/* dgetrs on device memory (ipiv device, 1-based).  Async on stream. */
+int flens_gb300_dgetrs(char trans, int n, int nrhs, const double *A, int ldA,
+                       const int *ipiv, double *B, int ldB, void *stream);
+
+/* dgesv on device memory.  Waits for the factorisation to read *info (a
+ * device int) and solves only when it is 0; the solve is queued async. */
+int flens_gb300_dgesv(int n, int nrhs, double *A, int ldA, int *ipiv, double *B,
+                      int ldB, int *info, void *stream);
+
+/* Waits for `stream` and reports device-side failures (a bounded wait that
+ * timed out) as FLENS_GB300_ERR_TIMEOUT. */
+int flens_gb300_sync(void *stream);
+
+/* Last error message of the calling thread ("" if none). */
+const char *flens_gb300_last_error(void);
+
+/* xerbla_ calls made by this library on the calling thread: count, the last
+ * parameter position and routine name (for callers that cannot override
+ * xerbla_). */
+int flens_gb300_xerbla_calls(void);
+int flens_gb300_xerbla_info(void);
+const char *flens_gb300_xerbla_name(void);
+
+/* Library version as an integer (major*100 + minor). */
+int flens_gb300_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLENS_GB300_H */

@@ -1,0 +1,280 @@
+"""Oracle loader -- TEST INFRASTRUCTURE ONLY.
+
+Loads the CPU restatement of FLENS's generic GEMM/TRSM/LU path
+(``libflens_oracle.so`` built from ``flens_oracle.c``) and, when it was built
+in this checkout, the reference's own Fortran-ABI shims compiled from source
+(``_ref/libflens_ref.so``).  Only ``tests/``, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py`` may import this package; the product
+library never does.
+
+All wrappers take numpy arrays in Fortran (column-major) order and work in
+place like the LAPACK routines they mirror.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "libflens_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libflens_ref.so")
+REFERENCE_SRC = "/root/reference"
+
+_c_int_p = ctypes.POINTER(ctypes.c_int)
+_c_double_p = ctypes.POINTER(ctypes.c_double)
+
+
+def build(with_ref: bool | None = None) -> None:
+    """Compile the restatement, and the reference shims if the sources exist."""
+    targets = ["port"]
+    if with_ref is None:
+        with_ref = os.path.isdir(REFERENCE_SRC)
+    if with_ref:
+        targets.append("ref")
+    subprocess.run(["make", "-s", "-j8", "-C", HERE] + targets, check=True)
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_c_double_p)
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(_c_int_p)
+
+
+def _check_f64(a: np.ndarray) -> None:
+    if a.dtype != np.float64 or not a.flags.f_contiguous:
+        raise ValueError("expected a Fortran-ordered float64 array")
+
+
+class Port:
+    """ctypes view of the C restatement (oracle_* symbols)."""
+
+    def __init__(self, path: str = PORT_SO):
+        if not os.path.exists(path):
+            build(with_ref=False)
+        self.lib = ctypes.CDLL(path)
+        L = self.lib
+        c, i, d = ctypes.c_char, ctypes.c_int, ctypes.c_double
+        L.oracle_dgemm.argtypes = [c, c, i, i, i, d, _c_double_p, i, _c_double_p, i,
+                                   d, _c_double_p, i]
+        L.oracle_dtrsm.argtypes = [c, c, c, c, i, i, d, _c_double_p, i, _c_double_p, i]
+        L.oracle_idamax.argtypes = [i, _c_double_p, i]
+        L.oracle_idamax.restype = i
+        L.oracle_dlaswp.argtypes = [i, _c_double_p, i, i, i, _c_int_p, i]
+        L.oracle_dgetf2.argtypes = [i, i, _c_double_p, i, _c_int_p]
+        L.oracle_dgetf2.restype = i
+        L.oracle_dgetrf_nb.argtypes = [i, i, _c_double_p, i, _c_int_p, i]
+        L.oracle_dgetrf_nb.restype = i
+        L.oracle_dgetrf.argtypes = [i, i, _c_double_p, i, _c_int_p]
+        L.oracle_dgetrf.restype = i
+        L.oracle_dgetrf_steps.argtypes = [i, i, _c_double_p, i, _c_int_p, i, i]
+        L.oracle_dgetrf_steps.restype = i
+        L.oracle_dgetrs.argtypes = [c, i, i, _c_double_p, i, _c_int_p, _c_double_p, i]
+        L.oracle_dgesv.argtypes = [i, i, _c_double_p, i, _c_int_p, _c_double_p, i]
+        L.oracle_dgesv.restype = i
+        L.oracle_time_dgetrf_steps.argtypes = [i, i, i, ctypes.c_ulonglong, _c_double_p]
+        L.oracle_time_dgetrf_steps.restype = d
+        L.oracle_time_dgemm_rows.argtypes = [i, i, i, i, i, ctypes.c_ulonglong]
+        L.oracle_time_dgemm_rows.restype = d
+
+    # -- level 3 ---------------------------------------------------------
+    def dgemm(self, transA, transB, alpha, A, B, beta, C):
+        _check_f64(A), _check_f64(B), _check_f64(C)
+        m, n = C.shape
+        k = A.shape[1] if transA.upper() == "N" else A.shape[0]
+        self.lib.oracle_dgemm(transA.encode(), transB.encode(), m, n, k, alpha,
+                              _dp(A), max(1, A.shape[0]), _dp(B), max(1, B.shape[0]),
+                              beta, _dp(C), max(1, m))
+        return C
+
+    def dtrsm(self, side, uplo, transA, diag, alpha, A, B):
+        _check_f64(A), _check_f64(B)
+        m, n = B.shape
+        self.lib.oracle_dtrsm(side.encode(), uplo.encode(), transA.encode(),
+                              diag.encode(), m, n, alpha, _dp(A), max(1, A.shape[0]),
+                              _dp(B), max(1, m))
+        return B
+
+    # -- LU ----------------------------------------------------------------
+    def idamax(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        return self.lib.oracle_idamax(x.size, _dp(x), 1)
+
+    def dgetrf(self, A, nb: int = 64):
+        _check_f64(A)
+        m, n = A.shape
+        piv = np.zeros(max(1, min(m, n)), dtype=np.int32)
+        info = self.lib.oracle_dgetrf_nb(m, n, _dp(A), max(1, m), _ip(piv), nb)
+        return piv[: min(m, n)], info
+
+    def dgetrs(self, trans, LU, piv, B):
+        _check_f64(LU), _check_f64(B)
+        n = LU.shape[0]
+        piv = np.ascontiguousarray(piv, dtype=np.int32)
+        self.lib.oracle_dgetrs(trans.encode(), n, B.shape[1], _dp(LU), max(1, n),
+                               _ip(piv), _dp(B), max(1, n))
+        return B
+
+    def dgesv(self, A, B):
+        _check_f64(A), _check_f64(B)
+        n = A.shape[0]
+        piv = np.zeros(max(1, n), dtype=np.int32)
+        info = self.lib.oracle_dgesv(n, B.shape[1], _dp(A), max(1, n), _ip(piv),
+                                     _dp(B), max(1, n))
+        return piv[:n], info
+
+    # -- timing (CPU baseline) ---------------------------------------------
+    def time_dgetrf_steps(self, n, n_blocks, n_threads, seed=1234):
+        fl = ctypes.c_double(0.0)
+        t = self.lib.oracle_time_dgetrf_steps(n, n_blocks, n_threads, seed,
+                                              ctypes.byref(fl))
+        return t, fl.value
+
+    def time_dgemm_rows(self, m, n, k, rows, n_threads, seed=1234):
+        return self.lib.oracle_time_dgemm_rows(m, n, k, rows, n_threads, seed)
+
+
+class Reference:
+    """ctypes view of the reference's own Fortran-ABI shims (oracle/_ref)."""
+
+    def __init__(self, path: str = REF_SO):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = ctypes.CDLL(path)
+        L = self.lib
+        cp = ctypes.c_char_p
+        L.dgemm_.argtypes = [cp, cp, _c_int_p, _c_int_p, _c_int_p, _c_double_p,
+                             _c_double_p, _c_int_p, _c_double_p, _c_int_p,
+                             _c_double_p, _c_double_p, _c_int_p]
+        L.dtrsm_.argtypes = [cp, cp, cp, cp, _c_int_p, _c_int_p, _c_double_p,
+                             _c_double_p, _c_int_p, _c_double_p, _c_int_p]
+        L.dgetrf_.argtypes = [_c_int_p, _c_int_p, _c_double_p, _c_int_p, _c_int_p,
+                              _c_int_p]
+        L.dgetrs_.argtypes = [cp, _c_int_p, _c_int_p, _c_double_p, _c_int_p,
+                              _c_int_p, _c_double_p, _c_int_p, _c_int_p]
+        L.dgesv_.argtypes = [_c_int_p, _c_int_p, _c_double_p, _c_int_p, _c_int_p,
+                             _c_double_p, _c_int_p, _c_int_p]
+        L.ref_xerbla_calls.restype = ctypes.c_int
+        L.ref_xerbla_info.restype = ctypes.c_int
+        L.ref_xerbla_name.restype = ctypes.c_char_p
+
+    @staticmethod
+    def _i(v):
+        return ctypes.byref(ctypes.c_int(int(v)))
+
+    @staticmethod
+    def _d(v):
+        return ctypes.byref(ctypes.c_double(float(v)))
+
+    def dgemm(self, transA, transB, alpha, A, B, beta, C):
+        _check_f64(A), _check_f64(B), _check_f64(C)
+        m, n = C.shape
+        k = A.shape[1] if transA.upper() == "N" else A.shape[0]
+        self.lib.dgemm_(transA.encode(), transB.encode(), self._i(m), self._i(n),
+                        self._i(k), self._d(alpha), _dp(A), self._i(max(1, A.shape[0])),
+                        _dp(B), self._i(max(1, B.shape[0])), self._d(beta), _dp(C),
+                        self._i(max(1, m)))
+        return C
+
+    def dtrsm(self, side, uplo, transA, diag, alpha, A, B):
+        _check_f64(A), _check_f64(B)
+        m, n = B.shape
+        self.lib.dtrsm_(side.encode(), uplo.encode(), transA.encode(), diag.encode(),
+                        self._i(m), self._i(n), self._d(alpha), _dp(A),
+                        self._i(max(1, A.shape[0])), _dp(B), self._i(max(1, m)))
+        return B
+
+    def dgetrf(self, A):
+        _check_f64(A)
+        m, n = A.shape
+        piv = np.zeros(max(1, min(m, n)), dtype=np.int32)
+        info = ctypes.c_int(0)
+        self.lib.dgetrf_(self._i(m), self._i(n), _dp(A), self._i(max(1, m)), _ip(piv),
+                         ctypes.byref(info))
+        return piv[: min(m, n)], info.value
+
+    def dgetrs(self, trans, LU, piv, B):
+        n = LU.shape[0]
+        piv = np.ascontiguousarray(piv, dtype=np.int32)
+        info = ctypes.c_int(0)
+        self.lib.dgetrs_(trans.encode(), self._i(n), self._i(B.shape[1]), _dp(LU),
+                         self._i(max(1, n)), _ip(piv), _dp(B), self._i(max(1, n)),
+                         ctypes.byref(info))
+        return B, info.value
+
+    def dgesv(self, A, B):
+        n = A.shape[0]
+        piv = np.zeros(max(1, n), dtype=np.int32)
+        info = ctypes.c_int(0)
+        self.lib.dgesv_(self._i(n), self._i(B.shape[1]), _dp(A), self._i(max(1, n)),
+                        _ip(piv), _dp(B), self._i(max(1, n)), ctypes.byref(info))
+        return piv[:n], info.value
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+# -------------------------------------------------------------- inputs --
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def splitmix_uniform(seed: int, m: int, n: int) -> np.ndarray:
+    """Column-major m x n matrix, entries uniform in [-1,1), from splitmix64.
+
+    Element e (column-major position) is 2*u-1 with u = (splitmix64(seed, e) >> 11) * 2^-53.
+    Pure integer arithmetic, so the same on every machine and numpy version;
+    the fixtures in tests/golden store only the reference's outputs for it.
+    """
+    with np.errstate(over="ignore"):
+        e = np.arange(m * n, dtype=np.uint64)
+        z = (np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15)) + (e + np.uint64(1)) * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    u = (z >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
+    return np.asfortranarray((2.0 * u - 1.0).reshape((n, m)).T)
+
+
+def uniform(rng, m: int, n: int) -> np.ndarray:
+    """uniform[-1,1] entries, column-major (rng: numpy Generator or an int seed)."""
+    if isinstance(rng, (int, np.integer)):
+        return splitmix_uniform(int(rng), m, n)
+    return np.asfortranarray(rng.uniform(-1.0, 1.0, size=(m, n)))
+
+
+def shifted_square(rng, n: int) -> np.ndarray:
+    """uniform[-1,1] + (n/4) I: the well-separated-pivot input of the LU configs."""
+    A = uniform(rng, n, n)
+    A[np.arange(n), np.arange(n)] += n / 4.0
+    return A
+
+
+# -------------------------------------------------------------- metrics --
+EPS64 = np.finfo(np.float64).eps
+
+
+def lu_backward_error(A0: np.ndarray, LU: np.ndarray, piv: np.ndarray) -> float:
+    """||P A - L U||_1 / (n ||A||_1 eps), the LAPACK dget01 style ratio."""
+    m, n = A0.shape
+    mn = min(m, n)
+    L = np.tril(LU[:, :mn], -1) + np.eye(m, mn)
+    U = np.triu(LU[:mn, :])
+    PA = A0.copy()
+    for i in range(mn):
+        p = int(piv[i]) - 1
+        if p != i:
+            PA[[i, p], :] = PA[[p, i], :]
+    r = np.abs(PA - L @ U).sum(axis=0).max()
+    an = max(np.abs(A0).sum(axis=0).max(), np.finfo(float).tiny)
+    return float(r / (max(n, 1) * an * EPS64))
+
+
+def normwise_rel(X: np.ndarray, Y: np.ndarray) -> float:
+    d = np.linalg.norm(X - Y)
+    s = np.linalg.norm(Y)
+    return float(d / s) if s > 0 else float(d)

@@ -1,0 +1,469 @@
+/*
+ * flens_oracle.c -- CPU restatement of FLENS's generic dense level-3 / LU path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle the CUDA library is
+ * checked against and the CPU baseline that bench.py times.  The product
+ * (flens_gb300/csrc) never links or calls it.
+ *
+ * Each function restates the reference's generic C++ template for real double
+ * precision, keeping its operation order (which element is scaled first, the
+ * direction and start value of every dot product, reciprocal-multiply versus
+ * divide), so that with -ffp-contract=off it is bitwise identical to the
+ * reference's dgemm_/dtrsm_/dgetrf_/dgetrs_/dgesv_ compiled from source.
+ * tests/test_oracle_pin.py checks that identity whenever oracle/_ref exists.
+ * Citations are file:line inside the FLENS source tree.
+ */
+#define _GNU_SOURCE
+#include "flens_oracle.h"
+
+#include <float.h>
+#include <stddef.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#define IDX(i, j, ld) ((size_t)(i) + (size_t)(j) * (size_t)(ld))
+
+static int is_notrans(char t) { return t == 'N' || t == 'n'; }
+
+/*
+ * GEMM.  cxxblas/level3/gemm.tcc:42-75 turns the column-major call into a
+ * row-major one, scales C by beta first (gescal, :66; multiply, not assign,
+ * cxxblas/level1/scal.tcc:40-49), returns when alpha==0 (:67-69) and then, per
+ * row of C, calls gemv (:70-75) whose per-element result is a dot product
+ * started at zero and summed in increasing k (cxxblas/level2/gemv.tcc:75-79,
+ * cxxblas/level1/dot.tcc:48-51), added as C += alpha*dot.
+ */
+void oracle_dgemm(char transA, char transB, int m, int n, int k,
+                  double alpha, const double *A, int ldA,
+                  const double *B, int ldB,
+                  double beta, double *C, int ldC)
+{
+    if (m == 0 || n == 0) {
+        return;
+    }
+    for (int j = 0; j < n; ++j) {
+        for (int i = 0; i < m; ++i) {
+            C[IDX(i, j, ldC)] *= beta;
+        }
+    }
+    if (alpha == 0.0) {
+        return;
+    }
+    const int nA = is_notrans(transA), nB = is_notrans(transB);
+    /* op(A)(i,p) and op(B)(p,j) as strides */
+    const size_t aI = nA ? 1 : (size_t)ldA, aP = nA ? (size_t)ldA : 1;
+    const size_t bP = nB ? 1 : (size_t)ldB, bJ = nB ? (size_t)ldB : 1;
+    /* Loop nest as the reference: rows of C outermost (one gemv per row),
+     * columns next, k innermost. */
+    for (int i = 0; i < m; ++i) {
+        for (int j = 0; j < n; ++j) {
+            double dot = 0.0;
+            const double *a = A + (size_t)i * aI;
+            const double *b = B + (size_t)j * bJ;
+            for (int p = 0; p < k; ++p) {
+                dot += b[(size_t)p * bP] * a[(size_t)p * aP];
+            }
+            C[IDX(i, j, ldC)] += alpha * dot;
+        }
+    }
+}
+
+/*
+ * TRSM.  cxxblas/level3/trsm.tcc:40-68: column-major is mapped to row-major,
+ * every right-hand side is solved by trsv (dot-form substitution,
+ * cxxblas/level2/trsv.tcc:48-200: x_i -= sum_p M(i,p) x_p with the sum started
+ * at zero and taken in increasing p, then x_i /= M(i,i) for non-unit), and
+ * alpha is applied AFTER the solve (:67, gescal).  For side=Left the effective
+ * triangle is op(A) and the vectors are the columns of B; for side=Right it is
+ * op(A)^T and the vectors are the rows of B.
+ */
+void oracle_dtrsm(char side, char upLo, char transA, char diag,
+                  int m, int n, double alpha,
+                  const double *A, int ldA, double *B, int ldB)
+{
+    const int left = (side == 'L' || side == 'l');
+    const int lowerA = (upLo == 'L' || upLo == 'l');
+    const int nT = is_notrans(transA);
+    const int unit = (diag == 'U' || diag == 'u');
+    const int ka = left ? m : n;
+    const int nVec = left ? n : m;
+    /* M(i,p) = A[i*mi + p*mp] */
+    size_t mi, mp;
+    int lowerM;
+    if (left) {
+        lowerM = lowerA ^ (!nT);
+        mi = nT ? 1 : (size_t)ldA;
+        mp = nT ? (size_t)ldA : 1;
+    } else {
+        lowerM = lowerA ^ nT;
+        mi = nT ? (size_t)ldA : 1;
+        mp = nT ? 1 : (size_t)ldA;
+    }
+    const size_t xs = left ? 1 : (size_t)ldB;      /* stride inside a vector */
+    const size_t vs = left ? (size_t)ldB : 1;      /* stride between vectors */
+    for (int v = 0; v < nVec; ++v) {
+        double *x = B + (size_t)v * vs;
+        if (lowerM) {
+            for (int i = 0; i < ka; ++i) {
+                double s = 0.0;
+                for (int p = 0; p < i; ++p) {
+                    s += A[(size_t)i * mi + (size_t)p * mp] * x[(size_t)p * xs];
+                }
+                x[(size_t)i * xs] -= s;
+                if (!unit) {
+                    x[(size_t)i * xs] /= A[(size_t)i * mi + (size_t)i * mp];
+                }
+            }
+        } else {
+            for (int i = ka - 1; i >= 0; --i) {
+                double s = 0.0;
+                for (int q = i + 1; q < ka; ++q) {
+                    s += A[(size_t)i * mi + (size_t)q * mp] * x[(size_t)q * xs];
+                }
+                x[(size_t)i * xs] -= s;
+                if (!unit) {
+                    x[(size_t)i * xs] /= A[(size_t)i * mi + (size_t)i * mp];
+                }
+            }
+        }
+    }
+    for (int j = 0; j < n; ++j) {
+        for (int i = 0; i < m; ++i) {
+            B[IDX(i, j, ldB)] *= alpha;
+        }
+    }
+}
+
+/*
+ * IAMAX.  cxxblas/level1/iamax.tcc:42-58 and :80-92: start from element 0,
+ * replace only on a strictly greater |x_i| (first maximum wins; a NaN never
+ * wins unless it is element 0); n<=0 gives -1.
+ */
+int oracle_idamax(int n, const double *x, int incX)
+{
+    if (incX < 0) {
+        x -= (ptrdiff_t)incX * (n - 1);
+    }
+    if (n <= 0) {
+        return -1;
+    }
+    int iMax = 0;
+    double absMax = fabs(x[0]);
+    for (int i = 0; i < n; ++i) {
+        const double a = fabs(x[(ptrdiff_t)i * incX]);
+        if (a > absMax) {
+            iMax = i;
+            absMax = a;
+        }
+    }
+    return iMax;
+}
+
+static void swap_row_segment(double *A, int ldA, int r1, int r2, int c0, int c1)
+{
+    for (int c = c0; c < c1; ++c) {
+        const double t = A[IDX(r1, c, ldA)];
+        A[IDX(r1, c, ldA)] = A[IDX(r2, c, ldA)];
+        A[IDX(r2, c, ldA)] = t;
+    }
+}
+
+/*
+ * LASWP.  flens/lapack/la/laswp.tcc:54-93: columns in blocks of 32, inside a
+ * block the interchanges i <-> piv(i) for i = k1..k2 (or k2..k1 when the pivot
+ * view is reversed, as trs.tcc:106 does for the transposed solve).
+ */
+void oracle_dlaswp(int nCols, double *A, int ldA, int k1, int k2,
+                   const int *piv, int inc)
+{
+    const int bs = 32;
+    const int nbs = (nCols / bs) * bs;
+    for (int c0 = 0; c0 < nCols; c0 += bs) {
+        const int c1 = (c0 < nbs) ? c0 + bs : nCols;
+        if (inc > 0) {
+            for (int i = k1; i <= k2; ++i) {
+                const int ip = piv[i - 1];
+                if (ip != i) swap_row_segment(A, ldA, i - 1, ip - 1, c0, c1);
+            }
+        } else {
+            for (int i = k2; i >= k1; --i) {
+                const int ip = piv[i - 1];
+                if (ip != i) swap_row_segment(A, ldA, i - 1, ip - 1, c0, c1);
+            }
+        }
+    }
+}
+
+/*
+ * TF2.  flens/lapack/ge/tf2.tcc:56-136.  Per column: iamax pivot (:101-102),
+ * swap of the whole panel row (:108), scale by the reciprocal when
+ * |pivot| >= SafeMin, else divide (:113-121), zero pivot sets info once
+ * (:123-125), then the rank-1 update A22 += (-1*row_j) * col_j column by column
+ * (:131 -> cxxblas/level2/ger.tcc:41-64 -> axpy).  SafeMin is DBL_MIN
+ * (flens/lapack/la/lamch.tcc:73-81: 1/DBL_MAX < DBL_MIN).
+ */
+int oracle_dgetf2(int m, int n, double *A, int ldA, int *piv)
+{
+    int info = 0;
+    if (m == 0 || n == 0) {
+        return info;
+    }
+    const double safeMin = DBL_MIN;
+    const int mn = m < n ? m : n;
+    for (int j = 0; j < mn; ++j) {
+        const int jp = j + oracle_idamax(m - j, &A[IDX(j, j, ldA)], 1);
+        piv[j] = jp + 1;
+        if (A[IDX(jp, j, ldA)] != 0.0) {
+            if (jp != j) {
+                swap_row_segment(A, ldA, j, jp, 0, n);
+            }
+            if (j < m - 1) {
+                const double ajj = A[IDX(j, j, ldA)];
+                if (fabs(ajj) >= safeMin) {
+                    const double r = 1.0 / ajj;
+                    for (int i = j + 1; i < m; ++i) A[IDX(i, j, ldA)] *= r;
+                } else {
+                    for (int i = j + 1; i < m; ++i) A[IDX(i, j, ldA)] /= ajj;
+                }
+            }
+        } else if (info == 0) {
+            info = j + 1;
+        }
+        if (j + 1 < mn) {
+            for (int c = j + 1; c < n; ++c) {
+                const double y = -1.0 * A[IDX(j, c, ldA)];
+                for (int i = j + 1; i < m; ++i) {
+                    A[IDX(i, c, ldA)] += y * A[IDX(i, j, ldA)];
+                }
+            }
+        }
+    }
+    return info;
+}
+
+/*
+ * TRF.  flens/lapack/ge/trf.tcc:59-152 with bs = ilaenv(1,"GETRF") = 64
+ * (flens/lapack/la/ilaenv.tcc:93-99); unblocked when bs<=1 or bs>=min(m,n)
+ * (:87-91).  Per block: panel tf2 (:113), info/pivot offset (:117-122),
+ * laswp left (:126) and right (:132), trsm for the U block row (:136-138),
+ * trailing gemm with alpha=-1, beta=1 (:144-146).
+ */
+static int dgetrf_impl(int m, int n, double *A, int ldA, int *piv, int nb,
+                       int maxBlocks)
+{
+    int info = 0;
+    if (m == 0 || n == 0) {
+        return info;
+    }
+    const int mn = m < n ? m : n;
+    if (nb <= 1 || nb >= mn) {
+        return oracle_dgetf2(m, n, A, ldA, piv);
+    }
+    int blocks = 0;
+    for (int j = 1; j <= mn; j += nb) {
+        if (maxBlocks >= 0 && blocks++ >= maxBlocks) {
+            break;
+        }
+        const int jb = (mn - j + 1 < nb) ? mn - j + 1 : nb;
+        const int info_ = oracle_dgetf2(m - j + 1, jb, &A[IDX(j - 1, j - 1, ldA)],
+                                        ldA, &piv[j - 1]);
+        if (info == 0 && info_ > 0) {
+            info = info_ + j - 1;
+        }
+        const int iEnd = (m < j + jb - 1) ? m : j + jb - 1;
+        for (int i = j; i <= iEnd; ++i) {
+            piv[i - 1] += j - 1;
+        }
+        oracle_dlaswp(j - 1, A, ldA, j, j + jb - 1, piv, 1);
+        if (j + jb <= n) {
+            oracle_dlaswp(n - j - jb + 1, &A[IDX(0, j + jb - 1, ldA)], ldA,
+                          j, j + jb - 1, piv, 1);
+            oracle_dtrsm('L', 'L', 'N', 'U', jb, n - j - jb + 1, 1.0,
+                         &A[IDX(j - 1, j - 1, ldA)], ldA,
+                         &A[IDX(j - 1, j + jb - 1, ldA)], ldA);
+            if (j + jb <= m) {
+                oracle_dgemm('N', 'N', m - j - jb + 1, n - j - jb + 1, jb,
+                             -1.0, &A[IDX(j + jb - 1, j - 1, ldA)], ldA,
+                             &A[IDX(j - 1, j + jb - 1, ldA)], ldA,
+                             1.0, &A[IDX(j + jb - 1, j + jb - 1, ldA)], ldA);
+            }
+        }
+    }
+    return info;
+}
+
+int oracle_dgetrf_nb(int m, int n, double *A, int ldA, int *piv, int nb)
+{
+    return dgetrf_impl(m, n, A, ldA, piv, nb, -1);
+}
+
+int oracle_dgetrf(int m, int n, double *A, int ldA, int *piv)
+{
+    return dgetrf_impl(m, n, A, ldA, piv, 64, -1);
+}
+
+int oracle_dgetrf_steps(int m, int n, double *A, int ldA, int *piv,
+                        int nb, int nBlocks)
+{
+    return dgetrf_impl(m, n, A, ldA, piv, nb, nBlocks);
+}
+
+/*
+ * TRS.  flens/lapack/ge/trs.tcc:59-109.  NoTrans: laswp forward, L (unit
+ * lower) then U (non-unit upper).  Trans/ConjTrans: U^T, L^T, then laswp with
+ * the pivot vector reversed.
+ */
+void oracle_dgetrs(char trans, int n, int nRhs, const double *A, int ldA,
+                   const int *piv, double *B, int ldB)
+{
+    if (n == 0 || nRhs == 0) {
+        return;
+    }
+    if (is_notrans(trans)) {
+        oracle_dlaswp(nRhs, B, ldB, 1, n, piv, 1);
+        oracle_dtrsm('L', 'L', 'N', 'U', n, nRhs, 1.0, A, ldA, B, ldB);
+        oracle_dtrsm('L', 'U', 'N', 'N', n, nRhs, 1.0, A, ldA, B, ldB);
+    } else {
+        oracle_dtrsm('L', 'U', trans, 'N', n, nRhs, 1.0, A, ldA, B, ldB);
+        oracle_dtrsm('L', 'L', trans, 'U', n, nRhs, 1.0, A, ldA, B, ldB);
+        oracle_dlaswp(nRhs, B, ldB, 1, n, piv, -1);
+    }
+}
+
+/* SV.  flens/lapack/ge/sv.tcc:58-77: trf, then trs only when info==0. */
+int oracle_dgesv(int n, int nRhs, double *A, int ldA, int *piv,
+                 double *B, int ldB)
+{
+    const int info = oracle_dgetrf(n, n, A, ldA, piv);
+    if (info == 0) {
+        oracle_dgetrs('N', n, nRhs, A, ldA, piv, B, ldB);
+    }
+    return info;
+}
+
+/* ---------------------------------------------------------------- timing -- */
+
+static unsigned long long splitmix64(unsigned long long *s)
+{
+    unsigned long long z = (*s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+static double uniform_pm1(unsigned long long *s)
+{
+    return 2.0 * ((double)(splitmix64(s) >> 11) * 0x1.0p-53) - 1.0;
+}
+
+static double now_seconds(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+typedef struct {
+    int kind;            /* 0 = dgetrf steps, 1 = dgemm rows */
+    int m, n, k, rows, nBlocks;
+    unsigned long long seed;
+    pthread_barrier_t *barrier;
+    double t0, t1, flops;
+} job_t;
+
+static void *run_job(void *arg)
+{
+    job_t *jb = (job_t *)arg;
+    unsigned long long s = jb->seed;
+    if (jb->kind == 0) {
+        const int n = jb->n;
+        double *A = (double *)malloc(sizeof(double) * (size_t)n * n);
+        int *piv = (int *)malloc(sizeof(int) * (size_t)n);
+        for (size_t i = 0; i < (size_t)n * n; ++i) A[i] = uniform_pm1(&s);
+        for (int i = 0; i < n; ++i) A[IDX(i, i, n)] += 0.25 * n;
+        pthread_barrier_wait(jb->barrier);
+        jb->t0 = now_seconds();
+        oracle_dgetrf_steps(n, n, A, n, piv, 64, jb->nBlocks);
+        jb->t1 = now_seconds();
+        double fl = 0.0;
+        for (int b = 0, j = 0; b < jb->nBlocks && j < n; ++b, j += 64) {
+            const double r = (double)(n - j), w = r < 64 ? r : 64;
+            /* panel + trsm + trailing update of one block step */
+            fl += r * w * w + w * w * (r - w) + 2.0 * (r - w) * (r - w) * w;
+        }
+        jb->flops = fl;
+        free(A);
+        free(piv);
+    } else {
+        const int m = jb->m, n = jb->n, k = jb->k, rows = jb->rows;
+        double *A = (double *)malloc(sizeof(double) * (size_t)m * k);
+        double *B = (double *)malloc(sizeof(double) * (size_t)k * n);
+        double *C = (double *)malloc(sizeof(double) * (size_t)m * n);
+        for (size_t i = 0; i < (size_t)m * k; ++i) A[i] = uniform_pm1(&s);
+        for (size_t i = 0; i < (size_t)k * n; ++i) B[i] = uniform_pm1(&s);
+        for (size_t i = 0; i < (size_t)m * n; ++i) C[i] = uniform_pm1(&s);
+        pthread_barrier_wait(jb->barrier);
+        jb->t0 = now_seconds();
+        oracle_dgemm('N', 'N', rows, n, k, 1.5, A, m, B, k, 0.5, C, m);
+        jb->t1 = now_seconds();
+        jb->flops = 2.0 * rows * (double)n * k;
+        free(A);
+        free(B);
+        free(C);
+    }
+    return NULL;
+}
+
+static double run_jobs(job_t *proto, int nThreads, double *flops_out)
+{
+    pthread_t *th = (pthread_t *)calloc((size_t)nThreads, sizeof(pthread_t));
+    job_t *jobs = (job_t *)calloc((size_t)nThreads, sizeof(job_t));
+    pthread_barrier_t bar;
+    pthread_barrier_init(&bar, NULL, (unsigned)nThreads);
+    for (int t = 0; t < nThreads; ++t) {
+        jobs[t] = *proto;
+        jobs[t].seed = proto->seed + 1000003ULL * (unsigned long long)t;
+        jobs[t].barrier = &bar;
+        pthread_create(&th[t], NULL, run_job, &jobs[t]);
+    }
+    for (int t = 0; t < nThreads; ++t) pthread_join(th[t], NULL);
+    double t0 = jobs[0].t0, t1 = jobs[0].t1;
+    for (int t = 1; t < nThreads; ++t) {
+        if (jobs[t].t0 < t0) t0 = jobs[t].t0;
+        if (jobs[t].t1 > t1) t1 = jobs[t].t1;
+    }
+    if (flops_out) *flops_out = jobs[0].flops;
+    pthread_barrier_destroy(&bar);
+    free(jobs);
+    free(th);
+    return t1 - t0;
+}
+
+double oracle_time_dgetrf_steps(int n, int nBlocks, int nThreads,
+                                unsigned long long seed, double *flops_out)
+{
+    job_t p;
+    memset(&p, 0, sizeof p);
+    p.kind = 0;
+    p.n = n;
+    p.nBlocks = nBlocks;
+    p.seed = seed;
+    return run_jobs(&p, nThreads < 1 ? 1 : nThreads, flops_out);
+}
+
+double oracle_time_dgemm_rows(int m, int n, int k, int rows, int nThreads,
+                              unsigned long long seed)
+{
+    job_t p;
+    memset(&p, 0, sizeof p);
+    p.kind = 1;
+    p.m = m;
+    p.n = n;
+    p.k = k;
+    p.rows = rows;
+    p.seed = seed;
+    return run_jobs(&p, nThreads < 1 ? 1 : nThreads, NULL);
+}

@@ -1,0 +1,81 @@
+/*
+ * flens_oracle.h -- CPU restatement of FLENS's generic dense GEMM / TRSM / LU
+ * path, used ONLY as test infrastructure (the checker for the CUDA library and
+ * the timed CPU baseline in bench.py).  Nothing in the product links this.
+ *
+ * Every routine follows the operation order of the reference's generic C++
+ * templates (cited per function in flens_oracle.c) so that, compiled with
+ * -ffp-contract=off, its results are bitwise identical to the reference's own
+ * Fortran-ABI shims compiled from source (oracle/Makefile target `ref`).
+ *
+ * Conventions: column-major storage, leading dimensions in elements,
+ * pivot vectors 1-based (LAPACK style), characters 'N','T','C','L','R','U'.
+ */
+#ifndef FLENS_ORACLE_H
+#define FLENS_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* C <- beta*C + alpha*op(A)*op(B)            cxxblas/level3/gemm.tcc:42-190 */
+void oracle_dgemm(char transA, char transB, int m, int n, int k,
+                  double alpha, const double *A, int ldA,
+                  const double *B, int ldB,
+                  double beta, double *C, int ldC);
+
+/* B <- alpha*op(A)^-1*B  or  alpha*B*op(A)^-1  cxxblas/level3/trsm.tcc:40-82 */
+void oracle_dtrsm(char side, char upLo, char transA, char diag,
+                  int m, int n, double alpha,
+                  const double *A, int ldA, double *B, int ldB);
+
+/* 0-based index of the first max |x_i|; -1 if n<=0  cxxblas/level1/iamax.tcc:42-92 */
+int oracle_idamax(int n, const double *x, int incX);
+
+/* row interchanges, rows k1..k2 (1-based), inc>0 forward, inc<0 reverse
+ *                                               flens/lapack/la/laswp.tcc:54-93 */
+void oracle_dlaswp(int nCols, double *A, int ldA, int k1, int k2,
+                   const int *piv, int inc);
+
+/* unblocked LU of an m x n panel, piv 1-based local   flens/lapack/ge/tf2.tcc:56-136 */
+int oracle_dgetf2(int m, int n, double *A, int ldA, int *piv);
+
+/* blocked right-looking LU, block size nb (reference: 64)
+ *                                               flens/lapack/ge/trf.tcc:59-152 */
+int oracle_dgetrf_nb(int m, int n, double *A, int ldA, int *piv, int nb);
+int oracle_dgetrf(int m, int n, double *A, int ldA, int *piv);
+
+/* First `nBlocks` block steps of oracle_dgetrf_nb only (a bounded sample of
+ * the full factorisation, for timing); returns info so far. */
+int oracle_dgetrf_steps(int m, int n, double *A, int ldA, int *piv,
+                        int nb, int nBlocks);
+
+/* solve op(A) X = B from the LU factors          flens/lapack/ge/trs.tcc:59-109 */
+void oracle_dgetrs(char trans, int n, int nRhs, const double *A, int ldA,
+                   const int *piv, double *B, int ldB);
+
+/* trf then trs(NoTrans) if info==0               flens/lapack/ge/sv.tcc:58-77 */
+int oracle_dgesv(int n, int nRhs, double *A, int ldA, int *piv,
+                 double *B, int ldB);
+
+/*
+ * Timing helper for the CPU baseline: nThreads independent copies of the
+ * seeded n x n input (uniform[-1,1] + n/4 on the diagonal), each factorised
+ * for the first nBlocks block steps with nb=64.  Returns the wall seconds of
+ * the factorisation phase (all threads started together).  flops_out gets the
+ * flops one thread performed (sum over the steps), so a caller can scale the
+ * sample to a full factorisation.
+ */
+double oracle_time_dgetrf_steps(int n, int nBlocks, int nThreads,
+                                unsigned long long seed, double *flops_out);
+
+/* Same for GEMM: nThreads independent C = 1.5*A*B + 0.5*C on the first
+ * `rows` rows of an m x n x k problem.  Returns wall seconds. */
+double oracle_time_dgemm_rows(int m, int n, int k, int rows, int nThreads,
+                              unsigned long long seed);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,181 @@
+"""Generate the golden fixtures in this directory from the REFERENCE itself.
+
+Runs the reference's own Fortran-ABI shims (dgemm_, dtrsm_, dgetrf_, dgetrs_,
+dgesv_ compiled from the FLENS sources into oracle/_ref/libflens_ref.so by
+``make -C oracle ref``) on seeded inputs and stores the outputs.  Inputs come
+from ``oracle.splitmix_uniform(seed, m, n)`` (integer hashing, identical on
+every machine), so only seeds and outputs are stored.  The fixtures travel
+with the repository: machines without the reference sources (the GPU host)
+still pin the oracle and check the GPU library against the reference's own
+results.
+
+    python tests/golden/make_golden.py            # small fixtures (seconds)
+    python tests/golden/make_golden.py --large    # + the n=8192 LU pivots (minutes)
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+
+U = oracle.splitmix_uniform
+
+
+# ----------------------------------------------------------- case lists --
+# Shared with the tests: each case is (name, parameters); inputs are rebuilt
+# from the parameters with gemm_inputs / trsm_inputs / lu_input.
+def gemm_case_list():
+    cases = []
+    for (m, n, k) in [(0, 3, 2), (1, 1, 1), (3, 0, 5), (4, 3, 0)]:
+        cases.append((m, n, k, "N", "N", 1.5, 0.5))
+    for ta in "NT":
+        for tb in "NT":
+            cases.append((7, 31, 63, ta, tb, 1.5, 0.5))
+    for (a, b) in [(0.0, 1.3), (0.7, 0.0), (1.0, 1.0), (-1.0, 1.0)]:
+        cases.append((7, 31, 63, "N", "N", a, b))
+    for ta in "NTC":
+        for tb in "NTC":
+            cases.append((65, 33, 130, ta, tb, 1.5, 0.5))
+    return [(f"gemm{i:03d}", c) for i, c in enumerate(cases)]
+
+
+def gemm_inputs(i, m, n, k, ta, tb):
+    s = 1000 + 10 * i
+    A = U(s, m if ta == "N" else k, k if ta == "N" else m)
+    B = U(s + 1, k if tb == "N" else n, n if tb == "N" else k)
+    C = U(s + 2, m, n)
+    return A, B, C
+
+
+def trsm_case_list():
+    cases = []
+    for (m, n) in [(33, 17), (70, 3)]:
+        for side in "LR":
+            for uplo in "UL":
+                for ta in "NT":
+                    for diag in "UN":
+                        cases.append((m, n, side, uplo, ta, diag, 0.7))
+    cases.append((33, 17, "L", "L", "C", "N", 1.0))
+    cases.append((1, 5, "L", "U", "N", "N", -2.0))
+    return [(f"trsm{i:03d}", c) for i, c in enumerate(cases)]
+
+
+def trsm_inputs(i, m, n, side):
+    s = 5000 + 10 * i
+    ka = m if side == "L" else n
+    A = U(s, ka, ka)
+    A[np.arange(ka), np.arange(ka)] += 2.0 + ka / 4.0
+    B = U(s + 1, m, n)
+    return A, B
+
+
+def lu_case_list():
+    cases = []
+    for (m, n) in [(1, 1), (2, 2), (4, 4), (10, 7), (7, 10), (31, 31), (64, 64), (65, 65),
+                   (100, 80), (80, 100), (129, 129)]:
+        for kind in ("uniform", "shifted"):
+            cases.append((m, n, kind))
+    return [(f"lu{i:03d}", c) for i, c in enumerate(cases)]
+
+
+def lu_input(i, m, n, kind):
+    A = U(9000 + 10 * i, m, n)
+    if kind == "shifted":
+        d = min(m, n)
+        A[np.arange(d), np.arange(d)] += max(m, n) / 4.0
+    return A
+
+
+def lu_rhs(i, n):
+    return U(9000 + 10 * i + 1, n, 3)
+
+
+def singular_input():
+    A = U(7777, 12, 12)
+    A[:, 2] = 0.0
+    return A
+
+
+def baby_problem():
+    """The 4x4 system of the reference example flens/examples/lapack-gesv.cc:39-47."""
+    A = np.asfortranarray([[2, 3, -1, 0], [-6, -5, 0, 2], [2, -5, 6, -6], [4, 6, 2, -3]],
+                          dtype=np.float64)
+    b = np.asfortranarray([[20], [-33], [-43], [49]], dtype=np.float64)
+    return A, b
+
+
+LARGE_N, LARGE_SEED = 8192, 20261203
+
+
+def large_lu_input():
+    """Config-2 input: n=8192, uniform[-1,1) + (n/4) I (splitmix seed LARGE_SEED)."""
+    return oracle.shifted_square(LARGE_SEED, LARGE_N)
+
+
+# ------------------------------------------------------------- generate --
+def generate_small(R):
+    out = {}
+    for i, (name, (m, n, k, ta, tb, a, b)) in enumerate(gemm_case_list()):
+        A, B, C = gemm_inputs(i, m, n, k, ta, tb)
+        out[name] = R.dgemm(ta, tb, a, A, B, b, C.copy(order="F"))
+    for i, (name, (m, n, side, uplo, ta, diag, alpha)) in enumerate(trsm_case_list()):
+        A, B = trsm_inputs(i, m, n, side)
+        out[name] = R.dtrsm(side, uplo, ta, diag, alpha, A, B.copy(order="F"))
+    for i, (name, (m, n, kind)) in enumerate(lu_case_list()):
+        LU = lu_input(i, m, n, kind)
+        piv, info = R.dgetrf(LU)
+        out[name + "_LU"], out[name + "_piv"] = LU, piv.astype(np.int32)
+        out[name + "_info"] = np.array([info])
+        if m == n:
+            Bm = lu_rhs(i, n)
+            for t in "NT":
+                X, _ = R.dgetrs(t, LU, piv, Bm.copy(order="F"))
+                out[name + f"_X{t}"] = X
+    LU = singular_input()
+    piv, info = R.dgetrf(LU)
+    out["sing_LU"], out["sing_piv"], out["sing_info"] = LU, piv.astype(np.int32), np.array([info])
+    A, b = baby_problem()
+    piv, info = R.dgesv(A, b)
+    out["baby_LU"], out["baby_x"], out["baby_piv"] = A, b, piv.astype(np.int32)
+    out["baby_info"] = np.array([info])
+    return out
+
+
+def generate_large(R):
+    A = large_lu_input()
+    piv, info = R.dgetrf(A)
+    n = LARGE_N
+    nonid = int(np.count_nonzero(piv != np.arange(1, n + 1)))
+    return {"meta": np.array([n, LARGE_SEED, info, nonid], dtype=np.int64),
+            "piv": piv.astype(np.int32),
+            "diagU": np.ascontiguousarray(np.diag(A)),
+            "colsum_LU": A.sum(axis=0)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--large", action="store_true")
+    args = ap.parse_args()
+    oracle.build(with_ref=True)
+    R = oracle.Reference()
+    small = generate_small(R)
+    path = os.path.join(HERE, "reference_small.npz")
+    np.savez_compressed(path, **small)
+    print(f"wrote {path} ({os.path.getsize(path)} bytes, {len(small)} arrays)")
+    if args.large:
+        big = generate_large(R)
+        p2 = os.path.join(HERE, "reference_lu8192.npz")
+        np.savez_compressed(p2, **big)
+        print(f"wrote {p2}: meta(n, seed, info, non-identity pivots)={big['meta'].tolist()}")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,146 @@
+"""C-ABI checks that need no GPU.
+
+* libflens_gb300.so loads and exports every function include/flens_gb300.h
+  declares.
+* Argument checking follows the reference shims: the same parameter
+  positions go to xerbla_ (flens/blas/interface/blas/gemm.cc:158-181,
+  trsm.cc:136-160) and INFO=-pos for the LAPACK routines
+  (flens/lapack/interface/src/getrf.cc:22-35, getrs.cc:25-40, gesv.cc:25-40).
+  These checks run before any CUDA call.
+* Without a GPU the compute paths fail loudly with FLENS_GB300_ERR_NO_DEVICE
+  rather than falling back to the CPU.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import flens_gb300 as fg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "flens_gb300.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(\w+)\s*\(", src, flags=re.M)))
+
+
+def test_header_lists_the_entry_points():
+    names = declared_functions()
+    for f in ("dgemm_", "dtrsm_", "dgetrf_", "dgetrs_", "dgesv_", "flens_gb300_dgetrf"):
+        assert f in names
+
+
+def test_library_exports_every_declared_symbol(flib):
+    missing = [n for n in declared_functions() if not hasattr(flib, n)]
+    assert not missing, missing
+
+
+def _i(v):
+    return ctypes.byref(ctypes.c_int(v))
+
+
+def _d(v):
+    return ctypes.byref(ctypes.c_double(v))
+
+
+NULLD = ctypes.POINTER(ctypes.c_double)()
+NULLI = ctypes.POINTER(ctypes.c_int)()
+
+
+def _xerbla_after(fn):
+    L = fg.lib()
+    before = L.flens_gb300_xerbla_calls()
+    fn()
+    assert L.flens_gb300_xerbla_calls() == before + 1
+    return L.flens_gb300_xerbla_name().decode().strip(), L.flens_gb300_xerbla_info()
+
+
+@pytest.mark.parametrize("args,pos", [
+    (("X", "N", 2, 2, 2, 2, 2, 2), 1),
+    (("N", "Q", 2, 2, 2, 2, 2, 2), 2),
+    (("N", "N", -1, 2, 2, 2, 2, 2), 3),
+    (("N", "N", 2, -1, 2, 2, 2, 2), 4),
+    (("N", "N", 2, 2, -1, 2, 2, 2), 5),
+    (("N", "N", 3, 2, 2, 2, 2, 3), 8),
+    (("T", "N", 2, 2, 3, 2, 3, 2), 8),
+    (("N", "N", 2, 2, 3, 2, 2, 2), 10),
+    (("N", "N", 3, 2, 2, 3, 2, 2), 13),
+])
+def test_dgemm_argument_errors(capfd, args, pos):
+    ta, tb, m, n, k, lda, ldb, ldc = args
+    name, info = _xerbla_after(lambda: fg.lib().dgemm_(
+        ta.encode(), tb.encode(), _i(m), _i(n), _i(k), _d(1.0), NULLD, _i(lda), NULLD, _i(ldb),
+        _d(0.0), NULLD, _i(ldc)))
+    assert name == "DGEMM" and info == pos
+    assert "DGEMM" in capfd.readouterr().err
+
+
+@pytest.mark.parametrize("args,pos", [
+    (("X", "U", "N", "N", 2, 2, 2, 2), 1),
+    (("L", "X", "N", "N", 2, 2, 2, 2), 2),
+    (("L", "U", "X", "N", 2, 2, 2, 2), 3),
+    (("L", "U", "N", "X", 2, 2, 2, 2), 4),
+    (("L", "U", "N", "N", -1, 2, 2, 2), 5),
+    (("L", "U", "N", "N", 2, -1, 2, 2), 6),
+    (("L", "U", "N", "N", 3, 2, 2, 3), 9),
+    (("R", "U", "N", "N", 2, 3, 2, 2), 9),
+    (("L", "U", "N", "N", 3, 2, 3, 2), 11),
+])
+def test_dtrsm_argument_errors(args, pos):
+    side, uplo, ta, diag, m, n, lda, ldb = args
+    name, info = _xerbla_after(lambda: fg.lib().dtrsm_(
+        side.encode(), uplo.encode(), ta.encode(), diag.encode(), _i(m), _i(n), _d(1.0), NULLD,
+        _i(lda), NULLD, _i(ldb)))
+    assert name == "DTRSM" and info == pos
+
+
+def test_lapack_argument_errors():
+    L = fg.lib()
+    info = ctypes.c_int(0)
+    for (m, n, lda, want) in [(-1, 2, 2, -1), (2, -1, 2, -2), (3, 2, 2, -4)]:
+        name, pos = _xerbla_after(lambda: L.dgetrf_(_i(m), _i(n), NULLD, _i(lda), NULLI,
+                                                    ctypes.byref(info)))
+        assert info.value == want and name == "DGETRF" and pos == -want
+    for (tr, n, nrhs, lda, ldb, want) in [("X", 2, 1, 2, 2, -1), ("N", -1, 1, 2, 2, -2),
+                                          ("N", 2, -1, 2, 2, -3), ("N", 3, 1, 2, 3, -5),
+                                          ("N", 3, 1, 3, 2, -8)]:
+        name, pos = _xerbla_after(lambda: L.dgetrs_(tr.encode(), _i(n), _i(nrhs), NULLD, _i(lda),
+                                                    NULLI, NULLD, _i(ldb), ctypes.byref(info)))
+        assert info.value == want and name == "DGETRS" and pos == -want
+    for (n, nrhs, lda, ldb, want) in [(-1, 1, 2, 2, -1), (2, -1, 2, 2, -2), (3, 1, 2, 3, -4),
+                                      (3, 1, 3, 2, -7)]:
+        name, pos = _xerbla_after(lambda: L.dgesv_(_i(n), _i(nrhs), NULLD, _i(lda), NULLI, NULLD,
+                                                   _i(ldb), ctypes.byref(info)))
+        assert info.value == want and name == "DGESV" and pos == -want
+
+
+def test_quick_returns_touch_nothing():
+    # m==0 / n==0 return before any device work (gemm.tcc:54-56, trf.tcc:81-83)
+    L = fg.lib()
+    info = ctypes.c_int(7)
+    L.dgetrf_(_i(0), _i(5), NULLD, _i(1), NULLI, ctypes.byref(info))
+    assert info.value == 0
+    L.dgemm_(b"N", b"N", _i(0), _i(3), _i(2), _d(1.0), NULLD, _i(1), NULLD, _i(2), _d(0.0),
+             NULLD, _i(1))
+
+
+def test_device_api_argument_errors(flib):
+    assert flib.flens_gb300_dgemm(b"X", b"N", 1, 1, 1, 1.0, None, 1, None, 1, 0.0, None, 1, None) == -1
+    assert flib.flens_gb300_dgetrf(-1, 1, None, 1, None, None, None) == -1
+    assert flib.flens_gb300_dgetrf(3, 1, None, 2, None, None, None) == -4
+    assert flib.flens_gb300_dgetrs(b"N", 3, 1, None, 3, None, None, 2, None) == -8
+
+
+def test_no_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    A = np.asfortranarray(np.eye(3))
+    piv, info = fg.dgetrf(A)
+    assert info == fg.ERR_NO_DEVICE, (info, fg.last_error())
+    assert fg.last_error() != ""

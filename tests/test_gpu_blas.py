@@ -1,0 +1,151 @@
+"""GPU parity for dgemm / dtrsm through the C ABI.
+
+Bars (written in each assert): GEMM normwise relative error <= 1e-13 against
+the reference's own result (the BASELINE gemm bar); TRSM <= 1e-12 on
+well-conditioned triangles.  Semantics that are bitwise in the reference
+(alpha==0 scaling, beta multiply) are checked bitwise.
+"""
+import numpy as np
+import pytest
+
+import flens_gb300 as fg
+import make_golden as G
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+GEMM_TOL = 1e-13
+TRSM_TOL = 1e-12
+
+
+def rel(x, y):
+    if y.size == 0:
+        return 0.0
+    return oracle.normwise_rel(x, y)
+
+
+def test_gemm_fixtures_host_api(cuda, golden):
+    for i, (name, (m, n, k, ta, tb, a, b)) in enumerate(G.gemm_case_list()):
+        A, B, C = G.gemm_inputs(i, m, n, k, ta, tb)
+        out = fg.dgemm(ta, tb, a, A, B, b, C.copy(order="F"))
+        ref = golden[name]
+        if a == 0.0:
+            assert np.array_equal(out, ref), name          # pure beta scaling: exact
+        else:
+            assert rel(out, ref) <= GEMM_TOL, (name, rel(out, ref))
+
+
+def test_gemm_fixtures_device_api(cuda, golden):
+    import torch
+    for i, (name, (m, n, k, ta, tb, a, b)) in enumerate(G.gemm_case_list()):
+        if min(m, n, k) == 0:
+            continue
+        A, B, C = G.gemm_inputs(i, m, n, k, ta, tb)
+        dA, dB, dC = (fg.to_colmajor(torch.from_numpy(x).to(cuda)) for x in (A, B, C))
+        fg.dgemm_dev(ta, tb, a, dA, dB, b, dC)
+        torch.cuda.synchronize()
+        assert rel(dC.cpu().numpy(), golden[name]) <= GEMM_TOL, name
+
+
+def test_gemm_alpha_zero_does_not_read_A_B(cuda):
+    # cxxblas/level3/gemm.tcc:66-69: scale by beta, then return when alpha==0
+    A = np.asfortranarray(np.full((5, 4), np.nan))
+    B = np.asfortranarray(np.full((4, 6), np.nan))
+    C = oracle.uniform(3, 5, 6)
+    out = fg.dgemm("N", "N", 0.0, A, B, 1.25, C.copy(order="F"))
+    assert np.array_equal(out, 1.25 * C)
+
+
+def test_gemm_beta_zero_multiplies(cuda, port):
+    # gescal multiplies by beta, so a NaN in C survives beta == 0 (as in the reference)
+    A, B = oracle.uniform(4, 6, 5), oracle.uniform(5, 5, 7)
+    C = oracle.uniform(6, 6, 7)
+    C[2, 3] = np.nan
+    out = fg.dgemm("N", "N", 1.0, A, B, 0.0, C.copy(order="F"))
+    ref = port.dgemm("N", "N", 1.0, A, B, 0.0, C.copy(order="F"))
+    assert np.isnan(out[2, 3]) and np.isnan(ref[2, 3])
+    mask = ~np.isnan(ref)
+    assert np.max(np.abs(out[mask] - ref[mask])) <= 1e-14
+
+
+@pytest.mark.parametrize("m,n,k", [(1, 1, 1), (2, 3, 1), (63, 65, 17), (127, 129, 200),
+                                   (300, 1, 64), (1, 300, 64), (64, 64, 64), (513, 257, 96)])
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
+def test_gemm_edge_sizes_vs_oracle(cuda, port, m, n, k, ta, tb):
+    A = oracle.uniform(m * 7 + n, m if ta == "N" else k, k if ta == "N" else m)
+    B = oracle.uniform(n * 5 + k, k if tb == "N" else n, n if tb == "N" else k)
+    C = oracle.uniform(k * 3 + m, m, n)
+    out = fg.dgemm(ta, tb, -0.75, A, B, 1.5, C.copy(order="F"))
+    ref = port.dgemm(ta, tb, -0.75, A, B, 1.5, C.copy(order="F"))
+    assert rel(out, ref) <= GEMM_TOL
+
+
+def test_gemm_leading_dimension_views(cuda, port):
+    # operands that are sub-blocks of larger arrays (ld > rows)
+    big = oracle.uniform(11, 100, 90)
+    A = big[3:40, 5:50]            # 37 x 45, ld = 100
+    Bbig = oracle.uniform(12, 80, 70)
+    B = Bbig[10:55, 0:33]          # 45 x 33, ld = 80
+    Cbig = oracle.uniform(13, 60, 40)
+    C = Cbig[1:38, 2:35]           # 37 x 33, ld = 60
+    ref = port.dgemm("N", "N", 1.5, np.asfortranarray(A), np.asfortranarray(B), 0.5,
+                     np.asfortranarray(C))
+    # call dgemm_ directly on the strided views with their true leading dimensions
+    import ctypes
+    L = fg.lib()
+    Cw = Cbig.copy(order="F")
+    i = lambda v: ctypes.byref(ctypes.c_int(v))
+    d = lambda v: ctypes.byref(ctypes.c_double(v))
+    ptr = lambda arr, r, c: ctypes.cast(arr.ctypes.data + 8 * (r + c * arr.shape[0]),
+                                        ctypes.POINTER(ctypes.c_double))
+    L.dgemm_(b"N", b"N", i(37), i(33), i(45), d(1.5), ptr(big, 3, 5), i(100), ptr(Bbig, 10, 0),
+             i(80), d(0.5), ptr(Cw, 1, 2), i(60))
+    assert rel(Cw[1:38, 2:35], ref) <= GEMM_TOL
+    untouched = np.ones_like(Cw, dtype=bool)
+    untouched[1:38, 2:35] = False
+    assert np.array_equal(Cw[untouched], Cbig[untouched])
+
+
+def test_gemm_config1_full_size(cuda, port):
+    # M=N=K=1024, alpha=1.5, beta=0.5, uniform[-1,1]: the GEMM workload config
+    n = 1024
+    A, B, C = oracle.uniform(101, n, n), oracle.uniform(102, n, n), oracle.uniform(103, n, n)
+    out = fg.dgemm("N", "N", 1.5, A, B, 0.5, C.copy(order="F"))
+    ref = port.dgemm("N", "N", 1.5, A, B, 0.5, C.copy(order="F"))
+    assert rel(out, ref) <= GEMM_TOL, rel(out, ref)
+
+
+def test_trsm_fixtures_host_api(cuda, golden):
+    for i, (name, (m, n, side, uplo, ta, diag, alpha)) in enumerate(G.trsm_case_list()):
+        A, B = G.trsm_inputs(i, m, n, side)
+        out = fg.dtrsm(side, uplo, ta, diag, alpha, A, B.copy(order="F"))
+        assert rel(out, golden[name]) <= TRSM_TOL, (name, rel(out, golden[name]))
+
+
+@pytest.mark.parametrize("side", "LR")
+@pytest.mark.parametrize("uplo", "UL")
+@pytest.mark.parametrize("ta", "NT")
+@pytest.mark.parametrize("diag", "UN")
+def test_trsm_blocked_vs_oracle(cuda, port, side, uplo, ta, diag):
+    # sizes that cross the 64-wide diagonal blocks
+    m, n = (200, 37) if side == "L" else (37, 200)
+    ka = m if side == "L" else n
+    A = oracle.uniform(ka + 1, ka, ka)
+    A[np.arange(ka), np.arange(ka)] += 2.0 + ka / 4.0
+    B = oracle.uniform(ka + 2, m, n)
+    out = fg.dtrsm(side, uplo, ta, diag, 1.5, A, B.copy(order="F"))
+    ref = port.dtrsm(side, uplo, ta, diag, 1.5, A, B.copy(order="F"))
+    assert rel(out, ref) <= TRSM_TOL
+
+
+def test_trsm_device_api(cuda, port):
+    import torch
+    A = oracle.uniform(21, 130, 130)
+    A[np.arange(130), np.arange(130)] += 40.0
+    B = oracle.uniform(22, 130, 20)
+    dA = fg.to_colmajor(torch.from_numpy(A).cuda())
+    dB = fg.to_colmajor(torch.from_numpy(B).cuda())
+    fg.dtrsm_dev("L", "U", "N", "N", 1.0, dA, dB)
+    torch.cuda.synchronize()
+    ref = port.dtrsm("L", "U", "N", "N", 1.0, A, B.copy(order="F"))
+    assert rel(dB.cpu().numpy(), ref) <= TRSM_TOL

@@ -1,0 +1,102 @@
+"""Pins the CPU oracle (oracle/flens_oracle.c) to the reference.
+
+1. Against the committed fixtures made by running the reference's own
+   dgemm_/dtrsm_/dgetrf_/dgetrs_/dgesv_ (tests/golden/make_golden.py): the
+   restatement must be BITWISE identical on every case.
+2. Live against oracle/_ref (the reference shims compiled from source) on
+   extra random cases, when that library was built in this checkout.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import make_golden as G
+import oracle
+
+
+def test_gemm_fixtures_bitwise(golden, port):
+    for i, (name, (m, n, k, ta, tb, a, b)) in enumerate(G.gemm_case_list()):
+        A, B, C = G.gemm_inputs(i, m, n, k, ta, tb)
+        out = port.dgemm(ta, tb, a, A, B, b, C.copy(order="F"))
+        assert np.array_equal(out, golden[name], equal_nan=True), name
+
+
+def test_trsm_fixtures_bitwise(golden, port):
+    for i, (name, (m, n, side, uplo, ta, diag, alpha)) in enumerate(G.trsm_case_list()):
+        A, B = G.trsm_inputs(i, m, n, side)
+        out = port.dtrsm(side, uplo, ta, diag, alpha, A, B.copy(order="F"))
+        assert np.array_equal(out, golden[name]), name
+
+
+def test_lu_fixtures_bitwise(golden, port):
+    for i, (name, (m, n, kind)) in enumerate(G.lu_case_list()):
+        LU = G.lu_input(i, m, n, kind)
+        piv, info = port.dgetrf(LU)
+        assert np.array_equal(LU, golden[name + "_LU"]), name
+        assert np.array_equal(piv, golden[name + "_piv"]), name
+        assert info == golden[name + "_info"][0], name
+        if m == n:
+            Bm = G.lu_rhs(i, n)
+            for t in "NT":
+                X = port.dgetrs(t, LU, piv, Bm.copy(order="F"))
+                assert np.array_equal(X, golden[name + f"_X{t}"]), (name, t)
+
+
+def test_singular_info(golden, port):
+    LU = G.singular_input()
+    piv, info = port.dgetrf(LU)
+    assert info == golden["sing_info"][0] == 3
+    assert np.array_equal(piv, golden["sing_piv"])
+    assert np.array_equal(LU, golden["sing_LU"])
+
+
+def test_baby_problem_known_answer(golden, port):
+    # flens/examples/lapack-gesv.cc: x = (1, 9, 9, 9), piv = (2, 3, 4, 4)
+    A, b = G.baby_problem()
+    piv, info = port.dgesv(A, b)
+    assert info == 0
+    assert np.array_equal(piv, [2, 3, 4, 4])
+    assert np.allclose(b[:, 0], [1, 9, 9, 9], rtol=0, atol=1e-13)
+    assert np.array_equal(b, golden["baby_x"])
+    assert np.array_equal(piv, golden["baby_piv"])
+    assert np.array_equal(A, golden["baby_LU"])
+
+
+def test_iamax_first_max_and_nan():
+    p = oracle.Port()
+    assert p.idamax([1.0, -3.0, 3.0, 2.0]) == 1          # first maximum wins
+    assert p.idamax([float("nan"), 5.0, 1.0]) == 0       # NaN at 0: nothing compares greater
+    assert p.idamax([1.0, float("nan"), 5.0]) == 2       # a later NaN never wins
+    assert p.idamax([]) == -1
+
+
+def test_large_pivot_fixture_consistent():
+    path = os.path.join(G.HERE, "reference_lu8192.npz")
+    if not os.path.exists(path):
+        pytest.skip("n=8192 fixture not generated")
+    d = np.load(path)
+    n, seed, info, nonid = d["meta"].tolist()
+    assert (n, seed) == (G.LARGE_N, G.LARGE_SEED)
+    assert info == 0
+    assert nonid == int(np.count_nonzero(d["piv"] != np.arange(1, n + 1)))
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="oracle/_ref not built here")
+def test_port_equals_reference_live():
+    R, P = oracle.Reference(), oracle.Port()
+    rng = np.random.default_rng(99)
+    for (m, n, k) in [(5, 9, 13), (40, 41, 42)]:
+        for ta in "NT":
+            for tb in "NT":
+                A = oracle.uniform(rng, m if ta == "N" else k, k if ta == "N" else m)
+                B = oracle.uniform(rng, k if tb == "N" else n, n if tb == "N" else k)
+                C = oracle.uniform(rng, m, n)
+                assert np.array_equal(P.dgemm(ta, tb, 0.3, A, B, -1.1, C.copy(order="F")),
+                                      R.dgemm(ta, tb, 0.3, A, B, -1.1, C.copy(order="F")))
+    for (m, n) in [(90, 90), (150, 120), (70, 200)]:
+        A = oracle.uniform(rng, m, n)
+        a1, a2 = A.copy(order="F"), A.copy(order="F")
+        p1, i1 = P.dgetrf(a1)
+        p2, i2 = R.dgetrf(a2)
+        assert np.array_equal(a1, a2) and np.array_equal(p1, p2) and i1 == i2
