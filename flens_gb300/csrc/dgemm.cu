@@ -216,6 +216,116 @@ dgemm_dmma_kernel(int m, int n, int k, double alpha,
     }
 }
 
+// ------------------------------------------------------------ skinny N ----
+// n <= NC columns (the block updates of a solve with few right-hand sides):
+// op(B) is staged in shared memory 64 rows of k at a time; op(A) is streamed
+// once from memory, which bounds these launches (they are GEMV-like).
+constexpr int SK_K = 64;
+
+// op(A) = A (rows contiguous): one thread per row of C.
+template <int NC, bool TB>
+__global__ void __launch_bounds__(256)
+dgemm_skinny_nn_kernel(int m, int n, int k, double alpha, const double *__restrict__ A, int ldA,
+                       const double *__restrict__ B, int ldB, double beta,
+                       double *__restrict__ C, int ldC) {
+    __shared__ double Bs[SK_K][NC];
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    double acc[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) acc[j] = 0.0;
+    for (int k0 = 0; k0 < k; k0 += SK_K) {
+        const int kk = min(SK_K, k - k0);
+        for (int e = threadIdx.x; e < SK_K * NC; e += 256) {
+            const int p = e % SK_K, j = e / SK_K;
+            double v = 0.0;
+            if (p < kk && j < n)
+                v = TB ? B[(size_t)j + (size_t)(k0 + p) * ldB] : B[(size_t)(k0 + p) + (size_t)j * ldB];
+            Bs[p][j] = v;
+        }
+        __syncthreads();
+        if (i < m) {
+            const double *a = A + i + (size_t)k0 * ldA;
+            for (int p = 0; p < kk; ++p) {
+                const double av = a[(size_t)p * ldA];
+#pragma unroll
+                for (int j = 0; j < NC; ++j) acc[j] = fma(av, Bs[p][j], acc[j]);
+            }
+        }
+        __syncthreads();
+    }
+    if (i < m) {
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+            if (j < n) {
+                double *c = &C[(size_t)i + (size_t)j * ldC];
+                *c = fma(alpha, acc[j], beta * *c);
+            }
+        }
+    }
+}
+
+// op(A) = A^T (each row of op(A) contiguous in memory): one warp per row of C.
+template <int NC, bool TB>
+__global__ void __launch_bounds__(256)
+dgemm_skinny_tn_kernel(int m, int n, int k, double alpha, const double *__restrict__ A, int ldA,
+                       const double *__restrict__ B, int ldB, double beta,
+                       double *__restrict__ C, int ldC) {
+    __shared__ double Bs[SK_K][NC];
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+    double acc[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) acc[j] = 0.0;
+    for (int k0 = 0; k0 < k; k0 += SK_K) {
+        const int kk = min(SK_K, k - k0);
+        for (int e = threadIdx.x; e < SK_K * NC; e += 256) {
+            const int p = e % SK_K, j = e / SK_K;
+            double v = 0.0;
+            if (p < kk && j < n)
+                v = TB ? B[(size_t)j + (size_t)(k0 + p) * ldB] : B[(size_t)(k0 + p) + (size_t)j * ldB];
+            Bs[p][j] = v;
+        }
+        __syncthreads();
+        if (i < m) {
+            const double *a = A + (size_t)i * ldA + k0;
+            for (int p = lane; p < kk; p += 32) {
+                const double av = a[p];
+#pragma unroll
+                for (int j = 0; j < NC; ++j) acc[j] = fma(av, Bs[p][j], acc[j]);
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc[j] += __shfl_down_sync(0xffffffffu, acc[j], off);
+    }
+    if (i < m && lane == 0) {
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+            if (j < n) {
+                double *c = &C[(size_t)i + (size_t)j * ldC];
+                *c = fma(alpha, acc[j], beta * *c);
+            }
+        }
+    }
+}
+
+template <int NC>
+void launch_skinny(bool ta, bool tb, int m, int n, int k, double alpha, const double *A, int ldA,
+                   const double *B, int ldB, double beta, double *C, int ldC, cudaStream_t s) {
+    if (!ta) {
+        const int grid = ceil_div(m, 256);
+        if (tb) dgemm_skinny_nn_kernel<NC, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+        else dgemm_skinny_nn_kernel<NC, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+    } else {
+        const int grid = ceil_div(m, 8);
+        if (tb) dgemm_skinny_tn_kernel<NC, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+        else dgemm_skinny_tn_kernel<NC, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+    }
+}
+
 __global__ void scale_kernel(int m, int n, double alpha, double *__restrict__ X, int ld) {
     const size_t total = (size_t)m * n;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
@@ -265,9 +375,19 @@ int dgemm_launch(char transA, char transB, int m, int n, int k, double alpha,
         set_last_error("dgemm: n=%d too large for one launch", n);
         return kErrUnsupported;
     }
-    const Engine e = pick_engine();
     KTimer kt(kFamGemm, stream, 2.0 * m * n * (double)k,
               8.0 * ((double)m * k + (double)k * n + 2.0 * m * n));
+    if (n <= 16) {
+        trace("dgemm %c%c m=%d n=%d k=%d engine=skinny", transA, transB, m, n, k);
+        if (n <= 1) launch_skinny<1>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
+        else if (n <= 2) launch_skinny<2>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
+        else if (n <= 4) launch_skinny<4>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
+        else if (n <= 8) launch_skinny<8>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
+        else launch_skinny<16>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
+        FG_CUDA(cudaGetLastError());
+        return kOk;
+    }
+    const Engine e = pick_engine();
     trace("dgemm %c%c m=%d n=%d k=%d engine=%s", transA, transB, m, n, k,
           e == Engine::Dmma ? "dmma" : "fma");
 #define FG_LAUNCH(KERNEL, NT)                                                          \

@@ -10,13 +10,16 @@
 // Structure (one stream, all asynchronous):
 //   for each block column j (width jb <= 64, the reference's ilaenv GETRF
 //   block size, flens/lapack/la/ilaenv.tcc:93-99):
-//     panel_kernel      cooperative grid, one CTA per SM; the (m-j) x jb panel
-//                       lives in shared memory split by rows; per column one
-//                       bounded grid barrier exchanges per-CTA pivot
-//                       candidates (warp-shuffle argmax, first maximum wins)
-//                       and the candidate rows, then every CTA swaps, scales
-//                       and applies the rank-1 update to its own rows.  At the
-//                       end it turns the jb interchanges into a list of
+//     panel_kernel      cooperative grid, up to one CTA per SM; the (m-j) x jb
+//                       panel lives in shared memory split by rows.  Per
+//                       column each CTA finds its best candidate (warp-shuffle
+//                       argmax, first maximum wins), publishes it with the
+//                       candidate row in its own slot (release store of a
+//                       sequence number) and reads every CTA's slot (acquire,
+//                       bounded wait), so all CTAs agree on the pivot without
+//                       a separate barrier; then every CTA swaps, scales and
+//                       applies the rank-1 update to its own rows.  At the end
+//                       it turns the jb interchanges into a list of
 //                       (destination row, source row) moves.
 //     laswp_pairs_kernel applies those moves to every column outside the
 //                       panel, one warp per column (loads, then stores).
@@ -40,46 +43,49 @@ constexpr int PANEL_GMAX = 256;        // max CTAs in a panel grid
 constexpr int PANEL_RMIN = 32;         // min rows per CTA
 constexpr size_t PANEL_SMEM_MAX = 200 * 1024;
 
+// One exchange slot per CTA and per step parity.  A CTA publishes its pivot
+// candidate (|value|, row, the row's jb panel entries) and, if it owns panel
+// row jj, that row; `seq` is written last with release semantics.
+struct PanelSlot {
+    unsigned long long seq;
+    double val;
+    int idx;
+    int pad;
+    double row[PANEL_NB];
+    double rowjj[PANEL_NB];
+};
+
 struct PanelScratch {
-    GridBarrierState *bar;
-    double *cand_val;   // [2][GMAX]
-    int *cand_idx;      // [2][GMAX]
-    double *cand_row;   // [2][GMAX][NB]
-    double *rowjj;      // [2][NB]
+    PanelSlot *slots;   // [2][GMAX]
     int *swap_cnt;      // [1]
     int *swap_dst;      // [2*NB]
     int *swap_src;      // [2*NB]
 };
 
-size_t panel_scratch_bytes() {
-    size_t b = 256;                                            // barrier
-    b += 2 * PANEL_GMAX * sizeof(double);
-    b += 2 * PANEL_GMAX * sizeof(int);
-    b += 2 * (size_t)PANEL_GMAX * PANEL_NB * sizeof(double);
-    b += 2 * PANEL_NB * sizeof(double);
-    b += 256 + 4 * PANEL_NB * sizeof(int);
-    return b + 1024;
-}
+constexpr size_t kSlotBytes = 2 * (size_t)PANEL_GMAX * sizeof(PanelSlot);
+
+size_t panel_scratch_bytes() { return kSlotBytes + 256 + 4 * PANEL_NB * sizeof(int) + 1024; }
 
 PanelScratch carve_panel_scratch(void *base) {
     char *p = (char *)base;
     PanelScratch s;
-    s.bar = (GridBarrierState *)p;
-    p += 256;
-    s.cand_val = (double *)p;
-    p += 2 * PANEL_GMAX * sizeof(double);
-    s.cand_idx = (int *)p;
-    p += 2 * PANEL_GMAX * sizeof(int);
-    s.cand_row = (double *)p;
-    p += 2 * (size_t)PANEL_GMAX * PANEL_NB * sizeof(double);
-    s.rowjj = (double *)p;
-    p += 2 * PANEL_NB * sizeof(double);
+    s.slots = (PanelSlot *)p;
+    p += kSlotBytes;
     s.swap_cnt = (int *)p;
     p += 256;
     s.swap_dst = (int *)p;
     p += 2 * PANEL_NB * sizeof(int);
     s.swap_src = (int *)p;
     return s;
+}
+
+__device__ __forceinline__ void st_release(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
 }
 
 // (key, row) "better than": larger key; on equal keys the smaller row, which
@@ -124,12 +130,13 @@ __device__ __forceinline__ void block_argmax(double &v, int &i, double *red_v, i
 __global__ void __launch_bounds__(PANEL_THREADS)
 panel_kernel(double *__restrict__ A, int lda, int mp, int jb, int j0,
              int *__restrict__ ipiv, int *__restrict__ info, int *__restrict__ status,
-             PanelScratch ps, int R) {
+             PanelScratch ps, int R, unsigned long long epoch) {
     extern __shared__ double S[];
     __shared__ double prow[PANEL_NB], orow[PANEL_NB];
     __shared__ double red_v[32];
     __shared__ int red_i[32];
     __shared__ int s_gs;
+    __shared__ int s_abort;
     __shared__ int s_list_row[2 * PANEL_NB], s_list_src[2 * PANEL_NB];
 
     const int b = blockIdx.x, G = gridDim.x, tid = threadIdx.x;
@@ -157,42 +164,57 @@ panel_kernel(double *__restrict__ A, int lda, int mp, int jb, int j0,
             }
         }
         block_argmax(bv, bi, red_v, red_i);
-        if (tid == 0) {
-            ps.cand_val[par * PANEL_GMAX + b] = bv;
-            ps.cand_idx[par * PANEL_GMAX + b] = bi;
-        }
+        PanelSlot *mine = &ps.slots[par * PANEL_GMAX + b];
         if (bi != INT_MAX) {
-            for (int c = tid; c < jb; c += PANEL_THREADS)
-                ps.cand_row[((size_t)par * PANEL_GMAX + b) * PANEL_NB + c] = S[c * R + (bi - rb)];
+            for (int c = tid; c < jb; c += PANEL_THREADS) mine->row[c] = S[c * R + (bi - rb)];
         }
         if (jj >= rb && jj < re) {
-            for (int c = tid; c < jb; c += PANEL_THREADS)
-                ps.rowjj[par * PANEL_NB + c] = S[c * R + (jj - rb)];
+            for (int c = tid; c < jb; c += PANEL_THREADS) mine->rowjj[c] = S[c * R + (jj - rb)];
         }
-        if (!grid_barrier(ps.bar, G, status)) return;
+        if (tid == 0) {
+            mine->val = bv;
+            mine->idx = bi;
+            s_abort = 0;
+        }
+        __threadfence();
+        __syncthreads();
+        const unsigned long long want = epoch * 128ull + (unsigned long long)jj + 1ull;
+        if (tid == 0) st_release(&mine->seq, want);
 
-        // -- global pivot: best candidate over CTAs
+        // -- every CTA reads every slot once its seq says step jj is published
         double gv = -3.0;
         int gi = INT_MAX;
         for (int t = tid; t < G; t += PANEL_THREADS) {
-            const double v = ld_cg(&ps.cand_val[par * PANEL_GMAX + t]);
-            const int i = ld_cg(&ps.cand_idx[par * PANEL_GMAX + t]);
+            const PanelSlot *sl = &ps.slots[par * PANEL_GMAX + t];
+            unsigned spins = 0;
+            while (ld_acquire(&sl->seq) != want) {
+                if (++spins > kSpinLimit) {
+                    atomicOr(status, kDevBarrierTimeout);
+                    s_abort = 1;
+                    break;
+                }
+                if (spins > 32) __nanosleep(32);
+            }
+            const double v = ld_cg(&sl->val);
+            const int i = ld_cg(&sl->idx);
             if (better(v, i, gv, gi)) { gv = v; gi = i; }
         }
         block_argmax(gv, gi, red_v, red_i);
+        if (s_abort) return;
+        const int ownjj = jj / R;
         if (tid == 0) {
             // iamax starts from element jj: if it is NaN nothing compares
             // greater and jj is the pivot (cxxblas/level1/iamax.tcc:50-57).
-            const double ajj = ld_cg(&ps.rowjj[par * PANEL_NB + jj]);
+            const double ajj = ld_cg(&ps.slots[par * PANEL_GMAX + ownjj].rowjj[jj]);
             s_gs = isnan(ajj) ? jj : gi;
         }
         __syncthreads();
         const int gs = s_gs;
         const int wb = gs / R;
         for (int c = tid; c < jb; c += PANEL_THREADS) {
-            const double o = ld_cg(&ps.rowjj[par * PANEL_NB + c]);
+            const double o = ld_cg(&ps.slots[par * PANEL_GMAX + ownjj].rowjj[c]);
             orow[c] = o;
-            prow[c] = (gs == jj) ? o : ld_cg(&ps.cand_row[((size_t)par * PANEL_GMAX + wb) * PANEL_NB + c]);
+            prow[c] = (gs == jj) ? o : ld_cg(&ps.slots[par * PANEL_GMAX + wb].row[c]);
         }
         __syncthreads();
         const double pv = prow[jj];
@@ -411,7 +433,8 @@ int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, cudaSt
     Workspace *w = workspace_for(stream, panel_scratch_bytes());
     if (!w) return kErrAlloc;
     PanelScratch ps = carve_panel_scratch(w->buf);
-    FG_CUDA(cudaMemsetAsync(ps.bar, 0, sizeof(GridBarrierState), stream));
+    FG_CUDA(cudaMemsetAsync(ps.slots, 0, kSlotBytes, stream));
+    unsigned long long epoch = 0;
     if (!g_panel_attr_set) {
         FG_CUDA(cudaFuncSetAttribute(panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)PANEL_SMEM_MAX));
@@ -443,7 +466,9 @@ int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, cudaSt
         int *status = w->status;
         int j0 = j;
         size_t smem = (size_t)R * jb * sizeof(double);
-        void *args[] = {&Ap, &ldA, (void *)&mp, (void *)&jb, &j0, &ipiv, &info, &status, &ps, &R};
+        ++epoch;
+        void *args[] = {&Ap, &ldA, (void *)&mp, (void *)&jb, &j0, &ipiv, &info, &status, &ps, &R,
+                        &epoch};
         {
             KTimer ktp(kFamPanel, stream, (double)mp * jb * jb - (double)jb * jb * jb / 3.0,
                        16.0 * (double)mp * jb);

@@ -9,81 +9,131 @@
 // triangle M (op(A) for side=Left, op(A)^T for side=Right) addressed as
 // M(i,p) = A[i*mi + p*mp], and a set of vectors (columns of B for Left, rows
 // of B for Right).  The blocked, right-looking driver solves 64x64 diagonal
-// blocks with trsm_diag_kernel (one thread per vector, the block of M and the
-// vectors staged in shared memory) and applies each solved block to the rest
-// of B with the FP64 GEMM.
+// blocks (trsm_diag_wide_kernel: a thread per vector; trsm_diag_narrow_kernel:
+// a warp per vector, for few right-hand sides) and applies each solved block to the rest
+// of B with the FP64 GEMM.  The diagonal solve uses the column-sweep (axpy)
+// form rather than the reference's dot form; the result agrees to rounding.
 #include "common.cuh"
 
 namespace fg {
 namespace {
 
 constexpr int TRSM_NB = 64;      // diagonal block size
-constexpr int TRSM_VEC = 128;    // vectors (threads) per CTA
+constexpr int TRSM_VEC = 64;     // vectors (threads) per CTA, wide kernel
+constexpr int TRSM_WARPS = 8;    // vectors (warps) per CTA, narrow kernel
+constexpr int TRSM_NARROW = 512; // below this many vectors use the warp kernel
 
+// Wide kernel: one thread per vector, the vector held in 64 registers and
+// solved column by column (x_r -= M(r,i) x_i for all r past i), so every step
+// issues independent FMAs instead of one dependent dot-product chain.  The
+// diagonal block of M is staged in shared memory and read as broadcasts.
+template <bool LOWER, bool UNIT>
 __global__ void __launch_bounds__(TRSM_VEC)
-trsm_diag_kernel(int nb, const double *__restrict__ M0, long long mi, long long mp,
-                 int lowerM, int unit, double *__restrict__ X0, long long xs,
-                 long long vs, int nvec) {
-    extern __shared__ double smem[];
-    double *Ms = smem;                                  // [TRSM_NB][TRSM_NB+1]: Ms[i*(NB+1)+p]
-    double *Xs = smem + TRSM_NB * (TRSM_NB + 1);        // [TRSM_NB][TRSM_VEC]:  Xs[i*VEC+t]
+trsm_diag_wide_kernel(int nb, const double *__restrict__ M0, long long mi, long long mp,
+                      double *__restrict__ X0, long long xs, long long vs, int nvec) {
+    __shared__ double Ms[TRSM_NB * TRSM_NB];   // Ms[r*NB + i] = M(r, i)
     const int t = threadIdx.x;
-    const long long v0 = (long long)blockIdx.x * TRSM_VEC;
-    const int nv = (int)((nvec - v0) < TRSM_VEC ? (nvec - v0) : TRSM_VEC);
-
     for (int e = t; e < nb * nb; e += TRSM_VEC) {
-        int i, p;
-        if (mi == 1) { i = e % nb; p = e / nb; }
-        else { p = e % nb; i = e / nb; }
-        Ms[i * (TRSM_NB + 1) + p] = M0[i * mi + p * mp];
-    }
-    double *X = X0 + v0 * vs;
-    if (xs == 1) {
-        for (int e = t; e < nb * nv; e += TRSM_VEC) {
-            const int i = e % nb, v = e / nb;
-            Xs[i * TRSM_VEC + v] = X[(long long)v * vs + i];
-        }
-    } else {
-        for (int e = t; e < nb * TRSM_VEC; e += TRSM_VEC) {
-            const int v = e % TRSM_VEC, i = e / TRSM_VEC;
-            if (v < nv) Xs[i * TRSM_VEC + v] = X[(long long)v * vs + (long long)i * xs];
-        }
+        int r, i;
+        if (mi == 1) { r = e % nb; i = e / nb; }
+        else { i = e % nb; r = e / nb; }
+        Ms[r * TRSM_NB + i] = M0[r * mi + i * mp];
     }
     __syncthreads();
-    if (t < nv) {
-        if (lowerM) {
-            for (int i = 0; i < nb; ++i) {
-                double s = 0.0;
-                for (int p = 0; p < i; ++p) s = fma(Ms[i * (TRSM_NB + 1) + p], Xs[p * TRSM_VEC + t], s);
-                double x = Xs[i * TRSM_VEC + t] - s;
-                if (!unit) x = x / Ms[i * (TRSM_NB + 1) + i];
-                Xs[i * TRSM_VEC + t] = x;
+    const long long v = (long long)blockIdx.x * TRSM_VEC + t;
+    if (v >= nvec) return;
+    double *x = X0 + v * vs;
+    double r_[TRSM_NB];
+#pragma unroll
+    for (int r = 0; r < TRSM_NB; ++r) r_[r] = (r < nb) ? x[r * xs] : 0.0;
+    if (LOWER) {
+#pragma unroll
+        for (int i = 0; i < TRSM_NB; ++i) {
+            if (i < nb) {
+                if (!UNIT) r_[i] = r_[i] / Ms[i * TRSM_NB + i];
+                const double xi = r_[i];
+#pragma unroll
+                for (int r = i + 1; r < TRSM_NB; ++r)
+                    if (r < nb) r_[r] = fma(-Ms[r * TRSM_NB + i], xi, r_[r]);
             }
-        } else {
-            for (int i = nb - 1; i >= 0; --i) {
-                double s = 0.0;
-                for (int q = i + 1; q < nb; ++q) s = fma(Ms[i * (TRSM_NB + 1) + q], Xs[q * TRSM_VEC + t], s);
-                double x = Xs[i * TRSM_VEC + t] - s;
-                if (!unit) x = x / Ms[i * (TRSM_NB + 1) + i];
-                Xs[i * TRSM_VEC + t] = x;
+        }
+    } else {
+#pragma unroll
+        for (int i = TRSM_NB - 1; i >= 0; --i) {
+            if (i < nb) {
+                if (!UNIT) r_[i] = r_[i] / Ms[i * TRSM_NB + i];
+                const double xi = r_[i];
+#pragma unroll
+                for (int r = 0; r < i; ++r) r_[r] = fma(-Ms[r * TRSM_NB + i], xi, r_[r]);
             }
         }
     }
-    __syncthreads();
-    if (xs == 1) {
-        for (int e = t; e < nb * nv; e += TRSM_VEC) {
-            const int i = e % nb, v = e / nb;
-            X[(long long)v * vs + i] = Xs[i * TRSM_VEC + v];
-        }
-    } else {
-        for (int e = t; e < nb * TRSM_VEC; e += TRSM_VEC) {
-            const int v = e % TRSM_VEC, i = e / TRSM_VEC;
-            if (v < nv) X[(long long)v * vs + (long long)i * xs] = Xs[i * TRSM_VEC + v];
-        }
-    }
+#pragma unroll
+    for (int r = 0; r < TRSM_NB; ++r)
+        if (r < nb) x[r * xs] = r_[r];
 }
 
-constexpr size_t kDiagSmem = sizeof(double) * (TRSM_NB * (TRSM_NB + 1) + TRSM_NB * TRSM_VEC);
+// Narrow kernel: one warp per vector, lane l holding rows l and l+32; the
+// finished x_i is broadcast with a shuffle and every lane updates its rows.
+template <bool LOWER, bool UNIT>
+__global__ void __launch_bounds__(32 * TRSM_WARPS)
+trsm_diag_narrow_kernel(int nb, const double *__restrict__ M0, long long mi, long long mp,
+                        double *__restrict__ X0, long long xs, long long vs, int nvec) {
+    __shared__ double Ms[TRSM_NB * (TRSM_NB + 1)];   // Ms[i*(NB+1) + r] = M(r, i)
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+        int r, i;
+        if (mi == 1) { r = e % nb; i = e / nb; }
+        else { i = e % nb; r = e / nb; }
+        Ms[i * (TRSM_NB + 1) + r] = M0[r * mi + i * mp];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const long long v = (long long)blockIdx.x * TRSM_WARPS + (threadIdx.x >> 5);
+    if (v >= nvec) return;
+    double *x = X0 + v * vs;
+    const int r0 = lane, r1 = lane + 32;
+    double x0 = (r0 < nb) ? x[r0 * xs] : 0.0;
+    double x1 = (r1 < nb) ? x[r1 * xs] : 0.0;
+    for (int s = 0; s < nb; ++s) {
+        const int i = LOWER ? s : nb - 1 - s;
+        const int owner = i & 31;
+        double xi = __shfl_sync(0xffffffffu, (i < 32) ? x0 : x1, owner);
+        if (!UNIT) xi = xi / Ms[i * (TRSM_NB + 1) + i];
+        if (lane == owner) {
+            if (i < 32) x0 = xi; else x1 = xi;
+        }
+        const double *col = &Ms[i * (TRSM_NB + 1)];
+        if (LOWER) {
+            if (r0 > i && r0 < nb) x0 = fma(-col[r0], xi, x0);
+            if (r1 > i && r1 < nb) x1 = fma(-col[r1], xi, x1);
+        } else {
+            if (r0 < i) x0 = fma(-col[r0], xi, x0);
+            if (r1 < i) x1 = fma(-col[r1], xi, x1);
+        }
+    }
+    if (r0 < nb) x[r0 * xs] = x0;
+    if (r1 < nb) x[r1 * xs] = x1;
+}
+
+int launch_diag(int kb, const double *M0, long long mi, long long mp, bool lowerM, bool unit,
+                double *X0, long long xs, long long vs, int nvec, cudaStream_t stream) {
+    KTimer kt(kFamTrsm, stream, (double)kb * kb * nvec, 16.0 * (double)kb * nvec);
+    if (nvec >= TRSM_NARROW) {
+        const int grid = ceil_div(nvec, TRSM_VEC);
+#define FG_WIDE(L, U) trsm_diag_wide_kernel<L, U><<<grid, TRSM_VEC, 0, stream>>>(kb, M0, mi, mp, X0, xs, vs, nvec)
+        if (lowerM) { if (unit) FG_WIDE(true, true); else FG_WIDE(true, false); }
+        else { if (unit) FG_WIDE(false, true); else FG_WIDE(false, false); }
+#undef FG_WIDE
+    } else {
+        const int grid = ceil_div(nvec, TRSM_WARPS);
+#define FG_NARROW(L, U) trsm_diag_narrow_kernel<L, U><<<grid, 32 * TRSM_WARPS, 0, stream>>>(kb, M0, mi, mp, X0, xs, vs, nvec)
+        if (lowerM) { if (unit) FG_NARROW(true, true); else FG_NARROW(true, false); }
+        else { if (unit) FG_NARROW(false, true); else FG_NARROW(false, false); }
+#undef FG_NARROW
+    }
+    FG_CUDA(cudaGetLastError());
+    return kOk;
+}
 
 }  // namespace
 
@@ -91,13 +141,6 @@ int dtrsm_launch(char side, char upLo, char transA, char diag, int m, int n,
                  double alpha, const double *A, int ldA, double *B, int ldB,
                  cudaStream_t stream) {
     if (m == 0 || n == 0) return kOk;
-    static bool attr_set = false;
-    if (!attr_set) {
-        FG_CUDA(cudaFuncSetAttribute(trsm_diag_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)kDiagSmem));
-        attr_set = true;
-    }
     const bool left = (side == 'L' || side == 'l');
     const bool lowerA = (upLo == 'L' || upLo == 'l');
     const bool nT = (transA == 'N' || transA == 'n');
@@ -121,17 +164,13 @@ int dtrsm_launch(char side, char upLo, char transA, char diag, int m, int n,
           diag, m, n, lowerM ? "lower" : "upper", nvec);
 
     const int nblk = ceil_div(ka, TRSM_NB);
-    const int grid = ceil_div(nvec, TRSM_VEC);
     for (int s = 0; s < nblk; ++s) {
         const int bi = lowerM ? s : nblk - 1 - s;
         const int k0 = bi * TRSM_NB;
         const int kb = (ka - k0) < TRSM_NB ? (ka - k0) : TRSM_NB;
-        {
-            KTimer kt(kFamTrsm, stream, (double)kb * kb * nvec, 16.0 * (double)kb * nvec);
-            trsm_diag_kernel<<<grid, TRSM_VEC, kDiagSmem, stream>>>(
-                kb, A + k0 * mi + k0 * mp, mi, mp, lowerM ? 1 : 0, unit, B + k0 * xs, xs, vs, nvec);
-            FG_CUDA(cudaGetLastError());
-        }
+        int st0 = launch_diag(kb, A + k0 * mi + k0 * mp, mi, mp, lowerM, unit != 0, B + k0 * xs, xs,
+                              vs, nvec, stream);
+        if (st0 != kOk) return st0;
         // rows still to solve: below the block (lower) or above it (upper)
         const int r0 = lowerM ? k0 + kb : 0;
         const int rn = lowerM ? ka - (k0 + kb) : k0;

@@ -126,9 +126,11 @@ def test_trsm_fixtures_host_api(cuda, golden):
 @pytest.mark.parametrize("uplo", "UL")
 @pytest.mark.parametrize("ta", "NT")
 @pytest.mark.parametrize("diag", "UN")
-def test_trsm_blocked_vs_oracle(cuda, port, side, uplo, ta, diag):
-    # sizes that cross the 64-wide diagonal blocks
-    m, n = (200, 37) if side == "L" else (37, 200)
+@pytest.mark.parametrize("nvec", [37, 600])
+def test_trsm_blocked_vs_oracle(cuda, port, side, uplo, ta, diag, nvec):
+    # sizes that cross the 64-wide diagonal blocks; 37 vectors take the
+    # warp-per-vector kernel, 600 the thread-per-vector kernel
+    m, n = (200, nvec) if side == "L" else (nvec, 200)
     ka = m if side == "L" else n
     A = oracle.uniform(ka + 1, ka, ka)
     A[np.arange(ka), np.arange(ka)] += 2.0 + ka / 4.0
