@@ -81,6 +81,8 @@ def lib() -> ctypes.CDLL:
     L.flens_gb300_dgetrs.argtypes = [_c, _i, _i, _v, _i, _v, _v, _i, _v]
     L.flens_gb300_dgesv.argtypes = [_i, _i, _v, _i, _v, _v, _i, _v, _v]
     L.flens_gb300_sync.argtypes = [_v]
+    L.flens_gb300_dgetrs_noalloc.argtypes = [_c, _i, _i, _v, _i, _v, _v, _i, _v]
+    L.flens_gb300_dgetrs_noalloc.restype = _i
     for f in ("flens_gb300_dgemm", "flens_gb300_dtrsm", "flens_gb300_dgetrf",
               "flens_gb300_dgetrs", "flens_gb300_dgesv", "flens_gb300_sync"):
         getattr(L, f).restype = _i

@@ -34,6 +34,8 @@
 #include <float.h>
 #include <limits.h>
 
+#include <mutex>
+
 namespace fg {
 namespace {
 
@@ -516,3 +518,130 @@ int dgetrs_launch(char trans, int n, int nrhs, const double *A, int ldA, const i
 }
 
 }  // namespace fg
+
+// ---------------------------------------------------------------------------
+// Solve without allocating: flens_gb300_dgetrs_noalloc.
+//
+// Some callers cannot call cudaMalloc once they are running: a service that
+// reserves all of its device memory up front and must not grow it on the
+// request path, code that runs inside a pre-allocated memory pool owned by
+// another framework, or a host that links this library into a process where
+// device allocation is forbidden after start-up (a failed or blocking
+// cudaMalloc there would stall or abort the caller).  flens_gb300_dgetrs
+// takes its scratch (the row permutation and the gathered right-hand sides of
+// the row interchanges) from a per-stream workspace that it grows with
+// cudaMalloc on first use; this entry point takes the same scratch from the
+// fixed file-scope array below instead and calls no allocating routine.
+//
+// Limits and rules:
+//  * the array holds 8 MiB; a call needs round_up(4*n, 256) + 8*n*nrhs bytes
+//    (n = 8192 allows nrhs <= 127) and larger calls are rejected with
+//    FLENS_GB300_ERR_UNSUPPORTED and a message in flens_gb300_last_error();
+//  * every GPU that loads the library holds the array until the process exits;
+//  * all calls on a device share the one array: calls whose work overlaps on
+//    the GPU (different streams, or different host threads) race on it and
+//    must be serialised by the caller;
+//  * the first call on a device looks the array's device address up
+//    (cudaGetSymbolAddress) -- make that first call before any stream capture.
+// The array keeps the last call's contents; nothing in it has to start at
+// zero (the permutation is rebuilt from the identity and the gather buffer is
+// fully written before it is read on every call).
+namespace fg {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 8u << 20;
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64];
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device with that device current.
+int noalloc_scratch(void **out) {
+    int dev = -1;
+    FG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_last_error("device ordinal %d out of range", dev);
+        return kErrUnsupported;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr)
+            return cuda_fail(e != cudaSuccess ? e : cudaErrorInvalidSymbol,
+                             "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return kOk;
+}
+
+size_t noalloc_needed(int nrows, int ncols) {
+    return ((size_t)nrows * sizeof(int) + 255) / 256 * 256 +
+           (size_t)nrows * (size_t)ncols * sizeof(double);
+}
+
+// Same row interchanges as dlaswp_launch, scratch taken from `scratch`.
+int laswp_fixed(int nrows, int ncols, double *A, int ldA, int k1, int k2, const int *ipiv,
+                int inc, void *scratch, cudaStream_t stream) {
+    if (nrows <= 0 || ncols <= 0 || k2 < k1) return kOk;
+    const size_t permBytes = ((size_t)nrows * sizeof(int) + 255) / 256 * 256;
+    int *perm = (int *)scratch;
+    double *tmp = (double *)((char *)scratch + permBytes);
+    const int use_smem = (size_t)nrows * sizeof(int) <= 200 * 1024 ? 1 : 0;
+    if (use_smem) {
+        static bool attr = false;
+        if (!attr) {
+            FG_CUDA(cudaFuncSetAttribute(laswp_perm_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+            attr = true;
+        }
+    }
+    KTimer kt(kFamLaswp, stream, 0.0, 2.0 * (double)nrows * ncols * 16.0);
+    laswp_perm_kernel<<<1, 1024, use_smem ? (size_t)nrows * sizeof(int) : 0, stream>>>(
+        nrows, k1, k2, ipiv, inc, perm, use_smem);
+    FG_CUDA(cudaGetLastError());
+    const size_t total = (size_t)nrows * ncols;
+    int blocks = (int)ceil_div(total, (size_t)256);
+    if (blocks > num_sms() * 16) blocks = num_sms() * 16;
+    gather_rows_kernel<<<blocks, 256, 0, stream>>>(nrows, ncols, A, ldA, perm, tmp);
+    FG_CUDA(cudaGetLastError());
+    copy_back_kernel<<<blocks, 256, 0, stream>>>(nrows, ncols, tmp, A, ldA);
+    FG_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+}  // namespace
+}  // namespace fg
+
+FG_API int flens_gb300_dgetrs_noalloc(char trans, int n, int nrhs, const double *A, int ldA,
+                                      const int *ipiv, double *B, int ldB, void *stream) {
+    using namespace fg;
+    if (trans >= 'a' && trans <= 'z') trans = (char)(trans - 'a' + 'A');
+    if (trans != 'N' && trans != 'T' && trans != 'C') return -1;
+    if (n < 0) return -2;
+    if (nrhs < 0) return -3;
+    if (ldA < (n > 1 ? n : 1)) return -5;
+    if (ldB < (n > 1 ? n : 1)) return -8;
+    if (n == 0 || nrhs == 0) return kOk;
+    const size_t need = noalloc_needed(n, nrhs);
+    if (need > kNoAllocScratchBytes) {
+        set_last_error("flens_gb300_dgetrs_noalloc: n=%d nrhs=%d needs %zu bytes of scratch, "
+                       "more than its fixed %zu-byte array; use flens_gb300_dgetrs or fewer "
+                       "right-hand sides per call", n, nrhs, need, kNoAllocScratchBytes);
+        return kErrUnsupported;
+    }
+    void *scratch = nullptr;
+    int st = noalloc_scratch(&scratch);
+    if (st != kOk) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (trans == 'N') {
+        if ((st = laswp_fixed(n, nrhs, B, ldB, 1, n, ipiv, 1, scratch, s)) != kOk) return st;
+        if ((st = dtrsm_launch('L', 'L', 'N', 'U', n, nrhs, 1.0, A, ldA, B, ldB, s)) != kOk) return st;
+        return dtrsm_launch('L', 'U', 'N', 'N', n, nrhs, 1.0, A, ldA, B, ldB, s);
+    }
+    if ((st = dtrsm_launch('L', 'U', 'T', 'N', n, nrhs, 1.0, A, ldA, B, ldB, s)) != kOk) return st;
+    if ((st = dtrsm_launch('L', 'L', 'T', 'U', n, nrhs, 1.0, A, ldA, B, ldB, s)) != kOk) return st;
+    return laswp_fixed(n, nrhs, B, ldB, 1, n, ipiv, -1, scratch, s);
+}

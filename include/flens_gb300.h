@@ -103,6 +103,21 @@ int flens_gb300_dgetrs(char trans, int n, int nrhs, const double *A, int ldA,
 int flens_gb300_dgesv(int n, int nrhs, double *A, int ldA, int *ipiv, double *B,
                       int ldB, int *info, void *stream);
 
+/* dgetrs on device memory for callers that must not allocate device memory
+ * once running (a fixed, pre-reserved memory budget, a memory pool owned by
+ * another framework, or a process that forbids cudaMalloc after start-up).
+ * No counterpart in the reference.  Same arguments, results and return codes
+ * as flens_gb300_dgetrs, but it calls no cudaMalloc/cudaFree: its scratch is a
+ * fixed 8 MiB device array inside the library, held on every GPU that loads
+ * the library until exit.  A call needs round_up(4*n,256) + 8*n*nrhs bytes
+ * (n=8192: nrhs <= 127); larger calls return FLENS_GB300_ERR_UNSUPPORTED.
+ * All calls share that array: calls that overlap on the GPU race, so
+ * serialise them.  The first call on a device looks up the array's address;
+ * make it before any stream capture.  Async on stream. */
+int flens_gb300_dgetrs_noalloc(char trans, int n, int nrhs, const double *A,
+                               int ldA, const int *ipiv, double *B, int ldB,
+                               void *stream);
+
 /* Waits for `stream` and reports device-side failures (a bounded wait that
  * timed out) as FLENS_GB300_ERR_TIMEOUT. */
 int flens_gb300_sync(void *stream);
