@@ -1,0 +1,177 @@
+/*
+ * flens_gb300.hpp -- route FLENS's dense GEMM / TRSM / LU to the GB300 library.
+ *
+ * Include this header INSTEAD OF <flens/flens.cxx> (it includes FLENS itself):
+ *
+ *     #include <flens_gb300/flens_gb300.hpp>     // was: #include <flens/flens.cxx>
+ *     ...   link with -lflens_gb300
+ *
+ * It plugs into the two places FLENS already provides for a faster backend:
+ *
+ *  - cxxblas level 3: like the cblas overloads FLENS adds under HAVE_CBLAS
+ *    (cxxblas/level3/gemm.tcc:218-240, cxxblas/level3/trsm.tcc:107-126), more
+ *    specialised overloads of cxxblas::gemm and cxxblas::trsm for double with
+ *    an integral index forward to dgemm_ / dtrsm_.  flens::blas::mm and
+ *    flens::blas::sm (flens/blas/level3/mm.tcc:463-472, sm.tcc:61-67), the
+ *    operator form C = beta*C + alpha*A*B, and every mm/sm call FLENS-LAPACK
+ *    makes reach them.
+ *  - FLENS-LAPACK's generic implementations: more specialised overloads of
+ *    flens::lapack::generic::trf_impl (flens/lapack/ge/trf.tcc:61) and
+ *    trs_impl (flens/lapack/ge/trs.tcc:61) for column-major double matrices
+ *    with int pivots forward to dgetrf_ / dgetrs_, so lapack::trf, lapack::trs
+ *    and lapack::sv (which calls both, flens/lapack/ge/sv.tcc:58-77) run on
+ *    the GPU.  Other element types, index types and storage orders keep the
+ *    reference's generic code.
+ *
+ * The overloads must be declared between flens.h and flens.tcc so that the
+ * qualified calls inside the FLENS templates see them; hence the include
+ * order below.  Memory may be host (copied to the GPU per call) or device /
+ * managed (used in place).
+ */
+#ifndef FLENS_GB300_FLENS_GB300_HPP
+#define FLENS_GB300_FLENS_GB300_HPP 1
+
+#ifdef FLENS_FLENS_CXX
+#error "include <flens_gb300/flens_gb300.hpp> instead of (not after) <flens/flens.cxx>"
+#endif
+
+#include <type_traits>
+#include <vector>
+
+#include <flens/flens.h>
+#include <flens_gb300.h>
+
+namespace flens_gb300 { namespace detail {
+
+inline char trans_char(cxxblas::Transpose t)
+{
+    return (static_cast<int>(t) & static_cast<int>(cxxblas::Trans)) ? 'T' : 'N';
+}
+
+template <typename IndexType>
+struct IsIndex
+{
+    static const bool value = std::is_integral<IndexType>::value;
+};
+
+template <typename S>
+struct IsDoubleColMajorFull : std::false_type {};
+
+template <typename I, typename A>
+struct IsDoubleColMajorFull<flens::FullStorage<double, cxxblas::ColMajor, I, A> >
+    : std::true_type {};
+
+template <typename I, typename A>
+struct IsDoubleColMajorFull<flens::FullStorageView<double, cxxblas::ColMajor, I, A> >
+    : std::true_type {};
+
+template <typename I, typename A>
+struct IsDoubleColMajorFull<flens::ConstFullStorageView<double, cxxblas::ColMajor, I, A> >
+    : std::true_type {};
+
+}  // namespace detail
+}  // namespace flens_gb300
+
+namespace cxxblas {
+
+//-- gemm: double, any integral index -> dgemm_ (column-major)
+template <typename IndexType>
+typename std::enable_if<flens_gb300::detail::IsIndex<IndexType>::value, void>::type
+gemm(StorageOrder order, Transpose transA, Transpose transB,
+     IndexType m, IndexType n, IndexType k,
+     double alpha, const double *A, IndexType ldA,
+     const double *B, IndexType ldB,
+     double beta, double *C, IndexType ldC)
+{
+    if (order == RowMajor) {
+        // C^T = op(B)^T op(A)^T in column-major terms (cxxblas/level3/gemm.tcc:57-64)
+        gemm(ColMajor, transB, transA, n, m, k, alpha, B, ldB, A, ldA, beta, C, ldC);
+        return;
+    }
+    const char ta = flens_gb300::detail::trans_char(transA);
+    const char tb = flens_gb300::detail::trans_char(transB);
+    const int M = int(m), N = int(n), K = int(k);
+    const int LDA = int(ldA), LDB = int(ldB), LDC = int(ldC);
+    dgemm_(&ta, &tb, &M, &N, &K, &alpha, A, &LDA, B, &LDB, &beta, C, &LDC);
+}
+
+//-- trsm: double, any integral index -> dtrsm_ (column-major)
+template <typename IndexType>
+typename std::enable_if<flens_gb300::detail::IsIndex<IndexType>::value, void>::type
+trsm(StorageOrder order, Side side, StorageUpLo upLo, Transpose transA, Diag diag,
+     IndexType m, IndexType n, double alpha,
+     const double *A, IndexType ldA, double *B, IndexType ldB)
+{
+    if (order == RowMajor) {
+        // row-major B is column-major B^T (cxxblas/level3/trsm.tcc:48-52)
+        trsm(ColMajor, side == Left ? Right : Left, upLo == Upper ? Lower : Upper, transA,
+             diag, n, m, alpha, A, ldA, B, ldB);
+        return;
+    }
+    const char s = static_cast<char>(side), u = static_cast<char>(upLo);
+    const char t = flens_gb300::detail::trans_char(transA), d = static_cast<char>(diag);
+    const int M = int(m), N = int(n), LDA = int(ldA), LDB = int(ldB);
+    dtrsm_(&s, &u, &t, &d, &M, &N, &alpha, A, &LDA, B, &LDB);
+}
+
+}  // namespace cxxblas
+
+namespace flens { namespace lapack { namespace generic {
+
+//-- trf for column-major double with int pivots -> dgetrf_
+template <template <typename, cxxblas::StorageOrder, typename, typename> class FS,
+          typename I, typename Alloc, typename VP>
+typename std::enable_if<
+    flens_gb300::detail::IsDoubleColMajorFull<FS<double, cxxblas::ColMajor, I, Alloc> >::value
+        && std::is_same<typename DenseVector<VP>::ElementType, int>::value,
+    typename GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> >::IndexType>::type
+trf_impl(GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> > &A, DenseVector<VP> &piv)
+{
+    typedef typename GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> >::IndexType IndexType;
+    const int m = int(A.numRows()), n = int(A.numCols());
+    const int ld = int(A.leadingDimension() > 0 ? A.leadingDimension() : 1);
+    const int mn = m < n ? m : n;
+    int info = 0;
+    if (m == 0 || n == 0) return IndexType(0);
+    if (piv.stride() == 1) {
+        dgetrf_(&m, &n, A.data(), &ld, piv.data(), &info);
+    } else {
+        std::vector<int> p(mn);
+        dgetrf_(&m, &n, A.data(), &ld, p.data(), &info);
+        for (int i = 0; i < mn; ++i) piv(piv.firstIndex() + i * (piv.inc() > 0 ? 1 : -1)) = p[i];
+    }
+    return IndexType(info);
+}
+
+//-- trs for column-major double with int pivots -> dgetrs_
+template <template <typename, cxxblas::StorageOrder, typename, typename> class FSA,
+          typename IA, typename AA,
+          template <typename, cxxblas::StorageOrder, typename, typename> class FSB,
+          typename IB, typename AB, typename VP>
+typename std::enable_if<
+    flens_gb300::detail::IsDoubleColMajorFull<FSA<double, cxxblas::ColMajor, IA, AA> >::value
+        && flens_gb300::detail::IsDoubleColMajorFull<FSB<double, cxxblas::ColMajor, IB, AB> >::value
+        && std::is_same<typename DenseVector<VP>::ElementType, int>::value,
+    void>::type
+trs_impl(Transpose trans, const GeMatrix<FSA<double, cxxblas::ColMajor, IA, AA> > &A,
+         const DenseVector<VP> &piv, GeMatrix<FSB<double, cxxblas::ColMajor, IB, AB> > &B)
+{
+    const int n = int(A.numCols()), nrhs = int(B.numCols());
+    if (n == 0 || nrhs == 0) return;
+    const int lda = int(A.leadingDimension()), ldb = int(B.leadingDimension());
+    const char t = flens_gb300::detail::trans_char(trans);
+    int info = 0;
+    if (piv.stride() == 1) {
+        dgetrs_(&t, &n, &nrhs, A.data(), &lda, piv.data(), B.data(), &ldb, &info);
+    } else {
+        std::vector<int> p(n);
+        for (int i = 0; i < n; ++i) p[i] = piv(piv.firstIndex() + i * (piv.inc() > 0 ? 1 : -1));
+        dgetrs_(&t, &n, &nrhs, A.data(), &lda, p.data(), B.data(), &ldb, &info);
+    }
+}
+
+} } }  // namespace generic, lapack, flens
+
+#include <flens/flens.tcc>
+
+#endif  // FLENS_GB300_FLENS_GB300_HPP

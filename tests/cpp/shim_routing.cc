@@ -1,0 +1,33 @@
+// Compiled by tests/test_cpp_shim.py against the FLENS headers and
+// include/flens_gb300/flens_gb300.hpp.  Prints one line per routed call so the
+// test can tell whether FLENS's own entry points reached libflens_gb300.so.
+#include <flens_gb300/flens_gb300.hpp>
+
+#include <cstdio>
+
+using namespace flens;
+
+typedef GeMatrix<FullStorage<double, ColMajor> > RealGeMatrix;
+typedef DenseVector<Array<int> > IndexVector;
+
+int main()
+{
+    const int n = 4;
+    RealGeMatrix A(n, n), B(n, n), C(n, n);
+    IndexVector piv(n);
+    // the system of flens/examples/lapack-gesv.cc
+    A = 2, 3, -1, 0,
+        -6, -5, 0, 2,
+        2, -5, 6, -6,
+        4, 6, 2, -3;
+    B = 1;
+    C = 0;
+    C = 2.0*A*B;                                       // -> blas::mm -> cxxblas::gemm
+    std::printf("mm C(1,1)=%g\n", C(1, 1));
+    blas::sm(Left, NoTrans, 1.0, A.lowerUnit(), B);    // -> cxxblas::trsm
+    std::printf("sm B(2,1)=%g\n", B(2, 1));
+    const int info = lapack::trf(A, piv);              // -> generic::trf_impl -> dgetrf_
+    std::printf("trf info=%d piv=%d,%d,%d,%d\n", info, piv(1), piv(2), piv(3), piv(4));
+    std::printf("last_error=%s\n", flens_gb300_last_error());
+    return 0;
+}
