@@ -40,7 +40,7 @@ constexpr int TC_BM = 128;
 constexpr int TC_BN = 256;
 constexpr int TC_STAGES = 4;
 constexpr int TC_THREADS = 128;
-constexpr uint32_t kMbarSpinLimit = 1u << 22;
+constexpr uint32_t kMbarSpinLimit = 1u << 20;
 constexpr uint32_t TC_A_BYTES = TC_BM * 128;       // one stage of A: 128 rows x 128 B
 constexpr uint32_t TC_B_BYTES = TC_BN * 128;       // one stage of B: BN rows x 128 B
 constexpr size_t TC_SMEM = 1024 + (size_t)TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + 256;
