@@ -51,8 +51,10 @@ inline size_t ceil_div(size_t a, size_t b) { return (a + b - 1) / b; }
 struct Workspace {
     int device = -1;
     cudaStream_t stream = nullptr;
-    void *buf = nullptr;         // general scratch
+    void *buf = nullptr;         // general scratch (slot 0)
     size_t bytes = 0;
+    void *slot_buf[4] = {nullptr, nullptr, nullptr, nullptr};   // slots 1..3
+    size_t slot_bytes[4] = {0, 0, 0, 0};
     int *status = nullptr;       // device status word (DeviceStatus bits)
     int *info = nullptr;         // device INFO for host-pointer entry points
 };
@@ -60,6 +62,10 @@ struct Workspace {
 // Returns the workspace bound to `stream` on the current device with at least
 // `bytes` of scratch (nullptr on allocation failure; last error set).
 Workspace *workspace_for(cudaStream_t stream, size_t bytes);
+
+// Independent buffers 1..3 of the same workspace, for callers that hold
+// pointers while calling routines that may grow slot 0.
+void *workspace_slot(cudaStream_t stream, int slot, size_t bytes);
 
 int num_sms();                 // SM count of the current device
 int device_id();               // current device ordinal
@@ -163,6 +169,16 @@ int dtrsm_launch(char side, char upLo, char transA, char diag, int m, int n,
 int dscal_matrix_launch(int m, int n, double alpha, double *B, int ldB,
                         cudaStream_t stream);
 
+// FP32 counterparts (CUDA cores), used by the precision form's solves.
+int sgemm_launch(char transA, char transB, int m, int n, int k, float alpha,
+                 const float *A, int ldA, const float *B, int ldB,
+                 float beta, float *C, int ldC, cudaStream_t stream);
+int sscal_matrix_launch(int m, int n, float alpha, float *B, int ldB,
+                        cudaStream_t stream);
+int strsm_launch(char side, char upLo, char transA, char diag, int m, int n,
+                 float alpha, const float *A, int ldA, float *B, int ldB,
+                 cudaStream_t stream);
+
 int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info,
                   cudaStream_t stream);
 
@@ -171,6 +187,23 @@ int dgetrs_launch(char trans, int n, int nrhs, const double *A, int ldA,
 
 int dlaswp_launch(int nrows, int ncols, double *A, int ldA, int k1, int k2,
                   const int *ipiv, int inc, cudaStream_t stream);
+
+int slaswp_launch(int nrows, int ncols, float *A, int ldA, int k1, int k2,
+                  const int *ipiv, int inc, cudaStream_t stream);
+// LU of FP32 storage (pivot search and scaling in FP64); the trailing update
+// on the tensor cores in precision tc_kind (TcKind), or FP32 CUDA cores if < 0
+int sgetrf_launch(int m, int n, float *A, int ldA, int *ipiv, int *info,
+                  int tc_kind, cudaStream_t stream);
+int sgetrs_launch(char trans, int n, int nrhs, const float *A, int ldA,
+                  const int *ipiv, float *B, int ldB, cudaStream_t stream);
+
+// Tensor-core trailing update C -= A21*U12 (m x n, depth k, FP32 storage)
+// in precision `kind`, operand buffers at `buf`
+// (tc_update_workspace_bytes(kind, m, n, k) bytes, 256-byte aligned).
+size_t tc_update_workspace_bytes(int kind, int m, int n, int k);
+int tc_trailing_update(int kind, int m, int n, int k, const float *A21, int ldA21,
+                       const float *U12, int ldU12, float *A22, int ldA22, void *buf,
+                       cudaStream_t stream);
 
 // Reads and clears the workspace status word for `stream` (synchronises).
 int check_device_status(cudaStream_t stream);

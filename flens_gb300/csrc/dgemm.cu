@@ -24,12 +24,12 @@ constexpr int BM = 64, BN = 64, BK = 16, PAD = 1;
 
 // Load the ROWS x BK slab of op(X) starting at (r0, k0) into S[kk][r].
 // CR: op(X) is contiguous along r in memory (else along kk).
-template <bool CR, int ROWS, int NT>
+template <typename T, bool CR, int ROWS, int NT>
 struct SlabLoader {
     static constexpr int PER = ROWS * BK / NT;
-    double v[PER];
+    T v[PER];
 
-    __device__ __forceinline__ void fetch(const double *__restrict__ X, int ld,
+    __device__ __forceinline__ void fetch(const T *__restrict__ X, int ld,
                                           int r0, int rTot, int k0, int kTot) {
 #pragma unroll
         for (int t = 0; t < PER; ++t) {
@@ -43,14 +43,14 @@ struct SlabLoader {
                 r = e / BK;
             }
             const int gr = r0 + r, gk = k0 + kk;
-            double x = 0.0;
+            T x = T(0);
             if (gr < rTot && gk < kTot) {
                 x = CR ? X[(size_t)gr + (size_t)gk * ld] : X[(size_t)gk + (size_t)gr * ld];
             }
             v[t] = x;
         }
     }
-    __device__ __forceinline__ void store(double (*S)[ROWS + PAD]) {
+    __device__ __forceinline__ void store(T (*S)[ROWS + PAD]) {
 #pragma unroll
         for (int t = 0; t < PER; ++t) {
             const int e = threadIdx.x + t * NT;
@@ -70,24 +70,24 @@ struct SlabLoader {
 // ---------------------------------------------------------------- DFMA ----
 // 64x64 CTA tile, 256 threads as 16x16, each thread a 4x4 sub-tile strided by
 // 16 so shared-memory reads are conflict-free broadcasts.
-template <bool TA, bool TB>
+template <typename T, bool TA, bool TB>
 __global__ void __launch_bounds__(256)
-dgemm_fma_kernel(int m, int n, int k, double alpha,
-                 const double *__restrict__ A, int ldA,
-                 const double *__restrict__ B, int ldB,
-                 double beta, double *__restrict__ C, int ldC) {
-    __shared__ double As[2][BK][BM + PAD];
-    __shared__ double Bs[2][BK][BN + PAD];
+dgemm_fma_kernel(int m, int n, int k, T alpha,
+                 const T *__restrict__ A, int ldA,
+                 const T *__restrict__ B, int ldB,
+                 T beta, T *__restrict__ C, int ldC) {
+    __shared__ T As[2][BK][BM + PAD];
+    __shared__ T Bs[2][BK][BN + PAD];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
 
-    SlabLoader<!TA, BM, 256> la;
-    SlabLoader<TB, BN, 256> lb;
-    double acc[4][4];
+    SlabLoader<T, !TA, BM, 256> la;
+    SlabLoader<T, TB, BN, 256> lb;
+    T acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
 
     const int nk = (k + BK - 1) / BK;
     if (nk > 0) {
@@ -105,7 +105,7 @@ dgemm_fma_kernel(int m, int n, int k, double alpha,
         }
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
-            double a[4], b[4];
+            T a[4], b[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) a[i] = As[cur][kk][tx + 16 * i];
 #pragma unroll
@@ -129,7 +129,7 @@ dgemm_fma_kernel(int m, int n, int k, double alpha,
         for (int i = 0; i < 4; ++i) {
             const int gi = m0 + tx + 16 * i;
             if (gi >= m) continue;
-            double *c = &C[(size_t)gi + (size_t)gj * ldC];
+            T *c = &C[(size_t)gi + (size_t)gj * ldC];
             *c = fma(alpha, acc[i][j], beta * *c);
         }
     }
@@ -158,8 +158,8 @@ dgemm_dmma_kernel(int m, int n, int k, double alpha,
     const int wm = warp & 1, wn = warp >> 1;
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
 
-    SlabLoader<!TA, BM, 128> la;
-    SlabLoader<TB, BN, 128> lb;
+    SlabLoader<double, !TA, BM, 128> la;
+    SlabLoader<double, TB, BN, 128> lb;
     double acc[4][4][2];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -223,30 +223,30 @@ dgemm_dmma_kernel(int m, int n, int k, double alpha,
 constexpr int SK_K = 64;
 
 // op(A) = A (rows contiguous): one thread per row of C.
-template <int NC, bool TB>
+template <typename T, int NC, bool TB>
 __global__ void __launch_bounds__(256)
-dgemm_skinny_nn_kernel(int m, int n, int k, double alpha, const double *__restrict__ A, int ldA,
-                       const double *__restrict__ B, int ldB, double beta,
-                       double *__restrict__ C, int ldC) {
-    __shared__ double Bs[SK_K][NC];
+dgemm_skinny_nn_kernel(int m, int n, int k, T alpha, const T *__restrict__ A, int ldA,
+                       const T *__restrict__ B, int ldB, T beta,
+                       T *__restrict__ C, int ldC) {
+    __shared__ T Bs[SK_K][NC];
     const int i = blockIdx.x * 256 + threadIdx.x;
-    double acc[NC];
+    T acc[NC];
 #pragma unroll
-    for (int j = 0; j < NC; ++j) acc[j] = 0.0;
+    for (int j = 0; j < NC; ++j) acc[j] = T(0);
     for (int k0 = 0; k0 < k; k0 += SK_K) {
         const int kk = min(SK_K, k - k0);
         for (int e = threadIdx.x; e < SK_K * NC; e += 256) {
             const int p = e % SK_K, j = e / SK_K;
-            double v = 0.0;
+            T v = T(0);
             if (p < kk && j < n)
                 v = TB ? B[(size_t)j + (size_t)(k0 + p) * ldB] : B[(size_t)(k0 + p) + (size_t)j * ldB];
             Bs[p][j] = v;
         }
         __syncthreads();
         if (i < m) {
-            const double *a = A + i + (size_t)k0 * ldA;
+            const T *a = A + i + (size_t)k0 * ldA;
             for (int p = 0; p < kk; ++p) {
-                const double av = a[(size_t)p * ldA];
+                const T av = a[(size_t)p * ldA];
 #pragma unroll
                 for (int j = 0; j < NC; ++j) acc[j] = fma(av, Bs[p][j], acc[j]);
             }
@@ -257,7 +257,7 @@ dgemm_skinny_nn_kernel(int m, int n, int k, double alpha, const double *__restri
 #pragma unroll
         for (int j = 0; j < NC; ++j) {
             if (j < n) {
-                double *c = &C[(size_t)i + (size_t)j * ldC];
+                T *c = &C[(size_t)i + (size_t)j * ldC];
                 *c = fma(alpha, acc[j], beta * *c);
             }
         }
@@ -265,31 +265,31 @@ dgemm_skinny_nn_kernel(int m, int n, int k, double alpha, const double *__restri
 }
 
 // op(A) = A^T (each row of op(A) contiguous in memory): one warp per row of C.
-template <int NC, bool TB>
+template <typename T, int NC, bool TB>
 __global__ void __launch_bounds__(256)
-dgemm_skinny_tn_kernel(int m, int n, int k, double alpha, const double *__restrict__ A, int ldA,
-                       const double *__restrict__ B, int ldB, double beta,
-                       double *__restrict__ C, int ldC) {
-    __shared__ double Bs[SK_K][NC];
+dgemm_skinny_tn_kernel(int m, int n, int k, T alpha, const T *__restrict__ A, int ldA,
+                       const T *__restrict__ B, int ldB, T beta,
+                       T *__restrict__ C, int ldC) {
+    __shared__ T Bs[SK_K][NC];
     const int lane = threadIdx.x & 31;
     const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
-    double acc[NC];
+    T acc[NC];
 #pragma unroll
-    for (int j = 0; j < NC; ++j) acc[j] = 0.0;
+    for (int j = 0; j < NC; ++j) acc[j] = T(0);
     for (int k0 = 0; k0 < k; k0 += SK_K) {
         const int kk = min(SK_K, k - k0);
         for (int e = threadIdx.x; e < SK_K * NC; e += 256) {
             const int p = e % SK_K, j = e / SK_K;
-            double v = 0.0;
+            T v = T(0);
             if (p < kk && j < n)
                 v = TB ? B[(size_t)j + (size_t)(k0 + p) * ldB] : B[(size_t)(k0 + p) + (size_t)j * ldB];
             Bs[p][j] = v;
         }
         __syncthreads();
         if (i < m) {
-            const double *a = A + (size_t)i * ldA + k0;
+            const T *a = A + (size_t)i * ldA + k0;
             for (int p = lane; p < kk; p += 32) {
-                const double av = a[p];
+                const T av = a[p];
 #pragma unroll
                 for (int j = 0; j < NC; ++j) acc[j] = fma(av, Bs[p][j], acc[j]);
             }
@@ -305,28 +305,29 @@ dgemm_skinny_tn_kernel(int m, int n, int k, double alpha, const double *__restri
 #pragma unroll
         for (int j = 0; j < NC; ++j) {
             if (j < n) {
-                double *c = &C[(size_t)i + (size_t)j * ldC];
+                T *c = &C[(size_t)i + (size_t)j * ldC];
                 *c = fma(alpha, acc[j], beta * *c);
             }
         }
     }
 }
 
-template <int NC>
-void launch_skinny(bool ta, bool tb, int m, int n, int k, double alpha, const double *A, int ldA,
-                   const double *B, int ldB, double beta, double *C, int ldC, cudaStream_t s) {
+template <typename T, int NC>
+void launch_skinny(bool ta, bool tb, int m, int n, int k, T alpha, const T *A, int ldA,
+                   const T *B, int ldB, T beta, T *C, int ldC, cudaStream_t s) {
     if (!ta) {
         const int grid = ceil_div(m, 256);
-        if (tb) dgemm_skinny_nn_kernel<NC, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
-        else dgemm_skinny_nn_kernel<NC, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+        if (tb) dgemm_skinny_nn_kernel<T, NC, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+        else dgemm_skinny_nn_kernel<T, NC, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
     } else {
         const int grid = ceil_div(m, 8);
-        if (tb) dgemm_skinny_tn_kernel<NC, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
-        else dgemm_skinny_tn_kernel<NC, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+        if (tb) dgemm_skinny_tn_kernel<T, NC, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+        else dgemm_skinny_tn_kernel<T, NC, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
     }
 }
 
-__global__ void scale_kernel(int m, int n, double alpha, double *__restrict__ X, int ld) {
+template <typename T>
+__global__ void scale_kernel(int m, int n, T alpha, T *__restrict__ X, int ld) {
     const size_t total = (size_t)m * n;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
          e += (size_t)gridDim.x * blockDim.x) {
@@ -351,14 +352,68 @@ Engine pick_engine() {
 
 }  // namespace
 
-int dscal_matrix_launch(int m, int n, double alpha, double *X, int ld, cudaStream_t stream) {
+template <typename T>
+int scal_matrix_launch_t(int m, int n, T alpha, T *X, int ld, cudaStream_t stream) {
     if (m <= 0 || n <= 0) return kOk;
     const size_t total = (size_t)m * n;
     int blocks = (int)ceil_div(total, (size_t)256);
     const int cap = num_sms() * 8;
     if (cap > 0 && blocks > cap) blocks = cap;
-    KTimer kt(kFamAux, stream, (double)m * n, 16.0 * m * n);
-    scale_kernel<<<blocks, 256, 0, stream>>>(m, n, alpha, X, ld);
+    KTimer kt(kFamAux, stream, (double)m * n, 2.0 * sizeof(T) * m * n);
+    scale_kernel<T><<<blocks, 256, 0, stream>>>(m, n, alpha, X, ld);
+    FG_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+int dscal_matrix_launch(int m, int n, double alpha, double *X, int ld, cudaStream_t stream) {
+    return scal_matrix_launch_t<double>(m, n, alpha, X, ld, stream);
+}
+
+int sscal_matrix_launch(int m, int n, float alpha, float *X, int ld, cudaStream_t stream) {
+    return scal_matrix_launch_t<float>(m, n, alpha, X, ld, stream);
+}
+
+template <typename T>
+int gemm_launch_t(char transA, char transB, int m, int n, int k, T alpha, const T *A, int ldA,
+                  const T *B, int ldB, T beta, T *C, int ldC, cudaStream_t stream) {
+    if (m == 0 || n == 0) return kOk;
+    if (alpha == T(0)) return scal_matrix_launch_t<T>(m, n, beta, C, ldC, stream);
+    const bool ta = !(transA == 'N' || transA == 'n');
+    const bool tb = !(transB == 'N' || transB == 'n');
+    const dim3 grid(ceil_div(m, BM), ceil_div(n, BN));
+    if (grid.y > 65535) {
+        set_last_error("gemm: n=%d too large for one launch", n);
+        return kErrUnsupported;
+    }
+    KTimer kt(sizeof(T) == 8 ? kFamGemm : kFamAux, stream, 2.0 * m * n * (double)k,
+              (double)sizeof(T) * ((double)m * k + (double)k * n + 2.0 * m * n));
+    if (n <= 16) {
+        trace("gemm<%d> %c%c m=%d n=%d k=%d engine=skinny", (int)sizeof(T), transA, transB, m, n, k);
+        if (n <= 1) launch_skinny<T, 1>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
+        else if (n <= 2) launch_skinny<T, 2>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
+        else if (n <= 4) launch_skinny<T, 4>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
+        else if (n <= 8) launch_skinny<T, 8>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
+        else launch_skinny<T, 16>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
+        FG_CUDA(cudaGetLastError());
+        return kOk;
+    }
+    const Engine e = sizeof(T) == 8 ? pick_engine() : Engine::Fma;
+    trace("gemm<%d> %c%c m=%d n=%d k=%d engine=%s", (int)sizeof(T), transA, transB, m, n, k,
+          e == Engine::Dmma ? "dmma" : "fma");
+    if (e == Engine::Dmma) {
+        const double *Ad = (const double *)A, *Bd = (const double *)B;
+        double *Cd = (double *)C;
+        const double al = (double)alpha, be = (double)beta;
+        if (!ta && !tb) dgemm_dmma_kernel<false, false><<<grid, 128, 0, stream>>>(m, n, k, al, Ad, ldA, Bd, ldB, be, Cd, ldC);
+        else if (ta && !tb) dgemm_dmma_kernel<true, false><<<grid, 128, 0, stream>>>(m, n, k, al, Ad, ldA, Bd, ldB, be, Cd, ldC);
+        else if (!ta && tb) dgemm_dmma_kernel<false, true><<<grid, 128, 0, stream>>>(m, n, k, al, Ad, ldA, Bd, ldB, be, Cd, ldC);
+        else dgemm_dmma_kernel<true, true><<<grid, 128, 0, stream>>>(m, n, k, al, Ad, ldA, Bd, ldB, be, Cd, ldC);
+    } else {
+        if (!ta && !tb) dgemm_fma_kernel<T, false, false><<<grid, 256, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+        else if (ta && !tb) dgemm_fma_kernel<T, true, false><<<grid, 256, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+        else if (!ta && tb) dgemm_fma_kernel<T, false, true><<<grid, 256, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+        else dgemm_fma_kernel<T, true, true><<<grid, 256, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+    }
     FG_CUDA(cudaGetLastError());
     return kOk;
 }
@@ -366,42 +421,15 @@ int dscal_matrix_launch(int m, int n, double alpha, double *X, int ld, cudaStrea
 int dgemm_launch(char transA, char transB, int m, int n, int k, double alpha,
                  const double *A, int ldA, const double *B, int ldB,
                  double beta, double *C, int ldC, cudaStream_t stream) {
-    if (m == 0 || n == 0) return kOk;
-    if (alpha == 0.0) return dscal_matrix_launch(m, n, beta, C, ldC, stream);
-    const bool ta = !(transA == 'N' || transA == 'n');
-    const bool tb = !(transB == 'N' || transB == 'n');
-    const dim3 grid(ceil_div(m, BM), ceil_div(n, BN));
-    if (grid.y > 65535) {
-        set_last_error("dgemm: n=%d too large for one launch", n);
-        return kErrUnsupported;
-    }
-    KTimer kt(kFamGemm, stream, 2.0 * m * n * (double)k,
-              8.0 * ((double)m * k + (double)k * n + 2.0 * m * n));
-    if (n <= 16) {
-        trace("dgemm %c%c m=%d n=%d k=%d engine=skinny", transA, transB, m, n, k);
-        if (n <= 1) launch_skinny<1>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
-        else if (n <= 2) launch_skinny<2>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
-        else if (n <= 4) launch_skinny<4>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
-        else if (n <= 8) launch_skinny<8>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
-        else launch_skinny<16>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
-        FG_CUDA(cudaGetLastError());
-        return kOk;
-    }
-    const Engine e = pick_engine();
-    trace("dgemm %c%c m=%d n=%d k=%d engine=%s", transA, transB, m, n, k,
-          e == Engine::Dmma ? "dmma" : "fma");
-#define FG_LAUNCH(KERNEL, NT)                                                          \
-    do {                                                                               \
-        if (!ta && !tb) KERNEL<false, false><<<grid, NT, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC); \
-        else if (ta && !tb) KERNEL<true, false><<<grid, NT, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC); \
-        else if (!ta && tb) KERNEL<false, true><<<grid, NT, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC); \
-        else KERNEL<true, true><<<grid, NT, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC); \
-    } while (0)
-    if (e == Engine::Dmma) FG_LAUNCH(dgemm_dmma_kernel, 128);
-    else FG_LAUNCH(dgemm_fma_kernel, 256);
-#undef FG_LAUNCH
-    FG_CUDA(cudaGetLastError());
-    return kOk;
+    return gemm_launch_t<double>(transA, transB, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC,
+                                 stream);
+}
+
+int sgemm_launch(char transA, char transB, int m, int n, int k, float alpha, const float *A,
+                 int ldA, const float *B, int ldB, float beta, float *C, int ldC,
+                 cudaStream_t stream) {
+    return gemm_launch_t<float>(transA, transB, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC,
+                                stream);
 }
 
 }  // namespace fg

@@ -129,8 +129,9 @@ __device__ __forceinline__ void block_argmax(double &v, int &i, double *red_v, i
 // A points at the panel's top-left element A(j,j); the panel is mp x jb.
 // CTA b owns panel rows [b*R, min(mp,(b+1)*R)), kept in shared memory as
 // S[c*R + r].
+template <typename T>
 __global__ void __launch_bounds__(PANEL_THREADS)
-panel_kernel(double *__restrict__ A, int lda, int mp, int jb, int j0,
+panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
              int *__restrict__ ipiv, int *__restrict__ info, int *__restrict__ status,
              PanelScratch ps, int R, unsigned long long epoch) {
     extern __shared__ double S[];
@@ -255,7 +256,7 @@ panel_kernel(double *__restrict__ A, int lda, int mp, int jb, int j0,
 
     for (int e = tid; e < nr * jb; e += PANEL_THREADS) {
         const int r = e % nr, c = e / nr;
-        A[(size_t)(rb + r) + (size_t)c * lda] = S[c * R + r];
+        A[(size_t)(rb + r) + (size_t)c * lda] = (T)S[c * R + r];
     }
 
     // -- block 0, warp 0: the jb interchanges as (dst, src) row moves.
@@ -311,8 +312,9 @@ panel_kernel(double *__restrict__ A, int lda, int mp, int jb, int j0,
 
 // Apply the panel's row moves to columns [0, cSplit) and [cSplit+skip, ...),
 // ncols columns in total; one warp per column.
+template <typename T>
 __global__ void __launch_bounds__(256)
-laswp_pairs_kernel(double *__restrict__ A, int lda, int ncols, int cSplit, int skip,
+laswp_pairs_kernel(T *__restrict__ A, int lda, int ncols, int cSplit, int skip,
                    const int *__restrict__ cntp, const int *__restrict__ dst,
                    const int *__restrict__ src) {
     __shared__ int s_dst[2 * PANEL_NB], s_src[2 * PANEL_NB];
@@ -327,8 +329,8 @@ laswp_pairs_kernel(double *__restrict__ A, int lda, int ncols, int cSplit, int s
     const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (q >= ncols) return;
     const int c = q < cSplit ? q : q + skip;
-    double *col = A + (size_t)c * lda;
-    double v[4];
+    T *col = A + (size_t)c * lda;
+    T v[4];
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
         const int e = lane + 32 * t;
@@ -372,8 +374,9 @@ __global__ void laswp_perm_kernel(int nrows, int k1, int k2, const int *__restri
 }
 
 // tmp[:, c] = A[perm, c] for the first nrows rows
-__global__ void gather_rows_kernel(int nrows, int ncols, const double *__restrict__ A, int lda,
-                                   const int *__restrict__ perm, double *__restrict__ tmp) {
+template <typename T>
+__global__ void gather_rows_kernel(int nrows, int ncols, const T *__restrict__ A, int lda,
+                                   const int *__restrict__ perm, T *__restrict__ tmp) {
     const size_t total = (size_t)nrows * ncols;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
          e += (size_t)gridDim.x * blockDim.x) {
@@ -382,8 +385,9 @@ __global__ void gather_rows_kernel(int nrows, int ncols, const double *__restric
     }
 }
 
-__global__ void copy_back_kernel(int nrows, int ncols, const double *__restrict__ tmp,
-                                 double *__restrict__ A, int lda) {
+template <typename T>
+__global__ void copy_back_kernel(int nrows, int ncols, const T *__restrict__ tmp,
+                                 T *__restrict__ A, int lda) {
     const size_t total = (size_t)nrows * ncols;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
          e += (size_t)gridDim.x * blockDim.x) {
@@ -394,17 +398,45 @@ __global__ void copy_back_kernel(int nrows, int ncols, const double *__restrict_
 
 bool g_panel_attr_set = false;
 
+template <typename T>
+int trsm_t(char side, char uplo, char ta, char diag, int m, int n, T alpha, const T *A, int ldA,
+           T *B, int ldB, cudaStream_t s);
+template <>
+int trsm_t<double>(char side, char uplo, char ta, char diag, int m, int n, double alpha,
+                   const double *A, int ldA, double *B, int ldB, cudaStream_t s) {
+    return dtrsm_launch(side, uplo, ta, diag, m, n, alpha, A, ldA, B, ldB, s);
+}
+template <>
+int trsm_t<float>(char side, char uplo, char ta, char diag, int m, int n, float alpha,
+                  const float *A, int ldA, float *B, int ldB, cudaStream_t s) {
+    return strsm_launch(side, uplo, ta, diag, m, n, alpha, A, ldA, B, ldB, s);
+}
+template <typename T>
+int gemm_tt(char ta, char tb, int m, int n, int k, T alpha, const T *A, int ldA, const T *B,
+            int ldB, T beta, T *C, int ldC, cudaStream_t s);
+template <>
+int gemm_tt<double>(char ta, char tb, int m, int n, int k, double alpha, const double *A, int ldA,
+                    const double *B, int ldB, double beta, double *C, int ldC, cudaStream_t s) {
+    return dgemm_launch(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, s);
+}
+template <>
+int gemm_tt<float>(char ta, char tb, int m, int n, int k, float alpha, const float *A, int ldA,
+                   const float *B, int ldB, float beta, float *C, int ldC, cudaStream_t s) {
+    return sgemm_launch(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, s);
+}
+
 }  // namespace
 
-int dlaswp_launch(int nrows, int ncols, double *A, int ldA, int k1, int k2, const int *ipiv,
-                  int inc, cudaStream_t stream) {
+template <typename T>
+int laswp_launch_t(int nrows, int ncols, T *A, int ldA, int k1, int k2, const int *ipiv, int inc,
+                   cudaStream_t stream) {
     if (nrows <= 0 || ncols <= 0 || k2 < k1) return kOk;
     const size_t permBytes = ((size_t)nrows * sizeof(int) + 255) / 256 * 256;
-    const size_t tmpBytes = (size_t)nrows * ncols * sizeof(double);
+    const size_t tmpBytes = (size_t)nrows * ncols * sizeof(T);
     Workspace *w = workspace_for(stream, permBytes + tmpBytes);
     if (!w) return kErrAlloc;
     int *perm = (int *)w->buf;
-    double *tmp = (double *)((char *)w->buf + permBytes);
+    T *tmp = (T *)((char *)w->buf + permBytes);
     const int use_smem = (size_t)nrows * sizeof(int) <= 200 * 1024 ? 1 : 0;
     if (use_smem) {
         static bool attr = false;
@@ -414,33 +446,78 @@ int dlaswp_launch(int nrows, int ncols, double *A, int ldA, int k1, int k2, cons
             attr = true;
         }
     }
-    KTimer kt(kFamLaswp, stream, 0.0, 2.0 * (double)nrows * ncols * 16.0);
+    KTimer kt(kFamLaswp, stream, 0.0, 4.0 * sizeof(T) * (double)nrows * ncols);
     laswp_perm_kernel<<<1, 1024, use_smem ? (size_t)nrows * sizeof(int) : 0, stream>>>(
         nrows, k1, k2, ipiv, inc, perm, use_smem);
     FG_CUDA(cudaGetLastError());
     const size_t total = (size_t)nrows * ncols;
     int blocks = (int)ceil_div(total, (size_t)256);
     if (blocks > num_sms() * 16) blocks = num_sms() * 16;
-    gather_rows_kernel<<<blocks, 256, 0, stream>>>(nrows, ncols, A, ldA, perm, tmp);
+    gather_rows_kernel<T><<<blocks, 256, 0, stream>>>(nrows, ncols, A, ldA, perm, tmp);
     FG_CUDA(cudaGetLastError());
-    copy_back_kernel<<<blocks, 256, 0, stream>>>(nrows, ncols, tmp, A, ldA);
+    copy_back_kernel<T><<<blocks, 256, 0, stream>>>(nrows, ncols, tmp, A, ldA);
     FG_CUDA(cudaGetLastError());
     return kOk;
 }
 
-int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, cudaStream_t stream) {
+// perm[r] = source row of row r after the interchanges ipiv(1..nrows): the
+// forward laswp as one gather (used by the solves of the precision form).
+int laswp_perm_launch(int nrows, const int *ipiv, int *perm, cudaStream_t stream) {
+    if (nrows <= 0) return kOk;
+    const int use_smem = (size_t)nrows * sizeof(int) <= 200 * 1024 ? 1 : 0;
+    if (use_smem) {
+        static bool attr = false;
+        if (!attr) {
+            FG_CUDA(cudaFuncSetAttribute(laswp_perm_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+            attr = true;
+        }
+    }
+    KTimer kt(kFamLaswp, stream, 0.0, 8.0 * nrows);
+    laswp_perm_kernel<<<1, 1024, use_smem ? (size_t)nrows * sizeof(int) : 0, stream>>>(
+        nrows, 1, nrows, ipiv, 1, perm, use_smem);
+    FG_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+int dlaswp_launch(int nrows, int ncols, double *A, int ldA, int k1, int k2, const int *ipiv,
+                  int inc, cudaStream_t stream) {
+    return laswp_launch_t<double>(nrows, ncols, A, ldA, k1, k2, ipiv, inc, stream);
+}
+
+int slaswp_launch(int nrows, int ncols, float *A, int ldA, int k1, int k2, const int *ipiv,
+                  int inc, cudaStream_t stream) {
+    return laswp_launch_t<float>(nrows, ncols, A, ldA, k1, k2, ipiv, inc, stream);
+}
+
+// Bytes of slot-0 workspace the blocked LU needs: the panel exchange area
+// plus, for a tensor-core trailing update, its operand buffers.
+size_t getrf_workspace_bytes(int m, int n, int tc_kind) {
+    size_t b = (panel_scratch_bytes() + 255) / 256 * 256;
+    if (tc_kind >= 0) b += tc_update_workspace_bytes(tc_kind, m, n, PANEL_NB);
+    return b;
+}
+
+// Blocked right-looking LU over storage T.  Panel, interchanges and the U12
+// solve always run here; the trailing update A22 -= A21*U12 runs in T on the
+// CUDA cores (tc_kind < 0) or, for T = float, on the tensor cores in the
+// precision `tc_kind` (see tc_gemm.cu).
+template <typename T>
+int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, cudaStream_t stream) {
     FG_CUDA(cudaMemsetAsync(info, 0, sizeof(int), stream));
     if (m == 0 || n == 0) return kOk;
     const int mn = m < n ? m : n;
-    Workspace *w = workspace_for(stream, panel_scratch_bytes());
+    Workspace *w = workspace_for(stream, getrf_workspace_bytes(m, n, tc_kind));
     if (!w) return kErrAlloc;
     PanelScratch ps = carve_panel_scratch(w->buf);
+    void *tc_buf = (char *)w->buf + (panel_scratch_bytes() + 255) / 256 * 256;
     FG_CUDA(cudaMemsetAsync(ps.slots, 0, kSlotBytes, stream));
     unsigned long long epoch = 0;
-    if (!g_panel_attr_set) {
-        FG_CUDA(cudaFuncSetAttribute(panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    static bool attr = false;
+    if (!attr) {
+        FG_CUDA(cudaFuncSetAttribute(panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)PANEL_SMEM_MAX));
-        g_panel_attr_set = true;
+        attr = true;
     }
     int sms = num_sms();
     if (sms <= 0) {
@@ -448,7 +525,8 @@ int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, cudaSt
         return kErrNoDevice;
     }
     const int gcap = sms < PANEL_GMAX ? sms : PANEL_GMAX;
-    trace("dgetrf m=%d n=%d lda=%d panel grid<=%d", m, n, ldA, gcap);
+    trace("getrf<%d> m=%d n=%d lda=%d panel grid<=%d update=%d", (int)sizeof(T), m, n, ldA, gcap,
+          tc_kind);
 
     for (int j = 0; j < mn;) {
         const int mp = m - j;
@@ -459,12 +537,12 @@ int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, cudaSt
         int nb = PANEL_NB;
         while (nb > 1 && (size_t)R * nb * sizeof(double) > PANEL_SMEM_MAX) nb >>= 1;
         if ((size_t)R * nb * sizeof(double) > PANEL_SMEM_MAX) {
-            set_last_error("dgetrf: m=%d too tall for the shared-memory panel", m);
+            set_last_error("getrf: m=%d too tall for the shared-memory panel", m);
             return kErrUnsupported;
         }
         const int jb = (mn - j) < nb ? (mn - j) : nb;
         const int G = ceil_div(mp, R);
-        double *Ap = A + j + (size_t)j * ldA;
+        T *Ap = A + j + (size_t)j * ldA;
         int *status = w->status;
         int j0 = j;
         size_t smem = (size_t)R * jb * sizeof(double);
@@ -473,8 +551,8 @@ int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, cudaSt
                         &epoch};
         {
             KTimer ktp(kFamPanel, stream, (double)mp * jb * jb - (double)jb * jb * jb / 3.0,
-                       16.0 * (double)mp * jb);
-            FG_CUDA(cudaLaunchCooperativeKernel((const void *)panel_kernel, dim3(G),
+                       2.0 * sizeof(T) * (double)mp * jb);
+            FG_CUDA(cudaLaunchCooperativeKernel((const void *)panel_kernel<T>, dim3(G),
                                                 dim3(PANEL_THREADS), args, smem, stream));
         }
         // interchanges on the columns outside the panel
@@ -482,19 +560,25 @@ int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, cudaSt
         if (ncols > 0) {
             const int blocks = ceil_div(ncols, 256 / 32);
             KTimer ktl(kFamLaswp, stream, 0.0, 0.0);
-            laswp_pairs_kernel<<<blocks, 256, 0, stream>>>(A, ldA, ncols, j, jb, ps.swap_cnt,
-                                                           ps.swap_dst, ps.swap_src);
+            laswp_pairs_kernel<T><<<blocks, 256, 0, stream>>>(A, ldA, ncols, j, jb, ps.swap_cnt,
+                                                              ps.swap_dst, ps.swap_src);
             FG_CUDA(cudaGetLastError());
         }
         if (j + jb < n) {
-            int st = dtrsm_launch('L', 'L', 'N', 'U', jb, n - j - jb, 1.0, Ap, ldA,
-                                  A + j + (size_t)(j + jb) * ldA, ldA, stream);
+            int st = trsm_t<T>('L', 'L', 'N', 'U', jb, n - j - jb, T(1), Ap, ldA,
+                               A + j + (size_t)(j + jb) * ldA, ldA, stream);
             if (st != kOk) return st;
             if (j + jb < m) {
-                st = dgemm_launch('N', 'N', m - j - jb, n - j - jb, jb, -1.0,
-                                  A + (j + jb) + (size_t)j * ldA, ldA,
-                                  A + j + (size_t)(j + jb) * ldA, ldA, 1.0,
-                                  A + (j + jb) + (size_t)(j + jb) * ldA, ldA, stream);
+                T *A21 = A + (j + jb) + (size_t)j * ldA;
+                T *U12 = A + j + (size_t)(j + jb) * ldA;
+                T *A22 = A + (j + jb) + (size_t)(j + jb) * ldA;
+                if (tc_kind >= 0)
+                    st = tc_trailing_update(tc_kind, m - j - jb, n - j - jb, jb, (const float *)A21,
+                                            ldA, (const float *)U12, ldA, (float *)A22, ldA, tc_buf,
+                                            stream);
+                else
+                    st = gemm_tt<T>('N', 'N', m - j - jb, n - j - jb, jb, T(-1), A21, ldA, U12, ldA,
+                                    T(1), A22, ldA, stream);
                 if (st != kOk) return st;
             }
         }
@@ -503,18 +587,38 @@ int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, cudaSt
     return kOk;
 }
 
-int dgetrs_launch(char trans, int n, int nrhs, const double *A, int ldA, const int *ipiv,
-                  double *B, int ldB, cudaStream_t stream) {
+int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, cudaStream_t stream) {
+    return getrf_t<double>(m, n, A, ldA, ipiv, info, -1, stream);
+}
+
+int sgetrf_launch(int m, int n, float *A, int ldA, int *ipiv, int *info, int tc_kind,
+                  cudaStream_t stream) {
+    return getrf_t<float>(m, n, A, ldA, ipiv, info, tc_kind, stream);
+}
+
+template <typename T>
+int getrs_t(char trans, int n, int nrhs, const T *A, int ldA, const int *ipiv, T *B, int ldB,
+            cudaStream_t stream) {
     if (n == 0 || nrhs == 0) return kOk;
     int st;
     if (trans == 'N' || trans == 'n') {
-        if ((st = dlaswp_launch(n, nrhs, B, ldB, 1, n, ipiv, 1, stream)) != kOk) return st;
-        if ((st = dtrsm_launch('L', 'L', 'N', 'U', n, nrhs, 1.0, A, ldA, B, ldB, stream)) != kOk) return st;
-        return dtrsm_launch('L', 'U', 'N', 'N', n, nrhs, 1.0, A, ldA, B, ldB, stream);
+        if ((st = laswp_launch_t<T>(n, nrhs, B, ldB, 1, n, ipiv, 1, stream)) != kOk) return st;
+        if ((st = trsm_t<T>('L', 'L', 'N', 'U', n, nrhs, T(1), A, ldA, B, ldB, stream)) != kOk) return st;
+        return trsm_t<T>('L', 'U', 'N', 'N', n, nrhs, T(1), A, ldA, B, ldB, stream);
     }
-    if ((st = dtrsm_launch('L', 'U', 'T', 'N', n, nrhs, 1.0, A, ldA, B, ldB, stream)) != kOk) return st;
-    if ((st = dtrsm_launch('L', 'L', 'T', 'U', n, nrhs, 1.0, A, ldA, B, ldB, stream)) != kOk) return st;
-    return dlaswp_launch(n, nrhs, B, ldB, 1, n, ipiv, -1, stream);
+    if ((st = trsm_t<T>('L', 'U', 'T', 'N', n, nrhs, T(1), A, ldA, B, ldB, stream)) != kOk) return st;
+    if ((st = trsm_t<T>('L', 'L', 'T', 'U', n, nrhs, T(1), A, ldA, B, ldB, stream)) != kOk) return st;
+    return laswp_launch_t<T>(n, nrhs, B, ldB, 1, n, ipiv, -1, stream);
+}
+
+int dgetrs_launch(char trans, int n, int nrhs, const double *A, int ldA, const int *ipiv,
+                  double *B, int ldB, cudaStream_t stream) {
+    return getrs_t<double>(trans, n, nrhs, A, ldA, ipiv, B, ldB, stream);
+}
+
+int sgetrs_launch(char trans, int n, int nrhs, const float *A, int ldA, const int *ipiv, float *B,
+                  int ldB, cudaStream_t stream) {
+    return getrs_t<float>(trans, n, nrhs, A, ldA, ipiv, B, ldB, stream);
 }
 
 }  // namespace fg
@@ -605,9 +709,9 @@ int laswp_fixed(int nrows, int ncols, double *A, int ldA, int k1, int k2, const 
     const size_t total = (size_t)nrows * ncols;
     int blocks = (int)ceil_div(total, (size_t)256);
     if (blocks > num_sms() * 16) blocks = num_sms() * 16;
-    gather_rows_kernel<<<blocks, 256, 0, stream>>>(nrows, ncols, A, ldA, perm, tmp);
+    gather_rows_kernel<double><<<blocks, 256, 0, stream>>>(nrows, ncols, A, ldA, perm, tmp);
     FG_CUDA(cudaGetLastError());
-    copy_back_kernel<<<blocks, 256, 0, stream>>>(nrows, ncols, tmp, A, ldA);
+    copy_back_kernel<double><<<blocks, 256, 0, stream>>>(nrows, ncols, tmp, A, ldA);
     FG_CUDA(cudaGetLastError());
     return kOk;
 }

@@ -82,6 +82,8 @@ struct Registry {
         for (auto &kv : map) {
             Workspace *w = kv.second;
             if (w->buf) cudaFree(w->buf);
+            for (int i = 0; i < 4; ++i)
+                if (w->slot_buf[i]) cudaFree(w->slot_buf[i]);
             if (w->status) cudaFree(w->status);
             delete w;
         }
@@ -137,6 +139,33 @@ Workspace *workspace_for(cudaStream_t stream, size_t bytes) {
         w->bytes = want;
     }
     return w;
+}
+
+void *workspace_slot(cudaStream_t stream, int slot, size_t bytes) {
+    if (slot < 1 || slot > 3) {
+        set_last_error("workspace slot %d out of range", slot);
+        return nullptr;
+    }
+    Workspace *w = workspace_for(stream, 0);
+    if (!w) return nullptr;
+    Registry &r = registry();
+    std::lock_guard<std::mutex> lock(r.mu);
+    if (w->slot_bytes[slot] < bytes) {
+        if (w->slot_buf[slot]) {
+            cudaStreamSynchronize(stream);
+            cudaFree(w->slot_buf[slot]);
+            w->slot_buf[slot] = nullptr;
+            w->slot_bytes[slot] = 0;
+        }
+        const size_t want = bytes < 256 ? 256 : bytes;
+        if (cudaMalloc(&w->slot_buf[slot], want) != cudaSuccess) {
+            cudaGetLastError();
+            set_last_error("cudaMalloc of %zu bytes (workspace slot %d) failed", want, slot);
+            return nullptr;
+        }
+        w->slot_bytes[slot] = want;
+    }
+    return w->slot_buf[slot];
 }
 
 int check_device_status(cudaStream_t stream) {

@@ -32,7 +32,11 @@
 
 namespace fg {
 
-enum TcKind : int { kTcTF32 = 0, kTcBF16 = 1, kTcFP8 = 2 };
+// Precisions of the tensor-core contraction.  kTcF32x3 is FP32-accurate: each
+// operand is split into a TF32 head and a TF32 tail and three TF32 products
+// (head*head + head*tail + tail*head) are accumulated.  kTcTF32Lo is only a
+// conversion mode (the tail of the split).
+enum TcKind : int { kTcTF32 = 0, kTcBF16 = 1, kTcFP8 = 2, kTcF32x3 = 3, kTcTF32Lo = 4 };
 
 namespace {
 
@@ -302,6 +306,14 @@ __device__ __forceinline__ void store_lp<kTcTF32>(void *out, size_t idx, float v
     ((uint32_t *)out)[idx] = t;
 }
 template <>
+__device__ __forceinline__ void store_lp<kTcTF32Lo>(void *out, size_t idx, float v) {
+    uint32_t h, t;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+    const float lo = v - __uint_as_float(h);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(lo));
+    ((uint32_t *)out)[idx] = t;
+}
+template <>
 __device__ __forceinline__ void store_lp<kTcFP8>(void *out, size_t idx, float v) {
     ((__nv_fp8_storage_t *)out)[idx] = __nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
 }
@@ -413,12 +425,18 @@ int make_map(CUtensorMap *map, int kind, const void *base, int rows, int K, int 
 }  // namespace
 
 // K-major leading dimension (elements) for `kind`: K rounded up to 16 bytes.
+static int gemm_kind(int kind) { return (kind == kTcF32x3 || kind == kTcTF32Lo) ? kTcTF32 : kind; }
+
 int tc_kmajor_ld(int kind, int K) {
+    kind = gemm_kind(kind);
     const int per16 = kind == kTcTF32 ? 4 : kind == kTcBF16 ? 8 : 16;
     return (K + per16 - 1) / per16 * per16;
 }
 
-size_t tc_elem_bytes(int kind) { return kind == kTcTF32 ? 4 : kind == kTcBF16 ? 2 : 1; }
+size_t tc_elem_bytes(int kind) {
+    kind = gemm_kind(kind);
+    return kind == kTcTF32 ? 4 : kind == kTcBF16 ? 2 : 1;
+}
 
 // Convert op(X) (R x K, FP32, column-major storage, transposed or not) to a
 // K-major low-precision operand.  For FP8, also computes per-row scales.
@@ -442,6 +460,7 @@ int tc_convert(int kind, bool trans, int R, int K, const float *X, int ldx, void
         else to_kmajor_kernel<KD, false><<<grid, 256, 0, stream>>>(R, K, X, ldx, out, ldo, inv);        \
     } while (0)
     if (kind == kTcTF32) FG_CONV(kTcTF32);
+    else if (kind == kTcTF32Lo) FG_CONV(kTcTF32Lo);
     else if (kind == kTcBF16) FG_CONV(kTcBF16);
     else FG_CONV(kTcFP8);
 #undef FG_CONV
@@ -488,17 +507,63 @@ int tc_gemm_launch(int kind, int M, int N, int K, float alpha, const void *A_lp,
     return kOk;
 }
 
+static size_t round256(size_t b) { return (b + 255) / 256 * 256; }
+
+size_t tc_update_workspace_bytes(int kind, int m, int n, int k) {
+    const int ld = tc_kmajor_ld(kind, k);
+    const size_t eb = tc_elem_bytes(kind);
+    const size_t a = round256((size_t)m * ld * eb), b = round256((size_t)n * ld * eb);
+    size_t total = a + b;
+    if (kind == kTcF32x3) total *= 2;
+    if (kind == kTcFP8) total += round256((size_t)(m + n) * 2 * sizeof(float));
+    return total;
+}
+
+int tc_trailing_update(int kind, int m, int n, int k, const float *A21, int ldA21,
+                       const float *U12, int ldU12, float *A22, int ldA22, void *buf,
+                       cudaStream_t stream) {
+    if (m <= 0 || n <= 0 || k <= 0) return kOk;
+    const int ld = tc_kmajor_ld(kind, k);
+    const size_t eb = tc_elem_bytes(kind);
+    const size_t a = round256((size_t)m * ld * eb), b = round256((size_t)n * ld * eb);
+    char *p = (char *)buf;
+    void *Ahi = p, *Bhi = p + a;
+    int st;
+    if (kind == kTcF32x3) {
+        void *Alo = p + a + b, *Blo = p + 2 * a + b;
+        if ((st = tc_convert(kTcTF32, false, m, k, A21, ldA21, Ahi, ld, nullptr, nullptr, stream))) return st;
+        if ((st = tc_convert(kTcTF32Lo, false, m, k, A21, ldA21, Alo, ld, nullptr, nullptr, stream))) return st;
+        if ((st = tc_convert(kTcTF32, true, n, k, U12, ldU12, Bhi, ld, nullptr, nullptr, stream))) return st;
+        if ((st = tc_convert(kTcTF32Lo, true, n, k, U12, ldU12, Blo, ld, nullptr, nullptr, stream))) return st;
+        // small terms first, then the head product
+        if ((st = tc_gemm_launch(kTcTF32, m, n, k, -1.0f, Alo, ld, Bhi, ld, 1.0f, A22, ldA22, nullptr, nullptr, stream))) return st;
+        if ((st = tc_gemm_launch(kTcTF32, m, n, k, -1.0f, Ahi, ld, Blo, ld, 1.0f, A22, ldA22, nullptr, nullptr, stream))) return st;
+        return tc_gemm_launch(kTcTF32, m, n, k, -1.0f, Ahi, ld, Bhi, ld, 1.0f, A22, ldA22, nullptr, nullptr, stream);
+    }
+    float *sa = nullptr, *sia = nullptr, *sb = nullptr, *sib = nullptr;
+    if (kind == kTcFP8) {
+        sa = (float *)(p + a + b);
+        sia = sa + m;
+        sb = sia + m;
+        sib = sb + n;
+    }
+    if ((st = tc_convert(kind, false, m, k, A21, ldA21, Ahi, ld, sa, sia, stream))) return st;
+    if ((st = tc_convert(kind, true, n, k, U12, ldU12, Bhi, ld, sb, sib, stream))) return st;
+    return tc_gemm_launch(kind, m, n, k, -1.0f, Ahi, ld, Bhi, ld, 1.0f, A22, ldA22, sa, sb, stream);
+}
+
 }  // namespace fg
 
 // ----------------------------------------------------------------- C ABI ----
 // C = alpha*op(A)*op(B) + beta*C with FP32 operands in device memory, the
 // products taken on the tensor cores in `precision` (0 = TF32, 1 = BF16,
-// 2 = FP8 e4m3 with per-row/per-column scaling) and accumulated in FP32.
+// 2 = FP8 e4m3 with per-row/per-column scaling, 3 = FP32-accurate 3xTF32) and
+// accumulated in FP32.
 FG_API int flens_gb300_sgemm_tc(int precision, char transA, char transB, int m, int n, int k,
                                 float alpha, const float *A, int ldA, const float *B, int ldB,
                                 float beta, float *C, int ldC, void *stream) {
     using namespace fg;
-    if (precision < 0 || precision > 2) return -1;
+    if (precision < 0 || precision > 3) return -1;
     const bool ta = !(transA == 'N' || transA == 'n');
     const bool tb = !(transB == 'N' || transB == 'n');
     if (!(transA == 'N' || transA == 'n' || transA == 'T' || transA == 't' || transA == 'C' || transA == 'c')) return -2;
@@ -520,22 +585,36 @@ FG_API int flens_gb300_sgemm_tc(int precision, char transA, char transB, int m, 
         FG_CUDA(cudaGetLastError());
         return kOk;
     }
+    // op(A) (m x k) and op(B) (k x n) as the trailing-update shapes: A with
+    // rows contiguous when not transposed, op(B)^T rows contiguous when B is.
+    const size_t need = tc_update_workspace_bytes(precision, m, n, k);
+    Workspace *w = workspace_for(s, need);
+    if (!w) return kErrAlloc;
     const int ld = tc_kmajor_ld(precision, k);
     const size_t eb = tc_elem_bytes(precision);
-    const size_t aBytes = ((size_t)m * ld * eb + 255) / 256 * 256;
-    const size_t bBytes = ((size_t)n * ld * eb + 255) / 256 * 256;
-    const size_t sBytes = ((size_t)(m + n) * 2 * sizeof(float) + 255) / 256 * 256;
-    Workspace *w = workspace_for(s, aBytes + bBytes + sBytes);
-    if (!w) return kErrAlloc;
+    const size_t a = round256((size_t)m * ld * eb), b = round256((size_t)n * ld * eb);
     char *p = (char *)w->buf;
-    void *Alp = p, *Blp = p + aBytes;
-    float *sa = (float *)(p + aBytes + bBytes), *sia = sa + m, *sb = sia + m, *sib = sb + n;
-    // op(A)(i, p): row i contiguous when A is not transposed
-    int st = tc_convert(precision, ta, m, k, A, ldA, Alp, ld, sa, sia, s);
-    if (st != kOk) return st;
+    int st;
+    if (precision == kTcF32x3) {
+        void *Ahi = p, *Bhi = p + a, *Alo = p + a + b, *Blo = p + 2 * a + b;
+        if ((st = tc_convert(kTcTF32, ta, m, k, A, ldA, Ahi, ld, nullptr, nullptr, s))) return st;
+        if ((st = tc_convert(kTcTF32Lo, ta, m, k, A, ldA, Alo, ld, nullptr, nullptr, s))) return st;
+        if ((st = tc_convert(kTcTF32, !tb, n, k, B, ldB, Bhi, ld, nullptr, nullptr, s))) return st;
+        if ((st = tc_convert(kTcTF32Lo, !tb, n, k, B, ldB, Blo, ld, nullptr, nullptr, s))) return st;
+        if ((st = tc_gemm_launch(kTcTF32, m, n, k, alpha, Alo, ld, Bhi, ld, beta, C, ldC, nullptr, nullptr, s))) return st;
+        if ((st = tc_gemm_launch(kTcTF32, m, n, k, alpha, Ahi, ld, Blo, ld, 1.0f, C, ldC, nullptr, nullptr, s))) return st;
+        return tc_gemm_launch(kTcTF32, m, n, k, alpha, Ahi, ld, Bhi, ld, 1.0f, C, ldC, nullptr, nullptr, s);
+    }
+    void *Alp = p, *Blp = p + a;
+    float *sa = nullptr, *sia = nullptr, *sb = nullptr, *sib = nullptr;
+    if (precision == kTcFP8) {
+        sa = (float *)(p + a + b);
+        sia = sa + m;
+        sb = sia + m;
+        sib = sb + n;
+    }
+    if ((st = tc_convert(precision, ta, m, k, A, ldA, Alp, ld, sa, sia, s))) return st;
     // B^T(j, p) = op(B)(p, j): for op(B) = B (K x N col-major) row j of B^T is contiguous in p
-    st = tc_convert(precision, !tb, n, k, B, ldB, Blp, ld, sb, sib, s);
-    if (st != kOk) return st;
-    return tc_gemm_launch(precision, m, n, k, alpha, Alp, ld, Blp, ld, beta, C, ldC,
-                          precision == kTcFP8 ? sa : nullptr, precision == kTcFP8 ? sb : nullptr, s);
+    if ((st = tc_convert(precision, !tb, n, k, B, ldB, Blp, ld, sb, sib, s))) return st;
+    return tc_gemm_launch(precision, m, n, k, alpha, Alp, ld, Blp, ld, beta, C, ldC, sa, sb, s);
 }

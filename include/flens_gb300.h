@@ -103,6 +103,36 @@ int flens_gb300_dgetrs(char trans, int n, int nrhs, const double *A, int ldA,
 int flens_gb300_dgesv(int n, int nrhs, double *A, int ldA, int *ipiv, double *B,
                       int ldB, int *info, void *stream);
 
+/* ------------------------------------------- precision form (extension) --- */
+
+/* C <- alpha*op(A)*op(B) + beta*C, FP32 operands in device memory, products
+ * on the tcgen05 tensor cores in `precision` (0 = TF32, 1 = BF16, 2 = FP8
+ * e4m3 with per-row / per-column scaling, 3 = FP32-accurate 3xTF32) with FP32
+ * accumulation.  Beta scales C by a multiply, as cxxblas gescal does.  No
+ * reference counterpart: FLENS's float gemm is the generic loop
+ * (cxxblas/level3/gemm.tcc:42-190).  Async on stream. */
+int flens_gb300_sgemm_tc(int precision, char transA, char transB, int m, int n,
+                         int k, float alpha, const float *A, int ldA,
+                         const float *B, int ldB, float beta, float *C, int ldC,
+                         void *stream);
+
+/* Solve A X = B (device, column-major FP64; A and B untouched) to FP64
+ * accuracy from an LU in FP32 storage whose trailing updates run on the
+ * tensor cores in `precision` (as above), refined in FP64: solver 0 =
+ * classical refinement (stops like the reference's rfs,
+ * flens/lapack/ge/rfs.tcc:182-188), 1 = GMRES-IR, 2 = classical switching to
+ * GMRES-IR per column when the backward error stops halving.  Stops when the
+ * normwise backward error ||b-Ax||inf/(||A||inf||x||inf+||b||inf) <= tol
+ * (tol <= 0: n*eps64) or after max_iter steps (<= 0: 30).  Outputs: refinement
+ * steps (classical steps + GMRES iterations), final backward error, INFO of
+ * the factorisation (>0: exactly singular pivot, no solve).  Returns
+ * FLENS_GB300_ERR_NOT_CONVERGED if the tolerance was not reached (X holds the
+ * last iterate).  Synchronises on stream. */
+int flens_gb300_dgesv_mixed(int n, int nrhs, const double *A, int ldA,
+                            const double *B, int ldB, double *X, int ldX,
+                            int precision, int solver, int max_iter, double tol,
+                            int *iters, double *berr, int *info, void *stream);
+
 /* dgetrs on device memory for callers that must not allocate device memory
  * once running (a fixed, pre-reserved memory budget, a memory pool owned by
  * another framework, or a process that forbids cudaMalloc after start-up).

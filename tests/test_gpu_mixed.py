@@ -1,0 +1,125 @@
+"""Precision form: low-precision LU on the tensor cores + FP64 refinement
+(flens_gb300_dgesv_mixed) must reach FP64-level accuracy.
+
+Systems follow the mixed-solve configuration: A = U diag(s) V^T, U and V the Q
+factors of Householder QR of seeded Gaussian matrices, s geometric from 1 to
+1/kappa, b = A x_true.  Bars (written in the asserts): the reported and the
+independently recomputed normwise backward error
+||b - Ax||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= 10 n eps64, and the
+forward error against x_true <= kappa * 1e3 * eps64 (the error a backward
+stable FP64 solve can have).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import flens_gb300 as fg
+
+pytestmark = pytest.mark.gpu
+
+EPS = np.finfo(np.float64).eps
+PREC = {"tf32": 0, "bf16": 1, "fp8": 2, "fp32": 3}
+SOLVER = {"classical": 0, "gmres": 1, "auto": 2}
+
+
+def make_system(cuda, n, kappa, nrhs, seed):
+    import torch
+    g = torch.Generator(device=cuda)
+    g.manual_seed(seed)
+    U, _ = torch.linalg.qr(torch.randn((n, n), generator=g, dtype=torch.float64, device=cuda))
+    V, _ = torch.linalg.qr(torch.randn((n, n), generator=g, dtype=torch.float64, device=cuda))
+    s = kappa ** (-torch.arange(n, dtype=torch.float64, device=cuda) / (n - 1))
+    A = fg.to_colmajor((U * s) @ V.t())
+    x = torch.rand((n, nrhs), generator=g, dtype=torch.float64, device=cuda).mul_(2).sub_(1)
+    b = fg.to_colmajor(A @ x)
+    return A, b, x
+
+
+def dgesv_mixed(A, b, prec, solver, max_iter=30, tol=0.0):
+    import torch
+    n, nrhs = b.shape
+    X = fg.colmajor_empty(n, nrhs, device=A.device)
+    f = fg.lib().flens_gb300_dgesv_mixed
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
+                  ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    it, be, inf = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
+    st = f(n, nrhs, A.data_ptr(), A.stride(1), b.data_ptr(), b.stride(1), X.data_ptr(), X.stride(1),
+           PREC[prec], SOLVER[solver], max_iter, tol, ctypes.byref(it), ctypes.byref(be),
+           ctypes.byref(inf), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    return st, X, it.value, be.value, inf.value
+
+
+def backward_error(A, X, b):
+    r = b - A @ X
+    anorm = A.abs().sum(1).max()
+    return (r.abs().amax(0) / (anorm * X.abs().amax(0) + b.abs().amax(0))).max().item()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "tf32", "bf16", "fp8"])
+@pytest.mark.parametrize("nrhs", [1, 3])
+def test_mixed_well_conditioned(cuda, prec, nrhs):
+    n, kappa = 512, 1e2
+    A, b, x = make_system(cuda, n, kappa, nrhs, 11)
+    st, X, it, be, inf = dgesv_mixed(A, b, prec, "auto")
+    assert st == 0 and inf == 0, (st, fg.last_error())
+    assert be <= 10 * n * EPS
+    assert backward_error(A, X, b) <= 10 * n * EPS
+    fwd = ((X - x).abs().max() / x.abs().max()).item()
+    assert fwd <= kappa * 1e3 * EPS, fwd
+
+
+@pytest.mark.parametrize("prec,solver", [("fp32", "classical"), ("bf16", "auto"),
+                                         ("tf32", "auto"), ("fp8", "auto")])
+def test_mixed_kappa_1e6(cuda, prec, solver):
+    n, kappa = 1024, 1e6
+    A, b, x = make_system(cuda, n, kappa, 2, 12)
+    st, X, it, be, inf = dgesv_mixed(A, b, prec, solver, max_iter=40)
+    assert st == 0, (st, fg.last_error(), it, be)
+    assert backward_error(A, X, b) <= 10 * n * EPS
+    fwd = ((X - x).abs().max() / x.abs().max()).item()
+    assert fwd <= kappa * 1e3 * EPS, fwd
+
+
+def test_mixed_gmres_kappa_1e10(cuda):
+    n, kappa = 1024, 1e10
+    A, b, x = make_system(cuda, n, kappa, 1, 13)
+    st, X, it, be, inf = dgesv_mixed(A, b, "fp32", "gmres", max_iter=10)
+    assert st == 0, (st, fg.last_error(), it, be)
+    assert backward_error(A, X, b) <= 10 * n * EPS
+    fwd = ((X - x).abs().max() / x.abs().max()).item()
+    assert fwd <= kappa * 1e3 * EPS, fwd
+
+
+def test_mixed_classical_reports_non_convergence(cuda):
+    # bf16 factors of a kappa=1e10 matrix: classical refinement cannot converge
+    # and must say so instead of returning a wrong "success"
+    n = 512
+    A, b, x = make_system(cuda, n, 1e10, 1, 14)
+    st, X, it, be, inf = dgesv_mixed(A, b, "bf16", "classical", max_iter=10)
+    assert st == fg.ERR_NOT_CONVERGED
+    assert be > 10 * n * EPS
+
+
+def test_mixed_singular_info(cuda):
+    import torch
+    n = 256
+    A, b, x = make_system(cuda, n, 10.0, 1, 15)
+    A[:, 7] = 0.0
+    st, X, it, be, inf = dgesv_mixed(A, b, "bf16", "auto")
+    assert st == 0 and inf == 8
+
+
+def test_mixed_argument_errors(cuda):
+    f = fg.lib().flens_gb300_dgesv_mixed
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                  ctypes.c_void_p, ctypes.c_void_p]
+    assert f(-1, 1, None, 1, None, 1, None, 1, 0, 0, 5, 0.0, None, None, None, None) == -1
+    assert f(4, 1, None, 3, None, 4, None, 4, 0, 0, 5, 0.0, None, None, None, None) == -4
+    assert f(4, 1, None, 4, None, 4, None, 4, 7, 0, 5, 0.0, None, None, None, None) == -9
