@@ -47,7 +47,8 @@ def dgesv_mixed(A, b, prec, solver, max_iter=30, tol=0.0):
                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
     f.restype = ctypes.c_int
     it, be, inf = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
-    st = f(n, nrhs, A.data_ptr(), A.stride(1), b.data_ptr(), b.stride(1), X.data_ptr(), X.stride(1),
+    ld = lambda t: max(t.stride(1), t.shape[0], 1)     # one-column tensors report stride 1
+    st = f(n, nrhs, A.data_ptr(), ld(A), b.data_ptr(), ld(b), X.data_ptr(), ld(X),
            PREC[prec], SOLVER[solver], max_iter, tol, ctypes.byref(it), ctypes.byref(be),
            ctypes.byref(inf), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     torch.cuda.synchronize()
