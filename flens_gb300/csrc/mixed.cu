@@ -13,8 +13,8 @@
 //      GMRES-IR:  d from left-preconditioned GMRES on (LU)^-1 A d = (LU)^-1 r
 //                 (Carson & Higham, SIAM J. Sci. Comput. 40(2), 2018): FP64
 //                 Arnoldi, classical Gram-Schmidt applied twice, the
-//                 preconditioner applied as the FP32 LU solve, Givens
-//                 rotations on the host; x += d.
+//                 preconditioner applied as FP64 triangular solves with the
+//                 (FP32) factors, Givens rotations on the host; x += d.
 //      Classical refinement stops like the reference's rfs
 //      (flens/lapack/ge/rfs.tcc:182-188): on reaching the tolerance, when the
 //      backward error stops halving, or after max_iter steps.  In the auto
@@ -152,6 +152,22 @@ __global__ void scale_into_kernel(int n, const double *__restrict__ a, const dou
 
 __global__ void sqrt_kernel(double *v) { *v = sqrt(*v); }
 
+// dst[i] = src[perm[i]]
+__global__ void gather_perm_kernel(int n, const double *__restrict__ src, const int *__restrict__ perm,
+                                   double *__restrict__ dst) {
+    for (int r = blockIdx.x * 256 + threadIdx.x; r < n; r += gridDim.x * 256) dst[r] = src[perm[r]];
+}
+
+__global__ void s2d_matrix_kernel(int n, const float *__restrict__ S, int lds, double *__restrict__ D,
+                                  int ldd) {
+    const size_t total = (size_t)n * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const size_t j = e / n, i = e % n;
+        D[i + j * ldd] = (double)S[i + j * lds];
+    }
+}
+
 int grid_for(size_t total) {
     int b = (int)ceil_div(total, (size_t)256);
     const int cap = num_sms() * 8;
@@ -183,6 +199,8 @@ struct Solver {
     unsigned long long *anorm_bits = nullptr;
     double *V = nullptr;        // n x (M+1) Krylov basis (GMRES)
     double *w = nullptr;        // n
+    double *t = nullptr;        // n
+    double *LU64 = nullptr;     // FP64 copy of the FP32 factors (GMRES preconditioner)
     double *h = nullptr;        // M+2 coefficients
     double *h2 = nullptr;       // M+2 (second Gram-Schmidt pass)
     double anorm = 0.0;
@@ -209,6 +227,19 @@ int lu_solve(Solver &S, int ncols, const double *X, int ldx, const double *scale
                                                                                 S.n, scale, out, ldo);
     FG_CUDA(cudaGetLastError());
     return kOk;
+}
+
+// dst = (L^ U^)^-1 P src with the FP32 factors applied in FP64 arithmetic:
+// GMRES-IR needs the preconditioned operator (LU)^-1 A in the residual
+// precision (Carson & Higham 2018, the u_r-precision matvec), an FP32 solve
+// makes it inconsistent at the kappa*u32 level and Arnoldi stalls.
+int precond64(Solver &S, const double *src, double *dst) {
+    KTimer kt(kFamRefine, S.s, 2.0 * S.n * (double)S.n, 8.0 * S.n * (double)S.n);
+    gather_perm_kernel<<<grid_for(S.n), 256, 0, S.s>>>(S.n, src, S.perm, dst);
+    FG_CUDA(cudaGetLastError());
+    int st = dtrsm_launch('L', 'L', 'N', 'U', S.n, 1, 1.0, S.LU64, S.n, dst, S.n, S.s);
+    if (st != kOk) return st;
+    return dtrsm_launch('L', 'U', 'N', 'N', S.n, 1, 1.0, S.LU64, S.n, dst, S.n, S.s);
 }
 
 // R = B - A X for columns [j0, j0+nc); berr[j] for those columns (host)
@@ -247,8 +278,7 @@ int gmres_cycle(Solver &S, int j, double rtol, int *steps) {
     double *sc = S.colv + 3 * S.nrhs;     // device scalars: [scale, norm]
     *steps = 0;
     // z = (LU)^-1 r  -> V(:, 0) unnormalised
-    col_absmax_kernel<<<1, 256, 0, S.s>>>(n, r, n, sc);
-    int st = lu_solve(S, 1, r, n, sc, S.V, n, false);
+    int st = precond64(S, r, S.V);
     if (st != kOk) return st;
     auto norm2_into = [&](const double *v, double *dst) -> int {
         FG_CUDA(cudaMemsetAsync(dst, 0, sizeof(double), S.s));
@@ -271,12 +301,11 @@ int gmres_cycle(Solver &S, int j, double rtol, int *steps) {
     int k = 0;
     for (; k < M; ++k) {
         double *vk = S.V + (size_t)k * n;
-        // w = (LU)^-1 A v_k
-        FG_CUDA(cudaMemsetAsync(S.w, 0, sizeof(double) * n, S.s));
-        if ((st = dgemm_launch('N', 'N', n, 1, n, 1.0, S.A, S.ldA, vk, n, 0.0, S.w, n, S.s)) != kOk)
+        // w = (LU)^-1 A v_k, all in FP64
+        FG_CUDA(cudaMemsetAsync(S.t, 0, sizeof(double) * n, S.s));
+        if ((st = dgemm_launch('N', 'N', n, 1, n, 1.0, S.A, S.ldA, vk, n, 0.0, S.t, n, S.s)) != kOk)
             return st;
-        col_absmax_kernel<<<1, 256, 0, S.s>>>(n, S.w, n, sc);
-        if ((st = lu_solve(S, 1, S.w, n, sc, S.w, n, false)) != kOk) return st;
+        if ((st = precond64(S, S.t, S.w)) != kOk) return st;
         // classical Gram-Schmidt, twice
         dim3 gd(std::max(1, std::min(ceil_div(n, 256 * 8), num_sms() * 2)), k + 1);
         FG_CUDA(cudaMemsetAsync(S.h, 0, sizeof(double) * (k + 1), S.s));
@@ -456,11 +485,18 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
         }
         if (!gmres.empty()) {
             if (!S.V) {
-                char *p2 = (char *)workspace_slot(s, 2, a256((size_t)n * (M + 1) * sizeof(double)) +
-                                                            a256((size_t)n * sizeof(double)));
+                const size_t vB = a256((size_t)n * (M + 1) * sizeof(double));
+                const size_t nB = a256((size_t)n * sizeof(double));
+                char *p2 = (char *)workspace_slot(s, 2, vB + 2 * nB);
                 if (!p2) return kErrAlloc;
                 S.V = (double *)p2;
-                S.w = (double *)(p2 + a256((size_t)n * (M + 1) * sizeof(double)));
+                S.w = (double *)(p2 + vB);
+                S.t = (double *)(p2 + vB + nB);
+                S.LU64 = (double *)workspace_slot(s, 3, (size_t)n * n * sizeof(double));
+                if (!S.LU64) return kErrAlloc;
+                KTimer kt(kFamAux, s, 0.0, 12.0 * n * (double)n);
+                s2d_matrix_kernel<<<grid_for((size_t)n * n), 256, 0, s>>>(n, S.A32, S.ld32, S.LU64, n);
+                FG_CUDA(cudaGetLastError());
             }
             for (int j : gmres) {
                 int steps = 0;
