@@ -176,7 +176,7 @@ int grid_for(size_t total) {
 
 size_t a256(size_t b) { return (b + 255) / 256 * 256; }
 
-constexpr int kGmresM = 50;       // restart length
+constexpr int kGmresM = 100;      // restart length
 
 struct Solver {
     int n = 0, nrhs = 0;
@@ -456,7 +456,9 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
                 done[j] = 1;
                 continue;
             }
-            if (step > 0 && !(berr[j] <= 0.5 * prev[j])) {
+            // classical steps must halve the backward error (rfs.tcc:182); a
+            // GMRES-IR cycle must improve it by at least 10%
+            if (step > 0 && !(berr[j] <= (use_gmres[j] ? 0.9 : 0.5) * prev[j])) {
                 if (!use_gmres[j] && solver == 2) {
                     use_gmres[j] = 1;
                 } else {
