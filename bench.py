@@ -311,6 +311,8 @@ def our_arm(args, rank: int, world: int) -> None:
                 "algorithmic": "2*m*n*k flops per trailing-update/trsm GEMM launch"}
         if not args.quick:
             result["gemm_fp64_config1"] = gemm_subbench(torch, fg, dev)
+        if not args.quick and not args.no_mixed:
+            result["mixed_config3"] = mixed_subbench(torch, fg, dev, n=args.mixed_n)
         # -- e2e through the Fortran ABI with pinned host buffers
         if not args.no_e2e:
             result["e2e"] = e2e_dgesv(torch, fg, A0, b0, args)
@@ -320,6 +322,91 @@ def our_arm(args, rank: int, world: int) -> None:
         print(json.dumps(result), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def mixed_subbench(torch, fg, dev, n=16384, reps=3):
+    """Mixed-solve configuration: A = U diag(s) V^T (U, V from Householder QR of
+    seeded Gaussian matrices, s geometric 1 -> 1/kappa), b = A x_true, one rhs.
+    Times flens_gb300_dgesv_mixed (LU in FP32 storage with tcgen05 trailing
+    updates + FP64 refinement) against the plain FP64 dgetrf+dgetrs on the same
+    matrix, and reports iterations, backward error and forward error."""
+    import ctypes
+    import numpy as np
+    eps = float(np.finfo(np.float64).eps)
+    g = torch.Generator(device=dev)
+    g.manual_seed(2026)
+    t0 = time.time()
+    U, _ = torch.linalg.qr(torch.randn((n, n), generator=g, dtype=torch.float64, device=dev))
+    V, _ = torch.linalg.qr(torch.randn((n, n), generator=g, dtype=torch.float64, device=dev))
+    gen_s = time.time() - t0
+    f = fg.lib().flens_gb300_dgesv_mixed
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
+                  ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    out = {"workload": f"dgesv_mixed n={n} 1 rhs, A=U diag(s) V^T", "n": n,
+           "generation_s": round(gen_s, 1), "cases": []}
+    plain_ms = None
+    for kappa in (1e2, 1e6):
+        s = kappa ** (-torch.arange(n, dtype=torch.float64, device=dev) / (n - 1))
+        A = fg.to_colmajor((U * s) @ V.t())
+        x = torch.rand((n, 1), generator=g, dtype=torch.float64, device=dev).mul_(2).sub_(1)
+        b = fg.to_colmajor(A @ x)
+        X = fg.colmajor_empty(n, 1, device=dev)
+        anorm = A.abs().sum(1).max()
+        if plain_ms is None:
+            # plain FP64 GPU solve on the same n (one timed run after one warm-up)
+            W = fg.to_colmajor(A.clone())
+            bb = b.clone()
+            ipiv = torch.zeros(n, dtype=torch.int32, device=dev)
+            inf = torch.zeros(1, dtype=torch.int32, device=dev)
+            for rep in range(2):
+                W.copy_(A)
+                bb.copy_(b)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fg.dgetrf_dev(W, ipiv, inf, stream)
+                fg.dgetrs_dev("N", W, ipiv, bb, stream)
+                e1.record(stream)
+                e1.synchronize()
+                plain_ms = e0.elapsed_time(e1)
+            r = b - A @ bb
+            plain_berr = (r.abs().max() / (anorm * bb.abs().max() + b.abs().max())).item()
+            out["plain_fp64"] = {"ms": plain_ms, "backward_error": plain_berr,
+                                 "backward_error_over_n_eps": plain_berr / (n * eps)}
+            del W, bb
+        for prec_name, prec in (("fp32(3xTF32)", 3), ("tf32", 0), ("bf16", 1)):
+            if kappa > 1e3 and prec != 3:
+                continue       # classical IR needs kappa*u_factor < 1
+            it, be, inf_ = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
+            times = []
+            st = 0
+            for rep in range(1 + reps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                st = f(n, 1, A.data_ptr(), n, b.data_ptr(), n, X.data_ptr(), n, prec, 2, 30, 0.0,
+                       ctypes.byref(it), ctypes.byref(be), ctypes.byref(inf_), sp)
+                torch.cuda.synchronize()
+                if rep > 0:
+                    times.append(1000.0 * (time.perf_counter() - t0))
+            ms = sum(times) / len(times)
+            r = b - A @ X
+            berr = (r.abs().max() / (anorm * X.abs().max() + b.abs().max())).item()
+            fwd = ((X - x).abs().max() / x.abs().max()).item()
+            out["cases"].append({"kappa": kappa, "factor_precision": prec_name, "status": st,
+                                 "ms": ms, "iterations": it.value, "backward_error": berr,
+                                 "backward_error_over_n_eps": berr / (n * eps),
+                                 "forward_error": fwd,
+                                 "time_ratio_vs_plain_fp64": ms / plain_ms,
+                                 "meets_10_n_eps": berr <= 10 * n * eps})
+        del A, b, X
+    del U, V
+    torch.cuda.empty_cache()
+    return out
 
 
 def e2e_dgesv(torch, fg, A0, b0, args):
@@ -379,6 +466,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip peak and sub-benchmarks")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--mixed-n", type=int, default=16384)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
