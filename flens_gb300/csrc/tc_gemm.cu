@@ -8,17 +8,19 @@
 // cxxblas/level3/gemm.tcc:42-190); this is the contraction its FP32 `mm`
 // would perform, carried out on the 5th-generation tensor cores.
 //
-// Kernel shape: one 128 x BN output tile per CTA (BN = 256), 128 threads.
+// Kernel shape: persistent, one CTA per SM over 128 x BN output tiles
+// (BN = 256), 320 threads:
 //   warp 0 lane 0  TMA producer: 128B-swizzled K-major tiles of A (128 rows)
 //                  and B (BN rows) into a STAGES-deep shared-memory ring,
 //                  one mbarrier (expect_tx) per stage;
-//   warp 1         allocates BN TMEM columns; lane 0 issues tcgen05.mma
-//                  (M=128, N=BN, K=32 bytes per instruction) and commits each
-//                  stage back to the producer, then the whole tile to the
-//                  epilogue;
-//   warps 0-3      epilogue: tcgen05.ld 32x32b.x32 chunks of their 32 TMEM
-//                  lanes (= tile rows), C = alpha*acc*(sa_i*sb_j) + beta*C,
-//                  coalesced column-major stores.
+//   warp 1         allocates 2*BN TMEM columns (two accumulators); lane 0
+//                  issues tcgen05.mma (M=128, N=BN, K=32 bytes per
+//                  instruction), commits each stage back to the producer and
+//                  each finished tile to the epilogue;
+//   warps 2-9      epilogue: tcgen05.ld 32x32b.x32 chunks of their TMEM lane
+//                  quarter (= tile rows), C = alpha*acc*(sa_i*sb_j) + beta*C,
+//                  coalesced column-major stores, then release the
+//                  accumulator to the MMA warp.
 // Every wait is bounded (kMbarSpinLimit); on a timeout the kernel sets the
 // status word, lets in-flight copies land, frees its TMEM and returns.
 #include "common.cuh"
@@ -43,7 +45,7 @@ namespace {
 constexpr int TC_BM = 128;
 constexpr int TC_BN = 256;
 constexpr int TC_STAGES = 4;
-constexpr int TC_THREADS = 128;
+constexpr int TC_THREADS = 320;                   // 10 warps: TMA, MMA, 8 epilogue
 constexpr uint32_t kMbarSpinLimit = 1u << 20;
 constexpr uint32_t TC_A_BYTES = TC_BM * 128;       // one stage of A: 128 rows x 128 B
 constexpr uint32_t TC_B_BYTES = TC_BN * 128;       // one stage of B: BN rows x 128 B
@@ -164,6 +166,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// Persistent kernel: one CTA per SM walks the output tiles
+// (tile = blockIdx.x + i*gridDim.x, m fastest), two TMEM accumulators of
+// TC_BN columns each, so the epilogue of one tile overlaps the TMA loads and
+// MMAs of the next.  Roles:
+//   warp 0 lane 0   TMA producer over (tile, k-block), STAGES-deep smem ring;
+//   warp 1          TMEM allocation; lane 0 issues the MMAs of a tile into
+//                   accumulator (tile & 1) once the epilogue has released it;
+//   warps 2..9      epilogue: warp w drains TMEM lanes 32*(w%4).. (the lane
+//                   quarter a warp may access) for column half (w-2)/4.
 template <int KIND>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
@@ -173,18 +184,21 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     constexpr int ELEM = KIND == kTcTF32 ? 4 : KIND == kTcBF16 ? 2 : 1;
     constexpr int BK = 128 / ELEM;               // elements per 128-byte row (one k-block)
     constexpr int KSTEPS = 4;                    // 32 bytes of K per MMA
+    constexpr int EPI_WARPS = 8;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem;
     uint8_t *sB = smem + TC_STAGES * TC_A_BYTES;
     uint64_t *full = (uint64_t *)(sB + TC_STAGES * TC_B_BYTES);
     uint64_t *empty = full + TC_STAGES;
-    uint64_t *accum = empty + TC_STAGES;
-    uint32_t *tmem_slot = (uint32_t *)(accum + 1);
+    uint64_t *tfull = empty + TC_STAGES;         // [2] accumulator ready
+    uint64_t *tempty = tfull + 2;                // [2] accumulator drained
+    uint32_t *tmem_slot = (uint32_t *)(tempty + 2);
     __shared__ int s_abort;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * TC_BN;
+    const int tiles_m = (M + TC_BM - 1) / TC_BM, tiles_n = (N + TC_BN - 1) / TC_BN;
+    const int ntiles = tiles_m * tiles_n;
     const int nkb = (K + BK - 1) / BK;
 
     if (threadIdx.x == 0) {
@@ -192,14 +206,17 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(accum, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], EPI_WARPS);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(tmem_slot)),
-                     "r"((uint32_t)TC_BN)
+                     "r"((uint32_t)(2 * TC_BN))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -208,81 +225,114 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    if (warp == 0 && lane == 0) {
-        // ---- TMA producer
-        int issued = 0;
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % TC_STAGES;
-            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
-            if (!mbar_wait(&empty[s], ph ^ 1u, status)) {
-                s_abort = 1;
-                break;
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---- TMA producer
+            int q = 0, issued = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                const int m0 = (t % tiles_m) * TC_BM, n0 = (t / tiles_m) * TC_BN;
+                for (int kb = 0; kb < nkb; ++kb, ++q) {
+                    const int s = q % TC_STAGES;
+                    const uint32_t ph = (uint32_t)(q / TC_STAGES) & 1u;
+                    if (s_abort || !mbar_wait(&empty[s], ph ^ 1u, status)) {
+                        s_abort = 1;
+                        ok = false;
+                        break;
+                    }
+                    mbar_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
+                    tma_load_2d(&tmA, &full[s], sA + s * TC_A_BYTES, kb * BK, m0);
+                    tma_load_2d(&tmB, &full[s], sB + s * TC_B_BYTES, kb * BK, n0);
+                    ++issued;
+                }
             }
-            mbar_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
-            tma_load_2d(&tmA, &full[s], sA + s * TC_A_BYTES, kb * BK, m0);
-            tma_load_2d(&tmB, &full[s], sB + s * TC_B_BYTES, kb * BK, n0);
-            ++issued;
+            if (!ok) {
+                // let the copies already issued land before the CTA can exit
+                for (int r = (issued > TC_STAGES ? issued - TC_STAGES : 0); r < issued; ++r)
+                    mbar_wait(&full[r % TC_STAGES], (uint32_t)(r / TC_STAGES) & 1u, status);
+            }
         }
-        if (s_abort) {
-            // let the copies already issued land before the CTA can exit
-            for (int kb = (issued > TC_STAGES ? issued - TC_STAGES : 0); kb < issued; ++kb)
-                mbar_wait(&full[kb % TC_STAGES], (uint32_t)(kb / TC_STAGES) & 1u, status);
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---- MMA issuer
+            const uint32_t idesc = idesc_for(KIND, TC_BM, TC_BN);
+            int q = 0, i = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++i) {
+                const int b = i & 1;
+                const uint32_t acc = tmem + (uint32_t)(b * TC_BN);
+                if (!mbar_wait(&tempty[b], ((uint32_t)(i >> 1) & 1u) ^ 1u, status)) {
+                    s_abort = 1;
+                    break;
+                }
+                tc_fence_after();
+                for (int kb = 0; kb < nkb; ++kb, ++q) {
+                    const int s = q % TC_STAGES;
+                    const uint32_t ph = (uint32_t)(q / TC_STAGES) & 1u;
+                    if (s_abort || !mbar_wait(&full[s], ph, status)) {
+                        s_abort = 1;
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a0 = smem_u32(sA + s * TC_A_BYTES);
+                    const uint32_t b0 = smem_u32(sB + s * TC_B_BYTES);
+#pragma unroll
+                    for (int kk = 0; kk < KSTEPS; ++kk)
+                        umma<KIND>(acc, sdesc_sw128(a0 + kk * 32), sdesc_sw128(b0 + kk * 32), idesc,
+                                   (kb | kk) != 0 ? 1u : 0u);
+                    umma_commit(&empty[s]);
+                }
+                if (ok) umma_commit(&tfull[b]);
+            }
         }
-    } else if (warp == 1 && lane == 0) {
-        // ---- MMA issuer
-        const uint32_t idesc = idesc_for(KIND, TC_BM, TC_BN);
-        bool ok = true;
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % TC_STAGES;
-            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
-            if (!mbar_wait(&full[s], ph, status)) {
+    } else {
+        // ---- epilogue
+        const int ew = warp - 2;                 // 0..7
+        const int quarter = warp & 3;            // TMEM lane quarter this warp may access
+        const int half = ew >> 2;                // column half
+        int i = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+            const int b = i & 1;
+            const int m0 = (t % tiles_m) * TC_BM, n0 = (t / tiles_m) * TC_BN;
+            const bool have = mbar_wait(&tfull[b], (uint32_t)(i >> 1) & 1u, status);
+            if (!have) {
                 s_abort = 1;
-                ok = false;
                 break;
             }
             tc_fence_after();
-            const uint32_t a0 = smem_u32(sA + s * TC_A_BYTES);
-            const uint32_t b0 = smem_u32(sB + s * TC_B_BYTES);
+            const int row = m0 + quarter * 32 + lane;
+            const float sa = (scale_a != nullptr && row < M) ? scale_a[row] : 1.0f;
+            const uint32_t base = tmem + (uint32_t)(b * TC_BN) + ((uint32_t)(quarter * 32) << 16);
+            for (int c0 = half * (TC_BN / 2); c0 < (half + 1) * (TC_BN / 2); c0 += 32) {
+                if (n0 + c0 >= N) break;         // uniform across the warp
+                uint32_t r[32];
+                tmem_ld32(base + (uint32_t)c0, r);
+                if (row < M) {
+                    float *crow = C + (size_t)row;
 #pragma unroll
-            for (int kk = 0; kk < KSTEPS; ++kk) {
-                umma<KIND>(tmem, sdesc_sw128(a0 + kk * 32), sdesc_sw128(b0 + kk * 32), idesc,
-                           (kb | kk) != 0 ? 1u : 0u);
-            }
-            umma_commit(&empty[s]);
-        }
-        if (ok) umma_commit(accum);
-    }
-    __syncwarp();
-
-    // ---- epilogue: every warp drains its 32 TMEM lanes
-    const bool have = mbar_wait(accum, 0, status);
-    tc_fence_after();
-    if (have) {
-        const int row = m0 + warp * 32 + lane;
-        const float sa = (scale_a != nullptr && row < M) ? scale_a[row] : 1.0f;
-        for (int c0 = 0; c0 < TC_BN; c0 += 32) {
-            if (n0 + c0 >= N) break;                 // uniform across the warp
-            uint32_t r[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
-            if (row < M) {
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int col = n0 + c0 + j;
-                    if (col < N) {
-                        float acc = __uint_as_float(r[j]);
-                        if (scale_b != nullptr) acc *= sa * scale_b[col];
-                        float *c = &C[(size_t)row + (size_t)col * ldc];
-                        *c = fmaf(alpha, acc, beta * *c);
+                    for (int j = 0; j < 32; ++j) {
+                        const int col = n0 + c0 + j;
+                        if (col < N) {
+                            float accv = __uint_as_float(r[j]);
+                            if (scale_b != nullptr) accv *= sa * scale_b[col];
+                            float *c = crow + (size_t)col * ldc;
+                            *c = fmaf(alpha, accv, beta * *c);
+                        }
                     }
                 }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+            if (s_abort) break;
         }
     }
     tc_fence_before();
     __syncthreads();
     if (warp == 1) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                     "r"((uint32_t)TC_BN)
+                     "r"((uint32_t)(2 * TC_BN))
                      : "memory");
     }
 }
@@ -486,7 +536,9 @@ int tc_gemm_launch(int kind, int M, int N, int K, float alpha, const void *A_lp,
     if (st != kOk) return st;
     if ((st = make_map(&mb, kind, B_lp, N, K, ldb, TC_BN)) != kOk) return st;
     static bool attr[3] = {false, false, false};
-    const dim3 grid(ceil_div(M, TC_BM), ceil_div(N, TC_BN));
+    const int ntiles = ceil_div(M, TC_BM) * ceil_div(N, TC_BN);
+    const int sms = num_sms();
+    const dim3 grid(ntiles < sms ? ntiles : sms);
     KTimer kt(kFamTcGemm, stream, 2.0 * M * (double)N * K,
               tc_elem_bytes(kind) * ((double)M * K + (double)N * K) + 8.0 * M * (double)N);
 #define FG_TC(KD)                                                                                 \
