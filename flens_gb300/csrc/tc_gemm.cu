@@ -309,15 +309,18 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 uint32_t r[32];
                 tmem_ld32(base + (uint32_t)c0, r);
                 if (row < M) {
-                    float *crow = C + (size_t)row;
+                    float *crow = C + (size_t)row + (size_t)(n0 + c0) * ldc;
+                    const int ncol = min(32, N - (n0 + c0));
+                    // all 32 loads of C in flight before any store
+                    float cv[32];
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) cv[j] = (j < ncol) ? __ldcs(crow + (size_t)j * ldc) : 0.0f;
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
-                        const int col = n0 + c0 + j;
-                        if (col < N) {
+                        if (j < ncol) {
                             float accv = __uint_as_float(r[j]);
-                            if (scale_b != nullptr) accv *= sa * scale_b[col];
-                            float *c = crow + (size_t)col * ldc;
-                            *c = fmaf(alpha, accv, beta * *c);
+                            if (scale_b != nullptr) accv *= sa * scale_b[n0 + c0 + j];
+                            __stcs(crow + (size_t)j * ldc, fmaf(alpha, accv, beta * cv[j]));
                         }
                     }
                 }
