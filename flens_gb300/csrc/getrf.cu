@@ -136,13 +136,15 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
              PanelScratch ps, int R, unsigned long long epoch) {
     extern __shared__ double S[];
     __shared__ double prow[PANEL_NB], orow[PANEL_NB];
-    __shared__ double red_v[32];
-    __shared__ int red_i[32];
-    __shared__ int s_gs;
-    __shared__ int s_abort;
+    __shared__ double red_v[2][PANEL_THREADS / 32];
+    __shared__ int red_i[2][PANEL_THREADS / 32];
+    __shared__ int s_gs, s_abort;
+    __shared__ double s_pv, s_rinv;
     __shared__ int s_list_row[2 * PANEL_NB], s_list_src[2 * PANEL_NB];
 
     const int b = blockIdx.x, G = gridDim.x, tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = PANEL_THREADS / 32;
     const int rb = b * R;
     const int re = min(mp, rb + R);
     const int nr = max(0, re - rb);
@@ -151,11 +153,15 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
         const int r = e % nr, c = e / nr;
         S[c * R + r] = A[(size_t)(rb + r) + (size_t)c * lda];
     }
+    if (tid == 0) s_abort = 0;
     __syncthreads();
 
+    // Each thread owns rows r = tid, tid+256, ... of this CTA's block for the
+    // whole panel: it computes their pivot keys, swaps, scales and updates
+    // them, so only cross-row exchanges need a barrier.
     for (int jj = 0; jj < jb; ++jj) {
         const int par = jj & 1;
-        // -- local pivot candidate among owned rows g >= jj (NaN never wins)
+        // -- [A] local pivot candidate among owned rows g >= jj (NaN never wins)
         double bv = -2.0;
         int bi = INT_MAX;
         for (int r = tid; r < nr; r += PANEL_THREADS) {
@@ -166,7 +172,21 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
                 if (better(key, g, bv, bi)) { bv = key; bi = g; }
             }
         }
-        block_argmax(bv, bi, red_v, red_i);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const double ov = __shfl_down_sync(0xffffffffu, bv, off);
+            const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+            if (better(ov, oi, bv, bi)) { bv = ov; bi = oi; }
+        }
+        if (lane == 0) { red_v[0][warp] = bv; red_i[0][warp] = bi; }
+        __syncthreads();                                             // B1
+        bv = red_v[0][0];
+        bi = red_i[0][0];
+#pragma unroll
+        for (int w = 1; w < NW; ++w)
+            if (better(red_v[0][w], red_i[0][w], bv, bi)) { bv = red_v[0][w]; bi = red_i[0][w]; }
+
+        // -- [B] publish the candidate (and row jj if owned) in this CTA's slot
         PanelSlot *mine = &ps.slots[par * PANEL_GMAX + b];
         if (bi != INT_MAX) {
             for (int c = tid; c < jb; c += PANEL_THREADS) mine->row[c] = S[c * R + (bi - rb)];
@@ -177,14 +197,15 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
         if (tid == 0) {
             mine->val = bv;
             mine->idx = bi;
-            s_abort = 0;
         }
-        __threadfence();
-        __syncthreads();
+        __syncthreads();                                             // B2
         const unsigned long long want = epoch * 128ull + (unsigned long long)jj + 1ull;
-        if (tid == 0) st_release(&mine->seq, want);
+        if (tid == 0) {
+            __threadfence();
+            st_release(&mine->seq, want);
+        }
 
-        // -- every CTA reads every slot once its seq says step jj is published
+        // -- [C] every CTA reads every slot once its seq says step jj is published
         double gv = -3.0;
         int gi = INT_MAX;
         for (int t = tid; t < G; t += PANEL_THREADS) {
@@ -202,57 +223,68 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
             const int i = ld_cg(&sl->idx);
             if (better(v, i, gv, gi)) { gv = v; gi = i; }
         }
-        block_argmax(gv, gi, red_v, red_i);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const double ov = __shfl_down_sync(0xffffffffu, gv, off);
+            const int oi = __shfl_down_sync(0xffffffffu, gi, off);
+            if (better(ov, oi, gv, gi)) { gv = ov; gi = oi; }
+        }
+        if (lane == 0) { red_v[1][warp] = gv; red_i[1][warp] = gi; }
+        __syncthreads();                                             // B3
         if (s_abort) return;
+        gv = red_v[1][0];
+        gi = red_i[1][0];
+#pragma unroll
+        for (int w = 1; w < NW; ++w)
+            if (better(red_v[1][w], red_i[1][w], gv, gi)) { gv = red_v[1][w]; gi = red_i[1][w]; }
+
+        // -- [D] fetch the old row jj and the winner's row in one round trip;
+        // thread 0 settles the pivot (iamax starts from element jj: if it is
+        // NaN nothing compares greater and jj is the pivot,
+        // cxxblas/level1/iamax.tcc:50-57) and its reciprocal once.
         const int ownjj = jj / R;
-        if (tid == 0) {
-            // iamax starts from element jj: if it is NaN nothing compares
-            // greater and jj is the pivot (cxxblas/level1/iamax.tcc:50-57).
-            const double ajj = ld_cg(&ps.slots[par * PANEL_GMAX + ownjj].rowjj[jj]);
-            s_gs = isnan(ajj) ? jj : gi;
-        }
-        __syncthreads();
-        const int gs = s_gs;
-        const int wb = gs / R;
+        const int wb = gi / R;
+        const PanelSlot *sj = &ps.slots[par * PANEL_GMAX + ownjj];
+        const PanelSlot *sw = &ps.slots[par * PANEL_GMAX + wb];
         for (int c = tid; c < jb; c += PANEL_THREADS) {
-            const double o = ld_cg(&ps.slots[par * PANEL_GMAX + ownjj].rowjj[c]);
-            orow[c] = o;
-            prow[c] = (gs == jj) ? o : ld_cg(&ps.slots[par * PANEL_GMAX + wb].row[c]);
+            orow[c] = ld_cg(&sj->rowjj[c]);
+            prow[c] = ld_cg(&sw->row[c]);
         }
-        __syncthreads();
-        const double pv = prow[jj];
-        if (b == 0 && tid == 0) {
-            ipiv[j0 + jj] = j0 + gs + 1;
-            if (pv == 0.0 && *info == 0) *info = j0 + jj + 1;
-        }
-        if (pv != 0.0) {
-            if (gs != jj) {
-                if (jj >= rb && jj < re)
-                    for (int c = tid; c < jb; c += PANEL_THREADS) S[c * R + (jj - rb)] = prow[c];
-                if (gs >= rb && gs < re)
-                    for (int c = tid; c < jb; c += PANEL_THREADS) S[c * R + (gs - rb)] = orow[c];
-            }
-            __syncthreads();
-            if (fabs(pv) >= DBL_MIN) {
-                const double rinv = 1.0 / pv;
-                for (int r = tid; r < nr; r += PANEL_THREADS)
-                    if (rb + r > jj) S[jj * R + r] *= rinv;
-            } else {
-                for (int r = tid; r < nr; r += PANEL_THREADS)
-                    if (rb + r > jj) S[jj * R + r] /= pv;
+        if (tid == 0) {
+            const double ajj = ld_cg(&sj->rowjj[jj]);
+            const int gs = isnan(ajj) ? jj : gi;
+            const double pv = (gs == jj) ? ajj : ld_cg(&sw->row[jj]);
+            s_gs = gs;
+            s_pv = pv;
+            s_rinv = (pv != 0.0 && fabs(pv) >= DBL_MIN) ? 1.0 / pv : 0.0;
+            if (b == 0) {
+                ipiv[j0 + jj] = j0 + gs + 1;
+                if (pv == 0.0 && *info == 0) *info = j0 + jj + 1;
             }
         }
-        __syncthreads();
-        // -- rank-1 update of the panel's trailing part (rows > jj, cols > jj)
-        if (jj + 1 < jb) {
-            const int nc = jb - jj - 1;
-            for (int e = tid; e < nr * nc; e += PANEL_THREADS) {
-                const int r = e % nr, c = jj + 1 + e / nr;
-                if (rb + r > jj) S[c * R + r] = fma(-prow[c], S[jj * R + r], S[c * R + r]);
+        __syncthreads();                                             // B4
+        const int gs = s_gs;
+        const double pv = s_pv, rinv = s_rinv;
+        const bool swap = (pv != 0.0) && (gs != jj);
+        const double *P = (gs == jj) ? orow : prow;                  // new row jj
+
+        // -- [E] swap, scale and rank-1 update, each thread on its own rows
+        for (int r = tid; r < nr; r += PANEL_THREADS) {
+            const int g = rb + r;
+            if (swap && g == jj) {
+                for (int c = 0; c < jb; ++c) S[c * R + r] = P[c];
+            } else if (swap && g == gs) {
+                for (int c = 0; c < jb; ++c) S[c * R + r] = orow[c];
+            }
+            if (g > jj) {
+                double l = S[jj * R + r];
+                if (pv != 0.0) l = (rinv != 0.0) ? l * rinv : l / pv;
+                S[jj * R + r] = l;
+                for (int c = jj + 1; c < jb; ++c) S[c * R + r] = fma(-P[c], l, S[c * R + r]);
             }
         }
-        __syncthreads();
     }
+    __syncthreads();
 
     for (int e = tid; e < nr * jb; e += PANEL_THREADS) {
         const int r = e % nr, c = e / nr;
