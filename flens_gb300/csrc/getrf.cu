@@ -159,19 +159,20 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
     // Each thread owns rows r = tid, tid+256, ... of this CTA's block for the
     // whole panel: it computes their pivot keys, swaps, scales and updates
     // them, so only cross-row exchanges need a barrier.
+    // pivot keys of column 0 (later columns: computed during the update)
+    double nbv = -2.0;
+    int nbi = INT_MAX;
+    for (int r = tid; r < nr; r += PANEL_THREADS) {
+        const double a = fabs(S[r]);
+        const double key = isnan(a) ? -1.0 : a;
+        if (better(key, rb + r, nbv, nbi)) { nbv = key; nbi = rb + r; }
+    }
+
     for (int jj = 0; jj < jb; ++jj) {
         const int par = jj & 1;
         // -- [A] local pivot candidate among owned rows g >= jj (NaN never wins)
-        double bv = -2.0;
-        int bi = INT_MAX;
-        for (int r = tid; r < nr; r += PANEL_THREADS) {
-            const int g = rb + r;
-            if (g >= jj) {
-                const double a = fabs(S[jj * R + r]);
-                const double key = isnan(a) ? -1.0 : a;
-                if (better(key, g, bv, bi)) { bv = key; bi = g; }
-            }
-        }
+        double bv = nbv;
+        int bi = nbi;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
             const double ov = __shfl_down_sync(0xffffffffu, bv, off);
@@ -200,10 +201,9 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
         }
         __syncthreads();                                             // B2
         const unsigned long long want = epoch * 128ull + (unsigned long long)jj + 1ull;
-        if (tid == 0) {
-            __threadfence();
-            st_release(&mine->seq, want);
-        }
+        // the release store orders this CTA's slot writes (made visible to
+        // thread 0 by the barrier) before the sequence number
+        if (tid == 0) st_release(&mine->seq, want);
 
         // -- [C] every CTA reads every slot once its seq says step jj is published
         double gv = -3.0;
@@ -268,7 +268,7 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
         const bool swap = (pv != 0.0) && (gs != jj);
         const double *P = (gs == jj) ? orow : prow;                  // new row jj
 
-        // -- [E] swap, scale and rank-1 update, each thread on its own rows
+        // -- [E1] row interchange and scaling, by the owner of each row
         for (int r = tid; r < nr; r += PANEL_THREADS) {
             const int g = rb + r;
             if (swap && g == jj) {
@@ -276,11 +276,31 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
             } else if (swap && g == gs) {
                 for (int c = 0; c < jb; ++c) S[c * R + r] = orow[c];
             }
-            if (g > jj) {
-                double l = S[jj * R + r];
-                if (pv != 0.0) l = (rinv != 0.0) ? l * rinv : l / pv;
-                S[jj * R + r] = l;
-                for (int c = jj + 1; c < jb; ++c) S[c * R + r] = fma(-P[c], l, S[c * R + r]);
+            if (g > jj && pv != 0.0) {
+                const double l = S[jj * R + r];
+                S[jj * R + r] = (rinv != 0.0) ? l * rinv : l / pv;
+            }
+        }
+        __syncthreads();                                             // B5
+        // -- [E2] rank-1 update of rows > jj, columns > jj, spread over all
+        // threads (rows fastest); the thread that updates (r, jj+1) also
+        // keeps the pivot key of row r for the next column
+        nbv = -2.0;
+        nbi = INT_MAX;
+        if (jj + 1 < jb) {
+            const int nc = jb - jj - 1;
+            for (int e = tid; e < nr * nc; e += PANEL_THREADS) {
+                const int r = e % nr, c = jj + 1 + e / nr;
+                const int g = rb + r;
+                if (g > jj) {
+                    const double v = fma(-P[c], S[jj * R + r], S[c * R + r]);
+                    S[c * R + r] = v;
+                    if (c == jj + 1) {
+                        const double a = fabs(v);
+                        const double key = isnan(a) ? -1.0 : a;
+                        if (better(key, g, nbv, nbi)) { nbv = key; nbi = g; }
+                    }
+                }
             }
         }
     }
