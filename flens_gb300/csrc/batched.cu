@@ -1,0 +1,707 @@
+// batched.cu -- thousands of independent, uneven-size LU factorisations and
+// solves in one persistent launch, replayed through a CUDA graph.
+//
+// Per matrix the work is the reference's dgesv (flens/lapack/ge/sv.tcc:58-77:
+// trf with partial pivoting -- first maximum wins, reciprocal scaling,
+// INFO = first zero pivot -- then the row interchanges and the L and U
+// solves of trs), done by a "team" of T threads of a persistent CTA:
+//   * the plan sorts the matrices into size buckets, largest first; the
+//     kernel walks the buckets in that order and, inside a bucket, the CTA
+//     splits into 256/T teams that take matrices from the bucket's queue
+//     (one atomic counter per bucket, no spin-waits);
+//   * a matrix and its right-hand sides live in the team's share of shared
+//     memory when they fit, otherwise the team works on them in place in
+//     global memory (at these sizes, L2-resident);
+//   * T per bucket comes from the autotuner below (candidates timed on
+//     synthetic matrices of the bucket, cached per device);
+//   * precision 0 = FP64; 1 = FP32 LU in shared memory + FP64 iterative
+//     refinement (A untouched; r = b - A x in FP64 from global A; stop at a
+//     normwise backward error <= n*eps64, when a step fails to halve it
+//     (flens/lapack/ge/rfs.tcc:182-188) or after max_iter steps).  Matrices
+//     whose FP32 working set does not fit are solved in FP64 (iters = -1).
+#include "common.cuh"
+
+#include <float.h>
+#include <limits.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <random>
+#include <vector>
+
+namespace fg {
+namespace {
+
+constexpr int BT_THREADS = 256;
+constexpr int BT_BUCKETS = 8;
+constexpr size_t BT_SMEM = 216 * 1024;
+
+__host__ __device__ inline int bucket_of(int n) {
+    return n <= 16 ? 0 : n <= 32 ? 1 : n <= 64 ? 2 : n <= 128 ? 3 : n <= 256 ? 4 : n <= 512 ? 5 : n <= 1024 ? 6 : 7;
+}
+
+struct BatchArgs {
+    int beg[BT_BUCKETS], end[BT_BUCKETS];   // ranges of `order` per bucket
+    int team[BT_BUCKETS];                   // threads per team per bucket
+    const int *order;
+    const int *n, *nrhs, *lda, *ldb;
+    double *const *A;
+    double *const *B;
+    int *const *ipiv;
+    int *info;
+    int *iters;
+    double *berr;
+    int *queue;                             // [BT_BUCKETS], zeroed before each launch
+    int precision;
+    int max_iter;
+};
+
+__device__ __forceinline__ void team_sync(int id, int nthreads) {
+    if (nthreads == 32) __syncwarp();
+    else asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+__device__ __forceinline__ bool better(double v1, int i1, double v2, int i2) {
+    return v1 > v2 || (v1 == v2 && i1 < i2);
+}
+
+__device__ void team_argmax(double &v, int &i, int lt, int T, int bar, double *red_v, int *red_i) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const double ov = __shfl_down_sync(0xffffffffu, v, off);
+        const int oi = __shfl_down_sync(0xffffffffu, i, off);
+        if (better(ov, oi, v, i)) { v = ov; i = oi; }
+    }
+    v = __shfl_sync(0xffffffffu, v, 0);
+    i = __shfl_sync(0xffffffffu, i, 0);
+    if (T == 32) return;
+    const int nw = T >> 5;
+    if ((lt & 31) == 0) { red_v[lt >> 5] = v; red_i[lt >> 5] = i; }
+    team_sync(bar, T);
+    v = red_v[0];
+    i = red_i[0];
+    for (int q = 1; q < nw; ++q)
+        if (better(red_v[q], red_i[q], v, i)) { v = red_v[q]; i = red_i[q]; }
+    team_sync(bar, T);
+}
+
+__device__ double team_max(double m, int lt, int T, int bar, double *red) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+    if (T == 32) return m;
+    if ((lt & 31) == 0) red[lt >> 5] = m;
+    team_sync(bar, T);
+    m = red[0];
+    for (int q = 1; q < (T >> 5); ++q) m = fmax(m, red[q]);
+    team_sync(bar, T);
+    return m;
+}
+
+// LU with partial pivoting of the n x n matrix M (storage S): pivot search
+// and scaling in FP64, the rank-1 updates in S.  If INFO == 0 the k columns
+// of X are then overwritten by U^-1 L^-1 P X; X is untouched otherwise.
+template <typename S>
+__device__ int team_gesv(int n, int k, S *M, int ldm, S *X, int ldx, int *piv, int lt, int T,
+                         int bar, double *red_v, int *red_i) {
+    int info = 0;
+    for (int j = 0; j < n; ++j) {
+        double bv = -2.0;
+        int bi = INT_MAX;
+        for (int r = j + lt; r < n; r += T) {
+            const double a = fabs((double)M[r + (size_t)j * ldm]);
+            const double key = isnan(a) ? -1.0 : a;
+            if (better(key, r, bv, bi)) { bv = key; bi = r; }
+        }
+        team_argmax(bv, bi, lt, T, bar, red_v, red_i);
+        const double ajj = (double)M[j + (size_t)j * ldm];
+        const int p = isnan(ajj) ? j : bi;      // iamax keeps element j if it is NaN
+        if (lt == 0) piv[j] = p + 1;
+        const double pv = (double)M[p + (size_t)j * ldm];
+        if (pv != 0.0) {
+            if (p != j) {
+                for (int c = lt; c < n; c += T) {
+                    const S t = M[j + (size_t)c * ldm];
+                    M[j + (size_t)c * ldm] = M[p + (size_t)c * ldm];
+                    M[p + (size_t)c * ldm] = t;
+                }
+                team_sync(bar, T);
+            }
+            const bool recip = fabs(pv) >= DBL_MIN;
+            const double rinv = recip ? 1.0 / pv : 0.0;
+            for (int r = j + 1 + lt; r < n; r += T) {
+                const double l = (double)M[r + (size_t)j * ldm];
+                M[r + (size_t)j * ldm] = (S)(recip ? l * rinv : l / pv);
+            }
+        } else if (info == 0) {
+            info = j + 1;
+        }
+        team_sync(bar, T);
+        const int m2 = n - j - 1;
+        for (int e = lt; e < m2 * m2; e += T) {
+            const int r = j + 1 + e % m2, c = j + 1 + e / m2;
+            M[r + (size_t)c * ldm] = fma(-M[j + (size_t)c * ldm], M[r + (size_t)j * ldm], M[r + (size_t)c * ldm]);
+        }
+        team_sync(bar, T);
+    }
+    if (info != 0) return info;
+    for (int j = 0; j < n; ++j) {                          // interchanges (trs.tcc:84)
+        const int p = piv[j] - 1;
+        if (p != j) {
+            for (int c = lt; c < k; c += T) {
+                const S t = X[j + (size_t)c * ldx];
+                X[j + (size_t)c * ldx] = X[p + (size_t)c * ldx];
+                X[p + (size_t)c * ldx] = t;
+            }
+            team_sync(bar, T);
+        }
+    }
+    for (int i = 0; i < n; ++i) {                          // unit lower
+        const int m2 = n - i - 1;
+        for (int e = lt; e < m2 * k; e += T) {
+            const int r = i + 1 + e % m2, c = e / m2;
+            X[r + (size_t)c * ldx] = fma(-M[r + (size_t)i * ldm], X[i + (size_t)c * ldx], X[r + (size_t)c * ldx]);
+        }
+        team_sync(bar, T);
+    }
+    for (int i = n - 1; i >= 0; --i) {                     // upper
+        for (int c = lt; c < k; c += T) X[i + (size_t)c * ldx] = X[i + (size_t)c * ldx] / M[i + (size_t)i * ldm];
+        team_sync(bar, T);
+        for (int e = lt; e < i * k; e += T) {
+            const int r = e % i, c = e / i;
+            X[r + (size_t)c * ldx] = fma(-M[r + (size_t)i * ldm], X[i + (size_t)c * ldx], X[r + (size_t)c * ldx]);
+        }
+        team_sync(bar, T);
+    }
+    return 0;
+}
+
+// X <- U^-1 L^-1 P X with the FP32 factors in M (the pivots of team_gesv)
+__device__ void team_lu_solve32(int n, int k, const float *M, const int *piv, float *X, int lt,
+                                int T, int bar) {
+    for (int j = 0; j < n; ++j) {
+        const int p = piv[j] - 1;
+        if (p != j) {
+            for (int c = lt; c < k; c += T) {
+                const float t = X[j + (size_t)c * n];
+                X[j + (size_t)c * n] = X[p + (size_t)c * n];
+                X[p + (size_t)c * n] = t;
+            }
+            team_sync(bar, T);
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        const int m2 = n - i - 1;
+        for (int e = lt; e < m2 * k; e += T) {
+            const int r = i + 1 + e % m2, c = e / m2;
+            X[r + (size_t)c * n] -= M[r + (size_t)i * n] * X[i + (size_t)c * n];
+        }
+        team_sync(bar, T);
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        for (int c = lt; c < k; c += T) X[i + (size_t)c * n] /= M[i + (size_t)i * n];
+        team_sync(bar, T);
+        for (int e = lt; e < i * k; e += T) {
+            const int r = e % i, c = e / i;
+            X[r + (size_t)c * n] -= M[r + (size_t)i * n] * X[i + (size_t)c * n];
+        }
+        team_sync(bar, T);
+    }
+}
+
+__device__ size_t fp64_need(int n, int k) { return ((size_t)n * n + (size_t)n * k) * 8; }
+// FP32 M and D, FP64 saved b and residual
+__device__ size_t mixed_need(int n, int k) { return (size_t)n * n * 4 + (size_t)n * k * (4 + 8 + 8); }
+
+__device__ void solve_fp64(const BatchArgs &a, int idx, unsigned char *sm, size_t share, int lt,
+                           int T, int bar, double *rv, int *ri) {
+    const int n = a.n[idx], k = a.nrhs[idx], lda = a.lda[idx], ldb = a.ldb[idx];
+    double *A = a.A[idx], *B = a.B[idx];
+    int info;
+    if (fp64_need(n, k) <= share) {
+        double *M = (double *)sm, *X = M + (size_t)n * n;
+        for (int e = lt; e < n * n; e += T) M[e] = A[e % n + (size_t)(e / n) * lda];
+        for (int e = lt; e < n * k; e += T) X[e] = B[e % n + (size_t)(e / n) * ldb];
+        team_sync(bar, T);
+        info = team_gesv<double>(n, k, M, n, X, n, a.ipiv[idx], lt, T, bar, rv, ri);
+        for (int e = lt; e < n * n; e += T) A[e % n + (size_t)(e / n) * lda] = M[e];
+        if (info == 0)
+            for (int e = lt; e < n * k; e += T) B[e % n + (size_t)(e / n) * ldb] = X[e];
+    } else {
+        info = team_gesv<double>(n, k, A, lda, B, ldb, a.ipiv[idx], lt, T, bar, rv, ri);
+    }
+    if (lt == 0) {
+        a.info[idx] = info;
+        if (a.iters) a.iters[idx] = -1;
+        if (a.berr) a.berr[idx] = 0.0;
+    }
+    team_sync(bar, T);
+}
+
+__device__ void solve_mixed(const BatchArgs &a, int idx, unsigned char *sm, int lt, int T, int bar,
+                            double *rv, int *ri) {
+    const int n = a.n[idx], k = a.nrhs[idx], lda = a.lda[idx], ldb = a.ldb[idx];
+    const double *A = a.A[idx];
+    double *B = a.B[idx];
+    int *piv = a.ipiv[idx];
+    double *Bs = (double *)sm;                         // n x k saved b (FP64)
+    double *Rr = Bs + (size_t)n * k;                   // n x k residual (FP64)
+    float *M = (float *)(Rr + (size_t)n * k);          // n x n FP32 factors
+    float *D = M + (size_t)n * n;                      // n x k FP32 solves
+    for (int e = lt; e < n * n; e += T) M[e] = (float)A[e % n + (size_t)(e / n) * lda];
+    for (int e = lt; e < n * k; e += T) {
+        const double v = B[e % n + (size_t)(e / n) * ldb];
+        Bs[e] = v;
+        D[e] = (float)v;
+    }
+    team_sync(bar, T);
+    const int info = team_gesv<float>(n, k, M, n, D, n, piv, lt, T, bar, rv, ri);
+    if (info != 0) {
+        if (lt == 0) a.info[idx] = info;
+        team_sync(bar, T);
+        return;
+    }
+    // x0 (FP64) lives in B from here on
+    for (int e = lt; e < n * k; e += T) B[e % n + (size_t)(e / n) * ldb] = (double)D[e];
+    double anorm = 0.0, worst = 0.0;
+    for (int r = lt; r < n; r += T) {
+        double s = 0.0;
+        for (int c = 0; c < n; ++c) s += fabs(A[r + (size_t)c * lda]);
+        anorm = fmax(anorm, s);
+    }
+    anorm = team_max(anorm, lt, T, bar, rv);
+    int steps = 0;
+    unsigned done = 0;                  // bit c: column c finished (k <= 32)
+    double prev[32];
+    for (int c = 0; c < k && c < 32; ++c) prev[c] = INFINITY;
+    for (int it = 0; it <= a.max_iter; ++it) {
+        team_sync(bar, T);
+        for (int e = lt; e < n * k; e += T) {          // r = b - A x, FP64
+            const int r = e % n, c = e / n;
+            double s = Bs[e];
+            for (int q = 0; q < n; ++q) s = fma(-A[r + (size_t)q * lda], B[q + (size_t)c * ldb], s);
+            Rr[e] = s;
+        }
+        team_sync(bar, T);
+        bool any = false;
+        worst = 0.0;
+        for (int c = 0; c < k; ++c) {
+            double rm = 0.0, xm = 0.0, bm = 0.0;
+            for (int r = lt; r < n; r += T) {
+                rm = fmax(rm, fabs(Rr[r + (size_t)c * n]));
+                xm = fmax(xm, fabs(B[r + (size_t)c * ldb]));
+                bm = fmax(bm, fabs(Bs[r + (size_t)c * n]));
+            }
+            rm = team_max(rm, lt, T, bar, rv);
+            xm = team_max(xm, lt, T, bar, rv);
+            bm = team_max(bm, lt, T, bar, rv);
+            const double den = anorm * xm + bm;
+            const double be = den > 0.0 ? rm / den : (rm > 0.0 ? INFINITY : 0.0);
+            worst = fmax(worst, be);
+            const bool fin = (done >> c) & 1u;
+            if (!fin && (be <= (double)n * DBL_EPSILON || !(be <= 0.5 * prev[c]) || it == a.max_iter))
+                done |= 1u << c;
+            prev[c] = be;
+            // scaled residual into D (zero for finished columns)
+            const bool go = !((done >> c) & 1u);
+            any = any || go;
+            const double sc = rm > 0.0 ? rm : 1.0;
+            for (int r = lt; r < n; r += T) D[r + (size_t)c * n] = go ? (float)(Rr[r + (size_t)c * n] / sc) : 0.0f;
+            if (lt == 0) Rr[(size_t)c * n] = go ? sc : 0.0;   // keep the scale in R(0, c)
+        }
+        team_sync(bar, T);
+        if (!any) break;
+        team_lu_solve32(n, k, M, piv, D, lt, T, bar);
+        for (int e = lt; e < n * k; e += T) {
+            const int c = e / n;
+            const double sc = Rr[(size_t)c * n];
+            if (sc != 0.0) B[e % n + (size_t)c * ldb] += sc * (double)D[e];
+        }
+        ++steps;
+    }
+    if (lt == 0) {
+        a.info[idx] = 0;
+        if (a.iters) a.iters[idx] = steps;
+        if (a.berr) a.berr[idx] = worst;
+    }
+    team_sync(bar, T);
+}
+
+__global__ void __launch_bounds__(BT_THREADS, 1)
+batched_gesv_kernel(BatchArgs a) {
+    extern __shared__ __align__(16) unsigned char bsm[];
+    __shared__ double red_v[8][8];
+    __shared__ int red_i[8][8];
+    __shared__ int s_item[8];
+    const int tid = threadIdx.x;
+    for (int bk = BT_BUCKETS - 1; bk >= 0; --bk) {
+        const int beg = a.beg[bk], end = a.end[bk];
+        if (beg >= end) continue;
+        const int T = a.team[bk];
+        const int nteams = BT_THREADS / T;
+        const int tm = tid / T, lt = tid % T;
+        const int bar = 1 + tm;
+        const size_t share = (BT_SMEM / nteams) / 16 * 16;
+        unsigned char *sm = bsm + share * tm;
+        // each pass takes one matrix; at most end-beg passes per team
+        for (int pass = 0; pass <= end - beg; ++pass) {
+            if (lt == 0) s_item[tm] = beg + atomicAdd(&a.queue[bk], 1);
+            team_sync(bar, T);
+            const int item = s_item[tm];
+            team_sync(bar, T);
+            if (item >= end) break;
+            const int idx = a.order[item];
+            if (a.precision == 1 && a.nrhs[idx] <= 32 && mixed_need(a.n[idx], a.nrhs[idx]) <= share)
+                solve_mixed(a, idx, sm, lt, T, bar, red_v[tm], red_i[tm]);
+            else
+                solve_fp64(a, idx, sm, share, lt, T, bar, red_v[tm], red_i[tm]);
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- plan -----
+struct BatchedPlan {
+    int device = -1;
+    int count = 0;
+    BatchArgs args;
+    int *d_meta = nullptr;          // order | n | nrhs | lda | ldb | queue
+    void **d_ptrs = nullptr;        // A | B | ipiv
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int team[BT_BUCKETS];
+    std::vector<int> hn;
+};
+
+namespace {
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int>, int> g_tuned;   // (device, bucket, precision) -> T
+
+int default_team(int bucket) { return bucket <= 1 ? 32 : bucket == 2 ? 64 : bucket == 3 ? 128 : 256; }
+
+int env_team() {
+    const char *s = getenv("FLENS_GB300_BATCH_TEAM");
+    if (!s) return 0;
+    const int t = atoi(s);
+    return (t == 32 || t == 64 || t == 128 || t == 256) ? t : 0;
+}
+
+bool tuning_enabled() {
+    const char *s = getenv("FLENS_GB300_BATCH_TUNE");
+    return !(s && s[0] == '0');
+}
+
+void fill_ranges(const std::vector<int> &hn, std::vector<int> &order, BatchArgs &a) {
+    const int count = (int)hn.size();
+    order.resize(count);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        const int bx = bucket_of(hn[x]), by = bucket_of(hn[y]);
+        if (bx != by) return bx > by;
+        return hn[x] > hn[y];
+    });
+    int i = 0;
+    for (int b = BT_BUCKETS - 1; b >= 0; --b) {
+        a.beg[b] = i;
+        while (i < count && bucket_of(hn[order[i]]) == b) ++i;
+        a.end[b] = i;
+    }
+}
+
+int set_attributes() {
+    static bool attr = false;
+    if (!attr) {
+        FG_CUDA(cudaFuncSetAttribute(batched_gesv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)BT_SMEM));
+        attr = true;
+    }
+    return kOk;
+}
+
+// queue reset + the persistent kernel (also what a plan's graph holds)
+int launch(const BatchArgs &a, cudaStream_t s) {
+    int st = set_attributes();
+    if (st != kOk) return st;
+    FG_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(int) * BT_BUCKETS, s));
+    batched_gesv_kernel<<<num_sms(), BT_THREADS, BT_SMEM, s>>>(a);
+    FG_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+// Time each candidate team size on synthetic matrices of the bucket's largest
+// size (diagonally dominant, uniform entries) and return the fastest.
+int tune_bucket(int bucket, int nmax, int kmax, int precision, cudaStream_t s) {
+    const int dev = device_id();
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tuned.find(std::make_tuple(dev, bucket, precision));
+        if (it != g_tuned.end()) return it->second;
+    }
+    const int sms = num_sms();
+    const int n = nmax, k = kmax;
+    const size_t aBytes = (size_t)n * n * 8, bBytes = (size_t)n * k * 8, pBytes = (size_t)n * 4;
+    const size_t per = (aBytes + bBytes + pBytes + 255) / 256 * 256;
+    // a few matrices per SM, at most 256 MiB of them
+    int count = 4 * sms;
+    while (count > sms && per * (size_t)count > (256u << 20)) count /= 2;
+    if (per * (size_t)count > (512u << 20)) return default_team(bucket);
+    const size_t metaBytes = (size_t)count * 4 * 6 + 3 * (size_t)count * sizeof(void *) +
+                             (size_t)count * (4 + 4 + 8) + 4096;
+    char *buf = (char *)workspace_slot(s, 3, per * (count + 1) + metaBytes);
+    if (!buf) return default_team(bucket);
+    char *master = buf + per * count + metaBytes;       // one pristine A | B
+    std::vector<double> hA((size_t)n * n), hB((size_t)n * k);
+    std::mt19937_64 rng(1234 + bucket);
+    std::uniform_real_distribution<double> U(-1.0, 1.0);
+    for (auto &v : hA) v = U(rng);
+    for (int i = 0; i < n; ++i) hA[i + (size_t)i * n] += n / 4.0;
+    for (auto &v : hB) v = U(rng);
+    std::vector<void *> pA(count), pB(count), pP(count);
+    std::vector<int> hn(count, n), hk(count, k), hld(count, n);
+    for (int i = 0; i < count; ++i) {
+        pA[i] = buf + per * i;
+        pB[i] = buf + per * i + aBytes;
+        pP[i] = buf + per * i + aBytes + bBytes;
+    }
+    char *m = buf + per * count;
+    int *d_order = (int *)m, *d_n = d_order + count, *d_k = d_n + count, *d_lda = d_k + count,
+        *d_ldb = d_lda + count, *d_q = d_ldb + count;
+    void **d_p = (void **)(((uintptr_t)(d_q + BT_BUCKETS) + 15) & ~(uintptr_t)15);
+    int *d_info = (int *)(d_p + 3 * count), *d_it = d_info + count;
+    double *d_be = (double *)(((uintptr_t)(d_it + count) + 15) & ~(uintptr_t)15);
+    BatchArgs a;
+    memset(&a, 0, sizeof a);
+    std::vector<int> order;
+    fill_ranges(hn, order, a);
+    cudaMemcpyAsync(d_order, order.data(), 4 * count, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_n, hn.data(), 4 * count, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_k, hk.data(), 4 * count, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_lda, hld.data(), 4 * count, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_ldb, hld.data(), 4 * count, cudaMemcpyHostToDevice, s);
+    std::vector<void *> hp(3 * count);
+    for (int i = 0; i < count; ++i) {
+        hp[i] = pA[i];
+        hp[count + i] = pB[i];
+        hp[2 * count + i] = pP[i];
+    }
+    cudaMemcpyAsync(d_p, hp.data(), sizeof(void *) * 3 * count, cudaMemcpyHostToDevice, s);
+    a.order = d_order;
+    a.n = d_n;
+    a.nrhs = d_k;
+    a.lda = d_lda;
+    a.ldb = d_ldb;
+    a.A = (double *const *)d_p;
+    a.B = (double *const *)(d_p + count);
+    a.ipiv = (int *const *)(d_p + 2 * count);
+    a.info = d_info;
+    a.iters = d_it;
+    a.berr = d_be;
+    a.queue = d_q;
+    a.precision = precision;
+    a.max_iter = 10;
+    cudaMemcpyAsync(master, hA.data(), aBytes, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(master + aBytes, hB.data(), bBytes, cudaMemcpyHostToDevice, s);
+    int best = default_team(bucket);
+    float best_ms = 1e30f;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int T : {32, 64, 128, 256}) {
+        for (int b = 0; b < BT_BUCKETS; ++b) a.team[b] = T;
+        float tot = 0.0f;
+        bool ok = true;
+        for (int rep = 0; rep < 3; ++rep) {
+            for (int i = 0; i < count; ++i) {
+                cudaMemcpyAsync(pA[i], master, aBytes, cudaMemcpyDeviceToDevice, s);
+                cudaMemcpyAsync(pB[i], master + aBytes, bBytes, cudaMemcpyDeviceToDevice, s);
+            }
+            cudaEventRecord(e0, s);
+            if (launch(a, s) != kOk) {
+                ok = false;
+                break;
+            }
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0) tot += ms;
+        }
+        if (ok && tot < best_ms) {
+            best_ms = tot;
+            best = T;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamSynchronize(s);
+    trace("batched tune bucket=%d n=%d k=%d precision=%d -> team %d (%.3f ms)", bucket, n, k,
+          precision, best, best_ms / 2);
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tuned[std::make_tuple(dev, bucket, precision)] = best;
+    return best;
+}
+
+}  // namespace
+
+int batched_plan_create(int count, const int *hn, const int *hk, double *const *hA, const int *hlda,
+                        int *const *hipiv, double *const *hB, const int *hldb, int *d_info,
+                        int precision, int *d_iters, double *d_berr, int max_iter,
+                        cudaStream_t s, BatchedPlan **out) {
+    *out = nullptr;
+    int st0 = kOk;
+    BatchedPlan *p = new BatchedPlan();
+    p->device = device_id();
+    p->count = count;
+    p->hn.assign(hn, hn + count);
+    BatchArgs &a = p->args;
+    memset(&a, 0, sizeof a);
+    std::vector<int> order;
+    fill_ranges(p->hn, order, a);
+    // team size per bucket
+    const int forced = env_team();
+    for (int b = 0; b < BT_BUCKETS; ++b) {
+        int T = default_team(b);
+        if (forced) T = forced;
+        else if (tuning_enabled() && a.end[b] > a.beg[b]) {
+            int nmax = 0, kmax = 0;
+            for (int i = a.beg[b]; i < a.end[b]; ++i) {
+                nmax = std::max(nmax, hn[order[i]]);
+                kmax = std::max(kmax, hk[order[i]]);
+            }
+            T = tune_bucket(b, nmax, kmax, precision, s);
+        }
+        a.team[b] = T;
+        p->team[b] = T;
+    }
+    const size_t intBytes = (size_t)count * 4;
+    if (cudaMalloc((void **)&p->d_meta, 5 * intBytes + BT_BUCKETS * 4) != cudaSuccess ||
+        cudaMalloc((void **)&p->d_ptrs, 3 * (size_t)count * sizeof(void *)) != cudaSuccess) {
+        cudaGetLastError();
+        set_last_error("batched plan: device allocation failed");
+        if (p->d_meta) cudaFree(p->d_meta);
+        delete p;
+        return kErrAlloc;
+    }
+    int *d_order = p->d_meta, *d_n = d_order + count, *d_k = d_n + count, *d_lda = d_k + count,
+        *d_ldb = d_lda + count, *d_q = d_ldb + count;
+    FG_CUDA(cudaMemcpyAsync(d_order, order.data(), intBytes, cudaMemcpyHostToDevice, s));
+    FG_CUDA(cudaMemcpyAsync(d_n, hn, intBytes, cudaMemcpyHostToDevice, s));
+    FG_CUDA(cudaMemcpyAsync(d_k, hk, intBytes, cudaMemcpyHostToDevice, s));
+    FG_CUDA(cudaMemcpyAsync(d_lda, hlda, intBytes, cudaMemcpyHostToDevice, s));
+    FG_CUDA(cudaMemcpyAsync(d_ldb, hldb, intBytes, cudaMemcpyHostToDevice, s));
+    std::vector<void *> hp(3 * (size_t)count);
+    for (int i = 0; i < count; ++i) {
+        hp[i] = hA[i];
+        hp[count + i] = hB[i];
+        hp[2 * (size_t)count + i] = hipiv[i];
+    }
+    FG_CUDA(cudaMemcpyAsync(p->d_ptrs, hp.data(), sizeof(void *) * 3 * (size_t)count,
+                            cudaMemcpyHostToDevice, s));
+    FG_CUDA(cudaStreamSynchronize(s));
+    a.order = d_order;
+    a.n = d_n;
+    a.nrhs = d_k;
+    a.lda = d_lda;
+    a.ldb = d_ldb;
+    a.A = (double *const *)p->d_ptrs;
+    a.B = (double *const *)(p->d_ptrs + count);
+    a.ipiv = (int *const *)(p->d_ptrs + 2 * (size_t)count);
+    a.info = d_info;
+    a.iters = d_iters;
+    a.berr = d_berr;
+    a.queue = d_q;
+    a.precision = precision;
+    a.max_iter = max_iter > 0 ? max_iter : 10;
+    // capture the queue reset + persistent launch as one graph
+    if ((st0 = set_attributes()) != kOk) return st0;
+    cudaStream_t cap;
+    FG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    FG_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    int st = launch(a, cap);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (st != kOk || ce != cudaSuccess) {
+        if (ce != cudaSuccess) cuda_fail(ce, "cudaStreamEndCapture");
+        cudaFree(p->d_meta);
+        cudaFree(p->d_ptrs);
+        delete p;
+        return st != kOk ? st : kErrCuda;
+    }
+    p->graph = g;
+    FG_CUDA(cudaGraphInstantiate(&p->exec, g, 0));
+    *out = p;
+    return kOk;
+}
+
+int batched_plan_execute(BatchedPlan *p, cudaStream_t s) {
+    if (!p || !p->exec) return kErrUnsupported;
+    KTimer kt(kFamBatched, s, 0.0, 0.0);
+    FG_CUDA(cudaGraphLaunch(p->exec, s));
+    return kOk;
+}
+
+void batched_plan_destroy(BatchedPlan *p) {
+    if (!p) return;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->d_meta) cudaFree(p->d_meta);
+    if (p->d_ptrs) cudaFree(p->d_ptrs);
+    delete p;
+}
+
+}  // namespace fg
+
+// ----------------------------------------------------------------- C ABI ----
+// A plan for solving `count` independent systems A_i X_i = B_i (n_i x n_i,
+// n_i x nrhs_i, column-major FP64 in device memory).  The metadata arrays
+// (n, nrhs, lda, ldb) and the pointer arrays (A, ipiv, B: device pointers)
+// are HOST arrays read at creation; info / iters / berr are device arrays of
+// `count` entries written by every execution.  Creating a plan autotunes the
+// team size of each size bucket (first time per device and bucket; disable
+// with FLENS_GB300_BATCH_TUNE=0) and captures one persistent launch in a
+// CUDA graph.
+FG_API int flens_gb300_dgesv_batched_plan(int count, const int *n, const int *nrhs,
+                                          double *const *A, const int *lda, int *const *ipiv,
+                                          double *const *B, const int *ldb, int *info,
+                                          int precision, int *iters, double *berr, int max_iter,
+                                          void *stream, void **plan) {
+    if (count < 0) return -1;
+    if (precision < 0 || precision > 1) return -10;
+    if (!plan) return -15;
+    for (int i = 0; i < count; ++i) {
+        if (n[i] < 0 || nrhs[i] < 0 || lda[i] < (n[i] > 1 ? n[i] : 1) ||
+            ldb[i] < (n[i] > 1 ? n[i] : 1)) {
+            fg::set_last_error("batched: matrix %d has an illegal size or leading dimension", i);
+            return -2;
+        }
+    }
+    fg::BatchedPlan *p = nullptr;
+    const int st = fg::batched_plan_create(count, n, nrhs, A, lda, ipiv, B, ldb, info, precision,
+                                           iters, berr, max_iter, (cudaStream_t)stream, &p);
+    *plan = p;
+    return st;
+}
+
+// Run a plan (one graph launch: the persistent kernel); async on stream.
+FG_API int flens_gb300_batched_execute(void *plan, void *stream) {
+    return fg::batched_plan_execute((fg::BatchedPlan *)plan, (cudaStream_t)stream);
+}
+
+FG_API void flens_gb300_batched_destroy(void *plan) {
+    fg::batched_plan_destroy((fg::BatchedPlan *)plan);
+}
+
+// Team size chosen for a bucket (0..7, upper bounds 16,32,...,2048) of a plan.
+FG_API int flens_gb300_batched_team(void *plan, int bucket) {
+    if (!plan || bucket < 0 || bucket > 7) return -1;
+    return ((fg::BatchedPlan *)plan)->team[bucket];
+}

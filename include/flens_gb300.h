@@ -133,6 +133,37 @@ int flens_gb300_dgesv_mixed(int n, int nrhs, const double *A, int ldA,
                             int precision, int solver, int max_iter, double tol,
                             int *iters, double *berr, int *info, void *stream);
 
+/* ---------------------------------------------- batched (extension) --- */
+
+/* Plan for solving `count` independent systems A_i X_i = B_i (A_i n_i x n_i,
+ * B_i n_i x nrhs_i, column-major FP64 in device memory), each as the
+ * reference's dgesv (flens/lapack/ge/sv.tcc:58-77).  n, nrhs, lda, ldb and the
+ * pointer arrays A, ipiv (n_i ints each, 1-based), B are HOST arrays read now;
+ * info, iters, berr are DEVICE arrays of `count` entries written by every
+ * execution.  precision 0 = FP64 (A_i <- LU factors); 1 = FP32 LU + FP64
+ * refinement (A_i untouched; iters_i = refinement steps, -1 where the FP64
+ * path was used; berr_i = final normwise backward error; max_iter bounds the
+ * steps).  B_i <- X_i when INFO_i == 0, untouched otherwise.  Creating a plan
+ * autotunes the team size of each size bucket (first use per device;
+ * FLENS_GB300_BATCH_TUNE=0 disables it, FLENS_GB300_BATCH_TEAM=T forces T) and
+ * captures one persistent launch in a CUDA graph.  Synchronises on stream. */
+int flens_gb300_dgesv_batched_plan(int count, const int *n, const int *nrhs,
+                                   double *const *A, const int *lda,
+                                   int *const *ipiv, double *const *B,
+                                   const int *ldb, int *info, int precision,
+                                   int *iters, double *berr, int max_iter,
+                                   void *stream, void **plan);
+
+/* Run a plan: one graph launch.  Async on stream. */
+int flens_gb300_batched_execute(void *plan, void *stream);
+
+/* Release a plan. */
+void flens_gb300_batched_destroy(void *plan);
+
+/* Team size (threads per matrix) the plan uses for size bucket 0..7
+ * (n <= 16, 32, 64, 128, 256, 512, 1024, larger). */
+int flens_gb300_batched_team(void *plan, int bucket);
+
 /* dgetrs on device memory for callers that must not allocate device memory
  * once running (a fixed, pre-reserved memory budget, a memory pool owned by
  * another framework, or a process that forbids cudaMalloc after start-up).

@@ -1,0 +1,128 @@
+"""Batched uneven-size dgesv in one persistent launch (graph replay) against
+the oracle, matrix by matrix.
+
+Each matrix is the reference's dgesv (flens/lapack/ge/sv.tcc:58-77): the bar
+is identical pivots and INFO on well-separated inputs, solutions within 1e-12
+normwise of the oracle's, B untouched when INFO > 0.  The mixed variant (FP32
+LU + FP64 refinement) must reach a normwise backward error <= 10 n eps64.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import flens_gb300 as fg
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+EPS = np.finfo(np.float64).eps
+
+
+def plan_fn():
+    L = fg.lib()
+    f = L.flens_gb300_dgesv_batched_plan
+    vp = ctypes.c_void_p
+    f.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int, vp, vp, ctypes.c_int,
+                  vp, ctypes.POINTER(ctypes.c_void_p)]
+    f.restype = ctypes.c_int
+    L.flens_gb300_batched_execute.argtypes = [vp, vp]
+    L.flens_gb300_batched_execute.restype = ctypes.c_int
+    L.flens_gb300_batched_destroy.argtypes = [vp]
+    L.flens_gb300_batched_team.argtypes = [vp, ctypes.c_int]
+    L.flens_gb300_batched_team.restype = ctypes.c_int
+    return f
+
+
+def make_batch(cuda, sizes, ks, seed, singular=()):
+    import torch
+    mats, rhs, host = [], [], []
+    for i, (n, k) in enumerate(zip(sizes, ks)):
+        A = oracle.uniform(seed + 2 * i, n, n)
+        A[np.arange(n), np.arange(n)] += n / 4.0
+        if i in singular:
+            A[:, n // 2] = 0.0
+        B = oracle.uniform(seed + 2 * i + 1, n, k)
+        host.append((A, B))
+        mats.append(fg.to_colmajor(torch.from_numpy(A).to(cuda)))
+        rhs.append(fg.to_colmajor(torch.from_numpy(B).to(cuda)))
+    return mats, rhs, host
+
+
+def run_batched(cuda, mats, rhs, precision, execs=1):
+    import torch
+    count = len(mats)
+    n = np.array([m.shape[0] for m in mats], dtype=np.int32)
+    k = np.array([b.shape[1] for b in rhs], dtype=np.int32)
+    lda = np.maximum(n, 1).astype(np.int32)
+    ipivs = [torch.zeros(max(1, int(x)), dtype=torch.int32, device=cuda) for x in n]
+    pa = np.array([m.data_ptr() for m in mats], dtype=np.uint64)
+    pb = np.array([b.data_ptr() for b in rhs], dtype=np.uint64)
+    pp = np.array([p.data_ptr() for p in ipivs], dtype=np.uint64)
+    info = torch.full((count,), -7, dtype=torch.int32, device=cuda)
+    iters = torch.zeros(count, dtype=torch.int32, device=cuda)
+    berr = torch.zeros(count, dtype=torch.float64, device=cuda)
+    plan = ctypes.c_void_p()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    st = plan_fn()(count, n.ctypes.data, k.ctypes.data, pa.ctypes.data, lda.ctypes.data,
+                   pp.ctypes.data, pb.ctypes.data, lda.ctypes.data, info.data_ptr(), precision,
+                   iters.data_ptr(), berr.data_ptr(), 10, stream, ctypes.byref(plan))
+    assert st == 0, fg.last_error()
+    for _ in range(execs):
+        assert fg.lib().flens_gb300_batched_execute(plan, stream) == 0
+    torch.cuda.synchronize()
+    teams = [fg.lib().flens_gb300_batched_team(plan, b) for b in range(8)]
+    fg.lib().flens_gb300_batched_destroy(plan)
+    fg.sync()
+    return ipivs, info.cpu().numpy(), iters.cpu().numpy(), berr.cpu().numpy(), teams
+
+
+SIZES = [1, 8, 9, 16, 17, 31, 32, 33, 48, 64, 65, 100, 128, 129, 160, 200, 256, 300, 13, 40]
+KS = [1, 4, 16, 1, 4, 16, 1, 4, 16, 1, 4, 16, 1, 4, 16, 1, 4, 16, 4, 1]
+
+
+def test_batched_fp64_vs_oracle(cuda, port):
+    mats, rhs, host = make_batch(cuda, SIZES, KS, 500, singular=(18,))
+    B0 = [b.clone() for b in rhs]
+    ipivs, info, iters, berr, teams = run_batched(cuda, mats, rhs, 0)
+    for i, (A0, Bh) in enumerate(host):
+        A1, B1 = A0.copy(order="F"), Bh.copy(order="F")
+        pivr, infor = port.dgesv(A1, B1)
+        assert info[i] == infor, (i, SIZES[i], info[i], infor)
+        n = SIZES[i]
+        assert np.array_equal(ipivs[i].cpu().numpy()[:n], pivr), i
+        if infor == 0:
+            assert oracle.normwise_rel(rhs[i].cpu().numpy(), B1) <= 1e-12, i
+            assert oracle.lu_backward_error(A0, mats[i].cpu().numpy(), pivr) <= 10.0
+        else:
+            assert np.array_equal(rhs[i].cpu().numpy(), B0[i].cpu().numpy())   # no solve
+    assert all(t in (32, 64, 128, 256) for t in teams)
+
+
+def test_batched_graph_replay(cuda, port):
+    # the plan's graph replays the same launch: second execution on fresh data
+    import torch
+    mats, rhs, host = make_batch(cuda, SIZES[:12], KS[:12], 700)
+    ipivs, info, _, _, _ = run_batched(cuda, mats, rhs, 0, execs=1)
+    assert (info == 0).all()
+    for i, (A0, Bh) in enumerate(host):
+        A1, B1 = A0.copy(order="F"), Bh.copy(order="F")
+        port.dgesv(A1, B1)
+        assert oracle.normwise_rel(rhs[i].cpu().numpy(), B1) <= 1e-12
+
+
+def test_batched_mixed_refinement(cuda):
+    import torch
+    sizes = [8, 20, 33, 64, 100, 128, 200, 17, 50, 90]
+    ks = [1, 4, 16, 1, 4, 16, 1, 4, 16, 1]
+    mats, rhs, host = make_batch(cuda, sizes, ks, 900)
+    ipivs, info, iters, berr, teams = run_batched(cuda, mats, rhs, 1)
+    assert (info == 0).all(), info
+    for i, (A0, Bh) in enumerate(host):
+        n = sizes[i]
+        X = rhs[i].cpu().numpy()
+        R = Bh - A0 @ X
+        be = (np.abs(R).max(0) / (np.abs(A0).sum(1).max() * np.abs(X).max(0) + np.abs(Bh).max(0))).max()
+        assert be <= 10 * n * EPS, (i, n, be, iters[i])
+        assert berr[i] <= 10 * n * EPS
+        np.testing.assert_array_equal(mats[i].cpu().numpy(), A0)      # A untouched
