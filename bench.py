@@ -292,7 +292,12 @@ def our_arm(args, rank: int, world: int) -> None:
 
     if rank == 0:
         # -- dominant kernel vs the measured FP64 peak
-        peak = None if args.quick else fp64_peak(torch, dev)
+        cublas_peak = None if args.quick else fp64_peak(torch, dev)
+        # FP64 pipe issue rate (ncu: 2 DFMA per cycle per SM) at the sampled clock
+        sm_mhz = result["clocks"].get("sm_mhz") or 2070.0
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        pipe_peak = 2 * 2 * sms * sm_mhz * 1e6 / 1e12
+        peak = max(p for p in (cublas_peak, pipe_peak) if p)
         dom = max(fam.items(), key=lambda kv: kv[1]["ms"])[0] if fam else None
         if dom:
             d = fam[dom]
@@ -305,14 +310,18 @@ def our_arm(args, rank: int, world: int) -> None:
                 "kernel": dom, "bound": "tensor", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None,
                 "traffic": traffic,
-                "peak_source": "cuBLAS FP64 dgemm 8192^3 measured in this run (MEASURED_PEAKS.json "
-                               "has no FP64 entry; tcgen05 has no f64 kind)",
+                "peak_source": ("max of cuBLAS FP64 dgemm 8192^3 measured in this run "
+                                f"({cublas_peak}) and the FP64 pipe issue rate 2 DFMA/clk/SM x "
+                                f"{sms} SMs x {sm_mhz} MHz ({pipe_peak:.3f}); MEASURED_PEAKS.json "
+                                "has no FP64 entry and tcgen05 has no f64 kind"),
                 "share_of_step": d["ms"] / ms_total,
                 "algorithmic": "2*m*n*k flops per trailing-update/trsm GEMM launch"}
         if not args.quick:
             result["gemm_fp64_config1"] = gemm_subbench(torch, fg, dev)
         if not args.quick and not args.no_mixed:
             result["mixed_config3"] = mixed_subbench(torch, fg, dev, n=args.mixed_n)
+        if not args.quick and not args.no_batched:
+            result["batched_config5"] = batched_subbench(torch, fg, dev, count=args.batch_count)
         # -- e2e through the Fortran ABI with pinned host buffers
         if not args.no_e2e:
             result["e2e"] = e2e_dgesv(torch, fg, A0, b0, args)
@@ -409,6 +418,127 @@ def mixed_subbench(torch, fg, dev, n=16384, reps=3):
     return out
 
 
+def batched_subbench(torch, fg, dev, count=20000, reps=3, loop_sample=2000):
+    """Batched configuration: `count` independent FP64 systems, n log-uniform
+    in [8, 512], entries uniform[-1,1] + (n/4) I, k uniform in {1, 4, 16}.
+    Times one plan execution (one persistent launch, graph replay) in FP64 and
+    in FP32 LU + FP64 refinement, against a per-matrix flens_gb300_dgesv loop
+    (timed on the first `loop_sample` matrices and scaled), and reports
+    p50/p99 normwise backward errors."""
+    import ctypes
+    import numpy as np
+    rng = np.random.default_rng(55)
+    n = np.floor(np.exp(rng.uniform(np.log(8), np.log(512.999), size=count))).astype(np.int32)
+    k = rng.choice(np.array([1, 4, 16], dtype=np.int32), size=count)
+    a_off = np.concatenate([[0], np.cumsum(n.astype(np.int64) ** 2)])
+    b_off = np.concatenate([[0], np.cumsum(n.astype(np.int64) * k)])
+    g = torch.Generator(device=dev)
+    g.manual_seed(77)
+    F0 = torch.rand(int(a_off[-1]), generator=g, dtype=torch.float64, device=dev).mul_(2).sub_(1)
+    diag = np.concatenate([a_off[i] + np.arange(n[i]) * (n[i] + 1) for i in range(count)])
+    shift = np.concatenate([np.full(n[i], n[i] / 4.0) for i in range(count)])
+    F0[torch.from_numpy(diag).to(dev)] += torch.from_numpy(shift).to(dev)
+    G0 = torch.rand(int(b_off[-1]), generator=g, dtype=torch.float64, device=dev).mul_(2).sub_(1)
+    F, G = F0.clone(), G0.clone()
+    P = torch.zeros(int(n.sum()), dtype=torch.int32, device=dev)
+    p_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))])
+    pa = (F.data_ptr() + 8 * a_off[:-1]).astype(np.uint64)
+    pb = (G.data_ptr() + 8 * b_off[:-1]).astype(np.uint64)
+    pp = (P.data_ptr() + 4 * p_off[:-1]).astype(np.uint64)
+    lda = n.copy()
+    info = torch.zeros(count, dtype=torch.int32, device=dev)
+    iters = torch.zeros(count, dtype=torch.int32, device=dev)
+    berr = torch.zeros(count, dtype=torch.float64, device=dev)
+    L = fg.lib()
+    vp = ctypes.c_void_p
+    f = L.flens_gb300_dgesv_batched_plan
+    f.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int, vp, vp, ctypes.c_int,
+                  vp, ctypes.POINTER(ctypes.c_void_p)]
+    f.restype = ctypes.c_int
+    L.flens_gb300_batched_execute.argtypes = [vp, vp]
+    L.flens_gb300_batched_destroy.argtypes = [vp]
+    L.flens_gb300_batched_team.argtypes = [vp, ctypes.c_int]
+    L.flens_gb300_batched_team.restype = ctypes.c_int
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    flops = float(np.sum(2.0 / 3.0 * n.astype(np.float64) ** 3 + 2.0 * n.astype(np.float64) ** 2 * k))
+    eps = float(np.finfo(np.float64).eps)
+    out = {"workload": f"{count} dgesv, n log-uniform [8,512], k in {{1,4,16}}", "count": count,
+           "flop": flops, "variants": {}}
+
+    def berr_sample(sample):
+        errs = []
+        for i in sample:
+            ni, ki = int(n[i]), int(k[i])
+            A = F0[a_off[i]:a_off[i + 1]].view(ni, ni).t()
+            B = G0[b_off[i]:b_off[i + 1]].view(ki, ni).t()
+            X = G[b_off[i]:b_off[i + 1]].view(ki, ni).t()
+            R = B - A @ X
+            den = A.abs().sum(1).max() * X.abs().amax(0) + B.abs().amax(0)
+            errs.append((R.abs().amax(0) / den).max().item())
+        return np.array(errs)
+
+    sample = rng.choice(count, size=min(1000, count), replace=False)
+    for prec, name in ((0, "fp64"), (1, "fp32_lu+fp64_ir")):
+        plan = ctypes.c_void_p()
+        t0 = time.time()
+        st = f(count, n.ctypes.data, k.ctypes.data, pa.ctypes.data, lda.ctypes.data, pp.ctypes.data,
+               pb.ctypes.data, lda.ctypes.data, info.data_ptr(), prec, iters.data_ptr(),
+               berr.data_ptr(), 10, sp, ctypes.byref(plan))
+        plan_s = time.time() - t0
+        if st != 0:
+            out["variants"][name] = {"error": fg.last_error()}
+            continue
+        times = []
+        for rep in range(1 + reps):
+            F.copy_(F0)
+            G.copy_(G0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            L.flens_gb300_batched_execute(plan, sp)
+            e1.record(stream)
+            e1.synchronize()
+            if rep > 0:
+                times.append(e0.elapsed_time(e1))
+        teams = [L.flens_gb300_batched_team(plan, b) for b in range(8)]
+        L.flens_gb300_batched_destroy(plan)
+        ms = sum(times) / len(times)
+        inf = info.cpu().numpy()
+        be = berr_sample(sample) / (n[sample] * eps)
+        v = {"ms": ms, "solves_per_s": count / (ms * 1e-3), "gflops": flops / (ms * 1e-3) / 1e9,
+             "plan_s": round(plan_s, 2), "teams_per_bucket": teams, "info_nonzero": int((inf != 0).sum()),
+             "backward_error_over_n_eps_p50": float(np.percentile(be, 50)),
+             "backward_error_over_n_eps_p99": float(np.percentile(be, 99)),
+             "backward_error_sample": f"{len(sample)} matrices"}
+        if prec == 1:
+            it = iters.cpu().numpy()
+            v["refinement_steps_mean"] = float(it[it >= 0].mean()) if (it >= 0).any() else None
+            v["fp64_fallback"] = int((it < 0).sum())
+        out["variants"][name] = v
+    # per-matrix launch loop (the baseline the batched launch must beat)
+    F.copy_(F0)
+    G.copy_(G0)
+    ipiv = torch.zeros(512, dtype=torch.int32, device=dev)
+    inf1 = torch.zeros(1, dtype=torch.int32, device=dev)
+    m = min(loop_sample, count)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(m):
+        ni, ki = int(n[i]), int(k[i])
+        L.flens_gb300_dgesv(ni, ki, ctypes.c_void_p(int(pa[i])), ni, ctypes.c_void_p(ipiv.data_ptr()),
+                            ctypes.c_void_p(int(pb[i])), ni, ctypes.c_void_p(inf1.data_ptr()), sp)
+    torch.cuda.synchronize()
+    loop_s = (time.perf_counter() - t0) * count / m
+    out["per_matrix_loop"] = {"solves_per_s": count / loop_s, "sample": f"first {m} matrices, scaled"}
+    fp64 = out["variants"].get("fp64", {})
+    if "solves_per_s" in fp64:
+        out["speedup_vs_loop_fp64"] = fp64["solves_per_s"] / out["per_matrix_loop"]["solves_per_s"]
+    del F0, F, G0, G, P
+    torch.cuda.empty_cache()
+    return out
+
+
 def e2e_dgesv(torch, fg, A0, b0, args):
     import ctypes
     import numpy as np
@@ -468,6 +598,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--mixed-n", type=int, default=16384)
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=20000)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
