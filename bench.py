@@ -302,10 +302,15 @@ def our_arm(args, rank: int, world: int) -> None:
         if dom:
             d = fam[dom]
             achieved = d["flops"] / (d["ms"] * 1e-3) / 1e12
+            # DRAM bytes per launch: the ncu-measured DRAM/algorithmic ratio of
+            # this kernel (profiles/traffic.json) times its per-launch
+            # algorithmic bytes in this run
             traffic = None
             tpath = os.path.join(ROOT, "profiles", "traffic.json")
             if os.path.exists(tpath):
-                traffic = json.load(open(tpath)).get(f"{dom}@n={n}")
+                ratio = json.load(open(tpath)).get(dom, {}).get("dram_over_algorithmic")
+                if ratio and d["launches"]:
+                    traffic = ratio * d["bytes"] / d["launches"]
             result["roofline"] = {
                 "kernel": dom, "bound": "tensor", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None,
@@ -586,6 +591,46 @@ def cpu_baseline(n):
             "gflops": f_sample / t / 1e9}
 
 
+def only(args):
+    """One sub-benchmark on its own, for ncu captures of a single kernel family."""
+    import torch
+    import flens_gb300 as fg
+    dev = torch.device("cuda:0")
+    if args.only == "tc_gemm":
+        import ctypes
+        m, n, k = (int(x) for x in args.tc_shape.split(","))
+        g = torch.Generator(device=dev)
+        g.manual_seed(1)
+        A = torch.rand((k, m), generator=g, dtype=torch.float32, device=dev).t()
+        B = torch.rand((n, k), generator=g, dtype=torch.float32, device=dev).t()
+        C = torch.rand((n, m), generator=g, dtype=torch.float32, device=dev).t()
+        f = fg.lib().flens_gb300_sgemm_tc
+        f.argtypes = [ctypes.c_int, ctypes.c_char, ctypes.c_char] + [ctypes.c_int] * 3 + [
+            ctypes.c_float, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+            ctypes.c_float, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        times = []
+        for rep in range(1 + args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            st = f(1, b"N", b"N", m, n, k, -1.0, A.data_ptr(), m, B.data_ptr(), k, 1.0,
+                   C.data_ptr(), m, s)
+            e1.record()
+            e1.synchronize()
+            assert st == 0, fg.last_error()
+            if rep:
+                times.append(e0.elapsed_time(e1))
+        ms = sum(times) / len(times)
+        print(json.dumps({"only": "tc_gemm", "shape": [m, n, k], "precision": "bf16", "ms": ms,
+                          "tflops": 2.0 * m * n * k / (ms * 1e-3) / 1e12,
+                          "c_traffic_gbs": 8.0 * m * n / (ms * 1e-3) / 1e9}))
+    elif args.only == "batched":
+        out = batched_subbench(torch, fg, dev, count=args.batch_count, reps=1, loop_sample=50)
+        print(json.dumps(out))
+    else:
+        print(json.dumps(mixed_subbench(torch, fg, dev, n=args.mixed_n, reps=1)))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -600,9 +645,15 @@ def main():
     ap.add_argument("--mixed-n", type=int, default=16384)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-count", type=int, default=20000)
+    ap.add_argument("--only", choices=["tc_gemm", "batched", "mixed"],
+                    help="run one sub-benchmark and print its JSON (for profiling)")
+    ap.add_argument("--tc-shape", default="8192,8192,256", help="M,N,K for --only tc_gemm")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.only:
+        only(args)
+        return
     if args.impl == "reference":
         reference_arm(args, rank)
     else:
