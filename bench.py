@@ -325,6 +325,8 @@ def our_arm(args, rank: int, world: int) -> None:
             result["gemm_fp64_config1"] = gemm_subbench(torch, fg, dev)
         if not args.quick and not args.no_mixed:
             result["mixed_config3"] = mixed_subbench(torch, fg, dev, n=args.mixed_n)
+        if not args.quick and not args.no_split:
+            result["split_gemm_config4"] = split_subbench(torch, fg, dev, cublas_tflops=cublas_peak)
         if not args.quick and not args.no_batched:
             result["batched_config5"] = batched_subbench(torch, fg, dev, count=args.batch_count)
         # -- e2e through the Fortran ABI with pinned host buffers
@@ -420,6 +422,97 @@ def mixed_subbench(torch, fg, dev, n=16384, reps=3):
         del A, b, X
     del U, V
     torch.cuda.empty_cache()
+    return out
+
+
+def measured_peak(key):
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        v = json.load(open(path)).get(key)
+        if v:
+            return float(v), "measured"
+    return {"bf16_tflops": 1900.0, "hbm_gbs": 6800.0}[key], "fallback"
+
+
+def wide_range_pair(torch, n, E, seed, dev):
+    """A, B (n x n, column-major FP64): u * 2^e, u uniform[-1,1], e uniform
+    integer in [-E, E] (seeded torch generator)."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    out = []
+    for _ in range(2):
+        u = torch.rand((n, n), generator=g, dtype=torch.float64, device=dev).mul_(2).sub_(1)
+        e = torch.randint(-E, E + 1, (n, n), generator=g, device=dev).to(torch.float64)
+        out.append(torch.ldexp(u, e).t())       # column-major view
+        del u, e
+    return out
+
+
+def split_subbench(torch, fg, dev, n=8192, Es=(0, 16, 48), reps=5, ref_slices=14,
+                   cublas_tflops=None):
+    """Split-precision FP64 GEMM configuration: C = A*B, M = N = K = n, entries
+    u*2^e with e uniform in [-E, E].  Times flens_gb300_dgemm_split (stats,
+    slicing, exact BF16 tcgen05 products, FP64 recombination; inputs 512 MiB
+    each > L2) and, beside it, the plain FP64 dgemm kernel.  Accuracy: max
+    elementwise relative error of both against the same kernel run with
+    `ref_slices` slices (7*ref_slices bits per operand; the kernel matches its
+    NumPy model bit for bit and the reference's gemm to 1e-13 in the tests)."""
+    import numpy as np
+    peak, peak_src = measured_peak("bf16_tflops")
+    out = {"workload": f"dgemm {n}^3 FP64 in/out, entries u*2^e, e in [-E,E]",
+           "fp64_equivalent_flops": 2.0 * n ** 3, "l2": "inputs 512 MiB each > L2 (no flush)",
+           "accuracy_reference": f"same kernel with {ref_slices} slices ({7 * ref_slices} bits)",
+           "per_E": {}}
+    stream = torch.cuda.current_stream()
+    plain_ms = None
+    for E in Es:
+        A, B = wide_range_pair(torch, n, E, 4000 + E, dev)
+        C = torch.zeros((n, n), dtype=torch.float64, device=dev).t()
+        S = fg.dgemm_split_dev("N", "N", 1.0, A, B, 0.0, C)      # warm-up, picks S
+        torch.cuda.synchronize()
+        fg.timing_enable(True)
+        times = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fg.dgemm_split_dev("N", "N", 1.0, A, B, 0.0, C)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        fam = fg.timing_read()
+        fg.timing_enable(False)
+        ms = sum(times) / len(times)
+        sp = fam.get("split_gemm", {"ms": 0.0, "flops": 0.0, "launches": 0})
+        k_ms = sp["ms"] / max(1, sp["launches"])
+        tc_tflops = sp["flops"] / max(1e-9, sp["ms"] * 1e-3) / 1e12
+        # accuracy against the many-slice result
+        Cref = torch.zeros((n, n), dtype=torch.float64, device=dev).t()
+        fg.dgemm_split_dev("N", "N", 1.0, A, B, 0.0, Cref, slices=ref_slices)
+        C64 = torch.zeros((n, n), dtype=torch.float64, device=dev).t()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fg.dgemm_dev("N", "N", 1.0, A, B, 0.0, C64)
+        e1.record(stream)
+        e1.synchronize()
+        plain_ms = e0.elapsed_time(e1)
+        den = Cref.abs()
+        nz = den > 0
+        rel_split = ((C - Cref).abs()[nz] / den[nz]).max().item()
+        rel_plain = ((C64 - Cref).abs()[nz] / den[nz]).max().item()
+        norm_split = ((C - Cref).abs().max() / den.max()).item()
+        out["per_E"][str(E)] = {
+            "slices": S, "ms": ms, "fp64_equiv_tflops": 2.0 * n ** 3 / (ms * 1e-3) / 1e12,
+            "products_kernel_ms": k_ms, "tensor_tflops": tc_tflops,
+            "tensor_frac_of_bf16_peak": tc_tflops / peak,
+            "max_rel_err_split": rel_split, "max_rel_err_plain_fp64": rel_plain,
+            "normwise_rel_err_split": norm_split,
+            "speedup_vs_plain_fp64": plain_ms / ms,
+            "kernels_ms_per_call": {k: v["ms"] / reps for k, v in fam.items() if v["ms"] > 0}}
+        del A, B, C, Cref, C64
+        torch.cuda.empty_cache()
+    out["plain_fp64_dgemm"] = {"ms": plain_ms, "tflops": 2.0 * n ** 3 / (plain_ms * 1e-3) / 1e12,
+                               "cublas_fp64_tflops": cublas_tflops}
+    out["bf16_peak_tflops"] = {"value": peak, "source": f"{peak_src} (MEASURED_PEAKS.json bf16_tflops)"}
     return out
 
 
@@ -627,6 +720,10 @@ def only(args):
     elif args.only == "batched":
         out = batched_subbench(torch, fg, dev, count=args.batch_count, reps=1, loop_sample=50)
         print(json.dumps(out))
+    elif args.only == "split":
+        out = split_subbench(torch, fg, dev, n=args.split_n, Es=(args.split_e,), reps=args.steps,
+                             ref_slices=args.split_ref_slices)
+        print(json.dumps(out))
     else:
         print(json.dumps(mixed_subbench(torch, fg, dev, n=args.mixed_n, reps=1)))
 
@@ -644,8 +741,12 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--mixed-n", type=int, default=16384)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-split", action="store_true")
+    ap.add_argument("--split-n", type=int, default=8192, help="n for --only split")
+    ap.add_argument("--split-e", type=int, default=48, help="exponent range E for --only split")
+    ap.add_argument("--split-ref-slices", type=int, default=14, help="reference slices for --only split")
     ap.add_argument("--batch-count", type=int, default=20000)
-    ap.add_argument("--only", choices=["tc_gemm", "batched", "mixed"],
+    ap.add_argument("--only", choices=["tc_gemm", "batched", "mixed", "split"],
                     help="run one sub-benchmark and print its JSON (for profiling)")
     ap.add_argument("--tc-shape", default="8192,8192,256", help="M,N,K for --only tc_gemm")
     args = ap.parse_args()

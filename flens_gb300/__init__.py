@@ -83,6 +83,9 @@ def lib() -> ctypes.CDLL:
     L.flens_gb300_sync.argtypes = [_v]
     L.flens_gb300_dgetrs_noalloc.argtypes = [_c, _i, _i, _v, _i, _v, _v, _i, _v]
     L.flens_gb300_dgetrs_noalloc.restype = _i
+    L.flens_gb300_dgemm_split.argtypes = [_c, _c, _i, _i, _i, _d, _v, _i, _v, _i, _d, _v, _i, _i,
+                                          ctypes.POINTER(ctypes.c_int), _v]
+    L.flens_gb300_dgemm_split.restype = _i
     for f in ("flens_gb300_dgemm", "flens_gb300_dtrsm", "flens_gb300_dgetrf",
               "flens_gb300_dgetrs", "flens_gb300_dgesv", "flens_gb300_sync"):
         getattr(L, f).restype = _i
@@ -109,7 +112,7 @@ def last_error() -> str:
 
 
 # ------------------------------------------------------ instrumentation ---
-N_FAMILIES = 8
+N_FAMILIES = 9
 
 
 def launch_count() -> int:
@@ -200,6 +203,8 @@ def dgesv(A: np.ndarray, B: np.ndarray):
 # -------------------------------------------------------- device (torch) ---
 def _colmajor(t):
     """(pointer, rows, cols, ld) of a column-major CUDA float64 tensor."""
+    if t.dim() == 2 and t.numel() == 0:
+        return t.data_ptr(), t.shape[0], t.shape[1], max(1, t.shape[0])
     if t.dim() != 2 or t.stride(0) != 1:
         raise ValueError("expected a 2-D column-major tensor (stride(0) == 1)")
     return t.data_ptr(), t.shape[0], t.shape[1], max(1, t.stride(1), t.shape[0])
@@ -235,6 +240,22 @@ def dgemm_dev(transA, transB, alpha, A, B, beta, C, stream=None):
     _check(lib().flens_gb300_dgemm(transA.encode(), transB.encode(), m, n, k, alpha, pa, lda,
                                    pb, ldb, beta, pc, ldc, _stream(stream)), "flens_gb300_dgemm")
     return C
+
+
+def dgemm_split_dev(transA, transB, alpha, A, B, beta, C, slices=0, stream=None):
+    """FP64-accurate C <- beta*C + alpha*op(A)*op(B) from exact BF16 tensor-core
+    products of exponent-aligned slices (device tensors, column-major).
+    slices = 0 picks the slice count from the data.  Returns the slice count
+    used (-1: the inputs needed the plain FP64 kernel).  Synchronises."""
+    pa, ra, ca, lda = _colmajor(A)
+    pb, rb, cb, ldb = _colmajor(B)
+    pc, m, n, ldc = _colmajor(C)
+    k = ca if transA.upper() == "N" else ra
+    used = ctypes.c_int(0)
+    _check(lib().flens_gb300_dgemm_split(transA.encode(), transB.encode(), m, n, k, alpha, pa, lda,
+                                         pb, ldb, beta, pc, ldc, slices, ctypes.byref(used),
+                                         _stream(stream)), "flens_gb300_dgemm_split")
+    return used.value
 
 
 def dtrsm_dev(side, uplo, transA, diag, alpha, A, B, stream=None):

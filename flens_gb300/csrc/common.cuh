@@ -88,7 +88,8 @@ enum Family : int {
     kFamTcGemm = 5,   // tcgen05 low-precision GEMM
     kFamRefine = 6,   // residual / refinement / Krylov helpers
     kFamBatched = 7,  // batched LU
-    kFamCount = 8
+    kFamSplit = 8,    // split-precision FP64 GEMM (slicing + tensor-core products)
+    kFamCount = 9
 };
 
 struct KTimer {

@@ -265,6 +265,7 @@ FG_API int flens_gb300_timing_read(int family, double *ms, long long *launches, 
 
 FG_API const char *flens_gb300_family_name(int family) {
     static const char *names[fg::kFamCount] = {"dgemm_fp64", "lu_panel", "laswp", "trsm_diag",
-                                               "aux", "tc_gemm", "refine", "batched_lu"};
+                                               "aux", "tc_gemm", "refine", "batched_lu",
+                                               "split_gemm"};
     return (family >= 0 && family < fg::kFamCount) ? names[family] : "";
 }

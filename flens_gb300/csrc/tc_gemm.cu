@@ -6,26 +6,13 @@
 // exposed as flens_gb300_sgemm_tc.  The reference has no low-precision path
 // (its float gemm is the same generic loop as for double,
 // cxxblas/level3/gemm.tcc:42-190); this is the contraction its FP32 `mm`
-// would perform, carried out on the 5th-generation tensor cores.
-//
-// Kernel shape: persistent, one CTA per SM over 128 x BN output tiles
-// (BN = 256), 320 threads:
-//   warp 0 lane 0  TMA producer: 128B-swizzled K-major tiles of A (128 rows)
-//                  and B (BN rows) into a STAGES-deep shared-memory ring,
-//                  one mbarrier (expect_tx) per stage;
-//   warp 1         allocates 2*BN TMEM columns (two accumulators); lane 0
-//                  issues tcgen05.mma (M=128, N=BN, K=32 bytes per
-//                  instruction), commits each stage back to the producer and
-//                  each finished tile to the epilogue;
-//   warps 2-9      epilogue: tcgen05.ld 32x32b.x32 chunks of their TMEM lane
-//                  quarter (= tile rows), C = alpha*acc*(sa_i*sb_j) + beta*C,
-//                  coalesced column-major stores, then release the
-//                  accumulator to the MMA warp.
-// Every wait is bounded (kMbarSpinLimit); on a timeout the kernel sets the
-// status word, lets in-flight copies land, frees its TMEM and returns.
-#include "common.cuh"
+// would perform, carried out on the 5th-generation tensor cores.  The kernel
+// (persistent, warp-specialised TMA / MMA / epilogue) is tc::tc_kernel of
+// tcgen05.cuh with the FP32 epilogue below: one work item per tile over the
+// whole K, C = alpha*acc*(sa_i*sb_j) + beta*C with coalesced column-major
+// loads and stores.
+#include "tcgen05.cuh"
 
-#include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_fp8.h>
@@ -34,311 +21,44 @@
 
 namespace fg {
 
-// Precisions of the tensor-core contraction.  kTcF32x3 is FP32-accurate: each
-// operand is split into a TF32 head and a TF32 tail and three TF32 products
-// (head*head + head*tail + tail*head) are accumulated.  kTcTF32Lo is only a
-// conversion mode (the tail of the split).
-enum TcKind : int { kTcTF32 = 0, kTcBF16 = 1, kTcFP8 = 2, kTcF32x3 = 3, kTcTF32Lo = 4 };
-
 namespace {
 
-constexpr int TC_BM = 128;
-constexpr int TC_BN = 256;
-constexpr int TC_STAGES = 4;
-constexpr int TC_THREADS = 320;                   // 10 warps: TMA, MMA, 8 epilogue
-constexpr uint32_t kMbarSpinLimit = 1u << 20;
-constexpr uint32_t TC_A_BYTES = TC_BM * 128;       // one stage of A: 128 rows x 128 B
-constexpr uint32_t TC_B_BYTES = TC_BN * 128;       // one stage of B: BN rows x 128 B
-constexpr size_t TC_SMEM = 1024 + (size_t)TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + 256;
+using tc::BM;
+using tc::BN;
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
+// FP32 output: C = alpha * acc * (sa_i * sb_j) + beta * C, one group over K.
+struct EpiF32 {
+    float alpha, beta;
+    float *C;
+    int ldc;
+    const float *scale_a, *scale_b;
+    int nkb;                                     // k-blocks of the whole K
 
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait on an mbarrier phase; false (and the status bit) on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status) {
-    for (uint32_t i = 0; i < kMbarSpinLimit; ++i) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (i > 32) __nanosleep(64);
+    __device__ int groups() const { return 1; }
+    __device__ void group(int, int &ka, int &kb, int &nk) const {
+        ka = 0;
+        kb = 0;
+        nk = nkb;
     }
-    atomicOr(status, kDevMbarTimeout);
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_2d(const CUtensorMap *map, uint64_t *bar, void *dst,
-                                            int x, int y) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
-        "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
-        "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
-        : "memory");
-}
-
-// UMMA shared-memory descriptor, K-major operand with 128-byte swizzle:
-// rows of 128 B, 8-row (1024 B) swizzle atoms stacked along M/N (SBO = 1024),
-// LBO unused for this layout, fixed 0b001 at bits 46-48, layout 2 = SW128.
-__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)1 << 16;
-    d |= (uint64_t)(1024u >> 4) << 32;
-    d |= (uint64_t)1 << 46;
-    d |= (uint64_t)2 << 61;
-    return d;
-}
-
-// Instruction descriptor: D = F32 (bits 4-5 = 1), A/B format at bits 7-9 and
-// 10-12, both K-major (bits 15/16 = 0), N>>3 at bits 17-22, M>>4 at 24-28.
-__host__ __device__ constexpr uint32_t idesc_for(int kind, int M, int N) {
-    return (1u << 4) | ((uint32_t)(kind == kTcTF32 ? 2 : kind == kTcBF16 ? 1 : 0) << 7) |
-           ((uint32_t)(kind == kTcTF32 ? 2 : kind == kTcBF16 ? 1 : 0) << 10) |
-           ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-template <int KIND>
-__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
-                                     uint32_t idesc, uint32_t accumulate) {
-    if (KIND == kTcBF16) {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-    } else if (KIND == kTcTF32) {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-    } else {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-            "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-    }
-}
-
-__device__ __forceinline__ void umma_commit(uint64_t *bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                     smem_u32(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() {
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-
-// 32 lanes x 32 columns of 32-bit accumulators: thread i gets row (lane i)
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-          "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
-// Persistent kernel: one CTA per SM walks the output tiles
-// (tile = blockIdx.x + i*gridDim.x, m fastest), two TMEM accumulators of
-// TC_BN columns each, so the epilogue of one tile overlaps the TMA loads and
-// MMAs of the next.  Roles:
-//   warp 0 lane 0   TMA producer over (tile, k-block), STAGES-deep smem ring;
-//   warp 1          TMEM allocation; lane 0 issues the MMAs of a tile into
-//                   accumulator (tile & 1) once the epilogue has released it;
-//   warps 2..9      epilogue: warp w drains TMEM lanes 32*(w%4).. (the lane
-//                   quarter a warp may access) for column half (w-2)/4.
-template <int KIND>
-__global__ void __launch_bounds__(TC_THREADS, 1)
-tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-               int M, int N, int K, float alpha, float beta, float *__restrict__ C, int ldc,
-               const float *__restrict__ scale_a, const float *__restrict__ scale_b,
-               int *__restrict__ status) {
-    constexpr int ELEM = KIND == kTcTF32 ? 4 : KIND == kTcBF16 ? 2 : 1;
-    constexpr int BK = 128 / ELEM;               // elements per 128-byte row (one k-block)
-    constexpr int KSTEPS = 4;                    // 32 bytes of K per MMA
-    constexpr int EPI_WARPS = 8;
-    extern __shared__ uint8_t smem_raw[];
-    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t *sA = smem;
-    uint8_t *sB = smem + TC_STAGES * TC_A_BYTES;
-    uint64_t *full = (uint64_t *)(sB + TC_STAGES * TC_B_BYTES);
-    uint64_t *empty = full + TC_STAGES;
-    uint64_t *tfull = empty + TC_STAGES;         // [2] accumulator ready
-    uint64_t *tempty = tfull + 2;                // [2] accumulator drained
-    uint32_t *tmem_slot = (uint32_t *)(tempty + 2);
-    __shared__ int s_abort;
-
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int tiles_m = (M + TC_BM - 1) / TC_BM, tiles_n = (N + TC_BN - 1) / TC_BN;
-    const int ntiles = tiles_m * tiles_n;
-    const int nkb = (K + BK - 1) / BK;
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < TC_STAGES; ++s) {
-            mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1);
-        }
-        for (int b = 0; b < 2; ++b) {
-            mbar_init(&tfull[b], 1);
-            mbar_init(&tempty[b], EPI_WARPS);
-        }
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        s_abort = 0;
-    }
-    if (warp == 1) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                         smem_u32(tmem_slot)),
-                     "r"((uint32_t)(2 * TC_BN))
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
-
-    if (warp == 0) {
-        if (lane == 0) {
-            // ---- TMA producer
-            int q = 0, issued = 0;
-            bool ok = true;
-            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-                const int m0 = (t % tiles_m) * TC_BM, n0 = (t / tiles_m) * TC_BN;
-                for (int kb = 0; kb < nkb; ++kb, ++q) {
-                    const int s = q % TC_STAGES;
-                    const uint32_t ph = (uint32_t)(q / TC_STAGES) & 1u;
-                    if (s_abort || !mbar_wait(&empty[s], ph ^ 1u, status)) {
-                        s_abort = 1;
-                        ok = false;
-                        break;
-                    }
-                    mbar_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
-                    tma_load_2d(&tmA, &full[s], sA + s * TC_A_BYTES, kb * BK, m0);
-                    tma_load_2d(&tmB, &full[s], sB + s * TC_B_BYTES, kb * BK, n0);
-                    ++issued;
-                }
-            }
-            if (!ok) {
-                // let the copies already issued land before the CTA can exit
-                for (int r = (issued > TC_STAGES ? issued - TC_STAGES : 0); r < issued; ++r)
-                    mbar_wait(&full[r % TC_STAGES], (uint32_t)(r / TC_STAGES) & 1u, status);
-            }
-        }
-    } else if (warp == 1) {
-        if (lane == 0) {
-            // ---- MMA issuer
-            const uint32_t idesc = idesc_for(KIND, TC_BM, TC_BN);
-            int q = 0, i = 0;
-            bool ok = true;
-            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++i) {
-                const int b = i & 1;
-                const uint32_t acc = tmem + (uint32_t)(b * TC_BN);
-                if (!mbar_wait(&tempty[b], ((uint32_t)(i >> 1) & 1u) ^ 1u, status)) {
-                    s_abort = 1;
-                    break;
-                }
-                tc_fence_after();
-                for (int kb = 0; kb < nkb; ++kb, ++q) {
-                    const int s = q % TC_STAGES;
-                    const uint32_t ph = (uint32_t)(q / TC_STAGES) & 1u;
-                    if (s_abort || !mbar_wait(&full[s], ph, status)) {
-                        s_abort = 1;
-                        ok = false;
-                        break;
-                    }
-                    tc_fence_after();
-                    const uint32_t a0 = smem_u32(sA + s * TC_A_BYTES);
-                    const uint32_t b0 = smem_u32(sB + s * TC_B_BYTES);
+    __device__ void apply(int, int row, bool row_ok, int col, int ncol,
+                          const uint32_t (&r)[32]) const {
+        if (!row_ok) return;
+        const float sa = scale_a != nullptr ? scale_a[row] : 1.0f;
+        float *crow = C + (size_t)row + (size_t)col * ldc;
+        // all 32 loads of C in flight before any store
+        float cv[32];
 #pragma unroll
-                    for (int kk = 0; kk < KSTEPS; ++kk)
-                        umma<KIND>(acc, sdesc_sw128(a0 + kk * 32), sdesc_sw128(b0 + kk * 32), idesc,
-                                   (kb | kk) != 0 ? 1u : 0u);
-                    umma_commit(&empty[s]);
-                }
-                if (ok) umma_commit(&tfull[b]);
+        for (int j = 0; j < 32; ++j) cv[j] = (j < ncol) ? __ldcs(crow + (size_t)j * ldc) : 0.0f;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            if (j < ncol) {
+                float accv = __uint_as_float(r[j]);
+                if (scale_b != nullptr) accv *= sa * scale_b[col + j];
+                __stcs(crow + (size_t)j * ldc, fmaf(alpha, accv, beta * cv[j]));
             }
         }
-    } else {
-        // ---- epilogue
-        const int ew = warp - 2;                 // 0..7
-        const int quarter = warp & 3;            // TMEM lane quarter this warp may access
-        const int half = ew >> 2;                // column half
-        int i = 0;
-        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
-            const int b = i & 1;
-            const int m0 = (t % tiles_m) * TC_BM, n0 = (t / tiles_m) * TC_BN;
-            const bool have = mbar_wait(&tfull[b], (uint32_t)(i >> 1) & 1u, status);
-            if (!have) {
-                s_abort = 1;
-                break;
-            }
-            tc_fence_after();
-            const int row = m0 + quarter * 32 + lane;
-            const float sa = (scale_a != nullptr && row < M) ? scale_a[row] : 1.0f;
-            const uint32_t base = tmem + (uint32_t)(b * TC_BN) + ((uint32_t)(quarter * 32) << 16);
-            for (int c0 = half * (TC_BN / 2); c0 < (half + 1) * (TC_BN / 2); c0 += 32) {
-                if (n0 + c0 >= N) break;         // uniform across the warp
-                uint32_t r[32];
-                tmem_ld32(base + (uint32_t)c0, r);
-                if (row < M) {
-                    float *crow = C + (size_t)row + (size_t)(n0 + c0) * ldc;
-                    const int ncol = min(32, N - (n0 + c0));
-                    // all 32 loads of C in flight before any store
-                    float cv[32];
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) cv[j] = (j < ncol) ? __ldcs(crow + (size_t)j * ldc) : 0.0f;
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        if (j < ncol) {
-                            float accv = __uint_as_float(r[j]);
-                            if (scale_b != nullptr) accv *= sa * scale_b[n0 + c0 + j];
-                            __stcs(crow + (size_t)j * ldc, fmaf(alpha, accv, beta * cv[j]));
-                        }
-                    }
-                }
-            }
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
-            if (s_abort) break;
-        }
     }
-    tc_fence_before();
-    __syncthreads();
-    if (warp == 1) {
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                     "r"((uint32_t)(2 * TC_BN))
-                     : "memory");
-    }
-}
+};
 
 // ------------------------------------------------------------ operands ----
 // out(r, k) = round(in(r, k) * inv_scale[r]) with in(r, k) = in[r + k*ld]
@@ -436,7 +156,11 @@ __global__ void sscale_kernel(int m, int n, float beta, float *__restrict__ C, i
     }
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+}  // namespace
+
+namespace tc {
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     static std::once_flag once;
     std::call_once(once, [] {
@@ -450,8 +174,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// 2-D map over a K-major operand: inner dim = K (elements), outer = rows.
-int make_map(CUtensorMap *map, int kind, const void *base, int rows, int K, int ldo, int box_rows) {
+int make_kmajor_map(CUtensorMap *map, int kind, const void *base, int rows, int K, int ldo, int box_rows) {
     PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
     if (!fn) {
         set_last_error("cuTensorMapEncodeTiled is not available from the driver");
@@ -475,7 +198,7 @@ int make_map(CUtensorMap *map, int kind, const void *base, int rows, int K, int 
     return kOk;
 }
 
-}  // namespace
+}  // namespace tc
 
 // K-major leading dimension (elements) for `kind`: K rounded up to 16 bytes.
 static int gemm_kind(int kind) { return (kind == kTcF32x3 || kind == kTcTF32Lo) ? kTcTF32 : kind; }
@@ -535,24 +258,21 @@ int tc_gemm_launch(int kind, int M, int N, int K, float alpha, const void *A_lp,
         return kErrUnsupported;
     }
     CUtensorMap ma, mb;
-    int st = make_map(&ma, kind, A_lp, M, K, lda, TC_BM);
+    int st = tc::make_kmajor_map(&ma, kind, A_lp, M, K, lda, BM);
     if (st != kOk) return st;
-    if ((st = make_map(&mb, kind, B_lp, N, K, ldb, TC_BN)) != kOk) return st;
-    static bool attr[3] = {false, false, false};
-    const int ntiles = ceil_div(M, TC_BM) * ceil_div(N, TC_BN);
+    if ((st = tc::make_kmajor_map(&mb, kind, B_lp, N, K, ldb, BN)) != kOk) return st;
+    const int ntiles = ceil_div(M, BM) * ceil_div(N, BN);
     const int sms = num_sms();
     const dim3 grid(ntiles < sms ? ntiles : sms);
+    const int bk = 128 / (int)tc_elem_bytes(kind);
+    const EpiF32 epi{alpha, beta, C, ldc, scale_a, scale_b, ceil_div(K, bk)};
     KTimer kt(kFamTcGemm, stream, 2.0 * M * (double)N * K,
               tc_elem_bytes(kind) * ((double)M * K + (double)N * K) + 8.0 * M * (double)N);
-#define FG_TC(KD)                                                                                 \
-    do {                                                                                          \
-        if (!attr[KD]) {                                                                          \
-            FG_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<KD>,                                      \
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM)); \
-            attr[KD] = true;                                                                      \
-        }                                                                                         \
-        tc_gemm_kernel<KD><<<grid, TC_THREADS, TC_SMEM, stream>>>(ma, mb, M, N, K, alpha, beta, C,  \
-                                                                 ldc, scale_a, scale_b, w->status); \
+#define FG_TC(KD)                                                                               \
+    do {                                                                                        \
+        if ((st = tc::prepare_kernel<KD, EpiF32>()) != kOk) return st;                          \
+        tc::tc_kernel<KD, EpiF32><<<grid, tc::THREADS, tc::SMEM, stream>>>(ma, mb, M, N, epi,   \
+                                                                         w->status);           \
     } while (0)
     if (kind == kTcTF32) FG_TC(kTcTF32);
     else if (kind == kTcBF16) FG_TC(kTcBF16);

@@ -116,6 +116,25 @@ int flens_gb300_sgemm_tc(int precision, char transA, char transB, int m, int n,
                          const float *B, int ldB, float beta, float *C, int ldC,
                          void *stream);
 
+/* FP64-accurate C <- beta*C + alpha*op(A)*op(B) on device memory without FP64
+ * arithmetic units: every row of op(A) / column of op(B) is scaled by a power
+ * of two and cut into `slices` balanced 7-bit integer digits (exact in BF16);
+ * the digit products of slice pairs s+t <= slices+1 run on the tcgen05 tensor
+ * cores in groups whose FP32 sums are provably exact (every partial sum an
+ * integer <= 2^24), and are recombined in FP64.  slices = 0 picks the count
+ * from the data (7*slices >= 53 + log2 max_i(2^e_i nnz_i / sum_k |a_ik|));
+ * *slices_used receives it, or -1 when non-finite entries or exponents beyond
+ * about 2^+-1000 sent the call to the plain FP64 kernel.  Argument positions
+ * and semantics as dgemm_ (flens/blas/interface/blas/gemm.cc:158-181; beta
+ * scaling by a multiply, alpha == 0 or k == 0 only scale C), slices at 14
+ * (0..20).  The dgemm_ counterpart replaced for FP64-accurate products is
+ * cxxblas::gemm (cxxblas/level3/gemm.tcc:176-190).  Reads its statistics back
+ * to the host, so it synchronises on stream before the product is queued. */
+int flens_gb300_dgemm_split(char transA, char transB, int m, int n, int k,
+                            double alpha, const double *A, int ldA,
+                            const double *B, int ldB, double beta, double *C,
+                            int ldC, int slices, int *slices_used, void *stream);
+
 /* Solve A X = B (device, column-major FP64; A and B untouched) to FP64
  * accuracy from an LU in FP32 storage whose trailing updates run on the
  * tensor cores in `precision` (as above), refined in FP64: solver 0 =
