@@ -76,6 +76,12 @@ class Port:
         L.oracle_dgetrs.argtypes = [c, i, i, _c_double_p, i, _c_int_p, _c_double_p, i]
         L.oracle_dgesv.argtypes = [i, i, _c_double_p, i, _c_int_p, _c_double_p, i]
         L.oracle_dgesv.restype = i
+        L.oracle_dsyrk.argtypes = [c, c, i, i, d, _c_double_p, i, d, _c_double_p, i]
+        L.oracle_dpotrf_nb.argtypes = [c, i, _c_double_p, i, i]
+        L.oracle_dpotrf_nb.restype = i
+        L.oracle_dpotrs.argtypes = [c, i, i, _c_double_p, i, _c_double_p, i]
+        L.oracle_dposv.argtypes = [c, i, i, _c_double_p, i, _c_double_p, i]
+        L.oracle_dposv.restype = i
         L.oracle_time_dgetrf_steps.argtypes = [i, i, i, ctypes.c_ulonglong, _c_double_p]
         L.oracle_time_dgetrf_steps.restype = d
         L.oracle_time_dgemm_rows.argtypes = [i, i, i, i, i, ctypes.c_ulonglong]
@@ -127,6 +133,33 @@ class Port:
                                      _dp(B), max(1, n))
         return piv[:n], info
 
+    # -- Cholesky and syrk --------------------------------------------------
+    def dsyrk(self, uplo, trans, alpha, A, beta, C):
+        _check_f64(A), _check_f64(C)
+        n = C.shape[0]
+        k = A.shape[1] if trans.upper() == "N" else A.shape[0]
+        self.lib.oracle_dsyrk(uplo.encode(), trans.encode(), n, k, alpha, _dp(A),
+                              max(1, A.shape[0]), beta, _dp(C), max(1, n))
+        return C
+
+    def dpotrf(self, uplo, A, nb: int = 64):
+        _check_f64(A)
+        n = A.shape[0]
+        return self.lib.oracle_dpotrf_nb(uplo.encode(), n, _dp(A), max(1, n), nb)
+
+    def dpotrs(self, uplo, A, B):
+        _check_f64(A), _check_f64(B)
+        n = A.shape[0]
+        self.lib.oracle_dpotrs(uplo.encode(), n, B.shape[1], _dp(A), max(1, n), _dp(B),
+                               max(1, n))
+        return B
+
+    def dposv(self, uplo, A, B):
+        _check_f64(A), _check_f64(B)
+        n = A.shape[0]
+        return self.lib.oracle_dposv(uplo.encode(), n, B.shape[1], _dp(A), max(1, n), _dp(B),
+                                     max(1, n))
+
     # -- timing (CPU baseline) ---------------------------------------------
     def time_dgetrf_steps(self, n, n_blocks, n_threads, seed=1234):
         fl = ctypes.c_double(0.0)
@@ -158,6 +191,13 @@ class Reference:
                               _c_int_p, _c_double_p, _c_int_p, _c_int_p]
         L.dgesv_.argtypes = [_c_int_p, _c_int_p, _c_double_p, _c_int_p, _c_int_p,
                              _c_double_p, _c_int_p, _c_int_p]
+        L.dsyrk_.argtypes = [cp, cp, _c_int_p, _c_int_p, _c_double_p, _c_double_p, _c_int_p,
+                             _c_double_p, _c_double_p, _c_int_p]
+        L.dpotrf_.argtypes = [cp, _c_int_p, _c_double_p, _c_int_p, _c_int_p]
+        L.dpotrs_.argtypes = [cp, _c_int_p, _c_int_p, _c_double_p, _c_int_p, _c_double_p,
+                              _c_int_p, _c_int_p]
+        L.dposv_.argtypes = [cp, _c_int_p, _c_int_p, _c_double_p, _c_int_p, _c_double_p,
+                             _c_int_p, _c_int_p]
         L.ref_xerbla_calls.restype = ctypes.c_int
         L.ref_xerbla_info.restype = ctypes.c_int
         L.ref_xerbla_name.restype = ctypes.c_char_p
@@ -213,6 +253,38 @@ class Reference:
         self.lib.dgesv_(self._i(n), self._i(B.shape[1]), _dp(A), self._i(max(1, n)),
                         _ip(piv), _dp(B), self._i(max(1, n)), ctypes.byref(info))
         return piv[:n], info.value
+
+
+    def dsyrk(self, uplo, trans, alpha, A, beta, C):
+        n = C.shape[0]
+        k = A.shape[1] if trans.upper() == "N" else A.shape[0]
+        self.lib.dsyrk_(uplo.encode(), trans.encode(), self._i(n), self._i(k), self._d(alpha),
+                        _dp(A), self._i(max(1, A.shape[0])), self._d(beta), _dp(C),
+                        self._i(max(1, n)))
+        return C
+
+    def dpotrf(self, uplo, A):
+        n = A.shape[0]
+        info = ctypes.c_int(0)
+        self.lib.dpotrf_(uplo.encode(), self._i(n), _dp(A), self._i(max(1, n)),
+                         ctypes.byref(info))
+        return info.value
+
+    def dpotrs(self, uplo, A, B):
+        n = A.shape[0]
+        info = ctypes.c_int(0)
+        self.lib.dpotrs_(uplo.encode(), self._i(n), self._i(B.shape[1]), _dp(A),
+                         self._i(max(1, n)), _dp(B), self._i(max(1, n)), ctypes.byref(info))
+        return B, info.value
+
+    def dposv(self, uplo, A, B):
+        """The reference's dposv_ (flens/lapack/interface/src/posv.cc:13-51, the call at :50)
+        discards posv's return value: INFO is 0 for every valid call."""
+        n = A.shape[0]
+        info = ctypes.c_int(0)
+        self.lib.dposv_(uplo.encode(), self._i(n), self._i(B.shape[1]), _dp(A),
+                        self._i(max(1, n)), _dp(B), self._i(max(1, n)), ctypes.byref(info))
+        return info.value
 
 
 def reference_available() -> bool:

@@ -346,6 +346,210 @@ int oracle_dgesv(int n, int nRhs, double *A, int ldA, int *piv,
 
 /* ---------------------------------------------------------------- timing -- */
 
+/*
+ * SYRK.  cxxblas/level3/syrk.tcc:42-90: column-major is mapped to row-major
+ * with the triangle and the transposition flipped; the triangle is scaled by
+ * beta unless beta == 1 (cxxblas/level1extensions/syscal.tcc:41-61, a
+ * multiply); k == 0 returns; then one rank-1 update per l = 0..k-1
+ * (cxxblas/level2/syr.tcc:42-70), each an axpy with the coefficient alpha*x_i
+ * computed first: C(r, c) += (alpha*x_c)*x_r for the column c being updated.
+ */
+void oracle_dsyrk(char upLo, char trans, int n, int k, double alpha,
+                  const double *A, int ldA, double beta, double *C, int ldC)
+{
+    const int lower = (upLo == 'L' || upLo == 'l');
+    const int nT = is_notrans(trans);
+    if (beta != 1.0) {
+        for (int c = 0; c < n; ++c) {
+            const int r0 = lower ? c : 0, r1 = lower ? n : c + 1;
+            for (int r = r0; r < r1; ++r) {
+                C[IDX(r, c, ldC)] *= beta;
+            }
+        }
+    }
+    if (k == 0) {
+        return;
+    }
+    /* x_l(i) = op(A)(i, l): column l of A (trans N) or row l (trans T) */
+    const size_t xi = nT ? 1 : (size_t)ldA, xl = nT ? (size_t)ldA : 1;
+    for (int l = 0; l < k; ++l) {
+        const double *x = A + (size_t)l * xl;
+        for (int c = 0; c < n; ++c) {
+            const double t = alpha * x[(size_t)c * xi];
+            const int r0 = lower ? c : 0, r1 = lower ? n : c + 1;
+            for (int r = r0; r < r1; ++r) {
+                C[IDX(r, c, ldC)] += t * x[(size_t)r * xi];
+            }
+        }
+    }
+}
+
+/*
+ * GEMV.  cxxblas/level2/gemv.tcc:160-176 returns when m or n is 0 (before
+ * any scaling); :42-130 maps column-major to row-major, scales y by beta
+ * (scal, a multiply) and adds alpha*dot per element, the dot started at zero
+ * in increasing index.
+ */
+void oracle_dgemv(char trans, int m, int n, double alpha, const double *A,
+                  int ldA, const double *x, int incX, double beta, double *y,
+                  int incY)
+{
+    if (m == 0 || n == 0) {
+        return;
+    }
+    const int nT = is_notrans(trans);
+    const int ny = nT ? m : n, nx = nT ? n : m;
+    if (incX < 0) {
+        x -= (ptrdiff_t)incX * (nx - 1);
+    }
+    if (incY < 0) {
+        y -= (ptrdiff_t)incY * (ny - 1);
+    }
+    for (int i = 0; i < ny; ++i) {
+        y[(ptrdiff_t)i * incY] *= beta;
+    }
+    for (int i = 0; i < ny; ++i) {
+        double s = 0.0;
+        for (int p = 0; p < nx; ++p) {
+            const double a = nT ? A[IDX(i, p, ldA)] : A[IDX(p, i, ldA)];
+            s += a * x[(ptrdiff_t)p * incX];
+        }
+        y[(ptrdiff_t)i * incY] += alpha * s;
+    }
+}
+
+/*
+ * POTF2.  flens/lapack/po/potf2.tcc:56-140 (left-looking, dot form): for each
+ * column j, ajj = A(j,j) - dot(a, a) over the finished part of row/column j;
+ * ajj <= 0 or NaN stores ajj, sets info = j and stops; otherwise A(j,j) =
+ * sqrt(ajj), the rest of column j (lower) or row j (upper) gets
+ * gemv(-1, ., +1) and is multiplied by 1/ajj (reciprocal computed once).
+ */
+int oracle_dpotf2(char upLo, int n, double *A, int ldA)
+{
+    const int lower = (upLo == 'L' || upLo == 'l');
+    for (int j = 0; j < n; ++j) {
+        /* a = A(j, 0:j) (lower: row, stride ldA) or A(0:j, j) (upper: column) */
+        const double *a = lower ? &A[IDX(j, 0, ldA)] : &A[IDX(0, j, ldA)];
+        const size_t as = lower ? (size_t)ldA : 1;
+        double dot = 0.0;
+        for (int p = 0; p < j; ++p) {
+            dot += a[(size_t)p * as] * a[(size_t)p * as];
+        }
+        double ajj = A[IDX(j, j, ldA)] - dot;
+        if (ajj <= 0.0 || isnan(ajj)) {
+            A[IDX(j, j, ldA)] = ajj;
+            return j + 1;
+        }
+        ajj = sqrt(ajj);
+        A[IDX(j, j, ldA)] = ajj;
+        if (j + 1 < n) {
+            const int rest = n - j - 1;
+            if (lower) {
+                /* a32 = a32 - A31 * a21^T ; a32 *= 1/ajj */
+                oracle_dgemv('N', rest, j, -1.0, &A[IDX(j + 1, 0, ldA)], ldA,
+                             &A[IDX(j, 0, ldA)], ldA, 1.0, &A[IDX(j + 1, j, ldA)], 1);
+                const double r = 1.0 / ajj;
+                for (int i = 0; i < rest; ++i) {
+                    A[IDX(j + 1 + i, j, ldA)] *= r;
+                }
+            } else {
+                /* a23 = a23 - A13^T * a12 ; a23 *= 1/ajj */
+                oracle_dgemv('T', j, rest, -1.0, &A[IDX(0, j + 1, ldA)], ldA,
+                             &A[IDX(0, j, ldA)], 1, 1.0, &A[IDX(j, j + 1, ldA)], ldA);
+                const double r = 1.0 / ajj;
+                for (int i = 0; i < rest; ++i) {
+                    A[IDX(j, j + 1 + i, ldA)] *= r;
+                }
+            }
+        }
+    }
+    return 0;
+}
+
+/*
+ * POTRF.  flens/lapack/po/potrf.tcc:56-150: unblocked when nb <= 1 or
+ * nb >= n; otherwise, per block column j (lower): A22 -= A21 A21^T (syrk),
+ * potf2(A22) (info offset by j, stop on failure), A32 -= A31 A21^T (gemm),
+ * A32 <- A32 L22^-T (trsm); upper mirrors it with A12, A13, A23.
+ */
+int oracle_dpotrf_nb(char upLo, int n, double *A, int ldA, int nb)
+{
+    const int lower = (upLo == 'L' || upLo == 'l');
+    if (n == 0) {
+        return 0;
+    }
+    if (nb <= 1 || nb >= n) {
+        return oracle_dpotf2(upLo, n, A, ldA);
+    }
+    for (int j = 0; j < n; j += nb) {
+        const int jb = (nb < n - j) ? nb : n - j;
+        const int r3 = n - j - jb;
+        double *A22 = &A[IDX(j, j, ldA)];
+        if (lower) {
+            oracle_dsyrk('L', 'N', jb, j, -1.0, &A[IDX(j, 0, ldA)], ldA, 1.0, A22, ldA);
+            const int info = oracle_dpotf2('L', jb, A22, ldA);
+            if (info != 0) {
+                return info + j;
+            }
+            if (r3 > 0) {
+                oracle_dgemm('N', 'T', r3, jb, j, -1.0, &A[IDX(j + jb, 0, ldA)], ldA,
+                             &A[IDX(j, 0, ldA)], ldA, 1.0, &A[IDX(j + jb, j, ldA)], ldA);
+                oracle_dtrsm('R', 'L', 'T', 'N', r3, jb, 1.0, A22, ldA,
+                             &A[IDX(j + jb, j, ldA)], ldA);
+            }
+        } else {
+            oracle_dsyrk('U', 'T', jb, j, -1.0, &A[IDX(0, j, ldA)], ldA, 1.0, A22, ldA);
+            const int info = oracle_dpotf2('U', jb, A22, ldA);
+            if (info != 0) {
+                return info + j;
+            }
+            if (r3 > 0) {
+                oracle_dgemm('T', 'N', jb, r3, j, -1.0, &A[IDX(0, j, ldA)], ldA,
+                             &A[IDX(0, j + jb, ldA)], ldA, 1.0, &A[IDX(j, j + jb, ldA)], ldA);
+                oracle_dtrsm('L', 'U', 'T', 'N', jb, r3, 1.0, A22, ldA,
+                             &A[IDX(j, j + jb, ldA)], ldA);
+            }
+        }
+    }
+    return 0;
+}
+
+int oracle_dpotrf(char upLo, int n, double *A, int ldA)
+{
+    return oracle_dpotrf_nb(upLo, n, A, ldA, 64);
+}
+
+/*
+ * POTRS.  flens/lapack/po/potrs.tcc:54-100: lower: L X = B then L^T X = B;
+ * upper: U^T X = B then U X = B; both triangular solves non-unit, alpha 1.
+ */
+void oracle_dpotrs(char upLo, int n, int nRhs, const double *A, int ldA,
+                   double *B, int ldB)
+{
+    const int lower = (upLo == 'L' || upLo == 'l');
+    if (n == 0 || nRhs == 0) {
+        return;
+    }
+    if (lower) {
+        oracle_dtrsm('L', 'L', 'N', 'N', n, nRhs, 1.0, A, ldA, B, ldB);
+        oracle_dtrsm('L', 'L', 'T', 'N', n, nRhs, 1.0, A, ldA, B, ldB);
+    } else {
+        oracle_dtrsm('L', 'U', 'T', 'N', n, nRhs, 1.0, A, ldA, B, ldB);
+        oracle_dtrsm('L', 'U', 'N', 'N', n, nRhs, 1.0, A, ldA, B, ldB);
+    }
+}
+
+int oracle_dposv(char upLo, int n, int nRhs, double *A, int ldA, double *B,
+                 int ldB)
+{
+    const int info = oracle_dpotrf(upLo, n, A, ldA);
+    if (info == 0) {
+        oracle_dpotrs(upLo, n, nRhs, A, ldA, B, ldB);
+    }
+    return info;
+}
+
 static unsigned long long splitmix64(unsigned long long *s)
 {
     unsigned long long z = (*s += 0x9E3779B97F4A7C15ULL);

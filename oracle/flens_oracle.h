@@ -58,6 +58,32 @@ void oracle_dgetrs(char trans, int n, int nRhs, const double *A, int ldA,
 int oracle_dgesv(int n, int nRhs, double *A, int ldA, int *piv,
                  double *B, int ldB);
 
+/* C <- beta*C + alpha*op(A)*op(A)^T on the uplo triangle of C
+ *                                               cxxblas/level3/syrk.tcc:42-90 */
+void oracle_dsyrk(char upLo, char trans, int n, int k, double alpha,
+                  const double *A, int ldA, double beta, double *C, int ldC);
+
+/* y <- beta*y + alpha*op(A)*x                  cxxblas/level2/gemv.tcc:42-200 */
+void oracle_dgemv(char trans, int m, int n, double alpha, const double *A,
+                  int ldA, const double *x, int incX, double beta, double *y,
+                  int incY);
+
+/* unblocked Cholesky of the uplo triangle       flens/lapack/po/potf2.tcc:56-140 */
+int oracle_dpotf2(char upLo, int n, double *A, int ldA);
+
+/* blocked Cholesky (reference block size 64: ilaenv PO TRF)
+ *                                               flens/lapack/po/potrf.tcc:56-150 */
+int oracle_dpotrf_nb(char upLo, int n, double *A, int ldA, int nb);
+int oracle_dpotrf(char upLo, int n, double *A, int ldA);
+
+/* solve A X = B from the Cholesky factor         flens/lapack/po/potrs.tcc:54-100 */
+void oracle_dpotrs(char upLo, int n, int nRhs, const double *A, int ldA,
+                   double *B, int ldB);
+
+/* potrf then potrs if info==0                    flens/lapack/po/posv.tcc:55-70 */
+int oracle_dposv(char upLo, int n, int nRhs, double *A, int ldA, double *B,
+                 int ldB);
+
 /*
  * Timing helper for the CPU baseline: nThreads independent copies of the
  * seeded n x n input (uniform[-1,1] + n/4 on the diagonal), each factorised

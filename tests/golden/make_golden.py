@@ -1,7 +1,8 @@
 """Generate the golden fixtures in this directory from the REFERENCE itself.
 
-Runs the reference's own Fortran-ABI shims (dgemm_, dtrsm_, dgetrf_, dgetrs_,
-dgesv_ compiled from the FLENS sources into oracle/_ref/libflens_ref.so by
+Runs the reference's own Fortran-ABI shims (dgemm_, dtrsm_, dsyrk_, dgetrf_,
+dgetrs_, dgesv_, dpotrf_, dpotrs_, dposv_ compiled from the FLENS sources into
+oracle/_ref/libflens_ref.so by
 ``make -C oracle ref``) on seeded inputs and stores the outputs.  Inputs come
 from ``oracle.splitmix_uniform(seed, m, n)`` (integer hashing, identical on
 every machine), so only seeds and outputs are stored.  The fixtures travel
@@ -112,6 +113,51 @@ def baby_problem():
     return A, b
 
 
+def syrk_case_list():
+    cases = []
+    for (n, k) in [(0, 3), (5, 0), (7, 9), (40, 33), (65, 130)]:
+        for uplo in "LU":
+            for tr in "NTC":
+                cases.append((n, k, uplo, tr, 1.5, 0.5))
+    for (a, b) in [(-1.0, 1.0), (0.0, 2.0), (2.0, 0.0)]:
+        cases.append((40, 33, "L", "N", a, b))
+    return [(f"syrk{i:03d}", c) for i, c in enumerate(cases)]
+
+
+def syrk_inputs(i, n, k, tr):
+    s = 11000 + 10 * i
+    A = U(s, n if tr == "N" else k, k if tr == "N" else n)
+    C = U(s + 1, n, n)
+    return A, C
+
+
+def chol_case_list():
+    """(n, uplo, kind): kind 'spd' (well conditioned) or 'notpd' (a negative
+    pivot at n//2, so INFO = n//2 + 1 with the factor of the leading block)."""
+    cases = []
+    for n in (1, 2, 5, 31, 63, 64, 65, 100, 129, 200):
+        for uplo in "LU":
+            cases.append((n, uplo, "spd"))
+    for n in (5, 64, 130):
+        for uplo in "LU":
+            cases.append((n, uplo, "notpd"))
+    return [(f"chol{i:03d}", c) for i, c in enumerate(cases)]
+
+
+def chol_input(i, n, kind):
+    """Symmetric positive definite: G G^T / n + I with G splitmix uniform; the
+    'notpd' kind sets A(n//2, n//2) = -1."""
+    G = U(13000 + 10 * i, n, n)
+    A = np.asfortranarray(G @ G.T / max(n, 1) + np.eye(n))
+    if kind == "notpd":
+        A[n // 2, n // 2] = -1.0
+    return A
+
+
+def chol_rhs(i, n):
+    return U(13000 + 10 * i + 1, n, 3)
+
+
 LARGE_N, LARGE_SEED = 8192, 20261203
 
 
@@ -142,6 +188,16 @@ def generate_small(R):
     LU = singular_input()
     piv, info = R.dgetrf(LU)
     out["sing_LU"], out["sing_piv"], out["sing_info"] = LU, piv.astype(np.int32), np.array([info])
+    for i, (name, (n, k, uplo, tr, a, b)) in enumerate(syrk_case_list()):
+        A, C = syrk_inputs(i, n, k, tr)
+        out[name] = R.dsyrk(uplo, tr, a, A, b, C.copy(order="F"))
+    for i, (name, (n, uplo, kind)) in enumerate(chol_case_list()):
+        A = chol_input(i, n, kind)
+        info = R.dpotrf(uplo, A)
+        out[name + "_A"], out[name + "_info"] = A, np.array([info])
+        if info == 0:
+            X, _ = R.dpotrs(uplo, A, chol_rhs(i, n).copy(order="F"))
+            out[name + "_X"] = X
     A, b = baby_problem()
     piv, info = R.dgesv(A, b)
     out["baby_LU"], out["baby_x"], out["baby_piv"] = A, b, piv.astype(np.int32)

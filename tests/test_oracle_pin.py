@@ -63,6 +63,27 @@ def test_baby_problem_known_answer(golden, port):
     assert np.array_equal(A, golden["baby_LU"])
 
 
+def test_syrk_fixtures_bitwise(golden, port):
+    for i, (name, (n, k, uplo, tr, a, b)) in enumerate(G.syrk_case_list()):
+        A, C = G.syrk_inputs(i, n, k, tr)
+        out = port.dsyrk(uplo, tr, a, A, b, C.copy(order="F"))
+        assert np.array_equal(out, golden[name]), name
+
+
+def test_cholesky_fixtures_bitwise(golden, port):
+    for i, (name, (n, uplo, kind)) in enumerate(G.chol_case_list()):
+        A = G.chol_input(i, n, kind)
+        info = port.dpotrf(uplo, A)
+        assert info == golden[name + "_info"][0], name
+        assert np.array_equal(A, golden[name + "_A"]), name
+        if kind == "notpd":
+            assert info == n // 2 + 1, name
+        else:
+            assert info == 0, name
+            X = port.dpotrs(uplo, A, G.chol_rhs(i, n).copy(order="F"))
+            assert np.array_equal(X, golden[name + "_X"]), name
+
+
 def test_iamax_first_max_and_nan():
     p = oracle.Port()
     assert p.idamax([1.0, -3.0, 3.0, 2.0]) == 1          # first maximum wins
@@ -100,3 +121,20 @@ def test_port_equals_reference_live():
         p1, i1 = P.dgetrf(a1)
         p2, i2 = R.dgetrf(a2)
         assert np.array_equal(a1, a2) and np.array_equal(p1, p2) and i1 == i2
+    for n in (70, 150):
+        G0 = oracle.uniform(rng, n, n)
+        A = np.asfortranarray(G0 @ G0.T / n + np.eye(n))
+        for uplo in "LU":
+            a1, a2 = A.copy(order="F"), A.copy(order="F")
+            assert P.dpotrf(uplo, a1) == R.dpotrf(uplo, a2) == 0
+            assert np.array_equal(a1, a2)
+            B = oracle.uniform(rng, n, 2)
+            b1 = P.dpotrs(uplo, a1, B.copy(order="F"))
+            b2, _ = R.dpotrs(uplo, a2, B.copy(order="F"))
+            assert np.array_equal(b1, b2)
+    # the reference's dposv_ drops posv's INFO (posv.cc:50); its C++ posv
+    # returns it, as the restatement does
+    A = np.asfortranarray(np.eye(6))
+    A[2, 2] = -1.0
+    assert R.dposv("L", A.copy(order="F"), np.ones((6, 1), order="F")) == 0
+    assert P.dposv("L", A.copy(order="F"), np.ones((6, 1), order="F")) == 3
