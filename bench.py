@@ -327,6 +327,8 @@ def our_arm(args, rank: int, world: int) -> None:
             result["mixed_config3"] = mixed_subbench(torch, fg, dev, n=args.mixed_n)
         if not args.quick and not args.no_split:
             result["split_gemm_config4"] = split_subbench(torch, fg, dev, cublas_tflops=cublas_peak)
+        if not args.quick and not args.no_cholesky:
+            result["cholesky_fp64"] = cholesky_subbench(torch, fg, dev)
         if not args.quick and not args.no_batched:
             result["batched_config5"] = batched_subbench(torch, fg, dev, count=args.batch_count)
         # -- e2e through the Fortran ABI with pinned host buffers
@@ -513,6 +515,58 @@ def split_subbench(torch, fg, dev, n=8192, Es=(0, 16, 48), reps=5, ref_slices=14
     out["plain_fp64_dgemm"] = {"ms": plain_ms, "tflops": 2.0 * n ** 3 / (plain_ms * 1e-3) / 1e12,
                                "cublas_fp64_tflops": cublas_tflops}
     out["bf16_peak_tflops"] = {"value": peak, "source": f"{peak_src} (MEASURED_PEAKS.json bf16_tflops)"}
+    return out
+
+
+def cholesky_subbench(torch, fg, dev, n=8192, reps=3):
+    """Cholesky solve configuration: A = G G^T / n + I (G seeded uniform[-1,1]),
+    b = A x_true, one rhs, through flens_gb300_dposv (dpotrf + dpotrs) with A
+    and b restored from pristine copies inside every timed repetition (A is
+    512 MiB > L2).  FLOP count n^3/3 + 2 n^2."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(81)
+    Gm = torch.rand((n, n), generator=g, dtype=torch.float64, device=dev).mul_(2).sub_(1)
+    A0 = torch.addmm(torch.eye(n, dtype=torch.float64, device=dev), Gm, Gm.T, alpha=1.0 / n)
+    del Gm
+    A0 = A0.t()                                   # column-major view (A0 is symmetric)
+    x = torch.rand((n, 1), generator=g, dtype=torch.float64, device=dev).mul_(2).sub_(1)
+    b0 = A0 @ x
+    A = fg.to_colmajor(A0.clone())
+    b = b0.clone()
+    info = torch.zeros(1, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+    A.copy_(A0)
+    b.copy_(b0)
+    fg.dposv_dev("L", A, b, info)
+    torch.cuda.synchronize()
+    fg.timing_enable(True)
+    times = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        A.copy_(A0)
+        b.copy_(b0)
+        fg.dposv_dev("L", A, b, info)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    fam = fg.timing_read()
+    fg.timing_enable(False)
+    ms = sum(times) / len(times)
+    flop = n ** 3 / 3.0 + 2.0 * n * n
+    L = torch.tril(A)
+    R = torch.tril(A0 - L @ L.T)
+    eps = float(torch.finfo(torch.float64).eps)
+    be = (R.abs().sum(0).max() / (n * A0.abs().sum(0).max() * eps)).item()
+    out = {"workload": f"dposv n={n} 1 rhs FP64, A = G G^T/n + I", "n": n, "ms": ms,
+           "tflops": flop / (ms * 1e-3) / 1e12, "info": int(info.item()),
+           "backward_error_over_n_eps": be,
+           "forward_error": ((b - x).abs().max() / x.abs().max()).item(),
+           "kernels_ms_per_call": {k: v["ms"] / reps for k, v in fam.items()},
+           "launches_per_call": {k: v["launches"] / reps for k, v in fam.items()},
+           "l2": "A restored from a pristine copy each rep (512 MiB > L2)"}
+    del A, A0, b, b0
+    torch.cuda.empty_cache()
     return out
 
 
@@ -720,6 +774,8 @@ def only(args):
     elif args.only == "batched":
         out = batched_subbench(torch, fg, dev, count=args.batch_count, reps=1, loop_sample=50)
         print(json.dumps(out))
+    elif args.only == "cholesky":
+        print(json.dumps(cholesky_subbench(torch, fg, dev, n=args.n, reps=args.steps)))
     elif args.only == "split":
         out = split_subbench(torch, fg, dev, n=args.split_n, Es=(args.split_e,), reps=args.steps,
                              ref_slices=args.split_ref_slices)
@@ -742,11 +798,12 @@ def main():
     ap.add_argument("--mixed-n", type=int, default=16384)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-split", action="store_true")
+    ap.add_argument("--no-cholesky", action="store_true")
     ap.add_argument("--split-n", type=int, default=8192, help="n for --only split")
     ap.add_argument("--split-e", type=int, default=48, help="exponent range E for --only split")
     ap.add_argument("--split-ref-slices", type=int, default=14, help="reference slices for --only split")
     ap.add_argument("--batch-count", type=int, default=20000)
-    ap.add_argument("--only", choices=["tc_gemm", "batched", "mixed", "split"],
+    ap.add_argument("--only", choices=["tc_gemm", "batched", "mixed", "split", "cholesky"],
                     help="run one sub-benchmark and print its JSON (for profiling)")
     ap.add_argument("--tc-shape", default="8192,8192,256", help="M,N,K for --only tc_gemm")
     args = ap.parse_args()

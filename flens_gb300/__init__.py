@@ -75,6 +75,18 @@ def lib() -> ctypes.CDLL:
     L.dgetrs_.restype = None
     L.dgesv_.argtypes = [_ip, _ip, _dp, _ip, _ip, _dp, _ip, _ip]
     L.dgesv_.restype = None
+    L.dsyrk_.argtypes = [cp, cp, _ip, _ip, _dp, _dp, _ip, _dp, _dp, _ip]
+    L.dsyrk_.restype = None
+    L.dpotrf_.argtypes = [cp, _ip, _dp, _ip, _ip]
+    L.dpotrf_.restype = None
+    L.dpotrs_.argtypes = [cp, _ip, _ip, _dp, _ip, _dp, _ip, _ip]
+    L.dpotrs_.restype = None
+    L.dposv_.argtypes = [cp, _ip, _ip, _dp, _ip, _dp, _ip, _ip]
+    L.dposv_.restype = None
+    L.flens_gb300_dsyrk.argtypes = [_c, _c, _i, _i, _d, _v, _i, _d, _v, _i, _v]
+    L.flens_gb300_dpotrf.argtypes = [_c, _i, _v, _i, _v, _v]
+    L.flens_gb300_dpotrs.argtypes = [_c, _i, _i, _v, _i, _v, _i, _v]
+    L.flens_gb300_dposv.argtypes = [_c, _i, _i, _v, _i, _v, _i, _v, _v]
     L.flens_gb300_dgemm.argtypes = [_c, _c, _i, _i, _i, _d, _v, _i, _v, _i, _d, _v, _i, _v]
     L.flens_gb300_dtrsm.argtypes = [_c, _c, _c, _c, _i, _i, _d, _v, _i, _v, _i, _v]
     L.flens_gb300_dgetrf.argtypes = [_i, _i, _v, _i, _v, _v, _v]
@@ -87,7 +99,9 @@ def lib() -> ctypes.CDLL:
                                           ctypes.POINTER(ctypes.c_int), _v]
     L.flens_gb300_dgemm_split.restype = _i
     for f in ("flens_gb300_dgemm", "flens_gb300_dtrsm", "flens_gb300_dgetrf",
-              "flens_gb300_dgetrs", "flens_gb300_dgesv", "flens_gb300_sync"):
+              "flens_gb300_dgetrs", "flens_gb300_dgesv", "flens_gb300_sync",
+              "flens_gb300_dsyrk", "flens_gb300_dpotrf", "flens_gb300_dpotrs",
+              "flens_gb300_dposv"):
         getattr(L, f).restype = _i
     L.flens_gb300_last_error.restype = ctypes.c_char_p
     L.flens_gb300_last_error.argtypes = []
@@ -200,12 +214,44 @@ def dgesv(A: np.ndarray, B: np.ndarray):
     return piv[:n], info.value
 
 
+def dsyrk(uplo: str, trans: str, alpha: float, A: np.ndarray, beta: float, C: np.ndarray):
+    n = C.shape[0]
+    k = A.shape[1] if trans.upper() == "N" else A.shape[0]
+    lib().dsyrk_(uplo.encode(), trans.encode(), _ref(n, _i), _ref(k, _i), _ref(alpha, _d), _fd(A),
+                 _ref(max(1, A.shape[0]), _i), _ref(beta, _d), _fd(C), _ref(max(1, n), _i))
+    return C
+
+
+def dpotrf(uplo: str, A: np.ndarray) -> int:
+    """In-place Cholesky through dpotrf_; returns info."""
+    n = A.shape[0]
+    info = ctypes.c_int(0)
+    lib().dpotrf_(uplo.encode(), _ref(n, _i), _fd(A), _ref(max(1, n), _i), ctypes.byref(info))
+    return info.value
+
+
+def dpotrs(uplo: str, A: np.ndarray, B: np.ndarray):
+    n = A.shape[0]
+    info = ctypes.c_int(0)
+    lib().dpotrs_(uplo.encode(), _ref(n, _i), _ref(B.shape[1], _i), _fd(A), _ref(max(1, n), _i),
+                  _fd(B), _ref(max(1, n), _i), ctypes.byref(info))
+    return B, info.value
+
+
+def dposv(uplo: str, A: np.ndarray, B: np.ndarray) -> int:
+    n = A.shape[0]
+    info = ctypes.c_int(0)
+    lib().dposv_(uplo.encode(), _ref(n, _i), _ref(B.shape[1], _i), _fd(A), _ref(max(1, n), _i),
+                 _fd(B), _ref(max(1, n), _i), ctypes.byref(info))
+    return info.value
+
+
 # -------------------------------------------------------- device (torch) ---
 def _colmajor(t):
     """(pointer, rows, cols, ld) of a column-major CUDA float64 tensor."""
     if t.dim() == 2 and t.numel() == 0:
         return t.data_ptr(), t.shape[0], t.shape[1], max(1, t.shape[0])
-    if t.dim() != 2 or t.stride(0) != 1:
+    if t.dim() != 2 or (t.stride(0) != 1 and t.shape[0] != 1):   # a 1-row stride is free
         raise ValueError("expected a 2-D column-major tensor (stride(0) == 1)")
     return t.data_ptr(), t.shape[0], t.shape[1], max(1, t.stride(1), t.shape[0])
 
@@ -256,6 +302,39 @@ def dgemm_split_dev(transA, transB, alpha, A, B, beta, C, slices=0, stream=None)
                                          pb, ldb, beta, pc, ldc, slices, ctypes.byref(used),
                                          _stream(stream)), "flens_gb300_dgemm_split")
     return used.value
+
+
+def dsyrk_dev(uplo, trans, alpha, A, beta, C, stream=None):
+    pa, ra, ca, lda = _colmajor(A)
+    pc, n, _, ldc = _colmajor(C)
+    k = ca if trans.upper() == "N" else ra
+    _check(lib().flens_gb300_dsyrk(uplo.encode(), trans.encode(), n, k, alpha, pa, lda, beta, pc,
+                                   ldc, _stream(stream)), "flens_gb300_dsyrk")
+    return C
+
+
+def dpotrf_dev(uplo, A, info, stream=None):
+    """In-place Cholesky of a column-major CUDA tensor; info is an int32 CUDA tensor."""
+    pa, n, _, lda = _colmajor(A)
+    _check(lib().flens_gb300_dpotrf(uplo.encode(), n, pa, lda, info.data_ptr(), _stream(stream)),
+           "flens_gb300_dpotrf")
+    return A
+
+
+def dpotrs_dev(uplo, A, B, stream=None):
+    pa, n, _, lda = _colmajor(A)
+    pb, _, nrhs, ldb = _colmajor(B)
+    _check(lib().flens_gb300_dpotrs(uplo.encode(), n, nrhs, pa, lda, pb, ldb, _stream(stream)),
+           "flens_gb300_dpotrs")
+    return B
+
+
+def dposv_dev(uplo, A, B, info, stream=None):
+    pa, n, _, lda = _colmajor(A)
+    pb, _, nrhs, ldb = _colmajor(B)
+    _check(lib().flens_gb300_dposv(uplo.encode(), n, nrhs, pa, lda, pb, ldb, info.data_ptr(),
+                                   _stream(stream)), "flens_gb300_dposv")
+    return B
 
 
 def dtrsm_dev(side, uplo, transA, diag, alpha, A, B, stream=None):

@@ -7,6 +7,10 @@
 //      dgetrf_  flens/lapack/interface/src/getrf.cc:10-45
 //      dgetrs_  flens/lapack/interface/src/getrs.cc:13-53
 //      dgesv_   flens/lapack/interface/src/gesv.cc:13-49
+//      dsyrk_   flens/blas/interface/blas/syrk.cc:104-160
+//      dpotrf_  flens/lapack/interface/src/potrf.cc:11-41
+//      dpotrs_  flens/lapack/interface/src/potrs.cc:13-49
+//      dposv_   flens/lapack/interface/src/posv.cc:13-51
 //    They take HOST pointers (as the reference does), copy the operands to
 //    the device, run the GPU path and copy the results back before
 //    returning.  Device (or managed) pointers are also accepted and used in
@@ -356,8 +360,202 @@ FG_API void dgesv_(const int *N, const int *NRHS, double *A, const int *LDA, int
     *INFO = (st != kOk) ? st : info;
 }
 
+// --------------------------------------------------------------- dsyrk_ --
+// flens/blas/interface/blas/syrk.cc:104-160: UPLO and TRANS upper-cased, then
+// checked in argument order (positions 1, 2, 3, 4, 7, 10).
+FG_API void dsyrk_(const char *UPLO, const char *TRANS, const int *N, const int *K,
+                   const double *ALPHA, const double *A, const int *LDA, const double *BETA,
+                   double *C, const int *LDC) {
+    const char uplo = (char)toupper(*UPLO), tr = (char)toupper(*TRANS);
+    const int nRowA = (tr == 'N') ? *N : *K;
+    int info = 0;
+    if (uplo != 'U' && uplo != 'L') info = 1;
+    else if (tr != 'N' && tr != 'T' && tr != 'C') info = 2;
+    else if (*N < 0) info = 3;
+    else if (*K < 0) info = 4;
+    else if (*LDA < std::max(1, nRowA)) info = 7;
+    else if (*LDC < std::max(1, *N)) info = 10;
+    if (info != 0) {
+        report_xerbla("DSYRK ", info);
+        return;
+    }
+    const int n = *N, k = *K;
+    if (n == 0) return;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    DevView a, c;
+    if (st == kOk && k > 0)
+        st = view_in(0, A, tr == 'N' ? n : k, tr == 'N' ? k : n, *LDA, true, s, &a);
+    if (st == kOk) st = view_in(1, C, n, n, *LDC, true, s, &c);
+    if (st == kOk)
+        st = dsyrk_launch(uplo, tr == 'N' ? 'N' : 'T', n, k, *ALPHA, a.p, a.ld, *BETA, c.p, c.ld, s);
+    if (st == kOk) st = view_out(c, C, n, n, *LDC, s);
+    if (st == kOk) st = finish(s);
+    if (st != kOk) fprintf(stderr, "[flens_gb300] dsyrk_ failed (%d): %s\n", st, flens_gb300_last_error());
+}
+
+// ------------------------------------------------------ LAPACK Cholesky --
+namespace {
+
+int potrf_host(char uplo, int n, double *A, int ldA, int *INFO) {
+    *INFO = 0;
+    if (n == 0) return kOk;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    if (st != kOk) return st;
+    DevView a;
+    if ((st = view_in(0, A, n, n, ldA, true, s, &a)) != kOk) return st;
+    Workspace *w = workspace_for(s, 0);
+    if (!w) return kErrAlloc;
+    if ((st = dpotrf_launch(uplo, n, a.p, a.ld, w->info, s)) != kOk) return st;
+    if ((st = view_out(a, A, n, n, ldA, s)) != kOk) return st;
+    FG_CUDA(cudaMemcpyAsync(INFO, w->info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return finish(s);
+}
+
+int potrs_host(char uplo, int n, int nrhs, const double *A, int ldA, double *B, int ldB) {
+    if (n == 0 || nrhs == 0) return kOk;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    if (st != kOk) return st;
+    DevView a, b;
+    if ((st = view_in(0, A, n, n, ldA, true, s, &a)) != kOk) return st;
+    if ((st = view_in(1, B, n, nrhs, ldB, true, s, &b)) != kOk) return st;
+    if ((st = dpotrs_launch(uplo, n, nrhs, a.p, a.ld, b.p, b.ld, s)) != kOk) return st;
+    if ((st = view_out(b, B, n, nrhs, ldB, s)) != kOk) return st;
+    return finish(s);
+}
+
+int posv_host(char uplo, int n, int nrhs, double *A, int ldA, double *B, int ldB, int *INFO) {
+    *INFO = 0;
+    if (n == 0) return kOk;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    if (st != kOk) return st;
+    DevView a, b;
+    if ((st = view_in(0, A, n, n, ldA, true, s, &a)) != kOk) return st;
+    if ((st = view_in(1, B, n, nrhs, ldB, true, s, &b)) != kOk) return st;
+    Workspace *w = workspace_for(s, 0);
+    if (!w) return kErrAlloc;
+    if ((st = dpotrf_launch(uplo, n, a.p, a.ld, w->info, s)) != kOk) return st;
+    FG_CUDA(cudaMemcpyAsync(INFO, w->info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FG_CUDA(cudaStreamSynchronize(s));
+    // flens/lapack/po/posv.tcc:58-64: solve only if the factorisation succeeded
+    if (*INFO == 0 && nrhs > 0) {
+        if ((st = dpotrs_launch(uplo, n, nrhs, a.p, a.ld, b.p, b.ld, s)) != kOk) return st;
+        if ((st = view_out(b, B, n, nrhs, ldB, s)) != kOk) return st;
+    }
+    if ((st = view_out(a, A, n, n, ldA, s)) != kOk) return st;
+    return finish(s);
+}
+
+}  // namespace
+
+// flens/lapack/interface/src/potrf.cc:11-41: UPLO must be exactly 'U' or 'L'.
+FG_API void dpotrf_(const char *UPLO, const int *N, double *A, const int *LDA, int *INFO) {
+    *INFO = 0;
+    if (*UPLO != 'U' && *UPLO != 'L') *INFO = -1;
+    else if (*N < 0) *INFO = -2;
+    else if (*LDA < std::max(1, *N)) *INFO = -4;
+    if (*INFO != 0) {
+        report_xerbla("DPOTRF", -*INFO);
+        return;
+    }
+    int info = 0;
+    const int st = potrf_host(*UPLO, *N, A, *LDA, &info);
+    *INFO = (st != kOk) ? st : info;
+}
+
+// flens/lapack/interface/src/potrs.cc:13-49
+FG_API void dpotrs_(const char *UPLO, const int *N, const int *NRHS, const double *A,
+                    const int *LDA, double *B, const int *LDB, int *INFO) {
+    *INFO = 0;
+    if (*UPLO != 'U' && *UPLO != 'L') *INFO = -1;
+    else if (*N < 0) *INFO = -2;
+    else if (*NRHS < 0) *INFO = -3;
+    else if (*LDA < std::max(1, *N)) *INFO = -5;
+    else if (*LDB < std::max(1, *N)) *INFO = -7;
+    if (*INFO != 0) {
+        report_xerbla("DPOTRS", -*INFO);
+        return;
+    }
+    const int st = potrs_host(*UPLO, *N, *NRHS, A, *LDA, B, *LDB);
+    if (st != kOk) *INFO = st;
+}
+
+// flens/lapack/interface/src/posv.cc:13-51.  The reference's shim discards
+// posv's return value (INFO stays 0 on a failed factorisation); this one
+// returns it, as LAPACK's DPOSV and FLENS's own posv() do.
+FG_API void dposv_(const char *UPLO, const int *N, const int *NRHS, double *A, const int *LDA,
+                   double *B, const int *LDB, int *INFO) {
+    *INFO = 0;
+    if (*UPLO != 'U' && *UPLO != 'L') *INFO = -1;
+    else if (*N < 0) *INFO = -2;
+    else if (*NRHS < 0) *INFO = -3;
+    else if (*LDA < std::max(1, *N)) *INFO = -5;
+    else if (*LDB < std::max(1, *N)) *INFO = -7;
+    if (*INFO != 0) {
+        report_xerbla("DPOSV ", -*INFO);
+        return;
+    }
+    int info = 0;
+    const int st = posv_host(*UPLO, *N, *NRHS, A, *LDA, B, *LDB, &info);
+    *INFO = (st != kOk) ? st : info;
+}
+
 // ------------------------------------------------ device-pointer API ----
 static inline cudaStream_t as_stream(void *s) { return (cudaStream_t)s; }
+
+FG_API int flens_gb300_dsyrk(char uplo, char trans, int n, int k, double alpha, const double *A,
+                             int ldA, double beta, double *C, int ldC, void *stream) {
+    uplo = (char)toupper(uplo);
+    trans = (char)toupper(trans);
+    if (uplo != 'U' && uplo != 'L') return -1;
+    if (trans != 'N' && trans != 'T' && trans != 'C') return -2;
+    if (n < 0) return -3;
+    if (k < 0) return -4;
+    if (ldA < std::max(1, trans == 'N' ? n : k)) return -7;
+    if (ldC < std::max(1, n)) return -10;
+    return dsyrk_launch(uplo, trans == 'N' ? 'N' : 'T', n, k, alpha, A, ldA, beta, C, ldC,
+                        as_stream(stream));
+}
+
+FG_API int flens_gb300_dpotrf(char uplo, int n, double *A, int ldA, int *info, void *stream) {
+    uplo = (char)toupper(uplo);
+    if (uplo != 'U' && uplo != 'L') return -1;
+    if (n < 0) return -2;
+    if (ldA < std::max(1, n)) return -4;
+    return dpotrf_launch(uplo, n, A, ldA, info, as_stream(stream));
+}
+
+FG_API int flens_gb300_dpotrs(char uplo, int n, int nrhs, const double *A, int ldA, double *B,
+                              int ldB, void *stream) {
+    uplo = (char)toupper(uplo);
+    if (uplo != 'U' && uplo != 'L') return -1;
+    if (n < 0) return -2;
+    if (nrhs < 0) return -3;
+    if (ldA < std::max(1, n)) return -5;
+    if (ldB < std::max(1, n)) return -7;
+    return dpotrs_launch(uplo, n, nrhs, A, ldA, B, ldB, as_stream(stream));
+}
+
+FG_API int flens_gb300_dposv(char uplo, int n, int nrhs, double *A, int ldA, double *B, int ldB,
+                             int *info, void *stream) {
+    uplo = (char)toupper(uplo);
+    if (uplo != 'U' && uplo != 'L') return -1;
+    if (n < 0) return -2;
+    if (nrhs < 0) return -3;
+    if (ldA < std::max(1, n)) return -5;
+    if (ldB < std::max(1, n)) return -7;
+    cudaStream_t s = as_stream(stream);
+    int st = dpotrf_launch(uplo, n, A, ldA, info, s);
+    if (st != kOk) return st;
+    int h = 0;
+    FG_CUDA(cudaMemcpyAsync(&h, info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FG_CUDA(cudaStreamSynchronize(s));
+    if (h != 0) return kOk;    // INFO>0 reported through *info; no solve (posv.tcc:58-64)
+    return dpotrs_launch(uplo, n, nrhs, A, ldA, B, ldB, s);
+}
 
 FG_API int flens_gb300_dgemm(char transA, char transB, int m, int n, int k, double alpha,
                              const double *A, int ldA, const double *B, int ldB, double beta,

@@ -170,6 +170,22 @@ int dtrsm_launch(char side, char upLo, char transA, char diag, int m, int n,
 int dscal_matrix_launch(int m, int n, double alpha, double *B, int ldB,
                         cudaStream_t stream);
 
+// C <- beta*C + alpha*op(A)*op(A)^T on the uplo triangle ('L'/'U') of C,
+// trans 'N' (A n x k) or 'T' (A k x n).
+int dsyrk_launch(char uplo, char trans, int n, int k, double alpha,
+                 const double *A, int ldA, double beta, double *C, int ldC,
+                 cudaStream_t stream);
+
+// Cholesky (uplo 'L': A = L L^T, 'U': A = U^T U) of the n x n uplo triangle
+// in place; *info (device) = first non-positive pivot (1-based) or 0.
+// Synchronises once per 64-column block to stop at the first failure.
+int dpotrf_launch(char uplo, int n, double *A, int ldA, int *info,
+                  cudaStream_t stream);
+
+// Solve A X = B with the Cholesky factor from dpotrf_launch.
+int dpotrs_launch(char uplo, int n, int nrhs, const double *A, int ldA,
+                  double *B, int ldB, cudaStream_t stream);
+
 // FP32 counterparts (CUDA cores), used by the precision form's solves.
 int sgemm_launch(char transA, char transB, int m, int n, int k, float alpha,
                  const float *A, int ldA, const float *B, int ldB,

@@ -69,8 +69,11 @@ struct SlabLoader {
 
 // ---------------------------------------------------------------- DFMA ----
 // 64x64 CTA tile, 256 threads as 16x16, each thread a 4x4 sub-tile strided by
-// 16 so shared-memory reads are conflict-free broadcasts.
-template <typename T, bool TA, bool TB>
+// 16 so shared-memory reads are conflict-free broadcasts.  TRI restricts the
+// update to one triangle of a square C (syrk): 1 = lower (i >= j), 2 = upper
+// (i <= j); tiles wholly outside it exit at once and diagonal tiles store only
+// their part, so the other triangle of C is never written.
+template <typename T, bool TA, bool TB, int TRI = 0>
 __global__ void __launch_bounds__(256)
 dgemm_fma_kernel(int m, int n, int k, T alpha,
                  const T *__restrict__ A, int ldA,
@@ -80,6 +83,8 @@ dgemm_fma_kernel(int m, int n, int k, T alpha,
     __shared__ T Bs[2][BK][BN + PAD];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    if (TRI == 1 && m0 + BM <= n0) return;       // tile strictly above the diagonal
+    if (TRI == 2 && n0 + BN <= m0) return;       // tile strictly below the diagonal
 
     SlabLoader<T, !TA, BM, 256> la;
     SlabLoader<T, TB, BN, 256> lb;
@@ -129,6 +134,8 @@ dgemm_fma_kernel(int m, int n, int k, T alpha,
         for (int i = 0; i < 4; ++i) {
             const int gi = m0 + tx + 16 * i;
             if (gi >= m) continue;
+            if (TRI == 1 && gi < gj) continue;
+            if (TRI == 2 && gi > gj) continue;
             T *c = &C[(size_t)gi + (size_t)gj * ldC];
             *c = fma(alpha, acc[i][j], beta * *c);
         }
@@ -413,6 +420,41 @@ int gemm_launch_t(char transA, char transB, int m, int n, int k, T alpha, const 
         else if (ta && !tb) dgemm_fma_kernel<T, true, false><<<grid, 256, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
         else if (!ta && tb) dgemm_fma_kernel<T, false, true><<<grid, 256, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
         else dgemm_fma_kernel<T, true, true><<<grid, 256, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+    }
+    FG_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+// C <- beta*C + alpha*op(A)*op(A)^T on the uplo triangle of the n x n C
+// (cxxblas/level3/syrk.tcc:42-90): op(A) = A (n x k, trans 'N') or A^T.  The
+// triangle is scaled by beta unless beta == 1 (syscal); k == 0 only scales.
+// No alpha == 0 shortcut, as in the reference: NaN in A still reaches C.
+int dsyrk_launch(char uplo, char trans, int n, int k, double alpha, const double *A, int ldA,
+                 double beta, double *C, int ldC, cudaStream_t stream) {
+    if (n == 0) return kOk;
+    if (k == 0) {
+        if (beta == 1.0) return kOk;
+        alpha = 0.0;                              // acc == 0: C = beta*C on the triangle
+    }
+    const bool lower = uplo == 'L' || uplo == 'l';
+    const bool nt = trans == 'N' || trans == 'n';
+    const dim3 grid(ceil_div(n, BM), ceil_div(n, BN));
+    if (grid.y > 65535) {
+        set_last_error("syrk: n=%d too large for one launch", n);
+        return kErrUnsupported;
+    }
+    KTimer kt(kFamGemm, stream, (double)n * (n + 1) * (double)k,
+              8.0 * ((double)n * k + (double)n * (n + 1)));
+    trace("syrk %c%c n=%d k=%d", uplo, trans, n, k);
+    const double *Ak = k > 0 ? A : nullptr;
+    const int ldk = k > 0 ? ldA : 1;
+    // op(A) op(A)^T as gemm(op, op^T) with both operands A
+    if (lower) {
+        if (nt) dgemm_fma_kernel<double, false, true, 1><<<grid, 256, 0, stream>>>(n, n, k, alpha, Ak, ldk, Ak, ldk, beta, C, ldC);
+        else dgemm_fma_kernel<double, true, false, 1><<<grid, 256, 0, stream>>>(n, n, k, alpha, Ak, ldk, Ak, ldk, beta, C, ldC);
+    } else {
+        if (nt) dgemm_fma_kernel<double, false, true, 2><<<grid, 256, 0, stream>>>(n, n, k, alpha, Ak, ldk, Ak, ldk, beta, C, ldC);
+        else dgemm_fma_kernel<double, true, false, 2><<<grid, 256, 0, stream>>>(n, n, k, alpha, Ak, ldk, Ak, ldk, beta, C, ldC);
     }
     FG_CUDA(cudaGetLastError());
     return kOk;

@@ -9,106 +9,135 @@
 // triangle M (op(A) for side=Left, op(A)^T for side=Right) addressed as
 // M(i,p) = A[i*mi + p*mp], and a set of vectors (columns of B for Left, rows
 // of B for Right).  The blocked, right-looking driver solves 64x64 diagonal
-// blocks (trsm_diag_wide_kernel: a thread per vector; trsm_diag_narrow_kernel:
-// a warp per vector, for few right-hand sides) and applies each solved block to the rest
-// of B with the FP64 GEMM.  The diagonal solve uses the column-sweep (axpy)
-// form rather than the reference's dot form; the result agrees to rounding.
+// blocks (trsm_diag_tile_kernel: 32 vectors per CTA, 8 rows per thread;
+// trsm_diag_warp_kernel: a warp per vector for up to 32 vectors) and applies
+// each solved block to the rest of B with the FP64 GEMM.  The
+// diagonal solve uses the column-sweep (axpy) form rather than the
+// reference's dot form, and multiplies by the reciprocal of the diagonal
+// instead of dividing; the result agrees to rounding.
 #include "common.cuh"
 
 namespace fg {
 namespace {
 
 constexpr int TRSM_NB = 64;      // diagonal block size
-constexpr int TRSM_VEC = 64;     // vectors (threads) per CTA, wide kernel
-constexpr int TRSM_WARPS = 8;    // vectors (warps) per CTA, narrow kernel
-constexpr int TRSM_NARROW = 512; // below this many vectors use the warp kernel
+constexpr int TRSM_VPC = 32;     // vectors per CTA
+constexpr int TRSM_THREADS = 256;
+constexpr int TRSM_RPT = TRSM_NB * TRSM_VPC / TRSM_THREADS;   // rows per thread (8)
 
-// Wide kernel: one thread per vector, the vector held in 64 registers and
-// solved column by column (x_r -= M(r,i) x_i for all r past i), so every step
-// issues independent FMAs instead of one dependent dot-product chain.  The
-// diagonal block of M is staged in shared memory and read as broadcasts.
+// Solves the kb x kb (kb <= 64) diagonal block M for 32 vectors per CTA.
+// Thread t owns vector v = t % 32 and rows g, g+8, ..., g+56 (g = t / 32)
+// of it in registers.  Column by column, the owner of row i finishes x_i
+// (times the precomputed 1/M(i,i) unless the diagonal is unit), publishes it
+// through a double-buffered shared slot, and after one barrier every thread
+// updates its rows below (lower) or above (upper) i: the cyclic row
+// assignment keeps all threads busy to the end.  The 64 x 32 tile of X is
+// staged through shared memory so that global loads and stores are coalesced
+// whichever of the row or vector index is contiguous.
 template <typename T, bool LOWER, bool UNIT>
-__global__ void __launch_bounds__(TRSM_VEC)
-trsm_diag_wide_kernel(int nb, const T *__restrict__ M0, long long mi, long long mp,
+__global__ void __launch_bounds__(TRSM_THREADS)
+trsm_diag_tile_kernel(int nb, const T *__restrict__ M0, long long mi, long long mp,
                       T *__restrict__ X0, long long xs, long long vs, int nvec) {
-    __shared__ T Ms[TRSM_NB * TRSM_NB];   // Ms[r*NB + i] = M(r, i)
+    __shared__ T Ms[TRSM_NB][TRSM_NB + 1];     // Ms[i][r] = M(r, i)
+    __shared__ T Xs[TRSM_NB][TRSM_VPC + 1];    // Xs[r][v]
+    __shared__ T rinv[TRSM_NB];
+    __shared__ T xb[2][TRSM_VPC];
     const int t = threadIdx.x;
-    for (int e = t; e < nb * nb; e += TRSM_VEC) {
+    const long long v0 = (long long)blockIdx.x * TRSM_VPC;
+    const int nv = (int)((nvec - v0) < TRSM_VPC ? (nvec - v0) : TRSM_VPC);
+    for (int e = t; e < nb * nb; e += TRSM_THREADS) {
         int r, i;
         if (mi == 1) { r = e % nb; i = e / nb; }
         else { i = e % nb; r = e / nb; }
-        Ms[r * TRSM_NB + i] = M0[r * mi + i * mp];
+        Ms[i][r] = M0[r * mi + i * mp];
+    }
+    // X tile: lanes run along whichever index is contiguous in memory
+    for (int e = t; e < TRSM_NB * TRSM_VPC; e += TRSM_THREADS) {
+        int r, v;
+        if (xs == 1) { r = e % TRSM_NB; v = e / TRSM_NB; }
+        else { v = e % TRSM_VPC; r = e / TRSM_VPC; }
+        Xs[r][v] = (r < nb && v < nv) ? X0[(v0 + v) * vs + r * xs] : T(0);
     }
     __syncthreads();
-    const long long v = (long long)blockIdx.x * TRSM_VEC + t;
-    if (v >= nvec) return;
-    T *x = X0 + v * vs;
-    T r_[TRSM_NB];
+    if (!UNIT && t < nb) rinv[t] = T(1) / Ms[t][t];
+    const int v = t % TRSM_VPC, g = t / TRSM_VPC;
+    T x[TRSM_RPT];
 #pragma unroll
-    for (int r = 0; r < TRSM_NB; ++r) r_[r] = (r < nb) ? x[r * xs] : T(0);
-    if (LOWER) {
+    for (int j = 0; j < TRSM_RPT; ++j) x[j] = Xs[g + 8 * j][v];
+    __syncthreads();
+    for (int s = 0; s < nb; ++s) {
+        const int i = LOWER ? s : nb - 1 - s;
+        if (g == (i & 7)) {
 #pragma unroll
-        for (int i = 0; i < TRSM_NB; ++i) {
-            if (i < nb) {
-                if (!UNIT) r_[i] = r_[i] / Ms[i * TRSM_NB + i];
-                const T xi = r_[i];
-#pragma unroll
-                for (int r = i + 1; r < TRSM_NB; ++r)
-                    if (r < nb) r_[r] = fma(-Ms[r * TRSM_NB + i], xi, r_[r]);
+            for (int j = 0; j < TRSM_RPT; ++j) {
+                if (j == (i >> 3)) {
+                    if (!UNIT) x[j] *= rinv[i];
+                    xb[s & 1][v] = x[j];
+                }
             }
         }
-    } else {
+        __syncthreads();
+        const T xi = xb[s & 1][v];
 #pragma unroll
-        for (int i = TRSM_NB - 1; i >= 0; --i) {
-            if (i < nb) {
-                if (!UNIT) r_[i] = r_[i] / Ms[i * TRSM_NB + i];
-                const T xi = r_[i];
-#pragma unroll
-                for (int r = 0; r < i; ++r) r_[r] = fma(-Ms[r * TRSM_NB + i], xi, r_[r]);
-            }
+        for (int j = 0; j < TRSM_RPT; ++j) {
+            const int r = g + 8 * j;
+            if (LOWER ? (r > i && r < nb) : (r < i)) x[j] = fma(-Ms[i][r], xi, x[j]);
         }
     }
 #pragma unroll
-    for (int r = 0; r < TRSM_NB; ++r)
-        if (r < nb) x[r * xs] = r_[r];
+    for (int j = 0; j < TRSM_RPT; ++j) Xs[g + 8 * j][v] = x[j];
+    __syncthreads();
+    for (int e = t; e < TRSM_NB * TRSM_VPC; e += TRSM_THREADS) {
+        int r, vv;
+        if (xs == 1) { r = e % TRSM_NB; vv = e / TRSM_NB; }
+        else { vv = e % TRSM_VPC; r = e / TRSM_VPC; }
+        if (r < nb && vv < nv) X0[(v0 + vv) * vs + r * xs] = Xs[r][vv];
+    }
 }
 
-// Narrow kernel: one warp per vector, lane l holding rows l and l+32; the
-// finished x_i is broadcast with a shuffle and every lane updates its rows.
+// Few vectors (the solves with one or a handful of right-hand sides): one warp
+// per vector, lane l holding rows l and l + 32.  A step is a shuffle of the
+// finished x_i, one multiply by the precomputed 1/M(i,i) and the FMAs of the
+// rows still open -- no block barrier on the dependency chain.
+constexpr int TRSM_WARP_VECS = 8;      // warps (vectors) per CTA
+constexpr int TRSM_WARP_MAX = 32;      // use the warp kernel up to this many vectors
+
 template <typename T, bool LOWER, bool UNIT>
-__global__ void __launch_bounds__(32 * TRSM_WARPS)
-trsm_diag_narrow_kernel(int nb, const T *__restrict__ M0, long long mi, long long mp,
-                        T *__restrict__ X0, long long xs, long long vs, int nvec) {
-    __shared__ T Ms[TRSM_NB * (TRSM_NB + 1)];   // Ms[i*(NB+1) + r] = M(r, i)
+__global__ void __launch_bounds__(32 * TRSM_WARP_VECS)
+trsm_diag_warp_kernel(int nb, const T *__restrict__ M0, long long mi, long long mp,
+                      T *__restrict__ X0, long long xs, long long vs, int nvec) {
+    __shared__ T Ms[TRSM_NB][TRSM_NB + 1];     // Ms[i][r] = M(r, i)
+    __shared__ T rinv[TRSM_NB];
     for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
         int r, i;
         if (mi == 1) { r = e % nb; i = e / nb; }
         else { i = e % nb; r = e / nb; }
-        Ms[i * (TRSM_NB + 1) + r] = M0[r * mi + i * mp];
+        Ms[i][r] = M0[r * mi + i * mp];
     }
     __syncthreads();
+    if (!UNIT && threadIdx.x < nb) rinv[threadIdx.x] = T(1) / Ms[threadIdx.x][threadIdx.x];
+    __syncthreads();
     const int lane = threadIdx.x & 31;
-    const long long v = (long long)blockIdx.x * TRSM_WARPS + (threadIdx.x >> 5);
+    const long long v = (long long)blockIdx.x * TRSM_WARP_VECS + (threadIdx.x >> 5);
     if (v >= nvec) return;
     T *x = X0 + v * vs;
     const int r0 = lane, r1 = lane + 32;
-    T x0 = (r0 < nb) ? x[r0 * xs] : T(0);
-    T x1 = (r1 < nb) ? x[r1 * xs] : T(0);
+    T x0 = r0 < nb ? x[r0 * xs] : T(0);
+    T x1 = r1 < nb ? x[r1 * xs] : T(0);
     for (int s = 0; s < nb; ++s) {
         const int i = LOWER ? s : nb - 1 - s;
-        const int owner = i & 31;
-        T xi = __shfl_sync(0xffffffffu, (i < 32) ? x0 : x1, owner);
-        if (!UNIT) xi = xi / Ms[i * (TRSM_NB + 1) + i];
-        if (lane == owner) {
-            if (i < 32) x0 = xi; else x1 = xi;
+        T xi = __shfl_sync(0xffffffffu, i < 32 ? x0 : x1, i & 31);
+        if (!UNIT) xi *= rinv[i];
+        if (lane == (i & 31)) {
+            if (i < 32) x0 = xi;
+            else x1 = xi;
         }
-        const T *col = &Ms[i * (TRSM_NB + 1)];
         if (LOWER) {
-            if (r0 > i && r0 < nb) x0 = fma(-col[r0], xi, x0);
-            if (r1 > i && r1 < nb) x1 = fma(-col[r1], xi, x1);
+            if (r0 > i && r0 < nb) x0 = fma(-Ms[i][r0], xi, x0);
+            if (r1 > i && r1 < nb) x1 = fma(-Ms[i][r1], xi, x1);
         } else {
-            if (r0 < i) x0 = fma(-col[r0], xi, x0);
-            if (r1 < i) x1 = fma(-col[r1], xi, x1);
+            if (r0 < i) x0 = fma(-Ms[i][r0], xi, x0);
+            if (r1 < i) x1 = fma(-Ms[i][r1], xi, x1);
         }
     }
     if (r0 < nb) x[r0 * xs] = x0;
@@ -119,18 +148,18 @@ template <typename T>
 int launch_diag(int kb, const T *M0, long long mi, long long mp, bool lowerM, bool unit,
                 T *X0, long long xs, long long vs, int nvec, cudaStream_t stream) {
     KTimer kt(kFamTrsm, stream, (double)kb * kb * nvec, 16.0 * (double)kb * nvec);
-    if (nvec >= TRSM_NARROW) {
-        const int grid = ceil_div(nvec, TRSM_VEC);
-#define FG_WIDE(L, U) trsm_diag_wide_kernel<T, L, U><<<grid, TRSM_VEC, 0, stream>>>(kb, M0, mi, mp, X0, xs, vs, nvec)
-        if (lowerM) { if (unit) FG_WIDE(true, true); else FG_WIDE(true, false); }
-        else { if (unit) FG_WIDE(false, true); else FG_WIDE(false, false); }
-#undef FG_WIDE
+    if (nvec <= TRSM_WARP_MAX) {
+        const int grid = ceil_div(nvec, TRSM_WARP_VECS);
+#define FG_WARP(L, U) trsm_diag_warp_kernel<T, L, U><<<grid, 32 * TRSM_WARP_VECS, 0, stream>>>(kb, M0, mi, mp, X0, xs, vs, nvec)
+        if (lowerM) { if (unit) FG_WARP(true, true); else FG_WARP(true, false); }
+        else { if (unit) FG_WARP(false, true); else FG_WARP(false, false); }
+#undef FG_WARP
     } else {
-        const int grid = ceil_div(nvec, TRSM_WARPS);
-#define FG_NARROW(L, U) trsm_diag_narrow_kernel<T, L, U><<<grid, 32 * TRSM_WARPS, 0, stream>>>(kb, M0, mi, mp, X0, xs, vs, nvec)
-        if (lowerM) { if (unit) FG_NARROW(true, true); else FG_NARROW(true, false); }
-        else { if (unit) FG_NARROW(false, true); else FG_NARROW(false, false); }
-#undef FG_NARROW
+        const int grid = ceil_div(nvec, TRSM_VPC);
+#define FG_TILE(L, U) trsm_diag_tile_kernel<T, L, U><<<grid, TRSM_THREADS, 0, stream>>>(kb, M0, mi, mp, X0, xs, vs, nvec)
+        if (lowerM) { if (unit) FG_TILE(true, true); else FG_TILE(true, false); }
+        else { if (unit) FG_TILE(false, true); else FG_TILE(false, false); }
+#undef FG_TILE
     }
     FG_CUDA(cudaGetLastError());
     return kOk;

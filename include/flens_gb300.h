@@ -71,6 +71,37 @@ void dgetrs_(const char *TRANS, const int *N, const int *NRHS, const double *A,
 void dgesv_(const int *N, const int *NRHS, double *A, const int *LDA, int *IPIV,
             double *B, const int *LDB, int *INFO);
 
+/* C <- alpha*A*A^T + beta*C (TRANS='N') or alpha*A^T*A + beta*C ('T'/'C') on
+ * the UPLO triangle of C.  Replaces dsyrk_ at
+ * flens/blas/interface/blas/syrk.cc:104-160 (-> blas::rk ->
+ * cxxblas::syrk, cxxblas/level3/syrk.tcc:42-90: the triangle is scaled by
+ * beta unless beta == 1, then k rank-1 updates; no alpha == 0 shortcut). */
+void dsyrk_(const char *UPLO, const char *TRANS, const int *N, const int *K,
+            const double *ALPHA, const double *A, const int *LDA,
+            const double *BETA, double *C, const int *LDC);
+
+/* Cholesky factorisation A = L*L^T (UPLO='L') or U^T*U ('U') of the UPLO
+ * triangle in place; INFO=k>0: the leading minor of order k is not positive
+ * definite.  UPLO must be exactly 'U' or 'L', as in the reference.
+ * Replaces dpotrf_ at flens/lapack/interface/src/potrf.cc:11-41
+ * (-> lapack::potrf flens/lapack/po/potrf.tcc:56-150). */
+void dpotrf_(const char *UPLO, const int *N, double *A, const int *LDA,
+             int *INFO);
+
+/* Solve A*X = B from dpotrf_'s factor.
+ * Replaces dpotrs_ at flens/lapack/interface/src/potrs.cc:13-49
+ * (-> lapack::potrs flens/lapack/po/potrs.tcc:54-100). */
+void dpotrs_(const char *UPLO, const int *N, const int *NRHS, const double *A,
+             const int *LDA, double *B, const int *LDB, int *INFO);
+
+/* Factor and solve a symmetric positive definite system (no solve when
+ * INFO>0).  Replaces dposv_ at flens/lapack/interface/src/posv.cc:13-51
+ * (-> lapack::posv flens/lapack/po/posv.tcc:55-70).  Unlike the reference's
+ * shim, which discards posv's return value, INFO reports a failed
+ * factorisation (LAPACK DPOSV semantics). */
+void dposv_(const char *UPLO, const int *N, const int *NRHS, double *A,
+            const int *LDA, double *B, const int *LDB, int *INFO);
+
 /* Weak default error handler (prints, does not stop).  Link your own
  * xerbla_ to override it, as with Netlib BLAS/LAPACK. */
 void xerbla_(const char *SRNAME, const int *INFO, int SRNAME_LEN);
@@ -102,6 +133,26 @@ int flens_gb300_dgetrs(char trans, int n, int nrhs, const double *A, int ldA,
  * device int) and solves only when it is 0; the solve is queued async. */
 int flens_gb300_dgesv(int n, int nrhs, double *A, int ldA, int *ipiv, double *B,
                       int ldB, int *info, void *stream);
+
+/* dsyrk on device memory (UPLO/TRANS in either case).  Async on stream. */
+int flens_gb300_dsyrk(char uplo, char trans, int n, int k, double alpha,
+                      const double *A, int ldA, double beta, double *C,
+                      int ldC, void *stream);
+
+/* dpotrf on device memory; info is a device int.  Blocked right-looking
+ * (64-column steps: potf2 of the diagonal block, trsm, syrk of the trailing
+ * triangle); waits for the stream once per step to stop at the first
+ * non-positive pivot. */
+int flens_gb300_dpotrf(char uplo, int n, double *A, int ldA, int *info,
+                       void *stream);
+
+/* dpotrs on device memory.  Async on stream. */
+int flens_gb300_dpotrs(char uplo, int n, int nrhs, const double *A, int ldA,
+                       double *B, int ldB, void *stream);
+
+/* dposv on device memory: dpotrf, then dpotrs when *info (device) is 0. */
+int flens_gb300_dposv(char uplo, int n, int nrhs, double *A, int ldA,
+                      double *B, int ldB, int *info, void *stream);
 
 /* ------------------------------------------- precision form (extension) --- */
 

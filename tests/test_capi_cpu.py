@@ -119,6 +119,39 @@ def test_lapack_argument_errors():
         assert info.value == want and name == "DGESV" and pos == -want
 
 
+@pytest.mark.parametrize("args,pos", [
+    (("X", "N", 2, 2, 2, 2), 1),
+    (("L", "X", 2, 2, 2, 2), 2),
+    (("L", "N", -1, 2, 2, 2), 3),
+    (("L", "N", 2, -1, 2, 2), 4),
+    (("L", "N", 3, 2, 2, 3), 7),
+    (("U", "T", 2, 3, 2, 2), 7),
+    (("L", "N", 3, 2, 3, 2), 10),
+])
+def test_dsyrk_argument_errors(args, pos):
+    uplo, tr, n, k, lda, ldc = args
+    name, info = _xerbla_after(lambda: fg.lib().dsyrk_(
+        uplo.encode(), tr.encode(), _i(n), _i(k), _d(1.0), NULLD, _i(lda), _d(0.0), NULLD, _i(ldc)))
+    assert name == "DSYRK" and info == pos
+
+
+def test_cholesky_argument_errors():
+    # flens/lapack/interface/src/{potrf,potrs,posv}.cc: UPLO exactly 'U' or 'L'
+    L = fg.lib()
+    info = ctypes.c_int(0)
+    for (uplo, n, lda, want) in [("X", 2, 2, -1), ("l", 2, 2, -1), ("L", -1, 2, -2), ("U", 3, 2, -4)]:
+        name, pos = _xerbla_after(lambda: L.dpotrf_(uplo.encode(), _i(n), NULLD, _i(lda),
+                                                    ctypes.byref(info)))
+        assert info.value == want and name == "DPOTRF" and pos == -want
+    for f, nm in ((L.dpotrs_, "DPOTRS"), (L.dposv_, "DPOSV")):
+        for (uplo, n, nrhs, lda, ldb, want) in [("u", 2, 1, 2, 2, -1), ("L", -1, 1, 2, 2, -2),
+                                                ("L", 2, -1, 2, 2, -3), ("U", 3, 1, 2, 3, -5),
+                                                ("L", 3, 1, 3, 2, -7)]:
+            name, pos = _xerbla_after(lambda: f(uplo.encode(), _i(n), _i(nrhs), NULLD, _i(lda),
+                                                NULLD, _i(ldb), ctypes.byref(info)))
+            assert info.value == want and name == nm and pos == -want
+
+
 def test_quick_returns_touch_nothing():
     # m==0 / n==0 return before any device work (gemm.tcc:54-56, trf.tcc:81-83)
     L = fg.lib()
@@ -127,6 +160,15 @@ def test_quick_returns_touch_nothing():
     assert info.value == 0
     L.dgemm_(b"N", b"N", _i(0), _i(3), _i(2), _d(1.0), NULLD, _i(1), NULLD, _i(2), _d(0.0),
              NULLD, _i(1))
+
+
+def test_device_api_argument_errors_cholesky(flib):
+    assert flib.flens_gb300_dpotrf(b"X", 1, None, 1, None, None) == -1
+    assert flib.flens_gb300_dpotrf(b"L", 3, None, 2, None, None) == -4
+    assert flib.flens_gb300_dpotrs(b"U", 2, -1, None, 2, None, 2, None) == -3
+    assert flib.flens_gb300_dposv(b"L", 3, 1, None, 3, None, 2, None, None) == -7
+    assert flib.flens_gb300_dsyrk(b"L", b"Q", 1, 1, 1.0, None, 1, 0.0, None, 1, None) == -2
+    assert flib.flens_gb300_dsyrk(b"U", b"T", 2, 3, 1.0, None, 2, 0.0, None, 2, None) == -7
 
 
 def test_device_api_argument_errors(flib):
