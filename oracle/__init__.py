@@ -77,6 +77,11 @@ class Port:
         L.oracle_dgesv.argtypes = [i, i, _c_double_p, i, _c_int_p, _c_double_p, i]
         L.oracle_dgesv.restype = i
         L.oracle_dsyrk.argtypes = [c, c, i, i, d, _c_double_p, i, d, _c_double_p, i]
+        L.oracle_dtrmm.argtypes = [c, c, c, c, i, i, d, _c_double_p, i, _c_double_p, i]
+        L.oracle_dsymm.argtypes = [c, c, i, i, d, _c_double_p, i, _c_double_p, i, d,
+                                   _c_double_p, i]
+        L.oracle_dsyr2k.argtypes = [c, c, i, i, d, _c_double_p, i, _c_double_p, i, d,
+                                    _c_double_p, i]
         L.oracle_dpotrf_nb.argtypes = [c, i, _c_double_p, i, i]
         L.oracle_dpotrf_nb.restype = i
         L.oracle_dpotrs.argtypes = [c, i, i, _c_double_p, i, _c_double_p, i]
@@ -142,6 +147,29 @@ class Port:
                               max(1, A.shape[0]), beta, _dp(C), max(1, n))
         return C
 
+    def dtrmm(self, side, uplo, transA, diag, alpha, A, B):
+        _check_f64(A), _check_f64(B)
+        m, n = B.shape
+        self.lib.oracle_dtrmm(side.encode(), uplo.encode(), transA.encode(), diag.encode(), m, n,
+                              alpha, _dp(A), max(1, A.shape[0]), _dp(B), max(1, m))
+        return B
+
+    def dsymm(self, side, uplo, alpha, A, B, beta, C):
+        _check_f64(A), _check_f64(B), _check_f64(C)
+        m, n = C.shape
+        self.lib.oracle_dsymm(side.encode(), uplo.encode(), m, n, alpha, _dp(A),
+                              max(1, A.shape[0]), _dp(B), max(1, m), beta, _dp(C), max(1, m))
+        return C
+
+    def dsyr2k(self, uplo, trans, alpha, A, B, beta, C):
+        _check_f64(A), _check_f64(B), _check_f64(C)
+        n = C.shape[0]
+        k = A.shape[1] if trans.upper() == "N" else A.shape[0]
+        self.lib.oracle_dsyr2k(uplo.encode(), trans.encode(), n, k, alpha, _dp(A),
+                               max(1, A.shape[0]), _dp(B), max(1, B.shape[0]), beta, _dp(C),
+                               max(1, n))
+        return C
+
     def dpotrf(self, uplo, A, nb: int = 64):
         _check_f64(A)
         n = A.shape[0]
@@ -194,6 +222,12 @@ class Reference:
         L.dsyrk_.argtypes = [cp, cp, _c_int_p, _c_int_p, _c_double_p, _c_double_p, _c_int_p,
                              _c_double_p, _c_double_p, _c_int_p]
         L.dpotrf_.argtypes = [cp, _c_int_p, _c_double_p, _c_int_p, _c_int_p]
+        L.dtrmm_.argtypes = [cp, cp, cp, cp, _c_int_p, _c_int_p, _c_double_p, _c_double_p,
+                             _c_int_p, _c_double_p, _c_int_p]
+        L.dsymm_.argtypes = [cp, cp, _c_int_p, _c_int_p, _c_double_p, _c_double_p, _c_int_p,
+                             _c_double_p, _c_int_p, _c_double_p, _c_double_p, _c_int_p]
+        L.dsyr2k_.argtypes = [cp, cp, _c_int_p, _c_int_p, _c_double_p, _c_double_p, _c_int_p,
+                              _c_double_p, _c_int_p, _c_double_p, _c_double_p, _c_int_p]
         L.dpotrs_.argtypes = [cp, _c_int_p, _c_int_p, _c_double_p, _c_int_p, _c_double_p,
                               _c_int_p, _c_int_p]
         L.dposv_.argtypes = [cp, _c_int_p, _c_int_p, _c_double_p, _c_int_p, _c_double_p,
@@ -261,6 +295,28 @@ class Reference:
         self.lib.dsyrk_(uplo.encode(), trans.encode(), self._i(n), self._i(k), self._d(alpha),
                         _dp(A), self._i(max(1, A.shape[0])), self._d(beta), _dp(C),
                         self._i(max(1, n)))
+        return C
+
+    def dtrmm(self, side, uplo, transA, diag, alpha, A, B):
+        m, n = B.shape
+        self.lib.dtrmm_(side.encode(), uplo.encode(), transA.encode(), diag.encode(),
+                        self._i(m), self._i(n), self._d(alpha), _dp(A),
+                        self._i(max(1, A.shape[0])), _dp(B), self._i(max(1, m)))
+        return B
+
+    def dsymm(self, side, uplo, alpha, A, B, beta, C):
+        m, n = C.shape
+        self.lib.dsymm_(side.encode(), uplo.encode(), self._i(m), self._i(n), self._d(alpha),
+                        _dp(A), self._i(max(1, A.shape[0])), _dp(B), self._i(max(1, m)),
+                        self._d(beta), _dp(C), self._i(max(1, m)))
+        return C
+
+    def dsyr2k(self, uplo, trans, alpha, A, B, beta, C):
+        n = C.shape[0]
+        k = A.shape[1] if trans.upper() == "N" else A.shape[0]
+        self.lib.dsyr2k_(uplo.encode(), trans.encode(), self._i(n), self._i(k), self._d(alpha),
+                         _dp(A), self._i(max(1, A.shape[0])), _dp(B), self._i(max(1, B.shape[0])),
+                         self._d(beta), _dp(C), self._i(max(1, n)))
         return C
 
     def dpotrf(self, uplo, A):

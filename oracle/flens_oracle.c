@@ -385,6 +385,166 @@ void oracle_dsyrk(char upLo, char trans, int n, int k, double alpha,
 }
 
 /*
+ * TRMM.  cxxblas/level3/trmm.tcc:40-70: every vector (column of B for
+ * side=Left, row for side=Right) is multiplied by the effective triangle M
+ * (op(A), or op(A)^T for side=Right) with trmv (cxxblas/level2/trmv.tcc:
+ * 42-200): x_i <- sum over the triangle row i of M(i,p) x_p, the dot started
+ * at zero in increasing p, the diagonal term included unless unit, where
+ * x_i + dot(off-diagonal) is taken; rows are visited so that only old values
+ * are read.  alpha multiplies B at the end (gescal).
+ */
+void oracle_dtrmm(char side, char upLo, char transA, char diag, int m, int n,
+                  double alpha, const double *A, int ldA, double *B, int ldB)
+{
+    if (m == 0 || n == 0) {
+        return;
+    }
+    const int left = (side == 'L' || side == 'l');
+    const int lowerA = (upLo == 'L' || upLo == 'l');
+    const int nT = is_notrans(transA);
+    const int unit = (diag == 'U' || diag == 'u');
+    const int ka = left ? m : n;
+    const int nVec = left ? n : m;
+    size_t mi, mp;
+    int lowerM;
+    if (left) {
+        lowerM = lowerA ^ (!nT);
+        mi = nT ? 1 : (size_t)ldA;
+        mp = nT ? (size_t)ldA : 1;
+    } else {
+        lowerM = lowerA ^ nT;
+        mi = nT ? (size_t)ldA : 1;
+        mp = nT ? 1 : (size_t)ldA;
+    }
+    const size_t xs = left ? 1 : (size_t)ldB;
+    const size_t vs = left ? (size_t)ldB : 1;
+    for (int v = 0; v < nVec; ++v) {
+        double *x = B + (size_t)v * vs;
+        if (lowerM) {
+            for (int i = ka - 1; i >= 0; --i) {
+                double s = 0.0;
+                const int pe = unit ? i : i + 1;
+                for (int p = 0; p < pe; ++p) {
+                    s += A[(size_t)i * mi + (size_t)p * mp] * x[(size_t)p * xs];
+                }
+                x[(size_t)i * xs] = unit ? x[(size_t)i * xs] + s : s;
+            }
+        } else {
+            for (int i = 0; i < ka; ++i) {
+                double s = 0.0;
+                for (int p = unit ? i + 1 : i; p < ka; ++p) {
+                    s += A[(size_t)i * mi + (size_t)p * mp] * x[(size_t)p * xs];
+                }
+                x[(size_t)i * xs] = unit ? x[(size_t)i * xs] + s : s;
+            }
+        }
+    }
+    for (int j = 0; j < n; ++j) {
+        for (int i = 0; i < m; ++i) {
+            B[IDX(i, j, ldB)] *= alpha;
+        }
+    }
+}
+
+/*
+ * SYMM.  cxxblas/level3/symm.tcc:40-70: C is scaled by beta first (gescal, a
+ * multiply), then every vector (column of C for side=Left, row for
+ * side=Right, with the matching vector x of B) gets symv with beta 1
+ * (cxxblas/level2/symv.tcc:42-80): two passes over all i, y_i += alpha*s1_i
+ * then y_i += alpha*s2_i, where with the lower triangle stored
+ * s1_i = sum_{p>=i} A(p,i) x_p and s2_i = sum_{p<i} A(i,p) x_p, and with the
+ * upper one s1_i = sum_{p<i} A(p,i) x_p and s2_i = sum_{p>=i} A(i,p) x_p;
+ * every dot started at zero in increasing p.  No alpha == 0 shortcut.
+ */
+void oracle_dsymm(char side, char upLo, int m, int n, double alpha,
+                  const double *A, int ldA, const double *B, int ldB,
+                  double beta, double *C, int ldC)
+{
+    if (m == 0 || n == 0) {
+        return;
+    }
+    const int left = (side == 'L' || side == 'l');
+    const int lower = (upLo == 'L' || upLo == 'l');
+    const int ka = left ? m : n;
+    const int nVec = left ? n : m;
+    const size_t xs = left ? 1 : (size_t)ldB, xv = left ? (size_t)ldB : 1;
+    const size_t ys = left ? 1 : (size_t)ldC, yv = left ? (size_t)ldC : 1;
+    for (int j = 0; j < n; ++j) {
+        for (int i = 0; i < m; ++i) {
+            C[IDX(i, j, ldC)] *= beta;
+        }
+    }
+    for (int v = 0; v < nVec; ++v) {
+        const double *x = B + (size_t)v * xv;
+        double *y = C + (size_t)v * yv;
+        for (int pass = 0; pass < 2; ++pass) {
+            for (int i = 0; i < ka; ++i) {
+                double s = 0.0;
+                /* pass 0: the column of the stored triangle through A(i,i) for
+                 * lower, above it for upper; pass 1: the row part */
+                const int from_lower = (pass == 0) == (lower != 0);
+                if (from_lower) {
+                    if (pass == 0) {
+                        for (int p = i; p < ka; ++p) s += A[IDX(p, i, ldA)] * x[(size_t)p * xs];
+                    } else {
+                        for (int p = i; p < ka; ++p) s += A[IDX(i, p, ldA)] * x[(size_t)p * xs];
+                    }
+                } else {
+                    if (pass == 0) {
+                        for (int p = 0; p < i; ++p) s += A[IDX(p, i, ldA)] * x[(size_t)p * xs];
+                    } else {
+                        for (int p = 0; p < i; ++p) s += A[IDX(i, p, ldA)] * x[(size_t)p * xs];
+                    }
+                }
+                y[(size_t)i * ys] += alpha * s;
+            }
+        }
+    }
+}
+
+/*
+ * SYR2K.  cxxblas/level3/syr2k.tcc:42-95: the triangle is scaled by beta
+ * unless beta == 1 (syscal); k == 0 returns; then for l = 0..k-1 one syr2
+ * (cxxblas/level2/syr2.tcc:42-75) with x, y the l-th vectors of op(A), op(B):
+ * per column c of the triangle, first C(r,c) += (alpha*x_c)*y_r for all its
+ * rows r, then C(r,c) += (alpha*y_c)*x_r.
+ */
+void oracle_dsyr2k(char upLo, char trans, int n, int k, double alpha,
+                   const double *A, int ldA, const double *B, int ldB,
+                   double beta, double *C, int ldC)
+{
+    const int lower = (upLo == 'L' || upLo == 'l');
+    const int nT = is_notrans(trans);
+    if (beta != 1.0) {
+        for (int c = 0; c < n; ++c) {
+            const int r0 = lower ? c : 0, r1 = lower ? n : c + 1;
+            for (int r = r0; r < r1; ++r) {
+                C[IDX(r, c, ldC)] *= beta;
+            }
+        }
+    }
+    if (k == 0) {
+        return;
+    }
+    const size_t ai = nT ? 1 : (size_t)ldA, al = nT ? (size_t)ldA : 1;
+    const size_t bi = nT ? 1 : (size_t)ldB, bl = nT ? (size_t)ldB : 1;
+    for (int l = 0; l < k; ++l) {
+        const double *x = A + (size_t)l * al;
+        const double *y = B + (size_t)l * bl;
+        for (int c = 0; c < n; ++c) {
+            const double t1 = alpha * x[(size_t)c * ai], t2 = alpha * y[(size_t)c * bi];
+            const int r0 = lower ? c : 0, r1 = lower ? n : c + 1;
+            for (int r = r0; r < r1; ++r) {
+                C[IDX(r, c, ldC)] += t1 * y[(size_t)r * bi];
+            }
+            for (int r = r0; r < r1; ++r) {
+                C[IDX(r, c, ldC)] += t2 * x[(size_t)r * ai];
+            }
+        }
+    }
+}
+
+/*
  * GEMV.  cxxblas/level2/gemv.tcc:160-176 returns when m or n is 0 (before
  * any scaling); :42-130 maps column-major to row-major, scales y by beta
  * (scal, a multiply) and adds alpha*dot per element, the dot started at zero

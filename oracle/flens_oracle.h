@@ -63,6 +63,23 @@ int oracle_dgesv(int n, int nRhs, double *A, int ldA, int *piv,
 void oracle_dsyrk(char upLo, char trans, int n, int k, double alpha,
                   const double *A, int ldA, double beta, double *C, int ldC);
 
+/* B <- alpha*op(A)*B or alpha*B*op(A), A triangular
+ *                                               cxxblas/level3/trmm.tcc:40-70 */
+void oracle_dtrmm(char side, char upLo, char transA, char diag, int m, int n,
+                  double alpha, const double *A, int ldA, double *B, int ldB);
+
+/* C <- beta*C + alpha*A*B or alpha*B*A, A symmetric (upLo triangle stored)
+ *                                               cxxblas/level3/symm.tcc:40-70 */
+void oracle_dsymm(char side, char upLo, int m, int n, double alpha,
+                  const double *A, int ldA, const double *B, int ldB,
+                  double beta, double *C, int ldC);
+
+/* C <- beta*C + alpha*(op(A)op(B)^T + op(B)op(A)^T) on the upLo triangle
+ *                                               cxxblas/level3/syr2k.tcc:42-95 */
+void oracle_dsyr2k(char upLo, char trans, int n, int k, double alpha,
+                   const double *A, int ldA, const double *B, int ldB,
+                   double beta, double *C, int ldC);
+
 /* y <- beta*y + alpha*op(A)*x                  cxxblas/level2/gemv.tcc:42-200 */
 void oracle_dgemv(char trans, int m, int n, double alpha, const double *A,
                   int ldA, const double *x, int incX, double beta, double *y,

@@ -1,7 +1,8 @@
 """Generate the golden fixtures in this directory from the REFERENCE itself.
 
-Runs the reference's own Fortran-ABI shims (dgemm_, dtrsm_, dsyrk_, dgetrf_,
-dgetrs_, dgesv_, dpotrf_, dpotrs_, dposv_ compiled from the FLENS sources into
+Runs the reference's own Fortran-ABI shims (dgemm_, dtrsm_, dsyrk_, dtrmm_,
+dsymm_, dsyr2k_, dgetrf_, dgetrs_, dgesv_, dpotrf_, dpotrs_, dposv_ compiled
+from the FLENS sources into
 oracle/_ref/libflens_ref.so by
 ``make -C oracle ref``) on seeded inputs and stores the outputs.  Inputs come
 from ``oracle.splitmix_uniform(seed, m, n)`` (integer hashing, identical on
@@ -131,6 +132,59 @@ def syrk_inputs(i, n, k, tr):
     return A, C
 
 
+def trmm_case_list():
+    cases = []
+    for (m, n) in [(33, 17), (70, 3), (1, 5)]:
+        for side in "LR":
+            for uplo in "UL":
+                for ta in "NT":
+                    for diag in "UN":
+                        cases.append((m, n, side, uplo, ta, diag, 0.7))
+    cases.append((33, 17, "L", "L", "C", "N", 1.0))
+    cases.append((0, 4, "L", "U", "N", "N", 1.0))
+    return [(f"trmm{i:03d}", c) for i, c in enumerate(cases)]
+
+
+def trmm_inputs(i, m, n, side):
+    s = 15000 + 10 * i
+    ka = m if side == "L" else n
+    return U(s, ka, ka), U(s + 1, m, n)
+
+
+def symm_case_list():
+    cases = []
+    for (m, n) in [(33, 17), (70, 3), (1, 5), (0, 4)]:
+        for side in "LR":
+            for uplo in "UL":
+                cases.append((m, n, side, uplo, 1.5, 0.5))
+    for (a, b) in [(-1.0, 1.0), (0.0, 2.0), (2.0, 0.0)]:
+        cases.append((33, 17, "L", "L", a, b))
+    return [(f"symm{i:03d}", c) for i, c in enumerate(cases)]
+
+
+def symm_inputs(i, m, n, side):
+    s = 17000 + 10 * i
+    ka = m if side == "L" else n
+    return U(s, ka, ka), U(s + 1, m, n), U(s + 2, m, n)
+
+
+def syr2k_case_list():
+    cases = []
+    for (n, k) in [(0, 3), (5, 0), (7, 9), (40, 33)]:
+        for uplo in "LU":
+            for tr in "NTC":
+                cases.append((n, k, uplo, tr, 1.5, 0.5))
+    for (a, b) in [(-1.0, 1.0), (0.0, 2.0)]:
+        cases.append((40, 33, "U", "N", a, b))
+    return [(f"syr2k{i:03d}", c) for i, c in enumerate(cases)]
+
+
+def syr2k_inputs(i, n, k, tr):
+    s = 19000 + 10 * i
+    shape = (n, k) if tr == "N" else (k, n)
+    return U(s, *shape), U(s + 1, *shape), U(s + 2, n, n)
+
+
 def chol_case_list():
     """(n, uplo, kind): kind 'spd' (well conditioned) or 'notpd' (a negative
     pivot at n//2, so INFO = n//2 + 1 with the factor of the leading block)."""
@@ -191,6 +245,15 @@ def generate_small(R):
     for i, (name, (n, k, uplo, tr, a, b)) in enumerate(syrk_case_list()):
         A, C = syrk_inputs(i, n, k, tr)
         out[name] = R.dsyrk(uplo, tr, a, A, b, C.copy(order="F"))
+    for i, (name, (m, n, side, uplo, ta, diag, alpha)) in enumerate(trmm_case_list()):
+        A, B = trmm_inputs(i, m, n, side)
+        out[name] = R.dtrmm(side, uplo, ta, diag, alpha, A, B.copy(order="F"))
+    for i, (name, (m, n, side, uplo, a, b)) in enumerate(symm_case_list()):
+        A, B, C = symm_inputs(i, m, n, side)
+        out[name] = R.dsymm(side, uplo, a, A, B, b, C.copy(order="F"))
+    for i, (name, (n, k, uplo, tr, a, b)) in enumerate(syr2k_case_list()):
+        A, B, C = syr2k_inputs(i, n, k, tr)
+        out[name] = R.dsyr2k(uplo, tr, a, A, B, b, C.copy(order="F"))
     for i, (name, (n, uplo, kind)) in enumerate(chol_case_list()):
         A = chol_input(i, n, kind)
         info = R.dpotrf(uplo, A)

@@ -70,6 +70,19 @@ def test_syrk_fixtures_bitwise(golden, port):
         assert np.array_equal(out, golden[name]), name
 
 
+def test_trmm_symm_syr2k_fixtures_bitwise(golden, port):
+    for i, (name, (m, n, side, uplo, ta, diag, alpha)) in enumerate(G.trmm_case_list()):
+        A, B = G.trmm_inputs(i, m, n, side)
+        out = port.dtrmm(side, uplo, ta, diag, alpha, A, B.copy(order="F"))
+        assert np.array_equal(out, golden[name]), name
+    for i, (name, (m, n, side, uplo, a, b)) in enumerate(G.symm_case_list()):
+        A, B, C = G.symm_inputs(i, m, n, side)
+        assert np.array_equal(port.dsymm(side, uplo, a, A, B, b, C.copy(order="F")), golden[name]), name
+    for i, (name, (n, k, uplo, tr, a, b)) in enumerate(G.syr2k_case_list()):
+        A, B, C = G.syr2k_inputs(i, n, k, tr)
+        assert np.array_equal(port.dsyr2k(uplo, tr, a, A, B, b, C.copy(order="F")), golden[name]), name
+
+
 def test_cholesky_fixtures_bitwise(golden, port):
     for i, (name, (n, uplo, kind)) in enumerate(G.chol_case_list()):
         A = G.chol_input(i, n, kind)
