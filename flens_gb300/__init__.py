@@ -83,6 +83,15 @@ def lib() -> ctypes.CDLL:
     L.dpotrs_.restype = None
     L.dposv_.argtypes = [cp, _ip, _ip, _dp, _ip, _dp, _ip, _ip]
     L.dposv_.restype = None
+    L.dtrmm_.argtypes = [cp, cp, cp, cp, _ip, _ip, _dp, _dp, _ip, _dp, _ip]
+    L.dtrmm_.restype = None
+    L.dsymm_.argtypes = [cp, cp, _ip, _ip, _dp, _dp, _ip, _dp, _ip, _dp, _dp, _ip]
+    L.dsymm_.restype = None
+    L.dsyr2k_.argtypes = [cp, cp, _ip, _ip, _dp, _dp, _ip, _dp, _ip, _dp, _dp, _ip]
+    L.dsyr2k_.restype = None
+    L.flens_gb300_dtrmm.argtypes = [_c, _c, _c, _c, _i, _i, _d, _v, _i, _v, _i, _v]
+    L.flens_gb300_dsymm.argtypes = [_c, _c, _i, _i, _d, _v, _i, _v, _i, _d, _v, _i, _v]
+    L.flens_gb300_dsyr2k.argtypes = [_c, _c, _i, _i, _d, _v, _i, _v, _i, _d, _v, _i, _v]
     L.flens_gb300_dsyrk.argtypes = [_c, _c, _i, _i, _d, _v, _i, _d, _v, _i, _v]
     L.flens_gb300_dpotrf.argtypes = [_c, _i, _v, _i, _v, _v]
     L.flens_gb300_dpotrs.argtypes = [_c, _i, _i, _v, _i, _v, _i, _v]
@@ -101,7 +110,8 @@ def lib() -> ctypes.CDLL:
     for f in ("flens_gb300_dgemm", "flens_gb300_dtrsm", "flens_gb300_dgetrf",
               "flens_gb300_dgetrs", "flens_gb300_dgesv", "flens_gb300_sync",
               "flens_gb300_dsyrk", "flens_gb300_dpotrf", "flens_gb300_dpotrs",
-              "flens_gb300_dposv"):
+              "flens_gb300_dposv", "flens_gb300_dtrmm", "flens_gb300_dsymm",
+              "flens_gb300_dsyr2k"):
         getattr(L, f).restype = _i
     L.flens_gb300_last_error.restype = ctypes.c_char_p
     L.flens_gb300_last_error.argtypes = []
@@ -219,6 +229,34 @@ def dsyrk(uplo: str, trans: str, alpha: float, A: np.ndarray, beta: float, C: np
     k = A.shape[1] if trans.upper() == "N" else A.shape[0]
     lib().dsyrk_(uplo.encode(), trans.encode(), _ref(n, _i), _ref(k, _i), _ref(alpha, _d), _fd(A),
                  _ref(max(1, A.shape[0]), _i), _ref(beta, _d), _fd(C), _ref(max(1, n), _i))
+    return C
+
+
+def dtrmm(side: str, uplo: str, transA: str, diag: str, alpha: float, A: np.ndarray,
+          B: np.ndarray) -> np.ndarray:
+    m, n = B.shape
+    lib().dtrmm_(side.encode(), uplo.encode(), transA.encode(), diag.encode(), _ref(m, _i),
+                 _ref(n, _i), _ref(alpha, _d), _fd(A), _ref(max(1, A.shape[0]), _i), _fd(B),
+                 _ref(max(1, m), _i))
+    return B
+
+
+def dsymm(side: str, uplo: str, alpha: float, A: np.ndarray, B: np.ndarray, beta: float,
+          C: np.ndarray) -> np.ndarray:
+    m, n = C.shape
+    lib().dsymm_(side.encode(), uplo.encode(), _ref(m, _i), _ref(n, _i), _ref(alpha, _d), _fd(A),
+                 _ref(max(1, A.shape[0]), _i), _fd(B), _ref(max(1, m), _i), _ref(beta, _d), _fd(C),
+                 _ref(max(1, m), _i))
+    return C
+
+
+def dsyr2k(uplo: str, trans: str, alpha: float, A: np.ndarray, B: np.ndarray, beta: float,
+           C: np.ndarray) -> np.ndarray:
+    n = C.shape[0]
+    k = A.shape[1] if trans.upper() == "N" else A.shape[0]
+    lib().dsyr2k_(uplo.encode(), trans.encode(), _ref(n, _i), _ref(k, _i), _ref(alpha, _d), _fd(A),
+                  _ref(max(1, A.shape[0]), _i), _fd(B), _ref(max(1, B.shape[0]), _i),
+                  _ref(beta, _d), _fd(C), _ref(max(1, n), _i))
     return C
 
 

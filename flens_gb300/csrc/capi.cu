@@ -8,6 +8,9 @@
 //      dgetrs_  flens/lapack/interface/src/getrs.cc:13-53
 //      dgesv_   flens/lapack/interface/src/gesv.cc:13-49
 //      dsyrk_   flens/blas/interface/blas/syrk.cc:104-160
+//      dtrmm_   flens/blas/interface/blas/trmm.cc:108-205
+//      dsymm_   flens/blas/interface/blas/symm.cc:93-174
+//      dsyr2k_  flens/blas/interface/blas/syr2k.cc:115-218
 //      dpotrf_  flens/lapack/interface/src/potrf.cc:11-41
 //      dpotrs_  flens/lapack/interface/src/potrs.cc:13-49
 //      dposv_   flens/lapack/interface/src/posv.cc:13-51
@@ -394,6 +397,110 @@ FG_API void dsyrk_(const char *UPLO, const char *TRANS, const int *N, const int 
     if (st != kOk) fprintf(stderr, "[flens_gb300] dsyrk_ failed (%d): %s\n", st, flens_gb300_last_error());
 }
 
+// ---------------------------------------------------------------- dtrmm_ --
+// flens/blas/interface/blas/trmm.cc:108-205: upper-cased, checked 1, 2, 3, 4, 5, 6, 9, 11
+FG_API void dtrmm_(const char *SIDE, const char *UPLO, const char *TRANSA, const char *DIAG,
+                   const int *M, const int *N, const double *ALPHA, const double *A,
+                   const int *LDA, double *B, const int *LDB) {
+    const char side = (char)toupper(*SIDE), uplo = (char)toupper(*UPLO);
+    const char ta = (char)toupper(*TRANSA), diag = (char)toupper(*DIAG);
+    const int nRowA = (side == 'L') ? *M : *N;
+    int info = 0;
+    if (side != 'L' && side != 'R') info = 1;
+    else if (uplo != 'U' && uplo != 'L') info = 2;
+    else if (ta != 'N' && ta != 'T' && ta != 'C') info = 3;
+    else if (diag != 'U' && diag != 'N') info = 4;
+    else if (*M < 0) info = 5;
+    else if (*N < 0) info = 6;
+    else if (*LDA < std::max(1, nRowA)) info = 9;
+    else if (*LDB < std::max(1, *M)) info = 11;
+    if (info != 0) {
+        report_xerbla("DTRMM ", info);
+        return;
+    }
+    const int m = *M, n = *N;
+    if (m == 0 || n == 0) return;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    DevView a, b;
+    const int ka = side == 'L' ? m : n;
+    if (st == kOk) st = view_in(0, A, ka, ka, *LDA, true, s, &a);
+    if (st == kOk) st = view_in(1, B, m, n, *LDB, true, s, &b);
+    if (st == kOk) st = dtrmm_launch(side, uplo, ta == 'C' ? 'T' : ta, diag, m, n, *ALPHA, a.p, a.ld, b.p, b.ld, s);
+    if (st == kOk) st = view_out(b, B, m, n, *LDB, s);
+    if (st == kOk) st = finish(s);
+    if (st != kOk) fprintf(stderr, "[flens_gb300] dtrmm_ failed (%d): %s\n", st, flens_gb300_last_error());
+}
+
+// ---------------------------------------------------------------- dsymm_ --
+// flens/blas/interface/blas/symm.cc:93-174: upper-cased, checked 1, 2, 3, 4, 7, 9, 12
+FG_API void dsymm_(const char *SIDE, const char *UPLO, const int *M, const int *N,
+                   const double *ALPHA, const double *A, const int *LDA, const double *B,
+                   const int *LDB, const double *BETA, double *C, const int *LDC) {
+    const char side = (char)toupper(*SIDE), uplo = (char)toupper(*UPLO);
+    const int nRowA = (side == 'L') ? *M : *N;
+    int info = 0;
+    if (side != 'L' && side != 'R') info = 1;
+    else if (uplo != 'U' && uplo != 'L') info = 2;
+    else if (*M < 0) info = 3;
+    else if (*N < 0) info = 4;
+    else if (*LDA < std::max(1, nRowA)) info = 7;
+    else if (*LDB < std::max(1, *M)) info = 9;
+    else if (*LDC < std::max(1, *M)) info = 12;
+    if (info != 0) {
+        report_xerbla("DSYMM ", info);
+        return;
+    }
+    const int m = *M, n = *N;
+    if (m == 0 || n == 0) return;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    DevView a, b, c;
+    const int ka = side == 'L' ? m : n;
+    if (st == kOk) st = view_in(0, A, ka, ka, *LDA, true, s, &a);
+    if (st == kOk) st = view_in(1, B, m, n, *LDB, true, s, &b);
+    if (st == kOk) st = view_in(2, C, m, n, *LDC, true, s, &c);
+    if (st == kOk) st = dsymm_launch(side, uplo, m, n, *ALPHA, a.p, a.ld, b.p, b.ld, *BETA, c.p, c.ld, s);
+    if (st == kOk) st = view_out(c, C, m, n, *LDC, s);
+    if (st == kOk) st = finish(s);
+    if (st != kOk) fprintf(stderr, "[flens_gb300] dsymm_ failed (%d): %s\n", st, flens_gb300_last_error());
+}
+
+// --------------------------------------------------------------- dsyr2k_ --
+// flens/blas/interface/blas/syr2k.cc:115-218: upper-cased, checked 1, 2, 3, 4, 7, 9, 12
+FG_API void dsyr2k_(const char *UPLO, const char *TRANS, const int *N, const int *K,
+                    const double *ALPHA, const double *A, const int *LDA, const double *B,
+                    const int *LDB, const double *BETA, double *C, const int *LDC) {
+    const char uplo = (char)toupper(*UPLO), tr = (char)toupper(*TRANS);
+    const int nRowA = (tr == 'N') ? *N : *K;
+    int info = 0;
+    if (uplo != 'U' && uplo != 'L') info = 1;
+    else if (tr != 'N' && tr != 'T' && tr != 'C') info = 2;
+    else if (*N < 0) info = 3;
+    else if (*K < 0) info = 4;
+    else if (*LDA < std::max(1, nRowA)) info = 7;
+    else if (*LDB < std::max(1, nRowA)) info = 9;
+    else if (*LDC < std::max(1, *N)) info = 12;
+    if (info != 0) {
+        report_xerbla("DSYR2K", info);
+        return;
+    }
+    const int n = *N, k = *K;
+    if (n == 0) return;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    DevView a, b, c;
+    const int ra = tr == 'N' ? n : k, ca = tr == 'N' ? k : n;
+    if (st == kOk && k > 0) st = view_in(0, A, ra, ca, *LDA, true, s, &a);
+    if (st == kOk && k > 0) st = view_in(1, B, ra, ca, *LDB, true, s, &b);
+    if (st == kOk) st = view_in(2, C, n, n, *LDC, true, s, &c);
+    if (st == kOk)
+        st = dsyr2k_launch(uplo, tr == 'N' ? 'N' : 'T', n, k, *ALPHA, a.p, a.ld, b.p, b.ld, *BETA, c.p, c.ld, s);
+    if (st == kOk) st = view_out(c, C, n, n, *LDC, s);
+    if (st == kOk) st = finish(s);
+    if (st != kOk) fprintf(stderr, "[flens_gb300] dsyr2k_ failed (%d): %s\n", st, flens_gb300_last_error());
+}
+
 // ------------------------------------------------------ LAPACK Cholesky --
 namespace {
 
@@ -518,6 +625,56 @@ FG_API int flens_gb300_dsyrk(char uplo, char trans, int n, int k, double alpha, 
     if (ldC < std::max(1, n)) return -10;
     return dsyrk_launch(uplo, trans == 'N' ? 'N' : 'T', n, k, alpha, A, ldA, beta, C, ldC,
                         as_stream(stream));
+}
+
+FG_API int flens_gb300_dtrmm(char side, char uplo, char transA, char diag, int m, int n,
+                             double alpha, const double *A, int ldA, double *B, int ldB,
+                             void *stream) {
+    side = (char)toupper(side);
+    uplo = (char)toupper(uplo);
+    transA = (char)toupper(transA);
+    diag = (char)toupper(diag);
+    if (side != 'L' && side != 'R') return -1;
+    if (uplo != 'U' && uplo != 'L') return -2;
+    if (transA != 'N' && transA != 'T' && transA != 'C') return -3;
+    if (diag != 'U' && diag != 'N') return -4;
+    if (m < 0) return -5;
+    if (n < 0) return -6;
+    if (ldA < std::max(1, side == 'L' ? m : n)) return -9;
+    if (ldB < std::max(1, m)) return -11;
+    return dtrmm_launch(side, uplo, transA == 'C' ? 'T' : transA, diag, m, n, alpha, A, ldA, B,
+                        ldB, as_stream(stream));
+}
+
+FG_API int flens_gb300_dsymm(char side, char uplo, int m, int n, double alpha, const double *A,
+                             int ldA, const double *B, int ldB, double beta, double *C, int ldC,
+                             void *stream) {
+    side = (char)toupper(side);
+    uplo = (char)toupper(uplo);
+    if (side != 'L' && side != 'R') return -1;
+    if (uplo != 'U' && uplo != 'L') return -2;
+    if (m < 0) return -3;
+    if (n < 0) return -4;
+    if (ldA < std::max(1, side == 'L' ? m : n)) return -7;
+    if (ldB < std::max(1, m)) return -9;
+    if (ldC < std::max(1, m)) return -12;
+    return dsymm_launch(side, uplo, m, n, alpha, A, ldA, B, ldB, beta, C, ldC, as_stream(stream));
+}
+
+FG_API int flens_gb300_dsyr2k(char uplo, char trans, int n, int k, double alpha, const double *A,
+                              int ldA, const double *B, int ldB, double beta, double *C, int ldC,
+                              void *stream) {
+    uplo = (char)toupper(uplo);
+    trans = (char)toupper(trans);
+    if (uplo != 'U' && uplo != 'L') return -1;
+    if (trans != 'N' && trans != 'T' && trans != 'C') return -2;
+    if (n < 0) return -3;
+    if (k < 0) return -4;
+    if (ldA < std::max(1, trans == 'N' ? n : k)) return -7;
+    if (ldB < std::max(1, trans == 'N' ? n : k)) return -9;
+    if (ldC < std::max(1, n)) return -12;
+    return dsyr2k_launch(uplo, trans == 'N' ? 'N' : 'T', n, k, alpha, A, ldA, B, ldB, beta, C, ldC,
+                         as_stream(stream));
 }
 
 FG_API int flens_gb300_dpotrf(char uplo, int n, double *A, int ldA, int *info, void *stream) {

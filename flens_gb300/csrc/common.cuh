@@ -176,6 +176,25 @@ int dsyrk_launch(char uplo, char trans, int n, int k, double alpha,
                  const double *A, int ldA, double beta, double *C, int ldC,
                  cudaStream_t stream);
 
+// C <- beta*C + alpha*op(A)*op(B)^T on the uplo triangle of C (trans 'N':
+// A, B n x k; 'T': k x n).
+int tri_gemm_launch(char uplo, char trans, int n, int k, double alpha,
+                    const double *A, int ldA, const double *B, int ldB,
+                    double beta, double *C, int ldC, cudaStream_t stream);
+
+// Level-3 BLAS on the GEMM engine (blas3.cu): trmm (B <- alpha op(A) B or
+// alpha B op(A), A triangular), symm (C <- beta C + alpha A B or alpha B A,
+// A symmetric), syr2k (C <- beta C + alpha (op(A) op(B)^T + op(B) op(A)^T)).
+int dtrmm_launch(char side, char uplo, char transA, char diag, int m, int n,
+                 double alpha, const double *A, int ldA, double *B, int ldB,
+                 cudaStream_t stream);
+int dsymm_launch(char side, char uplo, int m, int n, double alpha,
+                 const double *A, int ldA, const double *B, int ldB,
+                 double beta, double *C, int ldC, cudaStream_t stream);
+int dsyr2k_launch(char uplo, char trans, int n, int k, double alpha,
+                  const double *A, int ldA, const double *B, int ldB,
+                  double beta, double *C, int ldC, cudaStream_t stream);
+
 // Cholesky (uplo 'L': A = L L^T, 'U': A = U^T U) of the n x n uplo triangle
 // in place; *info (device) = first non-positive pivot (1-based) or 0.
 // Synchronises once per 64-column block to stop at the first failure.

@@ -425,12 +425,12 @@ int gemm_launch_t(char transA, char transB, int m, int n, int k, T alpha, const 
     return kOk;
 }
 
-// C <- beta*C + alpha*op(A)*op(A)^T on the uplo triangle of the n x n C
-// (cxxblas/level3/syrk.tcc:42-90): op(A) = A (n x k, trans 'N') or A^T.  The
-// triangle is scaled by beta unless beta == 1 (syscal); k == 0 only scales.
-// No alpha == 0 shortcut, as in the reference: NaN in A still reaches C.
-int dsyrk_launch(char uplo, char trans, int n, int k, double alpha, const double *A, int ldA,
-                 double beta, double *C, int ldC, cudaStream_t stream) {
+// C <- beta*C + alpha*op(A)*op(B)^T on the uplo triangle of the n x n C, op
+// = identity (trans 'N': A, B n x k) or transpose ('T': A, B k x n); only the
+// uplo triangle of C is read or written.  k == 0 only scales (unless beta ==
+// 1).  No alpha == 0 shortcut: the reference's syrk/syr2k have none.
+int tri_gemm_launch(char uplo, char trans, int n, int k, double alpha, const double *A, int ldA,
+                    const double *B, int ldB, double beta, double *C, int ldC, cudaStream_t stream) {
     if (n == 0) return kOk;
     if (k == 0) {
         if (beta == 1.0) return kOk;
@@ -444,20 +444,27 @@ int dsyrk_launch(char uplo, char trans, int n, int k, double alpha, const double
         return kErrUnsupported;
     }
     KTimer kt(kFamGemm, stream, (double)n * (n + 1) * (double)k,
-              8.0 * ((double)n * k + (double)n * (n + 1)));
-    trace("syrk %c%c n=%d k=%d", uplo, trans, n, k);
-    const double *Ak = k > 0 ? A : nullptr;
-    const int ldk = k > 0 ? ldA : 1;
-    // op(A) op(A)^T as gemm(op, op^T) with both operands A
+              8.0 * ((double)n * k * 2.0 + (double)n * (n + 1)));
+    const double *Ak = k > 0 ? A : nullptr, *Bk = k > 0 ? B : nullptr;
+    const int lda = k > 0 ? ldA : 1, ldb = k > 0 ? ldB : 1;
+    // op(A) op(B)^T as gemm(op, op^T)
     if (lower) {
-        if (nt) dgemm_fma_kernel<double, false, true, 1><<<grid, 256, 0, stream>>>(n, n, k, alpha, Ak, ldk, Ak, ldk, beta, C, ldC);
-        else dgemm_fma_kernel<double, true, false, 1><<<grid, 256, 0, stream>>>(n, n, k, alpha, Ak, ldk, Ak, ldk, beta, C, ldC);
+        if (nt) dgemm_fma_kernel<double, false, true, 1><<<grid, 256, 0, stream>>>(n, n, k, alpha, Ak, lda, Bk, ldb, beta, C, ldC);
+        else dgemm_fma_kernel<double, true, false, 1><<<grid, 256, 0, stream>>>(n, n, k, alpha, Ak, lda, Bk, ldb, beta, C, ldC);
     } else {
-        if (nt) dgemm_fma_kernel<double, false, true, 2><<<grid, 256, 0, stream>>>(n, n, k, alpha, Ak, ldk, Ak, ldk, beta, C, ldC);
-        else dgemm_fma_kernel<double, true, false, 2><<<grid, 256, 0, stream>>>(n, n, k, alpha, Ak, ldk, Ak, ldk, beta, C, ldC);
+        if (nt) dgemm_fma_kernel<double, false, true, 2><<<grid, 256, 0, stream>>>(n, n, k, alpha, Ak, lda, Bk, ldb, beta, C, ldC);
+        else dgemm_fma_kernel<double, true, false, 2><<<grid, 256, 0, stream>>>(n, n, k, alpha, Ak, lda, Bk, ldb, beta, C, ldC);
     }
     FG_CUDA(cudaGetLastError());
     return kOk;
+}
+
+// C <- beta*C + alpha*op(A)*op(A)^T on the uplo triangle of the n x n C
+// (cxxblas/level3/syrk.tcc:42-90): op(A) = A (n x k, trans 'N') or A^T.
+int dsyrk_launch(char uplo, char trans, int n, int k, double alpha, const double *A, int ldA,
+                 double beta, double *C, int ldC, cudaStream_t stream) {
+    trace("syrk %c%c n=%d k=%d", uplo, trans, n, k);
+    return tri_gemm_launch(uplo, trans, n, k, alpha, A, ldA, A, ldA, beta, C, ldC, stream);
 }
 
 int dgemm_launch(char transA, char transB, int m, int n, int k, double alpha,

@@ -80,6 +80,31 @@ void dsyrk_(const char *UPLO, const char *TRANS, const int *N, const int *K,
             const double *ALPHA, const double *A, const int *LDA,
             const double *BETA, double *C, const int *LDC);
 
+/* B <- alpha*op(A)*B (SIDE='L') or alpha*B*op(A) ('R'), A triangular.
+ * Replaces dtrmm_ at flens/blas/interface/blas/trmm.cc:108-205 (-> blas::mm
+ * -> cxxblas::trmm, cxxblas/level3/trmm.tcc:40-70: alpha applied after the
+ * product). */
+void dtrmm_(const char *SIDE, const char *UPLO, const char *TRANSA,
+            const char *DIAG, const int *M, const int *N, const double *ALPHA,
+            const double *A, const int *LDA, double *B, const int *LDB);
+
+/* C <- beta*C + alpha*A*B (SIDE='L') or alpha*B*A ('R'), A symmetric with
+ * the UPLO triangle stored.  Replaces dsymm_ at
+ * flens/blas/interface/blas/symm.cc:93-174 (-> cxxblas::symm,
+ * cxxblas/level3/symm.tcc:40-70). */
+void dsymm_(const char *SIDE, const char *UPLO, const int *M, const int *N,
+            const double *ALPHA, const double *A, const int *LDA,
+            const double *B, const int *LDB, const double *BETA, double *C,
+            const int *LDC);
+
+/* C <- beta*C + alpha*(op(A)*op(B)^T + op(B)*op(A)^T) on the UPLO triangle.
+ * Replaces dsyr2k_ at flens/blas/interface/blas/syr2k.cc:115-218
+ * (-> cxxblas::syr2k, cxxblas/level3/syr2k.tcc:42-95). */
+void dsyr2k_(const char *UPLO, const char *TRANS, const int *N, const int *K,
+             const double *ALPHA, const double *A, const int *LDA,
+             const double *B, const int *LDB, const double *BETA, double *C,
+             const int *LDC);
+
 /* Cholesky factorisation A = L*L^T (UPLO='L') or U^T*U ('U') of the UPLO
  * triangle in place; INFO=k>0: the leading minor of order k is not positive
  * definite.  UPLO must be exactly 'U' or 'L', as in the reference.
@@ -138,6 +163,19 @@ int flens_gb300_dgesv(int n, int nrhs, double *A, int ldA, int *ipiv, double *B,
 int flens_gb300_dsyrk(char uplo, char trans, int n, int k, double alpha,
                       const double *A, int ldA, double beta, double *C,
                       int ldC, void *stream);
+
+/* dtrmm, dsymm, dsyr2k on device memory (characters in either case).  The
+ * triangular / symmetric operand is expanded to a full matrix in the
+ * workspace and the product runs on the FP64 GEMM.  Async on stream. */
+int flens_gb300_dtrmm(char side, char uplo, char transA, char diag, int m,
+                      int n, double alpha, const double *A, int ldA,
+                      double *B, int ldB, void *stream);
+int flens_gb300_dsymm(char side, char uplo, int m, int n, double alpha,
+                      const double *A, int ldA, const double *B, int ldB,
+                      double beta, double *C, int ldC, void *stream);
+int flens_gb300_dsyr2k(char uplo, char trans, int n, int k, double alpha,
+                       const double *A, int ldA, const double *B, int ldB,
+                       double beta, double *C, int ldC, void *stream);
 
 /* dpotrf on device memory; info is a device int.  Blocked right-looking
  * (64-column steps: potf2 of the diagonal block, trsm, syrk of the trailing

@@ -135,6 +135,50 @@ def test_dsyrk_argument_errors(args, pos):
     assert name == "DSYRK" and info == pos
 
 
+@pytest.mark.parametrize("fn,args,pos", [
+    ("dtrmm_", ("X", "U", "N", "N", 2, 2, 2, 2), 1),
+    ("dtrmm_", ("L", "X", "N", "N", 2, 2, 2, 2), 2),
+    ("dtrmm_", ("L", "U", "X", "N", 2, 2, 2, 2), 3),
+    ("dtrmm_", ("L", "U", "N", "X", 2, 2, 2, 2), 4),
+    ("dtrmm_", ("L", "U", "N", "N", -1, 2, 2, 2), 5),
+    ("dtrmm_", ("L", "U", "N", "N", 2, -1, 2, 2), 6),
+    ("dtrmm_", ("R", "U", "N", "N", 2, 3, 2, 2), 9),
+    ("dtrmm_", ("L", "U", "N", "N", 3, 2, 3, 2), 11),
+])
+def test_dtrmm_argument_errors(fn, args, pos):
+    side, uplo, ta, diag, m, n, lda, ldb = args
+    name, info = _xerbla_after(lambda: fg.lib().dtrmm_(
+        side.encode(), uplo.encode(), ta.encode(), diag.encode(), _i(m), _i(n), _d(1.0), NULLD,
+        _i(lda), NULLD, _i(ldb)))
+    assert name == "DTRMM" and info == pos
+
+
+@pytest.mark.parametrize("args,pos", [
+    (("X", "U", 2, 2, 2, 2, 2), 1), (("L", "X", 2, 2, 2, 2, 2), 2), (("L", "U", -1, 2, 2, 2, 2), 3),
+    (("L", "U", 2, -1, 2, 2, 2), 4), (("R", "U", 2, 3, 2, 2, 2), 7), (("L", "U", 3, 2, 3, 2, 3), 9),
+    (("L", "U", 3, 2, 3, 3, 2), 12),
+])
+def test_dsymm_argument_errors(args, pos):
+    side, uplo, m, n, lda, ldb, ldc = args
+    name, info = _xerbla_after(lambda: fg.lib().dsymm_(
+        side.encode(), uplo.encode(), _i(m), _i(n), _d(1.0), NULLD, _i(lda), NULLD, _i(ldb), _d(0.0),
+        NULLD, _i(ldc)))
+    assert name == "DSYMM" and info == pos
+
+
+@pytest.mark.parametrize("args,pos", [
+    (("X", "N", 2, 2, 2, 2, 2), 1), (("L", "X", 2, 2, 2, 2, 2), 2), (("L", "N", -1, 2, 2, 2, 2), 3),
+    (("L", "N", 2, -1, 2, 2, 2), 4), (("L", "N", 3, 2, 2, 3, 3), 7), (("U", "T", 2, 3, 3, 2, 2), 9),
+    (("L", "N", 3, 2, 3, 3, 2), 12),
+])
+def test_dsyr2k_argument_errors(args, pos):
+    uplo, tr, n, k, lda, ldb, ldc = args
+    name, info = _xerbla_after(lambda: fg.lib().dsyr2k_(
+        uplo.encode(), tr.encode(), _i(n), _i(k), _d(1.0), NULLD, _i(lda), NULLD, _i(ldb), _d(0.0),
+        NULLD, _i(ldc)))
+    assert name == "DSYR2K" and info == pos
+
+
 def test_cholesky_argument_errors():
     # flens/lapack/interface/src/{potrf,potrs,posv}.cc: UPLO exactly 'U' or 'L'
     L = fg.lib()
