@@ -87,6 +87,10 @@ class Port:
         L.oracle_dpotrs.argtypes = [c, i, i, _c_double_p, i, _c_double_p, i]
         L.oracle_dposv.argtypes = [c, i, i, _c_double_p, i, _c_double_p, i]
         L.oracle_dposv.restype = i
+        L.oracle_dtrtri_nb.argtypes = [c, c, i, _c_double_p, i, i]
+        L.oracle_dtrtri_nb.restype = i
+        L.oracle_dgetri.argtypes = [i, _c_double_p, i, _c_int_p]
+        L.oracle_dgetri.restype = i
         L.oracle_time_dgetrf_steps.argtypes = [i, i, i, ctypes.c_ulonglong, _c_double_p]
         L.oracle_time_dgetrf_steps.restype = d
         L.oracle_time_dgemm_rows.argtypes = [i, i, i, i, i, ctypes.c_ulonglong]
@@ -170,6 +174,17 @@ class Port:
                                max(1, n))
         return C
 
+    def dtrtri(self, uplo, diag, A, nb: int = 64):
+        _check_f64(A)
+        n = A.shape[0]
+        return self.lib.oracle_dtrtri_nb(uplo.encode(), diag.encode(), n, _dp(A), max(1, n), nb)
+
+    def dgetri(self, A, piv):
+        _check_f64(A)
+        n = A.shape[0]
+        piv = np.ascontiguousarray(piv, dtype=np.int32)
+        return self.lib.oracle_dgetri(n, _dp(A), max(1, n), _ip(piv))
+
     def dpotrf(self, uplo, A, nb: int = 64):
         _check_f64(A)
         n = A.shape[0]
@@ -224,6 +239,9 @@ class Reference:
         L.dpotrf_.argtypes = [cp, _c_int_p, _c_double_p, _c_int_p, _c_int_p]
         L.dtrmm_.argtypes = [cp, cp, cp, cp, _c_int_p, _c_int_p, _c_double_p, _c_double_p,
                              _c_int_p, _c_double_p, _c_int_p]
+        L.dtrtri_.argtypes = [cp, cp, _c_int_p, _c_double_p, _c_int_p, _c_int_p]
+        L.dgetri_.argtypes = [_c_int_p, _c_double_p, _c_int_p, _c_int_p, _c_double_p, _c_int_p,
+                              _c_int_p]
         L.dsymm_.argtypes = [cp, cp, _c_int_p, _c_int_p, _c_double_p, _c_double_p, _c_int_p,
                              _c_double_p, _c_int_p, _c_double_p, _c_double_p, _c_int_p]
         L.dsyr2k_.argtypes = [cp, cp, _c_int_p, _c_int_p, _c_double_p, _c_double_p, _c_int_p,
@@ -318,6 +336,26 @@ class Reference:
                          _dp(A), self._i(max(1, A.shape[0])), _dp(B), self._i(max(1, B.shape[0])),
                          self._d(beta), _dp(C), self._i(max(1, n)))
         return C
+
+    def dtrtri(self, uplo, diag, A):
+        """The reference's dtrtri_ (flens/lapack/interface/src/trtri.cc:9-55)
+        discards tri's return value: INFO is 0 for every valid call."""
+        n = A.shape[0]
+        info = ctypes.c_int(0)
+        self.lib.dtrtri_(uplo.encode(), diag.encode(), self._i(n), _dp(A), self._i(max(1, n)),
+                         ctypes.byref(info))
+        return info.value
+
+    def dgetri(self, A, piv):
+        """dgetri_ with the optimal workspace (n*64); INFO is 0 for every valid
+        call (flens/lapack/interface/src/getri.cc:10-53 discards tri's value)."""
+        n = A.shape[0]
+        piv = np.ascontiguousarray(piv, dtype=np.int32)
+        work = np.zeros(max(1, n * 64))
+        info = ctypes.c_int(0)
+        self.lib.dgetri_(self._i(n), _dp(A), self._i(max(1, n)), _ip(piv), _dp(work),
+                         self._i(work.size), ctypes.byref(info))
+        return info.value
 
     def dpotrf(self, uplo, A):
         n = A.shape[0]

@@ -579,6 +579,177 @@ void oracle_dgemv(char trans, int m, int n, double alpha, const double *A,
 }
 
 /*
+ * TI2.  flens/lapack/tr/ti2.tcc (generic ti2_impl): upper: for j = 1..n,
+ * A(j,j) = 1/A(j,j) and Ajj = -A(j,j) (or Ajj = -1 for a unit diagonal), then
+ * u12 = A(1:j-1, j) <- U11 * u12 (trmv with the already inverted U11) and
+ * u12 *= Ajj; lower: j = n..1 with l21 = A(j+1:n, j) and L22.
+ */
+int oracle_dtrti2(char upLo, char diag, int n, double *A, int ldA)
+{
+    const int upper = (upLo == 'U' || upLo == 'u');
+    const int nonunit = (diag == 'N' || diag == 'n');
+    if (upper) {
+        for (int j = 0; j < n; ++j) {
+            double ajj;
+            if (nonunit) {
+                A[IDX(j, j, ldA)] = 1.0 / A[IDX(j, j, ldA)];
+                ajj = -A[IDX(j, j, ldA)];
+            } else {
+                ajj = -1.0;
+            }
+            if (j > 0) {
+                oracle_dtrmm('L', 'U', 'N', nonunit ? 'N' : 'U', j, 1, 1.0, A, ldA,
+                             &A[IDX(0, j, ldA)], ldA);
+                for (int i = 0; i < j; ++i) {
+                    A[IDX(i, j, ldA)] *= ajj;
+                }
+            }
+        }
+    } else {
+        for (int j = n - 1; j >= 0; --j) {
+            double ajj;
+            if (nonunit) {
+                A[IDX(j, j, ldA)] = 1.0 / A[IDX(j, j, ldA)];
+                ajj = -A[IDX(j, j, ldA)];
+            } else {
+                ajj = -1.0;
+            }
+            if (j < n - 1) {
+                const int r = n - 1 - j;
+                oracle_dtrmm('L', 'L', 'N', nonunit ? 'N' : 'U', r, 1, 1.0,
+                             &A[IDX(j + 1, j + 1, ldA)], ldA, &A[IDX(j + 1, j, ldA)], ldA);
+                for (int i = 0; i < r; ++i) {
+                    A[IDX(j + 1 + i, j, ldA)] *= ajj;
+                }
+            }
+        }
+    }
+    return 0;
+}
+
+/*
+ * TRTRI.  flens/lapack/tr/tri.tcc (generic tri_impl): a non-unit matrix with
+ * an exactly zero diagonal element returns its index untouched; unblocked
+ * (ti2) when nb <= 1 or nb >= n; else upper: for j = 1, 1+nb, ...:
+ * U12 <- U11 U12 (trmm), U12 <- -U12 U22^-1 (trsm), ti2(U22); lower: j from
+ * ((n-1)/nb)*nb+1 down: L21 <- L22 L21, L21 <- -L21 L11^-1, ti2(L11).
+ */
+int oracle_dtrtri_nb(char upLo, char diag, int n, double *A, int ldA, int nb)
+{
+    const int upper = (upLo == 'U' || upLo == 'u');
+    const int nonunit = (diag == 'N' || diag == 'n');
+    const char dg = nonunit ? 'N' : 'U';
+    if (n == 0) {
+        return 0;
+    }
+    if (nonunit) {
+        for (int i = 0; i < n; ++i) {
+            if (A[IDX(i, i, ldA)] == 0.0) {
+                return i + 1;
+            }
+        }
+    }
+    if (nb <= 1 || nb >= n) {
+        return oracle_dtrti2(upLo, diag, n, A, ldA);
+    }
+    if (upper) {
+        for (int j = 0; j < n; j += nb) {
+            const int jb = (nb < n - j) ? nb : n - j;
+            if (j > 0) {
+                oracle_dtrmm('L', 'U', 'N', dg, j, jb, 1.0, A, ldA, &A[IDX(0, j, ldA)], ldA);
+                oracle_dtrsm('R', 'U', 'N', dg, j, jb, -1.0, &A[IDX(j, j, ldA)], ldA,
+                             &A[IDX(0, j, ldA)], ldA);
+            }
+            oracle_dtrti2('U', dg, jb, &A[IDX(j, j, ldA)], ldA);
+        }
+    } else {
+        const int nn = ((n - 1) / nb) * nb;
+        for (int j = nn; j >= 0; j -= nb) {
+            const int jb = (nb < n - j) ? nb : n - j;
+            if (j + jb < n) {
+                const int r = n - j - jb;
+                oracle_dtrmm('L', 'L', 'N', dg, r, jb, 1.0, &A[IDX(j + jb, j + jb, ldA)], ldA,
+                             &A[IDX(j + jb, j, ldA)], ldA);
+                oracle_dtrsm('R', 'L', 'N', dg, r, jb, -1.0, &A[IDX(j, j, ldA)], ldA,
+                             &A[IDX(j + jb, j, ldA)], ldA);
+            }
+            oracle_dtrti2('L', dg, jb, &A[IDX(j, j, ldA)], ldA);
+        }
+    }
+    return 0;
+}
+
+int oracle_dtrtri(char upLo, char diag, int n, double *A, int ldA)
+{
+    return oracle_dtrtri_nb(upLo, diag, n, A, ldA, 64);
+}
+
+/*
+ * GETRI.  flens/lapack/ge/tri.tcc (generic tri_impl) with the full workspace
+ * (lwork = n*nb, nb = 64): trtri of U (return on a zero pivot); unblocked
+ * when nb >= n: for j = n..1, work = A(j+1:n, j), A(j+1:n, j) = 0,
+ * A(:, j) -= A(:, j+1:n) work (gemv); blocked: for j from nn down by nb, the
+ * strictly lower part of the block column goes to Work and is zeroed,
+ * A(:, J) -= A(:, j+jb:n) Work(j+jb:n, :) (gemm), A(:, J) <- A(:, J) Wunit^-1
+ * (trsm, Work's unit lower block); last the column interchanges
+ * j = n-1..1 with piv(j).
+ */
+int oracle_dgetri(int n, double *A, int ldA, const int *piv)
+{
+    const int nb = 64;
+    if (n == 0) {
+        return 0;
+    }
+    const int info = oracle_dtrtri('U', 'N', n, A, ldA);
+    if (info > 0) {
+        return info;
+    }
+    double *work = (double *)calloc((size_t)n * nb, sizeof(double));
+    if (nb >= n) {
+        for (int j = n - 1; j >= 0; --j) {
+            for (int i = j + 1; i < n; ++i) {
+                work[i] = A[IDX(i, j, ldA)];
+                A[IDX(i, j, ldA)] = 0.0;
+            }
+            if (j < n - 1) {
+                oracle_dgemv('N', n, n - j - 1, -1.0, &A[IDX(0, j + 1, ldA)], ldA, &work[j + 1], 1,
+                             1.0, &A[IDX(0, j, ldA)], 1);
+            }
+        }
+    } else {
+        const int ldw = n;
+        const int nn = ((n - 1) / nb) * nb;
+        for (int j = nn; j >= 0; j -= nb) {
+            const int jb = (nb < n - j) ? nb : n - j;
+            for (int jj = j, JJ = 0; jj < j + jb; ++jj, ++JJ) {
+                for (int i = jj + 1; i < n; ++i) {
+                    work[IDX(i, JJ, ldw)] = A[IDX(i, jj, ldA)];
+                    A[IDX(i, jj, ldA)] = 0.0;
+                }
+            }
+            if (j + jb < n) {
+                oracle_dgemm('N', 'N', n, jb, n - j - jb, -1.0, &A[IDX(0, j + jb, ldA)], ldA,
+                             &work[IDX(j + jb, 0, ldw)], ldw, 1.0, &A[IDX(0, j, ldA)], ldA);
+            }
+            oracle_dtrsm('R', 'L', 'N', 'U', n, jb, 1.0, &work[IDX(j, 0, ldw)], ldw,
+                         &A[IDX(0, j, ldA)], ldA);
+        }
+    }
+    free(work);
+    for (int j = n - 2; j >= 0; --j) {
+        const int jp = piv[j] - 1;
+        if (jp != j) {
+            for (int i = 0; i < n; ++i) {
+                const double t = A[IDX(i, j, ldA)];
+                A[IDX(i, j, ldA)] = A[IDX(i, jp, ldA)];
+                A[IDX(i, jp, ldA)] = t;
+            }
+        }
+    }
+    return 0;
+}
+
+/*
  * POTF2.  flens/lapack/po/potf2.tcc:56-140 (left-looking, dot form): for each
  * column j, ajj = A(j,j) - dot(a, a) over the finished part of row/column j;
  * ajj <= 0 or NaN stores ajj, sets info = j and stops; otherwise A(j,j) =

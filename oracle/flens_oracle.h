@@ -80,6 +80,19 @@ void oracle_dsyr2k(char upLo, char trans, int n, int k, double alpha,
                    const double *A, int ldA, const double *B, int ldB,
                    double beta, double *C, int ldC);
 
+/* inverse of a triangular matrix in place, unblocked  flens/lapack/tr/ti2.tcc */
+int oracle_dtrti2(char upLo, char diag, int n, double *A, int ldA);
+
+/* blocked triangular inverse (block 64, ilaenv TRTRI); info = first exactly
+ * zero diagonal element (non-unit), nothing changed then
+ *                                                flens/lapack/tr/tri.tcc */
+int oracle_dtrtri_nb(char upLo, char diag, int n, double *A, int ldA, int nb);
+int oracle_dtrtri(char upLo, char diag, int n, double *A, int ldA);
+
+/* inverse from the LU factors of dgetrf (block 64, ilaenv GETRI; workspace
+ * allocated inside); info as dtrtri of U         flens/lapack/ge/tri.tcc */
+int oracle_dgetri(int n, double *A, int ldA, const int *piv);
+
 /* y <- beta*y + alpha*op(A)*x                  cxxblas/level2/gemv.tcc:42-200 */
 void oracle_dgemv(char trans, int m, int n, double alpha, const double *A,
                   int ldA, const double *x, int incX, double beta, double *y,

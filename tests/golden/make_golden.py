@@ -1,7 +1,8 @@
 """Generate the golden fixtures in this directory from the REFERENCE itself.
 
 Runs the reference's own Fortran-ABI shims (dgemm_, dtrsm_, dsyrk_, dtrmm_,
-dsymm_, dsyr2k_, dgetrf_, dgetrs_, dgesv_, dpotrf_, dpotrs_, dposv_ compiled
+dsymm_, dsyr2k_, dgetrf_, dgetrs_, dgesv_, dgetri_, dtrtri_, dpotrf_, dpotrs_,
+dposv_ compiled
 from the FLENS sources into
 oracle/_ref/libflens_ref.so by
 ``make -C oracle ref``) on seeded inputs and stores the outputs.  Inputs come
@@ -185,6 +186,32 @@ def syr2k_inputs(i, n, k, tr):
     return U(s, *shape), U(s + 1, *shape), U(s + 2, n, n)
 
 
+def tri_case_list():
+    """(n, uplo, diag) for dtrtri and n for dgetri (on dgetrf's factors)."""
+    cases = []
+    for n in (1, 2, 5, 31, 64, 65, 129, 200):
+        for uplo in "UL":
+            for diag in "NU":
+                cases.append((n, uplo, diag))
+    return [(f"trtri{i:03d}", c) for i, c in enumerate(cases)]
+
+
+def tri_input(i, n):
+    A = U(21000 + 10 * i, n, n)
+    A[np.arange(n), np.arange(n)] += 2.0 + n / 4.0
+    return A
+
+
+def getri_case_list():
+    return [(f"getri{i:03d}", n) for i, n in enumerate((1, 2, 7, 31, 64, 65, 100, 129, 200))]
+
+
+def getri_input(i, n):
+    A = U(23000 + 10 * i, n, n)
+    A[np.arange(n), np.arange(n)] += n / 4.0
+    return A
+
+
 def chol_case_list():
     """(n, uplo, kind): kind 'spd' (well conditioned) or 'notpd' (a negative
     pivot at n//2, so INFO = n//2 + 1 with the factor of the leading block)."""
@@ -254,6 +281,15 @@ def generate_small(R):
     for i, (name, (n, k, uplo, tr, a, b)) in enumerate(syr2k_case_list()):
         A, B, C = syr2k_inputs(i, n, k, tr)
         out[name] = R.dsyr2k(uplo, tr, a, A, B, b, C.copy(order="F"))
+    for i, (name, (n, uplo, diag)) in enumerate(tri_case_list()):
+        A = tri_input(i, n)
+        R.dtrtri(uplo, diag, A)
+        out[name] = A
+    for i, (name, n) in enumerate(getri_case_list()):
+        LU = getri_input(i, n)
+        piv, info = R.dgetrf(LU)
+        R.dgetri(LU, piv)
+        out[name] = LU
     for i, (name, (n, uplo, kind)) in enumerate(chol_case_list()):
         A = chol_input(i, n, kind)
         info = R.dpotrf(uplo, A)

@@ -83,6 +83,23 @@ def test_trmm_symm_syr2k_fixtures_bitwise(golden, port):
         assert np.array_equal(port.dsyr2k(uplo, tr, a, A, B, b, C.copy(order="F")), golden[name]), name
 
 
+def test_trtri_getri_fixtures_bitwise(golden, port):
+    for i, (name, (n, uplo, diag)) in enumerate(G.tri_case_list()):
+        A = G.tri_input(i, n)
+        assert port.dtrtri(uplo, diag, A) == 0
+        assert np.array_equal(A, golden[name]), name
+    for i, (name, n) in enumerate(G.getri_case_list()):
+        LU = G.getri_input(i, n)
+        piv, info = port.dgetrf(LU)
+        assert port.dgetri(LU, piv) == 0
+        assert np.array_equal(LU, golden[name]), name
+    # a zero diagonal element: the routine's INFO, A untouched (tr/tri.tcc)
+    A = G.tri_input(0, 10)
+    A[3, 3] = 0.0
+    A0 = A.copy()
+    assert port.dtrtri("U", "N", A) == 4 and np.array_equal(A, A0)
+
+
 def test_cholesky_fixtures_bitwise(golden, port):
     for i, (name, (n, uplo, kind)) in enumerate(G.chol_case_list()):
         A = G.chol_input(i, n, kind)
