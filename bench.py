@@ -329,6 +329,7 @@ def our_arm(args, rank: int, world: int) -> None:
             result["split_gemm_config4"] = split_subbench(torch, fg, dev, cublas_tflops=cublas_peak)
         if not args.quick and not args.no_cholesky:
             result["cholesky_fp64"] = cholesky_subbench(torch, fg, dev)
+            result["inverse_fp64"] = inverse_subbench(torch, fg, dev)
         if not args.quick and not args.no_batched:
             result["batched_config5"] = batched_subbench(torch, fg, dev, count=args.batch_count)
         # -- e2e through the Fortran ABI with pinned host buffers
@@ -570,6 +571,59 @@ def cholesky_subbench(torch, fg, dev, n=8192, reps=3):
     return out
 
 
+def inverse_subbench(torch, fg, dev, n=8192, reps=2):
+    """Matrix inverse configuration: A uniform[-1,1] + n/4 I (n = 8192), dgetrf
+    then dgetri through the device entry points, A restored from a pristine
+    copy each repetition.  FLOP count 2 n^3 ((2/3) n^3 LU + (4/3) n^3 inverse)."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(91)
+    A0 = torch.rand((n, n), generator=g, dtype=torch.float64, device=dev).mul_(2).sub_(1)
+    A0.diagonal().add_(n / 4.0)
+    A0 = A0.t()
+    A = fg.to_colmajor(A0.clone())
+    ipiv = torch.zeros(n, dtype=torch.int32, device=dev)
+    info = torch.zeros(1, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def run():
+        A.copy_(A0)
+        fg.dgetrf_dev(A, ipiv, info, stream)
+        st = fg.lib().flens_gb300_dgetri(n, A.data_ptr(), n, ipiv.data_ptr(), info.data_ptr(),
+                                         ctypes_stream(stream))
+        assert st == 0, fg.last_error()
+
+    run()
+    torch.cuda.synchronize()
+    fg.timing_enable(True)
+    times = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    fam = fg.timing_read()
+    fg.timing_enable(False)
+    ms = sum(times) / len(times)
+    R = A0 @ A - torch.eye(n, dtype=torch.float64, device=dev)
+    nrm = lambda M: M.abs().sum(0).max().item()
+    eps = float(torch.finfo(torch.float64).eps)
+    out = {"workload": f"dgetrf+dgetri n={n} FP64", "n": n, "ms": ms,
+           "tflops": 2.0 * n ** 3 / (ms * 1e-3) / 1e12, "info": int(info.item()),
+           "residual_over_n_eps": nrm(R) / (n * nrm(A0) * nrm(A) * eps),
+           "kernels_ms_per_call": {k: v["ms"] / reps for k, v in fam.items()},
+           "l2": "A restored from a pristine copy each rep (512 MiB > L2)"}
+    del A, A0, R
+    torch.cuda.empty_cache()
+    return out
+
+
+def ctypes_stream(stream):
+    import ctypes
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
 def batched_subbench(torch, fg, dev, count=20000, reps=3, loop_sample=2000):
     """Batched configuration: `count` independent FP64 systems, n log-uniform
     in [8, 512], entries uniform[-1,1] + (n/4) I, k uniform in {1, 4, 16}.
@@ -776,6 +830,8 @@ def only(args):
         print(json.dumps(out))
     elif args.only == "cholesky":
         print(json.dumps(cholesky_subbench(torch, fg, dev, n=args.n, reps=args.steps)))
+    elif args.only == "inverse":
+        print(json.dumps(inverse_subbench(torch, fg, dev, n=args.n, reps=args.steps)))
     elif args.only == "split":
         out = split_subbench(torch, fg, dev, n=args.split_n, Es=(args.split_e,), reps=args.steps,
                              ref_slices=args.split_ref_slices)
@@ -803,7 +859,7 @@ def main():
     ap.add_argument("--split-e", type=int, default=48, help="exponent range E for --only split")
     ap.add_argument("--split-ref-slices", type=int, default=14, help="reference slices for --only split")
     ap.add_argument("--batch-count", type=int, default=20000)
-    ap.add_argument("--only", choices=["tc_gemm", "batched", "mixed", "split", "cholesky"],
+    ap.add_argument("--only", choices=["tc_gemm", "batched", "mixed", "split", "cholesky", "inverse"],
                     help="run one sub-benchmark and print its JSON (for profiling)")
     ap.add_argument("--tc-shape", default="8192,8192,256", help="M,N,K for --only tc_gemm")
     args = ap.parse_args()

@@ -89,6 +89,12 @@ def lib() -> ctypes.CDLL:
     L.dsymm_.restype = None
     L.dsyr2k_.argtypes = [cp, cp, _ip, _ip, _dp, _dp, _ip, _dp, _ip, _dp, _dp, _ip]
     L.dsyr2k_.restype = None
+    L.dtrtri_.argtypes = [cp, cp, _ip, _dp, _ip, _ip]
+    L.dtrtri_.restype = None
+    L.dgetri_.argtypes = [_ip, _dp, _ip, _ip, _dp, _ip, _ip]
+    L.dgetri_.restype = None
+    L.flens_gb300_dtrtri.argtypes = [_c, _c, _i, _v, _i, _v, _v]
+    L.flens_gb300_dgetri.argtypes = [_i, _v, _i, _v, _v, _v]
     L.flens_gb300_dtrmm.argtypes = [_c, _c, _c, _c, _i, _i, _d, _v, _i, _v, _i, _v]
     L.flens_gb300_dsymm.argtypes = [_c, _c, _i, _i, _d, _v, _i, _v, _i, _d, _v, _i, _v]
     L.flens_gb300_dsyr2k.argtypes = [_c, _c, _i, _i, _d, _v, _i, _v, _i, _d, _v, _i, _v]
@@ -111,7 +117,7 @@ def lib() -> ctypes.CDLL:
               "flens_gb300_dgetrs", "flens_gb300_dgesv", "flens_gb300_sync",
               "flens_gb300_dsyrk", "flens_gb300_dpotrf", "flens_gb300_dpotrs",
               "flens_gb300_dposv", "flens_gb300_dtrmm", "flens_gb300_dsymm",
-              "flens_gb300_dsyr2k"):
+              "flens_gb300_dsyr2k", "flens_gb300_dtrtri", "flens_gb300_dgetri"):
         getattr(L, f).restype = _i
     L.flens_gb300_last_error.restype = ctypes.c_char_p
     L.flens_gb300_last_error.argtypes = []
@@ -258,6 +264,26 @@ def dsyr2k(uplo: str, trans: str, alpha: float, A: np.ndarray, B: np.ndarray, be
                   _ref(max(1, A.shape[0]), _i), _fd(B), _ref(max(1, B.shape[0]), _i),
                   _ref(beta, _d), _fd(C), _ref(max(1, n), _i))
     return C
+
+
+def dtrtri(uplo: str, diag: str, A: np.ndarray) -> int:
+    """In-place triangular inverse through dtrtri_; returns info."""
+    n = A.shape[0]
+    info = ctypes.c_int(0)
+    lib().dtrtri_(uplo.encode(), diag.encode(), _ref(n, _i), _fd(A), _ref(max(1, n), _i),
+                  ctypes.byref(info))
+    return info.value
+
+
+def dgetri(A: np.ndarray, ipiv: np.ndarray) -> int:
+    """In-place inverse from dgetrf_'s factors through dgetri_; returns info."""
+    n = A.shape[0]
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    work = np.zeros(max(1, n))
+    info = ctypes.c_int(0)
+    lib().dgetri_(_ref(n, _i), _fd(A), _ref(max(1, n), _i), ipiv.ctypes.data_as(_ip),
+                  work.ctypes.data_as(_dp), _ref(work.size, _i), ctypes.byref(info))
+    return info.value
 
 
 def dpotrf(uplo: str, A: np.ndarray) -> int:

@@ -14,6 +14,8 @@
 //      dpotrf_  flens/lapack/interface/src/potrf.cc:11-41
 //      dpotrs_  flens/lapack/interface/src/potrs.cc:13-49
 //      dposv_   flens/lapack/interface/src/posv.cc:13-51
+//      dtrtri_  flens/lapack/interface/src/trtri.cc:9-55
+//      dgetri_  flens/lapack/interface/src/getri.cc:10-53
 //    They take HOST pointers (as the reference does), copy the operands to
 //    the device, run the GPU path and copy the results back before
 //    returning.  Device (or managed) pointers are also accepted and used in
@@ -610,6 +612,92 @@ FG_API void dposv_(const char *UPLO, const int *N, const int *NRHS, double *A, c
     *INFO = (st != kOk) ? st : info;
 }
 
+// ------------------------------------------------------ LAPACK inverses --
+namespace {
+
+int trtri_host(char uplo, char diag, int n, double *A, int ldA, int *INFO) {
+    *INFO = 0;
+    if (n == 0) return kOk;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    if (st != kOk) return st;
+    DevView a;
+    if ((st = view_in(0, A, n, n, ldA, true, s, &a)) != kOk) return st;
+    Workspace *w = workspace_for(s, 0);
+    if (!w) return kErrAlloc;
+    if ((st = dtrtri_launch(uplo, diag, n, a.p, a.ld, w->info, s)) != kOk) return st;
+    if ((st = view_out(a, A, n, n, ldA, s)) != kOk) return st;
+    FG_CUDA(cudaMemcpyAsync(INFO, w->info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return finish(s);
+}
+
+int getri_host(int n, double *A, int ldA, const int *IPIV, int *INFO) {
+    *INFO = 0;
+    if (n == 0) return kOk;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    if (st != kOk) return st;
+    DevView a;
+    if ((st = view_in(0, A, n, n, ldA, true, s, &a)) != kOk) return st;
+    int *dpiv;
+    bool pstaged;
+    if ((st = ipiv_dev(3, const_cast<int *>(IPIV), n, true, s, &dpiv, &pstaged)) != kOk) return st;
+    Workspace *w = workspace_for(s, 0);
+    if (!w) return kErrAlloc;
+    if ((st = dgetri_launch(n, a.p, a.ld, dpiv, w->info, s)) != kOk) return st;
+    if ((st = view_out(a, A, n, n, ldA, s)) != kOk) return st;
+    FG_CUDA(cudaMemcpyAsync(INFO, w->info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return finish(s);
+}
+
+}  // namespace
+
+// flens/lapack/interface/src/trtri.cc:9-55: UPLO exactly 'U'/'L', DIAG 'N'/'U'.
+// The reference's shim discards tri's return value; this one reports a zero
+// diagonal element in INFO (LAPACK DTRTRI semantics, A untouched then).
+FG_API void dtrtri_(const char *UPLO, const char *DIAG, const int *N, double *A, const int *LDA,
+                    int *INFO) {
+    *INFO = 0;
+    if (*UPLO != 'U' && *UPLO != 'L') *INFO = -1;
+    else if (*DIAG != 'N' && *DIAG != 'U') *INFO = -2;
+    else if (*N < 0) *INFO = -3;
+    else if (*LDA < std::max(1, *N)) *INFO = -5;
+    if (*INFO != 0) {
+        report_xerbla("DTRTRI", -*INFO);
+        return;
+    }
+    int info = 0;
+    const int st = trtri_host(*UPLO, *DIAG, *N, A, *LDA, &info);
+    *INFO = (st != kOk) ? st : info;
+}
+
+// flens/lapack/interface/src/getri.cc:10-53 (checks N, LDA, LWORK >= max(1,N)
+// unless LWORK == -1).  A workspace query returns WORK(1) = N*64 at once; the
+// GPU path uses its own device workspace and reports the same optimum.  INFO
+// reports an exactly zero U(i,i) (LAPACK DGETRI semantics; the reference's
+// shim discards it).
+FG_API void dgetri_(const int *N, double *A, const int *LDA, const int *IPIV, double *WORK,
+                    const int *LWORK, int *INFO) {
+    *INFO = 0;
+    const bool query = *LWORK == -1;
+    if (*N < 0) *INFO = -1;
+    else if (*LDA < std::max(1, *N)) *INFO = -3;
+    else if (*LWORK < std::max(1, *N) && !query) *INFO = -6;
+    if (*INFO != 0) {
+        report_xerbla("DGETRI", -*INFO);
+        return;
+    }
+    const double opt = (double)std::max(1, *N * 64);
+    if (query) {
+        WORK[0] = opt;
+        return;
+    }
+    int info = 0;
+    const int st = getri_host(*N, A, *LDA, IPIV, &info);
+    *INFO = (st != kOk) ? st : info;
+    WORK[0] = opt;
+}
+
 // ------------------------------------------------ device-pointer API ----
 static inline cudaStream_t as_stream(void *s) { return (cudaStream_t)s; }
 
@@ -675,6 +763,23 @@ FG_API int flens_gb300_dsyr2k(char uplo, char trans, int n, int k, double alpha,
     if (ldC < std::max(1, n)) return -12;
     return dsyr2k_launch(uplo, trans == 'N' ? 'N' : 'T', n, k, alpha, A, ldA, B, ldB, beta, C, ldC,
                          as_stream(stream));
+}
+
+FG_API int flens_gb300_dtrtri(char uplo, char diag, int n, double *A, int ldA, int *info,
+                              void *stream) {
+    uplo = (char)toupper(uplo);
+    diag = (char)toupper(diag);
+    if (uplo != 'U' && uplo != 'L') return -1;
+    if (diag != 'N' && diag != 'U') return -2;
+    if (n < 0) return -3;
+    if (ldA < std::max(1, n)) return -5;
+    return dtrtri_launch(uplo, diag, n, A, ldA, info, as_stream(stream));
+}
+
+FG_API int flens_gb300_dgetri(int n, double *A, int ldA, const int *ipiv, int *info, void *stream) {
+    if (n < 0) return -1;
+    if (ldA < std::max(1, n)) return -3;
+    return dgetri_launch(n, A, ldA, ipiv, info, as_stream(stream));
 }
 
 FG_API int flens_gb300_dpotrf(char uplo, int n, double *A, int ldA, int *info, void *stream) {

@@ -195,6 +195,17 @@ int dsyr2k_launch(char uplo, char trans, int n, int k, double alpha,
                   const double *A, int ldA, const double *B, int ldB,
                   double beta, double *C, int ldC, cudaStream_t stream);
 
+// Triangular inverse in place (tri.cu); *info (device) = first exactly zero
+// diagonal element (non-unit; A untouched then) or 0.  Synchronises to read
+// it.
+int dtrtri_launch(char uplo, char diag, int n, double *A, int ldA, int *info,
+                  cudaStream_t stream);
+
+// Inverse from dgetrf's factors and pivots (device ipiv, 1-based) in place;
+// *info as dtrtri of U (A holds the factors when it is > 0).
+int dgetri_launch(int n, double *A, int ldA, const int *ipiv, int *info,
+                  cudaStream_t stream);
+
 // Cholesky (uplo 'L': A = L L^T, 'U': A = U^T U) of the n x n uplo triangle
 // in place; *info (device) = first non-positive pivot (1-based) or 0.
 // Synchronises once per 64-column block to stop at the first failure.

@@ -127,6 +127,23 @@ void dpotrs_(const char *UPLO, const int *N, const int *NRHS, const double *A,
 void dposv_(const char *UPLO, const int *N, const int *NRHS, double *A,
             const int *LDA, double *B, const int *LDB, int *INFO);
 
+/* Inverse of a triangular matrix in place (UPLO exactly 'U'/'L', DIAG
+ * 'N'/'U', as in the reference); INFO=k>0: A(k,k) is exactly zero and A is
+ * untouched.  Replaces dtrtri_ at flens/lapack/interface/src/trtri.cc:9-55
+ * (-> lapack::tri flens/lapack/tr/tri.tcc).  The reference's shim discards
+ * tri's return value; this one reports it (LAPACK DTRTRI semantics). */
+void dtrtri_(const char *UPLO, const char *DIAG, const int *N, double *A,
+             const int *LDA, int *INFO);
+
+/* Inverse of A from dgetrf_'s factors and pivots, in place.  LWORK=-1 is a
+ * workspace query (WORK(1) = N*64); otherwise LWORK >= max(1,N) and WORK(1)
+ * receives the optimum on exit (the GPU path keeps its own workspace).
+ * INFO=k>0: U(k,k) is exactly zero, A holds the factors.  Replaces dgetri_
+ * at flens/lapack/interface/src/getri.cc:10-53 (-> lapack::tri
+ * flens/lapack/ge/tri.tcc). */
+void dgetri_(const int *N, double *A, const int *LDA, const int *IPIV,
+             double *WORK, const int *LWORK, int *INFO);
+
 /* Weak default error handler (prints, does not stop).  Link your own
  * xerbla_ to override it, as with Netlib BLAS/LAPACK. */
 void xerbla_(const char *SRNAME, const int *INFO, int SRNAME_LEN);
@@ -176,6 +193,13 @@ int flens_gb300_dsymm(char side, char uplo, int m, int n, double alpha,
 int flens_gb300_dsyr2k(char uplo, char trans, int n, int k, double alpha,
                        const double *A, int ldA, const double *B, int ldB,
                        double beta, double *C, int ldC, void *stream);
+
+/* dtrtri / dgetri on device memory (ipiv device, 1-based; info a device
+ * int).  Both wait for the stream once to read the zero-pivot check. */
+int flens_gb300_dtrtri(char uplo, char diag, int n, double *A, int ldA,
+                       int *info, void *stream);
+int flens_gb300_dgetri(int n, double *A, int ldA, const int *ipiv, int *info,
+                       void *stream);
 
 /* dpotrf on device memory; info is a device int.  Blocked right-looking
  * (64-column steps: potf2 of the diagonal block, trsm, syrk of the trailing

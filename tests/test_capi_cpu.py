@@ -196,6 +196,25 @@ def test_cholesky_argument_errors():
             assert info.value == want and name == nm and pos == -want
 
 
+def test_inverse_argument_errors_and_query():
+    # flens/lapack/interface/src/trtri.cc:19-31, getri.cc:20-37
+    L = fg.lib()
+    info = ctypes.c_int(0)
+    for (uplo, diag, n, lda, want) in [("X", "N", 2, 2, -1), ("u", "N", 2, 2, -1), ("U", "X", 2, 2, -2),
+                                       ("U", "n", 2, 2, -2), ("L", "N", -1, 2, -3), ("L", "U", 3, 2, -5)]:
+        name, pos = _xerbla_after(lambda: L.dtrtri_(uplo.encode(), diag.encode(), _i(n), NULLD,
+                                                    _i(lda), ctypes.byref(info)))
+        assert info.value == want and name == "DTRTRI" and pos == -want
+    work = (ctypes.c_double * 1)()
+    for (n, lda, lwork, want) in [(-1, 2, 2, -1), (3, 2, 3, -3), (3, 3, 2, -6)]:
+        name, pos = _xerbla_after(lambda: L.dgetri_(_i(n), NULLD, _i(lda), NULLI, work, _i(lwork),
+                                                    ctypes.byref(info)))
+        assert info.value == want and name == "DGETRI" and pos == -want
+    # workspace query: no device work, WORK(1) = N*64
+    L.dgetri_(_i(100), NULLD, _i(100), NULLI, work, _i(-1), ctypes.byref(info))
+    assert info.value == 0 and work[0] == 6400.0
+
+
 def test_quick_returns_touch_nothing():
     # m==0 / n==0 return before any device work (gemm.tcc:54-56, trf.tcc:81-83)
     L = fg.lib()
