@@ -91,6 +91,23 @@ class Port:
         L.oracle_dtrtri_nb.restype = i
         L.oracle_dgetri.argtypes = [i, _c_double_p, i, _c_int_p]
         L.oracle_dgetri.restype = i
+        L.oracle_dlange.argtypes = [c, i, i, _c_double_p, i]
+        L.oracle_dlange.restype = d
+        L.oracle_dgecon.argtypes = [c, i, _c_double_p, i, d, _c_double_p]
+        L.oracle_dgecon.restype = i
+        L.oracle_dgerfs.argtypes = [c, i, i, _c_double_p, i, _c_double_p, i, _c_int_p, _c_double_p,
+                                    i, _c_double_p, i, _c_double_p, _c_double_p]
+        L.oracle_dgerfs.restype = i
+        L.oracle_dgeequ.argtypes = [i, i, _c_double_p, i, _c_double_p, _c_double_p, _c_double_p,
+                                    _c_double_p, _c_double_p]
+        L.oracle_dgeequ.restype = i
+        L.oracle_dlaqge.argtypes = [i, i, _c_double_p, i, _c_double_p, _c_double_p, d, d, d]
+        L.oracle_dlaqge.restype = c
+        L.oracle_dgesvx.argtypes = [c, c, i, i, _c_double_p, i, _c_double_p, i, _c_int_p,
+                                    ctypes.c_char_p, _c_double_p, _c_double_p, _c_double_p, i,
+                                    _c_double_p, i, _c_double_p, _c_double_p, _c_double_p,
+                                    _c_double_p]
+        L.oracle_dgesvx.restype = i
         L.oracle_time_dgetrf_steps.argtypes = [i, i, i, ctypes.c_ulonglong, _c_double_p]
         L.oracle_time_dgetrf_steps.restype = d
         L.oracle_time_dgemm_rows.argtypes = [i, i, i, i, i, ctypes.c_ulonglong]
@@ -185,6 +202,50 @@ class Port:
         piv = np.ascontiguousarray(piv, dtype=np.int32)
         return self.lib.oracle_dgetri(n, _dp(A), max(1, n), _ip(piv))
 
+    # -- refinement, condition estimate, equilibration, expert driver -------
+    def dlange(self, norm, A):
+        return self.lib.oracle_dlange(norm.encode(), A.shape[0], A.shape[1], _dp(A), max(1, A.shape[0]))
+
+    def dgecon(self, norm, LU, anorm):
+        n = LU.shape[0]
+        rc = ctypes.c_double(0.0)
+        st = self.lib.oracle_dgecon(norm.encode(), n, _dp(LU), max(1, n), anorm, ctypes.byref(rc))
+        return rc.value, st
+
+    def dgerfs(self, trans, A, LU, piv, B, X):
+        n, k = B.shape
+        ferr, berr = np.zeros(max(1, k)), np.zeros(max(1, k))
+        piv = np.ascontiguousarray(piv, dtype=np.int32)
+        self.lib.oracle_dgerfs(trans.encode(), n, k, _dp(A), max(1, n), _dp(LU), max(1, n), _ip(piv),
+                               _dp(B), max(1, n), _dp(X), max(1, n), _dp(ferr), _dp(berr))
+        return ferr[:k], berr[:k]
+
+    def dgeequ(self, A):
+        m, n = A.shape
+        r, c = np.zeros(max(1, m)), np.zeros(max(1, n))
+        rc, cc, am = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        info = self.lib.oracle_dgeequ(m, n, _dp(A), max(1, m), _dp(r), _dp(c), ctypes.byref(rc),
+                                      ctypes.byref(cc), ctypes.byref(am))
+        return r[:m], c[:n], rc.value, cc.value, am.value, info
+
+    def dlaqge(self, A, r, c, rowcnd, colcnd, amax):
+        m, n = A.shape
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        return self.lib.oracle_dlaqge(m, n, _dp(A), max(1, m), _dp(r), _dp(c), rowcnd, colcnd,
+                                      amax).decode()
+
+    def dgesvx(self, fact, trans, A, AF, piv, equed, r, c, B, X):
+        n, k = B.shape
+        eq = ctypes.create_string_buffer(equed.encode(), 2)
+        rc, g = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        ferr, berr = np.zeros(max(1, k)), np.zeros(max(1, k))
+        info = self.lib.oracle_dgesvx(fact.encode(), trans.encode(), n, k, _dp(A), max(1, n),
+                                      _dp(AF), max(1, n), _ip(piv), eq, _dp(r), _dp(c), _dp(B),
+                                      max(1, n), _dp(X), max(1, n), ctypes.byref(rc), _dp(ferr),
+                                      _dp(berr), ctypes.byref(g))
+        return info, eq.value.decode(), rc.value, ferr[:k], berr[:k], g.value
+
     def dpotrf(self, uplo, A, nb: int = 64):
         _check_f64(A)
         n = A.shape[0]
@@ -240,6 +301,19 @@ class Reference:
         L.dtrmm_.argtypes = [cp, cp, cp, cp, _c_int_p, _c_int_p, _c_double_p, _c_double_p,
                              _c_int_p, _c_double_p, _c_int_p]
         L.dtrtri_.argtypes = [cp, cp, _c_int_p, _c_double_p, _c_int_p, _c_int_p]
+        L.dgecon_.argtypes = [cp, _c_int_p, _c_double_p, _c_int_p, _c_double_p, _c_double_p,
+                              _c_double_p, _c_int_p, _c_int_p]
+        L.dgerfs_.argtypes = [cp, _c_int_p, _c_int_p, _c_double_p, _c_int_p, _c_double_p, _c_int_p,
+                              _c_int_p, _c_double_p, _c_int_p, _c_double_p, _c_int_p, _c_double_p,
+                              _c_double_p, _c_double_p, _c_int_p, _c_int_p]
+        L.dgeequ_.argtypes = [_c_int_p, _c_int_p, _c_double_p, _c_int_p, _c_double_p, _c_double_p,
+                              _c_double_p, _c_double_p, _c_double_p, _c_int_p]
+        L.dlaqge_.argtypes = [_c_int_p, _c_int_p, _c_double_p, _c_int_p, _c_double_p, _c_double_p,
+                              _c_double_p, _c_double_p, _c_double_p, ctypes.c_char_p]
+        L.dgesvx_.argtypes = [cp, cp, _c_int_p, _c_int_p, _c_double_p, _c_int_p, _c_double_p,
+                              _c_int_p, _c_int_p, ctypes.c_char_p, _c_double_p, _c_double_p,
+                              _c_double_p, _c_int_p, _c_double_p, _c_int_p, _c_double_p,
+                              _c_double_p, _c_double_p, _c_double_p, _c_int_p, _c_int_p]
         L.dgetri_.argtypes = [_c_int_p, _c_double_p, _c_int_p, _c_int_p, _c_double_p, _c_int_p,
                               _c_int_p]
         L.dsymm_.argtypes = [cp, cp, _c_int_p, _c_int_p, _c_double_p, _c_double_p, _c_int_p,
@@ -336,6 +410,56 @@ class Reference:
                          _dp(A), self._i(max(1, A.shape[0])), _dp(B), self._i(max(1, B.shape[0])),
                          self._d(beta), _dp(C), self._i(max(1, n)))
         return C
+
+    def dgecon(self, norm, LU, anorm):
+        n = LU.shape[0]
+        rc, info = ctypes.c_double(0.0), ctypes.c_int(0)
+        work, iwork = np.zeros(max(1, 4 * n)), np.zeros(max(1, n), dtype=np.int32)
+        self.lib.dgecon_(norm.encode(), self._i(n), _dp(LU), self._i(max(1, n)), self._d(anorm),
+                         ctypes.byref(rc), _dp(work), _ip(iwork), ctypes.byref(info))
+        return rc.value, info.value
+
+    def dgerfs(self, trans, A, LU, piv, B, X):
+        n, k = B.shape
+        ferr, berr = np.zeros(max(1, k)), np.zeros(max(1, k))
+        work, iwork = np.zeros(max(1, 3 * n)), np.zeros(max(1, n), dtype=np.int32)
+        piv = np.ascontiguousarray(piv, dtype=np.int32)
+        info = ctypes.c_int(0)
+        self.lib.dgerfs_(trans.encode(), self._i(n), self._i(k), _dp(A), self._i(max(1, n)), _dp(LU),
+                         self._i(max(1, n)), _ip(piv), _dp(B), self._i(max(1, n)), _dp(X),
+                         self._i(max(1, n)), _dp(ferr), _dp(berr), _dp(work), _ip(iwork),
+                         ctypes.byref(info))
+        return ferr[:k], berr[:k]
+
+    def dgeequ(self, A):
+        m, n = A.shape
+        r, c = np.zeros(max(1, m)), np.zeros(max(1, n))
+        rc, cc, am, info = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        self.lib.dgeequ_(self._i(m), self._i(n), _dp(A), self._i(max(1, m)), _dp(r), _dp(c),
+                         ctypes.byref(rc), ctypes.byref(cc), ctypes.byref(am), ctypes.byref(info))
+        return r[:m], c[:n], rc.value, cc.value, am.value, info.value
+
+    def dlaqge(self, A, r, c, rowcnd, colcnd, amax):
+        m, n = A.shape
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        eq = ctypes.create_string_buffer(b"?", 2)
+        self.lib.dlaqge_(self._i(m), self._i(n), _dp(A), self._i(max(1, m)), _dp(r), _dp(c),
+                         self._d(rowcnd), self._d(colcnd), self._d(amax), eq)
+        return eq.value.decode()
+
+    def dgesvx(self, fact, trans, A, AF, piv, equed, r, c, B, X):
+        n, k = B.shape
+        eq = ctypes.create_string_buffer(equed.encode(), 2)
+        rc, info = ctypes.c_double(0.0), ctypes.c_int(0)
+        ferr, berr = np.zeros(max(1, k)), np.zeros(max(1, k))
+        work, iwork = np.zeros(max(1, 4 * n)), np.zeros(max(1, n), dtype=np.int32)
+        self.lib.dgesvx_(fact.encode(), trans.encode(), self._i(n), self._i(k), _dp(A),
+                         self._i(max(1, n)), _dp(AF), self._i(max(1, n)), _ip(piv), eq, _dp(r),
+                         _dp(c), _dp(B), self._i(max(1, n)), _dp(X), self._i(max(1, n)),
+                         ctypes.byref(rc), _dp(ferr), _dp(berr), _dp(work), _ip(iwork),
+                         ctypes.byref(info))
+        return info.value, eq.value.decode(), rc.value, ferr[:k], berr[:k], work[0]
 
     def dtrtri(self, uplo, diag, A):
         """The reference's dtrtri_ (flens/lapack/interface/src/trtri.cc:9-55)

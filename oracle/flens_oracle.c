@@ -749,6 +749,527 @@ int oracle_dgetri(int n, double *A, int ldA, const int *piv)
     return 0;
 }
 
+/* ---------------------------------------------------------------------- */
+/* FLENS's machine constants (flens/lapack/la/lamch.tcc: eps = epsilon/2,
+ * SafeMin = DBL_MIN, Precision = eps*2), sign (flens/lapack/auxiliary/
+ * sign.tcc: |x| with the sign bit of y) and nint (floor(x+1/2)). */
+static const double kEps = DBL_EPSILON * 0.5;
+static const double kSafeMin = DBL_MIN;
+static const double kPrecision = DBL_EPSILON;
+
+static double f_sign(double x, double y)
+{
+    if (y > 0.0) return fabs(x);
+    if (y < 0.0) return -fabs(x);
+    return signbit(y) ? -fabs(x) : fabs(x);
+}
+
+static double f_nint(double x) { return floor(x + 0.5); }
+
+static double f_asum(int n, const double *x)
+{
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += fabs(x[i]);
+    return s;
+}
+
+/* std::max(a, b) / std::min(a, b): (a < b) ? b : a  /  (b < a) ? b : a */
+static double f_max(double a, double b) { return (a < b) ? b : a; }
+static double f_min(double a, double b) { return (b < a) ? b : a; }
+
+/* LANGE.  flens/lapack/la/lan.tcc (GeMatrix): max |a_ij| in column order;
+ * one-norm = max column sum (each sum in increasing i); infinity-norm = max
+ * of the row sums accumulated column by column. */
+double oracle_dlange(char norm, int m, int n, const double *A, int ldA)
+{
+    if (m == 0 || n == 0) return 0.0;
+    double value = 0.0;
+    if (norm == 'M' || norm == 'm') {
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < m; ++i) value = f_max(value, fabs(A[IDX(i, j, ldA)]));
+    } else if (norm == 'I' || norm == 'i') {
+        double *w = (double *)calloc((size_t)m, sizeof(double));
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < m; ++i) w[i] += fabs(A[IDX(i, j, ldA)]);
+        for (int i = 0; i < m; ++i) value = f_max(value, w[i]);
+        free(w);
+    } else {
+        for (int j = 0; j < n; ++j) {
+            double sum = 0.0;
+            for (int i = 0; i < m; ++i) sum += fabs(A[IDX(i, j, ldA)]);
+            value = f_max(value, sum);
+        }
+    }
+    return value;
+}
+
+/* LACN2.  flens/lapack/la/lacn2.tcc (real variant), the reference's
+ * reverse-communication state machine step for step (isave[0..2] = its
+ * iSave(1..3), indices 1-based as there). */
+void oracle_dlacn2(int n, double *v, double *x, int *sgn, double *est, int *kase,
+                   int *isave)
+{
+    const int itMax = 5;
+    if (*kase == 0) {
+        for (int i = 0; i < n; ++i) x[i] = 1.0 / (double)n;
+        *kase = 1;
+        isave[0] = 1;
+        return;
+    }
+    int jlast, converged;
+    double estold, altsgn, temp;
+    switch (isave[0]) {
+    case 1:
+        if (n == 1) {
+            v[0] = x[0];
+            *est = fabs(v[0]);
+            goto QUIT;
+        }
+        *est = f_asum(n, x);
+        for (int i = 0; i < n; ++i) {
+            x[i] = f_sign(1.0, x[i]);
+            sgn[i] = (int)f_nint(x[i]);
+        }
+        *kase = 2;
+        isave[0] = 2;
+        return;
+    case 2:
+        isave[1] = oracle_idamax(n, x, 1) + 1;
+        isave[2] = 2;
+    MAIN:
+        for (int i = 0; i < n; ++i) x[i] = 0.0;
+        x[isave[1] - 1] = 1.0;
+        *kase = 1;
+        isave[0] = 3;
+        return;
+    case 3:
+        for (int i = 0; i < n; ++i) v[i] = x[i];
+        estold = *est;
+        *est = f_asum(n, v);
+        converged = 1;
+        for (int i = 0; i < n; ++i) {
+            if (f_nint(f_sign(1.0, x[i])) != (double)sgn[i]) {
+                converged = 0;
+                break;
+            }
+        }
+        if (converged) goto ITERATION_COMPLETE;
+        if (*est <= estold) goto ITERATION_COMPLETE;
+        for (int i = 0; i < n; ++i) {
+            x[i] = f_sign(1.0, x[i]);
+            sgn[i] = (int)f_nint(x[i]);
+        }
+        *kase = 2;
+        isave[0] = 4;
+        return;
+    case 4:
+        jlast = isave[1];
+        isave[1] = oracle_idamax(n, x, 1) + 1;
+        if (x[jlast - 1] != fabs(x[isave[1] - 1]) && isave[2] < itMax) {
+            ++isave[2];
+            goto MAIN;
+        }
+    ITERATION_COMPLETE:
+        altsgn = 1.0;
+        for (int i = 0; i < n; ++i) {
+            x[i] = altsgn * (1.0 + (double)i / (double)(n - 1));
+            altsgn = -altsgn;
+        }
+        *kase = 1;
+        isave[0] = 5;
+        return;
+    case 5:
+        temp = 2.0 * (f_asum(n, x) / (double)(3 * n));
+        if (temp > *est) {
+            for (int i = 0; i < n; ++i) v[i] = x[i];
+            *est = temp;
+        }
+    }
+QUIT:
+    *kase = 0;
+}
+
+/* LATRS.  flens/lapack/la/latrs.tcc (real variant), the part up to the
+ * choice of path: column norms of the off-diagonal triangle (asum, unless
+ * normIn), tscale from their max, xmax = |x(iamax)|, the growth bound grow
+ * from the loop over the diagonal, and when grow*tscale > smallNum the plain
+ * triangular solve blas::sv (the dot-form trsv of oracle_dtrsm).  The scaled
+ * careful path is not restated: -1 is returned instead. */
+int oracle_dlatrs(char upLo, char trans, char diag, int normIn, int n,
+                  const double *A, int ldA, double *x, double *scale,
+                  double *cnorm)
+{
+    const int upper = (upLo == 'U' || upLo == 'u');
+    const int nT = is_notrans(trans);
+    const int nonunit = (diag == 'N' || diag == 'n');
+    *scale = 1.0;
+    if (n == 0) return 0;
+    const double smallNum = kSafeMin / kPrecision;
+    const double bigNum = 1.0 / smallNum;
+    if (!normIn) {
+        if (upper) {
+            for (int j = 0; j < n; ++j) cnorm[j] = f_asum(j, &A[IDX(0, j, ldA)]);
+        } else {
+            for (int j = 0; j < n - 1; ++j) cnorm[j] = f_asum(n - 1 - j, &A[IDX(j + 1, j, ldA)]);
+            cnorm[n - 1] = 0.0;
+        }
+    }
+    const int imax = oracle_idamax(n, cnorm, 1);
+    const double tmax = cnorm[imax];
+    double tscale;
+    if (tmax <= bigNum) {
+        tscale = 1.0;
+    } else {
+        return -1;
+    }
+    const int jx = oracle_idamax(n, x, 1);
+    const double xmax = fabs(x[jx]);
+    double xbound = xmax, grow;
+    int jfirst, jlast, jinc;
+    if (nT) {
+        if (upper) { jfirst = n - 1; jlast = 0; jinc = -1; }
+        else { jfirst = 0; jlast = n - 1; jinc = 1; }
+    } else {
+        if (upper) { jfirst = 0; jlast = n - 1; jinc = 1; }
+        else { jfirst = n - 1; jlast = 0; jinc = -1; }
+    }
+    const int jend = jlast + jinc;
+    if (tscale != 1.0) {
+        grow = 0.0;
+    } else if (nT) {
+        if (nonunit) {
+            grow = 1.0 / f_max(xbound, smallNum);
+            xbound = grow;
+            int too_small = 0;
+            for (int j = jfirst; j != jend; j += jinc) {
+                if (grow <= smallNum) { too_small = 1; break; }
+                const double tjj = fabs(A[IDX(j, j, ldA)]);
+                xbound = f_min(xbound, f_min(1.0, tjj) * grow);
+                if (tjj + cnorm[j] >= smallNum) grow *= tjj / (tjj + cnorm[j]);
+                else grow = 0.0;
+            }
+            if (!too_small) grow = xbound;
+        } else {
+            grow = f_min(1.0, 1.0 / f_max(xbound, smallNum));
+            for (int j = jfirst; j != jend; j += jinc) {
+                if (grow <= smallNum) break;
+                grow *= 1.0 / (1.0 + cnorm[j]);
+            }
+        }
+    } else {
+        if (nonunit) {
+            grow = 1.0 / f_max(xbound, smallNum);
+            xbound = grow;
+            for (int j = jfirst; j != jend; j += jinc) {
+                if (grow <= smallNum) break;
+                const double xj = 1.0 + cnorm[j];
+                grow = f_min(grow, xbound / xj);
+                const double tjj = fabs(A[IDX(j, j, ldA)]);
+                if (xj > tjj) xbound *= tjj / xj;
+            }
+            grow = f_min(grow, xbound);
+        } else {
+            grow = f_min(1.0, 1.0 / f_max(xbound, smallNum));
+            for (int j = jfirst; j != jend; j += jinc) {
+                if (grow <= smallNum) break;
+                grow /= 1.0 + cnorm[j];
+            }
+        }
+    }
+    if (grow * tscale > smallNum) {
+        oracle_dtrsm('L', upper ? 'U' : 'L', nT ? 'N' : 'T', nonunit ? 'N' : 'U', n, 1, 1.0,
+                     A, ldA, x, n);
+        return 0;
+    }
+    return -1;
+}
+
+/* GECON.  flens/lapack/ge/cond.tcc (real variant): lacn2 drives solves with
+ * the unit-lower L and upper U of the factors through latrs (L then U for
+ * the chosen norm, U^T then L^T otherwise; column norms computed on the first
+ * pair only); rcond = (1/estimate)/anorm. */
+int oracle_dgecon(char norm, int n, const double *A, int ldA, double anorm,
+                  double *rcond)
+{
+    *rcond = 0.0;
+    if (n == 0) {
+        *rcond = 1.0;
+        return 0;
+    } else if (anorm == 0.0) {
+        return 0;
+    }
+    const int kase1 = (norm == '1' || norm == 'O' || norm == 'o') ? 1 : 2;
+    double *work = (double *)calloc((size_t)4 * n, sizeof(double));
+    int *iwork = (int *)calloc((size_t)n, sizeof(int));
+    double *x = work, *v = work + n, *cnL = work + 2 * n, *cnU = work + 3 * n;
+    int isave[3] = {0, 0, 0}, kase = 0, normIn = 0, status = 0;
+    double ainvnm = 0.0;
+    for (;;) {
+        oracle_dlacn2(n, v, x, iwork, &ainvnm, &kase, isave);
+        if (kase == 0) break;
+        double sl, su;
+        int r;
+        if (kase == kase1) {
+            r = oracle_dlatrs('L', 'N', 'U', normIn, n, A, ldA, x, &sl, cnL);
+            if (r == 0) r = oracle_dlatrs('U', 'N', 'N', normIn, n, A, ldA, x, &su, cnU);
+        } else {
+            r = oracle_dlatrs('U', 'T', 'N', normIn, n, A, ldA, x, &su, cnU);
+            if (r == 0) r = oracle_dlatrs('L', 'T', 'U', normIn, n, A, ldA, x, &sl, cnL);
+        }
+        if (r != 0) {
+            status = -1;
+            break;
+        }
+        normIn = 1;                       /* sl = su = 1 on the unscaled path */
+    }
+    if (status == 0 && ainvnm != 0.0) *rcond = (1.0 / ainvnm) / anorm;
+    free(work);
+    free(iwork);
+    return status;
+}
+
+/* GERFS.  flens/lapack/ge/rfs.tcc (generic rfs_impl), per right-hand side:
+ * r = b - op(A) x (gemv), w = |b| + |op(A)||x| (NoTrans accumulated column by
+ * column, Trans as column dots), berr = max_i |r_i|/w_i (with safe1 added
+ * where w_i <= safe2); while berr > eps, 2 berr <= last and at most 5 steps,
+ * solve op(AF) dx = r and x += dx; then the forward error bound from lacn2
+ * with w_i <- |r_i| + (n+1) eps w_i (+safe1), divided by max |x_i|. */
+int oracle_dgerfs(char trans, int n, int nRhs, const double *A, int ldA,
+                  const double *AF, int ldAF, const int *piv, const double *B,
+                  int ldB, double *X, int ldX, double *ferr, double *berr)
+{
+    const int nT = is_notrans(trans);
+    const char tr = nT ? 'N' : 'T', trT = nT ? 'T' : 'N';
+    if (n == 0 || nRhs == 0) {
+        for (int j = 0; j < nRhs; ++j) ferr[j] = berr[j] = 0.0;
+        return 0;
+    }
+    const int nz = n + 1;
+    const double eps = kEps, safeMin = kSafeMin;
+    const double safe1 = nz * safeMin, safe2 = safe1 / eps;
+    double *work = (double *)calloc((size_t)3 * n, sizeof(double));
+    int *iwork = (int *)calloc((size_t)n, sizeof(int));
+    double *w1 = work, *w2 = work + n, *w3 = work + 2 * n;
+    for (int j = 0; j < nRhs; ++j) {
+        int count = 1;
+        double lastres = 3.0;
+        double *x = &X[IDX(0, j, ldX)];
+        const double *b = &B[IDX(0, j, ldB)];
+        for (;;) {
+            for (int i = 0; i < n; ++i) w2[i] = b[i];
+            oracle_dgemv(tr, n, n, -1.0, A, ldA, x, 1, 1.0, w2, 1);
+            for (int i = 0; i < n; ++i) w1[i] = fabs(b[i]);
+            if (nT) {
+                for (int k = 0; k < n; ++k) {
+                    const double xk = fabs(x[k]);
+                    for (int i = 0; i < n; ++i) w1[i] += fabs(A[IDX(i, k, ldA)]) * xk;
+                }
+            } else {
+                for (int k = 0; k < n; ++k) {
+                    double s = 0.0;
+                    for (int i = 0; i < n; ++i) s += fabs(A[IDX(i, k, ldA)]) * fabs(x[i]);
+                    w1[k] += s;
+                }
+            }
+            double s = 0.0;
+            for (int i = 0; i < n; ++i) {
+                if (w1[i] > safe2) s = f_max(s, fabs(w2[i]) / w1[i]);
+                else s = f_max(s, (fabs(w2[i]) + safe1) / (w1[i] + safe1));
+            }
+            berr[j] = s;
+            if (berr[j] > eps && 2.0 * berr[j] <= lastres && count <= 5) {
+                oracle_dgetrs(tr, n, 1, AF, ldAF, piv, w2, n);
+                for (int i = 0; i < n; ++i) x[i] += w2[i];
+                lastres = berr[j];
+                ++count;
+                continue;
+            }
+            break;
+        }
+        for (int i = 0; i < n; ++i) {
+            if (w1[i] > safe2) w1[i] = fabs(w2[i]) + (double)nz * eps * w1[i];
+            else w1[i] = fabs(w2[i]) + (double)nz * eps * w1[i] + safe1;
+        }
+        int kase = 0, isave[3] = {0, 0, 0};
+        for (;;) {
+            oracle_dlacn2(n, w3, w2, iwork, &ferr[j], &kase, isave);
+            if (kase == 0) break;
+            if (kase == 1) {
+                oracle_dgetrs(trT, n, 1, AF, ldAF, piv, w2, n);
+                for (int i = 0; i < n; ++i) w2[i] *= w1[i];
+            } else {
+                for (int i = 0; i < n; ++i) w2[i] *= w1[i];
+                oracle_dgetrs(tr, n, 1, AF, ldAF, piv, w2, n);
+            }
+        }
+        lastres = 0.0;
+        for (int i = 0; i < n; ++i) lastres = f_max(lastres, fabs(x[i]));
+        if (lastres != 0.0) ferr[j] /= lastres;
+    }
+    free(work);
+    free(iwork);
+    return 0;
+}
+
+/* GEEQU.  flens/lapack/ge/equ.tcc: r_i = 1/clamp(max_j |a_ij|), c_j =
+ * 1/clamp(max_i |a_ij| r_i), the ratios rowcnd/colcnd and amax; info = i
+ * (or m+j) for the first zero row (column). */
+int oracle_dgeequ(int m, int n, const double *A, int ldA, double *r, double *c,
+                  double *rowcnd, double *colcnd, double *amax)
+{
+    if (m == 0 || n == 0) {
+        *rowcnd = 1.0;
+        *colcnd = 1.0;
+        *amax = 0.0;
+        return 0;
+    }
+    const double smallNum = kSafeMin, bigNum = 1.0 / smallNum;
+    for (int i = 0; i < m; ++i) r[i] = 0.0;
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < m; ++i) r[i] = f_max(r[i], fabs(A[IDX(i, j, ldA)]));
+    double rcmin = bigNum, rcmax = 0.0;
+    for (int i = 0; i < m; ++i) {
+        rcmax = f_max(rcmax, r[i]);
+        rcmin = f_min(rcmin, r[i]);
+    }
+    *amax = rcmax;
+    if (rcmin == 0.0) {
+        for (int i = 0; i < m; ++i)
+            if (r[i] == 0.0) return i + 1;
+    } else {
+        for (int i = 0; i < m; ++i) r[i] = 1.0 / f_min(f_max(r[i], smallNum), bigNum);
+        *rowcnd = f_max(rcmin, smallNum) / f_min(rcmax, bigNum);
+    }
+    for (int j = 0; j < n; ++j) c[j] = 0.0;
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < m; ++i) c[j] = f_max(c[j], fabs(A[IDX(i, j, ldA)]) * r[i]);
+    rcmin = bigNum;
+    rcmax = 0.0;
+    for (int j = 0; j < n; ++j) {
+        rcmin = f_min(rcmin, c[j]);
+        rcmax = f_max(rcmax, c[j]);
+    }
+    if (rcmin == 0.0) {
+        for (int j = 0; j < n; ++j)
+            if (c[j] == 0.0) return m + j + 1;
+    } else {
+        for (int j = 0; j < n; ++j) c[j] = 1.0 / f_min(f_max(c[j], smallNum), bigNum);
+        *colcnd = f_max(rcmin, smallNum) / f_min(rcmax, bigNum);
+    }
+    return 0;
+}
+
+/* LAQGE.  flens/lapack/la/laq.tcc: thresholds 0.1 and SafeMin/Precision. */
+char oracle_dlaqge(int m, int n, double *A, int ldA, const double *r,
+                   const double *c, double rowcnd, double colcnd, double amax)
+{
+    if (m == 0 || n == 0) return 'N';
+    const double small = kSafeMin / kPrecision, large = 1.0 / small;
+    if (rowcnd >= 0.1 && amax >= small && amax <= large) {
+        if (colcnd >= 0.1) return 'N';
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < m; ++i) A[IDX(i, j, ldA)] *= c[j];
+        return 'C';
+    } else if (colcnd >= 0.1) {
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < m; ++i) A[IDX(i, j, ldA)] *= r[i];
+        return 'R';
+    }
+    for (int j = 0; j < n; ++j) {
+        const double cj = c[j];
+        for (int i = 0; i < m; ++i) A[IDX(i, j, ldA)] *= cj * r[i];
+    }
+    return 'B';
+}
+
+/* maximum |a_ij| over the upper triangle (lan on a TrMatrix, max norm) */
+static double upper_max(int m, int n, const double *A, int ldA)
+{
+    double v = 0.0;
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i <= j && i < m; ++i) v = f_max(v, fabs(A[IDX(i, j, ldA)]));
+    return v;
+}
+
+/* GESVX.  flens/lapack/ge/svx.tcc (generic svx_impl). */
+int oracle_dgesvx(char fact, char trans, int n, int nRhs, double *A, int ldA,
+                  double *AF, int ldAF, int *piv, char *equed, double *r,
+                  double *c, double *B, int ldB, double *X, int ldX,
+                  double *rcond, double *ferr, double *berr, double *rpvgrw)
+{
+    const double smallNum = kSafeMin, bigNum = 1.0 / smallNum;
+    const int nT = is_notrans(trans);
+    int rowequ, colequ, info = 0;
+    double rowcnd = 1.0, colcnd = 1.0;
+    if (fact == 'N' || fact == 'E') {
+        *equed = 'N';
+        rowequ = colequ = 0;
+    } else {
+        rowequ = (*equed == 'R' || *equed == 'B');
+        colequ = (*equed == 'C' || *equed == 'B');
+    }
+    if (rowequ) {
+        double lo = bigNum, hi = 0.0;
+        for (int j = 0; j < n; ++j) { lo = f_min(lo, r[j]); hi = f_max(hi, r[j]); }
+        rowcnd = n > 0 ? f_max(lo, smallNum) / f_min(hi, bigNum) : 1.0;
+    }
+    if (colequ) {
+        double lo = bigNum, hi = 0.0;
+        for (int j = 0; j < n; ++j) { lo = f_min(lo, c[j]); hi = f_max(hi, c[j]); }
+        colcnd = n > 0 ? f_max(lo, smallNum) / f_min(hi, bigNum) : 1.0;
+    }
+    if (fact == 'E') {
+        double amax;
+        if (oracle_dgeequ(n, n, A, ldA, r, c, &rowcnd, &colcnd, &amax) == 0) {
+            *equed = oracle_dlaqge(n, n, A, ldA, r, c, rowcnd, colcnd, amax);
+            rowequ = (*equed == 'R' || *equed == 'B');
+            colequ = (*equed == 'C' || *equed == 'B');
+        }
+    }
+    if (nT) {
+        if (rowequ)
+            for (int j = 0; j < nRhs; ++j)
+                for (int i = 0; i < n; ++i) B[IDX(i, j, ldB)] *= r[i];
+    } else if (colequ) {
+        for (int j = 0; j < nRhs; ++j)
+            for (int i = 0; i < n; ++i) B[IDX(i, j, ldB)] *= c[i];
+    }
+    if (fact == 'N' || fact == 'E') {
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i) AF[IDX(i, j, ldAF)] = A[IDX(i, j, ldA)];
+        info = oracle_dgetrf(n, n, AF, ldAF, piv);
+        if (info > 0) {
+            double g = upper_max(info, info, AF, ldAF);
+            g = (g == 0.0) ? 1.0 : oracle_dlange('M', n, info, A, ldA) / g;
+            *rpvgrw = g;
+            *rcond = 0.0;
+            return info;
+        }
+    }
+    const double anorm = oracle_dlange(nT ? '1' : 'I', n, n, A, ldA);
+    double g = upper_max(n, n, AF, ldAF);
+    g = (g == 0.0) ? 1.0 : oracle_dlange('M', n, n, A, ldA) / g;
+    if (oracle_dgecon(nT ? '1' : 'I', n, AF, ldAF, anorm, rcond) != 0) return -1;
+    for (int j = 0; j < nRhs; ++j)
+        for (int i = 0; i < n; ++i) X[IDX(i, j, ldX)] = B[IDX(i, j, ldB)];
+    oracle_dgetrs(nT ? 'N' : 'T', n, nRhs, AF, ldAF, piv, X, ldX);
+    oracle_dgerfs(trans, n, nRhs, A, ldA, AF, ldAF, piv, B, ldB, X, ldX, ferr, berr);
+    if (nT) {
+        if (colequ) {
+            for (int j = 0; j < nRhs; ++j)
+                for (int i = 0; i < n; ++i) X[IDX(i, j, ldX)] *= c[i];
+            for (int j = 0; j < nRhs; ++j) ferr[j] /= colcnd;
+        }
+    } else if (rowequ) {
+        for (int j = 0; j < nRhs; ++j)
+            for (int i = 0; i < n; ++i) X[IDX(i, j, ldX)] *= r[i];
+        for (int j = 0; j < nRhs; ++j) ferr[j] /= rowcnd;
+    }
+    *rpvgrw = g;
+    if (*rcond < kEps) info = n + 1;
+    return info;
+}
+
 /*
  * POTF2.  flens/lapack/po/potf2.tcc:56-140 (left-looking, dot form): for each
  * column j, ajj = A(j,j) - dot(a, a) over the finished part of row/column j;

@@ -93,6 +93,52 @@ int oracle_dtrtri(char upLo, char diag, int n, double *A, int ldA);
  * allocated inside); info as dtrtri of U         flens/lapack/ge/tri.tcc */
 int oracle_dgetri(int n, double *A, int ldA, const int *piv);
 
+/* ---- refinement, condition estimate, equilibration (expert driver) ---- */
+/* norm '1'/'O' (max column sum), 'I' (max row sum), 'M' (max |a_ij|)
+ *                                                flens/lapack/la/lan.tcc */
+double oracle_dlange(char norm, int m, int n, const double *A, int ldA);
+
+/* Hager/Higham 1-norm estimator, reverse communication (v, x, sgn length n;
+ * isave[3]); kase = 0 on entry starts, on return 1: x <- A x, 2: x <- A^T x,
+ * 0: done, est holds the estimate               flens/lapack/la/lacn2.tcc */
+void oracle_dlacn2(int n, double *v, double *x, int *sgn, double *est, int *kase,
+                   int *isave);
+
+/* triangular solve with overflow protection: only the unscaled path
+ * (blas::sv) is restated.  Returns 0 and *scale = 1 when the reference takes
+ * it, -1 (x untouched) when the reference would scale
+ *                                                flens/lapack/la/latrs.tcc */
+int oracle_dlatrs(char upLo, char trans, char diag, int normIn, int n,
+                  const double *A, int ldA, double *x, double *scale,
+                  double *cnorm);
+
+/* reciprocal condition number estimate from the LU factors; returns -1
+ * where latrs would need its scaled path           flens/lapack/ge/cond.tcc */
+int oracle_dgecon(char norm, int n, const double *A, int ldA, double anorm,
+                  double *rcond);
+
+/* iterative refinement with componentwise backward error and forward error
+ * bound per right-hand side                        flens/lapack/ge/rfs.tcc */
+int oracle_dgerfs(char trans, int n, int nRhs, const double *A, int ldA,
+                  const double *AF, int ldAF, const int *piv, const double *B,
+                  int ldB, double *X, int ldX, double *ferr, double *berr);
+
+/* row/column equilibration scalings                flens/lapack/ge/equ.tcc */
+int oracle_dgeequ(int m, int n, const double *A, int ldA, double *r, double *c,
+                  double *rowcnd, double *colcnd, double *amax);
+
+/* apply the scalings when worthwhile; returns 'N','R','C','B'
+ *                                                   flens/lapack/la/laq.tcc */
+char oracle_dlaqge(int m, int n, double *A, int ldA, const double *r,
+                   const double *c, double rowcnd, double colcnd, double amax);
+
+/* expert driver: fact 'N'/'E'/'F', *equed in/out, rpvgrw = reciprocal pivot
+ * growth (WORK(1) of the reference)                 flens/lapack/ge/svx.tcc */
+int oracle_dgesvx(char fact, char trans, int n, int nRhs, double *A, int ldA,
+                  double *AF, int ldAF, int *piv, char *equed, double *r,
+                  double *c, double *B, int ldB, double *X, int ldX,
+                  double *rcond, double *ferr, double *berr, double *rpvgrw);
+
 /* y <- beta*y + alpha*op(A)*x                  cxxblas/level2/gemv.tcc:42-200 */
 void oracle_dgemv(char trans, int m, int n, double alpha, const double *A,
                   int ldA, const double *x, int incX, double beta, double *y,

@@ -2,7 +2,7 @@
 
 Runs the reference's own Fortran-ABI shims (dgemm_, dtrsm_, dsyrk_, dtrmm_,
 dsymm_, dsyr2k_, dgetrf_, dgetrs_, dgesv_, dgetri_, dtrtri_, dpotrf_, dpotrs_,
-dposv_ compiled
+dposv_, dgecon_, dgerfs_, dgeequ_, dlaqge_, dgesvx_ compiled
 from the FLENS sources into
 oracle/_ref/libflens_ref.so by
 ``make -C oracle ref``) on seeded inputs and stores the outputs.  Inputs come
@@ -212,6 +212,22 @@ def getri_input(i, n):
     return A
 
 
+def refine_case_list():
+    """n for gecon / gerfs / geequ / laqge / gesvx (diagonally weighted uniform
+    matrices, one column and one row badly scaled for the equilibration)."""
+    return [(f"rfs{i:03d}", n) for i, n in enumerate((1, 2, 5, 31, 64, 65, 100))]
+
+
+def refine_inputs(i, n):
+    A = U(25000 + 10 * i, n, n)
+    A[np.arange(n), np.arange(n)] += n / 8.0 + 0.5
+    Ae = A.copy(order="F")
+    Ae[:, 1 % n] *= 1.0e6
+    Ae[0, :] *= 1.0e-5
+    B = U(25000 + 10 * i + 1, n, 3)
+    return A, Ae, B
+
+
 def chol_case_list():
     """(n, uplo, kind): kind 'spd' (well conditioned) or 'notpd' (a negative
     pivot at n//2, so INFO = n//2 + 1 with the factor of the leading block)."""
@@ -290,6 +306,32 @@ def generate_small(R):
         piv, info = R.dgetrf(LU)
         R.dgetri(LU, piv)
         out[name] = LU
+    for i, (name, n) in enumerate(refine_case_list()):
+        A, Ae, B = refine_inputs(i, n)
+        LU = A.copy(order="F")
+        piv, _ = R.dgetrf(LU)
+        rc = [R.dgecon(nm, LU.copy(order="F"), oracle.Port().dlange("1" if nm != "I" else "I", A))[0]
+              for nm in ("1", "I")]
+        out[name + "_rcond"] = np.array(rc)
+        for tr in "NT":
+            X = B.copy(order="F")
+            R.dgetrs(tr, LU.copy(order="F"), piv, X)
+            X[0, :] += 1e-8                                   # start away from the solution
+            ferr, berr = R.dgerfs(tr, A, LU.copy(order="F"), piv, B, X)
+            out[name + f"_rfs{tr}_X"], out[name + f"_rfs{tr}_ferr"] = X, ferr
+            out[name + f"_rfs{tr}_berr"] = berr
+        r, c, rcnd, ccnd, amax, info = R.dgeequ(Ae.copy(order="F"))
+        out[name + "_equ"] = np.concatenate([r, c, [rcnd, ccnd, amax, info]])
+        for fact in "NE":
+            for tr in "NT":
+                Aw, Bw = Ae.copy(order="F"), B.copy(order="F")
+                AF, Xw = np.zeros((n, n), order="F"), np.zeros((n, 3), order="F")
+                pv = np.zeros(n, dtype=np.int32)
+                info, eq, rcn, fe, be, g = R.dgesvx(fact, tr, Aw, AF, pv, "N", np.zeros(n),
+                                                    np.zeros(n), Bw, Xw)
+                k = name + f"_svx{fact}{tr}"
+                out[k + "_X"], out[k + "_AF"], out[k + "_A"] = Xw, AF, Aw
+                out[k + "_s"] = np.concatenate([[info, rcn, g], fe, be])
     for i, (name, (n, uplo, kind)) in enumerate(chol_case_list()):
         A = chol_input(i, n, kind)
         info = R.dpotrf(uplo, A)

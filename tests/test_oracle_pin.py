@@ -100,6 +100,43 @@ def test_trtri_getri_fixtures_bitwise(golden, port):
     assert port.dtrtri("U", "N", A) == 4 and np.array_equal(A, A0)
 
 
+def test_refinement_condition_equilibration_bitwise(golden, port):
+    """gecon, gerfs, geequ, laqge, gesvx against the reference's results.  The
+    reference's dgesvx_ returns EQUED = 'N' even after equilibrating (svx
+    takes equed by value, flens/lapack/ge/svx.tcc): only the results are
+    compared, EQUED is checked against what the scaled A shows."""
+    for i, (name, n) in enumerate(G.refine_case_list()):
+        A, Ae, B = G.refine_inputs(i, n)
+        LU = A.copy(order="F")
+        piv, _ = port.dgetrf(LU)
+        rc = [port.dgecon(nm, LU, port.dlange("1" if nm != "I" else "I", A)) for nm in ("1", "I")]
+        assert all(st == 0 for _, st in rc), name
+        assert np.array_equal(np.array([v for v, _ in rc]), golden[name + "_rcond"]), name
+        for tr in "NT":
+            X = B.copy(order="F")
+            port.dgetrs(tr, LU, piv, X)
+            X[0, :] += 1e-8
+            ferr, berr = port.dgerfs(tr, A, LU, piv, B, X)
+            assert np.array_equal(X, golden[name + f"_rfs{tr}_X"]), (name, tr)
+            assert np.array_equal(ferr, golden[name + f"_rfs{tr}_ferr"]), (name, tr)
+            assert np.array_equal(berr, golden[name + f"_rfs{tr}_berr"]), (name, tr)
+        r, c, rcnd, ccnd, amax, info = port.dgeequ(Ae)
+        assert np.array_equal(np.concatenate([r, c, [rcnd, ccnd, amax, info]]), golden[name + "_equ"])
+        for fact in "NE":
+            for tr in "NT":
+                Aw, Bw = Ae.copy(order="F"), B.copy(order="F")
+                AF, Xw = np.zeros((n, n), order="F"), np.zeros((n, 3), order="F")
+                pv = np.zeros(n, dtype=np.int32)
+                info, eq, rcn, fe, be, g = port.dgesvx(fact, tr, Aw, AF, pv, "N", np.zeros(n),
+                                                       np.zeros(n), Bw, Xw)
+                k = name + f"_svx{fact}{tr}"
+                assert np.array_equal(Xw, golden[k + "_X"]), k
+                assert np.array_equal(AF, golden[k + "_AF"]), k
+                assert np.array_equal(Aw, golden[k + "_A"]), k
+                assert np.array_equal(np.concatenate([[info, rcn, g], fe, be]), golden[k + "_s"]), k
+                assert (eq == "N") == np.array_equal(Aw, Ae), k
+
+
 def test_cholesky_fixtures_bitwise(golden, port):
     for i, (name, (n, uplo, kind)) in enumerate(G.chol_case_list()):
         A = G.chol_input(i, n, kind)
