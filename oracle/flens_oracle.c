@@ -1239,8 +1239,9 @@ int oracle_dgesvx(char fact, char trans, int n, int nRhs, double *A, int ldA,
             for (int i = 0; i < n; ++i) AF[IDX(i, j, ldAF)] = A[IDX(i, j, ldA)];
         info = oracle_dgetrf(n, n, AF, ldAF, piv);
         if (info > 0) {
+            /* svx.tcc: max-norm of the whole A over that of U(1:info,1:info) */
             double g = upper_max(info, info, AF, ldAF);
-            g = (g == 0.0) ? 1.0 : oracle_dlange('M', n, info, A, ldA) / g;
+            g = (g == 0.0) ? 1.0 : oracle_dlange('M', n, n, A, ldA) / g;
             *rpvgrw = g;
             *rcond = 0.0;
             return info;

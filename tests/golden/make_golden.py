@@ -332,6 +332,13 @@ def generate_small(R):
                 k = name + f"_svx{fact}{tr}"
                 out[k + "_X"], out[k + "_AF"], out[k + "_A"] = Xw, AF, Aw
                 out[k + "_s"] = np.concatenate([[info, rcn, g], fe, be])
+    # a singular system through gesvx: INFO, reciprocal pivot growth, rcond 0
+    A = singular_input()
+    n = A.shape[0]
+    AF, X = np.zeros((n, n), order="F"), np.zeros((n, 1), order="F")
+    info, eq, rcn, fe, be, g = R.dgesvx("N", "N", A, AF, np.zeros(n, dtype=np.int32), "N",
+                                        np.zeros(n), np.zeros(n), U(7778, n, 1), X)
+    out["svx_sing_s"] = np.array([info, rcn, g])
     for i, (name, (n, uplo, kind)) in enumerate(chol_case_list()):
         A = chol_input(i, n, kind)
         info = R.dpotrf(uplo, A)

@@ -135,6 +135,12 @@ def test_refinement_condition_equilibration_bitwise(golden, port):
                 assert np.array_equal(Aw, golden[k + "_A"]), k
                 assert np.array_equal(np.concatenate([[info, rcn, g], fe, be]), golden[k + "_s"]), k
                 assert (eq == "N") == np.array_equal(Aw, Ae), k
+    A = G.singular_input()
+    n = A.shape[0]
+    AF, X = np.zeros((n, n), order="F"), np.zeros((n, 1), order="F")
+    info, eq, rcn, fe, be, g = port.dgesvx("N", "N", A, AF, np.zeros(n, dtype=np.int32), "N",
+                                           np.zeros(n), np.zeros(n), G.U(7778, n, 1), X)
+    assert np.array_equal(np.array([info, rcn, g]), golden["svx_sing_s"]) and info == 3
 
 
 def test_cholesky_fixtures_bitwise(golden, port):
