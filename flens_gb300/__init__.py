@@ -93,6 +93,24 @@ def lib() -> ctypes.CDLL:
     L.dtrtri_.restype = None
     L.dgetri_.argtypes = [_ip, _dp, _ip, _ip, _dp, _ip, _ip]
     L.dgetri_.restype = None
+    L.dgerfs_.argtypes = [cp, _ip, _ip, _dp, _ip, _dp, _ip, _ip, _dp, _ip, _dp, _ip, _dp, _dp, _dp,
+                          _ip, _ip]
+    L.dgerfs_.restype = None
+    L.dgecon_.argtypes = [cp, _ip, _dp, _ip, _dp, _dp, _dp, _ip, _ip]
+    L.dgecon_.restype = None
+    L.dgeequ_.argtypes = [_ip, _ip, _dp, _ip, _dp, _dp, _dp, _dp, _dp, _ip]
+    L.dgeequ_.restype = None
+    L.dlaqge_.argtypes = [_ip, _ip, _dp, _ip, _dp, _dp, _dp, _dp, _dp, cp]
+    L.dlaqge_.restype = None
+    L.dgesvx_.argtypes = [cp, cp, _ip, _ip, _dp, _ip, _dp, _ip, _ip, cp, _dp, _dp, _dp, _ip, _dp,
+                          _ip, _dp, _dp, _dp, _dp, _ip, _ip]
+    L.dgesvx_.restype = None
+    L.flens_gb300_dgecon.argtypes = [_c, _i, _v, _i, _d, _dp, _v]
+    L.flens_gb300_dgerfs.argtypes = [_c, _i, _i, _v, _i, _v, _i, _v, _v, _i, _v, _i, _dp, _dp, _v]
+    L.flens_gb300_dgeequ.argtypes = [_i, _i, _v, _i, _v, _v, _dp, _dp, _dp, _ip, _v]
+    L.flens_gb300_dlaqge.argtypes = [_i, _i, _v, _i, _v, _v, _d, _d, _d, ctypes.c_char_p, _v]
+    L.flens_gb300_dgesvx.argtypes = [_c, _c, _i, _i, _v, _i, _v, _i, _v, ctypes.c_char_p, _v, _v, _v,
+                                     _i, _v, _i, _dp, _dp, _dp, _dp, _ip, _v]
     L.flens_gb300_dtrtri.argtypes = [_c, _c, _i, _v, _i, _v, _v]
     L.flens_gb300_dgetri.argtypes = [_i, _v, _i, _v, _v, _v]
     L.flens_gb300_dtrmm.argtypes = [_c, _c, _c, _c, _i, _i, _d, _v, _i, _v, _i, _v]
@@ -117,7 +135,9 @@ def lib() -> ctypes.CDLL:
               "flens_gb300_dgetrs", "flens_gb300_dgesv", "flens_gb300_sync",
               "flens_gb300_dsyrk", "flens_gb300_dpotrf", "flens_gb300_dpotrs",
               "flens_gb300_dposv", "flens_gb300_dtrmm", "flens_gb300_dsymm",
-              "flens_gb300_dsyr2k", "flens_gb300_dtrtri", "flens_gb300_dgetri"):
+              "flens_gb300_dsyr2k", "flens_gb300_dtrtri", "flens_gb300_dgetri",
+              "flens_gb300_dgecon", "flens_gb300_dgerfs", "flens_gb300_dgeequ",
+              "flens_gb300_dlaqge", "flens_gb300_dgesvx"):
         getattr(L, f).restype = _i
     L.flens_gb300_last_error.restype = ctypes.c_char_p
     L.flens_gb300_last_error.argtypes = []
@@ -284,6 +304,68 @@ def dgetri(A: np.ndarray, ipiv: np.ndarray) -> int:
     lib().dgetri_(_ref(n, _i), _fd(A), _ref(max(1, n), _i), ipiv.ctypes.data_as(_ip),
                   work.ctypes.data_as(_dp), _ref(work.size, _i), ctypes.byref(info))
     return info.value
+
+
+def dgecon(norm: str, LU: np.ndarray, anorm: float):
+    """Reciprocal condition number estimate from dgetrf_'s factors: (rcond, info)."""
+    n = LU.shape[0]
+    rc, info = ctypes.c_double(0.0), ctypes.c_int(0)
+    work, iwork = np.zeros(max(1, 4 * n)), np.zeros(max(1, n), dtype=np.int32)
+    lib().dgecon_(norm.encode(), _ref(n, _i), _fd(LU), _ref(max(1, n), _i), _ref(anorm, _d),
+                  ctypes.byref(rc), work.ctypes.data_as(_dp), iwork.ctypes.data_as(_ip),
+                  ctypes.byref(info))
+    return rc.value, info.value
+
+
+def dgerfs(trans: str, A: np.ndarray, LU: np.ndarray, ipiv: np.ndarray, B: np.ndarray,
+           X: np.ndarray):
+    """Refine X in place through dgerfs_; returns (ferr, berr, info)."""
+    n, k = B.shape
+    ferr, berr = np.zeros(max(1, k)), np.zeros(max(1, k))
+    work, iwork = np.zeros(max(1, 3 * n)), np.zeros(max(1, n), dtype=np.int32)
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    info = ctypes.c_int(0)
+    lib().dgerfs_(trans.encode(), _ref(n, _i), _ref(k, _i), _fd(A), _ref(max(1, n), _i), _fd(LU),
+                  _ref(max(1, n), _i), ipiv.ctypes.data_as(_ip), _fd(B), _ref(max(1, n), _i), _fd(X),
+                  _ref(max(1, n), _i), ferr.ctypes.data_as(_dp), berr.ctypes.data_as(_dp),
+                  work.ctypes.data_as(_dp), iwork.ctypes.data_as(_ip), ctypes.byref(info))
+    return ferr[:k], berr[:k], info.value
+
+
+def dgeequ(A: np.ndarray):
+    m, n = A.shape
+    r, c = np.zeros(max(1, m)), np.zeros(max(1, n))
+    rc, cc, am, info = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+    lib().dgeequ_(_ref(m, _i), _ref(n, _i), _fd(A), _ref(max(1, m), _i), r.ctypes.data_as(_dp),
+                  c.ctypes.data_as(_dp), ctypes.byref(rc), ctypes.byref(cc), ctypes.byref(am),
+                  ctypes.byref(info))
+    return r[:m], c[:n], rc.value, cc.value, am.value, info.value
+
+
+def dlaqge(A: np.ndarray, r, c, rowcnd: float, colcnd: float, amax: float) -> str:
+    m, n = A.shape
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    c = np.ascontiguousarray(c, dtype=np.float64)
+    eq = ctypes.create_string_buffer(b"?", 2)
+    lib().dlaqge_(_ref(m, _i), _ref(n, _i), _fd(A), _ref(max(1, m), _i), r.ctypes.data_as(_dp),
+                  c.ctypes.data_as(_dp), _ref(rowcnd, _d), _ref(colcnd, _d), _ref(amax, _d), eq)
+    return eq.value.decode()
+
+
+def dgesvx(fact: str, trans: str, A: np.ndarray, AF: np.ndarray, ipiv: np.ndarray, equed: str,
+           r: np.ndarray, c: np.ndarray, B: np.ndarray, X: np.ndarray):
+    """Expert driver through dgesvx_: (info, equed, rcond, ferr, berr, rpvgrw)."""
+    n, k = B.shape
+    eq = ctypes.create_string_buffer(equed.encode(), 2)
+    rc, info = ctypes.c_double(0.0), ctypes.c_int(0)
+    ferr, berr = np.zeros(max(1, k)), np.zeros(max(1, k))
+    work, iwork = np.zeros(max(1, 4 * n)), np.zeros(max(1, n), dtype=np.int32)
+    lib().dgesvx_(fact.encode(), trans.encode(), _ref(n, _i), _ref(k, _i), _fd(A), _ref(max(1, n), _i),
+                  _fd(AF), _ref(max(1, n), _i), ipiv.ctypes.data_as(_ip), eq, r.ctypes.data_as(_dp),
+                  c.ctypes.data_as(_dp), _fd(B), _ref(max(1, n), _i), _fd(X), _ref(max(1, n), _i),
+                  ctypes.byref(rc), ferr.ctypes.data_as(_dp), berr.ctypes.data_as(_dp),
+                  work.ctypes.data_as(_dp), iwork.ctypes.data_as(_ip), ctypes.byref(info))
+    return info.value, eq.value.decode(), rc.value, ferr[:k], berr[:k], work[0]
 
 
 def dpotrf(uplo: str, A: np.ndarray) -> int:

@@ -16,6 +16,8 @@
 //      dposv_   flens/lapack/interface/src/posv.cc:13-51
 //      dtrtri_  flens/lapack/interface/src/trtri.cc:9-55
 //      dgetri_  flens/lapack/interface/src/getri.cc:10-53
+//      dgerfs_, dgecon_, dgeequ_, dlaqge_, dgesvx_
+//               flens/lapack/interface/src/{gerfs,gecon,geequ,laqge,gesvx}.cc
 //    They take HOST pointers (as the reference does), copy the operands to
 //    the device, run the GPU path and copy the results back before
 //    returning.  Device (or managed) pointers are also accepted and used in
@@ -23,6 +25,8 @@
 // 2. flens_gb300_* device-pointer entry points, asynchronous on a caller
 //    stream: the fast path for callers that keep matrices resident in HBM.
 #include "common.cuh"
+
+#include <cfloat>
 
 #include <ctype.h>
 #include <stdio.h>
@@ -698,6 +702,261 @@ FG_API void dgetri_(const int *N, double *A, const int *LDA, const int *IPIV, do
     WORK[0] = opt;
 }
 
+// ------------------------------ refinement, condition, equilibration ----
+namespace {
+
+int dvec_in(int slot, const double *h, int n, cudaStream_t s, double **d, bool *staged) {
+    if (is_device_ptr(h)) {
+        *d = const_cast<double *>(h);
+        *staged = false;
+        return kOk;
+    }
+    void *p;
+    int st = stage_buf(slot, (size_t)(n > 0 ? n : 1) * sizeof(double), &p);
+    if (st != kOk) return st;
+    *d = (double *)p;
+    *staged = true;
+    if (n > 0) FG_CUDA(cudaMemcpyAsync(*d, h, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s));
+    return kOk;
+}
+
+}  // namespace
+
+// flens/lapack/interface/src/gerfs.cc:13-66 (checks 1, 2, 3, 5, 7, 10, 12)
+FG_API void dgerfs_(const char *TRANS, const int *N, const int *NRHS, const double *A,
+                    const int *LDA, const double *AF, const int *LDAF, const int *IPIV,
+                    const double *B, const int *LDB, double *X, const int *LDX, double *FERR,
+                    double *BERR, double *WORK, int *IWORK, int *INFO) {
+    (void)WORK;
+    (void)IWORK;
+    *INFO = 0;
+    if (*TRANS != 'N' && *TRANS != 'T' && *TRANS != 'C') *INFO = -1;
+    else if (*N < 0) *INFO = -2;
+    else if (*NRHS < 0) *INFO = -3;
+    else if (*LDA < std::max(1, *N)) *INFO = -5;
+    else if (*LDAF < std::max(1, *N)) *INFO = -7;
+    else if (*LDB < std::max(1, *N)) *INFO = -10;
+    else if (*LDX < std::max(1, *N)) *INFO = -12;
+    if (*INFO != 0) {
+        report_xerbla("DGERFS", -*INFO);
+        return;
+    }
+    const int n = *N, nrhs = *NRHS;
+    if (n == 0 || nrhs == 0) {
+        for (int j = 0; j < nrhs; ++j) FERR[j] = BERR[j] = 0.0;
+        return;
+    }
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    DevView a, af, b, x;
+    int *dpiv = nullptr;
+    bool pst = false;
+    if (st == kOk) st = view_in(0, A, n, n, *LDA, true, s, &a);
+    if (st == kOk) st = view_in(1, AF, n, n, *LDAF, true, s, &af);
+    if (st == kOk) st = view_in(2, B, n, nrhs, *LDB, true, s, &b);
+    if (st == kOk) st = ipiv_dev(3, const_cast<int *>(IPIV), n, true, s, &dpiv, &pst);
+    // X is staged through a buffer of its own (slots 0..3 hold A, AF, B, IPIV)
+    double *dx = nullptr;
+    if (st == kOk) {
+        if (is_device_ptr(X)) {
+            dx = X;
+        } else {
+            Workspace *w = workspace_for(s, 0);
+            dx = w ? (double *)workspace_slot(s, 3, (size_t)n * nrhs * sizeof(double)) : nullptr;
+            if (!dx) st = kErrAlloc;
+            else if (cudaMemcpy2DAsync(dx, (size_t)n * sizeof(double), X, (size_t)*LDX * sizeof(double),
+                                       (size_t)n * sizeof(double), nrhs, cudaMemcpyHostToDevice, s) != cudaSuccess)
+                st = kErrCuda;
+        }
+    }
+    const int ldx = is_device_ptr(X) ? *LDX : n;
+    if (st == kOk)
+        st = dgerfs_launch(*TRANS == 'C' ? 'T' : *TRANS, n, nrhs, a.p, a.ld, af.p, af.ld, dpiv, b.p, b.ld,
+                           dx, ldx, FERR, BERR, s);
+    if (st == kOk && dx != X &&
+        cudaMemcpy2DAsync(X, (size_t)*LDX * sizeof(double), dx, (size_t)n * sizeof(double),
+                          (size_t)n * sizeof(double), nrhs, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        st = kErrCuda;
+    if (st == kOk) st = finish(s);
+    if (st != kOk) *INFO = st;
+}
+
+// flens/lapack/interface/src/gecon.cc:13-51 (NORM '1', 'O' or 'I')
+FG_API void dgecon_(const char *NORM, const int *N, const double *A, const int *LDA,
+                    const double *ANORM, double *RCOND, double *WORK, int *IWORK, int *INFO) {
+    (void)WORK;
+    (void)IWORK;
+    *INFO = 0;
+    if (*NORM != '1' && *NORM != 'O' && *NORM != 'I') *INFO = -1;
+    else if (*N < 0) *INFO = -2;
+    else if (*LDA < std::max(1, *N)) *INFO = -4;
+    else if (*ANORM < 0) *INFO = -5;
+    if (*INFO != 0) {
+        report_xerbla("DGECON", -*INFO);
+        return;
+    }
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    DevView a;
+    if (st == kOk && *N > 0) st = view_in(0, A, *N, *N, *LDA, true, s, &a);
+    if (st == kOk) st = dgecon_launch(*NORM, *N, a.p, a.ld, *ANORM, RCOND, s);
+    if (st == kErrUnsupported) st = kOk;           // latrs would scale: RCOND = 0
+    if (st == kOk) st = finish(s);
+    if (st != kOk) *INFO = st;
+}
+
+// flens/lapack/interface/src/geequ.cc:10-40 (checks 1, 2, 4)
+FG_API void dgeequ_(const int *M, const int *N, const double *A, const int *LDA, double *R,
+                    double *C, double *ROWCND, double *COLCND, double *AMAX, int *INFO) {
+    *INFO = 0;
+    if (*M < 0) *INFO = -1;
+    else if (*N < 0) *INFO = -2;
+    else if (*LDA < std::max(1, *M)) *INFO = -4;
+    if (*INFO != 0) {
+        report_xerbla("DGEEQU", -*INFO);
+        return;
+    }
+    const int m = *M, n = *N;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    DevView a;
+    double *dr = nullptr, *dc = nullptr;
+    bool rs = false, cs = false;
+    if (st == kOk && m > 0 && n > 0) st = view_in(0, A, m, n, *LDA, true, s, &a);
+    if (st == kOk) st = dvec_in(1, R, m, s, &dr, &rs);
+    if (st == kOk) st = dvec_in(2, C, n, s, &dc, &cs);
+    int info = 0;
+    if (st == kOk) st = dgeequ_launch(m, n, a.p, a.ld, dr, dc, ROWCND, COLCND, AMAX, &info, s);
+    if (st == kOk && rs && m > 0) st = cudaMemcpyAsync(R, dr, (size_t)m * sizeof(double), cudaMemcpyDeviceToHost, s) == cudaSuccess ? kOk : kErrCuda;
+    if (st == kOk && cs && n > 0) st = cudaMemcpyAsync(C, dc, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s) == cudaSuccess ? kOk : kErrCuda;
+    if (st == kOk) st = finish(s);
+    *INFO = st != kOk ? st : info;
+}
+
+// flens/lapack/interface/src/laqge.cc:10-27 (no argument checks)
+FG_API void dlaqge_(const int *M, const int *N, double *A, const int *LDA, const double *R,
+                    const double *C, const double *ROWCND, const double *COLCND, const double *AMAX,
+                    char *EQUED) {
+    const int m = *M, n = *N;
+    *EQUED = 'N';
+    if (m <= 0 || n <= 0) return;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    DevView a;
+    double *dr = nullptr, *dc = nullptr;
+    bool rs = false, cs = false;
+    if (st == kOk) st = view_in(0, A, m, n, *LDA, true, s, &a);
+    if (st == kOk) st = dvec_in(1, R, m, s, &dr, &rs);
+    if (st == kOk) st = dvec_in(2, C, n, s, &dc, &cs);
+    char eq = 'N';
+    if (st == kOk) {
+        eq = dlaqge_launch(m, n, a.p, a.ld, dr, dc, *ROWCND, *COLCND, *AMAX, s);
+        if (eq == '?') st = kErrCuda;
+    }
+    if (st == kOk) st = view_out(a, A, m, n, *LDA, s);
+    if (st == kOk) st = finish(s);
+    if (st != kOk) fprintf(stderr, "[flens_gb300] dlaqge_ failed (%d): %s\n", st, flens_gb300_last_error());
+    else *EQUED = eq;
+}
+
+// flens/lapack/interface/src/gesvx.cc:13-118.  EQUED reports the scaling
+// applied (the reference's svx takes it by value, so its shim returns 'N'
+// after equilibrating); WORK(1) = reciprocal pivot growth.
+FG_API void dgesvx_(const char *FACT, const char *TRANS, const int *N, const int *NRHS, double *A,
+                    const int *LDA, double *AF, const int *LDAF, int *IPIV, char *EQUED, double *R,
+                    double *C, double *B, const int *LDB, double *X, const int *LDX, double *RCOND,
+                    double *FERR, double *BERR, double *WORK, int *IWORK, int *INFO) {
+    (void)IWORK;
+    const double bigNum = 1.0 / DBL_MIN;
+    bool rowequ, colequ;
+    if (*FACT == 'N' || *FACT == 'E') {
+        *EQUED = 'N';
+        rowequ = colequ = false;
+    } else {
+        rowequ = *EQUED == 'R' || *EQUED == 'B';
+        colequ = *EQUED == 'C' || *EQUED == 'B';
+    }
+    *INFO = 0;
+    if (*FACT != 'F' && *FACT != 'N' && *FACT != 'E') *INFO = -1;
+    else if (*TRANS != 'N' && *TRANS != 'T' && *TRANS != 'C') *INFO = -2;
+    else if (*N < 0) *INFO = -3;
+    else if (*NRHS < 0) *INFO = -4;
+    else if (*LDA < std::max(1, *N)) *INFO = -6;
+    else if (*LDAF < std::max(1, *N)) *INFO = -8;
+    else if (*FACT == 'F' && !(rowequ || colequ || *EQUED == 'N')) *INFO = -10;
+    else {
+        if (rowequ) {
+            double lo = bigNum;
+            for (int j = 0; j < *N; ++j) lo = std::min(lo, R[j]);
+            if (lo <= 0.0) *INFO = -11;
+        }
+        if (colequ && *INFO == 0) {
+            double lo = bigNum;
+            for (int j = 0; j < *N; ++j) lo = std::min(lo, C[j]);
+            if (lo <= 0.0) *INFO = -12;
+        }
+        if (*INFO == 0) {
+            if (*LDB < std::max(1, *N)) *INFO = -14;
+            else if (*LDX < std::max(1, *N)) *INFO = -16;
+        }
+    }
+    if (*INFO != 0) {
+        report_xerbla("DGESVX", -*INFO);
+        return;
+    }
+    const int n = *N, nrhs = *NRHS;
+    cudaStream_t s;
+    int st = stage_stream(&s);
+    // device copies: A, AF, B, X (n x n, n x n, n x nrhs, n x nrhs), IPIV, R, C
+    const size_t nn = (size_t)(n > 0 ? n : 1), nr = (size_t)(nrhs > 0 ? nrhs : 1);
+    const size_t bytes = sizeof(double) * (2 * nn * nn + 2 * nn * nr + 2 * nn) + sizeof(int) * nn + 256;
+    char *buf = (char *)workspace_slot(s, 3, bytes);
+    if (!buf) st = kErrAlloc;
+    double *dA = (double *)buf, *dAF = dA + nn * nn, *dB = dAF + nn * nn, *dX = dB + nn * nr;
+    double *dR = dX + nn * nr, *dC = dR + nn;
+    int *dP = (int *)(dC + nn);
+    auto up2 = [&](double *d, const double *h, int rows, int cols, int ld) {
+        if (st != kOk || rows <= 0 || cols <= 0) return;
+        if (cudaMemcpy2DAsync(d, (size_t)rows * sizeof(double), h, (size_t)ld * sizeof(double),
+                              (size_t)rows * sizeof(double), cols, cudaMemcpyHostToDevice, s) != cudaSuccess)
+            st = kErrCuda;
+    };
+    auto down2 = [&](double *h, const double *d, int rows, int cols, int ld) {
+        if (st != kOk || rows <= 0 || cols <= 0) return;
+        if (cudaMemcpy2DAsync(h, (size_t)ld * sizeof(double), d, (size_t)rows * sizeof(double),
+                              (size_t)rows * sizeof(double), cols, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            st = kErrCuda;
+    };
+    up2(dA, A, n, n, *LDA);
+    up2(dB, B, n, nrhs, *LDB);
+    if (*FACT == 'F') {
+        up2(dAF, AF, n, n, *LDAF);
+        if (st == kOk && n > 0 &&
+            cudaMemcpyAsync(dP, IPIV, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess)
+            st = kErrCuda;
+    }
+    up2(dR, R, n, 1, n);
+    up2(dC, C, n, 1, n);
+    int info = 0;
+    double rpvgrw = 1.0;
+    if (st == kOk)
+        st = dgesvx_launch(*FACT, *TRANS == 'C' ? 'T' : *TRANS, n, nrhs, dA, std::max(1, n), dAF,
+                           std::max(1, n), dP, EQUED, dR, dC, dB, std::max(1, n), dX, std::max(1, n),
+                           RCOND, FERR, BERR, &rpvgrw, &info, s);
+    down2(A, dA, n, n, *LDA);
+    down2(AF, dAF, n, n, *LDAF);
+    down2(B, dB, n, nrhs, *LDB);
+    if (info == 0 || info == n + 1) down2(X, dX, n, nrhs, *LDX);
+    down2(R, dR, n, 1, n);
+    down2(C, dC, n, 1, n);
+    if (st == kOk && n > 0 &&
+        cudaMemcpyAsync(IPIV, dP, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        st = kErrCuda;
+    if (st == kOk) st = finish(s);
+    WORK[0] = rpvgrw;
+    *INFO = st != kOk ? st : info;
+}
+
 // ------------------------------------------------ device-pointer API ----
 static inline cudaStream_t as_stream(void *s) { return (cudaStream_t)s; }
 
@@ -780,6 +1039,68 @@ FG_API int flens_gb300_dgetri(int n, double *A, int ldA, const int *ipiv, int *i
     if (n < 0) return -1;
     if (ldA < std::max(1, n)) return -3;
     return dgetri_launch(n, A, ldA, ipiv, info, as_stream(stream));
+}
+
+FG_API int flens_gb300_dgecon(char norm, int n, const double *LU, int ldLU, double anorm,
+                              double *rcond, void *stream) {
+    if (norm != '1' && norm != 'O' && norm != 'I' && norm != 'o' && norm != 'i') return -1;
+    if (n < 0) return -2;
+    if (ldLU < std::max(1, n)) return -4;
+    if (anorm < 0) return -5;
+    return dgecon_launch(norm, n, LU, ldLU, anorm, rcond, as_stream(stream));
+}
+
+FG_API int flens_gb300_dgerfs(char trans, int n, int nrhs, const double *A, int ldA, const double *AF,
+                              int ldAF, const int *ipiv, const double *B, int ldB, double *X, int ldX,
+                              double *ferr, double *berr, void *stream) {
+    trans = (char)toupper(trans);
+    if (trans != 'N' && trans != 'T' && trans != 'C') return -1;
+    if (n < 0) return -2;
+    if (nrhs < 0) return -3;
+    if (ldA < std::max(1, n)) return -5;
+    if (ldAF < std::max(1, n)) return -7;
+    if (ldB < std::max(1, n)) return -10;
+    if (ldX < std::max(1, n)) return -12;
+    return dgerfs_launch(trans == 'C' ? 'T' : trans, n, nrhs, A, ldA, AF, ldAF, ipiv, B, ldB, X, ldX,
+                         ferr, berr, as_stream(stream));
+}
+
+FG_API int flens_gb300_dgeequ(int m, int n, const double *A, int ldA, double *r, double *c,
+                              double *rowcnd, double *colcnd, double *amax, int *info, void *stream) {
+    if (m < 0) return -1;
+    if (n < 0) return -2;
+    if (ldA < std::max(1, m)) return -4;
+    return dgeequ_launch(m, n, A, ldA, r, c, rowcnd, colcnd, amax, info, as_stream(stream));
+}
+
+FG_API int flens_gb300_dlaqge(int m, int n, double *A, int ldA, const double *r, const double *c,
+                              double rowcnd, double colcnd, double amax, char *equed, void *stream) {
+    if (m < 0) return -1;
+    if (n < 0) return -2;
+    if (ldA < std::max(1, m)) return -4;
+    const char eq = dlaqge_launch(m, n, A, ldA, r, c, rowcnd, colcnd, amax, as_stream(stream));
+    if (eq == '?') return kErrCuda;
+    *equed = eq;
+    return kOk;
+}
+
+FG_API int flens_gb300_dgesvx(char fact, char trans, int n, int nrhs, double *A, int ldA, double *AF,
+                              int ldAF, int *ipiv, char *equed, double *r, double *c, double *B,
+                              int ldB, double *X, int ldX, double *rcond, double *ferr, double *berr,
+                              double *rpvgrw, int *info, void *stream) {
+    fact = (char)toupper(fact);
+    trans = (char)toupper(trans);
+    if (fact != 'F' && fact != 'N' && fact != 'E') return -1;
+    if (trans != 'N' && trans != 'T' && trans != 'C') return -2;
+    if (n < 0) return -3;
+    if (nrhs < 0) return -4;
+    if (ldA < std::max(1, n)) return -6;
+    if (ldAF < std::max(1, n)) return -8;
+    if (fact == 'F' && *equed != 'N' && *equed != 'R' && *equed != 'C' && *equed != 'B') return -10;
+    if (ldB < std::max(1, n)) return -14;
+    if (ldX < std::max(1, n)) return -16;
+    return dgesvx_launch(fact, trans == 'C' ? 'T' : trans, n, nrhs, A, ldA, AF, ldAF, ipiv, equed, r, c,
+                         B, ldB, X, ldX, rcond, ferr, berr, rpvgrw, info, as_stream(stream));
 }
 
 FG_API int flens_gb300_dpotrf(char uplo, int n, double *A, int ldA, int *info, void *stream) {

@@ -206,6 +206,27 @@ int dtrtri_launch(char uplo, char diag, int n, double *A, int ldA, int *info,
 int dgetri_launch(int n, double *A, int ldA, const int *ipiv, int *info,
                   cudaStream_t stream);
 
+// Refinement, condition estimate, equilibration (refine.cu).  Matrices and
+// vectors on the device; scalars (rcond, ferr, berr, ...) on the host; all
+// synchronise.
+int dgecon_launch(char norm, int n, const double *LU, int ldLU, double anorm,
+                  double *rcond, cudaStream_t stream);
+int dgerfs_launch(char trans, int n, int nrhs, const double *A, int ldA,
+                  const double *AF, int ldAF, const int *ipiv, const double *B,
+                  int ldB, double *X, int ldX, double *ferr, double *berr,
+                  cudaStream_t stream);
+int dgeequ_launch(int m, int n, const double *A, int ldA, double *r, double *c,
+                  double *rowcnd, double *colcnd, double *amax, int *info,
+                  cudaStream_t stream);
+char dlaqge_launch(int m, int n, double *A, int ldA, const double *r,
+                   const double *c, double rowcnd, double colcnd, double amax,
+                   cudaStream_t stream);
+int dgesvx_launch(char fact, char trans, int n, int nrhs, double *A, int ldA,
+                  double *AF, int ldAF, int *ipiv, char *equed, double *r,
+                  double *c, double *B, int ldB, double *X, int ldX,
+                  double *rcond, double *ferr, double *berr, double *rpvgrw,
+                  int *info, cudaStream_t stream);
+
 // Cholesky (uplo 'L': A = L L^T, 'U': A = U^T U) of the n x n uplo triangle
 // in place; *info (device) = first non-positive pivot (1-based) or 0.
 // Synchronises once per 64-column block to stop at the first failure.

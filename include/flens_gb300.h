@@ -144,6 +144,48 @@ void dtrtri_(const char *UPLO, const char *DIAG, const int *N, double *A,
 void dgetri_(const int *N, double *A, const int *LDA, const int *IPIV,
              double *WORK, const int *LWORK, int *INFO);
 
+/* Iterative refinement of X (op(A) X = B) with componentwise backward
+ * error BERR and forward error bound FERR per right-hand side.  Replaces
+ * dgerfs_ at flens/lapack/interface/src/gerfs.cc:13-66 (-> lapack::rfs
+ * flens/lapack/ge/rfs.tcc).  WORK, IWORK are not used (device workspace). */
+void dgerfs_(const char *TRANS, const int *N, const int *NRHS, const double *A,
+             const int *LDA, const double *AF, const int *LDAF, const int *IPIV,
+             const double *B, const int *LDB, double *X, const int *LDX,
+             double *FERR, double *BERR, double *WORK, int *IWORK, int *INFO);
+
+/* Reciprocal condition number estimate (1-norm for NORM '1'/'O', infinity
+ * norm for 'I') from dgetrf_'s factors and the norm of A.  Replaces dgecon_
+ * at flens/lapack/interface/src/gecon.cc:13-51 (-> lapack::con
+ * flens/lapack/ge/cond.tcc).  Where the reference's latrs would switch to its
+ * overflow-scaled solve (condition beyond about 1e290), RCOND is 0. */
+void dgecon_(const char *NORM, const int *N, const double *A, const int *LDA,
+             const double *ANORM, double *RCOND, double *WORK, int *IWORK,
+             int *INFO);
+
+/* Row and column scalings that equilibrate A.  Replaces dgeequ_ at
+ * flens/lapack/interface/src/geequ.cc:10-40 (-> flens/lapack/ge/equ.tcc). */
+void dgeequ_(const int *M, const int *N, const double *A, const int *LDA,
+             double *R, double *C, double *ROWCND, double *COLCND, double *AMAX,
+             int *INFO);
+
+/* Apply them when worthwhile; EQUED 'N', 'R', 'C' or 'B'.  Replaces dlaqge_
+ * at flens/lapack/interface/src/laqge.cc:10-27 (-> flens/lapack/la/laq.tcc). */
+void dlaqge_(const int *M, const int *N, double *A, const int *LDA,
+             const double *R, const double *C, const double *ROWCND,
+             const double *COLCND, const double *AMAX, char *EQUED);
+
+/* Expert driver: equilibrate (FACT='E'), factor (or use AF/IPIV, FACT='F'),
+ * condition estimate, solve, refine, error bounds; WORK(1) = reciprocal
+ * pivot growth.  INFO = N+1 when RCOND < eps.  Replaces dgesvx_ at
+ * flens/lapack/interface/src/gesvx.cc:13-118 (-> lapack::svx
+ * flens/lapack/ge/svx.tcc).  EQUED reports the scaling actually applied; the
+ * reference's shim returns 'N' there (its svx takes EQUED by value). */
+void dgesvx_(const char *FACT, const char *TRANS, const int *N, const int *NRHS,
+             double *A, const int *LDA, double *AF, const int *LDAF, int *IPIV,
+             char *EQUED, double *R, double *C, double *B, const int *LDB,
+             double *X, const int *LDX, double *RCOND, double *FERR,
+             double *BERR, double *WORK, int *IWORK, int *INFO);
+
 /* Weak default error handler (prints, does not stop).  Link your own
  * xerbla_ to override it, as with Netlib BLAS/LAPACK. */
 void xerbla_(const char *SRNAME, const int *INFO, int SRNAME_LEN);
@@ -200,6 +242,29 @@ int flens_gb300_dtrtri(char uplo, char diag, int n, double *A, int ldA,
                        int *info, void *stream);
 int flens_gb300_dgetri(int n, double *A, int ldA, const int *ipiv, int *info,
                        void *stream);
+
+/* Device forms of gecon, gerfs, geequ, laqge, gesvx: matrices, pivots and
+ * the scaling vectors r, c in device memory; rcond, ferr, berr, rowcnd,
+ * colcnd, amax, rpvgrw, info and equed are host scalars / arrays.  All
+ * synchronise (their iterations branch on reductions).  gecon returns
+ * FLENS_GB300_ERR_UNSUPPORTED (with *rcond = 0) where latrs would scale. */
+int flens_gb300_dgecon(char norm, int n, const double *LU, int ldLU,
+                       double anorm, double *rcond, void *stream);
+int flens_gb300_dgerfs(char trans, int n, int nrhs, const double *A, int ldA,
+                       const double *AF, int ldAF, const int *ipiv,
+                       const double *B, int ldB, double *X, int ldX,
+                       double *ferr, double *berr, void *stream);
+int flens_gb300_dgeequ(int m, int n, const double *A, int ldA, double *r,
+                       double *c, double *rowcnd, double *colcnd, double *amax,
+                       int *info, void *stream);
+int flens_gb300_dlaqge(int m, int n, double *A, int ldA, const double *r,
+                       const double *c, double rowcnd, double colcnd,
+                       double amax, char *equed, void *stream);
+int flens_gb300_dgesvx(char fact, char trans, int n, int nrhs, double *A,
+                       int ldA, double *AF, int ldAF, int *ipiv, char *equed,
+                       double *r, double *c, double *B, int ldB, double *X,
+                       int ldX, double *rcond, double *ferr, double *berr,
+                       double *rpvgrw, int *info, void *stream);
 
 /* dpotrf on device memory; info is a device int.  Blocked right-looking
  * (64-column steps: potf2 of the diagonal block, trsm, syrk of the trailing

@@ -215,6 +215,48 @@ def test_inverse_argument_errors_and_query():
     assert info.value == 0 and work[0] == 6400.0
 
 
+def test_refinement_argument_errors():
+    # flens/lapack/interface/src/{gerfs,gecon,geequ,gesvx}.cc
+    L = fg.lib()
+    info = ctypes.c_int(0)
+    d = ctypes.c_double(1.0)
+    for (tr, n, k, lda, ldaf, ldb, ldx, want) in [
+            ("X", 2, 1, 2, 2, 2, 2, -1), ("N", -1, 1, 2, 2, 2, 2, -2), ("N", 2, -1, 2, 2, 2, 2, -3),
+            ("N", 3, 1, 2, 3, 3, 3, -5), ("T", 3, 1, 3, 2, 3, 3, -7), ("N", 3, 1, 3, 3, 2, 3, -10),
+            ("C", 3, 1, 3, 3, 3, 2, -12)]:
+        name, pos = _xerbla_after(lambda: L.dgerfs_(
+            tr.encode(), _i(n), _i(k), NULLD, _i(lda), NULLD, _i(ldaf), NULLI, NULLD, _i(ldb), NULLD,
+            _i(ldx), NULLD, NULLD, NULLD, NULLI, ctypes.byref(info)))
+        assert info.value == want and name == "DGERFS" and pos == -want
+    for (nm, n, lda, an, want) in [("X", 2, 2, 1.0, -1), ("1", -1, 2, 1.0, -2), ("O", 3, 2, 1.0, -4),
+                                   ("I", 2, 2, -1.0, -5)]:
+        name, pos = _xerbla_after(lambda: L.dgecon_(nm.encode(), _i(n), NULLD, _i(lda), _d(an),
+                                                    ctypes.byref(d), NULLD, NULLI, ctypes.byref(info)))
+        assert info.value == want and name == "DGECON" and pos == -want
+    for (m, n, lda, want) in [(-1, 2, 2, -1), (2, -1, 2, -2), (3, 2, 2, -4)]:
+        name, pos = _xerbla_after(lambda: L.dgeequ_(_i(m), _i(n), NULLD, _i(lda), NULLD, NULLD,
+                                                    ctypes.byref(d), ctypes.byref(d), ctypes.byref(d),
+                                                    ctypes.byref(info)))
+        assert info.value == want and name == "DGEEQU" and pos == -want
+    eq = ctypes.create_string_buffer(b"N", 2)
+    for (fact, tr, n, k, lda, ldaf, ldb, ldx, want) in [
+            ("X", "N", 2, 1, 2, 2, 2, 2, -1), ("N", "X", 2, 1, 2, 2, 2, 2, -2),
+            ("N", "N", -1, 1, 2, 2, 2, 2, -3), ("N", "N", 2, -1, 2, 2, 2, 2, -4),
+            ("N", "N", 3, 1, 2, 3, 3, 3, -6), ("E", "N", 3, 1, 3, 2, 3, 3, -8),
+            ("N", "T", 3, 1, 3, 3, 2, 3, -14), ("N", "N", 3, 1, 3, 3, 3, 2, -16)]:
+        name, pos = _xerbla_after(lambda: L.dgesvx_(
+            fact.encode(), tr.encode(), _i(n), _i(k), NULLD, _i(lda), NULLD, _i(ldaf), NULLI, eq,
+            NULLD, NULLD, NULLD, _i(ldb), NULLD, _i(ldx), ctypes.byref(d), NULLD, NULLD, NULLD,
+            NULLI, ctypes.byref(info)))
+        assert info.value == want and name == "DGESVX" and pos == -want
+    # FACT = 'F' with an invalid EQUED
+    bad = ctypes.create_string_buffer(b"Q", 2)
+    name, pos = _xerbla_after(lambda: L.dgesvx_(
+        b"F", b"N", _i(2), _i(1), NULLD, _i(2), NULLD, _i(2), NULLI, bad, NULLD, NULLD, NULLD, _i(2),
+        NULLD, _i(2), ctypes.byref(d), NULLD, NULLD, NULLD, NULLI, ctypes.byref(info)))
+    assert info.value == -10 and name == "DGESVX"
+
+
 def test_quick_returns_touch_nothing():
     # m==0 / n==0 return before any device work (gemm.tcc:54-56, trf.tcc:81-83)
     L = fg.lib()
