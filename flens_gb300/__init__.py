@@ -123,6 +123,7 @@ def lib() -> ctypes.CDLL:
     L.flens_gb300_dgemm.argtypes = [_c, _c, _i, _i, _i, _d, _v, _i, _v, _i, _d, _v, _i, _v]
     L.flens_gb300_dtrsm.argtypes = [_c, _c, _c, _c, _i, _i, _d, _v, _i, _v, _i, _v]
     L.flens_gb300_dgetrf.argtypes = [_i, _i, _v, _i, _v, _v, _v]
+    L.flens_gb300_dgetrf_split.argtypes = [_i, _i, _v, _i, _v, _v, _i, _v]
     L.flens_gb300_dgetrs.argtypes = [_c, _i, _i, _v, _i, _v, _v, _i, _v]
     L.flens_gb300_dgesv.argtypes = [_i, _i, _v, _i, _v, _v, _i, _v, _v]
     L.flens_gb300_sync.argtypes = [_v]
@@ -131,7 +132,7 @@ def lib() -> ctypes.CDLL:
     L.flens_gb300_dgemm_split.argtypes = [_c, _c, _i, _i, _i, _d, _v, _i, _v, _i, _d, _v, _i, _i,
                                           ctypes.POINTER(ctypes.c_int), _v]
     L.flens_gb300_dgemm_split.restype = _i
-    for f in ("flens_gb300_dgemm", "flens_gb300_dtrsm", "flens_gb300_dgetrf",
+    for f in ("flens_gb300_dgemm", "flens_gb300_dtrsm", "flens_gb300_dgetrf", "flens_gb300_dgetrf_split",
               "flens_gb300_dgetrs", "flens_gb300_dgesv", "flens_gb300_sync",
               "flens_gb300_dsyrk", "flens_gb300_dpotrf", "flens_gb300_dpotrs",
               "flens_gb300_dposv", "flens_gb300_dtrmm", "flens_gb300_dsymm",
@@ -497,6 +498,15 @@ def dgetrf_dev(A, ipiv, info, stream=None):
     pa, m, n, lda = _colmajor(A)
     _check(lib().flens_gb300_dgetrf(m, n, pa, lda, ipiv.data_ptr(), info.data_ptr(),
                                     _stream(stream)), "flens_gb300_dgetrf")
+    return A
+
+
+def dgetrf_split_dev(A, ipiv, info, outer_nb=0, stream=None):
+    """FP64-accurate LU of a column-major CUDA tensor with the trailing
+    updates on the tensor cores (split GEMM); ipiv/info int32 CUDA tensors."""
+    pa, m, n, lda = _colmajor(A)
+    _check(lib().flens_gb300_dgetrf_split(m, n, pa, lda, ipiv.data_ptr(), info.data_ptr(), outer_nb,
+                                          _stream(stream)), "flens_gb300_dgetrf_split")
     return A
 
 

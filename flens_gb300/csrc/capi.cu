@@ -1182,6 +1182,17 @@ FG_API int flens_gb300_dgetrf(int m, int n, double *A, int ldA, int *ipiv, int *
     return dgetrf_launch(m, n, A, ldA, ipiv, info, as_stream(stream));
 }
 
+// FP64-accurate LU with the trailing updates beyond each outer block on the
+// tensor cores (split GEMM).  Argument positions as flens_gb300_dgetrf, outer_nb 7.
+FG_API int flens_gb300_dgetrf_split(int m, int n, double *A, int ldA, int *ipiv, int *info,
+                                    int outer_nb, void *stream) {
+    if (m < 0) return -1;
+    if (n < 0) return -2;
+    if (ldA < std::max(1, m)) return -4;
+    if (outer_nb < 0 || outer_nb % 64 != 0) return -7;
+    return dgetrf_split_launch(m, n, A, ldA, ipiv, info, outer_nb, as_stream(stream));
+}
+
 FG_API int flens_gb300_dgetrs(char trans, int n, int nrhs, const double *A, int ldA,
                               const int *ipiv, double *B, int ldB, void *stream) {
     trans = (char)toupper(trans);

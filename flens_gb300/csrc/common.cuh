@@ -249,6 +249,24 @@ int strsm_launch(char side, char upLo, char transA, char diag, int m, int n,
 
 int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info,
                   cudaStream_t stream);
+// FP64-accurate LU whose trailing updates beyond each outer block of
+// `outer_nb` columns (a multiple of 64; <= 0: the default) run through the
+// split GEMM; panels, interchanges, solves and the updates inside an outer
+// block stay FP64.
+int dgetrf_split_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, int outer_nb,
+                        cudaStream_t stream);
+
+// FP64-accurate GEMM from exact BF16 products of exponent-aligned slices
+// (split_gemm.cu); the _at form keeps its slot-0 data at byte offset
+// ws0_off (split_ws0_bytes(m, n) bytes).
+int dgemm_split_launch(char transA, char transB, int m, int n, int k, double alpha,
+                       const double *A, int ldA, const double *B, int ldB, double beta,
+                       double *C, int ldC, int slices, int *slices_used, cudaStream_t s);
+int dgemm_split_launch_at(char transA, char transB, int m, int n, int k, double alpha,
+                          const double *A, int ldA, const double *B, int ldB, double beta,
+                          double *C, int ldC, int slices, int *slices_used, size_t ws0_off,
+                          cudaStream_t s);
+size_t split_ws0_bytes(int m, int n);
 
 int dgetrs_launch(char trans, int n, int nrhs, const double *A, int ldA,
                   const int *ipiv, double *B, int ldB, cudaStream_t stream);

@@ -477,6 +477,34 @@ int gemm_tt<float>(char ta, char tb, int m, int n, int k, float alpha, const flo
     return sgemm_launch(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, s);
 }
 
+// A22 -= L21 * U12 through the split GEMM (FP64 storage only).
+template <typename T>
+int split_update(int m, int n, int k, const T *L21, int ldL, const T *U12, int ldU, T *A22, int ldA22,
+                 size_t ws0_off, cudaStream_t s);
+template <>
+int split_update<double>(int m, int n, int k, const double *L21, int ldL, const double *U12, int ldU,
+                         double *A22, int ldA22, size_t ws0_off, cudaStream_t s) {
+    return dgemm_split_launch_at('N', 'N', m, n, k, -1.0, L21, ldL, U12, ldU, 1.0, A22, ldA22, 0,
+                                 nullptr, ws0_off, s);
+}
+template <>
+int split_update<float>(int, int, int, const float *, int, const float *, int, float *, int, size_t,
+                        cudaStream_t) {
+    set_last_error("split trailing update needs FP64 storage");
+    return kErrUnsupported;
+}
+
+// Outer block of the split-update LU: FLENS_GB300_SPLIT_NB (a multiple of 64),
+// else 512.
+int split_outer_nb() {
+    static int nb = [] {
+        const char *e = getenv("FLENS_GB300_SPLIT_NB");
+        const int v = e ? atoi(e) : 0;
+        return (v >= 64 && v % 64 == 0) ? v : 512;
+    }();
+    return nb;
+}
+
 }  // namespace
 
 template <typename T>
@@ -554,12 +582,25 @@ size_t getrf_workspace_bytes(int m, int n, int tc_kind) {
 // solve always run here; the trailing update A22 -= A21*U12 runs in T on the
 // CUDA cores (tc_kind < 0) or, for T = float, on the tensor cores in the
 // precision `tc_kind` (see tc_gemm.cu).
+//
+// split_nb > 0 (T = double): two-level blocking.  The 64-column steps of an
+// outer block of split_nb columns update only the columns of that block
+// (their interchanges still reach every column); when the block is done,
+// U12 = L11^-1 A12 for all columns to its right (FP64 trsm) and
+// A22 -= L21 U12 with depth split_nb through the split GEMM.  This is the
+// order of LAPACK's dgetrf with a recursive panel; in exact arithmetic the
+// factors and pivots are those of the right-looking loop.
 template <typename T>
-int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, cudaStream_t stream) {
+int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int split_nb,
+            cudaStream_t stream) {
     FG_CUDA(cudaMemsetAsync(info, 0, sizeof(int), stream));
     if (m == 0 || n == 0) return kOk;
     const int mn = m < n ? m : n;
-    Workspace *w = workspace_for(stream, getrf_workspace_bytes(m, n, tc_kind));
+    const size_t ws0 = getrf_workspace_bytes(m, n, tc_kind);
+    // the split GEMM's slot-0 data goes after ours; sized for the largest
+    // update now so that slot 0 never moves under the panel scratch
+    const size_t split_off = (ws0 + 255) / 256 * 256;
+    Workspace *w = workspace_for(stream, split_nb > 0 ? split_off + split_ws0_bytes(m, n) : ws0);
     if (!w) return kErrAlloc;
     PanelScratch ps = carve_panel_scratch(w->buf);
     void *tc_buf = (char *)w->buf + (panel_scratch_bytes() + 255) / 256 * 256;
@@ -580,6 +621,9 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, cuda
     trace("getrf<%d> m=%d n=%d lda=%d panel grid<=%d update=%d", (int)sizeof(T), m, n, ldA, gcap,
           tc_kind);
 
+    // columns [ob_start, ob_end) are updated by the 64-column steps
+    int ob_start = 0;
+    int ob_end = (split_nb > 0 && split_nb < mn) ? split_nb : n;
     for (int j = 0; j < mn;) {
         const int mp = m - j;
         int R = ceil_div(mp, gcap);
@@ -592,7 +636,8 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, cuda
             set_last_error("getrf: m=%d too tall for the shared-memory panel", m);
             return kErrUnsupported;
         }
-        const int jb = (mn - j) < nb ? (mn - j) : nb;
+        int jb = (mn - j) < nb ? (mn - j) : nb;
+        if (j + jb > ob_end) jb = ob_end - j;
         const int G = ceil_div(mp, R);
         T *Ap = A + j + (size_t)j * ldA;
         int *status = w->status;
@@ -616,8 +661,9 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, cuda
                                                               ps.swap_dst, ps.swap_src);
             FG_CUDA(cudaGetLastError());
         }
-        if (j + jb < n) {
-            int st = trsm_t<T>('L', 'L', 'N', 'U', jb, n - j - jb, T(1), Ap, ldA,
+        if (j + jb < ob_end) {
+            const int nr = ob_end - j - jb;
+            int st = trsm_t<T>('L', 'L', 'N', 'U', jb, nr, T(1), Ap, ldA,
                                A + j + (size_t)(j + jb) * ldA, ldA, stream);
             if (st != kOk) return st;
             if (j + jb < m) {
@@ -625,27 +671,53 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, cuda
                 T *U12 = A + j + (size_t)(j + jb) * ldA;
                 T *A22 = A + (j + jb) + (size_t)(j + jb) * ldA;
                 if (tc_kind >= 0)
-                    st = tc_trailing_update(tc_kind, m - j - jb, n - j - jb, jb, (const float *)A21,
+                    st = tc_trailing_update(tc_kind, m - j - jb, nr, jb, (const float *)A21,
                                             ldA, (const float *)U12, ldA, (float *)A22, ldA, tc_buf,
                                             stream);
                 else
-                    st = gemm_tt<T>('N', 'N', m - j - jb, n - j - jb, jb, T(-1), A21, ldA, U12, ldA,
+                    st = gemm_tt<T>('N', 'N', m - j - jb, nr, jb, T(-1), A21, ldA, U12, ldA,
                                     T(1), A22, ldA, stream);
                 if (st != kOk) return st;
             }
         }
         j += jb;
+        if (j == ob_end && ob_end < n) {
+            // outer block [ob_start, ob_end) done: its U12 and the trailing
+            // update of everything to the right
+            const int kb = ob_end - ob_start, nr = n - ob_end;
+            int st = trsm_t<T>('L', 'L', 'N', 'U', kb, nr, T(1), A + ob_start + (size_t)ob_start * ldA,
+                               ldA, A + ob_start + (size_t)ob_end * ldA, ldA, stream);
+            if (st != kOk) return st;
+            if (ob_end < m) {
+                st = split_update(m - ob_end, nr, kb, A + ob_end + (size_t)ob_start * ldA, ldA,
+                                  A + ob_start + (size_t)ob_end * ldA, ldA,
+                                  A + ob_end + (size_t)ob_end * ldA, ldA, split_off, stream);
+                if (st != kOk) return st;
+            }
+            ob_start = ob_end;
+            ob_end = (ob_start + split_nb < mn) ? ob_start + split_nb : n;
+        }
     }
     return kOk;
 }
 
 int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, cudaStream_t stream) {
-    return getrf_t<double>(m, n, A, ldA, ipiv, info, -1, stream);
+    return getrf_t<double>(m, n, A, ldA, ipiv, info, -1, 0, stream);
+}
+
+int dgetrf_split_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, int outer_nb,
+                        cudaStream_t stream) {
+    if (outer_nb <= 0) outer_nb = split_outer_nb();
+    if (outer_nb % PANEL_NB != 0) {
+        set_last_error("dgetrf_split: outer block %d is not a multiple of %d", outer_nb, PANEL_NB);
+        return kErrUnsupported;
+    }
+    return getrf_t<double>(m, n, A, ldA, ipiv, info, -1, outer_nb, stream);
 }
 
 int sgetrf_launch(int m, int n, float *A, int ldA, int *ipiv, int *info, int tc_kind,
                   cudaStream_t stream) {
-    return getrf_t<float>(m, n, A, ldA, ipiv, info, tc_kind, stream);
+    return getrf_t<float>(m, n, A, ldA, ipiv, info, tc_kind, 0, stream);
 }
 
 template <typename T>

@@ -21,6 +21,12 @@
 //      mode a stall above the tolerance switches the column to GMRES-IR.
 // The row interchanges of the LU are turned into one permutation after the
 // factorisation and applied inside the FP64 -> FP32 conversion of each solve.
+//
+// Precision 4 (split) keeps FP64 storage and makes the LU itself FP64-accurate
+// on the tensor cores: dgetrf_split_launch runs the trailing updates beyond
+// each outer block through the split GEMM (exact BF16 products of
+// exponent-aligned slices).  Its solves are FP64 triangular solves, so the
+// refinement converges in one or two steps at any kappa*u64 < 1.
 #include "common.cuh"
 
 #include <math.h>
@@ -66,6 +72,30 @@ __global__ void s2d_cols_kernel(int n, int ncols, const float *__restrict__ D, i
         const double v = s * (double)D[i + j * ldd];
         if (ADD) X[i + j * ldx] += v;
         else X[i + j * ldx] = v;
+    }
+}
+
+// D(:, j) = X(perm, j)
+__global__ void gather_cols_kernel(int n, int ncols, const double *__restrict__ X, int ldx,
+                                   const int *__restrict__ perm, double *__restrict__ D, int ldd) {
+    const size_t total = (size_t)n * ncols;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const size_t j = e / n, i = e % n;
+        D[i + j * ldd] = X[(size_t)perm[i] + j * ldx];
+    }
+}
+
+// X(:, j) (+)= D(:, j)
+template <bool ADD>
+__global__ void put_cols_kernel(int n, int ncols, const double *__restrict__ D, int ldd,
+                                double *__restrict__ X, int ldx) {
+    const size_t total = (size_t)n * ncols;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const size_t j = e / n, i = e % n;
+        if (ADD) X[i + j * ldx] += D[i + j * ldd];
+        else X[i + j * ldx] = D[i + j * ldd];
     }
 }
 
@@ -177,6 +207,7 @@ int grid_for(size_t total) {
 size_t a256(size_t b) { return (b + 255) / 256 * 256; }
 
 constexpr int kGmresM = 100;      // restart length
+constexpr int kPrecSplit = 4;     // FP64 storage, split-GEMM trailing updates
 
 struct Solver {
     int n = 0, nrhs = 0;
@@ -200,7 +231,9 @@ struct Solver {
     double *V = nullptr;        // n x (M+1) Krylov basis (GMRES)
     double *w = nullptr;        // n
     double *t = nullptr;        // n
-    double *LU64 = nullptr;     // FP64 copy of the FP32 factors (GMRES preconditioner)
+    double *LU64 = nullptr;     // FP64 copy of the FP32 factors (GMRES preconditioner),
+                                // or the FP64 factors themselves (split)
+    double *D64 = nullptr;      // n x nrhs fp64 work (split)
     double *h = nullptr;        // M+2 coefficients
     double *h2 = nullptr;       // M+2 (second Gram-Schmidt pass)
     double anorm = 0.0;
@@ -211,6 +244,25 @@ struct Solver {
 // `scale` (device, ncols); out may alias X.
 int lu_solve(Solver &S, int ncols, const double *X, int ldx, const double *scale, double *out,
              int ldo, bool add) {
+    if (S.precision == kPrecSplit) {
+        // FP64 factors: P, L^-1, U^-1 in FP64 (no scaling needed)
+        KTimer kt(kFamRefine, S.s, 2.0 * S.n * (double)S.n * ncols, 8.0 * S.n * (double)S.n);
+        gather_cols_kernel<<<grid_for((size_t)S.n * ncols), 256, 0, S.s>>>(S.n, ncols, X, ldx, S.perm,
+                                                                           S.D64, S.n);
+        FG_CUDA(cudaGetLastError());
+        int st = dtrsm_launch('L', 'L', 'N', 'U', S.n, ncols, 1.0, S.LU64, S.n, S.D64, S.n, S.s);
+        if (st != kOk) return st;
+        st = dtrsm_launch('L', 'U', 'N', 'N', S.n, ncols, 1.0, S.LU64, S.n, S.D64, S.n, S.s);
+        if (st != kOk) return st;
+        if (add)
+            put_cols_kernel<true><<<grid_for((size_t)S.n * ncols), 256, 0, S.s>>>(S.n, ncols, S.D64,
+                                                                                  S.n, out, ldo);
+        else
+            put_cols_kernel<false><<<grid_for((size_t)S.n * ncols), 256, 0, S.s>>>(S.n, ncols, S.D64,
+                                                                                   S.n, out, ldo);
+        FG_CUDA(cudaGetLastError());
+        return kOk;
+    }
     KTimer kt(kFamRefine, S.s, 2.0 * S.n * (double)S.n * ncols, 4.0 * S.n * (double)S.n);
     d2s_cols_kernel<<<grid_for((size_t)S.n * ncols), 256, 0, S.s>>>(S.n, ncols, X, ldx, S.perm,
                                                                       scale, S.D32, S.n);
@@ -386,26 +438,35 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
     if (!(tol > 0.0)) tol = (double)n * eps;
 
     // slot 1: A32 | ipiv | perm | info | R | D32 | colv | anorm | h | h2
+    // split: slot 3: LU64 | ipiv | perm | info | R | D64 | colv | anorm | h | h2
+    // (slots 0-2 belong to the split GEMM while the LU runs)
+    const bool split = precision == kPrecSplit;
     const int M = kGmresM;
     size_t off = 0;
-    const size_t oA32 = off; off += a256((size_t)S.ld32 * n * sizeof(float));
+    const size_t oA32 = off;
+    off += split ? a256((size_t)n * n * sizeof(double)) : a256((size_t)S.ld32 * n * sizeof(float));
     const size_t oPiv = off; off += a256((size_t)n * sizeof(int));
     const size_t oPerm = off; off += a256((size_t)n * sizeof(int));
     const size_t oInfo = off; off += 256;
     const size_t oR = off; off += a256((size_t)n * nrhs * sizeof(double));
-    const size_t oD = off; off += a256((size_t)n * nrhs * sizeof(float));
+    const size_t oD = off; off += a256((size_t)n * nrhs * (split ? sizeof(double) : sizeof(float)));
     const size_t oCol = off; off += a256((size_t)(4 * nrhs + 4) * sizeof(double));
     const size_t oAn = off; off += 256;
     const size_t oH = off; off += a256((size_t)(M + 2) * sizeof(double));
     const size_t oH2 = off; off += a256((size_t)(M + 2) * sizeof(double));
-    char *p = (char *)workspace_slot(s, 1, off);
+    char *p = (char *)workspace_slot(s, split ? 3 : 1, off);
     if (!p) return kErrAlloc;
-    S.A32 = (float *)(p + oA32);
+    if (split) {
+        S.LU64 = (double *)(p + oA32);
+        S.D64 = (double *)(p + oD);
+    } else {
+        S.A32 = (float *)(p + oA32);
+        S.D32 = (float *)(p + oD);
+    }
     S.ipiv = (int *)(p + oPiv);
     S.perm = (int *)(p + oPerm);
     S.dinfo = (int *)(p + oInfo);
     S.R = (double *)(p + oR);
-    S.D32 = (float *)(p + oD);
     S.colv = (double *)(p + oCol);
     S.anorm_bits = (unsigned long long *)(p + oAn);
     S.h = (double *)(p + oH);
@@ -414,14 +475,18 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
     // 1. FP32 copy, norms, LU
     {
         KTimer kt(kFamAux, s, 0.0, 12.0 * n * (double)n);
-        d2s_cols_kernel<<<grid_for((size_t)n * n), 256, 0, s>>>(n, n, A, ldA, nullptr, nullptr, S.A32,
-                                                                S.ld32);
+        if (split)
+            copy_cols_kernel<<<grid_for((size_t)n * n), 256, 0, s>>>(n, n, A, ldA, S.LU64, n);
+        else
+            d2s_cols_kernel<<<grid_for((size_t)n * n), 256, 0, s>>>(n, n, A, ldA, nullptr, nullptr,
+                                                                    S.A32, S.ld32);
         FG_CUDA(cudaMemsetAsync(S.anorm_bits, 0, sizeof(unsigned long long), s));
         inf_norm_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, A, ldA, S.anorm_bits);
         col_absmax_kernel<<<nrhs, 256, 0, s>>>(n, B, ldB, S.colv + 2 * nrhs);
         FG_CUDA(cudaGetLastError());
     }
-    int st = sgetrf_launch(n, n, S.A32, S.ld32, S.ipiv, S.dinfo, precision, s);
+    int st = split ? dgetrf_split_launch(n, n, S.LU64, n, S.ipiv, S.dinfo, 0, s)
+                   : sgetrf_launch(n, n, S.A32, S.ld32, S.ipiv, S.dinfo, precision, s);
     if (st != kOk) return st;
     if ((st = laswp_perm_launch(n, S.ipiv, S.perm, s)) != kOk) return st;
     int hinfo = 0;
@@ -494,11 +559,14 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
                 S.V = (double *)p2;
                 S.w = (double *)(p2 + vB);
                 S.t = (double *)(p2 + vB + nB);
-                S.LU64 = (double *)workspace_slot(s, 3, (size_t)n * n * sizeof(double));
-                if (!S.LU64) return kErrAlloc;
-                KTimer kt(kFamAux, s, 0.0, 12.0 * n * (double)n);
-                s2d_matrix_kernel<<<grid_for((size_t)n * n), 256, 0, s>>>(n, S.A32, S.ld32, S.LU64, n);
-                FG_CUDA(cudaGetLastError());
+                if (!split) {
+                    S.LU64 = (double *)workspace_slot(s, 3, (size_t)n * n * sizeof(double));
+                    if (!S.LU64) return kErrAlloc;
+                    KTimer kt(kFamAux, s, 0.0, 12.0 * n * (double)n);
+                    s2d_matrix_kernel<<<grid_for((size_t)n * n), 256, 0, s>>>(n, S.A32, S.ld32, S.LU64,
+                                                                            n);
+                    FG_CUDA(cudaGetLastError());
+                }
             }
             for (int j : gmres) {
                 int steps = 0;
@@ -534,7 +602,7 @@ FG_API int flens_gb300_dgesv_mixed(int n, int nrhs, const double *A, int ldA, co
     if (ldA < (n > 1 ? n : 1)) return -4;
     if (ldB < (n > 1 ? n : 1)) return -6;
     if (ldX < (n > 1 ? n : 1)) return -8;
-    if (precision < 0 || precision > 3) return -9;
+    if (precision < 0 || precision > 4) return -9;
     if (solver < 0 || solver > 2) return -10;
     int it = 0, inf = 0;
     double be = 0.0;

@@ -390,9 +390,17 @@ static SplitGeom split_geometry(int bits, int S, int k) {
     return g;
 }
 
-int dgemm_split_launch(char transA, char transB, int m, int n, int k, double alpha, const double *A,
-                       int ldA, const double *B, int ldB, double beta, double *C, int ldC,
-                       int slices, int *slices_used, cudaStream_t s) {
+// Bytes of slot-0 workspace the split GEMM uses for an m x n product: the
+// statistics and the per-row / per-column exponents.
+size_t split_ws0_bytes(int m, int n) {
+    return 256 + round256((size_t)m * sizeof(int)) + round256((size_t)n * sizeof(int));
+}
+
+// The split GEMM with its slot-0 data at byte offset ws0_off (callers that
+// keep their own data at the start of slot 0, the blocked LU, pass its size).
+int dgemm_split_launch_at(char transA, char transB, int m, int n, int k, double alpha,
+                          const double *A, int ldA, const double *B, int ldB, double beta, double *C,
+                          int ldC, int slices, int *slices_used, size_t ws0_off, cudaStream_t s) {
     if (slices_used) *slices_used = 0;
     if (m == 0 || n == 0) return kOk;
     if (k == 0 || alpha == 0.0) return dscal_matrix_launch(m, n, beta, C, ldC, s);
@@ -402,9 +410,9 @@ int dgemm_split_launch(char transA, char transB, int m, int n, int k, double alp
 
     // 1. exponents and slice-count statistics (slot 0: small)
     const size_t off_ea = 256, off_eb = off_ea + round256((size_t)m * sizeof(int));
-    Workspace *w = workspace_for(s, off_eb + round256((size_t)n * sizeof(int)));
+    Workspace *w = workspace_for(s, ws0_off + split_ws0_bytes(m, n));
     if (!w) return kErrAlloc;
-    char *ws = (char *)w->buf;
+    char *ws = (char *)w->buf + ws0_off;
     SplitStats *st = (SplitStats *)ws;
     int *ea = (int *)(ws + off_ea), *eb = (int *)(ws + off_eb);
     {
@@ -483,6 +491,13 @@ int dgemm_split_launch(char transA, char transB, int m, int n, int k, double alp
     trace("dgemm_split: m=%d n=%d k=%d bits=%d S=%d groups=%d", m, n, k, bits, S, geo.ngroups);
     if (slices_used) *slices_used = S;
     return kOk;
+}
+
+int dgemm_split_launch(char transA, char transB, int m, int n, int k, double alpha, const double *A,
+                       int ldA, const double *B, int ldB, double beta, double *C, int ldC,
+                       int slices, int *slices_used, cudaStream_t s) {
+    return dgemm_split_launch_at(transA, transB, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, slices,
+                                 slices_used, 0, s);
 }
 
 }  // namespace fg

@@ -209,6 +209,18 @@ int flens_gb300_dtrsm(char side, char uplo, char transA, char diag, int m,
 int flens_gb300_dgetrf(int m, int n, double *A, int ldA, int *ipiv, int *info,
                        void *stream);
 
+/* Precision form of dgetrf on device memory: the same factorisation (FP64
+ * storage, FP64 panels with the reference's pivot rule, FP64 interchanges and
+ * triangular solves) with the trailing update beyond each outer block of
+ * outer_nb columns (a multiple of 64; 0 = 512) computed by the split GEMM
+ * (flens_gb300_dgemm_split) on the BF16 tensor cores.  The factors are
+ * FP64-accurate, not bitwise those of flens_gb300_dgetrf; pivots can differ
+ * where two candidates are within rounding of each other.  Synchronises on
+ * stream once per outer block (the split GEMM's statistics).  Returns
+ * -7 for a bad outer_nb. */
+int flens_gb300_dgetrf_split(int m, int n, double *A, int ldA, int *ipiv,
+                             int *info, int outer_nb, void *stream);
+
 /* dgetrs on device memory (ipiv device, 1-based).  Async on stream. */
 int flens_gb300_dgetrs(char trans, int n, int nrhs, const double *A, int ldA,
                        const int *ipiv, double *B, int ldB, void *stream);
@@ -315,7 +327,10 @@ int flens_gb300_dgemm_split(char transA, char transB, int m, int n, int k,
 
 /* Solve A X = B (device, column-major FP64; A and B untouched) to FP64
  * accuracy from an LU in FP32 storage whose trailing updates run on the
- * tensor cores in `precision` (as above), refined in FP64: solver 0 =
+ * tensor cores in `precision` (as above), or, for precision 4, from the
+ * FP64-accurate flens_gb300_dgetrf_split factors (FP64 storage and solves;
+ * for systems too ill-conditioned for FP32 factors, kappa*u32 >> 1),
+ * refined in FP64: solver 0 =
  * classical refinement (stops like the reference's rfs,
  * flens/lapack/ge/rfs.tcc:182-188), 1 = GMRES-IR, 2 = classical switching to
  * GMRES-IR per column when the backward error stops halving.  Stops when the

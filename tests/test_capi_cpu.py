@@ -281,6 +281,11 @@ def test_device_api_argument_errors(flib):
     assert flib.flens_gb300_dgetrf(-1, 1, None, 1, None, None, None) == -1
     assert flib.flens_gb300_dgetrf(3, 1, None, 2, None, None, None) == -4
     assert flib.flens_gb300_dgetrs(b"N", 3, 1, None, 3, None, None, 2, None) == -8
+    assert flib.flens_gb300_dgetrf_split(-1, 4, None, 4, None, None, 0, None) == -1
+    assert flib.flens_gb300_dgetrf_split(4, -1, None, 4, None, None, 0, None) == -2
+    assert flib.flens_gb300_dgetrf_split(4, 4, None, 3, None, None, 0, None) == -4
+    assert flib.flens_gb300_dgetrf_split(4, 4, None, 4, None, None, 100, None) == -7
+    assert flib.flens_gb300_dgetrf_split(4, 4, None, 4, None, None, -64, None) == -7
 
 
 def test_no_gpu_fails_loudly():

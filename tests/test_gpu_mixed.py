@@ -19,7 +19,7 @@ import flens_gb300 as fg
 pytestmark = pytest.mark.gpu
 
 EPS = np.finfo(np.float64).eps
-PREC = {"tf32": 0, "bf16": 1, "fp8": 2, "fp32": 3}
+PREC = {"tf32": 0, "bf16": 1, "fp8": 2, "fp32": 3, "split": 4}
 SOLVER = {"classical": 0, "gmres": 1, "auto": 2}
 
 
