@@ -57,6 +57,10 @@ struct Workspace {
     size_t slot_bytes[4] = {0, 0, 0, 0};
     int *status = nullptr;       // device status word (DeviceStatus bits)
     int *info = nullptr;         // device INFO for host-pointer entry points
+    // look-ahead: a high-priority side stream and two events that order it
+    // against `stream` (created on first use)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fwd = nullptr, ev_back = nullptr;
 };
 
 // Returns the workspace bound to `stream` on the current device with at least
@@ -66,6 +70,10 @@ Workspace *workspace_for(cudaStream_t stream, size_t bytes);
 // Independent buffers 1..3 of the same workspace, for callers that hold
 // pointers while calling routines that may grow slot 0.
 void *workspace_slot(cudaStream_t stream, int slot, size_t bytes);
+
+// The side stream and events of the workspace bound to `stream` (created
+// on first use; nullptr on failure, last error set).
+Workspace *workspace_side(cudaStream_t stream);
 
 int num_sms();                 // SM count of the current device
 int device_id();               // current device ordinal

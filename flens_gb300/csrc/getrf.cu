@@ -33,7 +33,9 @@
 
 #include <float.h>
 #include <limits.h>
+#include <stdlib.h>
 
+#include <algorithm>
 #include <mutex>
 
 namespace fg {
@@ -50,7 +52,7 @@ constexpr size_t PANEL_SMEM_MAX = 200 * 1024;
 // row jj, that row; `seq` is written last with release semantics.
 struct PanelSlot {
     unsigned long long seq;
-    double val;
+    unsigned long long key;    // pivot key of the candidate (see pivot_key)
     int idx;
     int pad;
     double row[PANEL_NB];
@@ -90,61 +92,60 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
     return v;
 }
 
-// (key, row) "better than": larger key; on equal keys the smaller row, which
-// is cxxblas iamax's first-maximum rule (cxxblas/level1/iamax.tcc:52-56).
-__device__ __forceinline__ bool better(double v1, int i1, double v2, int i2) {
-    return v1 > v2 || (v1 == v2 && i1 < i2);
+// Pivot keys are integers, so the pivot search never touches the FP64 pipe
+// (2 instructions per clock per SM on this part): |x| of a double orders
+// like its bit pattern with the sign cleared.  0 = no candidate, 1 = NaN
+// (loses to every number: iamax's `>` is false for NaN), |x| bits + 2
+// otherwise.  (key, row) "better than": larger key; on equal keys the
+// smaller row, which is cxxblas iamax's first-maximum rule
+// (cxxblas/level1/iamax.tcc:52-56).
+constexpr unsigned long long kKeyNone = 0ull;
+
+__device__ __forceinline__ unsigned long long pivot_key(double x) {
+    const unsigned long long a = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+    return a > 0x7ff0000000000000ull ? 1ull : a + 2ull;
 }
 
-// Block-wide argmax of (key, row).  All threads get the result.
-__device__ __forceinline__ void block_argmax(double &v, int &i, double *red_v, int *red_i) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const double ov = __shfl_down_sync(0xffffffffu, v, off);
-        const int oi = __shfl_down_sync(0xffffffffu, i, off);
-        if (better(ov, oi, v, i)) { v = ov; i = oi; }
-    }
-    if (lane == 0) { red_v[warp] = v; red_i[warp] = i; }
-    __syncthreads();
-    if (warp == 0) {
-        const int nw = blockDim.x >> 5;
-        v = lane < nw ? red_v[lane] : -3.0;
-        i = lane < nw ? red_i[lane] : INT_MAX;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const double ov = __shfl_down_sync(0xffffffffu, v, off);
-            const int oi = __shfl_down_sync(0xffffffffu, i, off);
-            if (better(ov, oi, v, i)) { v = ov; i = oi; }
-        }
-        if (lane == 0) { red_v[0] = v; red_i[0] = i; }
-    }
-    __syncthreads();
-    v = red_v[0];
-    i = red_i[0];
-    __syncthreads();
+__device__ __forceinline__ bool better(unsigned long long k1, int i1, unsigned long long k2, int i2) {
+    return k1 > k2 || (k1 == k2 && i1 < i2);
+}
+
+// Warp-wide argmax of (key, row) with three redux.sync: the largest high
+// word, then the largest low word among those lanes, then the smallest row
+// among the lanes holding that key.  Every lane gets the result; all 32
+// lanes must call it.
+__device__ __forceinline__ void warp_argmax(unsigned long long &k, int &i) {
+    const unsigned hi = (unsigned)(k >> 32), lo = (unsigned)k;
+    const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+    const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
+    const unsigned cand = (hi == mhi && lo == mlo) ? (unsigned)i : 0xffffffffu;
+    i = (int)__reduce_min_sync(0xffffffffu, cand);
+    k = ((unsigned long long)mhi << 32) | mlo;
 }
 
 // Panel factorisation, tf2 semantics (flens/lapack/ge/tf2.tcc:56-136).
 // A points at the panel's top-left element A(j,j); the panel is mp x jb.
 // CTA b owns panel rows [b*R, min(mp,(b+1)*R)), kept in shared memory as
-// S[c*R + r].
+// S[c*R + r]; thread t owns local rows t, t+256, ... for the whole panel:
+// it swaps, scales and updates them and keeps their pivot keys, so a column
+// needs two block barriers: one to collect the warps' candidates, one to
+// hand the pivot to every thread.  Warp 0 does the cross-CTA exchange.
 template <typename T>
 __global__ void __launch_bounds__(PANEL_THREADS)
 panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
              int *__restrict__ ipiv, int *__restrict__ info, int *__restrict__ status,
              PanelScratch ps, int R, unsigned long long epoch) {
     extern __shared__ double S[];
+    constexpr int NW = PANEL_THREADS / 32;
     __shared__ double prow[PANEL_NB], orow[PANEL_NB];
-    __shared__ double red_v[2][PANEL_THREADS / 32];
-    __shared__ int red_i[2][PANEL_THREADS / 32];
+    __shared__ unsigned long long red_k[NW], red_k2[NW];
+    __shared__ int red_i[NW], red_i2[NW];
     __shared__ int s_gs, s_abort;
     __shared__ double s_pv, s_rinv;
     __shared__ int s_list_row[2 * PANEL_NB], s_list_src[2 * PANEL_NB];
 
     const int b = blockIdx.x, G = gridDim.x, tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
-    constexpr int NW = PANEL_THREADS / 32;
     const int rb = b * R;
     const int re = min(mp, rb + R);
     const int nr = max(0, re - rb);
@@ -156,60 +157,48 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
     if (tid == 0) s_abort = 0;
     __syncthreads();
 
-    // Each thread owns rows r = tid, tid+256, ... of this CTA's block for the
-    // whole panel: it computes their pivot keys, swaps, scales and updates
-    // them, so only cross-row exchanges need a barrier.
-    // pivot keys of column 0 (later columns: computed during the update)
-    double nbv = -2.0;
+    // pivot keys of column 0 over the owned rows (later columns: computed
+    // during the update)
+    unsigned long long nbk = kKeyNone;
     int nbi = INT_MAX;
     for (int r = tid; r < nr; r += PANEL_THREADS) {
-        const double a = fabs(S[r]);
-        const double key = isnan(a) ? -1.0 : a;
-        if (better(key, rb + r, nbv, nbi)) { nbv = key; nbi = rb + r; }
+        const unsigned long long key = pivot_key(S[r]);
+        if (better(key, rb + r, nbk, nbi)) { nbk = key; nbi = rb + r; }
     }
 
     for (int jj = 0; jj < jb; ++jj) {
         const int par = jj & 1;
-        // -- [A] local pivot candidate among owned rows g >= jj (NaN never wins)
-        double bv = nbv;
-        int bi = nbi;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const double ov = __shfl_down_sync(0xffffffffu, bv, off);
-            const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-            if (better(ov, oi, bv, bi)) { bv = ov; bi = oi; }
-        }
-        if (lane == 0) { red_v[0][warp] = bv; red_i[0][warp] = bi; }
-        __syncthreads();                                             // B1
-        bv = red_v[0][0];
-        bi = red_i[0][0];
-#pragma unroll
-        for (int w = 1; w < NW; ++w)
-            if (better(red_v[0][w], red_i[0][w], bv, bi)) { bv = red_v[0][w]; bi = red_i[0][w]; }
-
-        // -- [B] publish the candidate (and row jj if owned) in this CTA's slot
-        PanelSlot *mine = &ps.slots[par * PANEL_GMAX + b];
-        if (bi != INT_MAX) {
-            for (int c = tid; c < jb; c += PANEL_THREADS) mine->row[c] = S[c * R + (bi - rb)];
-        }
-        if (jj >= rb && jj < re) {
-            for (int c = tid; c < jb; c += PANEL_THREADS) mine->rowjj[c] = S[c * R + (jj - rb)];
-        }
-        if (tid == 0) {
-            mine->val = bv;
-            mine->idx = bi;
-        }
-        __syncthreads();                                             // B2
         const unsigned long long want = epoch * 128ull + (unsigned long long)jj + 1ull;
-        // the release store orders this CTA's slot writes (made visible to
-        // thread 0 by the barrier) before the sequence number
-        if (tid == 0) st_release(&mine->seq, want);
-
-        // -- [C] every CTA reads every slot once its seq says step jj is published
-        double gv = -3.0;
+        // -- [A] this CTA's candidate among its rows g >= jj
+        unsigned long long k = nbk;
+        int i = nbi;
+        warp_argmax(k, i);
+        if (lane == 0) { red_k[warp] = k; red_i[warp] = i; }
+        __syncthreads();                                             // B1
+        if (warp == 0) {
+            // -- [B] publish the candidate row (and row jj if owned); the
+            // release store by lane 0 after __syncwarp orders the warp's slot
+            // writes before the sequence number
+            k = lane < NW ? red_k[lane] : kKeyNone;
+            i = lane < NW ? red_i[lane] : INT_MAX;
+            warp_argmax(k, i);
+            PanelSlot *mine = &ps.slots[par * PANEL_GMAX + b];
+            if (i != INT_MAX)
+                for (int c = lane; c < jb; c += 32) mine->row[c] = S[c * R + (i - rb)];
+            if (jj >= rb && jj < re)
+                for (int c = lane; c < jb; c += 32) mine->rowjj[c] = S[c * R + (jj - rb)];
+            if (lane == 0) {
+                mine->key = k;
+                mine->idx = i;
+            }
+            __syncwarp();
+            if (lane == 0) st_release(&mine->seq, want);
+        }
+        // -- [C] thread t < G waits for slot t of this step and reads it
+        unsigned long long gk = kKeyNone;
         int gi = INT_MAX;
-        for (int t = tid; t < G; t += PANEL_THREADS) {
-            const PanelSlot *sl = &ps.slots[par * PANEL_GMAX + t];
+        if (tid < G) {
+            const PanelSlot *sl = &ps.slots[par * PANEL_GMAX + tid];
             unsigned spins = 0;
             while (ld_acquire(&sl->seq) != want) {
                 if (++spins > kSpinLimit) {
@@ -219,56 +208,54 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
                 }
                 if (spins > 32) __nanosleep(32);
             }
-            const double v = ld_cg(&sl->val);
-            const int i = ld_cg(&sl->idx);
-            if (better(v, i, gv, gi)) { gv = v; gi = i; }
+            gk = __ldcg(&sl->key);
+            gi = __ldcg(&sl->idx);
         }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const double ov = __shfl_down_sync(0xffffffffu, gv, off);
-            const int oi = __shfl_down_sync(0xffffffffu, gi, off);
-            if (better(ov, oi, gv, gi)) { gv = ov; gi = oi; }
+        if (warp * 32 < G) {                                          // warp-uniform
+            warp_argmax(gk, gi);
+            if (lane == 0) { red_k2[warp] = gk; red_i2[warp] = gi; }
         }
-        if (lane == 0) { red_v[1][warp] = gv; red_i[1][warp] = gi; }
-        __syncthreads();                                             // B3
+        __syncthreads();                                             // B2
         if (s_abort) return;
-        gv = red_v[1][0];
-        gi = red_i[1][0];
-#pragma unroll
-        for (int w = 1; w < NW; ++w)
-            if (better(red_v[1][w], red_i[1][w], gv, gi)) { gv = red_v[1][w]; gi = red_i[1][w]; }
-
-        // -- [D] fetch the old row jj and the winner's row in one round trip;
-        // thread 0 settles the pivot (iamax starts from element jj: if it is
-        // NaN nothing compares greater and jj is the pivot,
-        // cxxblas/level1/iamax.tcc:50-57) and its reciprocal once.
-        const int ownjj = jj / R;
-        const int wb = gi / R;
-        const PanelSlot *sj = &ps.slots[par * PANEL_GMAX + ownjj];
-        const PanelSlot *sw = &ps.slots[par * PANEL_GMAX + wb];
-        for (int c = tid; c < jb; c += PANEL_THREADS) {
-            orow[c] = ld_cg(&sj->rowjj[c]);
-            prow[c] = ld_cg(&sw->row[c]);
-        }
-        if (tid == 0) {
-            const double ajj = ld_cg(&sj->rowjj[jj]);
-            const int gs = isnan(ajj) ? jj : gi;
-            const double pv = (gs == jj) ? ajj : ld_cg(&sw->row[jj]);
-            s_gs = gs;
-            s_pv = pv;
-            s_rinv = (pv != 0.0 && fabs(pv) >= DBL_MIN) ? 1.0 / pv : 0.0;
-            if (b == 0) {
-                ipiv[j0 + jj] = j0 + gs + 1;
-                if (pv == 0.0 && *info == 0) *info = j0 + jj + 1;
+        if (warp == 0) {
+            const int nw = (G + 31) / 32;
+            gk = lane < nw ? red_k2[lane] : kKeyNone;
+            gi = lane < nw ? red_i2[lane] : INT_MAX;
+            warp_argmax(gk, gi);
+            // -- [D] the old row jj and the winner's row, one round trip;
+            // lane 0 settles the pivot (iamax starts from element jj: if it
+            // is NaN nothing compares greater and jj is the pivot,
+            // cxxblas/level1/iamax.tcc:50-57) and its reciprocal once
+            const PanelSlot *sj = &ps.slots[par * PANEL_GMAX + jj / R];
+            const PanelSlot *sw = &ps.slots[par * PANEL_GMAX + gi / R];
+            for (int c = lane; c < jb; c += 32) {
+                orow[c] = ld_cg(&sj->rowjj[c]);
+                prow[c] = ld_cg(&sw->row[c]);
+            }
+            __syncwarp();
+            if (lane == 0) {
+                const double ajj = orow[jj];
+                const int gs = isnan(ajj) ? jj : gi;
+                const double pv = (gs == jj) ? ajj : prow[jj];
+                s_gs = gs;
+                s_pv = pv;
+                s_rinv = (pv != 0.0 && fabs(pv) >= DBL_MIN) ? 1.0 / pv : 0.0;
+                if (b == 0) {
+                    ipiv[j0 + jj] = j0 + gs + 1;
+                    if (pv == 0.0 && *info == 0) *info = j0 + jj + 1;
+                }
             }
         }
-        __syncthreads();                                             // B4
+        __syncthreads();                                             // B3
         const int gs = s_gs;
         const double pv = s_pv, rinv = s_rinv;
         const bool swap = (pv != 0.0) && (gs != jj);
         const double *P = (gs == jj) ? orow : prow;                  // new row jj
 
-        // -- [E1] row interchange and scaling, by the owner of each row
+        // -- [E] per owned row: interchange, scaling, rank-1 update of the
+        // columns > jj, and the pivot key for column jj+1
+        nbk = kKeyNone;
+        nbi = INT_MAX;
         for (int r = tid; r < nr; r += PANEL_THREADS) {
             const int g = rb + r;
             if (swap && g == jj) {
@@ -276,30 +263,16 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
             } else if (swap && g == gs) {
                 for (int c = 0; c < jb; ++c) S[c * R + r] = orow[c];
             }
-            if (g > jj && pv != 0.0) {
-                const double l = S[jj * R + r];
-                S[jj * R + r] = (rinv != 0.0) ? l * rinv : l / pv;
-            }
-        }
-        __syncthreads();                                             // B5
-        // -- [E2] rank-1 update of rows > jj, columns > jj, spread over all
-        // threads (rows fastest); the thread that updates (r, jj+1) also
-        // keeps the pivot key of row r for the next column
-        nbv = -2.0;
-        nbi = INT_MAX;
-        if (jj + 1 < jb) {
-            const int nc = jb - jj - 1;
-            for (int e = tid; e < nr * nc; e += PANEL_THREADS) {
-                const int r = e % nr, c = jj + 1 + e / nr;
-                const int g = rb + r;
-                if (g > jj) {
-                    const double v = fma(-P[c], S[jj * R + r], S[c * R + r]);
-                    S[c * R + r] = v;
-                    if (c == jj + 1) {
-                        const double a = fabs(v);
-                        const double key = isnan(a) ? -1.0 : a;
-                        if (better(key, g, nbv, nbi)) { nbv = key; nbi = g; }
-                    }
+            if (g > jj) {
+                double l = S[jj * R + r];
+                if (pv != 0.0) {
+                    l = (rinv != 0.0) ? l * rinv : l / pv;
+                    S[jj * R + r] = l;
+                }
+                for (int c = jj + 1; c < jb; ++c) S[c * R + r] = fma(-P[c], l, S[c * R + r]);
+                if (jj + 1 < jb) {
+                    const unsigned long long key = pivot_key(S[(jj + 1) * R + r]);
+                    if (better(key, g, nbk, nbi)) { nbk = key; nbi = g; }
                 }
             }
         }
@@ -313,7 +286,6 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
 
     // -- block 0, warp 0: the jb interchanges as (dst, src) row moves.
     if (b == 0 && tid < 32) {
-        const int lane = tid;
         for (int i = lane; i < jb; i += 32) {
             s_list_row[i] = j0 + i;
             s_list_src[i] = j0 + i;
@@ -494,6 +466,27 @@ int split_update<float>(int, int, int, const float *, int, const float *, int, f
     return kErrUnsupported;
 }
 
+// Look-ahead in the blocked LU: on unless FLENS_GB300_LOOKAHEAD=0.
+bool lookahead_enabled() {
+    static bool on = [] {
+        const char *e = getenv("FLENS_GB300_LOOKAHEAD");
+        return !(e && atoi(e) == 0);
+    }();
+    return on;
+}
+
+// CTAs of a panel grid: at most one per SM and PANEL_GMAX, or
+// FLENS_GB300_PANEL_CTAS when set (1..that bound).
+int panel_ctas(int sms) {
+    int cap = sms < PANEL_GMAX ? sms : PANEL_GMAX;
+    static int env = [] {
+        const char *e = getenv("FLENS_GB300_PANEL_CTAS");
+        return e ? atoi(e) : 0;
+    }();
+    if (env >= 1 && env < cap) cap = env;
+    return cap;
+}
+
 // Outer block of the split-update LU: FLENS_GB300_SPLIT_NB (a multiple of 64),
 // else 512.
 int split_outer_nb() {
@@ -617,15 +610,24 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int 
         set_last_error("no CUDA device");
         return kErrNoDevice;
     }
-    const int gcap = sms < PANEL_GMAX ? sms : PANEL_GMAX;
-    trace("getrf<%d> m=%d n=%d lda=%d panel grid<=%d update=%d", (int)sizeof(T), m, n, ldA, gcap,
-          tc_kind);
+    const int gcap = panel_ctas(sms);
+    // look-ahead (CUDA-core updates only: the tensor-core update is a
+    // persistent kernel that leaves no SM free for a concurrent panel)
+    Workspace *wl = nullptr;
+    if (tc_kind < 0 && lookahead_enabled()) {
+        wl = workspace_side(stream);
+        if (!wl) return kErrCuda;
+    }
+    trace("getrf<%d> m=%d n=%d lda=%d panel grid<=%d update=%d lookahead=%d", (int)sizeof(T), m, n,
+          ldA, gcap, tc_kind, wl ? 1 : 0);
 
     // columns [ob_start, ob_end) are updated by the 64-column steps
     int ob_start = 0;
     int ob_end = (split_nb > 0 && split_nb < mn) ? split_nb : n;
-    for (int j = 0; j < mn;) {
-        const int mp = m - j;
+
+    // Launches the panel at column j on stream s; *jb_out = its width.
+    auto panel_at = [&](int j, cudaStream_t s, int *jb_out) -> int {
+        int mp = m - j;
         int R = ceil_div(mp, gcap);
         if (R < PANEL_RMIN) R = PANEL_RMIN;
         // panel width: the reference's 64, narrowed only if a CTA's rows
@@ -644,61 +646,99 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int 
         int j0 = j;
         size_t smem = (size_t)R * jb * sizeof(double);
         ++epoch;
-        void *args[] = {&Ap, &ldA, (void *)&mp, (void *)&jb, &j0, &ipiv, &info, &status, &ps, &R,
-                        &epoch};
-        {
-            KTimer ktp(kFamPanel, stream, (double)mp * jb * jb - (double)jb * jb * jb / 3.0,
-                       2.0 * sizeof(T) * (double)mp * jb);
-            FG_CUDA(cudaLaunchCooperativeKernel((const void *)panel_kernel<T>, dim3(G),
-                                                dim3(PANEL_THREADS), args, smem, stream));
-        }
-        // interchanges on the columns outside the panel
-        const int ncols = n - jb;
-        if (ncols > 0) {
-            const int blocks = ceil_div(ncols, 256 / 32);
-            KTimer ktl(kFamLaswp, stream, 0.0, 0.0);
-            laswp_pairs_kernel<T><<<blocks, 256, 0, stream>>>(A, ldA, ncols, j, jb, ps.swap_cnt,
-                                                              ps.swap_dst, ps.swap_src);
-            FG_CUDA(cudaGetLastError());
-        }
-        if (j + jb < ob_end) {
-            const int nr = ob_end - j - jb;
-            int st = trsm_t<T>('L', 'L', 'N', 'U', jb, nr, T(1), Ap, ldA,
-                               A + j + (size_t)(j + jb) * ldA, ldA, stream);
-            if (st != kOk) return st;
-            if (j + jb < m) {
-                T *A21 = A + (j + jb) + (size_t)j * ldA;
-                T *U12 = A + j + (size_t)(j + jb) * ldA;
-                T *A22 = A + (j + jb) + (size_t)(j + jb) * ldA;
-                if (tc_kind >= 0)
-                    st = tc_trailing_update(tc_kind, m - j - jb, nr, jb, (const float *)A21,
-                                            ldA, (const float *)U12, ldA, (float *)A22, ldA, tc_buf,
-                                            stream);
-                else
-                    st = gemm_tt<T>('N', 'N', m - j - jb, nr, jb, T(-1), A21, ldA, U12, ldA,
-                                    T(1), A22, ldA, stream);
-                if (st != kOk) return st;
+        void *args[] = {&Ap, &ldA, &mp, &jb, &j0, &ipiv, &info, &status, &ps, &R, &epoch};
+        KTimer ktp(kFamPanel, s, (double)mp * jb * jb - (double)jb * jb * jb / 3.0,
+                   2.0 * sizeof(T) * (double)mp * jb);
+        FG_CUDA(cudaLaunchCooperativeKernel((const void *)panel_kernel<T>, dim3(G),
+                                            dim3(PANEL_THREADS), args, smem, s));
+        *jb_out = jb;
+        return kOk;
+    };
+    auto update = [&](int j, int jb, int c0, int nc) -> int {
+        // A(j+jb:m, c0:c0+nc) -= A(j+jb:m, j:j+jb) * A(j:j+jb, c0:c0+nc)
+        T *A21 = A + (j + jb) + (size_t)j * ldA;
+        T *U12 = A + j + (size_t)c0 * ldA;
+        T *A22 = A + (j + jb) + (size_t)c0 * ldA;
+        if (tc_kind >= 0)
+            return tc_trailing_update(tc_kind, m - j - jb, nc, jb, (const float *)A21, ldA,
+                                      (const float *)U12, ldA, (float *)A22, ldA, tc_buf, stream);
+        return gemm_tt<T>('N', 'N', m - j - jb, nc, jb, T(-1), A21, ldA, U12, ldA, T(1), A22, ldA,
+                          stream);
+    };
+
+    bool ahead = false;     // the panel at j was launched on the side stream
+    auto body = [&]() -> int {
+        int jb = 0, st;
+        for (int j = 0; j < mn;) {
+            if (ahead) {
+                FG_CUDA(cudaStreamWaitEvent(stream, wl->ev_back, 0));
+                ahead = false;
+            } else if ((st = panel_at(j, stream, &jb)) != kOk) {
+                return st;
+            }
+            // interchanges on the columns outside the panel
+            const int ncols = n - jb;
+            if (ncols > 0) {
+                const int blocks = ceil_div(ncols, 256 / 32);
+                KTimer ktl(kFamLaswp, stream, 0.0, 0.0);
+                laswp_pairs_kernel<T><<<blocks, 256, 0, stream>>>(A, ldA, ncols, j, jb, ps.swap_cnt,
+                                                                  ps.swap_dst, ps.swap_src);
+                FG_CUDA(cudaGetLastError());
+            }
+            int next_jb = 0;
+            if (j + jb < ob_end) {
+                const int nr = ob_end - j - jb;
+                if ((st = trsm_t<T>('L', 'L', 'N', 'U', jb, nr, T(1), A + j + (size_t)j * ldA, ldA,
+                                    A + j + (size_t)(j + jb) * ldA, ldA, stream)) != kOk)
+                    return st;
+                if (j + jb < m) {
+                    const int nx = j + jb;
+                    if (wl && nx < mn) {
+                        // the next panel's columns first, then that panel on
+                        // the side stream while the rest of the update runs
+                        const int w2 = std::min(std::min(PANEL_NB, mn - nx), nr);
+                        if ((st = update(j, jb, nx, w2)) != kOk) return st;
+                        FG_CUDA(cudaEventRecord(wl->ev_fwd, stream));
+                        FG_CUDA(cudaStreamWaitEvent(wl->side, wl->ev_fwd, 0));
+                        if ((st = panel_at(nx, wl->side, &next_jb)) != kOk) return st;
+                        FG_CUDA(cudaEventRecord(wl->ev_back, wl->side));
+                        ahead = true;
+                        if (next_jb > w2) {
+                            set_last_error("getrf: look-ahead panel wider than its update");
+                            return kErrUnsupported;
+                        }
+                        if (nr > w2 && (st = update(j, jb, nx + w2, nr - w2)) != kOk) return st;
+                    } else if ((st = update(j, jb, j + jb, nr)) != kOk) {
+                        return st;
+                    }
+                }
+            }
+            j += jb;
+            if (ahead) jb = next_jb;
+            if (j == ob_end && ob_end < n) {
+                // outer block [ob_start, ob_end) done: its U12 and the trailing
+                // update of everything to the right
+                const int kb = ob_end - ob_start, nr = n - ob_end;
+                if ((st = trsm_t<T>('L', 'L', 'N', 'U', kb, nr, T(1),
+                                    A + ob_start + (size_t)ob_start * ldA, ldA,
+                                    A + ob_start + (size_t)ob_end * ldA, ldA, stream)) != kOk)
+                    return st;
+                if (ob_end < m) {
+                    st = split_update(m - ob_end, nr, kb, A + ob_end + (size_t)ob_start * ldA, ldA,
+                                      A + ob_start + (size_t)ob_end * ldA, ldA,
+                                      A + ob_end + (size_t)ob_end * ldA, ldA, split_off, stream);
+                    if (st != kOk) return st;
+                }
+                ob_start = ob_end;
+                ob_end = (ob_start + split_nb < mn) ? ob_start + split_nb : n;
             }
         }
-        j += jb;
-        if (j == ob_end && ob_end < n) {
-            // outer block [ob_start, ob_end) done: its U12 and the trailing
-            // update of everything to the right
-            const int kb = ob_end - ob_start, nr = n - ob_end;
-            int st = trsm_t<T>('L', 'L', 'N', 'U', kb, nr, T(1), A + ob_start + (size_t)ob_start * ldA,
-                               ldA, A + ob_start + (size_t)ob_end * ldA, ldA, stream);
-            if (st != kOk) return st;
-            if (ob_end < m) {
-                st = split_update(m - ob_end, nr, kb, A + ob_end + (size_t)ob_start * ldA, ldA,
-                                  A + ob_start + (size_t)ob_end * ldA, ldA,
-                                  A + ob_end + (size_t)ob_end * ldA, ldA, split_off, stream);
-                if (st != kOk) return st;
-            }
-            ob_start = ob_end;
-            ob_end = (ob_start + split_nb < mn) ? ob_start + split_nb : n;
-        }
-    }
-    return kOk;
+        return kOk;
+    };
+    const int st = body();
+    // never leave side-stream work unjoined, also on an error path
+    if (ahead) cudaStreamWaitEvent(stream, wl->ev_back, 0);
+    return st;
 }
 
 int dgetrf_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, cudaStream_t stream) {

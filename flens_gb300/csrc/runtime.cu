@@ -85,6 +85,9 @@ struct Registry {
             for (int i = 0; i < 4; ++i)
                 if (w->slot_buf[i]) cudaFree(w->slot_buf[i]);
             if (w->status) cudaFree(w->status);
+            if (w->ev_fwd) cudaEventDestroy(w->ev_fwd);
+            if (w->ev_back) cudaEventDestroy(w->ev_back);
+            if (w->side) cudaStreamDestroy(w->side);
             delete w;
         }
         map.clear();
@@ -137,6 +140,25 @@ Workspace *workspace_for(cudaStream_t stream, size_t bytes) {
             return nullptr;
         }
         w->bytes = want;
+    }
+    return w;
+}
+
+Workspace *workspace_side(cudaStream_t stream) {
+    Workspace *w = workspace_for(stream, 0);
+    if (!w) return nullptr;
+    Registry &r = registry();
+    std::lock_guard<std::mutex> lock(r.mu);
+    if (!w->side) {
+        int least = 0, greatest = 0;
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&w->side, cudaStreamNonBlocking, greatest) != cudaSuccess ||
+            cudaEventCreateWithFlags(&w->ev_fwd, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&w->ev_back, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            set_last_error("creating the look-ahead stream failed");
+            return nullptr;
+        }
     }
     return w;
 }
