@@ -61,6 +61,11 @@ struct Workspace {
     // against `stream` (created on first use)
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fwd = nullptr, ev_back = nullptr;
+    // ready flags of the chained triangular solve (flags_cap entries, never
+    // moved once allocated) and the epoch the next call publishes
+    unsigned long long *flags = nullptr;
+    int flags_cap = 0;
+    unsigned long long flag_epoch = 0;
 };
 
 // Returns the workspace bound to `stream` on the current device with at least
@@ -74,6 +79,12 @@ void *workspace_slot(cudaStream_t stream, int slot, size_t bytes);
 // The side stream and events of the workspace bound to `stream` (created
 // on first use; nullptr on failure, last error set).
 Workspace *workspace_side(cudaStream_t stream);
+
+// The ready-flag array of the workspace bound to `stream` (at least n
+// entries; allocated once with room for 4096) and a fresh epoch for one
+// call.  Returns kOk, kErrUnsupported (n too large) or kErrAlloc.
+int workspace_flags(cudaStream_t stream, int n, unsigned long long **flags,
+                    unsigned long long *epoch);
 
 int num_sms();                 // SM count of the current device
 int device_id();               // current device ordinal

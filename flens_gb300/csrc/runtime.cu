@@ -88,6 +88,7 @@ struct Registry {
             if (w->ev_fwd) cudaEventDestroy(w->ev_fwd);
             if (w->ev_back) cudaEventDestroy(w->ev_back);
             if (w->side) cudaStreamDestroy(w->side);
+            if (w->flags) cudaFree(w->flags);
             delete w;
         }
         map.clear();
@@ -161,6 +162,34 @@ Workspace *workspace_side(cudaStream_t stream) {
         }
     }
     return w;
+}
+
+int workspace_flags(cudaStream_t stream, int n, unsigned long long **flags,
+                    unsigned long long *epoch) {
+    constexpr int kCap = 4096;
+    if (n > kCap) return kErrUnsupported;
+    Workspace *w = workspace_for(stream, 0);
+    if (!w) return kErrAlloc;
+    Registry &r = registry();
+    std::lock_guard<std::mutex> lock(r.mu);
+    if (!w->flags) {
+        if (cudaMalloc((void **)&w->flags, kCap * sizeof(unsigned long long)) != cudaSuccess) {
+            cudaGetLastError();
+            w->flags = nullptr;
+            set_last_error("cudaMalloc of the solve flags failed");
+            return kErrAlloc;
+        }
+        // epoch 0 is never published, so zeroed flags read as "not ready"
+        if (cudaMemsetAsync(w->flags, 0, kCap * sizeof(unsigned long long), stream) != cudaSuccess) {
+            cudaGetLastError();
+            set_last_error("cudaMemsetAsync of the solve flags failed");
+            return kErrCuda;
+        }
+        w->flags_cap = kCap;
+    }
+    *flags = w->flags;
+    *epoch = ++w->flag_epoch;
+    return kOk;
 }
 
 void *workspace_slot(cudaStream_t stream, int slot, size_t bytes) {

@@ -17,6 +17,8 @@
 // instead of dividing; the result agrees to rounding.
 #include "common.cuh"
 
+#include <stdlib.h>
+
 namespace fg {
 namespace {
 
@@ -26,14 +28,18 @@ constexpr int TRSM_THREADS = 256;
 constexpr int TRSM_RPT = TRSM_NB * TRSM_VPC / TRSM_THREADS;   // rows per thread (8)
 
 // Solves the kb x kb (kb <= 64) diagonal block M for 32 vectors per CTA.
-// Thread t owns vector v = t % 32 and rows g, g+8, ..., g+56 (g = t / 32)
-// of it in registers.  Column by column, the owner of row i finishes x_i
-// (times the precomputed 1/M(i,i) unless the diagonal is unit), publishes it
-// through a double-buffered shared slot, and after one barrier every thread
-// updates its rows below (lower) or above (upper) i: the cyclic row
-// assignment keeps all threads busy to the end.  The 64 x 32 tile of X is
-// staged through shared memory so that global loads and stores are coalesced
-// whichever of the row or vector index is contiguous.
+// Lane l of every warp holds vector l; warp w holds the 8 consecutive rows
+// of row block blk(w) in registers.  Column by column, the warp owning row i
+// finishes x_i (times the precomputed 1/M(i,i) unless the diagonal is unit)
+// and publishes it through a double-buffered shared slot; after one barrier
+// the warps with rows still open below (lower) or above (upper) i update
+// them.  A warp whose rows are all finished skips the step as a whole, so
+// the FP64 instructions issued are about 1.1x the triangle's FMAs (the pipe
+// issues 2 FP64 lanes per clock per SM, so this is the kernel's bound); the
+// blocks are paired {0,7}, {1,6}, {2,5}, {3,4} on the warps that share a
+// scheduler so the schedulers get equal work.  The 64 x 32 tile of X is
+// staged through shared memory so that global loads and stores are
+// coalesced whichever of the row or vector index is contiguous.
 template <typename T, bool LOWER, bool UNIT>
 __global__ void __launch_bounds__(TRSM_THREADS)
 trsm_diag_tile_kernel(int nb, const T *__restrict__ M0, long long mi, long long mp,
@@ -60,32 +66,37 @@ trsm_diag_tile_kernel(int nb, const T *__restrict__ M0, long long mi, long long 
     }
     __syncthreads();
     if (!UNIT && t < nb) rinv[t] = T(1) / Ms[t][t];
-    const int v = t % TRSM_VPC, g = t / TRSM_VPC;
+    const int v = t & 31, w = t >> 5;
+    const int r0 = 8 * (w < 4 ? w : 11 - w);        // this warp's row block
     T x[TRSM_RPT];
 #pragma unroll
-    for (int j = 0; j < TRSM_RPT; ++j) x[j] = Xs[g + 8 * j][v];
+    for (int j = 0; j < TRSM_RPT; ++j) x[j] = Xs[r0 + j][v];
     __syncthreads();
     for (int s = 0; s < nb; ++s) {
         const int i = LOWER ? s : nb - 1 - s;
-        if (g == (i & 7)) {
+        if ((i >> 3) == (r0 >> 3)) {                  // warp-uniform: owner of row i
+            // selects, not x[i & 7]: an indexed access would move x to local memory
+            const int k = i & 7;
+            T xi = x[0];
 #pragma unroll
-            for (int j = 0; j < TRSM_RPT; ++j) {
-                if (j == (i >> 3)) {
-                    if (!UNIT) x[j] *= rinv[i];
-                    xb[s & 1][v] = x[j];
-                }
-            }
+            for (int j = 1; j < TRSM_RPT; ++j) xi = (j == k) ? x[j] : xi;
+            if (!UNIT) xi *= rinv[i];
+#pragma unroll
+            for (int j = 0; j < TRSM_RPT; ++j) x[j] = (j == k) ? xi : x[j];
+            xb[s & 1][v] = xi;
         }
         __syncthreads();
-        const T xi = xb[s & 1][v];
+        if (LOWER ? (r0 + 7 > i) : (r0 < i)) {          // warp-uniform: rows still open
+            const T xi = xb[s & 1][v];
 #pragma unroll
-        for (int j = 0; j < TRSM_RPT; ++j) {
-            const int r = g + 8 * j;
-            if (LOWER ? (r > i && r < nb) : (r < i)) x[j] = fma(-Ms[i][r], xi, x[j]);
+            for (int j = 0; j < TRSM_RPT; ++j) {
+                const int r = r0 + j;
+                if (LOWER ? (r > i && r < nb) : (r < i)) x[j] = fma(-Ms[i][r], xi, x[j]);
+            }
         }
     }
 #pragma unroll
-    for (int j = 0; j < TRSM_RPT; ++j) Xs[g + 8 * j][v] = x[j];
+    for (int j = 0; j < TRSM_RPT; ++j) Xs[r0 + j][v] = x[j];
     __syncthreads();
     for (int e = t; e < TRSM_NB * TRSM_VPC; e += TRSM_THREADS) {
         int r, vv;
@@ -100,7 +111,18 @@ trsm_diag_tile_kernel(int nb, const T *__restrict__ M0, long long mi, long long 
 // finished x_i, one multiply by the precomputed 1/M(i,i) and the FMAs of the
 // rows still open -- no block barrier on the dependency chain.
 constexpr int TRSM_WARP_VECS = 8;      // warps (vectors) per CTA
-constexpr int TRSM_WARP_MAX = 32;      // use the warp kernel up to this many vectors
+
+// The warp kernel is the lower-latency choice while the tile kernel would
+// run at most one CTA per SM (each tile CTA is ~17 us of FP64 pipe time):
+// up to FLENS_GB300_TRSM_WARP_MAX vectors, default 2560.
+int trsm_warp_max() {
+    static int v = [] {
+        const char *e = getenv("FLENS_GB300_TRSM_WARP_MAX");
+        const int x = e ? atoi(e) : 0;
+        return x > 0 ? x : 2560;
+    }();
+    return v;
+}
 
 template <typename T, bool LOWER, bool UNIT>
 __global__ void __launch_bounds__(32 * TRSM_WARP_VECS)
@@ -144,11 +166,177 @@ trsm_diag_warp_kernel(int nb, const T *__restrict__ M0, long long mi, long long 
     if (r1 < nb) x[r1 * xs] = x1;
 }
 
+// ------------------------------------------------------------------------
+// Few vectors (<= 4) against a triangle of more than one block, in ONE launch:
+// CTA s solves the s-th 64-row block in solve order (the first block for a
+// lower triangle, the last for an upper one).  It applies the blocks solved
+// before it as they are published -- staging each off-diagonal block of M
+// before it waits, so the read overlaps the wait -- then solves its own
+// diagonal block with one warp per vector and publishes it (release store of
+// the call's epoch into its flag; acquire spins with an iteration limit).
+// The launch is cooperative, so every CTA is resident and no wait can depend
+// on a CTA that has not started.  This replaces the 2 x blocks launches of
+// the blocked driver for the trs solves with one right-hand side.
+constexpr int CH_NB = 64;
+constexpr int CH_MAXV = 4;
+constexpr int CH_THREADS = 256;
+
+__device__ __forceinline__ void ch_release(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ch_acquire(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+template <typename T, bool LOWER, bool UNIT>
+__global__ void __launch_bounds__(CH_THREADS)
+trsv_chain_kernel(int ka, const T *__restrict__ M0, long long mi, long long mp, T *X0, long long xs,
+                  long long vs, int nvec, unsigned long long *flags, unsigned long long epoch,
+                  int *status) {
+    __shared__ T Mb[CH_NB][CH_NB + 1];                 // Mb[p][r] = M(R0 + r, K0 + p)
+    __shared__ T xk[CH_MAXV][CH_NB];
+    __shared__ T part[CH_THREADS / CH_NB][CH_MAXV][CH_NB];
+    __shared__ T rinv[CH_NB];
+    __shared__ int s_abort;
+    const int nblk = gridDim.x, s = blockIdx.x, tid = threadIdx.x;
+    const int b = LOWER ? s : nblk - 1 - s;
+    const int R0 = b * CH_NB, kb = min(CH_NB, ka - R0);
+    const int r = tid & (CH_NB - 1), q = tid / CH_NB;    // row; 16-column quarter
+    if (tid == 0) s_abort = 0;
+    T acc[CH_MAXV];
+#pragma unroll
+    for (int v = 0; v < CH_MAXV; ++v) acc[v] = T(0);
+
+    auto stage = [&](int K0, int kk) {
+        for (int e = tid; e < CH_NB * CH_NB; e += CH_THREADS) {
+            int rr, pp;
+            if (mi == 1) { rr = e % CH_NB; pp = e / CH_NB; }
+            else { pp = e % CH_NB; rr = e / CH_NB; }
+            Mb[pp][rr] = (rr < kb && pp < kk) ? M0[(R0 + rr) * mi + (K0 + pp) * mp] : T(0);
+        }
+    };
+
+    for (int s2 = 0; s2 < s; ++s2) {
+        const int k = LOWER ? s2 : nblk - 1 - s2;
+        const int K0 = k * CH_NB, kk = min(CH_NB, ka - K0);
+        stage(K0, kk);
+        if (tid == 0) {
+            unsigned spins = 0;
+            while (ch_acquire(&flags[s2]) != epoch) {
+                if (++spins > kSpinLimit) {
+                    atomicOr(status, kDevBarrierTimeout);
+                    s_abort = 1;
+                    break;
+                }
+                if (spins > 32) __nanosleep(64);
+            }
+        }
+        __syncthreads();
+        if (s_abort) return;
+        // block k of x, final (L2 reads: an L1 line could predate the solve)
+        for (int e = tid; e < nvec * CH_NB; e += CH_THREADS) {
+            const int v = e / CH_NB, p = e % CH_NB;
+            xk[v][p] = p < kk ? __ldcg(&X0[v * vs + (K0 + p) * xs]) : T(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int v = 0; v < CH_MAXV; ++v) {
+            if (v < nvec) {
+#pragma unroll 4
+                for (int p = q * 16; p < q * 16 + 16; ++p) acc[v] = fma(Mb[p][r], xk[v][p], acc[v]);
+            }
+        }
+        __syncthreads();                                   // Mb and xk are restaged next
+    }
+#pragma unroll
+    for (int v = 0; v < CH_MAXV; ++v) part[q][v][r] = acc[v];
+    stage(R0, kb);                                          // the diagonal block
+    __syncthreads();
+    if (!UNIT && tid < kb) rinv[tid] = T(1) / Mb[tid][tid];
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
+    if (warp < nvec) {
+        const int v = warp;
+        T *x = X0 + v * vs + (long long)R0 * xs;
+        auto rhs = [&](int rr) -> T {
+            if (rr >= kb) return T(0);
+            return x[rr * xs] - ((part[0][v][rr] + part[1][v][rr]) + (part[2][v][rr] + part[3][v][rr]));
+        };
+        T x0 = rhs(lane), x1 = rhs(lane + 32);
+        for (int st = 0; st < kb; ++st) {
+            const int i = LOWER ? st : kb - 1 - st;
+            T xi = __shfl_sync(0xffffffffu, i < 32 ? x0 : x1, i & 31);
+            if (!UNIT) xi *= rinv[i];
+            if (lane == (i & 31)) {
+                if (i < 32) x0 = xi;
+                else x1 = xi;
+            }
+            const int r1 = lane + 32;
+            if (LOWER) {
+                if (lane > i && lane < kb) x0 = fma(-Mb[i][lane], xi, x0);
+                if (r1 > i && r1 < kb) x1 = fma(-Mb[i][r1], xi, x1);
+            } else {
+                if (lane < i) x0 = fma(-Mb[i][lane], xi, x0);
+                if (r1 < i) x1 = fma(-Mb[i][r1], xi, x1);
+            }
+        }
+        if (lane < kb) x[lane * xs] = x0;
+        if (lane + 32 < kb) x[(lane + 32) * xs] = x1;
+    }
+    __syncthreads();
+    if (tid == 0) ch_release(&flags[s], epoch);
+}
+
+// Returns kErrUnsupported when the chained solve does not apply (too many
+// blocks to keep resident, or more than the flag array holds).
+template <typename T>
+int launch_chain(int ka, const T *M0, long long mi, long long mp, bool lowerM, bool unit, T *X0,
+                 long long xs, long long vs, int nvec, cudaStream_t stream) {
+    const int nblk = ceil_div(ka, CH_NB);
+    static int per_sm = -1;
+    if (per_sm < 0) {
+        int bps = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, trsv_chain_kernel<T, true, false>,
+                                                          CH_THREADS, 0) != cudaSuccess) {
+            cudaGetLastError();
+            bps = 0;
+        }
+        per_sm = bps;
+    }
+    if ((long long)per_sm * num_sms() < nblk) return kErrUnsupported;
+    unsigned long long *flags = nullptr, epoch = 0;
+    int st = workspace_flags(stream, nblk, &flags, &epoch);
+    if (st != kOk) return st;
+    Workspace *w = workspace_for(stream, 0);
+    if (!w) return kErrAlloc;
+    int *status = w->status;
+    void *args[] = {&ka, &M0, &mi, &mp, &X0, &xs, &vs, &nvec, &flags, &epoch, &status};
+    KTimer kt(kFamTrsm, stream, (double)ka * ka * nvec, 4.0 * (double)ka * ka + 16.0 * ka * nvec);
+    const void *fn;
+    if (lowerM) fn = unit ? (const void *)trsv_chain_kernel<T, true, true>
+                          : (const void *)trsv_chain_kernel<T, true, false>;
+    else fn = unit ? (const void *)trsv_chain_kernel<T, false, true>
+                   : (const void *)trsv_chain_kernel<T, false, false>;
+    FG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(nblk), dim3(CH_THREADS), args, 0, stream));
+    return kOk;
+}
+
+// Chained solves on (FLENS_GB300_TRSV_CHAIN=0 turns them off).
+bool chain_enabled() {
+    static bool on = [] {
+        const char *e = getenv("FLENS_GB300_TRSV_CHAIN");
+        return !(e && atoi(e) == 0);
+    }();
+    return on;
+}
+
 template <typename T>
 int launch_diag(int kb, const T *M0, long long mi, long long mp, bool lowerM, bool unit,
                 T *X0, long long xs, long long vs, int nvec, cudaStream_t stream) {
     KTimer kt(kFamTrsm, stream, (double)kb * kb * nvec, 16.0 * (double)kb * nvec);
-    if (nvec <= TRSM_WARP_MAX) {
+    if (nvec <= trsm_warp_max()) {
         const int grid = ceil_div(nvec, TRSM_WARP_VECS);
 #define FG_WARP(L, U) trsm_diag_warp_kernel<T, L, U><<<grid, 32 * TRSM_WARP_VECS, 0, stream>>>(kb, M0, mi, mp, X0, xs, vs, nvec)
         if (lowerM) { if (unit) FG_WARP(true, true); else FG_WARP(true, false); }
@@ -208,7 +396,13 @@ int trsm_launch_t(char side, char upLo, char transA, char diag, int m, int n,
           diag, m, n, lowerM ? "lower" : "upper", nvec);
 
     const int nblk = ceil_div(ka, TRSM_NB);
-    for (int s = 0; s < nblk; ++s) {
+    bool done = false;
+    if (nvec <= CH_MAXV && nblk >= 2 && chain_enabled()) {
+        const int st = launch_chain<T>(ka, A, mi, mp, lowerM, unit != 0, B, xs, vs, nvec, stream);
+        if (st == kOk) done = true;
+        else if (st != kErrUnsupported) return st;
+    }
+    for (int s = 0; !done && s < nblk; ++s) {
         const int bi = lowerM ? s : nblk - 1 - s;
         const int k0 = bi * TRSM_NB;
         const int kb = (ka - k0) < TRSM_NB ? (ka - k0) : TRSM_NB;
