@@ -143,11 +143,12 @@ def reference_arm(args, rank: int) -> None:
 
 
 # ------------------------------------------------------------ our arm --
-def make_inputs(torch, n, seed, dev):
+def make_inputs(torch, n, seed, dev, shift=True):
     g = torch.Generator(device=dev)
     g.manual_seed(seed)
     A0 = torch.rand((n, n), generator=g, dtype=torch.float64, device=dev).mul_(2).sub_(1)
-    A0.diagonal().add_(n / 4.0)
+    if shift:
+        A0.diagonal().add_(n / 4.0)
     A0 = A0.t()  # column-major view: stride(0) == 1
     x_true = torch.rand((n, 1), generator=g, dtype=torch.float64, device=dev).mul_(2).sub_(1)
     b0 = A0 @ x_true
@@ -216,7 +217,7 @@ def our_arm(args, rank: int, world: int) -> None:
         dist.init_process_group("nccl", device_id=dev)
     n = args.n
     stream = torch.cuda.current_stream()
-    A0, x_true, b0 = make_inputs(torch, n, 20261203 + rank, dev)
+    A0, x_true, b0 = make_inputs(torch, n, 20261203 + rank, dev, shift=not args.unshifted)
     A = fg.to_colmajor(A0.clone())
     b = b0.clone()
     ipiv = torch.zeros(n, dtype=torch.int32, device=dev)
@@ -274,7 +275,8 @@ def our_arm(args, rank: int, world: int) -> None:
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (torch seeded uniform[-1,1] + n/4 diagonal; b = A x_true)",
+        "data": ("synthetic (torch seeded uniform[-1,1], NO diagonal shift: profiling input; b = A x_true)"
+                 if args.unshifted else "synthetic (torch seeded uniform[-1,1] + n/4 diagonal; b = A x_true)"),
         "config": {"workload": f"dgetrf+dgetrs n={n} 1 rhs FP64 column-major",
                    "n": n, "nrhs": 1, "nb": NB, "parallelism": f"replicas x{world}",
                    "l2": "input 512 MiB > L2 (no flush)",
@@ -894,6 +896,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--quick", action="store_true", help="skip peak and sub-benchmarks")
+    ap.add_argument("--unshifted", action="store_true",
+                    help="profiling only: omit the n/4 diagonal shift so that the LU interchanges rows "
+                         "(the benchmark workload's pivots are the identity)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")

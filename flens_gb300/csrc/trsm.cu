@@ -196,6 +196,7 @@ trsv_chain_kernel(int ka, const T *__restrict__ M0, long long mi, long long mp, 
                   long long vs, int nvec, unsigned long long *flags, unsigned long long epoch,
                   int *status) {
     __shared__ T Mb[CH_NB][CH_NB + 1];                 // Mb[p][r] = M(R0 + r, K0 + p)
+    __shared__ T Md[CH_NB][CH_NB + 1];                 // the diagonal block, same layout
     __shared__ T xk[CH_MAXV][CH_NB];
     __shared__ T part[CH_THREADS / CH_NB][CH_MAXV][CH_NB];
     __shared__ T rinv[CH_NB];
@@ -209,19 +210,24 @@ trsv_chain_kernel(int ka, const T *__restrict__ M0, long long mi, long long mp, 
 #pragma unroll
     for (int v = 0; v < CH_MAXV; ++v) acc[v] = T(0);
 
-    auto stage = [&](int K0, int kk) {
+    auto stage = [&](T (*D)[CH_NB + 1], int K0, int kk) {
         for (int e = tid; e < CH_NB * CH_NB; e += CH_THREADS) {
             int rr, pp;
             if (mi == 1) { rr = e % CH_NB; pp = e / CH_NB; }
             else { pp = e % CH_NB; rr = e / CH_NB; }
-            Mb[pp][rr] = (rr < kb && pp < kk) ? M0[(R0 + rr) * mi + (K0 + pp) * mp] : T(0);
+            D[pp][rr] = (rr < kb && pp < kk) ? M0[(R0 + rr) * mi + (K0 + pp) * mp] : T(0);
         }
     };
+    // the diagonal block and its reciprocals do not depend on other blocks:
+    // off the critical path, before any wait
+    stage(Md, R0, kb);
+    __syncthreads();
+    if (!UNIT && tid < kb) rinv[tid] = T(1) / Md[tid][tid];
 
     for (int s2 = 0; s2 < s; ++s2) {
         const int k = LOWER ? s2 : nblk - 1 - s2;
         const int K0 = k * CH_NB, kk = min(CH_NB, ka - K0);
-        stage(K0, kk);
+        stage(Mb, K0, kk);
         if (tid == 0) {
             unsigned spins = 0;
             while (ch_acquire(&flags[s2]) != epoch) {
@@ -241,20 +247,22 @@ trsv_chain_kernel(int ka, const T *__restrict__ M0, long long mi, long long mp, 
             xk[v][p] = p < kk ? __ldcg(&X0[v * vs + (K0 + p) * xs]) : T(0);
         }
         __syncthreads();
+        // each block's 16 products summed on their own, then added to the
+        // running sum: (16 + blocks) roundings per row instead of 16 * blocks
+        // (this matters for the FP32 solves of the refinement)
 #pragma unroll
         for (int v = 0; v < CH_MAXV; ++v) {
             if (v < nvec) {
+                T blk = T(0);
 #pragma unroll 4
-                for (int p = q * 16; p < q * 16 + 16; ++p) acc[v] = fma(Mb[p][r], xk[v][p], acc[v]);
+                for (int p = q * 16; p < q * 16 + 16; ++p) blk = fma(Mb[p][r], xk[v][p], blk);
+                acc[v] += blk;
             }
         }
         __syncthreads();                                   // Mb and xk are restaged next
     }
 #pragma unroll
     for (int v = 0; v < CH_MAXV; ++v) part[q][v][r] = acc[v];
-    stage(R0, kb);                                          // the diagonal block
-    __syncthreads();
-    if (!UNIT && tid < kb) rinv[tid] = T(1) / Mb[tid][tid];
     __syncthreads();
     const int warp = tid >> 5, lane = tid & 31;
     if (warp < nvec) {
@@ -275,11 +283,11 @@ trsv_chain_kernel(int ka, const T *__restrict__ M0, long long mi, long long mp, 
             }
             const int r1 = lane + 32;
             if (LOWER) {
-                if (lane > i && lane < kb) x0 = fma(-Mb[i][lane], xi, x0);
-                if (r1 > i && r1 < kb) x1 = fma(-Mb[i][r1], xi, x1);
+                if (lane > i && lane < kb) x0 = fma(-Md[i][lane], xi, x0);
+                if (r1 > i && r1 < kb) x1 = fma(-Md[i][r1], xi, x1);
             } else {
-                if (lane < i) x0 = fma(-Mb[i][lane], xi, x0);
-                if (r1 < i) x1 = fma(-Mb[i][r1], xi, x1);
+                if (lane < i) x0 = fma(-Md[i][lane], xi, x0);
+                if (r1 < i) x1 = fma(-Md[i][r1], xi, x1);
             }
         }
         if (lane < kb) x[lane * xs] = x0;
