@@ -294,8 +294,8 @@ struct EpiSplit {
     double alpha, beta;
     double *C;
     int ldc;
-    double *W;                                   // group-sum accumulator, m x n, ld = ldw
-    int ldw;
+    double *W;                                   // group sums: one BM x BN tile per CTA
+    int ldw;                                     // unused (tiles are BM x BN, column-major)
     const int *ea, *eb;                          // row exponents of op(A), column exponents of op(B)
 
     __device__ int groups() const { return geo.ngroups; }
@@ -316,14 +316,17 @@ struct EpiSplit {
         // FP64 exponent field = FP32 field + (1023 - 127) + e_i + f_j - bits*dg
         const long long krow = row_ok ? (long long)(ea[row] - geo.bits * dg + 896) : 0;
         const size_t r0 = (size_t)(row_ok ? row : 0);
-        double *wrow = W + r0 + (size_t)col * ldw;
+        // this CTA's own tile of group sums, reused for each of its tiles: it
+        // stays in L2 (152 x 256 KB) instead of spanning m x n
+        double *wrow = W + (size_t)blockIdx.x * (tc::BM * tc::BN) + (r0 & (tc::BM - 1)) +
+                       (size_t)(col & (tc::BN - 1)) * tc::BM;
         double *crow = C + r0 + (size_t)col * ldc;
 #pragma unroll
         for (int h = 0; h < 32; h += 16) {
             double sv[16];
 #pragma unroll
             for (int j = 0; j < 16; ++j)
-                sv[j] = (!first && row_ok && h + j < ncol) ? __ldcg(wrow + (size_t)(h + j) * ldw) : 0.0;
+                sv[j] = (!first && row_ok && h + j < ncol) ? __ldcg(wrow + (size_t)(h + j) * tc::BM) : 0.0;
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const long long kj = krow + __shfl_sync(0xffffffffu, fl, h + j);
@@ -337,7 +340,7 @@ struct EpiSplit {
             if (row_ok && !last) {
 #pragma unroll
                 for (int j = 0; j < 16; ++j)
-                    if (h + j < ncol) __stcg(wrow + (size_t)(h + j) * ldw, sv[j]);
+                    if (h + j < ncol) __stcg(wrow + (size_t)(h + j) * tc::BM, sv[j]);
             } else if (row_ok) {
                 double cv[16];
 #pragma unroll
@@ -476,11 +479,11 @@ int dgemm_split_launch_at(char transA, char transB, int m, int n, int k, double 
     if (rc != kOk) return rc;
     if ((rc = tc::make_kmajor_map(&mb, kTcBF16, Bd, n, (int)ldS, (int)ldS, tc::BN)) != kOk) return rc;
     if ((rc = tc::prepare_kernel<kTcBF16, EpiSplit>()) != kOk) return rc;
-    double *W = (double *)workspace_slot(s, 2, (size_t)m * n * sizeof(double));
-    if (!W) return kErrAlloc;
-    const EpiSplit epi{geo, alpha, beta, C, ldC, W, m, ea, eb};
     const int ntiles = ceil_div(m, tc::BM) * ceil_div(n, tc::BN);
     const int grid = ntiles < num_sms() ? ntiles : num_sms();
+    double *W = (double *)workspace_slot(s, 2, (size_t)grid * tc::BM * tc::BN * sizeof(double));
+    if (!W) return kErrAlloc;
+    const EpiSplit epi{geo, alpha, beta, C, ldC, W, tc::BM, ea, eb};
     const double pairs = (double)S * (S + 1) / 2;
     {
         KTimer kt(kFamSplit, s, 2.0 * pairs * m * (double)n * geo.Kp,
