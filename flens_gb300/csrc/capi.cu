@@ -133,16 +133,23 @@ int view_in(int slot, const double *h, int rows, int cols, int ld, bool copy, cu
     v->p = (double *)d;
     v->ld = dld;
     v->staged = true;
-    if (copy && rows > 0 && cols > 0)
-        FG_CUDA(cudaMemcpy2DAsync(v->p, (size_t)dld * sizeof(double), h, (size_t)ld * sizeof(double),
-                                  (size_t)rows * sizeof(double), cols, cudaMemcpyHostToDevice, s));
+    if (copy && rows > 0 && cols > 0) {
+        if (ld == dld)      // one contiguous block: a plain copy
+            FG_CUDA(cudaMemcpyAsync(v->p, h, (size_t)dld * cols * sizeof(double), cudaMemcpyHostToDevice, s));
+        else
+            FG_CUDA(cudaMemcpy2DAsync(v->p, (size_t)dld * sizeof(double), h, (size_t)ld * sizeof(double),
+                                      (size_t)rows * sizeof(double), cols, cudaMemcpyHostToDevice, s));
+    }
     return kOk;
 }
 
 int view_out(const DevView &v, double *h, int rows, int cols, int ld, cudaStream_t s) {
     if (!v.staged || rows <= 0 || cols <= 0) return kOk;
-    FG_CUDA(cudaMemcpy2DAsync(h, (size_t)ld * sizeof(double), v.p, (size_t)v.ld * sizeof(double),
-                              (size_t)rows * sizeof(double), cols, cudaMemcpyDeviceToHost, s));
+    if (ld == v.ld)
+        FG_CUDA(cudaMemcpyAsync(h, v.p, (size_t)v.ld * cols * sizeof(double), cudaMemcpyDeviceToHost, s));
+    else
+        FG_CUDA(cudaMemcpy2DAsync(h, (size_t)ld * sizeof(double), v.p, (size_t)v.ld * sizeof(double),
+                                  (size_t)rows * sizeof(double), cols, cudaMemcpyDeviceToHost, s));
     return kOk;
 }
 
@@ -310,6 +317,17 @@ int gesv_host(int n, int nrhs, double *A, int ldA, int *IPIV, double *B, int ldB
     Workspace *w = workspace_for(s, 0);
     if (!w) return kErrAlloc;
     if ((st = dgetrf_launch(n, n, a.p, a.ld, dpiv, w->info, s)) != kOk) return st;
+    // the factors and pivots go back on the side stream while the solve runs
+    // (both only read them)
+    Workspace *ws = (a.staged || pstaged) ? workspace_side(s) : nullptr;
+    cudaStream_t cs = ws ? ws->side : s;
+    if (ws) {
+        FG_CUDA(cudaEventRecord(ws->ev_fwd, s));
+        FG_CUDA(cudaStreamWaitEvent(cs, ws->ev_fwd, 0));
+    }
+    if ((st = view_out(a, A, n, n, ldA, cs)) != kOk) return st;
+    if (pstaged) FG_CUDA(cudaMemcpyAsync(IPIV, dpiv, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, cs));
+    if (ws) FG_CUDA(cudaEventRecord(ws->ev_back, cs));
     FG_CUDA(cudaMemcpyAsync(INFO, w->info, sizeof(int), cudaMemcpyDeviceToHost, s));
     FG_CUDA(cudaStreamSynchronize(s));
     // flens/lapack/ge/sv.tcc:70-75: solve only if the factorisation succeeded
@@ -317,8 +335,7 @@ int gesv_host(int n, int nrhs, double *A, int ldA, int *IPIV, double *B, int ldB
         if ((st = dgetrs_launch('N', n, nrhs, a.p, a.ld, dpiv, b.p, b.ld, s)) != kOk) return st;
         if ((st = view_out(b, B, n, nrhs, ldB, s)) != kOk) return st;
     }
-    if ((st = view_out(a, A, n, n, ldA, s)) != kOk) return st;
-    if (pstaged) FG_CUDA(cudaMemcpyAsync(IPIV, dpiv, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (ws) FG_CUDA(cudaStreamWaitEvent(s, ws->ev_back, 0));
     return finish(s);
 }
 
