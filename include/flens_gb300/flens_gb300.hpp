@@ -10,18 +10,21 @@
  *
  *  - cxxblas level 3: like the cblas overloads FLENS adds under HAVE_CBLAS
  *    (cxxblas/level3/gemm.tcc:218-240, cxxblas/level3/trsm.tcc:107-126), more
- *    specialised overloads of cxxblas::gemm and cxxblas::trsm for double with
- *    an integral index forward to dgemm_ / dtrsm_.  flens::blas::mm and
- *    flens::blas::sm (flens/blas/level3/mm.tcc:463-472, sm.tcc:61-67), the
- *    operator form C = beta*C + alpha*A*B, and every mm/sm call FLENS-LAPACK
- *    makes reach them.
+ *    specialised overloads of cxxblas::gemm, trsm, syrk, syr2k, trmm and symm
+ *    for double with an integral index forward to dgemm_, dtrsm_, dsyrk_,
+ *    dsyr2k_, dtrmm_ and dsymm_.  flens::blas::mm, sm, rk, r2k
+ *    (flens/blas/level3/mm.tcc:463-472, sm.tcc:61-67, ...), the operator form
+ *    C = beta*C + alpha*A*B, and every level-3 call FLENS-LAPACK makes reach
+ *    them.
  *  - FLENS-LAPACK's generic implementations: more specialised overloads of
- *    flens::lapack::generic::trf_impl (flens/lapack/ge/trf.tcc:61) and
- *    trs_impl (flens/lapack/ge/trs.tcc:61) for column-major double matrices
- *    with int pivots forward to dgetrf_ / dgetrs_, so lapack::trf, lapack::trs
- *    and lapack::sv (which calls both, flens/lapack/ge/sv.tcc:58-77) run on
- *    the GPU.  Other element types, index types and storage orders keep the
- *    reference's generic code.
+ *    flens::lapack::generic::trf_impl (flens/lapack/ge/trf.tcc:61), trs_impl
+ *    (flens/lapack/ge/trs.tcc:61), potrf_impl (flens/lapack/po/potrf.tcc:61),
+ *    potrs_impl (flens/lapack/po/potrs.tcc:61) and the two tri_impl
+ *    (flens/lapack/ge/tri.tcc:64, flens/lapack/tr/tri.tcc:64) for
+ *    column-major double matrices with int pivots forward to dgetrf_,
+ *    dgetrs_, dpotrf_, dpotrs_, dgetri_ and dtrtri_, so lapack::trf, trs, sv,
+ *    potrf, potrs, posv and tri run on the GPU.  Other element types, index
+ *    types and storage orders keep the reference's generic code.
  *
  * The overloads must be declared between flens.h and flens.tcc so that the
  * qualified calls inside the FLENS templates see them; hence the include
@@ -35,6 +38,7 @@
 #error "include <flens_gb300/flens_gb300.hpp> instead of (not after) <flens/flens.cxx>"
 #endif
 
+#include <cstdio>
 #include <type_traits>
 #include <vector>
 
@@ -114,6 +118,80 @@ trsm(StorageOrder order, Side side, StorageUpLo upLo, Transpose transA, Diag dia
     dtrsm_(&s, &u, &t, &d, &M, &N, &alpha, A, &LDA, B, &LDB);
 }
 
+//-- syrk: double, any integral index -> dsyrk_ (column-major)
+template <typename IndexType>
+typename std::enable_if<flens_gb300::detail::IsIndex<IndexType>::value, void>::type
+syrk(StorageOrder order, StorageUpLo upLo, Transpose trans, IndexType n, IndexType k,
+     double alpha, const double *A, IndexType ldA, double beta, double *C, IndexType ldC)
+{
+    if (order == RowMajor) {
+        // the row-major triangle is the column-major opposite one, op(A)
+        // flips (cxxblas/level3/syrk.tcc:51-56)
+        syrk(ColMajor, upLo == Upper ? Lower : Upper, Transpose(trans ^ Trans), n, k, alpha, A, ldA,
+             beta, C, ldC);
+        return;
+    }
+    const char u = static_cast<char>(upLo), t = flens_gb300::detail::trans_char(trans);
+    const int N = int(n), K = int(k), LDA = int(ldA), LDC = int(ldC);
+    dsyrk_(&u, &t, &N, &K, &alpha, A, &LDA, &beta, C, &LDC);
+}
+
+//-- syr2k: double, any integral index -> dsyr2k_ (column-major)
+template <typename IndexType>
+typename std::enable_if<flens_gb300::detail::IsIndex<IndexType>::value, void>::type
+syr2k(StorageOrder order, StorageUpLo upLo, Transpose trans, IndexType n, IndexType k,
+      double alpha, const double *A, IndexType ldA, const double *B, IndexType ldB,
+      double beta, double *C, IndexType ldC)
+{
+    if (order == RowMajor) {
+        // (cxxblas/level3/syr2k.tcc:52-57)
+        syr2k(ColMajor, upLo == Upper ? Lower : Upper, Transpose(trans ^ Trans), n, k, alpha, A, ldA,
+              B, ldB, beta, C, ldC);
+        return;
+    }
+    const char u = static_cast<char>(upLo), t = flens_gb300::detail::trans_char(trans);
+    const int N = int(n), K = int(k), LDA = int(ldA), LDB = int(ldB), LDC = int(ldC);
+    dsyr2k_(&u, &t, &N, &K, &alpha, A, &LDA, B, &LDB, &beta, C, &LDC);
+}
+
+//-- trmm: double, any integral index -> dtrmm_ (column-major)
+template <typename IndexType>
+typename std::enable_if<flens_gb300::detail::IsIndex<IndexType>::value, void>::type
+trmm(StorageOrder order, Side side, StorageUpLo upLo, Transpose transA, Diag diag,
+     IndexType m, IndexType n, double alpha, const double *A, IndexType ldA,
+     double *B, IndexType ldB)
+{
+    if (order == RowMajor) {
+        // row-major B is column-major B^T: the other side, the other
+        // triangle, m and n swapped (cxxblas/level3/trmm.tcc:49-54)
+        trmm(ColMajor, side == Left ? Right : Left, upLo == Upper ? Lower : Upper, transA, diag, n, m,
+             alpha, A, ldA, B, ldB);
+        return;
+    }
+    const char sd = static_cast<char>(side), u = static_cast<char>(upLo);
+    const char t = flens_gb300::detail::trans_char(transA), d = static_cast<char>(diag);
+    const int M = int(m), N = int(n), LDA = int(ldA), LDB = int(ldB);
+    dtrmm_(&sd, &u, &t, &d, &M, &N, &alpha, A, &LDA, B, &LDB);
+}
+
+//-- symm: double, any integral index -> dsymm_ (column-major)
+template <typename IndexType>
+typename std::enable_if<flens_gb300::detail::IsIndex<IndexType>::value, void>::type
+symm(StorageOrder order, Side side, StorageUpLo upLo, IndexType m, IndexType n,
+     double alpha, const double *A, IndexType ldA, const double *B, IndexType ldB,
+     double beta, double *C, IndexType ldC)
+{
+    if (order == RowMajor) {
+        // (cxxblas/level3/symm.tcc:51-58)
+        symm(ColMajor, side == Left ? Right : Left, upLo == Upper ? Lower : Upper, n, m, alpha, A, ldA,
+             B, ldB, beta, C, ldC);
+        return;
+    }
+    const char sd = static_cast<char>(side), u = static_cast<char>(upLo);
+    const int M = int(m), N = int(n), LDA = int(ldA), LDB = int(ldB), LDC = int(ldC);
+    dsymm_(&sd, &u, &M, &N, &alpha, A, &LDA, B, &LDB, &beta, C, &LDC);
+}
+
 }  // namespace cxxblas
 
 namespace flens { namespace lapack { namespace generic {
@@ -168,6 +246,90 @@ trs_impl(Transpose trans, const GeMatrix<FSA<double, cxxblas::ColMajor, IA, AA> 
         for (int i = 0; i < n; ++i) p[i] = piv(piv.firstIndex() + i * (piv.inc() > 0 ? 1 : -1));
         dgetrs_(&t, &n, &nrhs, A.data(), &lda, p.data(), B.data(), &ldb, &info);
     }
+}
+
+//-- potrf for column-major double -> dpotrf_
+template <template <typename, cxxblas::StorageOrder, typename, typename> class FS,
+          typename I, typename Alloc>
+typename std::enable_if<
+    flens_gb300::detail::IsDoubleColMajorFull<FS<double, cxxblas::ColMajor, I, Alloc> >::value,
+    typename SyMatrix<FS<double, cxxblas::ColMajor, I, Alloc> >::IndexType>::type
+potrf_impl(SyMatrix<FS<double, cxxblas::ColMajor, I, Alloc> > &A)
+{
+    typedef typename SyMatrix<FS<double, cxxblas::ColMajor, I, Alloc> >::IndexType IndexType;
+    const int n = int(A.dim());
+    if (n == 0) return IndexType(0);
+    const int ld = int(A.leadingDimension());
+    const char u = static_cast<char>(A.upLo());
+    int info = 0;
+    dpotrf_(&u, &n, A.data(), &ld, &info);
+    return IndexType(info);
+}
+
+//-- potrs for column-major double -> dpotrs_
+template <template <typename, cxxblas::StorageOrder, typename, typename> class FSA,
+          typename IA, typename AA,
+          template <typename, cxxblas::StorageOrder, typename, typename> class FSB,
+          typename IB, typename AB>
+typename std::enable_if<
+    flens_gb300::detail::IsDoubleColMajorFull<FSA<double, cxxblas::ColMajor, IA, AA> >::value
+        && flens_gb300::detail::IsDoubleColMajorFull<FSB<double, cxxblas::ColMajor, IB, AB> >::value,
+    void>::type
+potrs_impl(const SyMatrix<FSA<double, cxxblas::ColMajor, IA, AA> > &A,
+           GeMatrix<FSB<double, cxxblas::ColMajor, IB, AB> > &B)
+{
+    const int n = int(A.dim()), nrhs = int(B.numCols());
+    if (n == 0 || nrhs == 0) return;
+    const int lda = int(A.leadingDimension()), ldb = int(B.leadingDimension());
+    const char u = static_cast<char>(A.upLo());
+    int info = 0;
+    dpotrs_(&u, &n, &nrhs, A.data(), &lda, B.data(), &ldb, &info);
+    // potrs has no INFO to return: report a library failure (a CUDA error,
+    // no device) the way the BLAS entry points do
+    if (info <= -1000)
+        std::fprintf(stderr, "[flens_gb300] dpotrs_ failed (%d): %s\n", info, flens_gb300_last_error());
+}
+
+//-- (ge)tri for column-major double with int pivots -> dgetri_ (the
+//   library keeps its own device workspace; `work` is not needed)
+template <template <typename, cxxblas::StorageOrder, typename, typename> class FS,
+          typename I, typename Alloc, typename VP, typename VWORK>
+typename std::enable_if<
+    flens_gb300::detail::IsDoubleColMajorFull<FS<double, cxxblas::ColMajor, I, Alloc> >::value
+        && std::is_same<typename DenseVector<VP>::ElementType, int>::value,
+    typename GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> >::IndexType>::type
+tri_impl(GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> > &A, const DenseVector<VP> &piv,
+         DenseVector<VWORK> &)
+{
+    typedef typename GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> >::IndexType IndexType;
+    const int n = int(A.numRows());
+    if (n == 0) return IndexType(0);
+    const int ld = int(A.leadingDimension());
+    std::vector<int> p(n);
+    for (int i = 0; i < n; ++i) p[i] = piv(piv.firstIndex() + i * (piv.inc() > 0 ? 1 : -1));
+    std::vector<double> work(n);
+    const int lwork = n;
+    int info = 0;
+    dgetri_(&n, A.data(), &ld, p.data(), work.data(), &lwork, &info);
+    return IndexType(info);
+}
+
+//-- (tr)tri for column-major double -> dtrtri_
+template <template <typename, cxxblas::StorageOrder, typename, typename> class FS,
+          typename I, typename Alloc>
+typename std::enable_if<
+    flens_gb300::detail::IsDoubleColMajorFull<FS<double, cxxblas::ColMajor, I, Alloc> >::value,
+    typename TrMatrix<FS<double, cxxblas::ColMajor, I, Alloc> >::IndexType>::type
+tri_impl(TrMatrix<FS<double, cxxblas::ColMajor, I, Alloc> > &A)
+{
+    typedef typename TrMatrix<FS<double, cxxblas::ColMajor, I, Alloc> >::IndexType IndexType;
+    const int n = int(A.dim());
+    if (n == 0) return IndexType(0);
+    const int ld = int(A.leadingDimension());
+    const char u = static_cast<char>(A.upLo()), d = static_cast<char>(A.diag());
+    int info = 0;
+    dtrtri_(&u, &d, &n, A.data(), &ld, &info);
+    return IndexType(info);
 }
 
 } } }  // namespace generic, lapack, flens

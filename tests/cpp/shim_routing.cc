@@ -28,6 +28,31 @@ int main()
     std::printf("sm B(2,1)=%g\n", B(2, 1));
     const int info = lapack::trf(A, piv);              // -> generic::trf_impl -> dgetrf_
     std::printf("trf info=%d piv=%d,%d,%d,%d\n", info, piv(1), piv(2), piv(3), piv(4));
+
+    // the rest of level 3
+    RealGeMatrix D(n, n), E(n, n);
+    D = 1;
+    E = 0;
+    blas::rk(NoTrans, 1.0, D, 0.0, E.upper().symmetric());          // -> cxxblas::syrk
+    blas::r2k(NoTrans, 1.0, D, D, 0.0, E.upper().symmetric());      // -> cxxblas::syr2k
+    blas::mm(Left, 1.0, D.upper().symmetric(), D, 0.0, E);          // -> cxxblas::symm
+    blas::mm(Left, NoTrans, 1.0, D.upper(), E);                      // -> cxxblas::trmm
+    std::printf("level3 E(1,1)=%g\n", E(1, 1));
+
+    // Cholesky and the inverses
+    RealGeMatrix S(n, n);
+    S = 4, 1, 0, 0,
+        1, 4, 1, 0,
+        0, 1, 4, 1,
+        0, 0, 1, 4;
+    const int pinfo = lapack::potrf(S.upper().symmetric());         // -> generic::potrf_impl
+    std::printf("potrf info=%d\n", pinfo);
+    lapack::potrs(S.upper().symmetric(), D);                         // -> generic::potrs_impl
+    const int tinfo = lapack::tri(S.upper());                        // -> (tr) generic::tri_impl
+    std::printf("trtri info=%d\n", tinfo);
+    DenseVector<Array<double> > work(n);
+    const int ginfo = lapack::tri(A, piv, work);                     // -> (ge) generic::tri_impl
+    std::printf("getri info=%d\n", ginfo);
     std::printf("last_error=%s\n", flens_gb300_last_error());
     return 0;
 }

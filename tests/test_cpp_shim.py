@@ -4,7 +4,8 @@ Builds tests/cpp/shim_routing.cc against the FLENS headers (only where they
 are present) and include/flens_gb300/flens_gb300.hpp, linked with
 libflens_gb300.so.  Without a GPU every routed call must fail loudly with the
 library's no-device error instead of computing on the CPU -- which proves that
-blas::mm, blas::sm and lapack::trf no longer run the reference's generic code.
+blas::mm, sm, rk, r2k and lapack::trf, potrf, potrs, tri no longer run the
+reference's generic code.
 With a GPU the same program must print the reference's answers.
 """
 import os
@@ -42,3 +43,7 @@ def test_flens_calls_reach_the_library_without_gpu(shim_binary):
     assert "dgemm_ failed (-1003)" in r.stderr
     assert "dtrsm_ failed (-1003)" in r.stderr
     assert "trf info=-1003" in r.stdout
+    for f in ("dsyrk_", "dsyr2k_", "dsymm_", "dtrmm_", "dpotrs_"):
+        assert f + " failed (-1003)" in r.stderr, f
+    for f in ("potrf", "trtri", "getri"):
+        assert f + " info=-1003" in r.stdout, f
