@@ -19,12 +19,16 @@
  *  - FLENS-LAPACK's generic implementations: more specialised overloads of
  *    flens::lapack::generic::trf_impl (flens/lapack/ge/trf.tcc:61), trs_impl
  *    (flens/lapack/ge/trs.tcc:61), potrf_impl (flens/lapack/po/potrf.tcc:61),
- *    potrs_impl (flens/lapack/po/potrs.tcc:61) and the two tri_impl
- *    (flens/lapack/ge/tri.tcc:64, flens/lapack/tr/tri.tcc:64) for
- *    column-major double matrices with int pivots forward to dgetrf_,
- *    dgetrs_, dpotrf_, dpotrs_, dgetri_ and dtrtri_, so lapack::trf, trs, sv,
- *    potrf, potrs, posv and tri run on the GPU.  Other element types, index
- *    types and storage orders keep the reference's generic code.
+ *    potrs_impl (flens/lapack/po/potrs.tcc:61), the two tri_impl
+ *    (flens/lapack/ge/tri.tcc:64, flens/lapack/tr/tri.tcc:64), rfs_impl
+ *    (flens/lapack/ge/rfs.tcc:63), con_impl (flens/lapack/ge/cond.tcc:62),
+ *    equ_impl (flens/lapack/ge/equ.tcc:62), laq_impl
+ *    (flens/lapack/la/laq.tcc:59) and svx_impl (flens/lapack/ge/svx.tcc:60)
+ *    for column-major double matrices with int pivots forward to dgetrf_,
+ *    dgetrs_, dpotrf_, dpotrs_, dgetri_, dtrtri_, dgerfs_, dgecon_, dgeequ_,
+ *    dlaqge_ and dgesvx_, so lapack::trf, trs, sv, potrf, potrs, posv, tri,
+ *    rfs, con, equ and svx run on the GPU.  Other element types, index types
+ *    and storage orders keep the reference's generic code.
  *
  * The overloads must be declared between flens.h and flens.tcc so that the
  * qualified calls inside the FLENS templates see them; hence the include
@@ -72,6 +76,21 @@ struct IsDoubleColMajorFull<flens::FullStorageView<double, cxxblas::ColMajor, I,
 template <typename I, typename A>
 struct IsDoubleColMajorFull<flens::ConstFullStorageView<double, cxxblas::ColMajor, I, A> >
     : std::true_type {};
+
+// element i (0-based, logical order) of a FLENS vector, copied out / in
+template <typename T, typename V>
+inline std::vector<T> to_vec(const flens::DenseVector<V> &x)
+{
+    std::vector<T> v(x.length() > 0 ? std::size_t(x.length()) : 1);
+    for (int i = 0; i < int(x.length()); ++i) v[i] = T(x(x.firstIndex() + i));
+    return v;
+}
+
+template <typename T, typename V>
+inline void from_vec(const std::vector<T> &v, flens::DenseVector<V> &x)
+{
+    for (int i = 0; i < int(x.length()); ++i) x(x.firstIndex() + i) = v[i];
+}
 
 }  // namespace detail
 }  // namespace flens_gb300
@@ -329,6 +348,158 @@ tri_impl(TrMatrix<FS<double, cxxblas::ColMajor, I, Alloc> > &A)
     const char u = static_cast<char>(A.upLo()), d = static_cast<char>(A.diag());
     int info = 0;
     dtrtri_(&u, &d, &n, A.data(), &ld, &info);
+    return IndexType(info);
+}
+
+//-- rfs (refinement and error bounds) -> dgerfs_
+template <template <typename, cxxblas::StorageOrder, typename, typename> class FS,
+          typename I, typename Alloc, typename MAF, typename VPIV, typename MB, typename MX,
+          typename VFERR, typename VBERR, typename VWORK, typename VIWORK>
+typename std::enable_if<
+    flens_gb300::detail::IsDoubleColMajorFull<FS<double, cxxblas::ColMajor, I, Alloc> >::value
+        && flens_gb300::detail::IsDoubleColMajorFull<MAF>::value
+        && flens_gb300::detail::IsDoubleColMajorFull<MB>::value
+        && flens_gb300::detail::IsDoubleColMajorFull<MX>::value
+        && std::is_same<typename DenseVector<VPIV>::ElementType, int>::value,
+    void>::type
+rfs_impl(Transpose trans, const GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> > &A,
+         const GeMatrix<MAF> &AF, const DenseVector<VPIV> &piv, const GeMatrix<MB> &B,
+         GeMatrix<MX> &X, DenseVector<VFERR> &fErr, DenseVector<VBERR> &bErr,
+         DenseVector<VWORK> &, DenseVector<VIWORK> &)
+{
+    const int n = int(A.numRows()), nrhs = int(B.numCols());
+    if (n == 0 || nrhs == 0) return;
+    const int lda = int(A.leadingDimension()), ldaf = int(AF.leadingDimension());
+    const int ldb = int(B.leadingDimension()), ldx = int(X.leadingDimension());
+    const char t = flens_gb300::detail::trans_char(trans);
+    std::vector<int> p = flens_gb300::detail::to_vec<int>(piv), iwork(n);
+    std::vector<double> fe(nrhs), be(nrhs), work(3 * std::size_t(n));
+    int info = 0;
+    dgerfs_(&t, &n, &nrhs, A.data(), &lda, AF.data(), &ldaf, p.data(), B.data(), &ldb, X.data(),
+            &ldx, fe.data(), be.data(), work.data(), iwork.data(), &info);
+    if (info <= -1000)
+        std::fprintf(stderr, "[flens_gb300] dgerfs_ failed (%d): %s\n", info, flens_gb300_last_error());
+    flens_gb300::detail::from_vec(fe, fErr);
+    flens_gb300::detail::from_vec(be, bErr);
+}
+
+//-- con (condition estimate from the LU factors) -> dgecon_
+template <template <typename, cxxblas::StorageOrder, typename, typename> class FS,
+          typename I, typename Alloc, typename NORMA, typename RCOND, typename VWORK,
+          typename VIWORK>
+typename std::enable_if<
+    flens_gb300::detail::IsDoubleColMajorFull<FS<double, cxxblas::ColMajor, I, Alloc> >::value,
+    void>::type
+con_impl(Norm norm, const GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> > &A,
+         const NORMA &normA, RCOND &rCond, DenseVector<VWORK> &, DenseVector<VIWORK> &)
+{
+    const int n = int(A.numRows());
+    const int lda = int(A.leadingDimension() > 0 ? A.leadingDimension() : 1);
+    const char nm = static_cast<char>(norm);
+    const double anorm = double(normA);
+    double rc = 0.0;
+    std::vector<double> work(4 * std::size_t(n > 0 ? n : 1));
+    std::vector<int> iwork(n > 0 ? n : 1);
+    int info = 0;
+    dgecon_(&nm, &n, A.data(), &lda, &anorm, &rc, work.data(), iwork.data(), &info);
+    if (info <= -1000)
+        std::fprintf(stderr, "[flens_gb300] dgecon_ failed (%d): %s\n", info, flens_gb300_last_error());
+    rCond = rc;
+}
+
+//-- equ (row and column scalings) -> dgeequ_
+template <template <typename, cxxblas::StorageOrder, typename, typename> class FS,
+          typename I, typename Alloc, typename VR, typename VC, typename ROWCOND,
+          typename COLCOND, typename AMAX>
+typename std::enable_if<
+    flens_gb300::detail::IsDoubleColMajorFull<FS<double, cxxblas::ColMajor, I, Alloc> >::value,
+    typename GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> >::IndexType>::type
+equ_impl(const GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> > &A, DenseVector<VR> &r,
+         DenseVector<VC> &c, ROWCOND &rowCond, COLCOND &colCond, AMAX &amax)
+{
+    typedef typename GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> >::IndexType IndexType;
+    const int m = int(A.numRows()), n = int(A.numCols());
+    const int lda = int(A.leadingDimension() > 0 ? A.leadingDimension() : 1);
+    std::vector<double> rv(m > 0 ? m : 1), cv(n > 0 ? n : 1);
+    double rc = 0.0, cc = 0.0, am = 0.0;
+    int info = 0;
+    dgeequ_(&m, &n, A.data(), &lda, rv.data(), cv.data(), &rc, &cc, &am, &info);
+    flens_gb300::detail::from_vec(rv, r);
+    flens_gb300::detail::from_vec(cv, c);
+    rowCond = rc;
+    colCond = cc;
+    amax = am;
+    return IndexType(info);
+}
+
+//-- laq (apply the scalings when worthwhile) -> dlaqge_
+template <template <typename, cxxblas::StorageOrder, typename, typename> class FS,
+          typename I, typename Alloc, typename VR, typename VC, typename ROWCOND,
+          typename COLCOND, typename AMAX>
+typename std::enable_if<
+    flens_gb300::detail::IsDoubleColMajorFull<FS<double, cxxblas::ColMajor, I, Alloc> >::value,
+    LAQ::Equilibration>::type
+laq_impl(GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> > &A, const DenseVector<VR> &r,
+         const DenseVector<VC> &c, const ROWCOND &rowCond, const COLCOND &colCond,
+         const AMAX &amax)
+{
+    const int m = int(A.numRows()), n = int(A.numCols());
+    const int lda = int(A.leadingDimension() > 0 ? A.leadingDimension() : 1);
+    const std::vector<double> rv = flens_gb300::detail::to_vec<double>(r);
+    const std::vector<double> cv = flens_gb300::detail::to_vec<double>(c);
+    const double rc = double(rowCond), cc = double(colCond), am = double(amax);
+    char equed = 'N';
+    dlaqge_(&m, &n, A.data(), &lda, rv.data(), cv.data(), &rc, &cc, &am, &equed);
+    return LAQ::Equilibration(equed);
+}
+
+//-- svx (expert driver) -> dgesvx_.  EQUED is taken by value, as in the
+//   reference's interface, so the scaling applied is not reported back
+//   through it; work(1) receives the reciprocal pivot growth.
+template <template <typename, cxxblas::StorageOrder, typename, typename> class FS,
+          typename I, typename Alloc, typename MAF, typename VPIV, typename VR, typename VC,
+          typename MB, typename MX, typename RCOND, typename FERR, typename BERR,
+          typename VWORK, typename VIWORK>
+typename std::enable_if<
+    flens_gb300::detail::IsDoubleColMajorFull<FS<double, cxxblas::ColMajor, I, Alloc> >::value
+        && flens_gb300::detail::IsDoubleColMajorFull<MAF>::value
+        && flens_gb300::detail::IsDoubleColMajorFull<MB>::value
+        && flens_gb300::detail::IsDoubleColMajorFull<MX>::value
+        && std::is_same<typename DenseVector<VPIV>::ElementType, int>::value,
+    typename GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> >::IndexType>::type
+svx_impl(SVX::Fact fact, Transpose trans, GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> > &A,
+         GeMatrix<MAF> &AF, DenseVector<VPIV> &piv, SVX::Equilibration equed,
+         DenseVector<VR> &r, DenseVector<VC> &c, GeMatrix<MB> &B, GeMatrix<MX> &X,
+         RCOND &rCond, DenseVector<FERR> &fErr, DenseVector<BERR> &bErr,
+         DenseVector<VWORK> &work, DenseVector<VIWORK> &)
+{
+    typedef typename GeMatrix<FS<double, cxxblas::ColMajor, I, Alloc> >::IndexType IndexType;
+    const int n = int(A.numRows()), nrhs = int(B.numCols());
+    const int lda = int(A.leadingDimension() > 0 ? A.leadingDimension() : 1);
+    const int ldaf = int(AF.leadingDimension() > 0 ? AF.leadingDimension() : 1);
+    const int ldb = int(B.leadingDimension() > 0 ? B.leadingDimension() : 1);
+    const int ldx = int(X.leadingDimension() > 0 ? X.leadingDimension() : 1);
+    const char f = static_cast<char>(fact), t = flens_gb300::detail::trans_char(trans);
+    char eq = static_cast<char>(equed);
+    std::vector<int> p = flens_gb300::detail::to_vec<int>(piv), iw(n > 0 ? n : 1);
+    std::vector<double> rv = flens_gb300::detail::to_vec<double>(r);
+    std::vector<double> cv = flens_gb300::detail::to_vec<double>(c);
+    std::vector<double> fe(nrhs > 0 ? nrhs : 1), be(nrhs > 0 ? nrhs : 1);
+    std::vector<double> w(4 * std::size_t(n > 0 ? n : 1));
+    double rc = 0.0;
+    int info = 0;
+    dgesvx_(&f, &t, &n, &nrhs, A.data(), &lda, AF.data(), &ldaf, p.data(), &eq, rv.data(),
+            cv.data(), B.data(), &ldb, X.data(), &ldx, &rc, fe.data(), be.data(), w.data(),
+            iw.data(), &info);
+    if (info <= -1000)
+        std::fprintf(stderr, "[flens_gb300] dgesvx_ failed (%d): %s\n", info, flens_gb300_last_error());
+    flens_gb300::detail::from_vec(p, piv);
+    flens_gb300::detail::from_vec(rv, r);
+    flens_gb300::detail::from_vec(cv, c);
+    flens_gb300::detail::from_vec(fe, fErr);
+    flens_gb300::detail::from_vec(be, bErr);
+    rCond = rc;
+    if (work.length() > 0) work(work.firstIndex()) = w[0];
     return IndexType(info);
 }
 

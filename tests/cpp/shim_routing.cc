@@ -53,6 +53,24 @@ int main()
     DenseVector<Array<double> > work(n);
     const int ginfo = lapack::tri(A, piv, work);                     // -> (ge) generic::tri_impl
     std::printf("getri info=%d\n", ginfo);
+
+    // refinement, condition, equilibration, expert driver
+    RealGeMatrix X(n, n);
+    X = 0;
+    DenseVector<Array<double> > fErr(n), bErr(n), r(n), c(n), w3(3 * n), w4(4 * n);
+    DenseVector<Array<int> > iw(n);
+    lapack::rfs(NoTrans, S, S, piv, D, X, fErr, bErr, w3, iw);       // -> generic::rfs_impl
+    double rcond = -1;
+    lapack::con(lapack::OneNorm, S, 1.0, rcond, w4, iw);             // -> generic::con_impl
+    std::printf("con rcond=%g\n", rcond);
+    double rowCond = -1, colCond = -1, amax = -1;
+    const int einfo = lapack::equ(S, r, c, rowCond, colCond, amax); // -> generic::equ_impl
+    std::printf("equ info=%d\n", einfo);
+    RealGeMatrix AF(n, n);
+    IndexVector piv2(n);
+    const int sinfo = lapack::svx(lapack::SVX::NotFactored, NoTrans, S, AF, piv2,
+                                  lapack::SVX::None, r, c, D, X, rcond, fErr, bErr, w4, iw);
+    std::printf("svx info=%d\n", sinfo);
     std::printf("last_error=%s\n", flens_gb300_last_error());
     return 0;
 }

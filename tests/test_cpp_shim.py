@@ -4,8 +4,8 @@ Builds tests/cpp/shim_routing.cc against the FLENS headers (only where they
 are present) and include/flens_gb300/flens_gb300.hpp, linked with
 libflens_gb300.so.  Without a GPU every routed call must fail loudly with the
 library's no-device error instead of computing on the CPU -- which proves that
-blas::mm, sm, rk, r2k and lapack::trf, potrf, potrs, tri no longer run the
-reference's generic code.
+blas::mm, sm, rk, r2k and lapack::trf, potrf, potrs, tri, rfs, con, equ, svx no
+longer run the reference's generic code.
 With a GPU the same program must print the reference's answers.
 """
 import os
@@ -45,5 +45,9 @@ def test_flens_calls_reach_the_library_without_gpu(shim_binary):
     assert "trf info=-1003" in r.stdout
     for f in ("dsyrk_", "dsyr2k_", "dsymm_", "dtrmm_", "dpotrs_"):
         assert f + " failed (-1003)" in r.stderr, f
-    for f in ("potrf", "trtri", "getri"):
+    for f in ("potrf", "trtri", "getri", "equ"):
         assert f + " info=-1003" in r.stdout, f
+    for f in ("dgerfs_", "dgecon_"):
+        assert f + " failed (-1003)" in r.stderr, f
+    # the expert driver fails in its workspace request: any library error
+    assert "dgesvx_ failed (-100" in r.stderr and "svx info=-100" in r.stdout
