@@ -417,13 +417,8 @@ void fill_ranges(const std::vector<int> &hn, std::vector<int> &order, BatchArgs 
 }
 
 int set_attributes() {
-    static bool attr = false;
-    if (!attr) {
-        FG_CUDA(cudaFuncSetAttribute(batched_gesv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)BT_SMEM));
-        attr = true;
-    }
-    return kOk;
+    static DeviceOnce once;
+    return set_smem_once(once, (const void *)batched_gesv_kernel, (int)BT_SMEM);
 }
 
 // queue reset + the persistent kernel (also what a plan's graph holds)

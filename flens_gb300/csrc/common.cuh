@@ -89,6 +89,23 @@ int workspace_flags(cudaStream_t stream, int n, unsigned long long **flags,
 int num_sms();                 // SM count of the current device
 int device_id();               // current device ordinal
 
+// Kernel attributes (the dynamic shared memory limit) belong to a device
+// context: DeviceOnce remembers, per device, that one was set.
+struct DeviceOnce {
+    unsigned long long mask = 0;     // bit d: done on device d (benign race: setting twice is harmless)
+    bool pending() const {
+        const int d = device_id();
+        return d < 0 || d >= 64 || !((__atomic_load_n(&mask, __ATOMIC_ACQUIRE) >> d) & 1ull);
+    }
+    void done() {
+        const int d = device_id();
+        if (d >= 0 && d < 64) __atomic_fetch_or(&mask, 1ull << d, __ATOMIC_ACQ_REL);
+    }
+};
+
+// Sets the dynamic shared memory limit of `fn` to `bytes` once per device.
+int set_smem_once(DeviceOnce &once, const void *fn, int bytes);
+
 // Tracing: FLENS_GB300_TRACE=1 prints one line per kernel family chosen.
 bool trace_enabled();
 void trace(const char *fmt, ...);

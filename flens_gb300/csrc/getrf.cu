@@ -512,12 +512,9 @@ int laswp_launch_t(int nrows, int ncols, T *A, int ldA, int k1, int k2, const in
     T *tmp = (T *)((char *)w->buf + permBytes);
     const int use_smem = (size_t)nrows * sizeof(int) <= 200 * 1024 ? 1 : 0;
     if (use_smem) {
-        static bool attr = false;
-        if (!attr) {
-            FG_CUDA(cudaFuncSetAttribute(laswp_perm_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-            attr = true;
-        }
+        static DeviceOnce once;
+        const int st0 = set_smem_once(once, (const void *)laswp_perm_kernel, 200 * 1024);
+        if (st0 != kOk) return st0;
     }
     KTimer kt(kFamLaswp, stream, 0.0, 4.0 * sizeof(T) * (double)nrows * ncols);
     laswp_perm_kernel<<<1, 1024, use_smem ? (size_t)nrows * sizeof(int) : 0, stream>>>(
@@ -539,12 +536,9 @@ int laswp_perm_launch(int nrows, const int *ipiv, int *perm, cudaStream_t stream
     if (nrows <= 0) return kOk;
     const int use_smem = (size_t)nrows * sizeof(int) <= 200 * 1024 ? 1 : 0;
     if (use_smem) {
-        static bool attr = false;
-        if (!attr) {
-            FG_CUDA(cudaFuncSetAttribute(laswp_perm_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-            attr = true;
-        }
+        static DeviceOnce once;
+        const int st0 = set_smem_once(once, (const void *)laswp_perm_kernel, 200 * 1024);
+        if (st0 != kOk) return st0;
     }
     KTimer kt(kFamLaswp, stream, 0.0, 8.0 * nrows);
     laswp_perm_kernel<<<1, 1024, use_smem ? (size_t)nrows * sizeof(int) : 0, stream>>>(
@@ -599,11 +593,10 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int 
     void *tc_buf = (char *)w->buf + (panel_scratch_bytes() + 255) / 256 * 256;
     FG_CUDA(cudaMemsetAsync(ps.slots, 0, kSlotBytes, stream));
     unsigned long long epoch = 0;
-    static bool attr = false;
-    if (!attr) {
-        FG_CUDA(cudaFuncSetAttribute(panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)PANEL_SMEM_MAX));
-        attr = true;
+    static DeviceOnce once;
+    {
+        const int st0 = set_smem_once(once, (const void *)panel_kernel<T>, (int)PANEL_SMEM_MAX);
+        if (st0 != kOk) return st0;
     }
     int sms = num_sms();
     if (sms <= 0) {
@@ -859,12 +852,9 @@ int laswp_fixed(int nrows, int ncols, double *A, int ldA, int k1, int k2, const 
     double *tmp = (double *)((char *)scratch + permBytes);
     const int use_smem = (size_t)nrows * sizeof(int) <= 200 * 1024 ? 1 : 0;
     if (use_smem) {
-        static bool attr = false;
-        if (!attr) {
-            FG_CUDA(cudaFuncSetAttribute(laswp_perm_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-            attr = true;
-        }
+        static DeviceOnce once;
+        const int st0 = set_smem_once(once, (const void *)laswp_perm_kernel, 200 * 1024);
+        if (st0 != kOk) return st0;
     }
     KTimer kt(kFamLaswp, stream, 0.0, 2.0 * (double)nrows * ncols * 16.0);
     laswp_perm_kernel<<<1, 1024, use_smem ? (size_t)nrows * sizeof(int) : 0, stream>>>(

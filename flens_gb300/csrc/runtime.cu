@@ -219,6 +219,13 @@ void *workspace_slot(cudaStream_t stream, int slot, size_t bytes) {
     return w->slot_buf[slot];
 }
 
+int set_smem_once(DeviceOnce &once, const void *fn, int bytes) {
+    if (!once.pending()) return kOk;
+    FG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    once.done();
+    return kOk;
+}
+
 int check_device_status(cudaStream_t stream) {
     Workspace *w = workspace_for(stream, 0);
     if (!w) return kErrAlloc;

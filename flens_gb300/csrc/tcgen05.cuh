@@ -352,16 +352,11 @@ tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
 int make_kmajor_map(CUtensorMap *map, int kind, const void *base, int rows, int K, int ldo,
                     int box_rows);
 
-// Set the kernel's dynamic shared memory limit once per instantiation.
+// Set the kernel's dynamic shared memory limit once per instantiation and device.
 template <int KIND, class Epi>
 int prepare_kernel() {
-    static bool done = false;             // per instantiation; idempotent if raced
-    if (!done) {
-        FG_CUDA(cudaFuncSetAttribute(tc_kernel<KIND, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)SMEM));
-        done = true;
-    }
-    return kOk;
+    static DeviceOnce once;               // per instantiation and device
+    return set_smem_once(once, (const void *)tc_kernel<KIND, Epi>, (int)SMEM);
 }
 
 }  // namespace tc
