@@ -78,8 +78,10 @@ int dtrmm_launch(char side, char uplo, char transA, char diag, int m, int n, dou
     }
     FG_CUDA(cudaMemsetAsync(W, 0, (size_t)m * n * sizeof(double), s));
     const char ta = (transA == 'N' || transA == 'n') ? 'N' : 'T';
-    int st = left ? dgemm_launch(ta, 'N', m, n, m, 1.0, T, ka, B, ldB, 0.0, W, m, s)
-                  : dgemm_launch('N', ta, m, n, n, 1.0, B, ldB, T, ka, 0.0, W, m, s);
+    // op(T) is upper when T is upper and not transposed, or lower and transposed
+    const bool op_upper = (uplo == 'U' || uplo == 'u') == (ta == 'N');
+    int st = left ? dgemm_kr_launch(ta, 'N', m, n, m, 1.0, T, ka, B, ldB, 0.0, W, m, op_upper ? 1 : 2, s)
+                  : dgemm_kr_launch('N', ta, m, n, n, 1.0, B, ldB, T, ka, 0.0, W, m, op_upper ? 3 : 4, s);
     if (st != kOk) return st;
     KTimer kt(kFamAux, s, (double)m * n, 16.0 * m * (double)n);
     scale_copy_kernel<<<grid_for((size_t)m * n), 256, 0, s>>>(m, n, alpha, W, B, ldB);

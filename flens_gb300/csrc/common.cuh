@@ -199,6 +199,12 @@ int dgemm_launch(char transA, char transB, int m, int n, int k, double alpha,
                  const double *A, int ldA, const double *B, int ldB,
                  double beta, double *C, int ldC, cudaStream_t stream);
 
+// dgemm with one triangular operand stored full (explicit zeros): kr 1/2 =
+// op(A) upper/lower, 3/4 = op(B) upper/lower; the zero k blocks are skipped.
+int dgemm_kr_launch(char transA, char transB, int m, int n, int k, double alpha,
+                    const double *A, int ldA, const double *B, int ldB, double beta,
+                    double *C, int ldC, int kr, cudaStream_t stream);
+
 int dtrsm_launch(char side, char upLo, char transA, char diag, int m, int n,
                  double alpha, const double *A, int ldA, double *B, int ldB,
                  cudaStream_t stream);

@@ -73,7 +73,11 @@ struct SlabLoader {
 // update to one triangle of a square C (syrk): 1 = lower (i >= j), 2 = upper
 // (i <= j); tiles wholly outside it exit at once and diagonal tiles store only
 // their part, so the other triangle of C is never written.
-template <typename T, bool TA, bool TB, int TRI = 0>
+// KR restricts the k range of each tile to where a triangular operand can be
+// nonzero (the skipped terms are exact zeros): 1 op(A) upper (k >= row),
+// 2 op(A) lower (k <= row), 3 op(B) upper (k <= column), 4 op(B) lower
+// (k >= column).
+template <typename T, bool TA, bool TB, int TRI = 0, int KR = 0>
 __global__ void __launch_bounds__(256)
 dgemm_fma_kernel(int m, int n, int k, T alpha,
                  const T *__restrict__ A, int ldA,
@@ -94,16 +98,20 @@ dgemm_fma_kernel(int m, int n, int k, T alpha,
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
 
-    const int nk = (k + BK - 1) / BK;
-    if (nk > 0) {
-        la.fetch(A, ldA, m0, m, 0, k);
-        lb.fetch(B, ldB, n0, n, 0, k);
+    int kb0 = 0, nk = (k + BK - 1) / BK;
+    if (KR == 1) kb0 = m0 / BK;
+    if (KR == 2) nk = min(nk, (m0 + BM + BK - 1) / BK);
+    if (KR == 3) nk = min(nk, (n0 + BN + BK - 1) / BK);
+    if (KR == 4) kb0 = n0 / BK;
+    if (kb0 < nk) {
+        la.fetch(A, ldA, m0, m, kb0 * BK, k);
+        lb.fetch(B, ldB, n0, n, kb0 * BK, k);
         la.store(As[0]);
         lb.store(Bs[0]);
         __syncthreads();
     }
-    for (int kt = 0; kt < nk; ++kt) {
-        const int cur = kt & 1;
+    for (int kt = kb0; kt < nk; ++kt) {
+        const int cur = (kt - kb0) & 1;
         if (kt + 1 < nk) {
             la.fetch(A, ldA, m0, m, (kt + 1) * BK, k);
             lb.fetch(B, ldB, n0, n, (kt + 1) * BK, k);
@@ -421,6 +429,41 @@ int gemm_launch_t(char transA, char transB, int m, int n, int k, T alpha, const 
         else if (!ta && tb) dgemm_fma_kernel<T, false, true><<<grid, 256, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
         else dgemm_fma_kernel<T, true, true><<<grid, 256, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
     }
+    FG_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+// C <- beta*C + alpha*op(A)*op(B) where one operand is a triangle stored as
+// a full matrix with explicit zeros: kr (1..4, see dgemm_fma_kernel) skips
+// the k blocks that only meet those zeros.  FMA engine, n > 16.
+int dgemm_kr_launch(char transA, char transB, int m, int n, int k, double alpha, const double *A,
+                    int ldA, const double *B, int ldB, double beta, double *C, int ldC, int kr,
+                    cudaStream_t stream) {
+    if (n <= 16 || kr < 1 || kr > 4 || pick_engine() != Engine::Fma)
+        return gemm_launch_t<double>(transA, transB, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC,
+                                     stream);
+    if (m == 0 || n == 0) return kOk;
+    if (alpha == 0.0) return scal_matrix_launch_t<double>(m, n, beta, C, ldC, stream);
+    const bool ta = !(transA == 'N' || transA == 'n');
+    const bool tb = !(transB == 'N' || transB == 'n');
+    const dim3 grid(ceil_div(m, BM), ceil_div(n, BN));
+    if (grid.y > 65535) {
+        set_last_error("gemm: n=%d too large for one launch", n);
+        return kErrUnsupported;
+    }
+    // the triangle's half of the flops
+    KTimer kt(kFamGemm, stream, 1.0 * m * n * (double)k,
+              8.0 * ((double)m * k + (double)k * n + 2.0 * m * n));
+    trace("gemm %c%c m=%d n=%d k=%d engine=fma k-range=%d", transA, transB, m, n, k, kr);
+#define FG_KR(TA_, TB_, K_) dgemm_fma_kernel<double, TA_, TB_, 0, K_><<<grid, 256, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC)
+#define FG_KR4(TA_, TB_) switch (kr) { case 1: FG_KR(TA_, TB_, 1); break; case 2: FG_KR(TA_, TB_, 2); break; \
+                                       case 3: FG_KR(TA_, TB_, 3); break; default: FG_KR(TA_, TB_, 4); }
+    if (!ta && !tb) { FG_KR4(false, false) }
+    else if (ta && !tb) { FG_KR4(true, false) }
+    else if (!ta && tb) { FG_KR4(false, true) }
+    else { FG_KR4(true, true) }
+#undef FG_KR4
+#undef FG_KR
     FG_CUDA(cudaGetLastError());
     return kOk;
 }

@@ -4,12 +4,14 @@
 // Follows FLENS-LAPACK:
 //   trtri  flens/lapack/tr/tri.tcc (generic tri_impl): a non-unit matrix with
 //          an exactly zero diagonal element returns its 1-based index and is
-//          left untouched; block size 64 (ilaenv TRTRI); upper: for each
+//          left untouched; block size 64 (ilaenv TRTRI), here inside outer
+//          blocks of 512 so that the trmm / trsm calls are wide; upper: for each
 //          block column j (forward) U12 <- U11^-1 U12 (trmm with the already
 //          inverted U11), U12 <- -U12 U22^-1 (trsm), then the diagonal block
 //          is inverted (ti2, flens/lapack/tr/ti2.tcc); lower runs backward.
 //   getri  flens/lapack/ge/tri.tcc (generic tri_impl): inv(U) by trtri, then
-//          for each block column J from the last: the strictly lower part of
+//          for each block column J from the last (512 columns here, 64 in
+//          the reference; the same operations in exact arithmetic): the strictly lower part of
 //          A(:,J) (the L factor) is moved to a workspace and zeroed,
 //          A(:,J) -= A(:, after J) * Work(after J, :) (gemm),
 //          A(:,J) <- A(:,J) * Wunit(J)^-1 (trsm with the unit lower block),
@@ -21,7 +23,8 @@ namespace fg {
 
 namespace {
 
-constexpr int TRI_NB = 64;
+constexpr int TRI_NB = 64;       // diagonal blocks of the inner loop (trti2 size)
+constexpr int TRI_OUTER = 512;   // outer block: the trmm / gemm / trsm calls get n >= 512 columns
 
 // In-place inverse of the jb x jb (jb <= 64) triangular block at A (ti2):
 // upper: for j = 0.., A(j,j) <- 1/A(j,j) (non-unit), u = A(0:j, j) <-
@@ -144,6 +147,50 @@ int *pinned_int() {
 
 }  // namespace
 
+namespace {
+
+// The blocked inverse of the k x k triangle at A in place (no zero check):
+// block columns of `nb` (forward for upper, backward for lower), each
+// U12 <- U11^-1 U12 (trmm with the part already inverted), U12 <- -U12 U22^-1
+// (trsm), then the diagonal block -- by trti2 when nb is the inner size,
+// else recursively with the inner size.
+int trtri_blocked(bool upper, bool unit, int k, double *A, int ldA, int nb, cudaStream_t s) {
+    const char dg = unit ? 'U' : 'N';
+    int st;
+    auto diag_block = [&](int jb, double *D) -> int {
+        return nb == TRI_NB ? trti2(jb, D, ldA, upper, unit, s) : trtri_blocked(upper, unit, jb, D, ldA, TRI_NB, s);
+    };
+    if (k <= nb) return diag_block(k, A);
+    if (upper) {
+        for (int j = 0; j < k; j += nb) {
+            const int jb = k - j < nb ? k - j : nb;
+            double *A12 = A + (size_t)j * ldA, *A22 = A + j + (size_t)j * ldA;
+            if (j > 0) {
+                if ((st = dtrmm_launch('L', 'U', 'N', dg, j, jb, 1.0, A, ldA, A12, ldA, s)) != kOk) return st;
+                if ((st = dtrsm_launch('R', 'U', 'N', dg, j, jb, -1.0, A22, ldA, A12, ldA, s)) != kOk) return st;
+            }
+            if ((st = diag_block(jb, A22)) != kOk) return st;
+        }
+    } else {
+        const int nn = ((k - 1) / nb) * nb;
+        for (int j = nn; j >= 0; j -= nb) {
+            const int jb = k - j < nb ? k - j : nb;
+            double *A11 = A + j + (size_t)j * ldA;
+            if (j + jb < k) {
+                const int r = k - j - jb;
+                double *A21 = A + (j + jb) + (size_t)j * ldA;
+                double *A22 = A + (j + jb) + (size_t)(j + jb) * ldA;
+                if ((st = dtrmm_launch('L', 'L', 'N', dg, r, jb, 1.0, A22, ldA, A21, ldA, s)) != kOk) return st;
+                if ((st = dtrsm_launch('R', 'L', 'N', dg, r, jb, -1.0, A11, ldA, A21, ldA, s)) != kOk) return st;
+            }
+            if ((st = diag_block(jb, A11)) != kOk) return st;
+        }
+    }
+    return kOk;
+}
+
+}  // namespace
+
 int dtrtri_launch(char uplo, char diag, int n, double *A, int ldA, int *info, cudaStream_t s) {
     const bool upper = uplo == 'U' || uplo == 'u';
     const bool unit = diag == 'U' || diag == 'u';
@@ -164,34 +211,9 @@ int dtrtri_launch(char uplo, char diag, int n, double *A, int ldA, int *info, cu
         set_int_kernel<<<1, 1, 0, s>>>(info, 0);
         FG_CUDA(cudaGetLastError());
     }
-    const char dg = unit ? 'U' : 'N';
-    int st;
-    if (n <= TRI_NB) return trti2(n, A, ldA, upper, unit, s);
-    if (upper) {
-        for (int j = 0; j < n; j += TRI_NB) {
-            const int jb = n - j < TRI_NB ? n - j : TRI_NB;
-            double *A12 = A + (size_t)j * ldA, *A22 = A + j + (size_t)j * ldA;
-            if (j > 0) {
-                if ((st = dtrmm_launch('L', 'U', 'N', dg, j, jb, 1.0, A, ldA, A12, ldA, s)) != kOk) return st;
-                if ((st = dtrsm_launch('R', 'U', 'N', dg, j, jb, -1.0, A22, ldA, A12, ldA, s)) != kOk) return st;
-            }
-            if ((st = trti2(jb, A22, ldA, true, unit, s)) != kOk) return st;
-        }
-    } else {
-        const int nn = ((n - 1) / TRI_NB) * TRI_NB;
-        for (int j = nn; j >= 0; j -= TRI_NB) {
-            const int jb = n - j < TRI_NB ? n - j : TRI_NB;
-            double *A11 = A + j + (size_t)j * ldA;
-            if (j + jb < n) {
-                const int r = n - j - jb;
-                double *A21 = A + (j + jb) + (size_t)j * ldA;
-                double *A22 = A + (j + jb) + (size_t)(j + jb) * ldA;
-                if ((st = dtrmm_launch('L', 'L', 'N', dg, r, jb, 1.0, A22, ldA, A21, ldA, s)) != kOk) return st;
-                if ((st = dtrsm_launch('R', 'L', 'N', dg, r, jb, -1.0, A11, ldA, A21, ldA, s)) != kOk) return st;
-            }
-            if ((st = trti2(jb, A11, ldA, false, unit, s)) != kOk) return st;
-        }
-    }
+    // outer blocks of 512 (wide trmm/trsm calls), 64-column blocks inside
+    const int st = trtri_blocked(upper, unit, n, A, ldA, n > TRI_OUTER ? TRI_OUTER : TRI_NB, s);
+    if (st != kOk) return st;
     trace("trtri %c%c n=%d", uplo, diag, n);
     return kOk;
 }
@@ -204,12 +226,15 @@ int dgetri_launch(int n, double *A, int ldA, const int *ipiv, int *info, cudaStr
     FG_CUDA(cudaMemcpyAsync(h, info, sizeof(int), cudaMemcpyDeviceToHost, s));
     FG_CUDA(cudaStreamSynchronize(s));
     if (*h != 0) return kOk;                        // singular U: A holds the factors
-    const int jbmax = n < TRI_NB ? n : TRI_NB;
+    // block columns of 512: the gemm and trsm calls then have 512 columns
+    // (the reference's 64-column blocks give 64-column calls with long k)
+    const int nbg = n > TRI_OUTER ? TRI_OUTER : TRI_NB;
+    const int jbmax = n < nbg ? n : nbg;
     double *W = (double *)workspace_slot(s, 1, (size_t)n * jbmax * sizeof(double));
     if (!W) return kErrAlloc;
-    const int nn = ((n - 1) / TRI_NB) * TRI_NB;
-    for (int j = nn; j >= 0; j -= TRI_NB) {
-        const int jb = n - j < TRI_NB ? n - j : TRI_NB;
+    const int nn = ((n - 1) / nbg) * nbg;
+    for (int j = nn; j >= 0; j -= nbg) {
+        const int jb = n - j < nbg ? n - j : nbg;
         {
             KTimer kt(kFamAux, s, 0.0, 24.0 * n * (double)jb);
             take_lower_kernel<<<grid_for((size_t)n * jb), 256, 0, s>>>(n, j, jb, A, ldA, W, n);

@@ -42,6 +42,34 @@ def test_getri_vs_reference(golden, port):
         assert oracle.normwise_rel(LU, golden[name]) <= 1e-12, name
 
 
+@pytest.mark.parametrize("uplo", "UL")
+@pytest.mark.parametrize("diag", "NU")
+def test_trtri_outer_blocks_vs_oracle(port, uplo, diag):
+    # n > 512: outer blocks of 512 around the 64-column inner algorithm
+    n = 1100
+    A0 = G.tri_input(3, n)
+    A = A0.copy(order="F")
+    assert fg.dtrtri(uplo, diag, A) == 0
+    R = A0.copy(order="F")
+    port.dtrtri(uplo, diag, R)
+    mask = np.triu(np.ones((n, n))) if uplo == "U" else np.tril(np.ones((n, n)))
+    if diag == "U":
+        np.fill_diagonal(mask, 0)
+    assert np.array_equal(A[mask == 0], A0[mask == 0])
+    assert oracle.normwise_rel(A * mask, R * mask) <= 1e-12
+
+
+def test_getri_outer_blocks_vs_oracle(port):
+    n = 1100
+    LU = G.getri_input(4, n)
+    piv, info = port.dgetrf(LU)
+    assert info == 0
+    R = LU.copy(order="F")
+    port.dgetri(R, piv)
+    assert fg.dgetri(LU, piv) == 0
+    assert oracle.normwise_rel(LU, R) <= 1e-12
+
+
 def test_zero_pivot_info():
     A = G.tri_input(0, 70)
     A[40, 40] = 0.0
