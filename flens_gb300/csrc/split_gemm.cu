@@ -290,6 +290,8 @@ struct SplitGeom {
 // a tile are summed in W (S = S + v, one FP64 add per element and group, the
 // first group stores v); the last group finishes C = (beta*C) + (alpha*S).
 struct EpiSplit {
+    static constexpr int kBN = 256;
+    static constexpr int kTmemExtra = 0;
     SplitGeom geo;
     double alpha, beta;
     double *C;
@@ -307,7 +309,7 @@ struct EpiSplit {
         nk = (shi - slo + 1) * ((k1 - k0) / kBK);
     }
     __device__ void apply(int g, int row, bool row_ok, int col, int ncol,
-                          const uint32_t (&r)[32]) const {
+                          const uint32_t (&r)[32], uint32_t) const {
         int dg, slo, shi, k0, k1;
         geo.decode(g, dg, slo, shi, k0, k1);
         const bool first = g == 0, last = g == geo.ngroups - 1;
@@ -318,8 +320,8 @@ struct EpiSplit {
         const size_t r0 = (size_t)(row_ok ? row : 0);
         // this CTA's own tile of group sums, reused for each of its tiles: it
         // stays in L2 (152 x 256 KB) instead of spanning m x n
-        double *wrow = W + (size_t)blockIdx.x * (tc::BM * tc::BN) + (r0 & (tc::BM - 1)) +
-                       (size_t)(col & (tc::BN - 1)) * tc::BM;
+        double *wrow = W + (size_t)blockIdx.x * (tc::BM * kBN) + (r0 & (tc::BM - 1)) +
+                       (size_t)(col & (kBN - 1)) * tc::BM;
         double *crow = C + r0 + (size_t)col * ldc;
 #pragma unroll
         for (int h = 0; h < 32; h += 16) {
@@ -356,6 +358,7 @@ struct EpiSplit {
 };
 
 size_t round256(size_t b) { return (b + 255) / 256 * 256; }
+
 
 // ceil(log2(x)) for x >= 1, exact (frexp based)
 int ceil_log2(double x) {
@@ -477,20 +480,19 @@ int dgemm_split_launch_at(char transA, char transB, int m, int n, int k, double 
     CUtensorMap ma, mb;
     int rc = tc::make_kmajor_map(&ma, kTcBF16, Ad, m, (int)ldS, (int)ldS, tc::BM);
     if (rc != kOk) return rc;
-    if ((rc = tc::make_kmajor_map(&mb, kTcBF16, Bd, n, (int)ldS, (int)ldS, tc::BN)) != kOk) return rc;
+    if ((rc = tc::make_kmajor_map(&mb, kTcBF16, Bd, n, (int)ldS, (int)ldS, EpiSplit::kBN)) != kOk) return rc;
     if ((rc = tc::prepare_kernel<kTcBF16, EpiSplit>()) != kOk) return rc;
-    const int ntiles = ceil_div(m, tc::BM) * ceil_div(n, tc::BN);
+    const int ntiles = ceil_div(m, tc::BM) * ceil_div(n, EpiSplit::kBN);
     const int grid = ntiles < num_sms() ? ntiles : num_sms();
-    double *W = (double *)workspace_slot(s, 2, (size_t)grid * tc::BM * tc::BN * sizeof(double));
+    double *W = (double *)workspace_slot(s, 2, (size_t)grid * tc::BM * EpiSplit::kBN * sizeof(double));
     if (!W) return kErrAlloc;
     const EpiSplit epi{geo, alpha, beta, C, ldC, W, tc::BM, ea, eb};
     const double pairs = (double)S * (S + 1) / 2;
-    {
-        KTimer kt(kFamSplit, s, 2.0 * pairs * m * (double)n * geo.Kp,
-                  2.0 * ldS * ((double)m + n) + 16.0 * m * (double)n);   // digits in, C in + out
-        tc::tc_kernel<kTcBF16, EpiSplit><<<grid, tc::THREADS, tc::SMEM, s>>>(ma, mb, m, n, epi, w->status);
-        FG_CUDA(cudaGetLastError());
-    }
+    KTimer kt(kFamSplit, s, 2.0 * pairs * m * (double)n * geo.Kp,
+              2.0 * ldS * ((double)m + n) + 16.0 * m * (double)n);   // digits in, C in + out
+    tc::tc_kernel<kTcBF16, EpiSplit><<<grid, tc::THREADS, tc::Shape<EpiSplit>::SMEM, s>>>(
+        ma, mb, m, n, epi, w->status);
+    FG_CUDA(cudaGetLastError());
     trace("dgemm_split: m=%d n=%d k=%d bits=%d S=%d groups=%d", m, n, k, bits, S, geo.ngroups);
     if (slices_used) *slices_used = S;
     return kOk;

@@ -28,6 +28,8 @@ using tc::BN;
 
 // FP32 output: C = alpha * acc * (sa_i * sb_j) + beta * C, one group over K.
 struct EpiF32 {
+    static constexpr int kBN = 256;
+    static constexpr int kTmemExtra = 0;
     float alpha, beta;
     float *C;
     int ldc;
@@ -41,7 +43,7 @@ struct EpiF32 {
         nk = nkb;
     }
     __device__ void apply(int, int row, bool row_ok, int col, int ncol,
-                          const uint32_t (&r)[32]) const {
+                          const uint32_t (&r)[32], uint32_t) const {
         if (!row_ok) return;
         const float sa = scale_a != nullptr ? scale_a[row] : 1.0f;
         float *crow = C + (size_t)row + (size_t)col * ldc;
@@ -271,7 +273,8 @@ int tc_gemm_launch(int kind, int M, int N, int K, float alpha, const void *A_lp,
 #define FG_TC(KD)                                                                               \
     do {                                                                                        \
         if ((st = tc::prepare_kernel<KD, EpiF32>()) != kOk) return st;                          \
-        tc::tc_kernel<KD, EpiF32><<<grid, tc::THREADS, tc::SMEM, stream>>>(ma, mb, M, N, epi,   \
+        tc::tc_kernel<KD, EpiF32><<<grid, tc::THREADS, tc::Shape<EpiF32>::SMEM, stream>>>(      \
+            ma, mb, M, N, epi,                                                                  \
                                                                          w->status);           \
     } while (0)
     if (kind == kTcTF32) FG_TC(kTcTF32);

@@ -3,8 +3,8 @@
 // by the FP32-output GEMM (tc_gemm.cu) and the split-precision FP64 GEMM
 // (split_gemm.cu).
 //
-// Kernel shape: persistent, one CTA per SM over 128 x 256 output tiles,
-// 320 threads:
+// Kernel shape: persistent, one CTA per SM over 128 x BN output tiles (BN =
+// 256, or 128 for a policy that keeps state in TMEM), 320 threads:
 //   warp 0 lane 0  TMA producer: 128B-swizzled K-major tiles of A (128 rows)
 //                  and B (256 rows) into a STAGES-deep shared-memory ring,
 //                  one mbarrier (expect_tx) per stage;
@@ -39,15 +39,26 @@ enum TcKind : int { kTcTF32 = 0, kTcBF16 = 1, kTcFP8 = 2, kTcF32x3 = 3, kTcTF32L
 namespace tc {
 
 constexpr int BM = 128;
-constexpr int BN = 256;
-constexpr int STAGES = 4;
+constexpr int BN = 256;                         // the default tile width
 constexpr int THREADS = 320;                    // 10 warps: TMA, MMA, 8 epilogue
 constexpr int EPI_WARPS = 8;
 constexpr int BAND = 16;                        // tile rows per raster band
 constexpr uint32_t kMbarSpinLimit = 1u << 20;
 constexpr uint32_t A_BYTES = BM * 128;          // one stage of A: 128 rows x 128 B
-constexpr uint32_t B_BYTES = BN * 128;          // one stage of B: BN rows x 128 B
-constexpr size_t SMEM = 1024 + (size_t)STAGES * (A_BYTES + B_BYTES) + 256;
+
+// Per epilogue policy: the tile width Epi::kBN (128 or 256) and
+// Epi::kTmemExtra TMEM columns the policy keeps beside the two accumulators.
+template <class Epi>
+struct Shape {
+    static constexpr int BN = Epi::kBN;
+    static constexpr int STAGES = BN >= 256 ? 4 : 6;      // ~192 KB of operand ring
+    static constexpr uint32_t B_BYTES = BN * 128;          // one stage of B: BN rows x 128 B
+    static constexpr size_t SMEM = 1024 + (size_t)STAGES * (A_BYTES + B_BYTES) + 256;
+    static constexpr uint32_t TMEM_COLS = 2 * BN + Epi::kTmemExtra;
+    static_assert(TMEM_COLS == 512 || TMEM_COLS == 256 || TMEM_COLS == 128,
+                  "TMEM allocation must be a power of two <= 512 columns");
+    static_assert(SMEM <= 227 * 1024, "shared memory per CTA");
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -167,25 +178,33 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 // Output tile t -> (m0, n0): bands of BAND tile rows, tile rows fastest
 // inside a band, so consecutive tiles (one wave of CTAs) cover a near-square
 // block of C.
-__device__ __forceinline__ void tile_origin(int t, int tiles_m, int tiles_n, int &m0, int &n0) {
+__device__ __forceinline__ void tile_origin(int t, int tiles_m, int tiles_n, int bn, int &m0, int &n0) {
     const int per_band = BAND * tiles_n;
     const int b = t / per_band, r = t - b * per_band;
     const int bm = min(BAND, tiles_m - b * BAND);
     m0 = (b * BAND + r % bm) * BM;
-    n0 = (r / bm) * BN;
+    n0 = (r / bm) * bn;
 }
 
 // Epi policy interface (all __device__, const):
 //   int  groups() const                          work items per tile (>= 1)
 //   void group(int g, int &ka, int &kb, int &nk) k offset (elements) of A and
 //                                                of B, number of k-blocks
-//   void apply(int g, int row, bool row_ok, int col, int ncol, const uint32_t (&r)[32])
+//   void apply(int g, int row, bool row_ok, int col, int ncol, const uint32_t (&r)[32],
+//              uint32_t xt)
 //        called by all 32 lanes of an epilogue warp for 32 accumulator
-//        columns col..col+31 of tile row `row` (ncol of them inside C).
+//        columns col..col+31 of tile row `row` (ncol of them inside C); xt is
+//        the TMEM address of the policy's own kTmemExtra columns for this
+//        warp's lane quarter (tile-local column 0).
+//   static constexpr int kBN, kTmemExtra (see Shape)
 template <int KIND, class Epi>
 __global__ void __launch_bounds__(THREADS, 1)
 tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M,
           int N, const __grid_constant__ Epi epi, int *__restrict__ status) {
+    constexpr int BN = Shape<Epi>::BN;
+    constexpr int STAGES = Shape<Epi>::STAGES;
+    constexpr uint32_t B_BYTES = Shape<Epi>::B_BYTES;
+    constexpr uint32_t TMEM_COLS = Shape<Epi>::TMEM_COLS;
     constexpr int ELEM = KIND == kTcTF32 ? 4 : KIND == kTcBF16 ? 2 : 1;
     constexpr int BK = 128 / ELEM;               // elements per 128-byte row (one k-block)
     constexpr int KSTEPS = 4;                    // 32 bytes of K per MMA
@@ -220,7 +239,7 @@ tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(tmem_slot)),
-                     "r"((uint32_t)(2 * BN))
+                     "r"(TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -236,7 +255,7 @@ tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 int m0, n0;
-                tile_origin(t, tiles_m, tiles_n, m0, n0);
+                tile_origin(t, tiles_m, tiles_n, BN, m0, n0);
                 for (int g = 0; g < ngroups && ok; ++g) {
                     int ka, kb, nk;
                     epi.group(g, ka, kb, nk);
@@ -309,7 +328,7 @@ tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
         bool live = true;
         for (int t = blockIdx.x; t < ntiles && live; t += gridDim.x) {
             int m0, n0;
-            tile_origin(t, tiles_m, tiles_n, m0, n0);
+            tile_origin(t, tiles_m, tiles_n, BN, m0, n0);
             const int row = m0 + quarter * 32 + lane;
             for (int g = 0; g < ngroups; ++g, ++i) {
                 const int b = i & 1;
@@ -319,12 +338,14 @@ tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
                     break;
                 }
                 fence_after();
-                const uint32_t base = tmem + (uint32_t)(b * BN) + ((uint32_t)(quarter * 32) << 16);
+                const uint32_t lanes = (uint32_t)(quarter * 32) << 16;
+                const uint32_t base = tmem + (uint32_t)(b * BN) + lanes;
+                const uint32_t xt = tmem + (uint32_t)(2 * BN) + lanes;
                 for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
                     if (n0 + c0 >= N) break;     // uniform across the warp
                     uint32_t r[32];
                     tmem_ld32(base + (uint32_t)c0, r);
-                    epi.apply(g, row, row < M, n0 + c0, min(32, N - (n0 + c0)), r);
+                    epi.apply(g, row, row < M, n0 + c0, min(32, N - (n0 + c0)), r, xt);
                 }
                 fence_before();
                 __syncwarp();
@@ -342,7 +363,7 @@ tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
     __syncthreads();
     if (warp == 1) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                     "r"((uint32_t)(2 * BN))
+                     "r"(TMEM_COLS)
                      : "memory");
     }
 }
@@ -356,7 +377,7 @@ int make_kmajor_map(CUtensorMap *map, int kind, const void *base, int rows, int 
 template <int KIND, class Epi>
 int prepare_kernel() {
     static DeviceOnce once;               // per instantiation and device
-    return set_smem_once(once, (const void *)tc_kernel<KIND, Epi>, (int)SMEM);
+    return set_smem_once(once, (const void *)tc_kernel<KIND, Epi>, (int)Shape<Epi>::SMEM);
 }
 
 }  // namespace tc
