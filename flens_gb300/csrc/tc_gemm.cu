@@ -96,7 +96,7 @@ __device__ __forceinline__ void store_lp<kTcFP8>(void *out, size_t idx, float v)
 template <int KIND, bool RCONTIG>
 __global__ void __launch_bounds__(256)
 to_kmajor_kernel(int R, int K, const float *__restrict__ in, int ld, void *__restrict__ out,
-                 int ldo, const float *__restrict__ inv_scale) {
+                 int ldo, int width, const float *__restrict__ inv_scale) {
     __shared__ float tile[32][33];
     const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
@@ -108,7 +108,7 @@ to_kmajor_kernel(int R, int K, const float *__restrict__ in, int ld, void *__res
         __syncthreads();
         for (int rr = ty; rr < 32; rr += 8) {
             const int r = r0 + rr, k = k0 + tx;
-            if (r < R && k < ldo) {
+            if (r < R && k < width) {
                 float v = tile[tx][rr];
                 if (inv_scale) v *= inv_scale[r];
                 store_lp<KIND>(out, (size_t)r * ldo + k, v);
@@ -117,7 +117,7 @@ to_kmajor_kernel(int R, int K, const float *__restrict__ in, int ld, void *__res
     } else {
         for (int rr = ty; rr < 32; rr += 8) {
             const int r = r0 + rr, k = k0 + tx;
-            if (r < R && k < ldo) {
+            if (r < R && k < width) {
                 float v = (k < K) ? in[(size_t)k + (size_t)r * ld] : 0.0f;
                 if (inv_scale) v *= inv_scale[r];
                 store_lp<KIND>(out, (size_t)r * ldo + k, v);
@@ -217,9 +217,11 @@ size_t tc_elem_bytes(int kind) {
 }
 
 // Convert op(X) (R x K, FP32, column-major storage, transposed or not) to a
-// K-major low-precision operand.  For FP8, also computes per-row scales.
+// K-major low-precision operand: columns 0..width-1 of rows of stride ldo
+// (zero beyond K).  For FP8, also computes per-row scales.
 int tc_convert(int kind, bool trans, int R, int K, const float *X, int ldx, void *out, int ldo,
-               float *scale, float *inv_scale, cudaStream_t stream) {
+               float *scale, float *inv_scale, cudaStream_t stream, int width = -1) {
+    if (width < 0) width = ldo;
     if (R <= 0 || K <= 0) return kOk;
     KTimer kt(kFamAux, stream, 0.0, (4.0 + tc_elem_bytes(kind)) * R * (double)K);
     // op(X)(r, k): r-contiguous when X is stored R x K (no transpose)
@@ -230,12 +232,12 @@ int tc_convert(int kind, bool trans, int R, int K, const float *X, int ldx, void
         else row_scale_kernel<false><<<g, 256, 0, stream>>>(R, K, X, ldx, scale, inv_scale);
         FG_CUDA(cudaGetLastError());
     }
-    const dim3 grid(ceil_div(R, 32), ceil_div(ldo, 32));
+    const dim3 grid(ceil_div(R, 32), ceil_div(width, 32));
     const float *inv = kind == kTcFP8 ? inv_scale : nullptr;
 #define FG_CONV(KD)                                                                          \
     do {                                                                                     \
-        if (rcontig) to_kmajor_kernel<KD, true><<<grid, 256, 0, stream>>>(R, K, X, ldx, out, ldo, inv); \
-        else to_kmajor_kernel<KD, false><<<grid, 256, 0, stream>>>(R, K, X, ldx, out, ldo, inv);        \
+        if (rcontig) to_kmajor_kernel<KD, true><<<grid, 256, 0, stream>>>(R, K, X, ldx, out, ldo, width, inv); \
+        else to_kmajor_kernel<KD, false><<<grid, 256, 0, stream>>>(R, K, X, ldx, out, ldo, width, inv);        \
     } while (0)
     if (kind == kTcTF32) FG_CONV(kTcTF32);
     else if (kind == kTcTF32Lo) FG_CONV(kTcTF32Lo);
@@ -288,14 +290,37 @@ int tc_gemm_launch(int kind, int M, int N, int K, float alpha, const void *A_lp,
 static size_t round256(size_t b) { return (b + 255) / 256 * 256; }
 
 size_t tc_update_workspace_bytes(int kind, int m, int n, int k) {
-    const int ld = tc_kmajor_ld(kind, k);
+    int ld = tc_kmajor_ld(kind, k);
+    if (kind == kTcF32x3) ld *= 3;                 // three K segments, see f32x3_gemm
     const size_t eb = tc_elem_bytes(kind);
     const size_t a = round256((size_t)m * ld * eb), b = round256((size_t)n * ld * eb);
     size_t total = a + b;
-    if (kind == kTcF32x3) total *= 2;
     if (kind == kTcFP8) total += round256((size_t)(m + n) * 2 * sizeof(float));
     return total;
 }
+
+namespace {
+
+// FP32-accurate product as ONE TF32 GEMM over K' = 3 kp: op(A) is stored as
+// [lo | hi | hi] and op(B)^T as [hi | lo | hi] along K, so the accumulator
+// sums lo*hi + hi*lo + hi*hi (the small terms first) and C is read and
+// written once (three separate products each read and wrote C).
+int f32x3_gemm(bool ta_rows, bool tb_rows, int m, int n, int k, float alpha, const float *A, int ldA,
+               const float *B, int ldB, float beta, float *C, int ldC, void *buf, cudaStream_t s) {
+    const int kp = tc_kmajor_ld(kTcTF32, k), ld3 = 3 * kp;
+    float *Ak = (float *)buf;
+    float *Bk = (float *)((char *)buf + round256((size_t)m * ld3 * sizeof(float)));
+    int st;
+    if ((st = tc_convert(kTcTF32Lo, ta_rows, m, k, A, ldA, Ak, ld3, nullptr, nullptr, s, kp))) return st;
+    if ((st = tc_convert(kTcTF32, ta_rows, m, k, A, ldA, Ak + kp, ld3, nullptr, nullptr, s, kp))) return st;
+    if ((st = tc_convert(kTcTF32, ta_rows, m, k, A, ldA, Ak + 2 * kp, ld3, nullptr, nullptr, s, kp))) return st;
+    if ((st = tc_convert(kTcTF32, tb_rows, n, k, B, ldB, Bk, ld3, nullptr, nullptr, s, kp))) return st;
+    if ((st = tc_convert(kTcTF32Lo, tb_rows, n, k, B, ldB, Bk + kp, ld3, nullptr, nullptr, s, kp))) return st;
+    if ((st = tc_convert(kTcTF32, tb_rows, n, k, B, ldB, Bk + 2 * kp, ld3, nullptr, nullptr, s, kp))) return st;
+    return tc_gemm_launch(kTcTF32, m, n, ld3, alpha, Ak, ld3, Bk, ld3, beta, C, ldC, nullptr, nullptr, s);
+}
+
+}  // namespace
 
 int tc_trailing_update(int kind, int m, int n, int k, const float *A21, int ldA21,
                        const float *U12, int ldU12, float *A22, int ldA22, void *buf,
@@ -307,17 +332,8 @@ int tc_trailing_update(int kind, int m, int n, int k, const float *A21, int ldA2
     char *p = (char *)buf;
     void *Ahi = p, *Bhi = p + a;
     int st;
-    if (kind == kTcF32x3) {
-        void *Alo = p + a + b, *Blo = p + 2 * a + b;
-        if ((st = tc_convert(kTcTF32, false, m, k, A21, ldA21, Ahi, ld, nullptr, nullptr, stream))) return st;
-        if ((st = tc_convert(kTcTF32Lo, false, m, k, A21, ldA21, Alo, ld, nullptr, nullptr, stream))) return st;
-        if ((st = tc_convert(kTcTF32, true, n, k, U12, ldU12, Bhi, ld, nullptr, nullptr, stream))) return st;
-        if ((st = tc_convert(kTcTF32Lo, true, n, k, U12, ldU12, Blo, ld, nullptr, nullptr, stream))) return st;
-        // small terms first, then the head product
-        if ((st = tc_gemm_launch(kTcTF32, m, n, k, -1.0f, Alo, ld, Bhi, ld, 1.0f, A22, ldA22, nullptr, nullptr, stream))) return st;
-        if ((st = tc_gemm_launch(kTcTF32, m, n, k, -1.0f, Ahi, ld, Blo, ld, 1.0f, A22, ldA22, nullptr, nullptr, stream))) return st;
-        return tc_gemm_launch(kTcTF32, m, n, k, -1.0f, Ahi, ld, Bhi, ld, 1.0f, A22, ldA22, nullptr, nullptr, stream);
-    }
+    if (kind == kTcF32x3)
+        return f32x3_gemm(false, true, m, n, k, -1.0f, A21, ldA21, U12, ldU12, 1.0f, A22, ldA22, buf, stream);
     float *sa = nullptr, *sia = nullptr, *sb = nullptr, *sib = nullptr;
     if (kind == kTcFP8) {
         sa = (float *)(p + a + b);
@@ -373,16 +389,8 @@ FG_API int flens_gb300_sgemm_tc(int precision, char transA, char transB, int m, 
     const size_t a = round256((size_t)m * ld * eb), b = round256((size_t)n * ld * eb);
     char *p = (char *)w->buf;
     int st;
-    if (precision == kTcF32x3) {
-        void *Ahi = p, *Bhi = p + a, *Alo = p + a + b, *Blo = p + 2 * a + b;
-        if ((st = tc_convert(kTcTF32, ta, m, k, A, ldA, Ahi, ld, nullptr, nullptr, s))) return st;
-        if ((st = tc_convert(kTcTF32Lo, ta, m, k, A, ldA, Alo, ld, nullptr, nullptr, s))) return st;
-        if ((st = tc_convert(kTcTF32, !tb, n, k, B, ldB, Bhi, ld, nullptr, nullptr, s))) return st;
-        if ((st = tc_convert(kTcTF32Lo, !tb, n, k, B, ldB, Blo, ld, nullptr, nullptr, s))) return st;
-        if ((st = tc_gemm_launch(kTcTF32, m, n, k, alpha, Alo, ld, Bhi, ld, beta, C, ldC, nullptr, nullptr, s))) return st;
-        if ((st = tc_gemm_launch(kTcTF32, m, n, k, alpha, Ahi, ld, Blo, ld, 1.0f, C, ldC, nullptr, nullptr, s))) return st;
-        return tc_gemm_launch(kTcTF32, m, n, k, alpha, Ahi, ld, Bhi, ld, 1.0f, C, ldC, nullptr, nullptr, s);
-    }
+    if (precision == kTcF32x3)
+        return f32x3_gemm(ta, !tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, p, s);
     void *Alp = p, *Blp = p + a;
     float *sa = nullptr, *sia = nullptr, *sb = nullptr, *sib = nullptr;
     if (precision == kTcFP8) {
