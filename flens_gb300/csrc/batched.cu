@@ -68,27 +68,40 @@ __device__ __forceinline__ void team_sync(int id, int nthreads) {
     else asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-__device__ __forceinline__ bool better(double v1, int i1, double v2, int i2) {
-    return v1 > v2 || (v1 == v2 && i1 < i2);
+// Pivot keys as integers (|x| orders like its bits; NaN below every number,
+// 0 = no candidate), so the search stays off the FP64 pipe.  (key, row)
+// "better than": larger key, on equal keys the smaller row -- cxxblas
+// iamax's first maximum (cxxblas/level1/iamax.tcc:52-56).
+__device__ __forceinline__ unsigned long long pivot_key(double x) {
+    const unsigned long long a = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+    return a > 0x7ff0000000000000ull ? 1ull : a + 2ull;
 }
 
-__device__ void team_argmax(double &v, int &i, int lt, int T, int bar, double *red_v, int *red_i) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const double ov = __shfl_down_sync(0xffffffffu, v, off);
-        const int oi = __shfl_down_sync(0xffffffffu, i, off);
-        if (better(ov, oi, v, i)) { v = ov; i = oi; }
-    }
-    v = __shfl_sync(0xffffffffu, v, 0);
-    i = __shfl_sync(0xffffffffu, i, 0);
+__device__ __forceinline__ bool better(unsigned long long k1, int i1, unsigned long long k2, int i2) {
+    return k1 > k2 || (k1 == k2 && i1 < i2);
+}
+
+// argmax over the warp with redux.sync (all 32 lanes call it)
+__device__ __forceinline__ void warp_argmax(unsigned long long &k, int &i) {
+    const unsigned hi = (unsigned)(k >> 32), lo = (unsigned)k;
+    const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+    const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
+    const unsigned cand = (hi == mhi && lo == mlo) ? (unsigned)i : 0xffffffffu;
+    i = (int)__reduce_min_sync(0xffffffffu, cand);
+    k = ((unsigned long long)mhi << 32) | mlo;
+}
+
+__device__ void team_argmax(unsigned long long &k, int &i, int lt, int T, int bar,
+                            unsigned long long *red_k, int *red_i) {
+    warp_argmax(k, i);
     if (T == 32) return;
     const int nw = T >> 5;
-    if ((lt & 31) == 0) { red_v[lt >> 5] = v; red_i[lt >> 5] = i; }
+    if ((lt & 31) == 0) { red_k[lt >> 5] = k; red_i[lt >> 5] = i; }
     team_sync(bar, T);
-    v = red_v[0];
+    k = red_k[0];
     i = red_i[0];
     for (int q = 1; q < nw; ++q)
-        if (better(red_v[q], red_i[q], v, i)) { v = red_v[q]; i = red_i[q]; }
+        if (better(red_k[q], red_i[q], k, i)) { k = red_k[q]; i = red_i[q]; }
     team_sync(bar, T);
 }
 
@@ -110,16 +123,16 @@ __device__ double team_max(double m, int lt, int T, int bar, double *red) {
 template <typename S>
 __device__ int team_gesv(int n, int k, S *M, int ldm, S *X, int ldx, int *piv, int lt, int T,
                          int bar, double *red_v, int *red_i) {
+    unsigned long long *red_k = (unsigned long long *)red_v;
     int info = 0;
     for (int j = 0; j < n; ++j) {
-        double bv = -2.0;
+        unsigned long long bv = 0ull;
         int bi = INT_MAX;
         for (int r = j + lt; r < n; r += T) {
-            const double a = fabs((double)M[r + (size_t)j * ldm]);
-            const double key = isnan(a) ? -1.0 : a;
+            const unsigned long long key = pivot_key((double)M[r + (size_t)j * ldm]);
             if (better(key, r, bv, bi)) { bv = key; bi = r; }
         }
-        team_argmax(bv, bi, lt, T, bar, red_v, red_i);
+        team_argmax(bv, bi, lt, T, bar, red_k, red_i);
         const double ajj = (double)M[j + (size_t)j * ldm];
         const int p = isnan(ajj) ? j : bi;      // iamax keeps element j if it is NaN
         if (lt == 0) piv[j] = p + 1;
@@ -143,10 +156,16 @@ __device__ int team_gesv(int n, int k, S *M, int ldm, S *X, int ldx, int *piv, i
             info = j + 1;
         }
         team_sync(bar, T);
-        const int m2 = n - j - 1;
-        for (int e = lt; e < m2 * m2; e += T) {
-            const int r = j + 1 + e % m2, c = j + 1 + e / m2;
-            M[r + (size_t)c * ldm] = fma(-M[j + (size_t)c * ldm], M[r + (size_t)j * ldm], M[r + (size_t)c * ldm]);
+        // rank-1 update: lane -> rows (32 apart), warp -> columns (T/32
+        // apart), so a warp touches consecutive rows of one column and there
+        // are no index divisions
+        {
+            const int tr = lt & 31, tc = lt >> 5, TC = T >> 5;
+            for (int r = j + 1 + tr; r < n; r += 32) {
+                const S l = M[r + (size_t)j * ldm];
+                for (int c = j + 1 + tc; c < n; c += TC)
+                    M[r + (size_t)c * ldm] = fma(-M[j + (size_t)c * ldm], l, M[r + (size_t)c * ldm]);
+            }
         }
         team_sync(bar, T);
     }
@@ -163,20 +182,17 @@ __device__ int team_gesv(int n, int k, S *M, int ldm, S *X, int ldx, int *piv, i
         }
     }
     for (int i = 0; i < n; ++i) {                          // unit lower
-        const int m2 = n - i - 1;
-        for (int e = lt; e < m2 * k; e += T) {
-            const int r = i + 1 + e % m2, c = e / m2;
-            X[r + (size_t)c * ldx] = fma(-M[r + (size_t)i * ldm], X[i + (size_t)c * ldx], X[r + (size_t)c * ldx]);
-        }
+        for (int c = 0; c < k; ++c)
+            for (int r = i + 1 + lt; r < n; r += T)
+                X[r + (size_t)c * ldx] = fma(-M[r + (size_t)i * ldm], X[i + (size_t)c * ldx], X[r + (size_t)c * ldx]);
         team_sync(bar, T);
     }
     for (int i = n - 1; i >= 0; --i) {                     // upper
         for (int c = lt; c < k; c += T) X[i + (size_t)c * ldx] = X[i + (size_t)c * ldx] / M[i + (size_t)i * ldm];
         team_sync(bar, T);
-        for (int e = lt; e < i * k; e += T) {
-            const int r = e % i, c = e / i;
-            X[r + (size_t)c * ldx] = fma(-M[r + (size_t)i * ldm], X[i + (size_t)c * ldx], X[r + (size_t)c * ldx]);
-        }
+        for (int c = 0; c < k; ++c)
+            for (int r = lt; r < i; r += T)
+                X[r + (size_t)c * ldx] = fma(-M[r + (size_t)i * ldm], X[i + (size_t)c * ldx], X[r + (size_t)c * ldx]);
         team_sync(bar, T);
     }
     return 0;
@@ -197,20 +213,15 @@ __device__ void team_lu_solve32(int n, int k, const float *M, const int *piv, fl
         }
     }
     for (int i = 0; i < n; ++i) {
-        const int m2 = n - i - 1;
-        for (int e = lt; e < m2 * k; e += T) {
-            const int r = i + 1 + e % m2, c = e / m2;
-            X[r + (size_t)c * n] -= M[r + (size_t)i * n] * X[i + (size_t)c * n];
-        }
+        for (int c = 0; c < k; ++c)
+            for (int r = i + 1 + lt; r < n; r += T) X[r + (size_t)c * n] -= M[r + (size_t)i * n] * X[i + (size_t)c * n];
         team_sync(bar, T);
     }
     for (int i = n - 1; i >= 0; --i) {
         for (int c = lt; c < k; c += T) X[i + (size_t)c * n] /= M[i + (size_t)i * n];
         team_sync(bar, T);
-        for (int e = lt; e < i * k; e += T) {
-            const int r = e % i, c = e / i;
-            X[r + (size_t)c * n] -= M[r + (size_t)i * n] * X[i + (size_t)c * n];
-        }
+        for (int c = 0; c < k; ++c)
+            for (int r = lt; r < i; r += T) X[r + (size_t)c * n] -= M[r + (size_t)i * n] * X[i + (size_t)c * n];
         team_sync(bar, T);
     }
 }
