@@ -332,6 +332,7 @@ def our_arm(args, rank: int, world: int) -> None:
         if not args.quick and not args.no_cholesky:
             result["cholesky_fp64"] = cholesky_subbench(torch, fg, dev)
             result["inverse_fp64"] = inverse_subbench(torch, fg, dev)
+            result["blas3_fp64"] = blas3_subbench(torch, fg, dev)
         if not args.quick and not args.no_batched:
             result["batched_config5"] = batched_subbench(torch, fg, dev, count=args.batch_count)
         # -- e2e through the Fortran ABI with pinned host buffers
@@ -564,6 +565,50 @@ def split_subbench(torch, fg, dev, n=8192, Es=(0, 16, 48), reps=5, ref_slices=14
     out["plain_fp64_dgemm"] = {"ms": plain_ms, "tflops": 2.0 * n ** 3 / (plain_ms * 1e-3) / 1e12,
                                "cublas_fp64_tflops": cublas_tflops}
     out["bf16_peak_tflops"] = {"value": peak, "source": f"{peak_src} (MEASURED_PEAKS.json bf16_tflops)"}
+    return out
+
+
+def blas3_subbench(torch, fg, dev, n=4096, reps=3):
+    """Level-3 BLAS at n = 4096 (FP64, column-major, device memory, L2
+    flushed by the 128 MiB operands): gemm in its four transpose variants,
+    syrk, syr2k, trmm, symm through the flens_gb300_* entry points, each as
+    TFLOP/s of its algorithmic count (gemm, symm 2n^3; syrk n^3, syr2k 2n^3,
+    trmm n^3)."""
+    import ctypes
+    L = fg.lib()
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    g = torch.Generator(device=dev)
+    g.manual_seed(33)
+    mk = lambda: fg.to_colmajor(torch.rand((n, n), generator=g, dtype=torch.float64, device=dev) - 0.5)
+    A, B, C = mk(), mk(), mk()
+    calls = {
+        "gemm NN": (2.0, lambda: L.flens_gb300_dgemm(b"N", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.5, C.data_ptr(), n, sp)),
+        "gemm NT": (2.0, lambda: L.flens_gb300_dgemm(b"N", b"T", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.5, C.data_ptr(), n, sp)),
+        "gemm TN": (2.0, lambda: L.flens_gb300_dgemm(b"T", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.5, C.data_ptr(), n, sp)),
+        "gemm TT": (2.0, lambda: L.flens_gb300_dgemm(b"T", b"T", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.5, C.data_ptr(), n, sp)),
+        "syrk LN": (1.0, lambda: L.flens_gb300_dsyrk(b"L", b"N", n, n, 1.0, A.data_ptr(), n, 0.5, C.data_ptr(), n, sp)),
+        "syr2k UT": (2.0, lambda: L.flens_gb300_dsyr2k(b"U", b"T", n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.5, C.data_ptr(), n, sp)),
+        "trmm LUNN": (1.0, lambda: L.flens_gb300_dtrmm(b"L", b"U", b"N", b"N", n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, sp)),
+        "symm LL": (2.0, lambda: L.flens_gb300_dsymm(b"L", b"L", n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.5, C.data_ptr(), n, sp)),
+    }
+    out = {"workload": f"level-3 BLAS n={n} FP64", "n": n, "tflops": {}, "ms": {}}
+    for name, (fmul, f) in calls.items():
+        times = []
+        for rep in range(1 + reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st = f()
+            e1.record(stream)
+            e1.synchronize()
+            assert st == 0, (name, fg.last_error())
+            if rep:
+                times.append(e0.elapsed_time(e1))
+        ms = sum(times) / len(times)
+        out["ms"][name] = ms
+        out["tflops"][name] = fmul * n ** 3 / (ms * 1e-3) / 1e12
+    del A, B, C
+    torch.cuda.empty_cache()
     return out
 
 
@@ -876,6 +921,8 @@ def only(args):
     elif args.only == "batched":
         out = batched_subbench(torch, fg, dev, count=args.batch_count, reps=1, loop_sample=50)
         print(json.dumps(out))
+    elif args.only == "blas3":
+        print(json.dumps(blas3_subbench(torch, fg, dev)))
     elif args.only == "cholesky":
         print(json.dumps(cholesky_subbench(torch, fg, dev, n=args.n, reps=args.steps)))
     elif args.only == "inverse":
@@ -910,7 +957,7 @@ def main():
     ap.add_argument("--split-e", type=int, default=48, help="exponent range E for --only split")
     ap.add_argument("--split-ref-slices", type=int, default=14, help="reference slices for --only split")
     ap.add_argument("--batch-count", type=int, default=20000)
-    ap.add_argument("--only", choices=["tc_gemm", "batched", "mixed", "split", "cholesky", "inverse"],
+    ap.add_argument("--only", choices=["tc_gemm", "batched", "mixed", "split", "cholesky", "inverse", "blas3"],
                     help="run one sub-benchmark and print its JSON (for profiling)")
     ap.add_argument("--tc-shape", default="8192,8192,256", help="M,N,K for --only tc_gemm")
     args = ap.parse_args()
