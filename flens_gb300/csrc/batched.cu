@@ -117,6 +117,10 @@ __device__ double team_max(double m, int lt, int T, int bar, double *red) {
     return m;
 }
 
+template <typename S>
+__device__ void team_trs(int n, int k, const S *M, int ldm, S *X, int ldx, const int *piv, int lt,
+                         int T, int bar);
+
 // LU with partial pivoting of the n x n matrix M (storage S): pivot search
 // and scaling in FP64, the rank-1 updates in S.  If INFO == 0 the k columns
 // of X are then overwritten by U^-1 L^-1 P X; X is untouched otherwise.
@@ -170,6 +174,15 @@ __device__ int team_gesv(int n, int k, S *M, int ldm, S *X, int ldx, int *piv, i
         team_sync(bar, T);
     }
     if (info != 0) return info;
+    team_trs<S>(n, k, M, ldm, X, ldx, piv, lt, T, bar);
+    return 0;
+}
+
+// X <- U^-1 L^-1 P X with the factors and pivots of a team LU (trs.tcc:84
+// interchanges, then the unit lower and the upper solve)
+template <typename S>
+__device__ void team_trs(int n, int k, const S *M, int ldm, S *X, int ldx, const int *piv, int lt,
+                         int T, int bar) {
     for (int j = 0; j < n; ++j) {                          // interchanges (trs.tcc:84)
         const int p = piv[j] - 1;
         if (p != j) {
@@ -195,7 +208,125 @@ __device__ int team_gesv(int n, int k, S *M, int ldm, S *X, int ldx, int *piv, i
                 X[r + (size_t)c * ldx] = fma(-M[r + (size_t)i * ldm], X[i + (size_t)c * ldx], X[r + (size_t)c * ldx]);
         team_sync(bar, T);
     }
-    return 0;
+}
+
+// Blocked form of team_gesv's factorisation for a matrix that stays in
+// global memory: 16-column panels factored in shared memory, their
+// interchanges applied to the other columns, U12 by forward substitution and
+// the trailing matrix updated once per panel (instead of once per column).
+// Every element receives the same FMAs in the same order as in the
+// unblocked loop, so the factors and pivots are bitwise the same.
+// Shared memory: P (n x BNB) and U12 (BNB x n) doubles.
+constexpr int BNB = 16;
+
+__device__ size_t blocked_need(int n) { return (size_t)2 * n * BNB * sizeof(double); }
+
+__device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int T, int bar,
+                               double *red_v, int *red_i, double *sm) {
+    unsigned long long *red_k = (unsigned long long *)red_v;
+    double *P = sm, *U = sm + (size_t)n * BNB;
+    const int tr = lt & 31, tc = lt >> 5, TC = T >> 5;
+    int info = 0;
+    for (int j0 = 0; j0 < n; j0 += BNB) {
+        const int jb = min(BNB, n - j0), mp = n - j0;
+        // panel rows j0.. of columns j0..j0+jb into P (ld mp)
+        for (int c = 0; c < jb; ++c)
+            for (int r = lt; r < mp; r += T) P[r + c * mp] = M[(j0 + r) + (size_t)(j0 + c) * ldm];
+        team_sync(bar, T);
+        for (int jj = 0; jj < jb; ++jj) {
+            unsigned long long bv = 0ull;
+            int bi = INT_MAX;
+            for (int r = jj + lt; r < mp; r += T) {
+                const unsigned long long key = pivot_key(P[r + jj * mp]);
+                if (better(key, r, bv, bi)) { bv = key; bi = r; }
+            }
+            team_argmax(bv, bi, lt, T, bar, red_k, red_i);
+            const double ajj = P[jj + jj * mp];
+            const int p = isnan(ajj) ? jj : bi;
+            if (lt == 0) piv[j0 + jj] = j0 + p + 1;
+            const double pv = P[p + jj * mp];
+            if (pv != 0.0) {
+                if (p != jj) {
+                    for (int c = lt; c < jb; c += T) {
+                        const double t = P[jj + c * mp];
+                        P[jj + c * mp] = P[p + c * mp];
+                        P[p + c * mp] = t;
+                    }
+                    team_sync(bar, T);
+                }
+                const bool recip = fabs(pv) >= DBL_MIN;
+                const double rinv = recip ? 1.0 / pv : 0.0;
+                for (int r = jj + 1 + lt; r < mp; r += T) {
+                    const double l = P[r + jj * mp];
+                    P[r + jj * mp] = recip ? l * rinv : l / pv;
+                }
+            } else if (info == 0) {
+                info = j0 + jj + 1;
+            }
+            team_sync(bar, T);
+            for (int r = jj + 1 + lt; r < mp; r += T) {
+                const double l = P[r + jj * mp];
+                for (int c = jj + 1; c < jb; ++c) P[r + c * mp] = fma(-P[jj + c * mp], l, P[r + c * mp]);
+            }
+            team_sync(bar, T);
+        }
+        for (int c = 0; c < jb; ++c)
+            for (int r = lt; r < mp; r += T) M[(j0 + r) + (size_t)(j0 + c) * ldm] = P[r + c * mp];
+        // the panel's interchanges on the columns left and right of it
+        for (int jj = 0; jj < jb; ++jj) {
+            const int p = piv[j0 + jj] - 1;          // written by lane 0, visible after the syncs
+            if (p != j0 + jj) {
+                for (int c = lt; c < n - jb; c += T) {
+                    const int col = c < j0 ? c : c + jb;
+                    double *a = &M[(j0 + jj) + (size_t)col * ldm], *b = &M[p + (size_t)col * ldm];
+                    const double t = *a;
+                    *a = *b;
+                    *b = t;
+                }
+            }
+            team_sync(bar, T);
+        }
+        const int nr = n - j0 - jb;
+        if (nr > 0) {
+            // U12 = L11^-1 A12, a thread per column, rows in the unblocked
+            // loop's order; kept in U (ld BNB) and written back
+            for (int c = lt; c < nr; c += T) {
+                double u[BNB];
+#pragma unroll
+                for (int q = 0; q < BNB; ++q) u[q] = q < jb ? M[(j0 + q) + (size_t)(j0 + jb + c) * ldm] : 0.0;
+#pragma unroll
+                for (int q = 0; q < BNB; ++q) {
+#pragma unroll
+                    for (int pp = q + 1; pp < BNB; ++pp)
+                        if (pp < jb) u[pp] = fma(-u[q], P[pp + q * mp], u[pp]);
+                }
+#pragma unroll
+                for (int q = 0; q < BNB; ++q) {
+                    if (q < jb) {
+                        U[q + (size_t)c * BNB] = u[q];
+                        M[(j0 + q) + (size_t)(j0 + jb + c) * ldm] = u[q];
+                    }
+                }
+            }
+            team_sync(bar, T);
+            // trailing update: lanes -> rows (32 apart), warps -> columns
+            for (int r = jb + tr; r < mp; r += 32) {
+                double l[BNB];
+#pragma unroll
+                for (int q = 0; q < BNB; ++q) l[q] = q < jb ? P[r + q * mp] : 0.0;
+                double *arow = &M[(j0 + r) + (size_t)(j0 + jb) * ldm];
+                for (int c = tc; c < nr; c += TC) {
+                    double acc = arow[(size_t)c * ldm];
+#pragma unroll
+                    for (int q = 0; q < BNB; ++q)
+                        if (q < jb) acc = fma(-U[q + (size_t)c * BNB], l[q], acc);
+                    arow[(size_t)c * ldm] = acc;
+                }
+            }
+            team_sync(bar, T);
+        }
+    }
+    return info;
 }
 
 // X <- U^-1 L^-1 P X with the FP32 factors in M (the pivots of team_gesv)
@@ -244,6 +375,10 @@ __device__ void solve_fp64(const BatchArgs &a, int idx, unsigned char *sm, size_
         for (int e = lt; e < n * n; e += T) A[e % n + (size_t)(e / n) * lda] = M[e];
         if (info == 0)
             for (int e = lt; e < n * k; e += T) B[e % n + (size_t)(e / n) * ldb] = X[e];
+    } else if (blocked_need(n) <= share) {
+        // in place in global memory, blocked (panels in shared memory)
+        info = team_lu_blocked(n, A, lda, a.ipiv[idx], lt, T, bar, rv, ri, (double *)sm);
+        if (info == 0) team_trs<double>(n, k, A, lda, B, ldb, a.ipiv[idx], lt, T, bar);
     } else {
         info = team_gesv<double>(n, k, A, lda, B, ldb, a.ipiv[idx], lt, T, bar, rv, ri);
     }

@@ -353,9 +353,11 @@ int flens_gb300_dgesv_mixed(int n, int nrhs, const double *A, int ldA,
  * pointer arrays A, ipiv (n_i ints each, 1-based), B are HOST arrays read now;
  * info, iters, berr are DEVICE arrays of `count` entries written by every
  * execution.  precision 0 = FP64 (A_i <- LU factors); 1 = FP32 LU + FP64
- * refinement (A_i untouched; iters_i = refinement steps, -1 where the FP64
- * path was used; berr_i = final normwise backward error; max_iter bounds the
- * steps).  B_i <- X_i when INFO_i == 0, untouched otherwise.  Creating a plan
+ * refinement (A_i untouched, iters_i = refinement steps, berr_i = final
+ * normwise backward error, max_iter bounds the steps) for every matrix whose
+ * FP32 working set fits its team's shared memory; the others take the FP64
+ * path (iters_i = -1, A_i <- LU factors).  B_i <- X_i when INFO_i == 0,
+ * untouched otherwise.  Creating a plan
  * autotunes the team size of each size bucket (first use per device;
  * FLENS_GB300_BATCH_TUNE=0 disables it, FLENS_GB300_BATCH_TEAM=T forces T) and
  * captures one persistent launch in a CUDA graph.  Synchronises on stream. */

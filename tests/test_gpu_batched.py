@@ -34,12 +34,13 @@ def plan_fn():
     return f
 
 
-def make_batch(cuda, sizes, ks, seed, singular=()):
+def make_batch(cuda, sizes, ks, seed, singular=(), shift=True):
     import torch
     mats, rhs, host = [], [], []
     for i, (n, k) in enumerate(zip(sizes, ks)):
         A = oracle.uniform(seed + 2 * i, n, n)
-        A[np.arange(n), np.arange(n)] += n / 4.0
+        if shift:
+            A[np.arange(n), np.arange(n)] += n / 4.0
         if i in singular:
             A[:, n // 2] = 0.0
         B = oracle.uniform(seed + 2 * i + 1, n, k)
@@ -99,6 +100,26 @@ def test_batched_fp64_vs_oracle(cuda, port):
     assert all(t in (32, 64, 128, 256) for t in teams)
 
 
+def test_batched_blocked_path_pivoting(cuda, port):
+    # n > 160 does not fit a team's shared memory: the blocked factorisation
+    # in global memory; unshifted inputs so that it interchanges rows
+    sizes, ks = [161, 200, 333, 512, 250], [1, 4, 16, 1, 3]
+    mats, rhs, host = make_batch(cuda, sizes, ks, 1500, singular=(4,), shift=False)
+    B0 = [b.clone() for b in rhs]
+    ipivs, info, _, _, _ = run_batched(cuda, mats, rhs, 0)
+    for i, (A0, Bh) in enumerate(host):
+        A1, B1 = A0.copy(order="F"), Bh.copy(order="F")
+        pivr, infor = port.dgesv(A1, B1)
+        n = sizes[i]
+        assert info[i] == infor, (i, n, info[i], infor)
+        assert np.array_equal(ipivs[i].cpu().numpy()[:n], pivr), i
+        assert oracle.lu_backward_error(A0, mats[i].cpu().numpy(), pivr) <= 10.0, i
+        if infor == 0:
+            assert oracle.normwise_rel(rhs[i].cpu().numpy(), B1) <= 1e-10, i
+        else:
+            assert np.array_equal(rhs[i].cpu().numpy(), B0[i].cpu().numpy())
+
+
 def test_batched_graph_replay(cuda, port):
     # the plan's graph replays the same launch: second execution on fresh data
     import torch
@@ -124,5 +145,10 @@ def test_batched_mixed_refinement(cuda):
         R = Bh - A0 @ X
         be = (np.abs(R).max(0) / (np.abs(A0).sum(1).max() * np.abs(X).max(0) + np.abs(Bh).max(0))).max()
         assert be <= 10 * n * EPS, (i, n, be, iters[i])
-        assert berr[i] <= 10 * n * EPS
-        np.testing.assert_array_equal(mats[i].cpu().numpy(), A0)      # A untouched
+        if iters[i] >= 0:
+            # the FP32 path: A untouched, its own backward error reported
+            assert berr[i] <= 10 * n * EPS
+            np.testing.assert_array_equal(mats[i].cpu().numpy(), A0)
+        else:
+            # FP32 working set too large for the team: the FP64 path, A <- LU
+            assert oracle.lu_backward_error(A0, mats[i].cpu().numpy(), ipivs[i].cpu().numpy()[:n]) <= 10.0
