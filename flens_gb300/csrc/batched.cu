@@ -91,18 +91,43 @@ __device__ __forceinline__ void warp_argmax(unsigned long long &k, int &i) {
     k = ((unsigned long long)mhi << 32) | mlo;
 }
 
-__device__ void team_argmax(unsigned long long &k, int &i, int lt, int T, int bar,
-                            unsigned long long *red_k, int *red_i) {
+// The pivot of column j (iamax's first maximum over the team's candidates,
+// element j itself when it is NaN) with its value and, when |pivot| >=
+// DBL_MIN, its reciprocal (tf2.tcc:101-121).  Warp 0 reduces the warps'
+// candidates and divides once between the two team barriers, instead of
+// every warp repeating the FP64 division.  col = column j, rows from 0.
+// Reduction slots: red_k/red_v[0..7] candidates, red_v[8..9] pivot value
+// and reciprocal, red_i[8] pivot row (red_k aliases red_v).
+template <typename S>
+__device__ void team_pivot(unsigned long long k, int i, const S *col, int j, int lt, int T, int bar,
+                           unsigned long long *red_k, int *red_i, int &p, double &pv,
+                           double &rinv) {
+    double *red_v = (double *)red_k;
     warp_argmax(k, i);
-    if (T == 32) return;
-    const int nw = T >> 5;
+    if (T == 32) {
+        p = isnan((double)col[j]) ? j : i;
+        pv = (double)col[p];
+        rinv = fabs(pv) >= DBL_MIN ? 1.0 / pv : 0.0;
+        return;
+    }
     if ((lt & 31) == 0) { red_k[lt >> 5] = k; red_i[lt >> 5] = i; }
     team_sync(bar, T);
-    k = red_k[0];
-    i = red_i[0];
-    for (int q = 1; q < nw; ++q)
-        if (better(red_k[q], red_i[q], k, i)) { k = red_k[q]; i = red_i[q]; }
+    if (lt < 32) {
+        unsigned long long kk = lt < (T >> 5) ? red_k[lt] : 0ull;
+        int ii = lt < (T >> 5) ? red_i[lt] : INT_MAX;
+        warp_argmax(kk, ii);
+        if (lt == 0) {
+            const int pp = isnan((double)col[j]) ? j : ii;
+            const double v = (double)col[pp];
+            red_i[8] = pp;
+            red_v[8] = v;
+            red_v[9] = fabs(v) >= DBL_MIN ? 1.0 / v : 0.0;
+        }
+    }
     team_sync(bar, T);
+    p = red_i[8];
+    pv = red_v[8];
+    rinv = red_v[9];
 }
 
 __device__ double team_max(double m, int lt, int T, int bar, double *red) {
@@ -136,11 +161,10 @@ __device__ int team_gesv(int n, int k, S *M, int ldm, S *X, int ldx, int *piv, i
             const unsigned long long key = pivot_key((double)M[r + (size_t)j * ldm]);
             if (better(key, r, bv, bi)) { bv = key; bi = r; }
         }
-        team_argmax(bv, bi, lt, T, bar, red_k, red_i);
-        const double ajj = (double)M[j + (size_t)j * ldm];
-        const int p = isnan(ajj) ? j : bi;      // iamax keeps element j if it is NaN
+        int p;
+        double pv, rinv;
+        team_pivot<S>(bv, bi, M + (size_t)j * ldm, j, lt, T, bar, red_k, red_i, p, pv, rinv);
         if (lt == 0) piv[j] = p + 1;
-        const double pv = (double)M[p + (size_t)j * ldm];
         if (pv != 0.0) {
             if (p != j) {
                 for (int c = lt; c < n; c += T) {
@@ -151,7 +175,6 @@ __device__ int team_gesv(int n, int k, S *M, int ldm, S *X, int ldx, int *piv, i
                 team_sync(bar, T);
             }
             const bool recip = fabs(pv) >= DBL_MIN;
-            const double rinv = recip ? 1.0 / pv : 0.0;
             for (int r = j + 1 + lt; r < n; r += T) {
                 const double l = (double)M[r + (size_t)j * ldm];
                 M[r + (size_t)j * ldm] = (S)(recip ? l * rinv : l / pv);
@@ -219,6 +242,24 @@ __device__ void team_trs(int n, int k, const S *M, int ldm, S *X, int ldx, const
 // Shared memory: P (n x BNB) and U12 (BNB x n) doubles.
 constexpr int BNB = 16;
 
+// dst(0:rows, 0:cols) = src(0:rows, 0:cols), column-major, eight columns'
+// loads issued before their stores (a load after a store through another
+// pointer would otherwise wait for the previous load's round trip)
+__device__ __forceinline__ void team_copy_cols(int rows, int cols, const double *__restrict__ src,
+                                               int lds, double *__restrict__ dst, int ldd, int lt,
+                                               int T) {
+    for (int c0 = 0; c0 < cols; c0 += 8)
+        for (int r = lt; r < rows; r += T) {
+            double v[8];
+#pragma unroll
+            for (int cc = 0; cc < 8; ++cc)
+                if (c0 + cc < cols) v[cc] = src[r + (size_t)(c0 + cc) * lds];
+#pragma unroll
+            for (int cc = 0; cc < 8; ++cc)
+                if (c0 + cc < cols) dst[r + (size_t)(c0 + cc) * ldd] = v[cc];
+        }
+}
+
 __device__ size_t blocked_need(int n) { return (size_t)2 * n * BNB * sizeof(double); }
 
 __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int T, int bar,
@@ -230,8 +271,7 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
     for (int j0 = 0; j0 < n; j0 += BNB) {
         const int jb = min(BNB, n - j0), mp = n - j0;
         // panel rows j0.. of columns j0..j0+jb into P (ld mp)
-        for (int c = 0; c < jb; ++c)
-            for (int r = lt; r < mp; r += T) P[r + c * mp] = M[(j0 + r) + (size_t)(j0 + c) * ldm];
+        team_copy_cols(mp, jb, M + j0 + (size_t)j0 * ldm, ldm, P, mp, lt, T);
         team_sync(bar, T);
         for (int jj = 0; jj < jb; ++jj) {
             unsigned long long bv = 0ull;
@@ -240,11 +280,10 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
                 const unsigned long long key = pivot_key(P[r + jj * mp]);
                 if (better(key, r, bv, bi)) { bv = key; bi = r; }
             }
-            team_argmax(bv, bi, lt, T, bar, red_k, red_i);
-            const double ajj = P[jj + jj * mp];
-            const int p = isnan(ajj) ? jj : bi;
+            int p;
+            double pv, rinv;
+            team_pivot<double>(bv, bi, P + jj * mp, jj, lt, T, bar, red_k, red_i, p, pv, rinv);
             if (lt == 0) piv[j0 + jj] = j0 + p + 1;
-            const double pv = P[p + jj * mp];
             if (pv != 0.0) {
                 if (p != jj) {
                     for (int c = lt; c < jb; c += T) {
@@ -255,7 +294,6 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
                     team_sync(bar, T);
                 }
                 const bool recip = fabs(pv) >= DBL_MIN;
-                const double rinv = recip ? 1.0 / pv : 0.0;
                 for (int r = jj + 1 + lt; r < mp; r += T) {
                     const double l = P[r + jj * mp];
                     P[r + jj * mp] = recip ? l * rinv : l / pv;
@@ -329,6 +367,131 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
     return info;
 }
 
+// X <- U^-1 L^-1 P X for FP64 factors that stay in global memory (the
+// blocked path): the n x k right-hand sides are staged in shared memory and
+// both triangles are solved in 32-row blocks -- the diagonal block by a warp
+// per column (lane = row, shuffles instead of barriers), the rows beyond it by
+// one coalesced pass over the block's columns of the factor.  Each element
+// receives the same FMAs and divisions in the same order as in team_trs (the
+// unit lower solve in ascending, the upper in descending column order), so
+// the solutions are bitwise those of the row-at-a-time loop, which spent a
+// team barrier and an L2 round trip per row.
+// Shared memory: X (n x k) and one 32 x 32 block of the factor.
+constexpr int SNB = 32;
+
+__device__ size_t staged_need(int n, int k) { return ((size_t)n * k + SNB * SNB) * sizeof(double); }
+
+// rows [r0, r1) of X (ld n, columns c0..c0+KC) minus the factor's columns
+// i0..i0+ib times the solved block rows of X, in ascending (lower) or
+// descending (upper) column order
+template <int KC, bool DESC>
+__device__ __forceinline__ void staged_rows_update(int r0, int r1, int i0, int ib, int c0, int k,
+                                                   const double *__restrict__ M, int ldm,
+                                                   double *X, int n, int lt, int T) {
+    for (int r = r0 + lt; r < r1; r += T) {
+        double acc[KC];
+#pragma unroll
+        for (int cc = 0; cc < KC; ++cc) acc[cc] = c0 + cc < k ? X[r + (size_t)(c0 + cc) * n] : 0.0;
+        const double *mrow = M + r;
+#pragma unroll 8
+        for (int s = 0; s < ib; ++s) {
+            const int q = DESC ? ib - 1 - s : s;
+            const double l = mrow[(size_t)(i0 + q) * ldm];
+#pragma unroll
+            for (int cc = 0; cc < KC; ++cc)
+                if (c0 + cc < k) acc[cc] = fma(-l, X[(i0 + q) + (size_t)(c0 + cc) * n], acc[cc]);
+        }
+#pragma unroll
+        for (int cc = 0; cc < KC; ++cc)
+            if (c0 + cc < k) X[r + (size_t)(c0 + cc) * n] = acc[cc];
+    }
+}
+
+template <int KC>
+__device__ void staged_update_all(bool upper, int r0, int r1, int i0, int ib, int k, const double *M,
+                                  int ldm, double *X, int n, int lt, int T) {
+    for (int c0 = 0; c0 < k; c0 += KC) {
+        if (upper) staged_rows_update<KC, true>(r0, r1, i0, ib, c0, k, M, ldm, X, n, lt, T);
+        else staged_rows_update<KC, false>(r0, r1, i0, ib, c0, k, M, ldm, X, n, lt, T);
+    }
+}
+
+__device__ void team_trs_staged(int n, int k, const double *M, int ldm, double *B, int ldb,
+                                const int *piv, int lt, int T, int bar, double *sm) {
+    double *X = sm, *Dg = sm + (size_t)n * k;
+    const int lane = lt & 31, warp = lt >> 5, nw = T >> 5;
+    team_copy_cols(n, k, B, ldb, X, n, lt, T);
+    team_sync(bar, T);
+    // interchanges in the order of trs.tcc:84: warp 0 reads 32 pivots at a
+    // time and applies the swaps among them in order, a lane per column
+    if (warp == 0) {
+        for (int j0 = 0; j0 < n; j0 += 32) {
+            const int j = j0 + lane;
+            const int p = j < n ? piv[j] - 1 : j;
+            unsigned m = __ballot_sync(0xffffffffu, p != j);
+            while (m) {
+                const int bit = __ffs(m) - 1;
+                m &= m - 1;
+                const int jj = j0 + bit, pj = __shfl_sync(0xffffffffu, p, bit);
+                for (int c = lane; c < k; c += 32) {
+                    double *x = X + (size_t)c * n;
+                    const double t = x[jj];
+                    x[jj] = x[pj];
+                    x[pj] = t;
+                }
+            }
+        }
+    }
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool upper = pass == 1;
+        for (int b = 0; b < n; b += SNB) {
+            // lower: blocks from the top; upper: from the bottom
+            const int i0 = upper ? max(0, n - b - SNB) : b;
+            const int ib = upper ? n - b - i0 : min(SNB, n - b);
+            team_sync(bar, T);
+            for (int e0 = lt; e0 < SNB * SNB; e0 += 4 * T) {
+                double v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int e = e0 + u * T, r = e & (SNB - 1), q = e >> 5;
+                    v[u] = e < SNB * SNB && r < ib && q < ib ? M[(i0 + r) + (size_t)(i0 + q) * ldm] : 0.0;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (e0 + u * T < SNB * SNB) Dg[e0 + u * T] = v[u];
+            }
+            team_sync(bar, T);
+            for (int c = warp; c < k; c += nw) {
+                double *xc = X + (size_t)c * n + i0;
+                double x = lane < ib ? xc[lane] : 0.0;
+                if (!upper) {
+                    for (int q = 0; q < ib - 1; ++q) {
+                        const double xq = __shfl_sync(0xffffffffu, x, q);
+                        if (lane > q) x = fma(-Dg[lane + q * SNB], xq, x);
+                    }
+                } else {
+                    for (int q = ib - 1; q >= 0; --q) {
+                        if (lane == q) x = x / Dg[q + q * SNB];
+                        const double xq = __shfl_sync(0xffffffffu, x, q);
+                        if (lane < q) x = fma(-Dg[lane + q * SNB], xq, x);
+                    }
+                }
+                if (lane < ib) xc[lane] = x;
+            }
+            team_sync(bar, T);
+            const int r0 = upper ? 0 : i0 + ib, r1 = upper ? i0 : n;
+            if (r0 < r1) {
+                if (k == 1) staged_update_all<1>(upper, r0, r1, i0, ib, k, M, ldm, X, n, lt, T);
+                else if (k <= 4) staged_update_all<4>(upper, r0, r1, i0, ib, k, M, ldm, X, n, lt, T);
+                else staged_update_all<8>(upper, r0, r1, i0, ib, k, M, ldm, X, n, lt, T);
+            }
+        }
+    }
+    team_sync(bar, T);
+    team_copy_cols(n, k, X, n, B, ldb, lt, T);
+    team_sync(bar, T);
+}
+
 // X <- U^-1 L^-1 P X with the FP32 factors in M (the pivots of team_gesv)
 __device__ void team_lu_solve32(int n, int k, const float *M, const int *piv, float *X, int lt,
                                 int T, int bar) {
@@ -378,7 +541,12 @@ __device__ void solve_fp64(const BatchArgs &a, int idx, unsigned char *sm, size_
     } else if (blocked_need(n) <= share) {
         // in place in global memory, blocked (panels in shared memory)
         info = team_lu_blocked(n, A, lda, a.ipiv[idx], lt, T, bar, rv, ri, (double *)sm);
-        if (info == 0) team_trs<double>(n, k, A, lda, B, ldb, a.ipiv[idx], lt, T, bar);
+        if (info == 0) {
+            if (staged_need(n, k) <= share)
+                team_trs_staged(n, k, A, lda, B, ldb, a.ipiv[idx], lt, T, bar, (double *)sm);
+            else
+                team_trs<double>(n, k, A, lda, B, ldb, a.ipiv[idx], lt, T, bar);
+        }
     } else {
         info = team_gesv<double>(n, k, A, lda, B, ldb, a.ipiv[idx], lt, T, bar, rv, ri);
     }
@@ -482,8 +650,8 @@ __device__ void solve_mixed(const BatchArgs &a, int idx, unsigned char *sm, int 
 __global__ void __launch_bounds__(BT_THREADS, 1)
 batched_gesv_kernel(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char bsm[];
-    __shared__ double red_v[8][8];
-    __shared__ int red_i[8][8];
+    __shared__ double red_v[8][10];
+    __shared__ int red_i[8][10];
     __shared__ int s_item[8];
     const int tid = threadIdx.x;
     for (int bk = BT_BUCKETS - 1; bk >= 0; --bk) {

@@ -23,7 +23,7 @@ enum Status : int {
     kErrTimeout = -1002,     // a bounded device-side wait gave up
     kErrNoDevice = -1003,    // no usable CUDA device
     kErrAlloc = -1004,       // device workspace allocation failed
-    kErrUnsupported = -1005, // size/shape outside what this build supports
+    kErrUnsupported = -1005, // size/shape outside what this library supports
     kErrNotConverged = -1006 // iterative refinement did not reach tolerance
 };
 

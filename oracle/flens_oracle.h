@@ -1,6 +1,6 @@
 /*
  * flens_oracle.h -- CPU restatement of FLENS's generic dense GEMM / TRSM / LU
- * path, used ONLY as test infrastructure (the checker for the CUDA library and
+ * path, used ONLY as test infrastructure (the reference results the CUDA library is tested against, and
  * the timed CPU baseline in bench.py).  Nothing in the product links this.
  *
  * Every routine follows the operation order of the reference's generic C++

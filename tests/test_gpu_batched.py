@@ -103,7 +103,10 @@ def test_batched_fp64_vs_oracle(cuda, port):
 def test_batched_blocked_path_pivoting(cuda, port):
     # n > 160 does not fit a team's shared memory: the blocked factorisation
     # in global memory; unshifted inputs so that it interchanges rows
-    sizes, ks = [161, 200, 333, 512, 250], [1, 4, 16, 1, 3]
+    # (the solves stage the right-hand sides in shared memory in column
+    # groups of 1, 4 or 8; k = 9 leaves a ragged group, k = 40 may exceed
+    # the team's share and solve in global memory)
+    sizes, ks = [161, 200, 333, 512, 250, 300, 400], [1, 4, 16, 1, 3, 9, 40]
     mats, rhs, host = make_batch(cuda, sizes, ks, 1500, singular=(4,), shift=False)
     B0 = [b.clone() for b in rhs]
     ipivs, info, _, _, _ = run_batched(cuda, mats, rhs, 0)

@@ -1,7 +1,7 @@
 """GPU parity for dgemm / dtrsm through the C ABI.
 
 Bars (written in each assert): GEMM normwise relative error <= 1e-13 against
-the reference's own result (the BASELINE gemm bar); TRSM <= 1e-12 on
+the reference's own result (the project's gemm parity bar); TRSM <= 1e-12 on
 well-conditioned triangles.  Semantics that are bitwise in the reference
 (alpha==0 scaling, beta multiply) are checked bitwise.
 """

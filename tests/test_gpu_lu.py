@@ -1,7 +1,7 @@
 """GPU parity for dgetrf / dgetrs / dgesv through the C ABI.
 
-Bars: backward error ||PA - LU||_1 / (n ||A||_1 eps) <= 10 (the BASELINE trf
-bar), identical pivot vectors and INFO on the reference fixtures (inputs whose
+Bars: backward error ||PA - LU||_1 / (n ||A||_1 eps) <= 10 (the project's trf
+parity bar), identical pivot vectors and INFO on the reference fixtures (inputs whose
 column maxima are well separated, and unshifted uniform inputs at these small
 sizes), solutions within 1e-12 normwise of the reference's.
 """
