@@ -347,18 +347,37 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
                 }
             }
             team_sync(bar, T);
-            // trailing update: lanes -> rows (32 apart), warps -> columns
+            // trailing update: lanes -> rows (32 apart), warps -> columns,
+            // two columns (two independent FMA chains) per step, and the
+            // next step's elements loaded before this step's FMAs so that
+            // their L2 round trip overlaps the FP64 work
             for (int r = jb + tr; r < mp; r += 32) {
                 double l[BNB];
 #pragma unroll
                 for (int q = 0; q < BNB; ++q) l[q] = q < jb ? P[r + q * mp] : 0.0;
                 double *arow = &M[(j0 + r) + (size_t)(j0 + jb) * ldm];
-                for (int c = tc; c < nr; c += TC) {
-                    double acc = arow[(size_t)c * ldm];
+                double n0 = tc < nr ? arow[(size_t)tc * ldm] : 0.0;
+                double n1 = tc + TC < nr ? arow[(size_t)(tc + TC) * ldm] : 0.0;
+                for (int c = tc; c < nr; c += 2 * TC) {
+                    const int c1 = c + TC, d = c + 2 * TC;
+                    double a0 = n0, a1 = n1;
+                    if (d < nr) n0 = arow[(size_t)d * ldm];
+                    if (d + TC < nr) n1 = arow[(size_t)(d + TC) * ldm];
+                    if (c1 < nr) {
 #pragma unroll
-                    for (int q = 0; q < BNB; ++q)
-                        if (q < jb) acc = fma(-U[q + (size_t)c * BNB], l[q], acc);
-                    arow[(size_t)c * ldm] = acc;
+                        for (int q = 0; q < BNB; ++q)
+                            if (q < jb) {
+                                a0 = fma(-U[q + (size_t)c * BNB], l[q], a0);
+                                a1 = fma(-U[q + (size_t)c1 * BNB], l[q], a1);
+                            }
+                        arow[(size_t)c * ldm] = a0;
+                        arow[(size_t)c1 * ldm] = a1;
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < BNB; ++q)
+                            if (q < jb) a0 = fma(-U[q + (size_t)c * BNB], l[q], a0);
+                        arow[(size_t)c * ldm] = a0;
+                    }
                 }
             }
             team_sync(bar, T);
