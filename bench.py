@@ -800,7 +800,8 @@ def batched_subbench(torch, fg, dev, count=20000, reps=3, loop_sample=2000):
             e1.synchronize()
             if rep > 0:
                 times.append(e0.elapsed_time(e1))
-        teams = [L.flens_gb300_batched_team(plan, b) for b in range(8)]
+        teams = [L.flens_gb300_batched_team(plan, b) for b in range(16)]
+        teams = teams[:teams.index(-1)] if -1 in teams else teams
         L.flens_gb300_batched_destroy(plan)
         ms = sum(times) / len(times)
         inf = info.cpu().numpy()

@@ -40,12 +40,22 @@ namespace fg {
 namespace {
 
 constexpr int BT_THREADS = 256;
-constexpr int BT_BUCKETS = 8;
 constexpr size_t BT_SMEM = 216 * 1024;
 
-__host__ __device__ inline int bucket_of(int n) {
-    return n <= 16 ? 0 : n <= 32 ? 1 : n <= 64 ? 2 : n <= 128 ? 3 : n <= 256 ? 4 : n <= 512 ? 5 : n <= 1024 ? 6 : 7;
+// Size buckets (upper bounds of n).  108, 216, 432 and 864 are the largest n
+// whose blocked factorisation fits a team's shared memory with 8, 4, 2 and 1
+// teams per CTA (T = 32, 64, 128, 256), so a team size the tuner picks for a
+// bucket keeps every matrix of the bucket off the unblocked global-memory path.
+constexpr int BT_BUCKETS = 10;
+constexpr int kBucketMax[BT_BUCKETS] = {16, 32, 48, 64, 108, 216, 320, 432, 864, INT_MAX};
+
+inline int bucket_of(int n) {
+    int b = 0;
+    while (b < BT_BUCKETS - 1 && n > kBucketMax[b]) ++b;
+    return b;
 }
+
+__host__ __device__ inline size_t team_share(int T) { return (BT_SMEM / (BT_THREADS / T)) / 16 * 16; }
 
 struct BatchArgs {
     int beg[BT_BUCKETS], end[BT_BUCKETS];   // ranges of `order` per bucket
@@ -260,7 +270,7 @@ __device__ __forceinline__ void team_copy_cols(int rows, int cols, const double 
         }
 }
 
-__device__ size_t blocked_need(int n) { return (size_t)2 * n * BNB * sizeof(double); }
+__host__ __device__ inline size_t blocked_need(int n) { return (size_t)2 * n * BNB * sizeof(double); }
 
 __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int T, int bar,
                                double *red_v, int *red_i, double *sm) {
@@ -273,57 +283,70 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
         // panel rows j0.. of columns j0..j0+jb into P (ld mp)
         team_copy_cols(mp, jb, M + j0 + (size_t)j0 * ldm, ldm, P, mp, lt, T);
         team_sync(bar, T);
+        // pivot keys of the panel's first column; later columns' keys come
+        // out of the previous column's update, whose rows each thread owns
+        unsigned long long bv = 0ull;
+        int bi = INT_MAX;
+        for (int r = lt; r < mp; r += T) {
+            const unsigned long long key = pivot_key(P[r]);
+            if (better(key, r, bv, bi)) { bv = key; bi = r; }
+        }
+        int *spiv = (int *)U;                   // the panel's pivots (U is free until U12)
         for (int jj = 0; jj < jb; ++jj) {
-            unsigned long long bv = 0ull;
-            int bi = INT_MAX;
-            for (int r = jj + lt; r < mp; r += T) {
-                const unsigned long long key = pivot_key(P[r + jj * mp]);
-                if (better(key, r, bv, bi)) { bv = key; bi = r; }
-            }
             int p;
             double pv, rinv;
             team_pivot<double>(bv, bi, P + jj * mp, jj, lt, T, bar, red_k, red_i, p, pv, rinv);
-            if (lt == 0) piv[j0 + jj] = j0 + p + 1;
-            if (pv != 0.0) {
-                if (p != jj) {
-                    for (int c = lt; c < jb; c += T) {
-                        const double t = P[jj + c * mp];
-                        P[jj + c * mp] = P[p + c * mp];
-                        P[p + c * mp] = t;
-                    }
-                    team_sync(bar, T);
-                }
-                const bool recip = fabs(pv) >= DBL_MIN;
-                for (int r = jj + 1 + lt; r < mp; r += T) {
-                    const double l = P[r + jj * mp];
-                    P[r + jj * mp] = recip ? l * rinv : l / pv;
-                }
-            } else if (info == 0) {
-                info = j0 + jj + 1;
+            if (lt == 0) {
+                piv[j0 + jj] = j0 + p + 1;
+                spiv[jj] = p;
             }
-            team_sync(bar, T);
+            const bool nz = pv != 0.0;
+            if (nz && p != jj) {
+                for (int c = lt; c < jb; c += T) {
+                    const double t = P[jj + c * mp];
+                    P[jj + c * mp] = P[p + c * mp];
+                    P[p + c * mp] = t;
+                }
+                team_sync(bar, T);
+            }
+            if (!nz && info == 0) info = j0 + jj + 1;
+            // scaling (a zero pivot leaves the column as it is), the rank-1
+            // update and the next column's keys, row by row: the rows a
+            // thread scales are the rows it updates
+            const bool recip = fabs(pv) >= DBL_MIN;
+            bv = 0ull;
+            bi = INT_MAX;
             for (int r = jj + 1 + lt; r < mp; r += T) {
-                const double l = P[r + jj * mp];
+                double l = P[r + jj * mp];
+                if (nz) {
+                    l = recip ? l * rinv : l / pv;
+                    P[r + jj * mp] = l;
+                }
                 for (int c = jj + 1; c < jb; ++c) P[r + c * mp] = fma(-P[jj + c * mp], l, P[r + c * mp]);
+                if (jj + 1 < jb) {
+                    const unsigned long long key = pivot_key(P[r + (jj + 1) * mp]);
+                    if (better(key, r, bv, bi)) { bv = key; bi = r; }
+                }
             }
             team_sync(bar, T);
         }
         for (int c = 0; c < jb; ++c)
             for (int r = lt; r < mp; r += T) M[(j0 + r) + (size_t)(j0 + c) * ldm] = P[r + c * mp];
-        // the panel's interchanges on the columns left and right of it
-        for (int jj = 0; jj < jb; ++jj) {
-            const int p = piv[j0 + jj] - 1;          // written by lane 0, visible after the syncs
-            if (p != j0 + jj) {
-                for (int c = lt; c < n - jb; c += T) {
-                    const int col = c < j0 ? c : c + jb;
-                    double *a = &M[(j0 + jj) + (size_t)col * ldm], *b = &M[p + (size_t)col * ldm];
-                    const double t = *a;
-                    *a = *b;
-                    *b = t;
+        // the panel's interchanges on the columns left and right of it: a
+        // thread per column applies the jb swaps in order (no barrier
+        // between swaps; pivots from shared memory)
+        for (int c = lt; c < n - jb; c += T) {
+            double *a = M + (size_t)(c < j0 ? c : c + jb) * ldm;
+            for (int jj = 0; jj < jb; ++jj) {
+                const int p = j0 + spiv[jj];
+                if (p != j0 + jj) {
+                    const double t = a[j0 + jj];
+                    a[j0 + jj] = a[p];
+                    a[p] = t;
                 }
             }
-            team_sync(bar, T);
         }
+        team_sync(bar, T);
         const int nr = n - j0 - jb;
         if (nr > 0) {
             // U12 = L11^-1 A12, a thread per column, rows in the unblocked
@@ -539,7 +562,7 @@ __device__ void team_lu_solve32(int n, int k, const float *M, const int *piv, fl
     }
 }
 
-__device__ size_t fp64_need(int n, int k) { return ((size_t)n * n + (size_t)n * k) * 8; }
+__host__ __device__ inline size_t fp64_need(int n, int k) { return ((size_t)n * n + (size_t)n * k) * 8; }
 // FP32 M and D, FP64 saved b and residual
 __device__ size_t mixed_need(int n, int k) { return (size_t)n * n * 4 + (size_t)n * k * (4 + 8 + 8); }
 
@@ -680,7 +703,7 @@ batched_gesv_kernel(BatchArgs a) {
         const int nteams = BT_THREADS / T;
         const int tm = tid / T, lt = tid % T;
         const int bar = 1 + tm;
-        const size_t share = (BT_SMEM / nteams) / 16 * 16;
+        const size_t share = team_share(T);
         unsigned char *sm = bsm + share * tm;
         // each pass takes one matrix; at most end-beg passes per team
         for (int pass = 0; pass <= end - beg; ++pass) {
@@ -718,7 +741,16 @@ namespace {
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int>, int> g_tuned;   // (device, bucket, precision) -> T
 
-int default_team(int bucket) { return bucket <= 1 ? 32 : bucket == 2 ? 64 : bucket == 3 ? 128 : 256; }
+int default_team(int bucket) {
+    const int ub = kBucketMax[bucket];
+    return ub <= 32 ? 32 : ub <= 216 ? 64 : ub <= 432 ? 128 : 256;
+}
+
+// T keeps an n x n matrix with k right-hand sides in shared memory or on the
+// blocked path (the unblocked global-memory path is several times slower)
+bool team_feasible(int T, int n, int k) {
+    return fp64_need(n, k) <= team_share(T) || blocked_need(n) <= team_share(T);
+}
 
 int env_team() {
     const char *s = getenv("FLENS_GB300_BATCH_TEAM");
@@ -764,6 +796,19 @@ int launch(const BatchArgs &a, cudaStream_t s) {
     return kOk;
 }
 
+// copies the pristine A | B at `master` over each of the tuner's `count`
+// matrices (stride `per` bytes; `words` doubles each)
+__global__ void tune_restore_kernel(char *buf, const char *master, size_t per, size_t words,
+                                    int count) {
+    const double *src = (const double *)master;
+    const size_t total = words * (size_t)count;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = e / words, w = e - i * words;
+        ((double *)(buf + per * i))[w] = src[w];
+    }
+}
+
 // Time each candidate team size on synthetic matrices of the bucket's largest
 // size (diagonally dominant, uniform entries) and return the fastest.
 int tune_bucket(int bucket, int nmax, int kmax, int precision, cudaStream_t s) {
@@ -775,12 +820,25 @@ int tune_bucket(int bucket, int nmax, int kmax, int precision, cudaStream_t s) {
     }
     const int sms = num_sms();
     const int n = nmax, k = kmax;
+    // candidates: team sizes that keep the bucket's largest matrix in shared
+    // memory or on the blocked path
+    std::vector<int> cand;
+    for (int T : {32, 64, 128, 256})
+        if (team_feasible(T, n, k)) cand.push_back(T);
+    if (cand.size() <= 1) {
+        const int T = cand.empty() ? 256 : cand[0];
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tuned[std::make_tuple(dev, bucket, precision)] = T;
+        return T;
+    }
     const size_t aBytes = (size_t)n * n * 8, bBytes = (size_t)n * k * 8, pBytes = (size_t)n * 4;
     const size_t per = (aBytes + bBytes + pBytes + 255) / 256 * 256;
-    // a few matrices per SM, at most 256 MiB of them
-    int count = 4 * sms;
-    while (count > sms && per * (size_t)count > (256u << 20)) count /= 2;
-    if (per * (size_t)count > (512u << 20)) return default_team(bucket);
+    // four matrices for every team of the smallest candidate on every SM (a
+    // smaller sample would leave SMs idle under the smaller teams and bias
+    // the choice towards large ones), at most 1 GiB of them
+    int count = 4 * sms * (BT_THREADS / cand[0]);
+    while (count > sms && per * (size_t)count > (1u << 30)) count /= 2;
+    if (per * (size_t)count > (1u << 30)) return default_team(bucket);
     const size_t metaBytes = (size_t)count * 4 * 6 + 3 * (size_t)count * sizeof(void *) +
                              (size_t)count * (4 + 4 + 8) + 4096;
     char *buf = (char *)workspace_slot(s, 3, per * (count + 1) + metaBytes);
@@ -842,15 +900,13 @@ int tune_bucket(int bucket, int nmax, int kmax, int precision, cudaStream_t s) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int T : {32, 64, 128, 256}) {
+    for (int T : cand) {
         for (int b = 0; b < BT_BUCKETS; ++b) a.team[b] = T;
         float tot = 0.0f;
         bool ok = true;
         for (int rep = 0; rep < 3; ++rep) {
-            for (int i = 0; i < count; ++i) {
-                cudaMemcpyAsync(pA[i], master, aBytes, cudaMemcpyDeviceToDevice, s);
-                cudaMemcpyAsync(pB[i], master + aBytes, bBytes, cudaMemcpyDeviceToDevice, s);
-            }
+            tune_restore_kernel<<<2 * sms, 256, 0, s>>>(buf, master, per, (aBytes + bBytes) / 8,
+                                                       count);
             cudaEventRecord(e0, s);
             if (launch(a, s) != kOk) {
                 ok = false;
@@ -1028,8 +1084,9 @@ FG_API void flens_gb300_batched_destroy(void *plan) {
     fg::batched_plan_destroy((fg::BatchedPlan *)plan);
 }
 
-// Team size chosen for a bucket (0..7, upper bounds 16,32,...,2048) of a plan.
+// Team size chosen for a size bucket of a plan (upper bounds of n: 16, 32, 48,
+// 64, 108, 216, 320, 432, 864, unbounded); -1 past the last bucket.
 FG_API int flens_gb300_batched_team(void *plan, int bucket) {
-    if (!plan || bucket < 0 || bucket > 7) return -1;
+    if (!plan || bucket < 0 || bucket >= fg::BT_BUCKETS) return -1;
     return ((fg::BatchedPlan *)plan)->team[bucket];
 }

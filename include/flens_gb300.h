@@ -374,8 +374,9 @@ int flens_gb300_batched_execute(void *plan, void *stream);
 /* Release a plan. */
 void flens_gb300_batched_destroy(void *plan);
 
-/* Team size (threads per matrix) the plan uses for size bucket 0..7
- * (n <= 16, 32, 64, 128, 256, 512, 1024, larger). */
+/* Team size (threads per matrix) the plan uses for size bucket 0..9
+ * (n <= 16, 32, 48, 64, 108, 216, 320, 432, 864, larger); -1 for any other
+ * bucket index. */
 int flens_gb300_batched_team(void *plan, int bucket);
 
 /* dgetrs on device memory for callers that must not allocate device memory

@@ -72,7 +72,8 @@ def run_batched(cuda, mats, rhs, precision, execs=1):
     for _ in range(execs):
         assert fg.lib().flens_gb300_batched_execute(plan, stream) == 0
     torch.cuda.synchronize()
-    teams = [fg.lib().flens_gb300_batched_team(plan, b) for b in range(8)]
+    teams = [fg.lib().flens_gb300_batched_team(plan, b) for b in range(16)]
+    teams = teams[:teams.index(-1)]
     fg.lib().flens_gb300_batched_destroy(plan)
     fg.sync()
     return ipivs, info.cpu().numpy(), iters.cpu().numpy(), berr.cpu().numpy(), teams
@@ -121,6 +122,34 @@ def test_batched_blocked_path_pivoting(cuda, port):
             assert oracle.normwise_rel(rhs[i].cpu().numpy(), B1) <= 1e-10, i
         else:
             assert np.array_equal(rhs[i].cpu().numpy(), B0[i].cpu().numpy())
+
+
+# upper bounds of the plan's size buckets (flens_gb300_batched_team)
+BUCKET_MAX = [16, 32, 48, 64, 108, 216, 320, 432, 864]
+
+
+def bucket_of(n):
+    return next((b for b, m in enumerate(BUCKET_MAX) if n <= m), len(BUCKET_MAX))
+
+
+def test_batched_team_sizes_fit_shared_memory(cuda, port):
+    # a bucket's team size keeps its largest matrix in shared memory or on
+    # the blocked path: 2 teams per CTA (T = 128) hold the panels of n <= 432,
+    # only one team (T = 256) those of n = 433..864
+    sizes, ks = [500, 432, 400, 216, 200, 108, 100], [4, 1, 16, 4, 1, 16, 4]
+    mats, rhs, host = make_batch(cuda, sizes, ks, 2100)
+    ipivs, info, _, _, teams = run_batched(cuda, mats, rhs, 0)
+    assert len(teams) == len(BUCKET_MAX) + 1
+    assert teams[bucket_of(500)] == 256
+    assert teams[bucket_of(432)] in (128, 256) and teams[bucket_of(400)] in (128, 256)
+    assert teams[bucket_of(216)] in (64, 128, 256)
+    assert teams[bucket_of(108)] in (32, 64, 128, 256)
+    for i, (A0, Bh) in enumerate(host):
+        A1, B1 = A0.copy(order="F"), Bh.copy(order="F")
+        pivr, infor = port.dgesv(A1, B1)
+        assert info[i] == infor == 0
+        assert np.array_equal(ipivs[i].cpu().numpy()[:sizes[i]], pivr), i
+        assert oracle.normwise_rel(rhs[i].cpu().numpy(), B1) <= 1e-12, i
 
 
 def test_batched_graph_replay(cuda, port):
