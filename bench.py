@@ -717,18 +717,22 @@ def ctypes_stream(stream):
     return ctypes.c_void_p(stream.cuda_stream)
 
 
-def batched_subbench(torch, fg, dev, count=20000, reps=3, loop_sample=2000):
+def batched_subbench(torch, fg, dev, count=20000, reps=3, loop_sample=2000, uniform=None):
     """Batched configuration: `count` independent FP64 systems, n log-uniform
     in [8, 512], entries uniform[-1,1] + (n/4) I, k uniform in {1, 4, 16}.
     Times one plan execution (one persistent launch, graph replay) in FP64 and
     in FP32 LU + FP64 refinement, against a per-matrix flens_gb300_dgesv loop
     (timed on the first `loop_sample` matrices and scaled), and reports
-    p50/p99 normwise backward errors."""
+    p50/p99 normwise backward errors.  uniform=(N, K): every matrix N x N
+    with K right-hand sides instead (for profiling one size)."""
     import ctypes
     import numpy as np
     rng = np.random.default_rng(55)
     n = np.floor(np.exp(rng.uniform(np.log(8), np.log(512.999), size=count))).astype(np.int32)
     k = rng.choice(np.array([1, 4, 16], dtype=np.int32), size=count)
+    if uniform:
+        n = np.full(count, uniform[0], dtype=np.int32)
+        k = np.full(count, uniform[1], dtype=np.int32)
     a_off = np.concatenate([[0], np.cumsum(n.astype(np.int64) ** 2)])
     b_off = np.concatenate([[0], np.cumsum(n.astype(np.int64) * k)])
     g = torch.Generator(device=dev)
@@ -762,7 +766,8 @@ def batched_subbench(torch, fg, dev, count=20000, reps=3, loop_sample=2000):
     sp = ctypes.c_void_p(stream.cuda_stream)
     flops = float(np.sum(2.0 / 3.0 * n.astype(np.float64) ** 3 + 2.0 * n.astype(np.float64) ** 2 * k))
     eps = float(np.finfo(np.float64).eps)
-    out = {"workload": f"{count} dgesv, n log-uniform [8,512], k in {{1,4,16}}", "count": count,
+    what = (f"n={uniform[0]}, k={uniform[1]}" if uniform else "n log-uniform [8,512], k in {1,4,16}")
+    out = {"workload": f"{count} dgesv, {what}", "count": count,
            "flop": flops, "variants": {}}
 
     def berr_sample(sample):
@@ -920,7 +925,9 @@ def only(args):
                           "tflops": 2.0 * m * n * k / (ms * 1e-3) / 1e12,
                           "c_traffic_gbs": 8.0 * m * n / (ms * 1e-3) / 1e9}))
     elif args.only == "batched":
-        out = batched_subbench(torch, fg, dev, count=args.batch_count, reps=1, loop_sample=50)
+        uni = tuple(int(v) for v in args.batch_uniform.split(",")) if args.batch_uniform else None
+        out = batched_subbench(torch, fg, dev, count=args.batch_count, reps=1, loop_sample=50,
+                               uniform=uni)
         print(json.dumps(out))
     elif args.only == "blas3":
         print(json.dumps(blas3_subbench(torch, fg, dev)))
@@ -958,6 +965,8 @@ def main():
     ap.add_argument("--split-e", type=int, default=48, help="exponent range E for --only split")
     ap.add_argument("--split-ref-slices", type=int, default=14, help="reference slices for --only split")
     ap.add_argument("--batch-count", type=int, default=20000)
+    ap.add_argument("--batch-uniform", default=None,
+                    help="N,K: --only batched on count matrices of one size (for profiling)")
     ap.add_argument("--only", choices=["tc_gemm", "batched", "mixed", "split", "cholesky", "inverse", "blas3"],
                     help="run one sub-benchmark and print its JSON (for profiling)")
     ap.add_argument("--tc-shape", default="8192,8192,256", help="M,N,K for --only tc_gemm")

@@ -276,7 +276,6 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
                                double *red_v, int *red_i, double *sm) {
     unsigned long long *red_k = (unsigned long long *)red_v;
     double *P = sm, *U = sm + (size_t)n * BNB;
-    const int tr = lt & 31, tc = lt >> 5, TC = T >> 5;
     int info = 0;
     for (int j0 = 0; j0 < n; j0 += BNB) {
         const int jb = min(BNB, n - j0), mp = n - j0;
@@ -370,36 +369,47 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
                 }
             }
             team_sync(bar, T);
-            // trailing update: lanes -> rows (32 apart), warps -> columns,
-            // two columns (two independent FMA chains) per step, and the
-            // next step's elements loaded before this step's FMAs so that
-            // their L2 round trip overlaps the FP64 work
-            for (int r = jb + tr; r < mp; r += 32) {
-                double l[BNB];
-#pragma unroll
-                for (int q = 0; q < BNB; ++q) l[q] = q < jb ? P[r + q * mp] : 0.0;
-                double *arow = &M[(j0 + r) + (size_t)(j0 + jb) * ldm];
-                double n0 = tc < nr ? arow[(size_t)tc * ldm] : 0.0;
-                double n1 = tc + TC < nr ? arow[(size_t)(tc + TC) * ldm] : 0.0;
-                for (int c = tc; c < nr; c += 2 * TC) {
-                    const int c1 = c + TC, d = c + 2 * TC;
+            // trailing update of the R x nr block in column-major element
+            // order: thread lt takes elements lt, lt + T, ... (consecutive
+            // lanes on consecutive rows), so lanes idle only in the block's
+            // last T elements (lanes mapped to rows 32 apart left up to 31
+            // of them idle in every column's last row group).  Two elements
+            // (two independent FMA chains) per step; the next step's two are
+            // loaded before this step's FMAs so that their L2 round trip
+            // overlaps the FP64 work.  nr > 0 implies jb == BNB.
+            {
+                const int R = mp - jb, total = R * nr;
+                const int dr = T % R, dc = T / R;
+                double *Mb = M + (j0 + jb) + (size_t)(j0 + jb) * ldm;
+                const double *Pl = P + jb;
+                int r0 = lt % R, c0 = lt / R;          // element e
+                int r1 = r0 + dr, c1 = c0 + dc;        // element e + T
+                if (r1 >= R) { r1 -= R; ++c1; }
+                double n0 = lt < total ? Mb[r0 + (size_t)c0 * ldm] : 0.0;
+                double n1 = lt + T < total ? Mb[r1 + (size_t)c1 * ldm] : 0.0;
+                for (int e = lt; e < total; e += 2 * T) {
+                    const int ra = r0, ca = c0, rb = r1, cb = c1;
                     double a0 = n0, a1 = n1;
-                    if (d < nr) n0 = arow[(size_t)d * ldm];
-                    if (d + TC < nr) n1 = arow[(size_t)(d + TC) * ldm];
-                    if (c1 < nr) {
+                    r0 = r1 + dr;                      // elements e + 2T, e + 3T
+                    c0 = c1 + dc;
+                    if (r0 >= R) { r0 -= R; ++c0; }
+                    r1 = r0 + dr;
+                    c1 = c0 + dc;
+                    if (r1 >= R) { r1 -= R; ++c1; }
+                    if (e + 2 * T < total) n0 = Mb[r0 + (size_t)c0 * ldm];
+                    if (e + 3 * T < total) n1 = Mb[r1 + (size_t)c1 * ldm];
+                    if (e + T < total) {
 #pragma unroll
-                        for (int q = 0; q < BNB; ++q)
-                            if (q < jb) {
-                                a0 = fma(-U[q + (size_t)c * BNB], l[q], a0);
-                                a1 = fma(-U[q + (size_t)c1 * BNB], l[q], a1);
-                            }
-                        arow[(size_t)c * ldm] = a0;
-                        arow[(size_t)c1 * ldm] = a1;
+                        for (int q = 0; q < BNB; ++q) {
+                            a0 = fma(-U[q + (size_t)ca * BNB], Pl[ra + q * mp], a0);
+                            a1 = fma(-U[q + (size_t)cb * BNB], Pl[rb + q * mp], a1);
+                        }
+                        Mb[ra + (size_t)ca * ldm] = a0;
+                        Mb[rb + (size_t)cb * ldm] = a1;
                     } else {
 #pragma unroll
-                        for (int q = 0; q < BNB; ++q)
-                            if (q < jb) a0 = fma(-U[q + (size_t)c * BNB], l[q], a0);
-                        arow[(size_t)c * ldm] = a0;
+                        for (int q = 0; q < BNB; ++q) a0 = fma(-U[q + (size_t)ca * BNB], Pl[ra + q * mp], a0);
+                        Mb[ra + (size_t)ca * ldm] = a0;
                     }
                 }
             }
@@ -700,7 +710,6 @@ batched_gesv_kernel(BatchArgs a) {
         const int beg = a.beg[bk], end = a.end[bk];
         if (beg >= end) continue;
         const int T = a.team[bk];
-        const int nteams = BT_THREADS / T;
         const int tm = tid / T, lt = tid % T;
         const int bar = 1 + tm;
         const size_t share = team_share(T);
