@@ -80,6 +80,23 @@ def test_gemm_edge_sizes_vs_oracle(cuda, port, m, n, k, ta, tb):
     assert rel(out, ref) <= GEMM_TOL
 
 
+@pytest.mark.parametrize("m,n,k", [(1000, 900, 64), (1100, 700, 255), (640, 2048, 16)])
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
+def test_gemm_short_k_many_tiles_vs_oracle(cuda, port, m, n, k, ta, tb):
+    # more 64x64 tiles than SMs and a short K (the LU's trailing-update
+    # shape), ragged edges in m, n and k
+    A = oracle.uniform(m + 3 * k, m if ta == "N" else k, k if ta == "N" else m)
+    B = oracle.uniform(n + 5 * k, k if tb == "N" else n, n if tb == "N" else k)
+    C = oracle.uniform(m + n, m, n)
+    C[5, 7] = np.nan                     # beta*C is a multiply: NaN survives beta = 0
+    out0 = fg.dgemm(ta, tb, 1.25, A, B, 0.0, C.copy(order="F"))
+    assert np.isnan(out0[5, 7]) and np.isfinite(np.delete(out0.ravel(order="F"), 5 + 7 * m)).all()
+    C[5, 7] = 0.25
+    out = fg.dgemm(ta, tb, -0.75, A, B, 1.5, C.copy(order="F"))
+    ref = port.dgemm(ta, tb, -0.75, A, B, 1.5, C.copy(order="F"))
+    assert rel(out, ref) <= GEMM_TOL
+
+
 def test_gemm_leading_dimension_views(cuda, port):
     # operands that are sub-blocks of larger arrays (ld > rows)
     big = oracle.uniform(11, 100, 90)
