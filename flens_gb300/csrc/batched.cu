@@ -468,6 +468,19 @@ __device__ void staged_update_all(bool upper, int r0, int r1, int i0, int ib, in
     }
 }
 
+// x(0:ib) <- U^-1 x(0:ib) for the ib x ib upper block D (ld SNB), one
+// column, rows from the bottom: per element the FMAs of the rows below in
+// descending order, then the division (the order of team_trs's upper solve)
+__device__ __forceinline__ void upper_block_by_column(double *__restrict__ xc,
+                                                      const double *__restrict__ D, int ib) {
+    for (int q = ib - 1; q >= 0; --q) {
+        const double xq = xc[q] / D[q + q * SNB];
+        xc[q] = xq;
+#pragma unroll 4
+        for (int r = 0; r < q; ++r) xc[r] = fma(-D[r + q * SNB], xq, xc[r]);
+    }
+}
+
 __device__ void team_trs_staged(int n, int k, const double *M, int ldm, double *B, int ldb,
                                 const int *piv, int lt, int T, int bar, double *sm) {
     double *X = sm, *Dg = sm + (size_t)n * k;
@@ -513,22 +526,30 @@ __device__ void team_trs_staged(int n, int k, const double *M, int ldm, double *
                     if (e0 + u * T < SNB * SNB) Dg[e0 + u * T] = v[u];
             }
             team_sync(bar, T);
-            for (int c = warp; c < k; c += nw) {
-                double *xc = X + (size_t)c * n + i0;
-                double x = lane < ib ? xc[lane] : 0.0;
-                if (!upper) {
-                    for (int q = 0; q < ib - 1; ++q) {
-                        const double xq = __shfl_sync(0xffffffffu, x, q);
-                        if (lane > q) x = fma(-Dg[lane + q * SNB], xq, x);
+            if (upper && k >= 3) {
+                // a thread per column: each row's division is one instruction
+                // sequence for all k columns, where a warp per column spent a
+                // whole warp's FP64 slots on every one-lane division
+                for (int c = lt; c < k; c += T)
+                    upper_block_by_column(X + (size_t)c * n + i0, Dg, ib);
+            } else {
+                for (int c = warp; c < k; c += nw) {
+                    double *xc = X + (size_t)c * n + i0;
+                    double x = lane < ib ? xc[lane] : 0.0;
+                    if (!upper) {
+                        for (int q = 0; q < ib - 1; ++q) {
+                            const double xq = __shfl_sync(0xffffffffu, x, q);
+                            if (lane > q) x = fma(-Dg[lane + q * SNB], xq, x);
+                        }
+                    } else {
+                        for (int q = ib - 1; q >= 0; --q) {
+                            if (lane == q) x = x / Dg[q + q * SNB];
+                            const double xq = __shfl_sync(0xffffffffu, x, q);
+                            if (lane < q) x = fma(-Dg[lane + q * SNB], xq, x);
+                        }
                     }
-                } else {
-                    for (int q = ib - 1; q >= 0; --q) {
-                        if (lane == q) x = x / Dg[q + q * SNB];
-                        const double xq = __shfl_sync(0xffffffffu, x, q);
-                        if (lane < q) x = fma(-Dg[lane + q * SNB], xq, x);
-                    }
+                    if (lane < ib) xc[lane] = x;
                 }
-                if (lane < ib) xc[lane] = x;
             }
             team_sync(bar, T);
             const int r0 = upper ? 0 : i0 + ib, r1 = upper ? i0 : n;
