@@ -193,10 +193,27 @@ __device__ int team_gesv(int n, int k, S *M, int ldm, S *X, int ldx, int *piv, i
             info = j + 1;
         }
         team_sync(bar, T);
-        // rank-1 update: lane -> rows (32 apart), warp -> columns (T/32
-        // apart), so a warp touches consecutive rows of one column and there
-        // are no index divisions
-        {
+        // rank-1 update of the R x R block below and right of (j, j)
+        const int R = n - 1 - j;
+        if (R > 0 && __isShared(M)) {
+            // in shared memory: the team walks the block in column-major
+            // element order (consecutive lanes on consecutive rows), so
+            // lanes idle only in its last T elements -- lanes mapped to rows
+            // 32 apart left up to 31 idle per column
+            const int total = R * R, dr = T % R, dc = T / R;
+            S *Mb = M + (j + 1) + (size_t)(j + 1) * ldm;
+            const S *lcol = M + (j + 1) + (size_t)j * ldm;
+            const S *urow = M + j + (size_t)(j + 1) * ldm;
+            int r = lt % R, c = lt / R;
+            for (int e = lt; e < total; e += T) {
+                Mb[r + (size_t)c * ldm] = fma(-urow[(size_t)c * ldm], lcol[r], Mb[r + (size_t)c * ldm]);
+                r += dr;
+                c += dc;
+                if (r >= R) { r -= R; ++c; }
+            }
+        } else {
+            // in global memory: lane -> rows (32 apart), warp -> columns
+            // (T/32 apart), the row's multiplier loaded once
             const int tr = lt & 31, tc = lt >> 5, TC = T >> 5;
             for (int r = j + 1 + tr; r < n; r += 32) {
                 const S l = M[r + (size_t)j * ldm];
