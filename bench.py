@@ -338,6 +338,7 @@ def our_arm(args, rank: int, world: int) -> None:
             result["cholesky_fp64"] = cholesky_subbench(torch, fg, dev)
             result["inverse_fp64"] = inverse_subbench(torch, fg, dev)
             result["blas3_fp64"] = blas3_subbench(torch, fg, dev)
+            result["tcgen05_kinds"] = tc_kinds_subbench(torch, fg, dev)
         if not args.quick and not args.no_batched:
             result["batched_config5"] = batched_subbench(torch, fg, dev, count=args.batch_count)
         # -- CPU baseline (oracle C restatement, 1 thread, bounded sample)
@@ -567,6 +568,52 @@ def split_subbench(torch, fg, dev, n=8192, Es=(0, 16, 48), reps=5, ref_slices=14
     out["plain_fp64_dgemm"] = {"ms": plain_ms, "tflops": 2.0 * n ** 3 / (plain_ms * 1e-3) / 1e12,
                                "cublas_fp64_tflops": cublas_tflops}
     out["bf16_peak_tflops"] = {"value": peak, "source": f"{peak_src} (MEASURED_PEAKS.json bf16_tflops)"}
+    return out
+
+
+def tc_kinds_subbench(torch, fg, dev, n=8192, reps=3):
+    """The tcgen05 GEMM kernel per operand kind at a compute-bound shape
+    (flens_gb300_sgemm_tc, M = N = K = 8192, FP32 in/out): kernel-only
+    TFLOP/s from the library's per-launch CUDA events (the call also converts
+    the FP32 operands to the kind's K-major copies, timed separately as aux),
+    against the measured dense BF16 peak scaled by the kind's nominal rate
+    (TF32 1/2, FP8 2x; 3xTF32 runs one TF32 product over 3K)."""
+    import ctypes
+    bf16, src = measured_peak("bf16_tflops")
+    g = torch.Generator(device=dev)
+    g.manual_seed(3)
+    A = torch.rand((n, n), generator=g, dtype=torch.float32, device=dev).t()
+    B = torch.rand((n, n), generator=g, dtype=torch.float32, device=dev).t()
+    C = torch.zeros((n, n), dtype=torch.float32, device=dev).t()
+    f = fg.lib().flens_gb300_sgemm_tc
+    f.argtypes = [ctypes.c_int, ctypes.c_char, ctypes.c_char] + [ctypes.c_int] * 3 + [
+        ctypes.c_float, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+        ctypes.c_float, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    out = {"workload": f"sgemm_tc {n}^3, FP32 in/out, tcgen05 kernel only", "kinds": {},
+           "bf16_peak_tflops": {"value": bf16, "source": f"{src} (MEASURED_PEAKS.json bf16_tflops)"}}
+    for prec, name, rate in ((0, "tf32", 0.5), (1, "bf16", 1.0), (2, "fp8_e4m3", 2.0),
+                             (3, "3xtf32", 0.5)):
+        st = f(prec, b"N", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0,
+               C.data_ptr(), n, sp)
+        if st != 0:
+            out["kinds"][name] = {"error": fg.last_error()}
+            continue
+        torch.cuda.synchronize()
+        fg.timing_enable(True)
+        for _ in range(reps):
+            f(prec, b"N", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0,
+              C.data_ptr(), n, sp)
+        fam = fg.timing_read()
+        fg.timing_enable(False)
+        tc = fam.get("tc_gemm", {"ms": 0.0, "flops": 0.0})
+        tfl = tc["flops"] / max(1e-9, tc["ms"] * 1e-3) / 1e12
+        kind_peak = bf16 * rate
+        out["kinds"][name] = {"kernel_ms": tc["ms"] / reps, "tensor_tflops": tfl,
+                              "kind_peak_tflops": kind_peak, "frac_of_kind_peak": tfl / kind_peak,
+                              "conversion_ms": fam.get("aux", {"ms": 0.0})["ms"] / reps}
+    del A, B, C
+    torch.cuda.empty_cache()
     return out
 
 
@@ -881,7 +928,8 @@ def e2e_dgesv(torch, fg, A0, b0, args):
             "d2h_bytes_per_step": 8 * n * n + 8 * n + 4 * n,
             "api": "dgesv_ (Fortran ABI, host pointers, pinned)", "ok": ok,
             "ms_per_step": 1000.0 * sum(times) / len(times),
-            "ms_per_step_min": 1000.0 * min(times), "clocks": clk.summary()}
+            "ms_per_step_min": 1000.0 * min(times),
+            "ms_steps": [round(1000.0 * t, 2) for t in times], "clocks": clk.summary()}
 
 
 def cpu_baseline(n):
@@ -930,6 +978,8 @@ def only(args):
         print(json.dumps({"only": "tc_gemm", "shape": [m, n, k], "precision": "bf16", "ms": ms,
                           "tflops": 2.0 * m * n * k / (ms * 1e-3) / 1e12,
                           "c_traffic_gbs": 8.0 * m * n / (ms * 1e-3) / 1e9}))
+    elif args.only == "tc_kinds":
+        print(json.dumps(tc_kinds_subbench(torch, fg, dev)))
     elif args.only == "batched":
         uni = tuple(int(v) for v in args.batch_uniform.split(",")) if args.batch_uniform else None
         out = batched_subbench(torch, fg, dev, count=args.batch_count, reps=1, loop_sample=50,
@@ -973,7 +1023,8 @@ def main():
     ap.add_argument("--batch-count", type=int, default=20000)
     ap.add_argument("--batch-uniform", default=None,
                     help="N,K: --only batched on count matrices of one size (for profiling)")
-    ap.add_argument("--only", choices=["tc_gemm", "batched", "mixed", "split", "cholesky", "inverse", "blas3"],
+    ap.add_argument("--only", choices=["tc_gemm", "tc_kinds", "batched", "mixed", "split", "cholesky",
+                                       "inverse", "blas3"],
                     help="run one sub-benchmark and print its JSON (for profiling)")
     ap.add_argument("--tc-shape", default="8192,8192,256", help="M,N,K for --only tc_gemm")
     args = ap.parse_args()
