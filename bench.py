@@ -814,6 +814,8 @@ def batched_subbench(torch, fg, dev, count=20000, reps=3, loop_sample=2000, unif
     L.flens_gb300_batched_destroy.argtypes = [vp]
     L.flens_gb300_batched_team.argtypes = [vp, ctypes.c_int]
     L.flens_gb300_batched_team.restype = ctypes.c_int
+    L.flens_gb300_batched_panel.argtypes = [vp, ctypes.c_int]
+    L.flens_gb300_batched_panel.restype = ctypes.c_int
     stream = torch.cuda.current_stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
     flops = float(np.sum(2.0 / 3.0 * n.astype(np.float64) ** 3 + 2.0 * n.astype(np.float64) ** 2 * k))
@@ -859,12 +861,14 @@ def batched_subbench(torch, fg, dev, count=20000, reps=3, loop_sample=2000, unif
                 times.append(e0.elapsed_time(e1))
         teams = [L.flens_gb300_batched_team(plan, b) for b in range(16)]
         teams = teams[:teams.index(-1)] if -1 in teams else teams
+        panels = [L.flens_gb300_batched_panel(plan, b) for b in range(len(teams))]
         L.flens_gb300_batched_destroy(plan)
         ms = sum(times) / len(times)
         inf = info.cpu().numpy()
         be = berr_sample(sample) / (n[sample] * eps)
         v = {"ms": ms, "solves_per_s": count / (ms * 1e-3), "gflops": flops / (ms * 1e-3) / 1e9,
-             "plan_s": round(plan_s, 2), "teams_per_bucket": teams, "info_nonzero": int((inf != 0).sum()),
+             "plan_s": round(plan_s, 2), "teams_per_bucket": teams, "panel_per_bucket": panels,
+             "info_nonzero": int((inf != 0).sum()),
              "backward_error_over_n_eps_p50": float(np.percentile(be, 50)),
              "backward_error_over_n_eps_p99": float(np.percentile(be, 99)),
              "backward_error_sample": f"{len(sample)} matrices"}

@@ -60,6 +60,7 @@ __host__ __device__ inline size_t team_share(int T) { return (BT_SMEM / (BT_THRE
 struct BatchArgs {
     int beg[BT_BUCKETS], end[BT_BUCKETS];   // ranges of `order` per bucket
     int team[BT_BUCKETS];                   // threads per team per bucket
+    int panel[BT_BUCKETS];                  // panel width of the blocked path (8 or 16)
     const int *order;
     const int *n, *nrhs, *lda, *ldb;
     double *const *A;
@@ -261,13 +262,13 @@ __device__ void team_trs(int n, int k, const S *M, int ldm, S *X, int ldx, const
 }
 
 // Blocked form of team_gesv's factorisation for a matrix that stays in
-// global memory: 16-column panels factored in shared memory, their
+// global memory: NB-column panels factored in shared memory, their
 // interchanges applied to the other columns, U12 by forward substitution and
 // the trailing matrix updated once per panel (instead of once per column).
 // Every element receives the same FMAs in the same order as in the
-// unblocked loop, so the factors and pivots are bitwise the same.
-// Shared memory: P (n x BNB) and U12 (BNB x n) doubles.
-constexpr int BNB = 16;
+// unblocked loop, so the factors and pivots are bitwise the same, whatever
+// the panel width NB (8 or 16, picked per size bucket by the tuner).
+// Shared memory: P (n x NB) and U12 (NB x n) doubles.
 
 // dst(0:rows, 0:cols) = src(0:rows, 0:cols), column-major, eight columns'
 // loads issued before their stores (a load after a store through another
@@ -287,8 +288,11 @@ __device__ __forceinline__ void team_copy_cols(int rows, int cols, const double 
         }
 }
 
-__host__ __device__ inline size_t blocked_need(int n) { return (size_t)2 * n * BNB * sizeof(double); }
+__host__ __device__ inline size_t blocked_need(int n, int nb) {
+    return (size_t)2 * n * nb * sizeof(double);
+}
 
+template <int BNB>
 __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int T, int bar,
                                double *red_v, int *red_i, double *sm) {
     unsigned long long *red_k = (unsigned long long *)red_v;
@@ -614,8 +618,8 @@ __host__ __device__ inline size_t fp64_need(int n, int k) { return ((size_t)n * 
 // FP32 M and D, FP64 saved b and residual
 __device__ size_t mixed_need(int n, int k) { return (size_t)n * n * 4 + (size_t)n * k * (4 + 8 + 8); }
 
-__device__ void solve_fp64(const BatchArgs &a, int idx, unsigned char *sm, size_t share, int lt,
-                           int T, int bar, double *rv, int *ri) {
+__device__ void solve_fp64(const BatchArgs &a, int idx, unsigned char *sm, size_t share, int nb,
+                           int lt, int T, int bar, double *rv, int *ri) {
     const int n = a.n[idx], k = a.nrhs[idx], lda = a.lda[idx], ldb = a.ldb[idx];
     double *A = a.A[idx], *B = a.B[idx];
     int info;
@@ -628,9 +632,10 @@ __device__ void solve_fp64(const BatchArgs &a, int idx, unsigned char *sm, size_
         for (int e = lt; e < n * n; e += T) A[e % n + (size_t)(e / n) * lda] = M[e];
         if (info == 0)
             for (int e = lt; e < n * k; e += T) B[e % n + (size_t)(e / n) * ldb] = X[e];
-    } else if (blocked_need(n) <= share) {
+    } else if (blocked_need(n, nb) <= share) {
         // in place in global memory, blocked (panels in shared memory)
-        info = team_lu_blocked(n, A, lda, a.ipiv[idx], lt, T, bar, rv, ri, (double *)sm);
+        info = nb == 8 ? team_lu_blocked<8>(n, A, lda, a.ipiv[idx], lt, T, bar, rv, ri, (double *)sm)
+                       : team_lu_blocked<16>(n, A, lda, a.ipiv[idx], lt, T, bar, rv, ri, (double *)sm);
         if (info == 0) {
             if (staged_need(n, k) <= share)
                 team_trs_staged(n, k, A, lda, B, ldb, a.ipiv[idx], lt, T, bar, (double *)sm);
@@ -747,7 +752,7 @@ batched_gesv_kernel(BatchArgs a) {
     for (int bk = BT_BUCKETS - 1; bk >= 0; --bk) {
         const int beg = a.beg[bk], end = a.end[bk];
         if (beg >= end) continue;
-        const int T = a.team[bk];
+        const int T = a.team[bk], nb = a.panel[bk];
         const int tm = tid / T, lt = tid % T;
         const int bar = 1 + tm;
         const size_t share = team_share(T);
@@ -763,7 +768,7 @@ batched_gesv_kernel(BatchArgs a) {
             if (a.precision == 1 && a.nrhs[idx] <= 32 && mixed_need(a.n[idx], a.nrhs[idx]) <= share)
                 solve_mixed(a, idx, sm, lt, T, bar, red_v[tm], red_i[tm]);
             else
-                solve_fp64(a, idx, sm, share, lt, T, bar, red_v[tm], red_i[tm]);
+                solve_fp64(a, idx, sm, share, nb, lt, T, bar, red_v[tm], red_i[tm]);
         }
         __syncthreads();
     }
@@ -781,22 +786,39 @@ struct BatchedPlan {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int team[BT_BUCKETS];
+    int panel[BT_BUCKETS];
     std::vector<int> hn;
 };
 
 namespace {
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int>, int> g_tuned;   // (device, bucket, precision) -> T
+// (device, bucket, precision) -> (team size, panel width)
+std::map<std::tuple<int, int, int>, std::pair<int, int>> g_tuned;
 
 int default_team(int bucket) {
     const int ub = kBucketMax[bucket];
     return ub <= 32 ? 32 : ub <= 216 ? 64 : ub <= 432 ? 128 : 256;
 }
 
-// T keeps an n x n matrix with k right-hand sides in shared memory or on the
-// blocked path (the unblocked global-memory path is several times slower)
-bool team_feasible(int T, int n, int k) {
-    return fp64_need(n, k) <= team_share(T) || blocked_need(n) <= team_share(T);
+// T keeps an n x n matrix with k right-hand sides in shared memory
+bool fits_shared(int T, int n, int k) { return fp64_need(n, k) <= team_share(T); }
+
+// (T, nb) keeps it in shared memory or on the blocked path with nb-column
+// panels (the unblocked global-memory path is several times slower).  The
+// limits this gives for the blocked path -- 16-column panels: n <= 108, 216,
+// 432, 864 for T = 32..256; 8-column panels, offered from T = 64 on: n <= 432,
+// 864, 1728 -- are bucket bounds (all but 1728, inside the last, unbounded
+// bucket), so a choice feasible for a bucket's largest matrix is feasible for
+// all of its matrices.
+bool team_feasible(int T, int nb, int n, int k) {
+    if (nb == 8 && T < 64) return false;
+    return fits_shared(T, n, k) || blocked_need(n, nb) <= team_share(T);
+}
+
+int env_panel() {
+    const char *s = getenv("FLENS_GB300_BATCH_PANEL");
+    const int v = s ? atoi(s) : 0;
+    return (v == 8 || v == 16) ? v : 0;
 }
 
 int env_team() {
@@ -858,7 +880,7 @@ __global__ void tune_restore_kernel(char *buf, const char *master, size_t per, s
 
 // Time each candidate team size on synthetic matrices of the bucket's largest
 // size (diagonally dominant, uniform entries) and return the fastest.
-int tune_bucket(int bucket, int nmax, int kmax, int precision, cudaStream_t s) {
+std::pair<int, int> tune_bucket(int bucket, int nmax, int kmax, int precision, cudaStream_t s) {
     const int dev = device_id();
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
@@ -867,29 +889,37 @@ int tune_bucket(int bucket, int nmax, int kmax, int precision, cudaStream_t s) {
     }
     const int sms = num_sms();
     const int n = nmax, k = kmax;
-    // candidates: team sizes that keep the bucket's largest matrix in shared
-    // memory or on the blocked path
-    std::vector<int> cand;
-    for (int T : {32, 64, 128, 256})
-        if (team_feasible(T, n, k)) cand.push_back(T);
+    const std::pair<int, int> fallback(default_team(bucket), 16);
+    // candidates: (team size, panel width) pairs that keep the bucket's
+    // largest matrix in shared memory or on the blocked path; the panel width
+    // is only a choice where the blocked path runs
+    std::vector<std::pair<int, int>> cand;
+    for (int T : {32, 64, 128, 256}) {
+        if (fits_shared(T, n, k)) {
+            cand.emplace_back(T, 16);
+            continue;
+        }
+        for (int nb : {16, 8})
+            if (team_feasible(T, nb, n, k)) cand.emplace_back(T, nb);
+    }
     if (cand.size() <= 1) {
-        const int T = cand.empty() ? 256 : cand[0];
+        const std::pair<int, int> c = cand.empty() ? std::make_pair(256, 16) : cand[0];
         std::lock_guard<std::mutex> lock(g_tune_mu);
-        g_tuned[std::make_tuple(dev, bucket, precision)] = T;
-        return T;
+        g_tuned[std::make_tuple(dev, bucket, precision)] = c;
+        return c;
     }
     const size_t aBytes = (size_t)n * n * 8, bBytes = (size_t)n * k * 8, pBytes = (size_t)n * 4;
     const size_t per = (aBytes + bBytes + pBytes + 255) / 256 * 256;
     // four matrices for every team of the smallest candidate on every SM (a
     // smaller sample would leave SMs idle under the smaller teams and bias
     // the choice towards large ones), at most 1 GiB of them
-    int count = 4 * sms * (BT_THREADS / cand[0]);
+    int count = 4 * sms * (BT_THREADS / cand[0].first);
     while (count > sms && per * (size_t)count > (1u << 30)) count /= 2;
-    if (per * (size_t)count > (1u << 30)) return default_team(bucket);
+    if (per * (size_t)count > (1u << 30)) return fallback;
     const size_t metaBytes = (size_t)count * 4 * 6 + 3 * (size_t)count * sizeof(void *) +
                              (size_t)count * (4 + 4 + 8) + 4096;
     char *buf = (char *)workspace_slot(s, 3, per * (count + 1) + metaBytes);
-    if (!buf) return default_team(bucket);
+    if (!buf) return fallback;
     char *master = buf + per * count + metaBytes;       // one pristine A | B
     std::vector<double> hA((size_t)n * n), hB((size_t)n * k);
     std::mt19937_64 rng(1234 + bucket);
@@ -942,13 +972,16 @@ int tune_bucket(int bucket, int nmax, int kmax, int precision, cudaStream_t s) {
     a.max_iter = 10;
     cudaMemcpyAsync(master, hA.data(), aBytes, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(master + aBytes, hB.data(), bBytes, cudaMemcpyHostToDevice, s);
-    int best = default_team(bucket);
+    std::pair<int, int> best = fallback;
     float best_ms = 1e30f;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int T : cand) {
-        for (int b = 0; b < BT_BUCKETS; ++b) a.team[b] = T;
+    for (const auto &c : cand) {
+        for (int b = 0; b < BT_BUCKETS; ++b) {
+            a.team[b] = c.first;
+            a.panel[b] = c.second;
+        }
         float tot = 0.0f;
         bool ok = true;
         for (int rep = 0; rep < 3; ++rep) {
@@ -967,14 +1000,14 @@ int tune_bucket(int bucket, int nmax, int kmax, int precision, cudaStream_t s) {
         }
         if (ok && tot < best_ms) {
             best_ms = tot;
-            best = T;
+            best = c;
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaStreamSynchronize(s);
-    trace("batched tune bucket=%d n=%d k=%d precision=%d -> team %d (%.3f ms)", bucket, n, k,
-          precision, best, best_ms / 2);
+    trace("batched tune bucket=%d n=%d k=%d precision=%d -> team %d panel %d (%.3f ms)", bucket, n,
+          k, precision, best.first, best.second, best_ms / 2);
     std::lock_guard<std::mutex> lock(g_tune_mu);
     g_tuned[std::make_tuple(dev, bucket, precision)] = best;
     return best;
@@ -996,21 +1029,23 @@ int batched_plan_create(int count, const int *hn, const int *hk, double *const *
     memset(&a, 0, sizeof a);
     std::vector<int> order;
     fill_ranges(p->hn, order, a);
-    // team size per bucket
-    const int forced = env_team();
+    // team size and panel width per bucket
+    const int forced = env_team(), forced_nb = env_panel();
     for (int b = 0; b < BT_BUCKETS; ++b) {
-        int T = default_team(b);
-        if (forced) T = forced;
-        else if (tuning_enabled() && a.end[b] > a.beg[b]) {
+        std::pair<int, int> c(default_team(b), 16);
+        if (forced || forced_nb) {
+            if (forced) c.first = forced;
+            if (forced_nb) c.second = forced_nb;
+        } else if (tuning_enabled() && a.end[b] > a.beg[b]) {
             int nmax = 0, kmax = 0;
             for (int i = a.beg[b]; i < a.end[b]; ++i) {
                 nmax = std::max(nmax, hn[order[i]]);
                 kmax = std::max(kmax, hk[order[i]]);
             }
-            T = tune_bucket(b, nmax, kmax, precision, s);
+            c = tune_bucket(b, nmax, kmax, precision, s);
         }
-        a.team[b] = T;
-        p->team[b] = T;
+        a.team[b] = p->team[b] = c.first;
+        a.panel[b] = p->panel[b] = c.second;
     }
     const size_t intBytes = (size_t)count * 4;
     if (cudaMalloc((void **)&p->d_meta, 5 * intBytes + BT_BUCKETS * 4) != cudaSuccess ||
@@ -1136,4 +1171,11 @@ FG_API void flens_gb300_batched_destroy(void *plan) {
 FG_API int flens_gb300_batched_team(void *plan, int bucket) {
     if (!plan || bucket < 0 || bucket >= fg::BT_BUCKETS) return -1;
     return ((fg::BatchedPlan *)plan)->team[bucket];
+}
+
+// Panel width (8 or 16 columns) of the blocked factorisation the plan uses
+// for a size bucket; -1 past the last bucket.
+FG_API int flens_gb300_batched_panel(void *plan, int bucket) {
+    if (!plan || bucket < 0 || bucket >= fg::BT_BUCKETS) return -1;
+    return ((fg::BatchedPlan *)plan)->panel[bucket];
 }

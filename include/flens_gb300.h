@@ -379,6 +379,13 @@ void flens_gb300_batched_destroy(void *plan);
  * bucket index. */
 int flens_gb300_batched_team(void *plan, int bucket);
 
+/* Panel width (8 or 16 columns) of the blocked factorisation that the plan
+ * uses for size bucket 0..9: matrices that do not fit their team's shared
+ * memory are factored in place, one panel at a time.  Tuned together with the
+ * team size; FLENS_GB300_BATCH_PANEL=8|16 forces it.  -1 for any other bucket
+ * index.  No counterpart in the reference. */
+int flens_gb300_batched_panel(void *plan, int bucket);
+
 /* dgetrs on device memory for callers that must not allocate device memory
  * once running (a fixed, pre-reserved memory budget, a memory pool owned by
  * another framework, or a process that forbids cudaMalloc after start-up).

@@ -31,6 +31,8 @@ def plan_fn():
     L.flens_gb300_batched_destroy.argtypes = [vp]
     L.flens_gb300_batched_team.argtypes = [vp, ctypes.c_int]
     L.flens_gb300_batched_team.restype = ctypes.c_int
+    L.flens_gb300_batched_panel.argtypes = [vp, ctypes.c_int]
+    L.flens_gb300_batched_panel.restype = ctypes.c_int
     return f
 
 
@@ -74,9 +76,19 @@ def run_batched(cuda, mats, rhs, precision, execs=1):
     torch.cuda.synchronize()
     teams = [fg.lib().flens_gb300_batched_team(plan, b) for b in range(16)]
     teams = teams[:teams.index(-1)]
+    panels = [fg.lib().flens_gb300_batched_panel(plan, b) for b in range(len(teams) + 1)]
+    assert panels[-1] == -1 and all(p in (8, 16) for p in panels[:-1])
+    # the blocked path's panels fit the team's share of 216 KB of shared memory
+    # for every bucket bound up to 864
+    for b, (t, p) in enumerate(zip(teams, panels)):
+        if b < len(BUCKET_MAX) and BUCKET_MAX[b] > 64:
+            share = 216 * 1024 // (256 // t)
+            fits_shared = (BUCKET_MAX[b] ** 2 + BUCKET_MAX[b] * 16) * 8 <= share
+            assert fits_shared or 2 * BUCKET_MAX[b] * p * 8 <= share or t == 256, (b, t, p)
     fg.lib().flens_gb300_batched_destroy(plan)
     fg.sync()
-    return ipivs, info.cpu().numpy(), iters.cpu().numpy(), berr.cpu().numpy(), teams
+    # (team size, panel width) per bucket
+    return ipivs, info.cpu().numpy(), iters.cpu().numpy(), berr.cpu().numpy(), list(zip(teams, panels))
 
 
 SIZES = [1, 8, 9, 16, 17, 31, 32, 33, 48, 64, 65, 100, 128, 129, 160, 200, 256, 300, 13, 40]
@@ -98,7 +110,7 @@ def test_batched_fp64_vs_oracle(cuda, port):
             assert oracle.lu_backward_error(A0, mats[i].cpu().numpy(), pivr) <= 10.0
         else:
             assert np.array_equal(rhs[i].cpu().numpy(), B0[i].cpu().numpy())   # no solve
-    assert all(t in (32, 64, 128, 256) for t in teams)
+    assert all(t in (32, 64, 128, 256) and p in (8, 16) for t, p in teams)
 
 
 def test_batched_blocked_path_pivoting(cuda, port):
@@ -133,17 +145,19 @@ def bucket_of(n):
 
 
 def test_batched_team_sizes_fit_shared_memory(cuda, port):
-    # a bucket's team size keeps its largest matrix in shared memory or on
-    # the blocked path: 2 teams per CTA (T = 128) hold the panels of n <= 432,
-    # only one team (T = 256) those of n = 433..864
+    # a bucket's (team size, panel width) keeps its largest matrix in shared
+    # memory or on the blocked path.  With 16-column panels, 2 teams per CTA
+    # (T = 128) hold the panels of n <= 432 and only one team (T = 256) those
+    # of n = 433..864; 8-column panels halve that need.
     sizes, ks = [500, 432, 400, 216, 200, 108, 100], [4, 1, 16, 4, 1, 16, 4]
     mats, rhs, host = make_batch(cuda, sizes, ks, 2100)
     ipivs, info, _, _, teams = run_batched(cuda, mats, rhs, 0)
     assert len(teams) == len(BUCKET_MAX) + 1
-    assert teams[bucket_of(500)] == 256
-    assert teams[bucket_of(432)] in (128, 256) and teams[bucket_of(400)] in (128, 256)
-    assert teams[bucket_of(216)] in (64, 128, 256)
-    assert teams[bucket_of(108)] in (32, 64, 128, 256)
+    assert teams[bucket_of(500)] in ((256, 16), (256, 8), (128, 8))
+    for n in (432, 400):
+        assert teams[bucket_of(n)] in ((128, 16), (128, 8), (256, 16), (256, 8), (64, 8))
+    assert teams[bucket_of(216)][0] in (64, 128, 256)
+    assert teams[bucket_of(108)][0] in (32, 64, 128, 256)
     for i, (A0, Bh) in enumerate(host):
         A1, B1 = A0.copy(order="F"), Bh.copy(order="F")
         pivr, infor = port.dgesv(A1, B1)
