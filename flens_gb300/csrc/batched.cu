@@ -267,7 +267,8 @@ __device__ void team_trs(int n, int k, const S *M, int ldm, S *X, int ldx, const
 // the trailing matrix updated once per panel (instead of once per column).
 // Every element receives the same FMAs in the same order as in the
 // unblocked loop, so the factors and pivots are bitwise the same, whatever
-// the panel width NB (8 or 16, picked per size bucket by the tuner).
+// the panel width NB (8 or 16, picked per size bucket by the tuner; 4-column
+// panels measured 10-17% slower than 8 at n = 200..480).
 // Shared memory: P (n x NB) and U12 (NB x n) doubles.
 
 // dst(0:rows, 0:cols) = src(0:rows, 0:cols), column-major, eight columns'
@@ -634,8 +635,9 @@ __device__ void solve_fp64(const BatchArgs &a, int idx, unsigned char *sm, size_
             for (int e = lt; e < n * k; e += T) B[e % n + (size_t)(e / n) * ldb] = X[e];
     } else if (blocked_need(n, nb) <= share) {
         // in place in global memory, blocked (panels in shared memory)
-        info = nb == 8 ? team_lu_blocked<8>(n, A, lda, a.ipiv[idx], lt, T, bar, rv, ri, (double *)sm)
-                       : team_lu_blocked<16>(n, A, lda, a.ipiv[idx], lt, T, bar, rv, ri, (double *)sm);
+        double *ps = (double *)sm;
+        info = nb == 8 ? team_lu_blocked<8>(n, A, lda, a.ipiv[idx], lt, T, bar, rv, ri, ps)
+                       : team_lu_blocked<16>(n, A, lda, a.ipiv[idx], lt, T, bar, rv, ri, ps);
         if (info == 0) {
             if (staged_need(n, k) <= share)
                 team_trs_staged(n, k, A, lda, B, ldb, a.ipiv[idx], lt, T, bar, (double *)sm);
@@ -805,13 +807,11 @@ bool fits_shared(int T, int n, int k) { return fp64_need(n, k) <= team_share(T);
 
 // (T, nb) keeps it in shared memory or on the blocked path with nb-column
 // panels (the unblocked global-memory path is several times slower).  The
-// limits this gives for the blocked path -- 16-column panels: n <= 108, 216,
-// 432, 864 for T = 32..256; 8-column panels, offered from T = 64 on: n <= 432,
-// 864, 1728 -- are bucket bounds (all but 1728, inside the last, unbounded
-// bucket), so a choice feasible for a bucket's largest matrix is feasible for
-// all of its matrices.
+// limits this gives for the blocked path, n <= 108 * 16/nb * T/32 (108, 216,
+// 432, 864, or inside the last, unbounded bucket), are bucket bounds, so a
+// choice feasible for a bucket's largest matrix is feasible for all of its
+// matrices.
 bool team_feasible(int T, int nb, int n, int k) {
-    if (nb == 8 && T < 64) return false;
     return fits_shared(T, n, k) || blocked_need(n, nb) <= team_share(T);
 }
 
