@@ -72,6 +72,11 @@ struct BatchArgs {
     int *queue;                             // [BT_BUCKETS], zeroed before each launch
     int precision;
     int max_iter;
+    // precision 1, matrices beyond the team's shared memory: FP32 factors and
+    // FP64 refinement vectors in a plan-owned pool, one slot per team
+    void *mx_pool;
+    size_t mx_stride;                       // bytes per slot
+    int mx_teams;                           // slots per CTA (CTA b owns b*mx_teams..)
 };
 
 __device__ __forceinline__ void team_sync(int id, int nthreads) {
@@ -274,12 +279,13 @@ __device__ void team_trs(int n, int k, const S *M, int ldm, S *X, int ldx, const
 // dst(0:rows, 0:cols) = src(0:rows, 0:cols), column-major, eight columns'
 // loads issued before their stores (a load after a store through another
 // pointer would otherwise wait for the previous load's round trip)
-__device__ __forceinline__ void team_copy_cols(int rows, int cols, const double *__restrict__ src,
-                                               int lds, double *__restrict__ dst, int ldd, int lt,
+template <typename S>
+__device__ __forceinline__ void team_copy_cols(int rows, int cols, const S *__restrict__ src,
+                                               int lds, S *__restrict__ dst, int ldd, int lt,
                                                int T) {
     for (int c0 = 0; c0 < cols; c0 += 8)
         for (int r = lt; r < rows; r += T) {
-            double v[8];
+            S v[8];
 #pragma unroll
             for (int cc = 0; cc < 8; ++cc)
                 if (c0 + cc < cols) v[cc] = src[r + (size_t)(c0 + cc) * lds];
@@ -289,15 +295,15 @@ __device__ __forceinline__ void team_copy_cols(int rows, int cols, const double 
         }
 }
 
-__host__ __device__ inline size_t blocked_need(int n, int nb) {
-    return (size_t)2 * n * nb * sizeof(double);
+__host__ __device__ inline size_t blocked_need(int n, int nb, size_t elem = sizeof(double)) {
+    return (size_t)2 * n * nb * elem;
 }
 
-template <int BNB>
-__device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int T, int bar,
-                               double *red_v, int *red_i, double *sm) {
+template <typename S, int BNB>
+__device__ int team_lu_blocked(int n, S *M, int ldm, int *piv, int lt, int T, int bar,
+                               double *red_v, int *red_i, S *sm) {
     unsigned long long *red_k = (unsigned long long *)red_v;
-    double *P = sm, *U = sm + (size_t)n * BNB;
+    S *P = sm, *U = sm + (size_t)n * BNB;
     int info = 0;
     for (int j0 = 0; j0 < n; j0 += BNB) {
         const int jb = min(BNB, n - j0), mp = n - j0;
@@ -309,14 +315,14 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
         unsigned long long bv = 0ull;
         int bi = INT_MAX;
         for (int r = lt; r < mp; r += T) {
-            const unsigned long long key = pivot_key(P[r]);
+            const unsigned long long key = pivot_key((double)P[r]);
             if (better(key, r, bv, bi)) { bv = key; bi = r; }
         }
         int *spiv = (int *)U;                   // the panel's pivots (U is free until U12)
         for (int jj = 0; jj < jb; ++jj) {
             int p;
             double pv, rinv;
-            team_pivot<double>(bv, bi, P + jj * mp, jj, lt, T, bar, red_k, red_i, p, pv, rinv);
+            team_pivot<S>(bv, bi, P + jj * mp, jj, lt, T, bar, red_k, red_i, p, pv, rinv);
             if (lt == 0) {
                 piv[j0 + jj] = j0 + p + 1;
                 spiv[jj] = p;
@@ -324,7 +330,7 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
             const bool nz = pv != 0.0;
             if (nz && p != jj) {
                 for (int c = lt; c < jb; c += T) {
-                    const double t = P[jj + c * mp];
+                    const S t = P[jj + c * mp];
                     P[jj + c * mp] = P[p + c * mp];
                     P[p + c * mp] = t;
                 }
@@ -338,14 +344,15 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
             bv = 0ull;
             bi = INT_MAX;
             for (int r = jj + 1 + lt; r < mp; r += T) {
-                double l = P[r + jj * mp];
-                if (nz) {
-                    l = recip ? l * rinv : l / pv;
+                S l = P[r + jj * mp];
+                if (nz) {                       // scaled in FP64, stored in S
+                    const double d = (double)l;
+                    l = (S)(recip ? d * rinv : d / pv);
                     P[r + jj * mp] = l;
                 }
                 for (int c = jj + 1; c < jb; ++c) P[r + c * mp] = fma(-P[jj + c * mp], l, P[r + c * mp]);
                 if (jj + 1 < jb) {
-                    const unsigned long long key = pivot_key(P[r + (jj + 1) * mp]);
+                    const unsigned long long key = pivot_key((double)P[r + (jj + 1) * mp]);
                     if (better(key, r, bv, bi)) { bv = key; bi = r; }
                 }
             }
@@ -357,11 +364,11 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
         // thread per column applies the jb swaps in order (no barrier
         // between swaps; pivots from shared memory)
         for (int c = lt; c < n - jb; c += T) {
-            double *a = M + (size_t)(c < j0 ? c : c + jb) * ldm;
+            S *a = M + (size_t)(c < j0 ? c : c + jb) * ldm;
             for (int jj = 0; jj < jb; ++jj) {
                 const int p = j0 + spiv[jj];
                 if (p != j0 + jj) {
-                    const double t = a[j0 + jj];
+                    const S t = a[j0 + jj];
                     a[j0 + jj] = a[p];
                     a[p] = t;
                 }
@@ -373,9 +380,9 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
             // U12 = L11^-1 A12, a thread per column, rows in the unblocked
             // loop's order; kept in U (ld BNB) and written back
             for (int c = lt; c < nr; c += T) {
-                double u[BNB];
+                S u[BNB];
 #pragma unroll
-                for (int q = 0; q < BNB; ++q) u[q] = q < jb ? M[(j0 + q) + (size_t)(j0 + jb + c) * ldm] : 0.0;
+                for (int q = 0; q < BNB; ++q) u[q] = q < jb ? M[(j0 + q) + (size_t)(j0 + jb + c) * ldm] : S(0);
 #pragma unroll
                 for (int q = 0; q < BNB; ++q) {
 #pragma unroll
@@ -398,20 +405,20 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
             // of them idle in every column's last row group).  Two elements
             // (two independent FMA chains) per step; the next step's two are
             // loaded before this step's FMAs so that their L2 round trip
-            // overlaps the FP64 work.  nr > 0 implies jb == BNB.
+            // overlaps the FMA work.  nr > 0 implies jb == BNB.
             {
                 const int R = mp - jb, total = R * nr;
                 const int dr = T % R, dc = T / R;
-                double *Mb = M + (j0 + jb) + (size_t)(j0 + jb) * ldm;
-                const double *Pl = P + jb;
+                S *Mb = M + (j0 + jb) + (size_t)(j0 + jb) * ldm;
+                const S *Pl = P + jb;
                 int r0 = lt % R, c0 = lt / R;          // element e
                 int r1 = r0 + dr, c1 = c0 + dc;        // element e + T
                 if (r1 >= R) { r1 -= R; ++c1; }
-                double n0 = lt < total ? Mb[r0 + (size_t)c0 * ldm] : 0.0;
-                double n1 = lt + T < total ? Mb[r1 + (size_t)c1 * ldm] : 0.0;
+                S n0 = lt < total ? Mb[r0 + (size_t)c0 * ldm] : S(0);
+                S n1 = lt + T < total ? Mb[r1 + (size_t)c1 * ldm] : S(0);
                 for (int e = lt; e < total; e += 2 * T) {
                     const int ra = r0, ca = c0, rb = r1, cb = c1;
-                    double a0 = n0, a1 = n1;
+                    S a0 = n0, a1 = n1;
                     r0 = r1 + dr;                      // elements e + 2T, e + 3T
                     c0 = c1 + dc;
                     if (r0 >= R) { r0 -= R; ++c0; }
@@ -453,24 +460,26 @@ __device__ int team_lu_blocked(int n, double *M, int ldm, int *piv, int lt, int 
 // Shared memory: X (n x k) and one 32 x 32 block of the factor.
 constexpr int SNB = 32;
 
-__device__ size_t staged_need(int n, int k) { return ((size_t)n * k + SNB * SNB) * sizeof(double); }
+__device__ size_t staged_need(int n, int k, size_t elem = sizeof(double)) {
+    return ((size_t)n * k + SNB * SNB) * elem;
+}
 
 // rows [r0, r1) of X (ld n, columns c0..c0+KC) minus the factor's columns
 // i0..i0+ib times the solved block rows of X, in ascending (lower) or
 // descending (upper) column order
-template <int KC, bool DESC>
+template <typename S, int KC, bool DESC>
 __device__ __forceinline__ void staged_rows_update(int r0, int r1, int i0, int ib, int c0, int k,
-                                                   const double *__restrict__ M, int ldm,
-                                                   double *X, int n, int lt, int T) {
+                                                   const S *__restrict__ M, int ldm,
+                                                   S *X, int n, int lt, int T) {
     for (int r = r0 + lt; r < r1; r += T) {
-        double acc[KC];
+        S acc[KC];
 #pragma unroll
-        for (int cc = 0; cc < KC; ++cc) acc[cc] = c0 + cc < k ? X[r + (size_t)(c0 + cc) * n] : 0.0;
-        const double *mrow = M + r;
+        for (int cc = 0; cc < KC; ++cc) acc[cc] = c0 + cc < k ? X[r + (size_t)(c0 + cc) * n] : S(0);
+        const S *mrow = M + r;
 #pragma unroll 8
         for (int s = 0; s < ib; ++s) {
             const int q = DESC ? ib - 1 - s : s;
-            const double l = mrow[(size_t)(i0 + q) * ldm];
+            const S l = mrow[(size_t)(i0 + q) * ldm];
 #pragma unroll
             for (int cc = 0; cc < KC; ++cc)
                 if (c0 + cc < k) acc[cc] = fma(-l, X[(i0 + q) + (size_t)(c0 + cc) * n], acc[cc]);
@@ -481,31 +490,33 @@ __device__ __forceinline__ void staged_rows_update(int r0, int r1, int i0, int i
     }
 }
 
-template <int KC>
-__device__ void staged_update_all(bool upper, int r0, int r1, int i0, int ib, int k, const double *M,
-                                  int ldm, double *X, int n, int lt, int T) {
+template <typename S, int KC>
+__device__ void staged_update_all(bool upper, int r0, int r1, int i0, int ib, int k, const S *M,
+                                  int ldm, S *X, int n, int lt, int T) {
     for (int c0 = 0; c0 < k; c0 += KC) {
-        if (upper) staged_rows_update<KC, true>(r0, r1, i0, ib, c0, k, M, ldm, X, n, lt, T);
-        else staged_rows_update<KC, false>(r0, r1, i0, ib, c0, k, M, ldm, X, n, lt, T);
+        if (upper) staged_rows_update<S, KC, true>(r0, r1, i0, ib, c0, k, M, ldm, X, n, lt, T);
+        else staged_rows_update<S, KC, false>(r0, r1, i0, ib, c0, k, M, ldm, X, n, lt, T);
     }
 }
 
 // x(0:ib) <- U^-1 x(0:ib) for the ib x ib upper block D (ld SNB), one
 // column, rows from the bottom: per element the FMAs of the rows below in
 // descending order, then the division (the order of team_trs's upper solve)
-__device__ __forceinline__ void upper_block_by_column(double *__restrict__ xc,
-                                                      const double *__restrict__ D, int ib) {
+template <typename S>
+__device__ __forceinline__ void upper_block_by_column(S *__restrict__ xc, const S *__restrict__ D,
+                                                      int ib) {
     for (int q = ib - 1; q >= 0; --q) {
-        const double xq = xc[q] / D[q + q * SNB];
+        const S xq = xc[q] / D[q + q * SNB];
         xc[q] = xq;
 #pragma unroll 4
         for (int r = 0; r < q; ++r) xc[r] = fma(-D[r + q * SNB], xq, xc[r]);
     }
 }
 
-__device__ void team_trs_staged(int n, int k, const double *M, int ldm, double *B, int ldb,
-                                const int *piv, int lt, int T, int bar, double *sm) {
-    double *X = sm, *Dg = sm + (size_t)n * k;
+template <typename S>
+__device__ void team_trs_staged(int n, int k, const S *M, int ldm, S *B, int ldb,
+                                const int *piv, int lt, int T, int bar, S *sm) {
+    S *X = sm, *Dg = sm + (size_t)n * k;
     const int lane = lt & 31, warp = lt >> 5, nw = T >> 5;
     team_copy_cols(n, k, B, ldb, X, n, lt, T);
     team_sync(bar, T);
@@ -521,8 +532,8 @@ __device__ void team_trs_staged(int n, int k, const double *M, int ldm, double *
                 m &= m - 1;
                 const int jj = j0 + bit, pj = __shfl_sync(0xffffffffu, p, bit);
                 for (int c = lane; c < k; c += 32) {
-                    double *x = X + (size_t)c * n;
-                    const double t = x[jj];
+                    S *x = X + (size_t)c * n;
+                    const S t = x[jj];
                     x[jj] = x[pj];
                     x[pj] = t;
                 }
@@ -537,11 +548,11 @@ __device__ void team_trs_staged(int n, int k, const double *M, int ldm, double *
             const int ib = upper ? n - b - i0 : min(SNB, n - b);
             team_sync(bar, T);
             for (int e0 = lt; e0 < SNB * SNB; e0 += 4 * T) {
-                double v[4];
+                S v[4];
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const int e = e0 + u * T, r = e & (SNB - 1), q = e >> 5;
-                    v[u] = e < SNB * SNB && r < ib && q < ib ? M[(i0 + r) + (size_t)(i0 + q) * ldm] : 0.0;
+                    v[u] = e < SNB * SNB && r < ib && q < ib ? M[(i0 + r) + (size_t)(i0 + q) * ldm] : S(0);
                 }
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
@@ -556,17 +567,17 @@ __device__ void team_trs_staged(int n, int k, const double *M, int ldm, double *
                     upper_block_by_column(X + (size_t)c * n + i0, Dg, ib);
             } else {
                 for (int c = warp; c < k; c += nw) {
-                    double *xc = X + (size_t)c * n + i0;
-                    double x = lane < ib ? xc[lane] : 0.0;
+                    S *xc = X + (size_t)c * n + i0;
+                    S x = lane < ib ? xc[lane] : S(0);
                     if (!upper) {
                         for (int q = 0; q < ib - 1; ++q) {
-                            const double xq = __shfl_sync(0xffffffffu, x, q);
+                            const S xq = __shfl_sync(0xffffffffu, x, q);
                             if (lane > q) x = fma(-Dg[lane + q * SNB], xq, x);
                         }
                     } else {
                         for (int q = ib - 1; q >= 0; --q) {
                             if (lane == q) x = x / Dg[q + q * SNB];
-                            const double xq = __shfl_sync(0xffffffffu, x, q);
+                            const S xq = __shfl_sync(0xffffffffu, x, q);
                             if (lane < q) x = fma(-Dg[lane + q * SNB], xq, x);
                         }
                     }
@@ -576,9 +587,9 @@ __device__ void team_trs_staged(int n, int k, const double *M, int ldm, double *
             team_sync(bar, T);
             const int r0 = upper ? 0 : i0 + ib, r1 = upper ? i0 : n;
             if (r0 < r1) {
-                if (k == 1) staged_update_all<1>(upper, r0, r1, i0, ib, k, M, ldm, X, n, lt, T);
-                else if (k <= 4) staged_update_all<4>(upper, r0, r1, i0, ib, k, M, ldm, X, n, lt, T);
-                else staged_update_all<8>(upper, r0, r1, i0, ib, k, M, ldm, X, n, lt, T);
+                if (k == 1) staged_update_all<S, 1>(upper, r0, r1, i0, ib, k, M, ldm, X, n, lt, T);
+                else if (k <= 4) staged_update_all<S, 4>(upper, r0, r1, i0, ib, k, M, ldm, X, n, lt, T);
+                else staged_update_all<S, 8>(upper, r0, r1, i0, ib, k, M, ldm, X, n, lt, T);
             }
         }
     }
@@ -617,7 +628,15 @@ __device__ void team_lu_solve32(int n, int k, const float *M, const int *piv, fl
 
 __host__ __device__ inline size_t fp64_need(int n, int k) { return ((size_t)n * n + (size_t)n * k) * 8; }
 // FP32 M and D, FP64 saved b and residual
-__device__ size_t mixed_need(int n, int k) { return (size_t)n * n * 4 + (size_t)n * k * (4 + 8 + 8); }
+__host__ __device__ inline size_t mixed_need(int n, int k) {
+    return (size_t)n * n * 4 + (size_t)n * k * (4 + 8 + 8);
+}
+// pool slot of the blocked mixed path: FP32 factors, then saved b and the
+// residual (FP64) and the FP32 corrections, n x k each
+__host__ __device__ inline size_t mx_factor_bytes(int n) { return ((size_t)n * n * 4 + 255) / 256 * 256; }
+__host__ __device__ inline size_t mx_need(int n, int k) {
+    return mx_factor_bytes(n) + (size_t)n * k * (8 + 8 + 4);
+}
 
 __device__ void solve_fp64(const BatchArgs &a, int idx, unsigned char *sm, size_t share, int nb,
                            int lt, int T, int bar, double *rv, int *ri) {
@@ -636,11 +655,11 @@ __device__ void solve_fp64(const BatchArgs &a, int idx, unsigned char *sm, size_
     } else if (blocked_need(n, nb) <= share) {
         // in place in global memory, blocked (panels in shared memory)
         double *ps = (double *)sm;
-        info = nb == 8 ? team_lu_blocked<8>(n, A, lda, a.ipiv[idx], lt, T, bar, rv, ri, ps)
-                       : team_lu_blocked<16>(n, A, lda, a.ipiv[idx], lt, T, bar, rv, ri, ps);
+        info = nb == 8 ? team_lu_blocked<double, 8>(n, A, lda, a.ipiv[idx], lt, T, bar, rv, ri, ps)
+                       : team_lu_blocked<double, 16>(n, A, lda, a.ipiv[idx], lt, T, bar, rv, ri, ps);
         if (info == 0) {
             if (staged_need(n, k) <= share)
-                team_trs_staged(n, k, A, lda, B, ldb, a.ipiv[idx], lt, T, bar, (double *)sm);
+                team_trs_staged<double>(n, k, A, lda, B, ldb, a.ipiv[idx], lt, T, bar, (double *)sm);
             else
                 team_trs<double>(n, k, A, lda, B, ldb, a.ipiv[idx], lt, T, bar);
         }
@@ -655,29 +674,16 @@ __device__ void solve_fp64(const BatchArgs &a, int idx, unsigned char *sm, size_
     team_sync(bar, T);
 }
 
-__device__ void solve_mixed(const BatchArgs &a, int idx, unsigned char *sm, int lt, int T, int bar,
-                            double *rv, int *ri) {
-    const int n = a.n[idx], k = a.nrhs[idx], lda = a.lda[idx], ldb = a.ldb[idx];
-    const double *A = a.A[idx];
-    double *B = a.B[idx];
-    int *piv = a.ipiv[idx];
-    double *Bs = (double *)sm;                         // n x k saved b (FP64)
-    double *Rr = Bs + (size_t)n * k;                   // n x k residual (FP64)
-    float *M = (float *)(Rr + (size_t)n * k);          // n x n FP32 factors
-    float *D = M + (size_t)n * n;                      // n x k FP32 solves
-    for (int e = lt; e < n * n; e += T) M[e] = (float)A[e % n + (size_t)(e / n) * lda];
-    for (int e = lt; e < n * k; e += T) {
-        const double v = B[e % n + (size_t)(e / n) * ldb];
-        Bs[e] = v;
-        D[e] = (float)v;
-    }
-    team_sync(bar, T);
-    const int info = team_gesv<float>(n, k, M, n, D, n, piv, lt, T, bar, rv, ri);
-    if (info != 0) {
-        if (lt == 0) a.info[idx] = info;
-        team_sync(bar, T);
-        return;
-    }
+// FP64 iterative refinement of the k solutions of A X = B (A, B in FP64,
+// global): the first FP32 solution is in D (n x k, ld n); b is saved in Bs
+// and the residuals go to Rr (FP64, ld n).  solve32() overwrites D with the
+// FP32 factors' solution of D.  Stops per column at a normwise backward error
+// <= n*eps64, when a step fails to halve it (flens/lapack/ge/rfs.tcc:182-188)
+// or after max_iter steps.
+template <typename Solve32>
+__device__ void refine_fp64(const BatchArgs &a, int idx, const double *A, int lda, double *B,
+                            int ldb, const double *Bs, double *Rr, float *D, int n, int k, int lt,
+                            int T, int bar, double *rv, Solve32 solve32) {
     // x0 (FP64) lives in B from here on
     for (int e = lt; e < n * k; e += T) B[e % n + (size_t)(e / n) * ldb] = (double)D[e];
     double anorm = 0.0, worst = 0.0;
@@ -728,7 +734,7 @@ __device__ void solve_mixed(const BatchArgs &a, int idx, unsigned char *sm, int 
         }
         team_sync(bar, T);
         if (!any) break;
-        team_lu_solve32(n, k, M, piv, D, lt, T, bar);
+        solve32();
         for (int e = lt; e < n * k; e += T) {
             const int c = e / n;
             const double sc = Rr[(size_t)c * n];
@@ -744,6 +750,93 @@ __device__ void solve_mixed(const BatchArgs &a, int idx, unsigned char *sm, int 
     team_sync(bar, T);
 }
 
+__device__ __noinline__ void solve_mixed(const BatchArgs &a, int idx, unsigned char *sm, int lt, int T, int bar,
+                            double *rv, int *ri) {
+    const int n = a.n[idx], k = a.nrhs[idx], lda = a.lda[idx], ldb = a.ldb[idx];
+    const double *A = a.A[idx];
+    double *B = a.B[idx];
+    int *piv = a.ipiv[idx];
+    double *Bs = (double *)sm;                         // n x k saved b (FP64)
+    double *Rr = Bs + (size_t)n * k;                   // n x k residual (FP64)
+    float *M = (float *)(Rr + (size_t)n * k);          // n x n FP32 factors
+    float *D = M + (size_t)n * n;                      // n x k FP32 solves
+    for (int e = lt; e < n * n; e += T) M[e] = (float)A[e % n + (size_t)(e / n) * lda];
+    for (int e = lt; e < n * k; e += T) {
+        const double v = B[e % n + (size_t)(e / n) * ldb];
+        Bs[e] = v;
+        D[e] = (float)v;
+    }
+    team_sync(bar, T);
+    const int info = team_gesv<float>(n, k, M, n, D, n, piv, lt, T, bar, rv, ri);
+    if (info != 0) {
+        if (lt == 0) a.info[idx] = info;
+        team_sync(bar, T);
+        return;
+    }
+    refine_fp64(a, idx, A, lda, B, ldb, Bs, Rr, D, n, k, lt, T, bar, rv,
+                [&]() { team_lu_solve32(n, k, M, piv, D, lt, T, bar); });
+}
+
+// The mixed variant for a matrix beyond the team's shared memory: FP32 copy
+// of A factored in place in the team's pool slot by the blocked LU (FP32
+// panels in shared memory, FP64 pivot search and scaling), the FP32 solves
+// staged in shared memory, FP64 residuals from the untouched A.
+__device__ bool mixed_blocked_ok(const BatchArgs &a, int n, int k, int nb, int T, size_t share) {
+    return a.mx_pool != nullptr && k <= 32 && BT_THREADS / T <= a.mx_teams &&
+           mx_need(n, k) <= a.mx_stride && blocked_need(n, nb, sizeof(float)) <= share;
+}
+
+__device__ __noinline__ void solve_mixed_blocked(const BatchArgs &a, int idx, unsigned char *sm, size_t share,
+                                    int nb, int slot, int lt, int T, int bar, double *rv,
+                                    int *ri) {
+    const int n = a.n[idx], k = a.nrhs[idx], lda = a.lda[idx], ldb = a.ldb[idx];
+    const double *A = a.A[idx];
+    double *B = a.B[idx];
+    int *piv = a.ipiv[idx];
+    char *base = (char *)a.mx_pool + (size_t)slot * a.mx_stride;
+    float *F = (float *)base;                                  // n x n FP32 factors
+    double *Bs = (double *)(base + mx_factor_bytes(n));        // n x k saved b
+    double *Rr = Bs + (size_t)n * k;                           // n x k residual
+    float *D = (float *)(Rr + (size_t)n * k);                  // n x k FP32 solves
+    for (int c0 = 0; c0 < n; c0 += 8)                          // eight loads before their stores
+        for (int r = lt; r < n; r += T) {
+            double v[8];
+#pragma unroll
+            for (int cc = 0; cc < 8; ++cc)
+                if (c0 + cc < n) v[cc] = A[r + (size_t)(c0 + cc) * lda];
+#pragma unroll
+            for (int cc = 0; cc < 8; ++cc)
+                if (c0 + cc < n) F[r + (size_t)(c0 + cc) * n] = (float)v[cc];
+        }
+    for (int c = 0; c < k; ++c)
+        for (int r = lt; r < n; r += T) {
+            const double v = B[r + (size_t)c * ldb];
+            Bs[r + (size_t)c * n] = v;
+            D[r + (size_t)c * n] = (float)v;
+        }
+    team_sync(bar, T);
+    float *ps = (float *)sm;
+    const int info = nb == 8 ? team_lu_blocked<float, 8>(n, F, n, piv, lt, T, bar, rv, ri, ps)
+                             : team_lu_blocked<float, 16>(n, F, n, piv, lt, T, bar, rv, ri, ps);
+    if (info != 0) {
+        if (lt == 0) a.info[idx] = info;
+        team_sync(bar, T);
+        return;
+    }
+    auto solve32 = [&]() {
+        if (staged_need(n, k, sizeof(float)) <= share)
+            team_trs_staged<float>(n, k, F, n, D, n, piv, lt, T, bar, ps);
+        else
+            team_trs<float>(n, k, F, n, D, n, piv, lt, T, bar);
+    };
+    solve32();
+    refine_fp64(a, idx, A, lda, B, ldb, Bs, Rr, D, n, k, lt, T, bar, rv, solve32);
+}
+
+// MIXED: the precision-1 kernel (FP32 LU + FP64 refinement paths); the FP64
+// kernel is compiled without them, so that their registers do not weigh on
+// the FP64 paths.
+template <bool MIXED>
 __global__ void __launch_bounds__(BT_THREADS, 1)
 batched_gesv_kernel(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char bsm[];
@@ -767,8 +860,13 @@ batched_gesv_kernel(BatchArgs a) {
             team_sync(bar, T);
             if (item >= end) break;
             const int idx = a.order[item];
-            if (a.precision == 1 && a.nrhs[idx] <= 32 && mixed_need(a.n[idx], a.nrhs[idx]) <= share)
+            if (MIXED && a.nrhs[idx] <= 32 && mixed_need(a.n[idx], a.nrhs[idx]) <= share)
                 solve_mixed(a, idx, sm, lt, T, bar, red_v[tm], red_i[tm]);
+            else if (MIXED && mixed_blocked_ok(a, a.n[idx], a.nrhs[idx], nb, T, share))
+                // slots [blockIdx.x * mx_teams, +teams): the same for every
+                // bucket, since CTAs move through the buckets independently
+                solve_mixed_blocked(a, idx, sm, share, nb, blockIdx.x * a.mx_teams + tm, lt, T, bar,
+                                    red_v[tm], red_i[tm]);
             else
                 solve_fp64(a, idx, sm, share, nb, lt, T, bar, red_v[tm], red_i[tm]);
         }
@@ -789,6 +887,7 @@ struct BatchedPlan {
     cudaGraphExec_t exec = nullptr;
     int team[BT_BUCKETS];
     int panel[BT_BUCKETS];
+    void *mx_pool = nullptr;        // precision 1: FP32 factors beyond shared memory
     std::vector<int> hn;
 };
 
@@ -851,8 +950,10 @@ void fill_ranges(const std::vector<int> &hn, std::vector<int> &order, BatchArgs 
 }
 
 int set_attributes() {
-    static DeviceOnce once;
-    return set_smem_once(once, (const void *)batched_gesv_kernel, (int)BT_SMEM);
+    static DeviceOnce once64, once32;
+    const int st = set_smem_once(once64, (const void *)batched_gesv_kernel<false>, (int)BT_SMEM);
+    if (st != kOk) return st;
+    return set_smem_once(once32, (const void *)batched_gesv_kernel<true>, (int)BT_SMEM);
 }
 
 // queue reset + the persistent kernel (also what a plan's graph holds)
@@ -860,7 +961,8 @@ int launch(const BatchArgs &a, cudaStream_t s) {
     int st = set_attributes();
     if (st != kOk) return st;
     FG_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(int) * BT_BUCKETS, s));
-    batched_gesv_kernel<<<num_sms(), BT_THREADS, BT_SMEM, s>>>(a);
+    if (a.precision == 1) batched_gesv_kernel<true><<<num_sms(), BT_THREADS, BT_SMEM, s>>>(a);
+    else batched_gesv_kernel<false><<<num_sms(), BT_THREADS, BT_SMEM, s>>>(a);
     FG_CUDA(cudaGetLastError());
     return kOk;
 }
@@ -1086,6 +1188,35 @@ int batched_plan_create(int count, const int *hn, const int *hk, double *const *
     a.queue = d_q;
     a.precision = precision;
     a.max_iter = max_iter > 0 ? max_iter : 10;
+    if (precision == 1) {
+        // pool for the matrices that take the blocked mixed path: a slot per
+        // team of the CTAs, as large as the largest such matrix needs (if it
+        // cannot be had, those matrices are solved in FP64 instead)
+        size_t stride = 0;
+        int teams = 0;
+        for (int b = 0; b < BT_BUCKETS; ++b) {
+            const int T = a.team[b];
+            const size_t share = team_share(T);
+            for (int i = a.beg[b]; i < a.end[b]; ++i) {
+                const int ni = hn[order[i]], ki = hk[order[i]];
+                if (ki > 32 || mixed_need(ni, ki) <= share) continue;
+                if (blocked_need(ni, a.panel[b], sizeof(float)) > share) continue;
+                stride = std::max(stride, mx_need(ni, ki));
+                teams = std::max(teams, BT_THREADS / T);
+            }
+        }
+        if (stride > 0) {
+            stride = (stride + 255) / 256 * 256;
+            if (cudaMalloc(&p->mx_pool, stride * (size_t)num_sms() * teams) == cudaSuccess) {
+                a.mx_pool = p->mx_pool;
+                a.mx_stride = stride;
+                a.mx_teams = teams;
+            } else {
+                cudaGetLastError();
+                p->mx_pool = nullptr;
+            }
+        }
+    }
     // capture the queue reset + persistent launch as one graph
     if ((st0 = set_attributes()) != kOk) return st0;
     cudaStream_t cap;
@@ -1097,8 +1228,10 @@ int batched_plan_create(int count, const int *hn, const int *hk, double *const *
     cudaStreamDestroy(cap);
     if (st != kOk || ce != cudaSuccess) {
         if (ce != cudaSuccess) cuda_fail(ce, "cudaStreamEndCapture");
+        if (g) cudaGraphDestroy(g);
         cudaFree(p->d_meta);
         cudaFree(p->d_ptrs);
+        if (p->mx_pool) cudaFree(p->mx_pool);
         delete p;
         return st != kOk ? st : kErrCuda;
     }
@@ -1121,6 +1254,7 @@ void batched_plan_destroy(BatchedPlan *p) {
     if (p->graph) cudaGraphDestroy(p->graph);
     if (p->d_meta) cudaFree(p->d_meta);
     if (p->d_ptrs) cudaFree(p->d_ptrs);
+    if (p->mx_pool) cudaFree(p->mx_pool);
     delete p;
 }
 

@@ -199,3 +199,58 @@ def test_batched_mixed_refinement(cuda):
         else:
             # FP32 working set too large for the team: the FP64 path, A <- LU
             assert oracle.lu_backward_error(A0, mats[i].cpu().numpy(), ipivs[i].cpu().numpy()[:n]) <= 10.0
+
+
+def test_batched_mixed_refinement_blocked_fp32(cuda, port):
+    # matrices whose FP32 working set does not fit a team's shared memory:
+    # FP32 factors of a copy of A in the plan's pool (blocked LU, panels in
+    # shared memory), FP64 refinement against the untouched A; k = 40 exceeds
+    # the 32 columns the refinement tracks and takes the FP64 path
+    sizes = [170, 257, 300, 431, 512, 333, 480]
+    ks = [1, 4, 16, 3, 1, 9, 40]
+    mats, rhs, host = make_batch(cuda, sizes, ks, 3100)
+    ipivs, info, iters, berr, teams = run_batched(cuda, mats, rhs, 1)
+    assert (info == 0).all(), info
+    for i, (A0, Bh) in enumerate(host):
+        n = sizes[i]
+        X = rhs[i].cpu().numpy()
+        R = Bh - A0 @ X
+        be = (np.abs(R).max(0) / (np.abs(A0).sum(1).max() * np.abs(X).max(0) + np.abs(Bh).max(0))).max()
+        assert be <= 10 * n * EPS, (i, n, be, iters[i])
+        A1, B1 = A0.copy(order="F"), Bh.copy(order="F")
+        pivr, _ = port.dgesv(A1, B1)
+        assert oracle.normwise_rel(X, B1) <= 1e-12, i
+        if ks[i] <= 32:
+            # the FP32 path ran: A untouched, refinement steps and backward error reported
+            assert iters[i] >= 0, (i, iters[i])
+            assert berr[i] <= 10 * n * EPS
+            np.testing.assert_array_equal(mats[i].cpu().numpy(), A0)
+            # FP64 pivot search on the FP32 factors of a diagonally dominant A
+            assert np.array_equal(ipivs[i].cpu().numpy()[:n], pivr), i
+        else:
+            assert iters[i] == -1
+            assert oracle.lu_backward_error(A0, mats[i].cpu().numpy(), ipivs[i].cpu().numpy()[:n]) <= 10.0
+
+
+def test_batched_mixed_many_buckets_no_slot_sharing(cuda):
+    # many matrices in buckets with different team sizes: CTAs move through
+    # the buckets independently, so the pool slots of the blocked FP32 path
+    # must not depend on the bucket's team size (a shared slot gives wrong
+    # or non-finite solutions for a few matrices, different from run to run)
+    import torch
+    sizes = [100, 200, 300, 420, 500, 96, 330] * 90
+    ks = [16, 4, 16, 16, 1, 16, 16] * 90
+    mats, rhs, host = make_batch(cuda, sizes, ks, 4100)
+    ipivs, info, iters, berr, teams = run_batched(cuda, mats, rhs, 1)
+    assert (info == 0).all()
+    assert (iters >= 0).all()
+    for i, (A0, Bh) in enumerate(host):
+        n = sizes[i]
+        A = torch.from_numpy(A0).to(cuda)
+        B = torch.from_numpy(Bh).to(cuda)
+        X = rhs[i]
+        assert torch.isfinite(X).all(), (i, n)
+        R = B - A @ X
+        den = A.abs().sum(1).max() * X.abs().amax(0) + B.abs().amax(0)
+        be = (R.abs().amax(0) / den).max().item()
+        assert be <= 10 * n * EPS, (i, n, ks[i], be, iters[i])
