@@ -14,11 +14,13 @@
 //     global memory (at these sizes, L2-resident);
 //   * T per bucket comes from the autotuner below (candidates timed on
 //     synthetic matrices of the bucket, cached per device);
-//   * precision 0 = FP64; 1 = FP32 LU in shared memory + FP64 iterative
-//     refinement (A untouched; r = b - A x in FP64 from global A; stop at a
-//     normwise backward error <= n*eps64, when a step fails to halve it
-//     (flens/lapack/ge/rfs.tcc:182-188) or after max_iter steps).  Matrices
-//     whose FP32 working set does not fit are solved in FP64 (iters = -1).
+//   * precision 0 = FP64; 1 = FP32 LU + FP64 iterative refinement (A
+//     untouched; r = b - A x in FP64 from global A; stop at a normwise
+//     backward error <= n*eps64, when a step fails to halve it
+//     (flens/lapack/ge/rfs.tcc:182-188) or after max_iter steps).  The FP32
+//     factors live in shared memory when they fit, otherwise in the plan's
+//     pool (blocked LU); matrices with more than 32 right-hand sides are
+//     solved in FP64 (iters = -1).
 #include "common.cuh"
 
 #include <float.h>

@@ -354,13 +354,17 @@ int flens_gb300_dgesv_mixed(int n, int nrhs, const double *A, int ldA,
  * info, iters, berr are DEVICE arrays of `count` entries written by every
  * execution.  precision 0 = FP64 (A_i <- LU factors); 1 = FP32 LU + FP64
  * refinement (A_i untouched, iters_i = refinement steps, berr_i = final
- * normwise backward error, max_iter bounds the steps) for every matrix whose
- * FP32 working set fits its team's shared memory; the others take the FP64
- * path (iters_i = -1, A_i <- LU factors).  B_i <- X_i when INFO_i == 0,
- * untouched otherwise.  Creating a plan
- * autotunes the team size of each size bucket (first use per device;
- * FLENS_GB300_BATCH_TUNE=0 disables it, FLENS_GB300_BATCH_TEAM=T forces T) and
- * captures one persistent launch in a CUDA graph.  Synchronises on stream. */
+ * normwise backward error, max_iter bounds the steps) for every matrix with
+ * nrhs_i <= 32: in the team's shared memory when its FP32 working set fits
+ * there, otherwise on FP32 factors of a copy of A_i in a device pool that the
+ * plan allocates (one slot per team, sized for the largest such matrix).
+ * Matrices with more right-hand sides, or all of them if that pool cannot be
+ * allocated, take the FP64 path (iters_i = -1, A_i <- LU factors).  B_i <- X_i
+ * when INFO_i == 0, untouched otherwise.  Creating a plan autotunes the team
+ * size and panel width of each size bucket (first use per device;
+ * FLENS_GB300_BATCH_TUNE=0 disables it, FLENS_GB300_BATCH_TEAM=T and
+ * FLENS_GB300_BATCH_PANEL=8|16 force them) and captures one persistent launch
+ * in a CUDA graph.  Synchronises on stream. */
 int flens_gb300_dgesv_batched_plan(int count, const int *n, const int *nrhs,
                                    double *const *A, const int *lda,
                                    int *const *ipiv, double *const *B,
