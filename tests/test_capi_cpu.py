@@ -296,3 +296,36 @@ def test_no_gpu_fails_loudly():
     piv, info = fg.dgetrf(A)
     assert info == fg.ERR_NO_DEVICE, (info, fg.last_error())
     assert fg.last_error() != ""
+
+
+def test_batched_queries_reject_missing_plans_and_buckets(flib):
+    # the plan queries answer -1 instead of reading through a null plan or past
+    # the last size bucket (no CUDA call is made)
+    vp = ctypes.c_void_p
+    for fn in (flib.flens_gb300_batched_team, flib.flens_gb300_batched_panel):
+        fn.argtypes = [vp, ctypes.c_int]
+        fn.restype = ctypes.c_int
+        assert fn(None, 0) == -1
+        assert fn(None, -1) == -1
+
+
+def test_batched_plan_argument_errors(flib):
+    # argument checks before any device work: negative count, bad precision,
+    # no output pointer, an illegal size in the metadata
+    vp = ctypes.c_void_p
+    f = flib.flens_gb300_dgesv_batched_plan
+    f.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int, vp, vp, ctypes.c_int,
+                  vp, ctypes.POINTER(ctypes.c_void_p)]
+    f.restype = ctypes.c_int
+    plan = ctypes.c_void_p()
+    n = np.array([4, -1], dtype=np.int32)
+    k = np.array([1, 1], dtype=np.int32)
+    ld = np.array([4, 4], dtype=np.int32)
+    assert f(-1, None, None, None, None, None, None, None, None, 0, None, None, 0, None,
+             ctypes.byref(plan)) == -1
+    assert f(0, None, None, None, None, None, None, None, None, 2, None, None, 0, None,
+             ctypes.byref(plan)) == -10
+    assert f(0, None, None, None, None, None, None, None, None, 0, None, None, 0, None, None) == -15
+    assert f(2, n.ctypes.data, k.ctypes.data, None, ld.ctypes.data, None, None, ld.ctypes.data,
+             None, 0, None, None, 0, None, ctypes.byref(plan)) == -2
+    assert "illegal size" in fg.last_error()
