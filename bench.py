@@ -769,6 +769,42 @@ def ctypes_stream(stream):
     return ctypes.c_void_p(stream.cuda_stream)
 
 
+def batched_cpu_baseline(sample=2000, seed=55):
+    """The batched configuration on the host cores: the oracle's dgesv (the C
+    restatement of the reference's trf + trs, bitwise the reference) over a
+    sample of matrices drawn like the batch (n log-uniform in [8, 512],
+    uniform[-1,1] + n/4 on the diagonal, k in {1, 4, 16}), one worker thread
+    per host core, each solving its share of the sample (the C calls release
+    the interpreter lock).  Returns solves/s for the whole host."""
+    import concurrent.futures as cf
+    import numpy as np
+    import oracle
+    rng = np.random.default_rng(seed)
+    n = np.floor(np.exp(rng.uniform(np.log(8), np.log(512.999), size=sample))).astype(np.int32)
+    k = rng.choice(np.array([1, 4, 16], dtype=np.int32), size=sample)
+    mats = []
+    for i in range(sample):
+        A = oracle.uniform(rng, int(n[i]), int(n[i]))
+        A[np.arange(n[i]), np.arange(n[i])] += n[i] / 4.0
+        mats.append((A, oracle.uniform(rng, int(n[i]), int(k[i]))))
+    port = oracle.Port()
+    threads = os.cpu_count() or 1
+
+    def work(lo):
+        for i in range(lo, sample, threads):
+            port.dgesv(mats[i][0], mats[i][1])
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(work, range(threads)))
+    t = time.perf_counter() - t0
+    flops = float(np.sum(2.0 / 3.0 * n.astype(np.float64) ** 3 + 2.0 * n.astype(np.float64) ** 2 * k))
+    return {"value": sample / t, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": (f"{sample} matrices drawn like the batch, oracle dgesv (bitwise the "
+                       f"reference's trf+trs), {threads} threads, {t:.2f} s"),
+            "gflops": flops / t / 1e9}
+
+
 def batched_subbench(torch, fg, dev, count=20000, reps=3, loop_sample=2000, uniform=None):
     """Batched configuration: `count` independent FP64 systems, n log-uniform
     in [8, 512], entries uniform[-1,1] + (n/4) I, k uniform in {1, 4, 16}.
@@ -897,6 +933,8 @@ def batched_subbench(torch, fg, dev, count=20000, reps=3, loop_sample=2000, unif
         out["speedup_vs_loop_fp64"] = fp64["solves_per_s"] / out["per_matrix_loop"]["solves_per_s"]
     del F0, F, G0, G, P
     torch.cuda.empty_cache()
+    if not uniform:
+        out["cpu_baseline"] = batched_cpu_baseline()
     return out
 
 
