@@ -769,7 +769,7 @@ def ctypes_stream(stream):
     return ctypes.c_void_p(stream.cuda_stream)
 
 
-def batched_cpu_baseline(sample=8000, seed=55):
+def batched_cpu_baseline(sample=4000, seed=55):
     """The batched configuration on the host cores: the oracle's dgesv (the C
     restatement of the reference's trf + trs, bitwise the reference) over a
     sample of matrices drawn like the batch (n log-uniform in [8, 512],
