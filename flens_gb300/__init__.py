@@ -163,7 +163,7 @@ def last_error() -> str:
 
 
 # ------------------------------------------------------ instrumentation ---
-N_FAMILIES = 9
+N_FAMILIES = 12
 
 
 def launch_count() -> int:

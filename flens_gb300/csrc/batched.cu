@@ -1152,8 +1152,8 @@ int batched_plan_create(int count, const int *hn, const int *hk, double *const *
         a.panel[b] = p->panel[b] = c.second;
     }
     const size_t intBytes = (size_t)count * 4;
-    if (cudaMalloc((void **)&p->d_meta, 5 * intBytes + BT_BUCKETS * 4) != cudaSuccess ||
-        cudaMalloc((void **)&p->d_ptrs, 3 * (size_t)count * sizeof(void *)) != cudaSuccess) {
+    if (device_malloc((void **)&p->d_meta, 5 * intBytes + BT_BUCKETS * 4) != cudaSuccess ||
+        device_malloc((void **)&p->d_ptrs, 3 * (size_t)count * sizeof(void *)) != cudaSuccess) {
         cudaGetLastError();
         set_last_error("batched plan: device allocation failed");
         if (p->d_meta) cudaFree(p->d_meta);
@@ -1209,7 +1209,7 @@ int batched_plan_create(int count, const int *hn, const int *hk, double *const *
         }
         if (stride > 0) {
             stride = (stride + 255) / 256 * 256;
-            if (cudaMalloc(&p->mx_pool, stride * (size_t)num_sms() * teams) == cudaSuccess) {
+            if (device_malloc(&p->mx_pool, stride * (size_t)num_sms() * teams) == cudaSuccess) {
                 a.mx_pool = p->mx_pool;
                 a.mx_stride = stride;
                 a.mx_teams = teams;

@@ -93,7 +93,13 @@ int stage_buf(int slot, size_t bytes, void **out) {
             t_stage.buf[slot] = nullptr;
             t_stage.bytes[slot] = 0;
         }
-        FG_CUDA(cudaMalloc(&t_stage.buf[slot], bytes < 256 ? 256 : bytes));
+        const cudaError_t e = device_malloc(&t_stage.buf[slot], bytes < 256 ? 256 : bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            t_stage.buf[slot] = nullptr;
+            set_last_error("cudaMalloc of %zu bytes of host-call staging failed", bytes);
+            return kErrAlloc;
+        }
         t_stage.bytes[slot] = bytes;
     }
     *out = t_stage.buf[slot];

@@ -37,6 +37,12 @@ enum DeviceStatus : int {
 void set_last_error(const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 
+// Every device allocation of the library goes through here: it counts the
+// allocations (flens_gb300_device_alloc_count) and honours the host-side
+// failure hook flens_gb300_test_fail_device_allocs, which makes the next
+// allocations fail as cudaMalloc does when the device is out of memory.
+cudaError_t device_malloc(void **p, size_t bytes);
+
 #define FG_CUDA(call)                                                     \
     do {                                                                  \
         cudaError_t _e = (call);                                          \
@@ -125,7 +131,10 @@ enum Family : int {
     kFamRefine = 6,   // residual / refinement / Krylov helpers
     kFamBatched = 7,  // batched LU
     kFamSplit = 8,    // split-precision FP64 GEMM (slicing + tensor-core products)
-    kFamCount = 9
+    kFamTrsv = 9,     // chained triangular solves with few vectors (trs, refinement)
+    kFamKrylov = 10,  // GMRES: permutation, Gram-Schmidt, norms, updates
+    kFamPrecond = 11, // GMRES preconditioner: block inverses and chained solves
+    kFamCount = 12
 };
 
 struct KTimer {
@@ -208,6 +217,19 @@ int dgemm_kr_launch(char transA, char transB, int m, int n, int k, double alpha,
 int dtrsm_launch(char side, char upLo, char transA, char diag, int m, int n,
                  double alpha, const double *A, int ldA, double *B, int ldB,
                  cudaStream_t stream);
+
+// Scratch of the chained triangular solve supplied by the caller instead of
+// the stream's workspace: `flags` holds `cap` ready flags, which the solve
+// clears on its stream (cudaMemsetAsync) before each use, so every call
+// publishes the same epoch; `status` receives the bounded-wait timeout bit.
+struct ChainFixed {
+    unsigned long long *flags;
+    int cap;
+    int *status;
+};
+int dtrsm_launch_fixed(char side, char upLo, char transA, char diag, int m, int n,
+                       double alpha, const double *A, int ldA, double *B, int ldB,
+                       const ChainFixed &fx, cudaStream_t stream);
 
 int dscal_matrix_launch(int m, int n, double alpha, double *B, int ldB,
                         cudaStream_t stream);

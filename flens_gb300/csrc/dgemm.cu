@@ -331,6 +331,79 @@ dgemm_skinny_tn_kernel(int m, int n, int k, T alpha, const T *__restrict__ A, in
     }
 }
 
+// op(A) = A with a long k and at most 4 vectors (the residuals and Krylov
+// products of the refinement, n x n times n x 1..4).  The kernel above gives
+// a thread one row and walks k with one load in flight, so a 16384^2 GEMV
+// streams A at a few percent of HBM.  Here a CTA owns one memory line of rows
+// (128 bytes: 16 doubles or 32 floats); its 256 threads are G column groups
+// of LR lanes, group g reading columns g, g+G, g+2G, ...  Each thread issues
+// 8 column loads before their FMAs, and there are k/G of them per group, so
+// the grid of m/LR CTAs keeps enough lines in flight to stream A at HBM
+// speed.  The groups' partial sums are added in a fixed order at the end
+// (deterministic).
+constexpr int GV_UNROLL = 8;
+
+template <typename T, int NC, bool TB>
+__global__ void __launch_bounds__(256)
+gemv_rows_kernel(int m, int n, int k, T alpha, const T *__restrict__ A, int ldA,
+                 const T *__restrict__ B, int ldB, T beta, T *__restrict__ C, int ldC) {
+    constexpr int LR = 128 / (int)sizeof(T);     // rows per CTA = lanes per column
+    constexpr int G = 256 / LR;                  // column groups
+    __shared__ T red[G][NC][LR];
+    const int r = threadIdx.x % LR, g = threadIdx.x / LR;
+    const int i = blockIdx.x * LR + r;
+    T acc[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) acc[j] = T(0);
+    if (i < m) {
+        const T *a = A + i;
+        auto xv = [&](int p, int j) -> T {
+            return TB ? __ldg(&B[(size_t)j + (size_t)p * ldB]) : __ldg(&B[(size_t)p + (size_t)j * ldB]);
+        };
+        int p = g;
+        for (; p + (GV_UNROLL - 1) * G < k; p += GV_UNROLL * G) {
+            T av[GV_UNROLL];
+#pragma unroll
+            for (int u = 0; u < GV_UNROLL; ++u) av[u] = __ldg(&a[(size_t)(p + u * G) * ldA]);
+#pragma unroll
+            for (int u = 0; u < GV_UNROLL; ++u) {
+#pragma unroll
+                for (int j = 0; j < NC; ++j)
+                    if (j < n) acc[j] = fma(av[u], xv(p + u * G, j), acc[j]);
+            }
+        }
+        for (; p < k; p += G) {
+            const T av = __ldg(&a[(size_t)p * ldA]);
+#pragma unroll
+            for (int j = 0; j < NC; ++j)
+                if (j < n) acc[j] = fma(av, xv(p, j), acc[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NC; ++j) red[g][j][r] = acc[j];
+    __syncthreads();
+    if (threadIdx.x < LR * NC) {
+        const int rr = threadIdx.x % LR, j = threadIdx.x / LR;
+        const int ii = blockIdx.x * LR + rr;
+        if (ii < m && j < n) {
+            T s = T(0);
+#pragma unroll
+            for (int q = 0; q < G; ++q) s += red[q][j][rr];
+            T *c = &C[(size_t)ii + (size_t)j * ldC];
+            *c = fma(alpha, s, beta * *c);
+        }
+    }
+}
+
+template <typename T, int NC>
+void launch_gemv_rows(bool tb, int m, int n, int k, T alpha, const T *A, int ldA, const T *B,
+                      int ldB, T beta, T *C, int ldC, cudaStream_t s) {
+    constexpr int LR = 128 / (int)sizeof(T);
+    const int grid = ceil_div(m, LR);
+    if (tb) gemv_rows_kernel<T, NC, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+    else gemv_rows_kernel<T, NC, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
+}
+
 template <typename T, int NC>
 void launch_skinny(bool ta, bool tb, int m, int n, int k, T alpha, const T *A, int ldA,
                    const T *B, int ldB, T beta, T *C, int ldC, cudaStream_t s) {
@@ -406,6 +479,14 @@ int gemm_launch_t(char transA, char transB, int m, int n, int k, T alpha, const 
     }
     KTimer kt(sizeof(T) == 8 ? kFamGemm : kFamAux, stream, 2.0 * m * n * (double)k,
               (double)sizeof(T) * ((double)m * k + (double)k * n + 2.0 * m * n));
+    if (!ta && n <= 4 && k >= 256 && (size_t)m * k >= ((size_t)1 << 20)) {
+        trace("gemm<%d> %c%c m=%d n=%d k=%d engine=gemv_rows", (int)sizeof(T), transA, transB, m, n, k);
+        if (n <= 1) launch_gemv_rows<T, 1>(tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
+        else if (n <= 2) launch_gemv_rows<T, 2>(tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
+        else launch_gemv_rows<T, 4>(tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);
+        FG_CUDA(cudaGetLastError());
+        return kOk;
+    }
     if (n <= 16) {
         trace("gemm<%d> %c%c m=%d n=%d k=%d engine=skinny", (int)sizeof(T), transA, transB, m, n, k);
         if (n <= 1) launch_skinny<T, 1>(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, stream);

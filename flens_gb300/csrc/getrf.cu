@@ -789,14 +789,17 @@ int sgetrs_launch(char trans, int n, int nrhs, const float *A, int ldA, const in
 // another framework, or a host that links this library into a process where
 // device allocation is forbidden after start-up (a failed or blocking
 // cudaMalloc there would stall or abort the caller).  flens_gb300_dgetrs
-// takes its scratch (the row permutation and the gathered right-hand sides of
-// the row interchanges) from a per-stream workspace that it grows with
-// cudaMalloc on first use; this entry point takes the same scratch from the
-// fixed file-scope array below instead and calls no allocating routine.
+// takes its scratch (the row permutation and gathered right-hand sides of the
+// row interchanges, and for up to 4 right-hand sides the ready flags and
+// status word of the chained triangular solve) from a per-stream workspace
+// that it creates with cudaMalloc on first use; this entry point takes all of
+// it from the fixed file-scope array below instead and calls no allocating
+// routine.
 //
 // Limits and rules:
-//  * the array holds 8 MiB; a call needs round_up(4*n, 256) + 8*n*nrhs bytes
-//    (n = 8192 allows nrhs <= 127) and larger calls are rejected with
+//  * the array holds 8 MiB: 32 KiB of chain flags, a 256-byte status word,
+//    and round_up(4*n, 256) + 8*n*nrhs bytes of interchange scratch per call
+//    (n = 8192 allows nrhs <= 127); larger calls are rejected with
 //    FLENS_GB300_ERR_UNSUPPORTED and a message in flens_gb300_last_error();
 //  * every GPU that loads the library holds the array until the process exits;
 //  * all calls on a device share the one array: calls whose work overlaps on
@@ -804,13 +807,20 @@ int sgetrs_launch(char trans, int n, int nrhs, const float *A, int ldA, const in
 //    must be serialised by the caller;
 //  * the first call on a device looks the array's device address up
 //    (cudaGetSymbolAddress) -- make that first call before any stream capture.
-// The array keeps the last call's contents; nothing in it has to start at
-// zero (the permutation is rebuilt from the identity and the gather buffer is
-// fully written before it is read on every call).
+// The array keeps the last call's contents.  What must start at zero is
+// cleared on the call's stream by each call (cudaMemsetAsync, which does not
+// allocate): the chain flags before every chained solve, and the status
+// word.  The permutation is rebuilt from the identity and the gather buffer
+// is fully written before it is read.  The chained solve's waits are bounded;
+// a wait that gave up (not expected: every block of that cooperative launch is
+// resident) leaves its bit in the array's status word, where this entry point
+// does not report it.
 namespace fg {
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = 8u << 20;
+constexpr int kNoAllocFlags = 4096;                                   // chain flags
+constexpr size_t kNoAllocHead = kNoAllocFlags * sizeof(unsigned long long) + 256;   // + status word
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 std::mutex g_noalloc_mu;
@@ -883,23 +893,32 @@ FG_API int flens_gb300_dgetrs_noalloc(char trans, int n, int nrhs, const double 
     if (ldA < (n > 1 ? n : 1)) return -5;
     if (ldB < (n > 1 ? n : 1)) return -8;
     if (n == 0 || nrhs == 0) return kOk;
-    const size_t need = noalloc_needed(n, nrhs);
+    const size_t need = kNoAllocHead + noalloc_needed(n, nrhs);
     if (need > kNoAllocScratchBytes) {
         set_last_error("flens_gb300_dgetrs_noalloc: n=%d nrhs=%d needs %zu bytes of scratch, "
                        "more than its fixed %zu-byte array; use flens_gb300_dgetrs or fewer "
                        "right-hand sides per call", n, nrhs, need, kNoAllocScratchBytes);
         return kErrUnsupported;
     }
-    void *scratch = nullptr;
-    int st = noalloc_scratch(&scratch);
+    void *base = nullptr;
+    int st = noalloc_scratch(&base);
     if (st != kOk) return st;
     cudaStream_t s = (cudaStream_t)stream;
+    ChainFixed fx;
+    fx.flags = (unsigned long long *)base;
+    fx.cap = kNoAllocFlags;
+    fx.status = (int *)((char *)base + kNoAllocFlags * sizeof(unsigned long long));
+    void *scratch = (char *)base + kNoAllocHead;
+    FG_CUDA(cudaMemsetAsync(fx.status, 0, sizeof(int), s));
     if (trans == 'N') {
         if ((st = laswp_fixed(n, nrhs, B, ldB, 1, n, ipiv, 1, scratch, s)) != kOk) return st;
-        if ((st = dtrsm_launch('L', 'L', 'N', 'U', n, nrhs, 1.0, A, ldA, B, ldB, s)) != kOk) return st;
-        return dtrsm_launch('L', 'U', 'N', 'N', n, nrhs, 1.0, A, ldA, B, ldB, s);
+        if ((st = dtrsm_launch_fixed('L', 'L', 'N', 'U', n, nrhs, 1.0, A, ldA, B, ldB, fx, s)) != kOk)
+            return st;
+        return dtrsm_launch_fixed('L', 'U', 'N', 'N', n, nrhs, 1.0, A, ldA, B, ldB, fx, s);
     }
-    if ((st = dtrsm_launch('L', 'U', 'T', 'N', n, nrhs, 1.0, A, ldA, B, ldB, s)) != kOk) return st;
-    if ((st = dtrsm_launch('L', 'L', 'T', 'U', n, nrhs, 1.0, A, ldA, B, ldB, s)) != kOk) return st;
+    if ((st = dtrsm_launch_fixed('L', 'U', 'T', 'N', n, nrhs, 1.0, A, ldA, B, ldB, fx, s)) != kOk)
+        return st;
+    if ((st = dtrsm_launch_fixed('L', 'L', 'T', 'U', n, nrhs, 1.0, A, ldA, B, ldB, fx, s)) != kOk)
+        return st;
     return laswp_fixed(n, nrhs, B, ldB, 1, n, ipiv, -1, scratch, s);
 }

@@ -133,14 +133,42 @@ col_absmax_kernel(int n, const double *__restrict__ X, int ldx, double *__restri
     }
 }
 
-// ||A||_inf = max_i sum_j |A(i, j)|; non-negative doubles order like their bits
+// ||A||_inf = max_i sum_j |A(i, j)|.  A CTA per 16 rows (one 128-byte line of
+// each column) and 16 column groups, 8 loads in flight per thread, so the
+// sweep streams A at HBM speed (a thread per row walking all columns with one
+// load in flight took milliseconds at n = 16384).  The row sums are added in
+// a fixed order and the maximum is an integer atomic: non-negative doubles
+// order like their bit patterns, and a NaN sum wins.
 __global__ void __launch_bounds__(256)
 inf_norm_kernel(int n, const double *__restrict__ A, int lda, unsigned long long *__restrict__ out) {
-    const int i = blockIdx.x * 256 + threadIdx.x;
-    if (i >= n) return;
+    constexpr int LR = 16, G = 16, U = 8;
+    __shared__ double red[G][LR];
+    const int r = threadIdx.x % LR, g = threadIdx.x / LR;
+    const int i = blockIdx.x * LR + r;
     double s = 0.0;
-    for (int j = 0; j < n; ++j) s += fabs(A[(size_t)i + (size_t)j * lda]);
-    atomicMax(out, (unsigned long long)__double_as_longlong(s));
+    if (i < n) {
+        const double *a = A + i;
+        int p = g;
+        for (; p + (U - 1) * G < n; p += U * G) {
+            double v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) v[u] = __ldg(&a[(size_t)(p + u * G) * lda]);
+#pragma unroll
+            for (int u = 0; u < U; ++u) s += fabs(v[u]);
+        }
+        for (; p < n; p += G) s += fabs(__ldg(&a[(size_t)p * lda]));
+    }
+    red[g][r] = s;
+    __syncthreads();
+    if (threadIdx.x < LR) {
+        const int ii = blockIdx.x * LR + threadIdx.x;
+        if (ii < n) {
+            double t = 0.0;
+#pragma unroll
+            for (int q = 0; q < G; ++q) t += red[q][threadIdx.x];
+            atomicMax(out, (unsigned long long)__double_as_longlong(t));
+        }
+    }
 }
 
 // h[c] += sum_r V(r, c) w(r), c < k (h zeroed by the caller); grid (chunks, k)
@@ -198,6 +226,228 @@ __global__ void s2d_matrix_kernel(int n, const float *__restrict__ S, int lds, d
     }
 }
 
+// ---------------------------------------------------------------------------
+// The GMRES preconditioner z = U^-1 L^-1 P v: the factors as stored (FP32, or
+// FP64 for the split LU) applied in FP64 arithmetic, one vector.  A
+// substitution solve is a chain of 64-row blocks, and GB300 issues FP64 at 2
+// lanes per clock per SM, so a 64-step substitution inside each block (about
+// 4 us in one warp) would dominate the chain.  Instead, per block b of the
+// triangle (pred = the block solved just before b, b-1 for L and b+1 for U):
+//   Dinv_b = inverse of the diagonal block (FP64, from the stored values),
+//   P_b    = Dinv_b * M(b, pred),
+//   x_b    = Dinv_b (v_b - sum over blocks before pred of M(b,k) x_k) - P_b x_pred.
+// Everything but the last product is computed while the predecessor is still
+// being solved, so the chain's critical path per block is one 64x64 FP64
+// product (4096 FMAs, about 1 us on one SM) plus the flag hand-over.  The
+// inverses make this a slightly different (equally fixed, linear) operator
+// than substitution: its error is of order cond(diagonal block) * u64, far
+// below the factors' own low-precision error, and GMRES only needs the
+// preconditioner to be the same operator every time it is applied.
+constexpr int PC_NB = 64;
+constexpr int PC_THREADS = 256;
+constexpr int PC_PREP_SMEM = 2 * PC_NB * (PC_NB + 1) * (int)sizeof(double);
+
+// Dinv and P of every block, stored [block][p][r] (column-major 64 x 64);
+// rows and columns beyond the matrix are identity (Dinv) and zero (P).
+template <typename MT, bool LOWER>
+__global__ void __launch_bounds__(PC_THREADS)
+pc_prep_kernel(int n, const MT *__restrict__ F, int ldf, double *__restrict__ Dinv,
+               double *__restrict__ P) {
+    extern __shared__ double pc_sm[];
+    double(*D)[PC_NB + 1] = (double(*)[PC_NB + 1])pc_sm;                       // D[i][j] = M(R0+i, j)
+    double(*Y)[PC_NB + 1] = (double(*)[PC_NB + 1])(pc_sm + PC_NB * (PC_NB + 1));   // Y[i][c] = Dinv(i, c)
+    const int nblk = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
+    const int R0 = b * PC_NB, kb = min(PC_NB, n - R0);
+    for (int e = tid; e < PC_NB * PC_NB; e += PC_THREADS) {
+        const int i = e % PC_NB, j = e / PC_NB;
+        double v = (i == j) ? 1.0 : 0.0;
+        if (i < kb && j < kb && (LOWER ? j < i : j >= i))
+            v = (double)F[(size_t)(R0 + i) + (size_t)(R0 + j) * ldf];
+        D[i][j] = v;
+    }
+    __syncthreads();
+    if (tid < PC_NB) {          // column c of the inverse by substitution
+        const int c = tid;
+        if (LOWER) {
+            for (int i = 0; i < c; ++i) Y[i][c] = 0.0;
+            Y[c][c] = 1.0;
+            for (int i = c + 1; i < PC_NB; ++i) {
+                double s = 0.0;
+                for (int j = c; j < i; ++j) s = fma(D[i][j], Y[j][c], s);
+                Y[i][c] = -s;
+            }
+        } else {
+            for (int i = c + 1; i < PC_NB; ++i) Y[i][c] = 0.0;
+            Y[c][c] = 1.0 / D[c][c];
+            for (int i = c - 1; i >= 0; --i) {
+                double s = 0.0;
+                for (int j = i + 1; j <= c; ++j) s = fma(D[i][j], Y[j][c], s);
+                Y[i][c] = -s / D[i][i];
+            }
+        }
+    }
+    __syncthreads();
+    double *dout = Dinv + (size_t)b * PC_NB * PC_NB;
+    for (int e = tid; e < PC_NB * PC_NB; e += PC_THREADS) dout[e] = Y[e % PC_NB][e / PC_NB];
+    const int pred = LOWER ? b - 1 : b + 1;
+    if (pred < 0 || pred >= nblk) return;                 // uniform over the CTA
+    const int K0 = pred * PC_NB, kk = min(PC_NB, n - K0);
+    for (int e = tid; e < PC_NB * PC_NB; e += PC_THREADS) {   // D no longer read: reuse
+        const int i = e % PC_NB, j = e / PC_NB;
+        D[i][j] = (i < kb && j < kk) ? (double)F[(size_t)(R0 + i) + (size_t)(K0 + j) * ldf] : 0.0;
+    }
+    __syncthreads();
+    double *pout = P + (size_t)b * PC_NB * PC_NB;
+    for (int e = tid; e < PC_NB * PC_NB; e += PC_THREADS) {
+        const int r = e % PC_NB, p = e / PC_NB;
+        double s = 0.0;
+        for (int t = 0; t < PC_NB; ++t) s = fma(Y[r][t], D[t][p], s);
+        pout[e] = s;
+    }
+}
+
+__device__ __forceinline__ void pc_release(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long pc_acquire(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Thread (r, q) of a block's solve: row r, 16-column quarter q.  The stored
+// block M(b, k) in registers: 16 values along row R0+r (coalesced over r).
+template <typename MT>
+__device__ __forceinline__ void pc_fetch(MT (&v)[16], const MT *__restrict__ F, int ldf, int n,
+                                         int row, bool rok, int K0, int q) {
+    const MT *src = F + (size_t)row + (size_t)(K0 + 16 * q) * ldf;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) v[u] = (rok && K0 + 16 * q + u < n) ? src[(size_t)u * ldf] : MT(0);
+}
+
+// Waits (thread 0, bounded) until flags[idx] holds the call's epoch; false
+// on a timeout (status set), after which the CTA must return.
+__device__ __forceinline__ bool pc_wait(const unsigned long long *flags, int idx,
+                                        unsigned long long epoch, int *status, int *s_abort) {
+    if (threadIdx.x == 0) {
+        unsigned spins = 0;
+        while (pc_acquire(&flags[idx]) != epoch) {
+            if (++spins > kSpinLimit) {
+                atomicOr(status, kDevBarrierTimeout);
+                *s_abort = 1;
+                break;
+            }
+            if (spins > 32) __nanosleep(32);
+        }
+    }
+    __syncthreads();
+    return *s_abort == 0;
+}
+
+// One triangle of the preconditioner in place on X (n), in ONE cooperative
+// launch: CTA s solves the s-th block in solve order (the first rows for L,
+// the last for U) and publishes it with a release store of the call's epoch.
+// The stored blocks before the predecessor are applied as they are published,
+// the next one loaded into registers while waiting for the current one.
+template <typename MT, bool LOWER>
+__global__ void __launch_bounds__(PC_THREADS, 2)
+pc_chain_kernel(int n, const MT *__restrict__ F, int ldf, const double *__restrict__ Dinv,
+                const double *__restrict__ P, double *X, unsigned long long *flags,
+                unsigned long long epoch, int *status) {
+    __shared__ double xk[2][PC_NB];
+    __shared__ double part[4][PC_NB];
+    __shared__ double rhs[PC_NB];
+    __shared__ int s_abort;
+    const int nblk = gridDim.x, s = blockIdx.x, tid = threadIdx.x;
+    const int b = LOWER ? s : nblk - 1 - s;
+    const int R0 = b * PC_NB, kb = min(PC_NB, n - R0);
+    const int r = tid & (PC_NB - 1), q = tid >> 6;
+    const bool rok = r < kb;
+    if (tid == 0) s_abort = 0;
+    double di[16], pi[16];
+    {
+        const double *dsrc = Dinv + (size_t)b * PC_NB * PC_NB + (size_t)(16 * q) * PC_NB + r;
+        const double *psrc = P + (size_t)b * PC_NB * PC_NB + (size_t)(16 * q) * PC_NB + r;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            di[u] = dsrc[u * PC_NB];
+            pi[u] = s > 0 ? psrc[u * PC_NB] : 0.0;
+        }
+    }
+    // blocks solved before the predecessor: solve-order indices 0 .. s-2
+    const int npre = s - 1;
+    double acc = 0.0;
+    MT c0[16], c1[16];
+    auto kblk = [&](int s2) { return (LOWER ? s2 : nblk - 1 - s2) * PC_NB; };
+    auto apply = [&](MT(&v)[16], int s2, int buf) -> bool {
+        if (!pc_wait(flags, s2, epoch, status, &s_abort)) return false;
+        const int K0 = kblk(s2);
+        if (tid < PC_NB) xk[buf][tid] = (K0 + tid < n) ? __ldcg(&X[K0 + tid]) : 0.0;
+        __syncthreads();
+        // the block's 16 products summed on their own, then added
+        double blk = 0.0;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) blk = fma((double)v[u], xk[buf][16 * q + u], blk);
+        acc += blk;
+        return true;
+    };
+    if (npre > 0) pc_fetch(c0, F, ldf, n, R0 + r, rok, kblk(0), q);
+    for (int s2 = 0; s2 < npre; s2 += 2) {
+        if (s2 + 1 < npre) pc_fetch(c1, F, ldf, n, R0 + r, rok, kblk(s2 + 1), q);
+        if (!apply(c0, s2, 0)) return;
+        if (s2 + 1 >= npre) break;
+        if (s2 + 2 < npre) pc_fetch(c0, F, ldf, n, R0 + r, rok, kblk(s2 + 2), q);
+        if (!apply(c1, s2 + 1, 1)) return;
+    }
+    part[q][r] = acc;
+    __syncthreads();
+    if (q == 0) rhs[r] = rok ? __ldcg(&X[R0 + r]) - ((part[0][r] + part[1][r]) + (part[2][r] + part[3][r]))
+                             : 0.0;
+    __syncthreads();
+    double cp = 0.0;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) cp = fma(di[u], rhs[16 * q + u], cp);
+    part[q][r] = cp;                 // every read of part above precedes the last barrier
+    __syncthreads();
+    double xr = (part[0][r] + part[1][r]) + (part[2][r] + part[3][r]);
+    if (s > 0) {
+        if (!pc_wait(flags, s - 1, epoch, status, &s_abort)) return;
+        const int P0 = (LOWER ? b - 1 : b + 1) * PC_NB;
+        if (tid < PC_NB) xk[0][tid] = (P0 + tid < n) ? __ldcg(&X[P0 + tid]) : 0.0;
+        __syncthreads();
+        double pp = 0.0;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) pp = fma(pi[u], xk[0][16 * q + u], pp);
+        part[q][r] = pp;
+        __syncthreads();
+        xr -= (part[0][r] + part[1][r]) + (part[2][r] + part[3][r]);
+    }
+    if (q == 0 && rok) X[R0 + r] = xr;
+    __syncthreads();
+    if (tid == 0) pc_release(&flags[s], epoch);
+}
+
+// Blocks per SM of the chain kernel (0 if the query fails), per device.
+template <typename MT>
+int pc_chain_per_sm() {
+    static int cached[64];
+    const int d = device_id();
+    if (d < 0 || d >= 64) return 0;
+    if (cached[d] == 0) {
+        int lo = 0, up = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lo, pc_chain_kernel<MT, true>, PC_THREADS,
+                                                          0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&up, pc_chain_kernel<MT, false>, PC_THREADS,
+                                                          0) != cudaSuccess) {
+            cudaGetLastError();
+            lo = up = 0;
+        }
+        const int bps = lo < up ? lo : up;
+        cached[d] = bps > 0 ? bps : -1;
+    }
+    return cached[d] > 0 ? cached[d] : 0;
+}
+
 int grid_for(size_t total) {
     int b = (int)ceil_div(total, (size_t)256);
     const int cap = num_sms() * 8;
@@ -238,7 +488,57 @@ struct Solver {
     double *h2 = nullptr;       // M+2 (second Gram-Schmidt pass)
     double anorm = 0.0;
     std::vector<double> bnorm;
+    // preconditioner blocks (pc_prep_kernel): Dinv and P of L, then of U
+    double *pcDL = nullptr, *pcPL = nullptr, *pcDU = nullptr, *pcPU = nullptr;
+    bool pc = false;            // chained block-inverse preconditioner in use
 };
+
+// Whether the chained block-inverse preconditioner fits (every block of the
+// triangle resident at once for the cooperative launch).
+bool pc_fits(int n, bool fp64_factors) {
+    const int nblk = ceil_div(n, PC_NB);
+    const int per = fp64_factors ? pc_chain_per_sm<double>() : pc_chain_per_sm<float>();
+    return per > 0 && (long long)per * num_sms() >= nblk && nblk <= 4096;
+}
+
+size_t pc_bytes(int n) { return 4 * a256((size_t)ceil_div(n, PC_NB) * PC_NB * PC_NB * sizeof(double)); }
+
+// Dinv and P of both triangles of the stored factors.
+template <typename MT>
+int pc_prepare(Solver &S, const MT *F, int ldf) {
+    const int nblk = ceil_div(S.n, PC_NB);
+    static DeviceOnce onceL, onceU;
+    int st = set_smem_once(onceL, (const void *)pc_prep_kernel<MT, true>, PC_PREP_SMEM);
+    if (st != kOk) return st;
+    if ((st = set_smem_once(onceU, (const void *)pc_prep_kernel<MT, false>, PC_PREP_SMEM)) != kOk)
+        return st;
+    KTimer kt(kFamPrecond, S.s, 2.0 * nblk * 4.0 * PC_NB * PC_NB * PC_NB,
+              2.0 * S.n * (double)S.n * sizeof(MT));
+    pc_prep_kernel<MT, true><<<nblk, PC_THREADS, PC_PREP_SMEM, S.s>>>(S.n, F, ldf, S.pcDL, S.pcPL);
+    pc_prep_kernel<MT, false><<<nblk, PC_THREADS, PC_PREP_SMEM, S.s>>>(S.n, F, ldf, S.pcDU, S.pcPU);
+    FG_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+// One triangle of the preconditioner in place on x (device, n).
+template <typename MT>
+int pc_solve(Solver &S, const MT *F, int ldf, bool lower, double *x) {
+    int n = S.n;
+    const int nblk = ceil_div(n, PC_NB);
+    unsigned long long *flags = nullptr, epoch = 0;
+    int st = workspace_flags(S.s, nblk, &flags, &epoch);
+    if (st != kOk) return st;
+    Workspace *w = workspace_for(S.s, 0);
+    if (!w) return kErrAlloc;
+    int *status = w->status;
+    const double *Dv = lower ? S.pcDL : S.pcDU;
+    const double *Pv = lower ? S.pcPL : S.pcPU;
+    void *args[] = {&n, &F, &ldf, &Dv, &Pv, &x, &flags, &epoch, &status};
+    KTimer kt(kFamPrecond, S.s, (double)n * n, (double)n * n * sizeof(MT) / 2.0 + 16.0 * n * PC_NB);
+    const void *fn = lower ? (const void *)pc_chain_kernel<MT, true> : (const void *)pc_chain_kernel<MT, false>;
+    FG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(nblk), dim3(PC_THREADS), args, 0, S.s));
+    return kOk;
+}
 
 // out(:, 0:ncols) = (LU)^-1 X(:, 0:ncols), in FP32 on X scaled per column by
 // `scale` (device, ncols); out may alias X.
@@ -246,14 +546,17 @@ int lu_solve(Solver &S, int ncols, const double *X, int ldx, const double *scale
              int ldo, bool add) {
     if (S.precision == kPrecSplit) {
         // FP64 factors: P, L^-1, U^-1 in FP64 (no scaling needed)
-        KTimer kt(kFamRefine, S.s, 2.0 * S.n * (double)S.n * ncols, 8.0 * S.n * (double)S.n);
-        gather_cols_kernel<<<grid_for((size_t)S.n * ncols), 256, 0, S.s>>>(S.n, ncols, X, ldx, S.perm,
-                                                                           S.D64, S.n);
-        FG_CUDA(cudaGetLastError());
+        {
+            KTimer kt(kFamRefine, S.s, 0.0, 16.0 * S.n * (double)ncols);
+            gather_cols_kernel<<<grid_for((size_t)S.n * ncols), 256, 0, S.s>>>(S.n, ncols, X, ldx,
+                                                                               S.perm, S.D64, S.n);
+            FG_CUDA(cudaGetLastError());
+        }
         int st = dtrsm_launch('L', 'L', 'N', 'U', S.n, ncols, 1.0, S.LU64, S.n, S.D64, S.n, S.s);
         if (st != kOk) return st;
         st = dtrsm_launch('L', 'U', 'N', 'N', S.n, ncols, 1.0, S.LU64, S.n, S.D64, S.n, S.s);
         if (st != kOk) return st;
+        KTimer kt(kFamRefine, S.s, 0.0, 24.0 * S.n * (double)ncols);
         if (add)
             put_cols_kernel<true><<<grid_for((size_t)S.n * ncols), 256, 0, S.s>>>(S.n, ncols, S.D64,
                                                                                   S.n, out, ldo);
@@ -263,14 +566,17 @@ int lu_solve(Solver &S, int ncols, const double *X, int ldx, const double *scale
         FG_CUDA(cudaGetLastError());
         return kOk;
     }
-    KTimer kt(kFamRefine, S.s, 2.0 * S.n * (double)S.n * ncols, 4.0 * S.n * (double)S.n);
-    d2s_cols_kernel<<<grid_for((size_t)S.n * ncols), 256, 0, S.s>>>(S.n, ncols, X, ldx, S.perm,
-                                                                      scale, S.D32, S.n);
-    FG_CUDA(cudaGetLastError());
+    {
+        KTimer kt(kFamRefine, S.s, 0.0, 12.0 * S.n * (double)ncols);
+        d2s_cols_kernel<<<grid_for((size_t)S.n * ncols), 256, 0, S.s>>>(S.n, ncols, X, ldx, S.perm,
+                                                                          scale, S.D32, S.n);
+        FG_CUDA(cudaGetLastError());
+    }
     int st = strsm_launch('L', 'L', 'N', 'U', S.n, ncols, 1.0f, S.A32, S.ld32, S.D32, S.n, S.s);
     if (st != kOk) return st;
     st = strsm_launch('L', 'U', 'N', 'N', S.n, ncols, 1.0f, S.A32, S.ld32, S.D32, S.n, S.s);
     if (st != kOk) return st;
+    KTimer kt(kFamRefine, S.s, 0.0, 20.0 * S.n * (double)ncols);
     if (add)
         s2d_cols_kernel<true><<<grid_for((size_t)S.n * ncols), 256, 0, S.s>>>(S.n, ncols, S.D32, S.n,
                                                                                scale, out, ldo);
@@ -281,14 +587,28 @@ int lu_solve(Solver &S, int ncols, const double *X, int ldx, const double *scale
     return kOk;
 }
 
-// dst = (L^ U^)^-1 P src with the FP32 factors applied in FP64 arithmetic:
-// GMRES-IR needs the preconditioned operator (LU)^-1 A in the residual
-// precision (Carson & Higham 2018, the u_r-precision matvec), an FP32 solve
-// makes it inconsistent at the kappa*u32 level and Arnoldi stalls.
+// dst = (L^ U^)^-1 P src with the stored (FP32) factors applied in FP64
+// arithmetic: GMRES-IR needs the preconditioned operator (LU)^-1 A in the
+// residual precision (Carson & Higham 2018, the u_r-precision matvec); an FP32
+// solve makes it inconsistent at the kappa*u32 level and Arnoldi stalls.  The
+// chained block-inverse solves read the factors as stored; where they do not
+// fit (n beyond what one cooperative launch holds) the FP64 copy LU64 goes
+// through the blocked triangular solves.
 int precond64(Solver &S, const double *src, double *dst) {
-    KTimer kt(kFamRefine, S.s, 2.0 * S.n * (double)S.n, 8.0 * S.n * (double)S.n);
-    gather_perm_kernel<<<grid_for(S.n), 256, 0, S.s>>>(S.n, src, S.perm, dst);
-    FG_CUDA(cudaGetLastError());
+    {
+        KTimer kt(kFamKrylov, S.s, 0.0, 20.0 * S.n);
+        gather_perm_kernel<<<grid_for(S.n), 256, 0, S.s>>>(S.n, src, S.perm, dst);
+        FG_CUDA(cudaGetLastError());
+    }
+    if (S.pc) {
+        int st;
+        if (S.precision == kPrecSplit) {
+            if ((st = pc_solve<double>(S, S.LU64, S.n, true, dst)) != kOk) return st;
+            return pc_solve<double>(S, S.LU64, S.n, false, dst);
+        }
+        if ((st = pc_solve<float>(S, S.A32, S.ld32, true, dst)) != kOk) return st;
+        return pc_solve<float>(S, S.A32, S.ld32, false, dst);
+    }
     int st = dtrsm_launch('L', 'L', 'N', 'U', S.n, 1, 1.0, S.LU64, S.n, dst, S.n, S.s);
     if (st != kOk) return st;
     return dtrsm_launch('L', 'U', 'N', 'N', S.n, 1, 1.0, S.LU64, S.n, dst, S.n, S.s);
@@ -305,9 +625,13 @@ int residual(Solver &S, int j0, int nc, std::vector<double> &berr) {
     int st = dgemm_launch('N', 'N', S.n, nc, S.n, -1.0, S.A, S.ldA, S.X + (size_t)j0 * S.ldX, S.ldX,
                           1.0, S.R + (size_t)j0 * S.n, S.n, S.s);
     if (st != kOk) return st;
-    col_absmax_kernel<<<nc, 256, 0, S.s>>>(S.n, S.R + (size_t)j0 * S.n, S.n, S.colv + j0);
-    col_absmax_kernel<<<nc, 256, 0, S.s>>>(S.n, S.X + (size_t)j0 * S.ldX, S.ldX, S.colv + S.nrhs + j0);
-    FG_CUDA(cudaGetLastError());
+    {
+        KTimer kt(kFamRefine, S.s, 0.0, 16.0 * S.n * (double)nc);
+        col_absmax_kernel<<<nc, 256, 0, S.s>>>(S.n, S.R + (size_t)j0 * S.n, S.n, S.colv + j0);
+        col_absmax_kernel<<<nc, 256, 0, S.s>>>(S.n, S.X + (size_t)j0 * S.ldX, S.ldX,
+                                               S.colv + S.nrhs + j0);
+        FG_CUDA(cudaGetLastError());
+    }
     std::vector<double> hr(nc), hx(nc);
     FG_CUDA(cudaMemcpyAsync(hr.data(), S.colv + j0, sizeof(double) * nc, cudaMemcpyDeviceToHost, S.s));
     FG_CUDA(cudaMemcpyAsync(hx.data(), S.colv + S.nrhs + j0, sizeof(double) * nc,
@@ -333,6 +657,7 @@ int gmres_cycle(Solver &S, int j, double rtol, int *steps) {
     int st = precond64(S, r, S.V);
     if (st != kOk) return st;
     auto norm2_into = [&](const double *v, double *dst) -> int {
+        KTimer kt(kFamKrylov, S.s, 2.0 * n, 8.0 * n);
         FG_CUDA(cudaMemsetAsync(dst, 0, sizeof(double), S.s));
         dim3 g(std::max(1, std::min(ceil_div(n, 256 * 8), num_sms() * 2)), 1);
         multi_dot_kernel<<<g, 256, 0, S.s>>>(n, v, n, v, dst);
@@ -345,8 +670,11 @@ int gmres_cycle(Solver &S, int j, double rtol, int *steps) {
     FG_CUDA(cudaMemcpyAsync(&beta, sc + 1, sizeof(double), cudaMemcpyDeviceToHost, S.s));
     FG_CUDA(cudaStreamSynchronize(S.s));
     if (!(beta > 0.0) || !isfinite(beta)) return kOk;
-    scale_into_kernel<<<grid_for(n), 256, 0, S.s>>>(n, sc + 1, S.V, S.V);
-    FG_CUDA(cudaGetLastError());
+    {
+        KTimer kt(kFamKrylov, S.s, (double)n, 16.0 * n);
+        scale_into_kernel<<<grid_for(n), 256, 0, S.s>>>(n, sc + 1, S.V, S.V);
+        FG_CUDA(cudaGetLastError());
+    }
 
     std::vector<double> H((size_t)(M + 1) * M, 0.0), cs(M), sn(M), g(M + 1, 0.0);
     g[0] = beta;
@@ -359,14 +687,17 @@ int gmres_cycle(Solver &S, int j, double rtol, int *steps) {
             return st;
         if ((st = precond64(S, S.t, S.w)) != kOk) return st;
         // classical Gram-Schmidt, twice
-        dim3 gd(std::max(1, std::min(ceil_div(n, 256 * 8), num_sms() * 2)), k + 1);
-        FG_CUDA(cudaMemsetAsync(S.h, 0, sizeof(double) * (k + 1), S.s));
-        multi_dot_kernel<<<gd, 256, 0, S.s>>>(n, S.V, n, S.w, S.h);
-        combination_kernel<<<grid_for(n), 256, 0, S.s>>>(n, k + 1, S.V, n, S.h, -1.0, S.w);
-        FG_CUDA(cudaMemsetAsync(S.h2, 0, sizeof(double) * (k + 1), S.s));
-        multi_dot_kernel<<<gd, 256, 0, S.s>>>(n, S.V, n, S.w, S.h2);
-        combination_kernel<<<grid_for(n), 256, 0, S.s>>>(n, k + 1, S.V, n, S.h2, -1.0, S.w);
-        FG_CUDA(cudaGetLastError());
+        {
+            KTimer kt(kFamKrylov, S.s, 8.0 * n * (k + 1), 32.0 * n * (k + 1));
+            dim3 gd(std::max(1, std::min(ceil_div(n, 256 * 8), num_sms() * 2)), k + 1);
+            FG_CUDA(cudaMemsetAsync(S.h, 0, sizeof(double) * (k + 1), S.s));
+            multi_dot_kernel<<<gd, 256, 0, S.s>>>(n, S.V, n, S.w, S.h);
+            combination_kernel<<<grid_for(n), 256, 0, S.s>>>(n, k + 1, S.V, n, S.h, -1.0, S.w);
+            FG_CUDA(cudaMemsetAsync(S.h2, 0, sizeof(double) * (k + 1), S.s));
+            multi_dot_kernel<<<gd, 256, 0, S.s>>>(n, S.V, n, S.w, S.h2);
+            combination_kernel<<<grid_for(n), 256, 0, S.s>>>(n, k + 1, S.V, n, S.h2, -1.0, S.w);
+            FG_CUDA(cudaGetLastError());
+        }
         if ((st = norm2_into(S.w, S.h + k + 1)) != kOk) return st;
         std::vector<double> hh(k + 2), hh2(k + 1);
         FG_CUDA(cudaMemcpyAsync(hh.data(), S.h, sizeof(double) * (k + 2), cudaMemcpyDeviceToHost, S.s));
@@ -375,6 +706,7 @@ int gmres_cycle(Solver &S, int j, double rtol, int *steps) {
         for (int i = 0; i <= k; ++i) hh[i] += hh2[i];
         const double hk1 = hh[k + 1];
         if (k + 1 < M + 1 && hk1 > 0.0 && isfinite(hk1)) {
+            KTimer kt(kFamKrylov, S.s, (double)n, 16.0 * n);
             scale_into_kernel<<<grid_for(n), 256, 0, S.s>>>(n, S.h + k + 1, S.w,
                                                             S.V + (size_t)(k + 1) * n);
             FG_CUDA(cudaGetLastError());
@@ -407,6 +739,7 @@ int gmres_cycle(Solver &S, int j, double rtol, int *steps) {
         y[i] = H[(size_t)i * M + i] != 0.0 ? t / H[(size_t)i * M + i] : 0.0;
     }
     FG_CUDA(cudaMemcpyAsync(S.h, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, S.s));
+    KTimer kt(kFamKrylov, S.s, 2.0 * n * k, 8.0 * n * (k + 2));
     combination_kernel<<<grid_for(n), 256, 0, S.s>>>(n, k, S.V, n, S.h, 1.0, S.X + (size_t)j * S.ldX);
     FG_CUDA(cudaGetLastError());
     *steps = k;
@@ -481,7 +814,7 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
             d2s_cols_kernel<<<grid_for((size_t)n * n), 256, 0, s>>>(n, n, A, ldA, nullptr, nullptr,
                                                                     S.A32, S.ld32);
         FG_CUDA(cudaMemsetAsync(S.anorm_bits, 0, sizeof(unsigned long long), s));
-        inf_norm_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, A, ldA, S.anorm_bits);
+        inf_norm_kernel<<<ceil_div(n, 16), 256, 0, s>>>(n, A, ldA, S.anorm_bits);
         col_absmax_kernel<<<nrhs, 256, 0, s>>>(n, B, ldB, S.colv + 2 * nrhs);
         FG_CUDA(cudaGetLastError());
     }
@@ -554,12 +887,22 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
             if (!S.V) {
                 const size_t vB = a256((size_t)n * (M + 1) * sizeof(double));
                 const size_t nB = a256((size_t)n * sizeof(double));
-                char *p2 = (char *)workspace_slot(s, 2, vB + 2 * nB);
+                S.pc = pc_fits(n, split);
+                const size_t pB = S.pc ? pc_bytes(n) / 4 : 0;
+                char *p2 = (char *)workspace_slot(s, 2, vB + 2 * nB + 4 * pB);
                 if (!p2) return kErrAlloc;
                 S.V = (double *)p2;
                 S.w = (double *)(p2 + vB);
                 S.t = (double *)(p2 + vB + nB);
-                if (!split) {
+                if (S.pc) {
+                    char *pp = p2 + vB + 2 * nB;
+                    S.pcDL = (double *)pp;
+                    S.pcPL = (double *)(pp + pB);
+                    S.pcDU = (double *)(pp + 2 * pB);
+                    S.pcPU = (double *)(pp + 3 * pB);
+                    st = split ? pc_prepare<double>(S, S.LU64, n) : pc_prepare<float>(S, S.A32, S.ld32);
+                    if (st != kOk) return st;
+                } else if (!split) {
                     S.LU64 = (double *)workspace_slot(s, 3, (size_t)n * n * sizeof(double));
                     if (!S.LU64) return kErrAlloc;
                     KTimer kt(kFamAux, s, 0.0, 12.0 * n * (double)n);

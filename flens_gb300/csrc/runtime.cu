@@ -34,6 +34,24 @@ int cuda_fail(cudaError_t e, const char *what) {
     return kErrCuda;
 }
 
+namespace {
+std::atomic<long long> g_dev_allocs{0};
+std::atomic<int> g_fail_allocs{0};
+}  // namespace
+
+cudaError_t device_malloc(void **p, size_t bytes) {
+    int k = g_fail_allocs.load();
+    while (k > 0) {
+        if (g_fail_allocs.compare_exchange_weak(k, k - 1)) {
+            *p = nullptr;
+            return cudaErrorMemoryAllocation;
+        }
+    }
+    const cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) g_dev_allocs.fetch_add(1);
+    return e;
+}
+
 bool trace_enabled() {
     static int flag = -1;
     if (flag < 0) {
@@ -114,7 +132,7 @@ Workspace *workspace_for(cudaStream_t stream, size_t bytes) {
         w->device = dev;
         w->stream = stream;
         // status word + info word, zeroed
-        if (cudaMalloc((void **)&w->status, 2 * sizeof(int)) != cudaSuccess) {
+        if (device_malloc((void **)&w->status, 2 * sizeof(int)) != cudaSuccess) {
             set_last_error("cudaMalloc of the status word failed");
             delete w;
             w = nullptr;
@@ -136,7 +154,7 @@ Workspace *workspace_for(cudaStream_t stream, size_t bytes) {
             w->bytes = 0;
         }
         size_t want = bytes < (1u << 20) ? (1u << 20) : bytes;
-        if (cudaMalloc(&w->buf, want) != cudaSuccess) {
+        if (device_malloc(&w->buf, want) != cudaSuccess) {
             set_last_error("cudaMalloc of %zu bytes of workspace failed", want);
             return nullptr;
         }
@@ -173,7 +191,7 @@ int workspace_flags(cudaStream_t stream, int n, unsigned long long **flags,
     Registry &r = registry();
     std::lock_guard<std::mutex> lock(r.mu);
     if (!w->flags) {
-        if (cudaMalloc((void **)&w->flags, kCap * sizeof(unsigned long long)) != cudaSuccess) {
+        if (device_malloc((void **)&w->flags, kCap * sizeof(unsigned long long)) != cudaSuccess) {
             cudaGetLastError();
             w->flags = nullptr;
             set_last_error("cudaMalloc of the solve flags failed");
@@ -209,7 +227,7 @@ void *workspace_slot(cudaStream_t stream, int slot, size_t bytes) {
             w->slot_bytes[slot] = 0;
         }
         const size_t want = bytes < 256 ? 256 : bytes;
-        if (cudaMalloc(&w->slot_buf[slot], want) != cudaSuccess) {
+        if (device_malloc(&w->slot_buf[slot], want) != cudaSuccess) {
             cudaGetLastError();
             set_last_error("cudaMalloc of %zu bytes (workspace slot %d) failed", want, slot);
             return nullptr;
@@ -293,6 +311,15 @@ KTimer::~KTimer() {
 
 FG_API const char *flens_gb300_last_error(void) { return fg::t_last_error; }
 
+// Device allocations (cudaMalloc) the library has made since load.
+FG_API long long flens_gb300_device_alloc_count(void) { return fg::g_dev_allocs.load(); }
+
+// Test hook: the next `count` device allocations of the library fail as an
+// out-of-memory cudaMalloc would (count <= 0 clears the hook).
+FG_API void flens_gb300_test_fail_device_allocs(int count) {
+    fg::g_fail_allocs.store(count > 0 ? count : 0);
+}
+
 // Number of kernel launches the library has issued since load.
 FG_API long long flens_gb300_launch_count(void) { return fg::g_launches.load(); }
 
@@ -324,6 +351,7 @@ FG_API int flens_gb300_timing_read(int family, double *ms, long long *launches, 
 FG_API const char *flens_gb300_family_name(int family) {
     static const char *names[fg::kFamCount] = {"dgemm_fp64", "lu_panel", "laswp", "trsm_diag",
                                                "aux", "tc_gemm", "refine", "batched_lu",
-                                               "split_gemm"};
+                                               "split_gemm", "trsv_chain", "krylov",
+                                               "precond_chain"};
     return (family >= 0 && family < fg::kFamCount) ? names[family] : "";
 }

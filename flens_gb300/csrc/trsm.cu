@@ -19,6 +19,8 @@
 
 #include <stdlib.h>
 
+#include <atomic>
+
 namespace fg {
 namespace {
 
@@ -181,6 +183,9 @@ constexpr int CH_NB = 64;
 constexpr int CH_MAXV = 4;
 constexpr int CH_THREADS = 256;
 
+// spin limit of the next chained solve when it is made to stall (0: none)
+std::atomic<unsigned> g_stall_next_chain{0};
+
 __device__ __forceinline__ void ch_release(unsigned long long *p, unsigned long long v) {
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
@@ -190,11 +195,15 @@ __device__ __forceinline__ unsigned long long ch_acquire(const unsigned long lon
     return v;
 }
 
+// spin_limit bounds every wait (kSpinLimit when 0).  stall != 0 is the
+// failure-detection test: block 0 first waits for a flag value that nothing
+// publishes, so it gives up, sets the status word and returns, and every
+// block after it gives up in turn.
 template <typename T, bool LOWER, bool UNIT>
 __global__ void __launch_bounds__(CH_THREADS)
 trsv_chain_kernel(int ka, const T *__restrict__ M0, long long mi, long long mp, T *X0, long long xs,
                   long long vs, int nvec, unsigned long long *flags, unsigned long long epoch,
-                  int *status) {
+                  int *status, unsigned spin_limit, int stall) {
     __shared__ T Mb[CH_NB][CH_NB + 1];                 // Mb[p][r] = M(R0 + r, K0 + p)
     __shared__ T Md[CH_NB][CH_NB + 1];                 // the diagonal block, same layout
     __shared__ T xk[CH_MAXV][CH_NB];
@@ -205,7 +214,22 @@ trsv_chain_kernel(int ka, const T *__restrict__ M0, long long mi, long long mp, 
     const int b = LOWER ? s : nblk - 1 - s;
     const int R0 = b * CH_NB, kb = min(CH_NB, ka - R0);
     const int r = tid & (CH_NB - 1), q = tid / CH_NB;    // row; 16-column quarter
-    if (tid == 0) s_abort = 0;
+    const unsigned limit = spin_limit ? spin_limit : kSpinLimit;
+    if (tid == 0) {
+        s_abort = 0;
+        if (stall && s == 0) {
+            // its own flag never holds epoch + 1 during this launch
+            unsigned spins = 0;
+            while (ch_acquire(&flags[0]) != epoch + 1) {
+                if (++spins > limit) {
+                    atomicOr(status, kDevBarrierTimeout);
+                    s_abort = 1;
+                    break;
+                }
+                if (spins > 32) __nanosleep(64);
+            }
+        }
+    }
     T acc[CH_MAXV];
 #pragma unroll
     for (int v = 0; v < CH_MAXV; ++v) acc[v] = T(0);
@@ -222,6 +246,7 @@ trsv_chain_kernel(int ka, const T *__restrict__ M0, long long mi, long long mp, 
     // off the critical path, before any wait
     stage(Md, R0, kb);
     __syncthreads();
+    if (s_abort) return;
     if (!UNIT && tid < kb) rinv[tid] = T(1) / Md[tid][tid];
 
     for (int s2 = 0; s2 < s; ++s2) {
@@ -231,7 +256,7 @@ trsv_chain_kernel(int ka, const T *__restrict__ M0, long long mi, long long mp, 
         if (tid == 0) {
             unsigned spins = 0;
             while (ch_acquire(&flags[s2]) != epoch) {
-                if (++spins > kSpinLimit) {
+                if (++spins > limit) {
                     atomicOr(status, kDevBarrierTimeout);
                     s_abort = 1;
                     break;
@@ -301,7 +326,8 @@ trsv_chain_kernel(int ka, const T *__restrict__ M0, long long mi, long long mp, 
 // blocks to keep resident, or more than the flag array holds).
 template <typename T>
 int launch_chain(int ka, const T *M0, long long mi, long long mp, bool lowerM, bool unit, T *X0,
-                 long long xs, long long vs, int nvec, cudaStream_t stream) {
+                 long long xs, long long vs, int nvec, cudaStream_t stream,
+                 const ChainFixed *fx) {
     const int nblk = ceil_div(ka, CH_NB);
     static int per_sm = -1;
     if (per_sm < 0) {
@@ -315,13 +341,35 @@ int launch_chain(int ka, const T *M0, long long mi, long long mp, bool lowerM, b
     }
     if ((long long)per_sm * num_sms() < nblk) return kErrUnsupported;
     unsigned long long *flags = nullptr, epoch = 0;
-    int st = workspace_flags(stream, nblk, &flags, &epoch);
-    if (st != kOk) return st;
-    Workspace *w = workspace_for(stream, 0);
-    if (!w) return kErrAlloc;
-    int *status = w->status;
-    void *args[] = {&ka, &M0, &mi, &mp, &X0, &xs, &vs, &nvec, &flags, &epoch, &status};
-    KTimer kt(kFamTrsm, stream, (double)ka * ka * nvec, 4.0 * (double)ka * ka + 16.0 * ka * nvec);
+    int *status = nullptr;
+    if (fx) {
+        // caller-supplied flags: cleared in stream order, one fixed epoch
+        if (nblk > fx->cap) return kErrUnsupported;
+        FG_CUDA(cudaMemsetAsync(fx->flags, 0, sizeof(unsigned long long) * nblk, stream));
+        flags = fx->flags;
+        epoch = 1;
+        status = fx->status;
+    } else {
+        int st = workspace_flags(stream, nblk, &flags, &epoch);
+        if (st != kOk) return st;
+        Workspace *w = workspace_for(stream, 0);
+        if (!w) return kErrAlloc;
+        status = w->status;
+    }
+    // failure-detection test hook (flens_gb300_test_stall_next_chain)
+    unsigned spin_limit = 0;
+    int stall = 0;
+    {
+        const unsigned lim = g_stall_next_chain.exchange(0);
+        if (lim) {
+            spin_limit = lim;
+            stall = 1;
+        }
+    }
+    void *args[] = {&ka, &M0, &mi, &mp, &X0, &xs, &vs, &nvec, &flags, &epoch, &status,
+                    &spin_limit, &stall};
+    KTimer kt(kFamTrsv, stream, (double)ka * ka * nvec,
+              (double)sizeof(T) * ka * (double)ka / 2.0 + 16.0 * ka * nvec);
     const void *fn;
     if (lowerM) fn = unit ? (const void *)trsv_chain_kernel<T, true, true>
                           : (const void *)trsv_chain_kernel<T, true, false>;
@@ -379,7 +427,8 @@ int gemm_t<float>(char ta, char tb, int m, int n, int k, float alpha, const floa
 
 template <typename T>
 int trsm_launch_t(char side, char upLo, char transA, char diag, int m, int n,
-                  T alpha, const T *A, int ldA, T *B, int ldB, cudaStream_t stream) {
+                  T alpha, const T *A, int ldA, T *B, int ldB, cudaStream_t stream,
+                  const ChainFixed *fx = nullptr) {
     if (m == 0 || n == 0) return kOk;
     const bool left = (side == 'L' || side == 'l');
     const bool lowerA = (upLo == 'L' || upLo == 'l');
@@ -406,7 +455,7 @@ int trsm_launch_t(char side, char upLo, char transA, char diag, int m, int n,
     const int nblk = ceil_div(ka, TRSM_NB);
     bool done = false;
     if (nvec <= CH_MAXV && nblk >= 2 && chain_enabled()) {
-        const int st = launch_chain<T>(ka, A, mi, mp, lowerM, unit != 0, B, xs, vs, nvec, stream);
+        const int st = launch_chain<T>(ka, A, mi, mp, lowerM, unit != 0, B, xs, vs, nvec, stream, fx);
         if (st == kOk) done = true;
         else if (st != kErrUnsupported) return st;
     }
@@ -449,9 +498,26 @@ int dtrsm_launch(char side, char upLo, char transA, char diag, int m, int n, dou
     return trsm_launch_t<double>(side, upLo, transA, diag, m, n, alpha, A, ldA, B, ldB, stream);
 }
 
+int dtrsm_launch_fixed(char side, char upLo, char transA, char diag, int m, int n, double alpha,
+                       const double *A, int ldA, double *B, int ldB, const ChainFixed &fx,
+                       cudaStream_t stream) {
+    return trsm_launch_t<double>(side, upLo, transA, diag, m, n, alpha, A, ldA, B, ldB, stream, &fx);
+}
+
 int strsm_launch(char side, char upLo, char transA, char diag, int m, int n, float alpha,
                  const float *A, int ldA, float *B, int ldB, cudaStream_t stream) {
     return trsm_launch_t<float>(side, upLo, transA, diag, m, n, alpha, A, ldA, B, ldB, stream);
 }
 
 }  // namespace fg
+
+// Failure-detection test hook: the next chained triangular solve (trs and
+// trsm with at most 4 right-hand sides against more than one 64-row block)
+// makes its first block wait for a flag that nothing sets, bounded by
+// `spin_limit` spins, so that every block gives up and the stream's status
+// word reports FLENS_GB300_ERR_TIMEOUT at the next flens_gb300_sync.  No
+// fault, trap or unbounded wait is involved: the kernel returns and the
+// context stays usable.
+FG_API void flens_gb300_test_stall_next_chain(unsigned spin_limit) {
+    fg::g_stall_next_chain.store(spin_limit);
+}

@@ -394,13 +394,17 @@ int flens_gb300_batched_panel(void *plan, int bucket);
  * once running (a fixed, pre-reserved memory budget, a memory pool owned by
  * another framework, or a process that forbids cudaMalloc after start-up).
  * No counterpart in the reference.  Same arguments, results and return codes
- * as flens_gb300_dgetrs, but it calls no cudaMalloc/cudaFree: its scratch is a
+ * as flens_gb300_dgetrs, but it calls no cudaMalloc/cudaFree, not even on a
+ * stream it has never seen: all of its scratch (interchange buffers, and the
+ * ready flags and status word of the chained solve used for nrhs <= 4) is a
  * fixed 8 MiB device array inside the library, held on every GPU that loads
- * the library until exit.  A call needs round_up(4*n,256) + 8*n*nrhs bytes
- * (n=8192: nrhs <= 127); larger calls return FLENS_GB300_ERR_UNSUPPORTED.
- * All calls share that array: calls that overlap on the GPU race, so
- * serialise them.  The first call on a device looks up the array's address;
- * make it before any stream capture.  Async on stream. */
+ * the library until exit.  A call needs 33024 + round_up(4*n,256) +
+ * 8*n*nrhs bytes of it (n=8192: nrhs <= 127); larger calls return
+ * FLENS_GB300_ERR_UNSUPPORTED with a message.  Each call clears the parts
+ * that must start at zero on its own stream.  All calls share that array:
+ * calls that overlap on the GPU race, so serialise them.  The first call on a
+ * device looks up the array's address; make it before any stream capture.
+ * Async on stream. */
 int flens_gb300_dgetrs_noalloc(char trans, int n, int nrhs, const double *A,
                                int ldA, const int *ipiv, double *B, int ldB,
                                void *stream);
@@ -411,6 +415,26 @@ int flens_gb300_sync(void *stream);
 
 /* Last error message of the calling thread ("" if none). */
 const char *flens_gb300_last_error(void);
+
+/* Diagnostics, no counterpart in the reference.  Device allocations
+ * (cudaMalloc) the library has made since it was loaded. */
+long long flens_gb300_device_alloc_count(void);
+
+/* Test hook for the allocation-failure paths: the next `count` device
+ * allocations of the library fail as an out-of-memory cudaMalloc would, so
+ * the calls that needed them return FLENS_GB300_ERR_ALLOC (or INFO =
+ * FLENS_GB300_ERR_ALLOC for the Fortran-ABI LAPACK symbols) with a message.
+ * count <= 0 clears it. */
+void flens_gb300_test_fail_device_allocs(int count);
+
+/* Launch accounting: kernel launches issued since load; per-family CUDA-event
+ * timing on the launching streams (enable clears the totals; read waits for
+ * the recorded events and returns -1 for an unknown family); family names. */
+long long flens_gb300_launch_count(void);
+void flens_gb300_timing_enable(int on);
+int flens_gb300_timing_read(int family, double *ms, long long *launches,
+                            double *flops, double *bytes);
+const char *flens_gb300_family_name(int family);
 
 /* xerbla_ calls made by this library on the calling thread: count, the last
  * parameter position and routine name (for callers that cannot override

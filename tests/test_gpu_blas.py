@@ -168,3 +168,38 @@ def test_trsm_device_api(cuda, port):
     torch.cuda.synchronize()
     ref = port.dtrsm("L", "U", "N", "N", 1.0, A, B.copy(order="F"))
     assert rel(dB.cpu().numpy(), ref) <= TRSM_TOL
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4])
+@pytest.mark.parametrize("tb", ["N", "T"])
+def test_gemm_long_k_few_vectors_vs_oracle(cuda, port, n, tb):
+    # op(A) = A with k >= 256, m*k >= 2^20 and n <= 4 runs the row-tile GEMV
+    # (the residual and Krylov products of the refinement); m not a multiple
+    # of the 16-row tile, a leading dimension larger than m
+    m, k, lda = 1029, 1100, 1040
+    Afull = oracle.uniform(91 + n, lda, k)
+    A = np.asfortranarray(Afull[:m, :])
+    B = oracle.uniform(92 + n, k if tb == "N" else n, n if tb == "N" else k)
+    C = oracle.uniform(93 + n, m, n)
+    out = fg.dgemm("N", tb, 1.5, A, B, -0.5, C.copy(order="F"))
+    ref = port.dgemm("N", tb, 1.5, A, B, -0.5, C.copy(order="F"))
+    assert rel(out, ref) <= GEMM_TOL, rel(out, ref)
+
+
+def test_gemm_long_k_ld_view_device(cuda):
+    import torch
+    # device operands with ld > m: only the m x k view may be read
+    m, k, lda = 2000, 3000, 2048
+    g = torch.Generator(device=cuda)
+    g.manual_seed(5)
+    Abig = fg.to_colmajor(torch.rand((lda, k), generator=g, dtype=torch.float64, device=cuda) - 0.5)
+    Abig[m:, :] = float("nan")
+    A = Abig[:m, :]
+    x = fg.to_colmajor(torch.rand((k, 1), generator=g, dtype=torch.float64, device=cuda))
+    y = fg.colmajor_empty(m, 1, device=cuda)
+    y.zero_()
+    fg.dgemm_dev("N", "N", 1.0, A, x, 0.0, y)
+    torch.cuda.synchronize()
+    ref = A @ x
+    assert torch.isfinite(y).all()
+    assert ((y - ref).abs().max() / ref.abs().max()).item() <= GEMM_TOL

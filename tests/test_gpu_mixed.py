@@ -137,3 +137,28 @@ def test_mixed_argument_errors(cuda):
     assert f(-1, 1, None, 1, None, 1, None, 1, 0, 0, 5, 0.0, None, None, None, None) == -1
     assert f(4, 1, None, 3, None, 4, None, 4, 0, 0, 5, 0.0, None, None, None, None) == -4
     assert f(4, 1, None, 4, None, 4, None, 4, 7, 0, 5, 0.0, None, None, None, None) == -9
+
+
+@pytest.mark.parametrize("n", [256, 300, 64, 50])
+@pytest.mark.parametrize("prec", ["fp32", "split"])
+def test_mixed_gmres_preconditioner_quality(cuda, n, prec):
+    # GMRES-IR with well-conditioned A: with the exact preconditioner
+    # (LU)^-1 A = I + O(u_f), GMRES needs a handful of iterations; a wrong
+    # block (inverse, neighbour product, partial last block) would leave it
+    # near n iterations.  n = 300 and 50 end in a partial 64-row block.
+    A, b, x = make_system(cuda, n, 1e2, 1, 17)
+    st, X, it, be, inf = dgesv_mixed(A, b, prec, "gmres", max_iter=5)
+    assert st == 0, (st, fg.last_error(), it, be)
+    assert it <= (12 if prec == "fp32" else 4), it
+    assert backward_error(A, X, b) <= 10 * n * EPS
+
+
+def test_mixed_gmres_ill_conditioned_partial_block(cuda):
+    # n = 300 ends in a partial 64-row block.  kappa = 1e8 leaves about 30
+    # singular values below 1/(u32*growth), within one restart cycle (at
+    # kappa = 1e10 it is about 80 of 300, and restarted GMRES(100) stagnates)
+    n = 300
+    A, b, x = make_system(cuda, n, 1e8, 1, 13)
+    st, X, it, be, inf = dgesv_mixed(A, b, "fp32", "gmres", max_iter=10)
+    assert st == 0, (st, fg.last_error(), it, be)
+    assert backward_error(A, X, b) <= 10 * n * EPS
