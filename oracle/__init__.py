@@ -21,7 +21,25 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "libflens_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libflens_ref.so")
-REFERENCE_SRC = "/root/reference"
+
+
+def _reference_src() -> str:
+    """Where the FLENS sources are read from: $FLENS_REFERENCE, else the REF
+    default of this directory's Makefile (the recipe that compiles them)."""
+    env = os.environ.get("FLENS_REFERENCE")
+    if env:
+        return env
+    try:
+        with open(os.path.join(HERE, "Makefile")) as f:
+            for line in f:
+                if line.split("?=")[0].strip() == "REF" and "?=" in line:
+                    return line.split("?=", 1)[1].strip()
+    except OSError:
+        pass
+    return ""
+
+
+REFERENCE_SRC = _reference_src()
 
 _c_int_p = ctypes.POINTER(ctypes.c_int)
 _c_double_p = ctypes.POINTER(ctypes.c_double)
@@ -31,10 +49,11 @@ def build(with_ref: bool | None = None) -> None:
     """Compile the restatement, and the reference shims if the sources exist."""
     targets = ["port"]
     if with_ref is None:
-        with_ref = os.path.isdir(REFERENCE_SRC)
+        with_ref = bool(REFERENCE_SRC) and os.path.isdir(REFERENCE_SRC)
     if with_ref:
         targets.append("ref")
-    subprocess.run(["make", "-s", "-j8", "-C", HERE] + targets, check=True)
+    extra = [f"REF={REFERENCE_SRC}"] if with_ref and REFERENCE_SRC else []
+    subprocess.run(["make", "-s", "-j8", "-C", HERE] + targets + extra, check=True)
 
 
 def _dp(a: np.ndarray):
@@ -108,8 +127,12 @@ class Port:
                                     _c_double_p, i, _c_double_p, _c_double_p, _c_double_p,
                                     _c_double_p]
         L.oracle_dgesvx.restype = i
+        L.oracle_dgetrf_gaps.argtypes = [i, i, _c_double_p, i, _c_int_p, _c_double_p]
+        L.oracle_dgetrf_gaps.restype = i
         L.oracle_time_dgetrf_steps.argtypes = [i, i, i, ctypes.c_ulonglong, _c_double_p]
         L.oracle_time_dgetrf_steps.restype = d
+        L.oracle_time_dgetrf_step_at.argtypes = [i, i, i, ctypes.c_ulonglong, _c_double_p]
+        L.oracle_time_dgetrf_step_at.restype = d
         L.oracle_time_dgemm_rows.argtypes = [i, i, i, i, i, ctypes.c_ulonglong]
         L.oracle_time_dgemm_rows.restype = d
 
@@ -142,6 +165,17 @@ class Port:
         piv = np.zeros(max(1, min(m, n)), dtype=np.int32)
         info = self.lib.oracle_dgetrf_nb(m, n, _dp(A), max(1, m), _ip(piv), nb)
         return piv[: min(m, n)], info
+
+    def dgetrf_gaps(self, A):
+        """dgetrf (nb = 64) that also returns, per pivot search, the relative
+        gap (|first| - |second|) / |first| of the two largest candidates."""
+        _check_f64(A)
+        m, n = A.shape
+        mn = min(m, n)
+        piv = np.zeros(max(1, mn), dtype=np.int32)
+        gap = np.zeros(max(1, mn), dtype=np.float64)
+        info = self.lib.oracle_dgetrf_gaps(m, n, _dp(A), max(1, m), _ip(piv), _dp(gap))
+        return piv[:mn], info, gap[:mn]
 
     def dgetrs(self, trans, LU, piv, B):
         _check_f64(LU), _check_f64(B)
@@ -269,6 +303,12 @@ class Port:
         fl = ctypes.c_double(0.0)
         t = self.lib.oracle_time_dgetrf_steps(n, n_blocks, n_threads, seed,
                                               ctypes.byref(fl))
+        return t, fl.value
+
+    def time_dgetrf_step_at(self, n, block, n_threads, seed=1234):
+        """(seconds, flops) of block step `block` of an n x n LU, per thread."""
+        fl = ctypes.c_double(0.0)
+        t = self.lib.oracle_time_dgetrf_step_at(n, block, n_threads, seed, ctypes.byref(fl))
         return t, fl.value
 
     def time_dgemm_rows(self, m, n, k, rows, n_threads, seed=1234):

@@ -205,7 +205,29 @@ void oracle_dlaswp(int nCols, double *A, int ldA, int k1, int k2,
  * (:131 -> cxxblas/level2/ger.tcc:41-64 -> axpy).  SafeMin is DBL_MIN
  * (flens/lapack/la/lamch.tcc:73-81: 1/DBL_MAX < DBL_MIN).
  */
-int oracle_dgetf2(int m, int n, double *A, int ldA, int *piv)
+/*
+ * Relative separation of the two largest |candidates| of one pivot search,
+ * (|first| - |second|) / |first| (1 with a single candidate, 0 for an exact
+ * tie or a zero column).  Test instrumentation only: it reads the column and
+ * changes nothing, so the factorisation is the same with or without it.
+ */
+static double pivot_gap(int n, const double *x)
+{
+    double a1 = 0.0, a2 = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double a = fabs(x[i]);
+        if (a > a1) {
+            a2 = a1;
+            a1 = a;
+        } else if (a > a2) {
+            a2 = a;
+        }
+    }
+    if (n <= 1) return 1.0;
+    return a1 > 0.0 ? (a1 - a2) / a1 : 0.0;
+}
+
+static int dgetf2_impl(int m, int n, double *A, int ldA, int *piv, double *gap)
 {
     int info = 0;
     if (m == 0 || n == 0) {
@@ -214,6 +236,7 @@ int oracle_dgetf2(int m, int n, double *A, int ldA, int *piv)
     const double safeMin = DBL_MIN;
     const int mn = m < n ? m : n;
     for (int j = 0; j < mn; ++j) {
+        if (gap) gap[j] = pivot_gap(m - j, &A[IDX(j, j, ldA)]);
         const int jp = j + oracle_idamax(m - j, &A[IDX(j, j, ldA)], 1);
         piv[j] = jp + 1;
         if (A[IDX(jp, j, ldA)] != 0.0) {
@@ -244,6 +267,11 @@ int oracle_dgetf2(int m, int n, double *A, int ldA, int *piv)
     return info;
 }
 
+int oracle_dgetf2(int m, int n, double *A, int ldA, int *piv)
+{
+    return dgetf2_impl(m, n, A, ldA, piv, NULL);
+}
+
 /*
  * TRF.  flens/lapack/ge/trf.tcc:59-152 with bs = ilaenv(1,"GETRF") = 64
  * (flens/lapack/la/ilaenv.tcc:93-99); unblocked when bs<=1 or bs>=min(m,n)
@@ -252,7 +280,7 @@ int oracle_dgetf2(int m, int n, double *A, int ldA, int *piv)
  * trailing gemm with alpha=-1, beta=1 (:144-146).
  */
 static int dgetrf_impl(int m, int n, double *A, int ldA, int *piv, int nb,
-                       int maxBlocks)
+                       int maxBlocks, double *gap)
 {
     int info = 0;
     if (m == 0 || n == 0) {
@@ -260,7 +288,7 @@ static int dgetrf_impl(int m, int n, double *A, int ldA, int *piv, int nb,
     }
     const int mn = m < n ? m : n;
     if (nb <= 1 || nb >= mn) {
-        return oracle_dgetf2(m, n, A, ldA, piv);
+        return dgetf2_impl(m, n, A, ldA, piv, gap);
     }
     int blocks = 0;
     for (int j = 1; j <= mn; j += nb) {
@@ -268,8 +296,8 @@ static int dgetrf_impl(int m, int n, double *A, int ldA, int *piv, int nb,
             break;
         }
         const int jb = (mn - j + 1 < nb) ? mn - j + 1 : nb;
-        const int info_ = oracle_dgetf2(m - j + 1, jb, &A[IDX(j - 1, j - 1, ldA)],
-                                        ldA, &piv[j - 1]);
+        const int info_ = dgetf2_impl(m - j + 1, jb, &A[IDX(j - 1, j - 1, ldA)],
+                                      ldA, &piv[j - 1], gap ? &gap[j - 1] : NULL);
         if (info == 0 && info_ > 0) {
             info = info_ + j - 1;
         }
@@ -297,18 +325,25 @@ static int dgetrf_impl(int m, int n, double *A, int ldA, int *piv, int nb,
 
 int oracle_dgetrf_nb(int m, int n, double *A, int ldA, int *piv, int nb)
 {
-    return dgetrf_impl(m, n, A, ldA, piv, nb, -1);
+    return dgetrf_impl(m, n, A, ldA, piv, nb, -1, NULL);
 }
 
 int oracle_dgetrf(int m, int n, double *A, int ldA, int *piv)
 {
-    return dgetrf_impl(m, n, A, ldA, piv, 64, -1);
+    return dgetrf_impl(m, n, A, ldA, piv, 64, -1, NULL);
+}
+
+/* oracle_dgetrf that also records, per pivot search j, the relative gap
+ * between the two largest |candidates| (gap[min(m,n)]). */
+int oracle_dgetrf_gaps(int m, int n, double *A, int ldA, int *piv, double *gap)
+{
+    return dgetrf_impl(m, n, A, ldA, piv, 64, -1, gap);
 }
 
 int oracle_dgetrf_steps(int m, int n, double *A, int ldA, int *piv,
                         int nb, int nBlocks)
 {
-    return dgetrf_impl(m, n, A, ldA, piv, nb, nBlocks);
+    return dgetrf_impl(m, n, A, ldA, piv, nb, nBlocks, NULL);
 }
 
 /*
@@ -1424,7 +1459,7 @@ static double now_seconds(void)
 }
 
 typedef struct {
-    int kind;            /* 0 = dgetrf steps, 1 = dgemm rows */
+    int kind;            /* 0 = dgetrf steps, 1 = dgemm rows, 2 = one dgetrf step at block b */
     int m, n, k, rows, nBlocks;
     unsigned long long seed;
     pthread_barrier_t *barrier;
@@ -1452,6 +1487,23 @@ static void *run_job(void *arg)
             fl += r * w * w + w * w * (r - w) + 2.0 * (r - w) * (r - w) * w;
         }
         jb->flops = fl;
+        free(A);
+        free(piv);
+    } else if (jb->kind == 2) {
+        /* block step b of the n x n LU: the step on the trailing (n-j) x (n-j)
+         * matrix at column j = 64 b, addressed with the full leading
+         * dimension n as inside the factorisation */
+        const int n = jb->n, j = 64 * jb->nBlocks, r = n - j;
+        double *A = (double *)malloc(sizeof(double) * (size_t)n * n);
+        int *piv = (int *)malloc(sizeof(int) * (size_t)n);
+        for (size_t i = 0; i < (size_t)n * n; ++i) A[i] = uniform_pm1(&s);
+        for (int i = 0; i < n; ++i) A[IDX(i, i, n)] += 0.25 * n;
+        pthread_barrier_wait(jb->barrier);
+        jb->t0 = now_seconds();
+        dgetrf_impl(r, r, &A[IDX(j, j, n)], n, piv, 64, 1, NULL);
+        jb->t1 = now_seconds();
+        const double w = r < 64 ? r : 64;
+        jb->flops = r * w * w + w * w * (r - w) + 2.0 * (r - w) * (r - w) * w;
         free(A);
         free(piv);
     } else {
@@ -1507,6 +1559,18 @@ double oracle_time_dgetrf_steps(int n, int nBlocks, int nThreads,
     p.kind = 0;
     p.n = n;
     p.nBlocks = nBlocks;
+    p.seed = seed;
+    return run_jobs(&p, nThreads < 1 ? 1 : nThreads, flops_out);
+}
+
+double oracle_time_dgetrf_step_at(int n, int block, int nThreads,
+                                  unsigned long long seed, double *flops_out)
+{
+    job_t p;
+    memset(&p, 0, sizeof p);
+    p.kind = 2;
+    p.n = n;
+    p.nBlocks = block;
     p.seed = seed;
     return run_jobs(&p, nThreads < 1 ? 1 : nThreads, flops_out);
 }

@@ -44,6 +44,9 @@ int oracle_dgetf2(int m, int n, double *A, int ldA, int *piv);
  *                                               flens/lapack/ge/trf.tcc:59-152 */
 int oracle_dgetrf_nb(int m, int n, double *A, int ldA, int *piv, int nb);
 int oracle_dgetrf(int m, int n, double *A, int ldA, int *piv);
+/* oracle_dgetrf plus, per pivot search j, (|first| - |second|) / |first| of
+ * the two largest candidates (gap[min(m,n)]); same factors and pivots. */
+int oracle_dgetrf_gaps(int m, int n, double *A, int ldA, int *piv, double *gap);
 
 /* First `nBlocks` block steps of oracle_dgetrf_nb only (a bounded sample of
  * the full factorisation, for timing); returns info so far. */
@@ -168,6 +171,11 @@ int oracle_dposv(char upLo, int n, int nRhs, double *A, int ldA, double *B,
  * flops one thread performed (sum over the steps), so a caller can scale the
  * sample to a full factorisation.
  */
+/* Wall time of block step `block` (nb = 64) of an n x n LU, run on the
+ * trailing matrix at column 64*block with leading dimension n, by nThreads
+ * threads each on its own copy; *flops_out = that step's flops. */
+double oracle_time_dgetrf_step_at(int n, int block, int nThreads,
+                                  unsigned long long seed, double *flops_out);
 double oracle_time_dgetrf_steps(int n, int nBlocks, int nThreads,
                                 unsigned long long seed, double *flops_out);
 

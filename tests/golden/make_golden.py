@@ -14,6 +14,7 @@ results.
 
     python tests/golden/make_golden.py            # small fixtures (seconds)
     python tests/golden/make_golden.py --large    # + the n=8192 LU pivots (minutes)
+    python tests/golden/make_golden.py --no-small --pivots   # unshifted n=2048/4096 pivots
 """
 from __future__ import annotations
 
@@ -364,16 +365,52 @@ def generate_large(R):
             "colsum_LU": A.sum(axis=0)}
 
 
+# Unshifted uniform[-1,1) matrices: LU with real row interchanges at sizes
+# where the GPU's blocked summation order differs from the reference's, for
+# pivot-vector parity at scale.  Stored per n: the reference's pivots and
+# INFO, diag(U) of its factors, and the relative gap between the two largest
+# |candidates| of every pivot search (from the oracle restatement, which must
+# give the reference's pivots bit for bit on the same input).
+PIVOT_CASES = ((2048, 777), (4096, 778))
+
+
+def generate_pivots(R):
+    P = oracle.Port()
+    out = {}
+    for n, seed in PIVOT_CASES:
+        A = oracle.splitmix_uniform(seed, n, n)
+        Ar = A.copy(order="F")
+        piv, info = R.dgetrf(Ar)
+        pp, pinfo, gap = P.dgetrf_gaps(A.copy(order="F"))
+        assert info == pinfo and np.array_equal(piv, pp), "restatement differs from the reference"
+        out[f"n{n}_meta"] = np.array([n, seed, info], dtype=np.int64)
+        out[f"n{n}_piv"] = piv.astype(np.int32)
+        out[f"n{n}_gap"] = gap
+        out[f"n{n}_diagU"] = np.ascontiguousarray(np.diag(Ar))
+        print(f"n={n}: {int(np.count_nonzero(piv != np.arange(1, n + 1)))} interchanges, "
+              f"smallest gap {gap.min():.3e}")
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--large", action="store_true")
+    ap.add_argument("--pivots", action="store_true",
+                    help="+ the unshifted n=2048/4096 pivot fixtures (a few minutes)")
+    ap.add_argument("--no-small", action="store_true")
     args = ap.parse_args()
     oracle.build(with_ref=True)
     R = oracle.Reference()
-    small = generate_small(R)
-    path = os.path.join(HERE, "reference_small.npz")
-    np.savez_compressed(path, **small)
-    print(f"wrote {path} ({os.path.getsize(path)} bytes, {len(small)} arrays)")
+    if not args.no_small:
+        small = generate_small(R)
+        path = os.path.join(HERE, "reference_small.npz")
+        np.savez_compressed(path, **small)
+        print(f"wrote {path} ({os.path.getsize(path)} bytes, {len(small)} arrays)")
+    if args.pivots:
+        piv = generate_pivots(R)
+        p3 = os.path.join(HERE, "reference_lu_unshifted.npz")
+        np.savez_compressed(p3, **piv)
+        print(f"wrote {p3} ({os.path.getsize(p3)} bytes)")
     if args.large:
         big = generate_large(R)
         p2 = os.path.join(HERE, "reference_lu8192.npz")

@@ -14,12 +14,19 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+
+
+def _ref_dir():
+    import oracle
+    return oracle.REFERENCE_SRC
+
+
+REF = _ref_dir()
 
 
 @pytest.fixture(scope="module")
 def shim_binary(tmp_path_factory):
-    if not os.path.isdir(REF):
+    if not REF or not os.path.isdir(REF):
         pytest.skip("FLENS headers not present on this machine")
     import flens_gb300
     flens_gb300.lib()
@@ -94,7 +101,7 @@ dgesvx_ E N equed=N n=4 nrhs=2 lda=4 ldaf=4 ldb=4 ldx=4
 
 
 def test_flens_calls_map_to_the_fortran_abi(tmp_path):
-    if not os.path.isdir(REF):
+    if not REF or not os.path.isdir(REF):
         pytest.skip("FLENS headers not present on this machine")
     rec = str(tmp_path / "abi_recorder.o")
     r = subprocess.run(["gcc", "-c", "-O1", os.path.join(ROOT, "tests", "cpp", "abi_recorder.c"),

@@ -254,3 +254,22 @@ def test_batched_mixed_many_buckets_no_slot_sharing(cuda):
         den = A.abs().sum(1).max() * X.abs().amax(0) + B.abs().amax(0)
         be = (R.abs().amax(0) / den).max().item()
         assert be <= 10 * n * EPS, (i, n, ks[i], be, iters[i])
+
+
+def test_batched_unshifted_n512_pivots(cuda, port):
+    # eight unshifted 512 x 512 systems (the blocked global-memory path, about
+    # 500 interchanges each): pivots entry by entry on every pivot search whose
+    # two largest |candidates| differ by more than 1e-10 relative
+    sizes, ks = [512] * 8, [1, 4, 16, 1, 4, 16, 1, 4]
+    mats, rhs, host = make_batch(cuda, sizes, ks, 2500, shift=False)
+    ipivs, info, _, _, _ = run_batched(cuda, mats, rhs, 0)
+    for i, (A0, Bh) in enumerate(host):
+        pivr, infor, gap = port.dgetrf_gaps(A0.copy(order="F"))
+        assert info[i] == infor == 0
+        piv = ipivs[i].cpu().numpy()[:512]
+        sep = gap > 1e-10
+        assert sep.mean() > 0.99
+        assert np.array_equal(piv[sep], pivr[sep]), i
+        assert np.count_nonzero(pivr != np.arange(1, 513)) > 400
+        x = np.linalg.solve(A0, Bh)
+        assert oracle.normwise_rel(rhs[i].cpu().numpy(), x) <= 1e-10, i

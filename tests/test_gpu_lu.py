@@ -159,3 +159,69 @@ def test_config2_full_size(cuda):
     x = db.cpu().numpy()
     fwd = np.abs(x - x_true).max() / np.abs(x_true).max()
     assert fwd <= 1e-12, fwd
+
+
+def _unshifted_case(n):
+    path = os.path.join(G.HERE, "reference_lu_unshifted.npz")
+    ref = np.load(path)
+    _, seed, info = (int(v) for v in ref[f"n{n}_meta"])
+    return (oracle.splitmix_uniform(seed, n, n), ref[f"n{n}_piv"], info, ref[f"n{n}_gap"],
+            ref[f"n{n}_diagU"])
+
+
+def _check_unshifted(cuda, n, dA0, dA, piv, info, ref_piv, ref_info, gap, ref_diag):
+    import torch
+    # pivots entry by entry on every pivot search whose two largest |candidates|
+    # differ by more than 1e-10 relative (flens/lapack/ge/tf2.tcc:101-108,
+    # cxxblas/level1/iamax.tcc:50-57); the fixture's smallest gap is ~1e-6, so
+    # this is every column
+    sep = gap > 1e-10
+    assert sep.mean() > 0.99
+    bad = np.nonzero((piv != ref_piv) & sep)[0]
+    assert bad.size == 0, (bad[:10], piv[bad[:10]], ref_piv[bad[:10]])
+    assert info == ref_info == 0
+    assert np.count_nonzero(piv != np.arange(1, n + 1)) > 0.9 * n      # it really pivots
+    d = torch.diagonal(dA).cpu().numpy()
+    assert np.max(np.abs(d - ref_diag)) / np.max(np.abs(ref_diag)) <= 1e-9
+    # backward error of the factorisation, on the GPU in FP64
+    L = torch.tril(dA, -1) + torch.eye(n, dtype=torch.float64, device=cuda)
+    U = torch.triu(dA)
+    P = np.arange(n)
+    for i, p in enumerate(piv.tolist()):
+        if p - 1 != i:
+            P[[i, p - 1]] = P[[p - 1, i]]
+    R = dA0[torch.from_numpy(P).to(cuda)] - L @ U
+    eps = np.finfo(np.float64).eps
+    berr = (R.abs().sum(0).max() / (n * dA0.abs().sum(0).max() * eps)).item()
+    assert berr <= BERR_TOL, berr
+
+
+@pytest.mark.parametrize("n", [2048, 4096])
+def test_pivots_unshifted_at_scale(cuda, n):
+    """Unshifted uniform[-1,1) LU at n = 2048 and 4096 (about n interchanges)
+    against the reference's own pivots and diag(U)."""
+    import torch
+    A0, ref_piv, ref_info, gap, ref_diag = _unshifted_case(n)
+    dA0 = fg.to_colmajor(torch.from_numpy(A0).to(cuda))
+    dA = fg.to_colmajor(dA0.clone())
+    ipiv = torch.zeros(n, dtype=torch.int32, device=cuda)
+    info = torch.zeros(1, dtype=torch.int32, device=cuda)
+    fg.dgetrf_dev(dA, ipiv, info)
+    fg.sync()
+    _check_unshifted(cuda, n, dA0, dA, ipiv.cpu().numpy(), int(info.item()), ref_piv, ref_info,
+                     gap, ref_diag)
+
+
+def test_split_lu_pivots_unshifted_n2048(cuda):
+    """The FP64-accurate split-update LU on the same n = 2048 unshifted input."""
+    import torch
+    n = 2048
+    A0, ref_piv, ref_info, gap, ref_diag = _unshifted_case(n)
+    dA0 = fg.to_colmajor(torch.from_numpy(A0).to(cuda))
+    dA = fg.to_colmajor(dA0.clone())
+    ipiv = torch.zeros(n, dtype=torch.int32, device=cuda)
+    info = torch.zeros(1, dtype=torch.int32, device=cuda)
+    fg.dgetrf_split_dev(dA, ipiv, info, 512)
+    fg.sync()
+    _check_unshifted(cuda, n, dA0, dA, ipiv.cpu().numpy(), int(info.item()), ref_piv, ref_info,
+                     gap, ref_diag)
