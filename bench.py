@@ -48,6 +48,42 @@ def lu_block_flops(n: int, nblocks: int | None = None) -> float:
     return fl
 
 
+def lu_step_flops(n: int, b: int) -> float:
+    """Flops of block step b (nb = 64) of the n x n blocked LU."""
+    r = n - NB * b
+    w = min(NB, r)
+    return r * w * w + w * w * (r - w) + 2.0 * (r - w) * (r - w) * w
+
+
+def lu_sample_blocks(n: int) -> list[int]:
+    """Block steps spread over the factorisation (n = 8192: 0, 32, 64, 96, 120):
+    the first carries the largest trailing update, the late ones are small
+    and cache-resident, so their per-flop rates differ."""
+    nsteps = -(-n // NB)
+    return sorted({min(nsteps - 1, int(round(f * nsteps))) for f in (0.0, 0.25, 0.5, 0.75, 0.9375)})
+
+
+def lu_seconds_from_samples(n: int, rates: dict) -> float:
+    """Time of the whole LU plus the two triangular solves from per-flop rates
+    measured at a few block steps: the rate is interpolated linearly in the
+    step index between the samples (flat beyond the last), each step's flops
+    divided by its rate, and the 2 n^2 flops of trs taken at the mean rate."""
+    nsteps = -(-n // NB)
+    bs = sorted(rates)
+    total = 0.0
+    for b in range(nsteps):
+        if b <= bs[0]:
+            rt = rates[bs[0]]
+        elif b >= bs[-1]:
+            rt = rates[bs[-1]]
+        else:
+            hi = next(x for x in bs if x >= b)
+            lo = max(x for x in bs if x <= b)
+            rt = rates[lo] if hi == lo else rates[lo] + (rates[hi] - rates[lo]) * (b - lo) / (hi - lo)
+        total += lu_step_flops(n, b) / rt
+    return total + 2.0 * n * n / (sum(rates.values()) / len(rates))
+
+
 # ------------------------------------------------------------- clocks --
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -114,17 +150,28 @@ def reference_arm(args, rank: int) -> None:
     # (pinned by tests/test_oracle_pin.py); oracle/_ref is only on machines
     # that hold the FLENS sources, and has no partial-factorisation entry.
     port = oracle.Port()
-    steps_blocks = 1
-    f_sample = lu_block_flops(n, steps_blocks)
-    f_total = lu_block_flops(n) + 2.0 * n * n
-    for _ in range(args.warmup):
-        port.time_dgetrf_steps(n, steps_blocks, threads, seed=7)
-    times = []
+    # each timed step runs one block step of the factorisation on every host
+    # thread (each on its own n x n copy), cycling through block steps spread
+    # over the factorisation; the per-flop rate of each sampled step is the
+    # mean over its repetitions, and the whole dgetrf+dgetrs time follows from
+    # those rates (lu_seconds_from_samples)
+    blocks = lu_sample_blocks(n)
+    for w in range(args.warmup):
+        port.time_dgetrf_step_at(n, blocks[-1], threads, seed=7 + w)
+    times, per_block = [], {b: [] for b in blocks}
     for s in range(args.steps):
-        t, _ = port.time_dgetrf_steps(n, steps_blocks, threads, seed=11 + s)
+        b = blocks[s % len(blocks)]
+        t, fl = port.time_dgetrf_step_at(n, b, threads, seed=11 + s)
         times.append(t)
-    # each thread factorised its own copy: `threads` samples per wall time
-    per_solve_s = statistics.mean(times) * f_total / f_sample
+        per_block[b].append(fl / t)
+    if any(not v for v in per_block.values()):       # fewer steps than sample points
+        for b, v in per_block.items():
+            if not v:
+                t, fl = port.time_dgetrf_step_at(n, b, threads, seed=99 + b)
+                v.append(fl / t)
+    rates = {b: statistics.mean(v) for b, v in per_block.items()}
+    per_solve_s = lu_seconds_from_samples(n, rates)
+    # each thread factorised its own copy: `threads` solves per that wall time
     value = threads / per_solve_s
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
@@ -136,9 +183,11 @@ def reference_arm(args, rank: int) -> None:
                    "nrhs": 1, "l2": "input 512 MiB > L2"},
         "cpu_baseline": {
             "value": value, "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": (f"each step: {threads} threads each run the first {steps_blocks} block step "
+            "sample": (f"step s: {threads} threads each run block step {blocks}[s mod {len(blocks)}] "
                        f"(panel+laswp+trsm+trailing gemm, nb=64) of the n={n} LU on its own copy; "
-                       f"scaled by flops {f_total:.3e}/{f_sample:.3e}")},
+                       f"whole dgetrf+dgetrs from the per-flop rates of those steps interpolated "
+                       f"over all {-(-n // NB)} block steps ({per_solve_s:.1f} s per thread)"),
+            "rates_gflops_per_thread": {str(b): round(r / 1e9, 4) for b, r in rates.items()}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -322,7 +371,7 @@ def our_arm(args, rank: int, world: int) -> None:
                 if ratio and d["launches"]:
                     traffic = ratio * d["bytes"] / d["launches"]
             result["roofline"] = {
-                "kernel": dom, "bound": "tensor", "achieved": achieved, "peak": peak,
+                "kernel": dom, "bound": "fp64_pipe", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None,
                 "traffic": traffic,
                 "peak_source": ("max of cuBLAS FP64 dgemm 8192^3 measured in this run "
@@ -374,7 +423,7 @@ MIXED_CASES = (
 )
 
 
-def mixed_subbench(torch, fg, dev, n=16384, reps=3):
+def mixed_subbench(torch, fg, dev, n=16384, reps=3, cases=None, gen="svd"):
     """Mixed-solve configuration: A = U diag(s) V^T (U, V from Householder QR of
     seeded Gaussian matrices, s geometric 1 -> 1/kappa), b = A x_true with 1 or
     64 right-hand sides.  Times flens_gb300_dgesv_mixed in every factor
@@ -387,8 +436,13 @@ def mixed_subbench(torch, fg, dev, n=16384, reps=3):
     g = torch.Generator(device=dev)
     g.manual_seed(2026)
     t0 = time.time()
-    U, _ = torch.linalg.qr(torch.randn((n, n), generator=g, dtype=torch.float64, device=dev))
-    V, _ = torch.linalg.qr(torch.randn((n, n), generator=g, dtype=torch.float64, device=dev))
+    if gen == "svd":
+        U, _ = torch.linalg.qr(torch.randn((n, n), generator=g, dtype=torch.float64, device=dev))
+        V, _ = torch.linalg.qr(torch.randn((n, n), generator=g, dtype=torch.float64, device=dev))
+    else:
+        # profiling input without torch.linalg (which a profiler may fail to
+        # load): unshifted uniform[-1,1), kappa in the 1e4-1e5 range
+        U = V = None
     gen_s = time.time() - t0
     f = fg.lib().flens_gb300_dgesv_mixed
     f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
@@ -409,8 +463,12 @@ def mixed_subbench(torch, fg, dev, n=16384, reps=3):
             mats.clear()
             rhs.clear()
             torch.cuda.empty_cache()
-            s = kappa ** (-torch.arange(n, dtype=torch.float64, device=dev) / (n - 1))
-            A = fg.to_colmajor((U * s) @ V.t())
+            if U is None:
+                A = fg.to_colmajor(torch.rand((n, n), generator=g, dtype=torch.float64,
+                                              device=dev).mul_(2).sub_(1))
+            else:
+                s = kappa ** (-torch.arange(n, dtype=torch.float64, device=dev) / (n - 1))
+                A = fg.to_colmajor((U * s) @ V.t())
             mats[kappa] = (A, A.abs().sum(1).max())
         A, anorm = mats[kappa]
         if nrhs not in rhs:
@@ -424,6 +482,8 @@ def mixed_subbench(torch, fg, dev, n=16384, reps=3):
         return (r.abs().amax(0) / (anorm * X.abs().amax(0) + b.abs().amax(0))).max().item()
 
     for kappa, nrhs, label, prec, solver, max_iter in MIXED_CASES:
+        if cases and label not in cases:
+            continue
         A, b, x, anorm = system(kappa, nrhs)
         if nrhs not in plain:
             # plain FP64 GPU solve on the same n and nrhs (timed after one warm-up)
@@ -466,6 +526,17 @@ def mixed_subbench(torch, fg, dev, n=16384, reps=3):
                 times.append(dt)
             rep += 1
         ms = sum(times) / len(times)
+        # one more run with per-launch event timing: where the time goes
+        fg.timing_enable(True)
+        torch.cuda.synchronize()
+        f(n, nrhs, A.data_ptr(), n, b.data_ptr(), n, X.data_ptr(), n, prec, solver, max_iter,
+          0.0, ctypes.byref(it), ctypes.byref(be), ctypes.byref(inf_), sp)
+        torch.cuda.synchronize()
+        fam = fg.timing_read()
+        fg.timing_enable(False)
+        kernels = {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
+                       "gbs": (round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1) if v["ms"] > 0 else None)}
+                   for k, v in sorted(fam.items(), key=lambda kv: -kv[1]["ms"])}
         berr = berr_of(A, X, b, anorm)
         fwd = ((X - x).abs().amax(0) / x.abs().amax(0)).max().item()
         out["cases"].append({"kappa": kappa, "nrhs": nrhs, "factor_precision": label,
@@ -474,11 +545,12 @@ def mixed_subbench(torch, fg, dev, n=16384, reps=3):
                              "backward_error": berr, "backward_error_over_n_eps": berr / (n * eps),
                              "forward_error": fwd,
                              "time_ratio_vs_plain_fp64": ms / plain[nrhs],
-                             "meets_10_n_eps": berr <= 10 * n * eps})
+                             "meets_10_n_eps": berr <= 10 * n * eps,
+                             "kernels": kernels})
         del X
     mats.clear()
     rhs.clear()
-    del U, V
+    U = V = None
     torch.cuda.empty_cache()
     return out
 
@@ -985,16 +1057,23 @@ def e2e_dgesv(torch, fg, A0, b0, args):
 
 
 def cpu_baseline(n):
+    """The oracle restatement on 1 host thread: block steps spread over the
+    n = 8192 factorisation, the whole dgetrf+dgetrs from their per-flop rates
+    (lu_seconds_from_samples)."""
     import oracle
     port = oracle.Port()
-    nblocks = 2
-    t, f_sample = port.time_dgetrf_steps(n, nblocks, 1, seed=5)
-    f_total = lu_block_flops(n) + 2.0 * n * n
-    per_solve = t * f_total / f_sample
+    blocks = lu_sample_blocks(n)
+    rates, spent = {}, 0.0
+    for b in blocks:
+        t, fl = port.time_dgetrf_step_at(n, b, 1, seed=5 + b)
+        rates[b] = fl / t
+        spent += t
+    per_solve = lu_seconds_from_samples(n, rates)
     return {"value": 1.0 / per_solve, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": (f"first {nblocks} block steps (nb=64) of the n={n} LU on 1 thread, "
-                       f"{t:.1f} s, scaled by flops {f_total:.3e}/{f_sample:.3e}"),
-            "gflops": f_sample / t / 1e9}
+            "sample": (f"block steps {blocks} (nb=64) of the n={n} LU on 1 thread ({spent:.1f} s); "
+                       f"whole dgetrf+dgetrs from their per-flop rates interpolated over all "
+                       f"{-(-n // NB)} block steps: {per_solve:.1f} s"),
+            "rates_gflops": {str(b): round(r / 1e9, 4) for b, r in rates.items()}}
 
 
 def only(args):
@@ -1048,7 +1127,9 @@ def only(args):
                              ref_slices=args.split_ref_slices)
         print(json.dumps(out))
     else:
-        print(json.dumps(mixed_subbench(torch, fg, dev, n=args.mixed_n, reps=1)))
+        cases = set(args.mixed_cases.split(",")) if args.mixed_cases else None
+        print(json.dumps(mixed_subbench(torch, fg, dev, n=args.mixed_n, reps=1, cases=cases,
+                                        gen=args.mixed_gen)))
 
 
 def main():
@@ -1068,6 +1149,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--mixed-n", type=int, default=16384)
+    ap.add_argument("--mixed-gen", choices=["svd", "uniform"], default="svd",
+                    help="--only mixed input: U diag(s) V^T (default) or unshifted uniform (profiling)")
+    ap.add_argument("--mixed-cases", default=None,
+                    help="comma-separated factor precisions for --only mixed (e.g. bf16,fp8)")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-split", action="store_true")
     ap.add_argument("--no-cholesky", action="store_true")

@@ -51,6 +51,22 @@ extern "C" __attribute__((weak, visibility("default"))) void xerbla_(const char 
     fprintf(stderr, " ** On entry to %6s parameter number %2d had an illegal value\n", buf, *info);
 }
 
+// BLAS routines have no INFO argument: a failure inside the library (a CUDA
+// error, a failed allocation, a device wait that timed out) goes to the
+// caller's hook if one is set (flens_gb300_set_blas_error_hook), else to
+// stderr, and is kept per thread for flens_gb300_blas_status().
+FG_API const char *flens_gb300_last_error(void);
+static thread_local int g_blas_status;
+static void (*g_blas_hook)(const char *routine, int status, const char *message) = nullptr;
+
+static void report_blas_failure(const char *routine, int st) {
+    g_blas_status = st;
+    if (st == kOk) return;
+    void (*hook)(const char *, int, const char *) = __atomic_load_n(&g_blas_hook, __ATOMIC_ACQUIRE);
+    if (hook) hook(routine, st, flens_gb300_last_error());
+    else fprintf(stderr, "[flens_gb300] %s failed (%d): %s\n", routine, st, flens_gb300_last_error());
+}
+
 static void report_xerbla(const char *name, int info) {
     memset(g_xerbla_name, 0, sizeof g_xerbla_name);
     for (int i = 0; i < 6 && name[i]; ++i) g_xerbla_name[i] = name[i];
@@ -213,7 +229,7 @@ FG_API void dgemm_(const char *TRANSA, const char *TRANSB, const int *M, const i
     }
     const int st = dgemm_host(ta == 'C' ? 'T' : ta, tb == 'C' ? 'T' : tb, *M, *N, *K, *ALPHA, A,
                               *LDA, B, *LDB, *BETA, C, *LDC);
-    if (st != kOk) fprintf(stderr, "[flens_gb300] dgemm_ failed (%d): %s\n", st, flens_gb300_last_error());
+    report_blas_failure("dgemm_", st);
 }
 
 // --------------------------------------------------------------- dtrsm_ --
@@ -248,7 +264,7 @@ FG_API void dtrsm_(const char *SIDE, const char *UPLO, const char *TRANSA, const
         st = dtrsm_launch(side, uplo, ta == 'C' ? 'T' : ta, diag, m, n, *ALPHA, a.p, a.ld, b.p, b.ld, s);
     if (st == kOk) st = view_out(b, B, m, n, *LDB, s);
     if (st == kOk) st = finish(s);
-    if (st != kOk) fprintf(stderr, "[flens_gb300] dtrsm_ failed (%d): %s\n", st, flens_gb300_last_error());
+    report_blas_failure("dtrsm_", st);
 }
 
 // ----------------------------------------------------------- LAPACK LU --
@@ -423,7 +439,7 @@ FG_API void dsyrk_(const char *UPLO, const char *TRANS, const int *N, const int 
         st = dsyrk_launch(uplo, tr == 'N' ? 'N' : 'T', n, k, *ALPHA, a.p, a.ld, *BETA, c.p, c.ld, s);
     if (st == kOk) st = view_out(c, C, n, n, *LDC, s);
     if (st == kOk) st = finish(s);
-    if (st != kOk) fprintf(stderr, "[flens_gb300] dsyrk_ failed (%d): %s\n", st, flens_gb300_last_error());
+    report_blas_failure("dsyrk_", st);
 }
 
 // ---------------------------------------------------------------- dtrmm_ --
@@ -458,7 +474,7 @@ FG_API void dtrmm_(const char *SIDE, const char *UPLO, const char *TRANSA, const
     if (st == kOk) st = dtrmm_launch(side, uplo, ta == 'C' ? 'T' : ta, diag, m, n, *ALPHA, a.p, a.ld, b.p, b.ld, s);
     if (st == kOk) st = view_out(b, B, m, n, *LDB, s);
     if (st == kOk) st = finish(s);
-    if (st != kOk) fprintf(stderr, "[flens_gb300] dtrmm_ failed (%d): %s\n", st, flens_gb300_last_error());
+    report_blas_failure("dtrmm_", st);
 }
 
 // ---------------------------------------------------------------- dsymm_ --
@@ -492,7 +508,7 @@ FG_API void dsymm_(const char *SIDE, const char *UPLO, const int *M, const int *
     if (st == kOk) st = dsymm_launch(side, uplo, m, n, *ALPHA, a.p, a.ld, b.p, b.ld, *BETA, c.p, c.ld, s);
     if (st == kOk) st = view_out(c, C, m, n, *LDC, s);
     if (st == kOk) st = finish(s);
-    if (st != kOk) fprintf(stderr, "[flens_gb300] dsymm_ failed (%d): %s\n", st, flens_gb300_last_error());
+    report_blas_failure("dsymm_", st);
 }
 
 // --------------------------------------------------------------- dsyr2k_ --
@@ -527,7 +543,7 @@ FG_API void dsyr2k_(const char *UPLO, const char *TRANS, const int *N, const int
         st = dsyr2k_launch(uplo, tr == 'N' ? 'N' : 'T', n, k, *ALPHA, a.p, a.ld, b.p, b.ld, *BETA, c.p, c.ld, s);
     if (st == kOk) st = view_out(c, C, n, n, *LDC, s);
     if (st == kOk) st = finish(s);
-    if (st != kOk) fprintf(stderr, "[flens_gb300] dsyr2k_ failed (%d): %s\n", st, flens_gb300_last_error());
+    report_blas_failure("dsyr2k_", st);
 }
 
 // ------------------------------------------------------ LAPACK Cholesky --
@@ -878,8 +894,8 @@ FG_API void dlaqge_(const int *M, const int *N, double *A, const int *LDA, const
     }
     if (st == kOk) st = view_out(a, A, m, n, *LDA, s);
     if (st == kOk) st = finish(s);
-    if (st != kOk) fprintf(stderr, "[flens_gb300] dlaqge_ failed (%d): %s\n", st, flens_gb300_last_error());
-    else *EQUED = eq;
+    report_blas_failure("dlaqge_", st);
+    if (st == kOk) *EQUED = eq;
 }
 
 // flens/lapack/interface/src/gesvx.cc:13-118.  EQUED reports the scaling
@@ -1250,3 +1266,15 @@ FG_API int flens_gb300_sync(void *stream) {
 }
 
 FG_API int flens_gb300_version(void) { return 100; }
+
+// Where failures of the BLAS routines (which have no INFO) are reported:
+// hook(routine, status, message) on the calling thread instead of stderr;
+// nullptr restores the stderr report.
+FG_API void flens_gb300_set_blas_error_hook(void (*hook)(const char *routine, int status,
+                                                         const char *message)) {
+    __atomic_store_n(&g_blas_hook, hook, __ATOMIC_RELEASE);
+}
+
+// Status of the calling thread's last BLAS call (dgemm_, dtrsm_, dsyrk_,
+// dtrmm_, dsymm_, dsyr2k_, dlaqge_): 0, or a FLENS_GB300_ERR_* code.
+FG_API int flens_gb300_blas_status(void) { return g_blas_status; }

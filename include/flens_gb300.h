@@ -416,6 +416,17 @@ int flens_gb300_sync(void *stream);
 /* Last error message of the calling thread ("" if none). */
 const char *flens_gb300_last_error(void);
 
+/* BLAS routines have no INFO: an internal failure (FLENS_GB300_ERR_*) of
+ * dgemm_, dtrsm_, dsyrk_, dtrmm_, dsymm_, dsyr2k_ or dlaqge_ goes to `hook`
+ * (routine name, status, message; called on the failing thread) instead of a
+ * line on stderr; nullptr restores the stderr line.  The calling thread's last
+ * such status (0 on success) is flens_gb300_blas_status().  The reference's
+ * BLAS shims can fail only through xerbla_ (flens/blas/interface/blas/
+ * gemm.cc:158-181); these have no counterpart there. */
+void flens_gb300_set_blas_error_hook(void (*hook)(const char *routine, int status,
+                                                  const char *message));
+int flens_gb300_blas_status(void);
+
 /* Diagnostics, no counterpart in the reference.  Device allocations
  * (cudaMalloc) the library has made since it was loaded. */
 long long flens_gb300_device_alloc_count(void);
