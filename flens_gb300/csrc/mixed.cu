@@ -30,6 +30,7 @@
 #include "common.cuh"
 
 #include <math.h>
+#include <stdlib.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -306,12 +307,17 @@ pc_prep_kernel(int n, const MT *__restrict__ F, int ldf, double *__restrict__ Di
     }
 }
 
-__device__ __forceinline__ void pc_release(unsigned long long *p, unsigned long long v) {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+// A solved block is published as 128 tagged 64-bit words, (epoch << 32) |
+// one 32-bit half of a double, written with single-copy-atomic 64-bit stores.
+// A reader polls the words themselves until all carry the call's epoch: one
+// L2 round trip per hand-off, where a ready flag costs the flag's round trip,
+// then the data's, plus the writer's release fence.
+__device__ __forceinline__ void pc_put(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
-__device__ __forceinline__ unsigned long long pc_acquire(const unsigned long long *p) {
+__device__ __forceinline__ unsigned long long pc_get(const unsigned long long *p) {
     unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
 
@@ -325,20 +331,32 @@ __device__ __forceinline__ void pc_fetch(MT (&v)[16], const MT *__restrict__ F, 
     for (int u = 0; u < 16; ++u) v[u] = (rok && K0 + 16 * q + u < n) ? src[(size_t)u * ldf] : MT(0);
 }
 
-// Waits (thread 0, bounded) until flags[idx] holds the call's epoch; false
-// on a timeout (status set), after which the CTA must return.
-__device__ __forceinline__ bool pc_wait(const unsigned long long *flags, int idx,
-                                        unsigned long long epoch, int *status, int *s_abort) {
-    if (threadIdx.x == 0) {
-        unsigned spins = 0;
-        while (pc_acquire(&flags[idx]) != epoch) {
-            if (++spins > kSpinLimit) {
-                atomicOr(status, kDevBarrierTimeout);
-                *s_abort = 1;
-                break;
+// Reads the published block of x starting at row K0 into dst[0..63] (rows at
+// or beyond n read as zero): threads 0..127 each poll one tagged word, bounded
+// by kSpinLimit.  false on a timeout (status set), after which the CTA must
+// return; ends with a block barrier either way.
+__device__ __forceinline__ bool pc_take(const unsigned long long *tag, int K0, int n,
+                                        unsigned epoch, double *dst, int *status, int *s_abort) {
+    const int t = threadIdx.x;
+    if (t < 2 * PC_NB) {
+        const int p = t >> 1;
+        unsigned half = 0;
+        if (K0 + p < n) {
+            const unsigned long long *w = tag + 2 * (size_t)K0 + t;
+            unsigned long long v = pc_get(w);
+            unsigned spins = 0;
+            while ((unsigned)(v >> 32) != epoch) {
+                if (++spins > kSpinLimit) {
+                    atomicOr(status, kDevBarrierTimeout);
+                    *s_abort = 1;
+                    break;
+                }
+                if (spins > 64) __nanosleep(32);
+                v = pc_get(w);
             }
-            if (spins > 32) __nanosleep(32);
+            half = (unsigned)v;
         }
+        reinterpret_cast<unsigned *>(dst + p)[t & 1] = half;
     }
     __syncthreads();
     return *s_abort == 0;
@@ -346,14 +364,14 @@ __device__ __forceinline__ bool pc_wait(const unsigned long long *flags, int idx
 
 // One triangle of the preconditioner in place on X (n), in ONE cooperative
 // launch: CTA s solves the s-th block in solve order (the first rows for L,
-// the last for U) and publishes it with a release store of the call's epoch.
-// The stored blocks before the predecessor are applied as they are published,
+// the last for U) and publishes it into `tag` with the call's epoch.  The
+// stored blocks before the predecessor are applied as they are published,
 // the next one loaded into registers while waiting for the current one.
 template <typename MT, bool LOWER>
 __global__ void __launch_bounds__(PC_THREADS, 2)
 pc_chain_kernel(int n, const MT *__restrict__ F, int ldf, const double *__restrict__ Dinv,
-                const double *__restrict__ P, double *X, unsigned long long *flags,
-                unsigned long long epoch, int *status) {
+                const double *__restrict__ P, double *X, unsigned long long *tag, unsigned epoch,
+                int *status) {
     __shared__ double xk[2][PC_NB];
     __shared__ double part[4][PC_NB];
     __shared__ double rhs[PC_NB];
@@ -374,16 +392,14 @@ pc_chain_kernel(int n, const MT *__restrict__ F, int ldf, const double *__restri
             pi[u] = s > 0 ? psrc[u * PC_NB] : 0.0;
         }
     }
+    __syncthreads();                 // s_abort initialised
     // blocks solved before the predecessor: solve-order indices 0 .. s-2
     const int npre = s - 1;
     double acc = 0.0;
     MT c0[16], c1[16];
     auto kblk = [&](int s2) { return (LOWER ? s2 : nblk - 1 - s2) * PC_NB; };
     auto apply = [&](MT(&v)[16], int s2, int buf) -> bool {
-        if (!pc_wait(flags, s2, epoch, status, &s_abort)) return false;
-        const int K0 = kblk(s2);
-        if (tid < PC_NB) xk[buf][tid] = (K0 + tid < n) ? __ldcg(&X[K0 + tid]) : 0.0;
-        __syncthreads();
+        if (!pc_take(tag, kblk(s2), n, epoch, xk[buf], status, &s_abort)) return false;
         // the block's 16 products summed on their own, then added
         double blk = 0.0;
 #pragma unroll
@@ -401,7 +417,7 @@ pc_chain_kernel(int n, const MT *__restrict__ F, int ldf, const double *__restri
     }
     part[q][r] = acc;
     __syncthreads();
-    if (q == 0) rhs[r] = rok ? __ldcg(&X[R0 + r]) - ((part[0][r] + part[1][r]) + (part[2][r] + part[3][r]))
+    if (q == 0) rhs[r] = rok ? X[R0 + r] - ((part[0][r] + part[1][r]) + (part[2][r] + part[3][r]))
                              : 0.0;
     __syncthreads();
     double cp = 0.0;
@@ -411,10 +427,8 @@ pc_chain_kernel(int n, const MT *__restrict__ F, int ldf, const double *__restri
     __syncthreads();
     double xr = (part[0][r] + part[1][r]) + (part[2][r] + part[3][r]);
     if (s > 0) {
-        if (!pc_wait(flags, s - 1, epoch, status, &s_abort)) return;
-        const int P0 = (LOWER ? b - 1 : b + 1) * PC_NB;
-        if (tid < PC_NB) xk[0][tid] = (P0 + tid < n) ? __ldcg(&X[P0 + tid]) : 0.0;
-        __syncthreads();
+        // xk[0] was last read before two barriers ago
+        if (!pc_take(tag, (LOWER ? b - 1 : b + 1) * PC_NB, n, epoch, xk[0], status, &s_abort)) return;
         double pp = 0.0;
 #pragma unroll
         for (int u = 0; u < 16; ++u) pp = fma(pi[u], xk[0][16 * q + u], pp);
@@ -422,9 +436,14 @@ pc_chain_kernel(int n, const MT *__restrict__ F, int ldf, const double *__restri
         __syncthreads();
         xr -= (part[0][r] + part[1][r]) + (part[2][r] + part[3][r]);
     }
-    if (q == 0 && rok) X[R0 + r] = xr;
-    __syncthreads();
-    if (tid == 0) pc_release(&flags[s], epoch);
+    if (q == 0 && rok) {
+        X[R0 + r] = xr;
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(xr);
+        const unsigned long long e = (unsigned long long)epoch << 32;
+        unsigned long long *w = tag + 2 * (size_t)(R0 + r);
+        pc_put(w, e | (bits & 0xffffffffull));
+        pc_put(w + 1, e | (bits >> 32));
+    }
 }
 
 // Blocks per SM of the chain kernel (0 if the query fails), per device.
@@ -456,7 +475,16 @@ int grid_for(size_t total) {
 
 size_t a256(size_t b) { return (b + 255) / 256 * 256; }
 
-constexpr int kGmresM = 100;      // restart length
+// GMRES restart length: 100, or FLENS_GB300_GMRES_RESTART (2..4000); the
+// Krylov basis takes n x (restart+1) doubles
+int gmres_restart() {
+    static int m = [] {
+        const char *e = getenv("FLENS_GB300_GMRES_RESTART");
+        const int v = e ? atoi(e) : 0;
+        return (v >= 2 && v <= 4000) ? v : 100;
+    }();
+    return m;
+}
 constexpr int kPrecSplit = 4;     // FP64 storage, split-GEMM trailing updates
 
 struct Solver {
@@ -490,6 +518,8 @@ struct Solver {
     std::vector<double> bnorm;
     // preconditioner blocks (pc_prep_kernel): Dinv and P of L, then of U
     double *pcDL = nullptr, *pcPL = nullptr, *pcDU = nullptr, *pcPU = nullptr;
+    unsigned long long *pcTag = nullptr;   // 2n tagged words: the solved blocks of a call
+    unsigned pc_epoch = 0;
     bool pc = false;            // chained block-inverse preconditioner in use
 };
 
@@ -501,7 +531,8 @@ bool pc_fits(int n, bool fp64_factors) {
     return per > 0 && (long long)per * num_sms() >= nblk && nblk <= 4096;
 }
 
-size_t pc_bytes(int n) { return 4 * a256((size_t)ceil_div(n, PC_NB) * PC_NB * PC_NB * sizeof(double)); }
+// bytes of Dinv or P of one triangle
+size_t pc_block_bytes(int n) { return a256((size_t)ceil_div(n, PC_NB) * PC_NB * PC_NB * sizeof(double)); }
 
 // Dinv and P of both triangles of the stored factors.
 template <typename MT>
@@ -525,15 +556,19 @@ template <typename MT>
 int pc_solve(Solver &S, const MT *F, int ldf, bool lower, double *x) {
     int n = S.n;
     const int nblk = ceil_div(n, PC_NB);
-    unsigned long long *flags = nullptr, epoch = 0;
-    int st = workspace_flags(S.s, nblk, &flags, &epoch);
-    if (st != kOk) return st;
     Workspace *w = workspace_for(S.s, 0);
     if (!w) return kErrAlloc;
     int *status = w->status;
+    // a fresh epoch per call; the tag words start at zero (epoch 0 is never used)
+    unsigned epoch = ++S.pc_epoch;
+    if (epoch == 0) {
+        FG_CUDA(cudaMemsetAsync(S.pcTag, 0, 2 * sizeof(unsigned long long) * (size_t)n, S.s));
+        epoch = S.pc_epoch = 1;
+    }
     const double *Dv = lower ? S.pcDL : S.pcDU;
     const double *Pv = lower ? S.pcPL : S.pcPU;
-    void *args[] = {&n, &F, &ldf, &Dv, &Pv, &x, &flags, &epoch, &status};
+    unsigned long long *tag = S.pcTag;
+    void *args[] = {&n, &F, &ldf, &Dv, &Pv, &x, &tag, &epoch, &status};
     KTimer kt(kFamPrecond, S.s, (double)n * n, (double)n * n * sizeof(MT) / 2.0 + 16.0 * n * PC_NB);
     const void *fn = lower ? (const void *)pc_chain_kernel<MT, true> : (const void *)pc_chain_kernel<MT, false>;
     FG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(nblk), dim3(PC_THREADS), args, 0, S.s));
@@ -649,7 +684,7 @@ int residual(Solver &S, int j0, int nc, std::vector<double> &berr) {
 // one restarted GMRES(M) cycle for column j: x_j += d with (LU)^-1 A d ~ (LU)^-1 r_j
 // (r_j already in R).  Returns the number of Arnoldi steps taken in *steps.
 int gmres_cycle(Solver &S, int j, double rtol, int *steps) {
-    const int n = S.n, M = kGmresM;
+    const int n = S.n, M = gmres_restart();
     double *r = S.R + (size_t)j * n;
     double *sc = S.colv + 3 * S.nrhs;     // device scalars: [scale, norm]
     *steps = 0;
@@ -774,7 +809,7 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
     // split: slot 3: LU64 | ipiv | perm | info | R | D64 | colv | anorm | h | h2
     // (slots 0-2 belong to the split GEMM while the LU runs)
     const bool split = precision == kPrecSplit;
-    const int M = kGmresM;
+    const int M = gmres_restart();
     size_t off = 0;
     const size_t oA32 = off;
     off += split ? a256((size_t)n * n * sizeof(double)) : a256((size_t)S.ld32 * n * sizeof(float));
@@ -888,8 +923,9 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
                 const size_t vB = a256((size_t)n * (M + 1) * sizeof(double));
                 const size_t nB = a256((size_t)n * sizeof(double));
                 S.pc = pc_fits(n, split);
-                const size_t pB = S.pc ? pc_bytes(n) / 4 : 0;
-                char *p2 = (char *)workspace_slot(s, 2, vB + 2 * nB + 4 * pB);
+                const size_t pB = S.pc ? pc_block_bytes(n) : 0;
+                const size_t tB = S.pc ? a256(2 * sizeof(unsigned long long) * (size_t)n) : 0;
+                char *p2 = (char *)workspace_slot(s, 2, vB + 2 * nB + 4 * pB + tB);
                 if (!p2) return kErrAlloc;
                 S.V = (double *)p2;
                 S.w = (double *)(p2 + vB);
@@ -900,6 +936,8 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
                     S.pcPL = (double *)(pp + pB);
                     S.pcDU = (double *)(pp + 2 * pB);
                     S.pcPU = (double *)(pp + 3 * pB);
+                    S.pcTag = (unsigned long long *)(pp + 4 * pB);
+                    FG_CUDA(cudaMemsetAsync(S.pcTag, 0, tB, s));
                     st = split ? pc_prepare<double>(S, S.LU64, n) : pc_prepare<float>(S, S.A32, S.ld32);
                     if (st != kOk) return st;
                 } else if (!split) {

@@ -265,11 +265,19 @@ struct SplitGeom {
         return nchunks == 1 ? (dg - 1 + per - 1) / per : (dg - 1) * nchunks;
     }
     __host__ __device__ void decode(int g, int &dg, int &slo, int &shi, int &k0, int &k1) const {
+        int gi, cnt;
+        decode(g, dg, slo, shi, k0, k1, gi, cnt);
+    }
+    // also: gi = the group's index within its diagonal, cnt = count(dg)
+    __host__ __device__ void decode(int g, int &dg, int &slo, int &shi, int &k0, int &k1, int &gi,
+                                    int &cnt) const {
         for (dg = S + 1; dg > 2; --dg) {
             const int c = count(dg);
             if (g < c) break;
             g -= c;
         }
+        gi = g;
+        cnt = count(dg);
         if (nchunks == 1) {
             slo = 1 + g * per;
             shi = slo + per - 1 < dg - 1 ? slo + per - 1 : dg - 1;
@@ -284,11 +292,20 @@ struct SplitGeom {
     }
 };
 
-// FP64 recombination epilogue.  An exact group sum acc (an integer <= 2^24
-// held in FP32) times 2^(e_i + f_j - bits*dg) is built by moving the FP32
-// exponent field into an FP64 one (exact; no FP64 multiply), and the groups of
-// a tile are summed in W (S = S + v, one FP64 add per element and group, the
-// first group stores v); the last group finishes C = (beta*C) + (alpha*S).
+// Recombination epilogue.  Every group sum acc is an exact integer of
+// magnitude <= 2^24 held in FP32, and all groups of one diagonal dg share the
+// scale 2^(e_i + f_j - bits*dg).  So the groups of a diagonal are summed
+// exactly in int32, in segments of at most kSegGroups groups (127 * 2^24 <
+// 2^31), in Wi; at the end of a segment the integer sum is converted to FP64
+// (exact), scaled by moving its exponent field (exact) and added to the FP64
+// sum Wd (one rounding per segment, largest dg first).  The last segment of
+// the last diagonal finishes C = (beta*C) + (alpha*S).  Per group this is an
+// int32 read-modify-write of the CTA's group-sum tile and no FP64 work; the
+// FP64 add and its 8-byte traffic come once per diagonal.  (Summing every
+// group into FP64 costs one FP64 add and a 16-byte read-modify-write per
+// element and group, and that epilogue, not the MMAs, bounded the kernel.)
+constexpr int kSegGroups = 127;
+
 struct EpiSplit {
     static constexpr int kBN = 256;
     static constexpr int kTmemExtra = 0;
@@ -296,8 +313,8 @@ struct EpiSplit {
     double alpha, beta;
     double *C;
     int ldc;
-    double *W;                                   // group sums: one BM x BN tile per CTA
-    int ldw;                                     // unused (tiles are BM x BN, column-major)
+    double *Wd;                                  // FP64 sums: one BM x BN tile per CTA
+    int *Wi;                                     // int32 segment sums: one BM x BN tile per CTA
     const int *ea, *eb;                          // row exponents of op(A), column exponents of op(B)
 
     __device__ int groups() const { return geo.ngroups; }
@@ -310,39 +327,61 @@ struct EpiSplit {
     }
     __device__ void apply(int g, int row, bool row_ok, int col, int ncol,
                           const uint32_t (&r)[32], uint32_t) const {
-        int dg, slo, shi, k0, k1;
-        geo.decode(g, dg, slo, shi, k0, k1);
-        const bool first = g == 0, last = g == geo.ngroups - 1;
+        int dg, slo, shi, k0, k1, gi, cnt;
+        geo.decode(g, dg, slo, shi, k0, k1, gi, cnt);
+        const bool seg_first = gi % kSegGroups == 0;
+        const bool seg_last = gi % kSegGroups == kSegGroups - 1 || gi == cnt - 1;
+        const bool first = dg == geo.S + 1 && gi < kSegGroups;          // first segment of all
+        const bool last = dg == 2 && gi == cnt - 1;                     // last segment of all
+        // these depend on g only: uniform over the warp, whose lanes all take
+        // part in the shuffles below
         const int lane = threadIdx.x & 31;
         const int fl = lane < ncol ? eb[col + lane] : 0;
-        // FP64 exponent field = FP32 field + (1023 - 127) + e_i + f_j - bits*dg
-        const long long krow = row_ok ? (long long)(ea[row] - geo.bits * dg + 896) : 0;
+        const int erow = row_ok ? ea[row] - geo.bits * dg : 0;
         const size_t r0 = (size_t)(row_ok ? row : 0);
-        // this CTA's own tile of group sums, reused for each of its tiles: it
-        // stays in L2 (152 x 256 KB) instead of spanning m x n
-        double *wrow = W + (size_t)blockIdx.x * (tc::BM * kBN) + (r0 & (tc::BM - 1)) +
-                       (size_t)(col & (kBN - 1)) * tc::BM;
+        // this CTA's own tiles of sums, reused for each of its tiles: they
+        // stay in L2 (152 x 384 KB) instead of spanning m x n
+        const size_t off = (size_t)blockIdx.x * (tc::BM * kBN) + (r0 & (tc::BM - 1)) +
+                           (size_t)(col & (kBN - 1)) * tc::BM;
+        int *wi = Wi + off;
+        // the segment's integer sums: all 32 loads in flight before any use
+        int iv[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            iv[j] = (!seg_first && row_ok && j < ncol) ? __ldcg(wi + (size_t)j * tc::BM) : 0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) iv[j] += __float2int_rn(__uint_as_float(r[j]));   // exact
+        if (!seg_last) {
+            if (row_ok) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (j < ncol) __stcg(wi + (size_t)j * tc::BM, iv[j]);
+            }
+            return;
+        }
+        // end of a segment: S = S + I * 2^(e_i + f_j - bits*dg)
+        double *wd = Wd + off;
         double *crow = C + r0 + (size_t)col * ldc;
 #pragma unroll
         for (int h = 0; h < 32; h += 16) {
             double sv[16];
 #pragma unroll
             for (int j = 0; j < 16; ++j)
-                sv[j] = (!first && row_ok && h + j < ncol) ? __ldcg(wrow + (size_t)(h + j) * tc::BM) : 0.0;
+                sv[j] = (!first && row_ok && h + j < ncol) ? __ldcg(wd + (size_t)(h + j) * tc::BM) : 0.0;
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-                const long long kj = krow + __shfl_sync(0xffffffffu, fl, h + j);
-                const uint32_t fb = r[h + j];
+                const int sh = erow + __shfl_sync(0xffffffffu, fl, h + j);
                 double v = 0.0;
-                if (fb & 0x7FFFFFFFu)
-                    v = __longlong_as_double((long long)((unsigned long long)(fb & 0x80000000u) << 32) |
-                                             ((long long)(fb & 0x7FFFFFFFu) * (1ll << 29) + kj * (1ll << 52)));
+                if (iv[h + j] != 0) {
+                    const long long bits = __double_as_longlong(__int2double_rn(iv[h + j]));
+                    v = __longlong_as_double(bits + ((long long)sh << 52));
+                }
                 sv[j] = first ? v : __dadd_rn(sv[j], v);
             }
             if (row_ok && !last) {
 #pragma unroll
                 for (int j = 0; j < 16; ++j)
-                    if (h + j < ncol) __stcg(wrow + (size_t)(h + j) * tc::BM, sv[j]);
+                    if (h + j < ncol) __stcg(wd + (size_t)(h + j) * tc::BM, sv[j]);
             } else if (row_ok) {
                 double cv[16];
 #pragma unroll
@@ -484,9 +523,11 @@ int dgemm_split_launch_at(char transA, char transB, int m, int n, int k, double 
     if ((rc = tc::prepare_kernel<kTcBF16, EpiSplit>()) != kOk) return rc;
     const int ntiles = ceil_div(m, tc::BM) * ceil_div(n, EpiSplit::kBN);
     const int grid = ntiles < num_sms() ? ntiles : num_sms();
-    double *W = (double *)workspace_slot(s, 2, (size_t)grid * tc::BM * EpiSplit::kBN * sizeof(double));
+    const size_t tileB = (size_t)tc::BM * EpiSplit::kBN;
+    char *W = (char *)workspace_slot(s, 2, (size_t)grid * tileB * (sizeof(double) + sizeof(int)));
     if (!W) return kErrAlloc;
-    const EpiSplit epi{geo, alpha, beta, C, ldC, W, tc::BM, ea, eb};
+    const EpiSplit epi{geo, alpha, beta, C, ldC, (double *)W,
+                       (int *)(W + (size_t)grid * tileB * sizeof(double)), ea, eb};
     const double pairs = (double)S * (S + 1) / 2;
     KTimer kt(kFamSplit, s, 2.0 * pairs * m * (double)n * geo.Kp,
               2.0 * ldS * ((double)m + n) + 16.0 * m * (double)n);   // digits in, C in + out

@@ -11,9 +11,11 @@ GPU result can be compared with it bit for bit:
   summed over k in FP32 on the tensor cores; every group of pairs and k range
   is small enough that all partial sums are integers of magnitude <= 2^24, so
   the sums are exact (here: int64 matmul);
-* the group sums, scaled exactly by 2^(e_i + f_j - beta*dg), are added in
-  FP64 largest dg first, S = S + acc * 2^(...) (one rounding per group), and
-  C = (beta*C) + (alpha*S) at the end.
+* the group sums of one diagonal dg share the scale 2^(e_i + f_j - beta*dg):
+  they are added exactly as integers, in segments of at most SEG_GROUPS
+  groups (in the diagonal's group order), and each segment's integer sum,
+  scaled exactly, is added in FP64, largest dg first, S = S + I * 2^(...)
+  (one rounding per segment); C = (beta*C) + (alpha*S) at the end.
 
 The digits are the balanced base-2^beta digits of x = a 2^(beta - e_i),
 d_s = R_s - 2^beta R_{s-1} with R_s = rint(x 2^(beta (s-1))) (round half to
@@ -27,6 +29,7 @@ import math
 import numpy as np
 
 ACC_LIMIT = 1 << 24          # exact FP32 integer range
+SEG_GROUPS = 127             # groups per exact int32 segment sum: 127 * 2^24 < 2^31
 BK = 64                      # k-block of the tensor-core kernel (bf16: 128 bytes)
 
 
@@ -95,14 +98,24 @@ def split_gemm_model(alpha, opA, opB, beta_c, C, beta, S):
     dA = digits(opA, e, beta, S).astype(np.float64)
     dB = digits(opB.T, f, beta, S).astype(np.float64)
     Ssum = np.zeros((M, N))
-    for (dg, slo, shi, k0, k1) in plan_groups(beta, S, K):
+    groups = plan_groups(beta, S, K)
+    seg = None            # exact integer sum of the open segment
+    gi = 0                # index of the group within its diagonal
+    for idx, (dg, slo, shi, k0, k1) in enumerate(groups):
+        if idx > 0 and groups[idx - 1][0] != dg:
+            gi = 0
         k1 = min(k1, K)
         if k0 >= k1:
             acc = np.zeros((M, N))
         else:
             acc = sum(dA[s - 1][:, k0:k1] @ dB[dg - s - 1][:, k0:k1].T for s in range(slo, shi + 1))
         assert np.abs(acc).max(initial=0) <= ACC_LIMIT
-        Ssum += np.ldexp(acc, (e[:, None] + f[None, :] - beta * dg).astype(np.int32))
+        seg = acc if gi % SEG_GROUPS == 0 else seg + acc
+        assert np.abs(seg).max(initial=0) < 2 ** 31
+        last_of_diag = idx == len(groups) - 1 or groups[idx + 1][0] != dg
+        if gi % SEG_GROUPS == SEG_GROUPS - 1 or last_of_diag:
+            Ssum += np.ldexp(seg, (e[:, None] + f[None, :] - beta * dg).astype(np.int32))
+        gi += 1
     C[...] = (beta_c * C) + (alpha * Ssum)
     return C
 

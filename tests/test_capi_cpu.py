@@ -329,3 +329,38 @@ def test_batched_plan_argument_errors(flib):
     assert f(2, n.ctypes.data, k.ctypes.data, None, ld.ctypes.data, None, None, ld.ctypes.data,
              None, 0, None, None, 0, None, ctypes.byref(plan)) == -2
     assert "illegal size" in fg.last_error()
+
+
+def test_blas_failure_goes_to_the_hook_without_gpu(capfd):
+    # BLAS routines have no INFO: an internal failure (here: no device) goes to
+    # the caller's hook instead of stderr, and the thread's BLAS status keeps it
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    L = fg.lib()
+    HOOK = ctypes.CFUNCTYPE(None, ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p)
+    seen = []
+    hook = HOOK(lambda r, st, msg: seen.append((r.decode(), st, msg.decode())))
+    L.flens_gb300_set_blas_error_hook.argtypes = [HOOK]
+    L.flens_gb300_set_blas_error_hook.restype = None
+    L.flens_gb300_blas_status.restype = ctypes.c_int
+    L.flens_gb300_set_blas_error_hook(hook)
+    try:
+        A, B, C = (np.asfortranarray(np.ones((3, 3))) for _ in range(3))
+        fg.dgemm("N", "N", 1.0, A, B, 0.0, C)
+        assert L.flens_gb300_blas_status() == fg.ERR_NO_DEVICE
+        assert seen and seen[-1][0] == "dgemm_" and seen[-1][1] == fg.ERR_NO_DEVICE
+        assert "dgemm_ failed" not in capfd.readouterr().err
+    finally:
+        L.flens_gb300_set_blas_error_hook(HOOK())
+    fg.dgemm("N", "N", 1.0, A, B, 0.0, C)
+    assert "dgemm_ failed (-1003)" in capfd.readouterr().err
+
+
+def test_allocation_diagnostics_without_gpu():
+    L = fg.lib()
+    L.flens_gb300_device_alloc_count.restype = ctypes.c_longlong
+    L.flens_gb300_test_fail_device_allocs.argtypes = [ctypes.c_int]
+    before = L.flens_gb300_device_alloc_count()
+    L.flens_gb300_test_fail_device_allocs(0)
+    assert L.flens_gb300_device_alloc_count() == before >= 0

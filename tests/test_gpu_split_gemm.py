@@ -205,3 +205,15 @@ def test_split_full_size_wide_range(cuda, port):
     Cs = np.zeros((64, n), order="F")
     port.dgemm("N", "N", 1.0, As, Bh, 0.0, Cs)
     assert oracle.normwise_rel(C.cpu().numpy()[rows, :], Cs) <= 1e-13
+
+
+def test_split_bitwise_vs_model_several_groups_per_diagonal(cuda):
+    # k = 2048: one K chunk, one slice pair per group, so every diagonal dg
+    # has dg - 1 groups whose exact integer sums are added before the FP64 sum
+    m, n, k = 130, 270, 2048
+    A = wide_range(31, m, k, 16)
+    B = wide_range(32, k, n, 16)
+    C = wide_range(33, m, n, 0)
+    got, used = run_split(cuda, "N", "N", 1.5, A, B, 0.5, C)
+    want = sm.split_gemm_model(1.5, A, B, 0.5, C.copy(), BITS, used)
+    np.testing.assert_array_equal(got, want)
