@@ -140,6 +140,64 @@ struct DevView {
     bool staged = false;
 };
 
+// Copies between device memory and PINNED host memory can run as a kernel
+// that loads or stores the host array through its device mapping (pinned
+// memory is mapped into the GPU's address space), instead of a copy-engine
+// DMA.  On this part a 512 MiB DMA to pinned host memory took either 2.8 ms
+// or 22-45 ms from one call to the next (the LU beside it did not change); a
+// kernel takes the same path every time.  FLENS_GB300_HOST_COPY=dma keeps the
+// DMA.  Pageable host memory always goes through the DMA path.
+__global__ void host_copy_kernel(int rows, int cols, const double *__restrict__ src, long long lds,
+                                 double *__restrict__ dst, long long ldd) {
+    if (lds == rows && ldd == rows && ((((uintptr_t)src) | ((uintptr_t)dst)) & 15) == 0) {
+        const size_t total = (size_t)rows * cols, pairs = total / 2;
+        const double2 *s2 = (const double2 *)src;
+        double2 *d2 = (double2 *)dst;
+        for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < pairs;
+             e += (size_t)gridDim.x * blockDim.x)
+            d2[e] = s2[e];
+        if ((total & 1) && blockIdx.x == 0 && threadIdx.x == 0) dst[total - 1] = src[total - 1];
+        return;
+    }
+    const size_t total = (size_t)rows * cols;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const size_t j = e / rows, i = e % rows;
+        dst[i + j * ldd] = src[i + j * lds];
+    }
+}
+
+bool host_copy_by_kernel() {
+    static bool on = [] {
+        const char *e = getenv("FLENS_GB300_HOST_COPY");
+        return !(e && strcmp(e, "dma") == 0);
+    }();
+    return on;
+}
+
+// Device address of pinned (mapped) host memory, or nullptr for pageable
+// memory and device memory.
+void *mapped_host(const void *h) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+int host_copy_launch(int rows, int cols, const double *src, long long lds, double *dst, long long ldd,
+                     cudaStream_t s) {
+    const size_t total = (size_t)rows * cols;
+    int blocks = (int)ceil_div(total, (size_t)512);
+    if (blocks > num_sms() * 8) blocks = num_sms() * 8;
+    if (blocks < 1) blocks = 1;
+    KTimer kt(kFamAux, s, 0.0, 16.0 * (double)total);
+    host_copy_kernel<<<blocks, 256, 0, s>>>(rows, cols, src, lds, dst, ldd);
+    FG_CUDA(cudaGetLastError());
+    return kOk;
+}
+
 int view_in(int slot, const double *h, int rows, int cols, int ld, bool copy, cudaStream_t s,
             DevView *v) {
     if (is_device_ptr(h)) {
@@ -156,6 +214,8 @@ int view_in(int slot, const double *h, int rows, int cols, int ld, bool copy, cu
     v->ld = dld;
     v->staged = true;
     if (copy && rows > 0 && cols > 0) {
+        const void *hd = host_copy_by_kernel() ? mapped_host(h) : nullptr;
+        if (hd) return host_copy_launch(rows, cols, (const double *)hd, ld, v->p, dld, s);
         if (ld == dld)      // one contiguous block: a plain copy
             FG_CUDA(cudaMemcpyAsync(v->p, h, (size_t)dld * cols * sizeof(double), cudaMemcpyHostToDevice, s));
         else
@@ -167,6 +227,8 @@ int view_in(int slot, const double *h, int rows, int cols, int ld, bool copy, cu
 
 int view_out(const DevView &v, double *h, int rows, int cols, int ld, cudaStream_t s) {
     if (!v.staged || rows <= 0 || cols <= 0) return kOk;
+    void *hd = host_copy_by_kernel() ? mapped_host(h) : nullptr;
+    if (hd) return host_copy_launch(rows, cols, v.p, v.ld, (double *)hd, ld, s);
     if (ld == v.ld)
         FG_CUDA(cudaMemcpyAsync(h, v.p, (size_t)v.ld * cols * sizeof(double), cudaMemcpyDeviceToHost, s));
     else

@@ -48,16 +48,15 @@ constexpr int PANEL_RMIN = 32;         // min rows per CTA
 constexpr size_t PANEL_SMEM_MAX = 200 * 1024;
 
 // One exchange slot per CTA and per step parity.  A CTA publishes its pivot
-// candidate (row, pivot key, the row's jb panel entries) and, if it owns
-// panel row jj, that row.  Every word is tagged: (tag << 32) | 32 bits of
-// payload, written with single-copy-atomic 64-bit stores, the tag being the
-// step's sequence number, so a reader polls the words it needs until they
-// carry the step's tag.  No release fence and no flag-then-data round trip:
-// one L2 round trip for the candidates, one for the winning row.
+// candidate (|value|, row, the row's jb panel entries) and, if it owns panel
+// row jj, that row; `seq` is written last with release semantics.
 struct PanelSlot {
-    unsigned long long head[4];              // idx, key low word, key high word, -
-    unsigned long long row[2 * PANEL_NB];    // the candidate row, two halves per entry
-    unsigned long long rowjj[2 * PANEL_NB];  // row jj (its owner only)
+    unsigned long long seq;
+    unsigned long long key;    // pivot key of the candidate (see pivot_key)
+    int idx;
+    int pad;
+    double row[PANEL_NB];
+    double rowjj[PANEL_NB];
 };
 
 struct PanelScratch {
@@ -84,13 +83,12 @@ PanelScratch carve_panel_scratch(void *base) {
     return s;
 }
 
-__device__ __forceinline__ void st_tagged(unsigned long long *p, unsigned tag, unsigned payload) {
-    const unsigned long long v = ((unsigned long long)tag << 32) | payload;
-    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+__device__ __forceinline__ void st_release(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
-__device__ __forceinline__ unsigned long long ld_word(const unsigned long long *p) {
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
     unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
 
@@ -170,9 +168,7 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
 
     for (int jj = 0; jj < jb; ++jj) {
         const int par = jj & 1;
-        // the step's tag: never 0 (the slots start zeroed), different from
-        // every earlier step of this factorisation
-        const unsigned want = (unsigned)(epoch * 128ull + (unsigned long long)jj + 1ull);
+        const unsigned long long want = epoch * 128ull + (unsigned long long)jj + 1ull;
         // -- [A] this CTA's candidate among its rows g >= jj
         unsigned long long k = nbk;
         int i = nbi;
@@ -180,53 +176,40 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
         if (lane == 0) { red_k[warp] = k; red_i[warp] = i; }
         __syncthreads();                                             // B1
         if (warp == 0) {
-            // -- [B] publish the candidate row (and row jj if owned), then the
-            // candidate itself; each word carries the step's tag
+            // -- [B] publish the candidate row (and row jj if owned); the
+            // release store by lane 0 after __syncwarp orders the warp's slot
+            // writes before the sequence number
             k = lane < NW ? red_k[lane] : kKeyNone;
             i = lane < NW ? red_i[lane] : INT_MAX;
             warp_argmax(k, i);
             PanelSlot *mine = &ps.slots[par * PANEL_GMAX + b];
             if (i != INT_MAX)
-                for (int c = lane; c < jb; c += 32) {
-                    const unsigned long long bits =
-                        (unsigned long long)__double_as_longlong(S[c * R + (i - rb)]);
-                    st_tagged(&mine->row[2 * c], want, (unsigned)bits);
-                    st_tagged(&mine->row[2 * c + 1], want, (unsigned)(bits >> 32));
-                }
+                for (int c = lane; c < jb; c += 32) mine->row[c] = S[c * R + (i - rb)];
             if (jj >= rb && jj < re)
-                for (int c = lane; c < jb; c += 32) {
-                    const unsigned long long bits =
-                        (unsigned long long)__double_as_longlong(S[c * R + (jj - rb)]);
-                    st_tagged(&mine->rowjj[2 * c], want, (unsigned)bits);
-                    st_tagged(&mine->rowjj[2 * c + 1], want, (unsigned)(bits >> 32));
-                }
-            if (lane < 3)
-                st_tagged(&mine->head[lane], want,
-                          lane == 0 ? (unsigned)i : lane == 1 ? (unsigned)k : (unsigned)(k >> 32));
+                for (int c = lane; c < jb; c += 32) mine->rowjj[c] = S[c * R + (jj - rb)];
+            if (lane == 0) {
+                mine->key = k;
+                mine->idx = i;
+            }
+            __syncwarp();
+            if (lane == 0) st_release(&mine->seq, want);
         }
-        // -- [C] thread t < G waits for the candidate of slot t of this step:
-        // its three words in flight together, re-read until all carry the tag
+        // -- [C] thread t < G waits for slot t of this step and reads it
         unsigned long long gk = kKeyNone;
         int gi = INT_MAX;
         if (tid < G) {
             const PanelSlot *sl = &ps.slots[par * PANEL_GMAX + tid];
-            unsigned long long v0 = ld_word(&sl->head[0]), v1 = ld_word(&sl->head[1]),
-                               v2 = ld_word(&sl->head[2]);
             unsigned spins = 0;
-            while (((unsigned)(v0 >> 32) != want) | ((unsigned)(v1 >> 32) != want) |
-                   ((unsigned)(v2 >> 32) != want)) {
+            while (ld_acquire(&sl->seq) != want) {
                 if (++spins > kSpinLimit) {
                     atomicOr(status, kDevBarrierTimeout);
                     s_abort = 1;
                     break;
                 }
                 if (spins > 32) __nanosleep(32);
-                v0 = ld_word(&sl->head[0]);
-                v1 = ld_word(&sl->head[1]);
-                v2 = ld_word(&sl->head[2]);
             }
-            gk = ((unsigned long long)(unsigned)v2 << 32) | (unsigned)v1;
-            gi = (int)(unsigned)v0;
+            gk = __ldcg(&sl->key);
+            gi = __ldcg(&sl->idx);
         }
         if (warp * 32 < G) {                                          // warp-uniform
             warp_argmax(gk, gi);
@@ -245,43 +228,9 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
             // cxxblas/level1/iamax.tcc:50-57) and its reciprocal once
             const PanelSlot *sj = &ps.slots[par * PANEL_GMAX + jj / R];
             const PanelSlot *sw = &ps.slots[par * PANEL_GMAX + gi / R];
-            // each lane's words of both rows in flight together (jb <= 64:
-            // at most 4 + 4), re-read until all carry the tag
-            constexpr int WPL = 2 * PANEL_NB / 32;
-            unsigned long long vo[WPL], vp[WPL];
-#pragma unroll
-            for (int u = 0; u < WPL; ++u) {
-                const int w = lane + 32 * u;
-                vo[u] = w < 2 * jb ? ld_word(&sj->rowjj[w]) : ((unsigned long long)want << 32);
-                vp[u] = w < 2 * jb ? ld_word(&sw->row[w]) : ((unsigned long long)want << 32);
-            }
-            unsigned spins = 0;
-            for (;;) {
-                bool all = true;
-#pragma unroll
-                for (int u = 0; u < WPL; ++u)
-                    all &= ((unsigned)(vo[u] >> 32) == want) & ((unsigned)(vp[u] >> 32) == want);
-                if (all) break;
-                if (++spins > kSpinLimit) {
-                    atomicOr(status, kDevBarrierTimeout);
-                    s_abort = 1;
-                    break;
-                }
-                if (spins > 32) __nanosleep(32);
-#pragma unroll
-                for (int u = 0; u < WPL; ++u) {
-                    const int w = lane + 32 * u;
-                    if (w < 2 * jb && (unsigned)(vo[u] >> 32) != want) vo[u] = ld_word(&sj->rowjj[w]);
-                    if (w < 2 * jb && (unsigned)(vp[u] >> 32) != want) vp[u] = ld_word(&sw->row[w]);
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < WPL; ++u) {
-                const int w = lane + 32 * u;
-                if (w < 2 * jb) {
-                    reinterpret_cast<unsigned *>(orow + (w >> 1))[w & 1] = (unsigned)vo[u];
-                    reinterpret_cast<unsigned *>(prow + (w >> 1))[w & 1] = (unsigned)vp[u];
-                }
+            for (int c = lane; c < jb; c += 32) {
+                orow[c] = ld_cg(&sj->rowjj[c]);
+                prow[c] = ld_cg(&sw->row[c]);
             }
             __syncwarp();
             if (lane == 0) {
@@ -298,7 +247,6 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
             }
         }
         __syncthreads();                                             // B3
-        if (s_abort) return;
         const int gs = s_gs;
         const double pv = s_pv, rinv = s_rinv;
         const bool swap = (pv != 0.0) && (gs != jj);
