@@ -605,7 +605,10 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int 
     }
     const int gcap = panel_ctas(sms);
     // look-ahead (CUDA-core updates only: the tensor-core update is a
-    // persistent kernel that leaves no SM free for a concurrent panel)
+    // persistent kernel that leaves no SM free for a concurrent panel; with
+    // its operand ring cut to 3 stages so that a panel CTA fits beside it, the
+    // n = 16384 FP32 LU spent 114 ms in its updates instead of 49 and the
+    // panels did not shorten)
     Workspace *wl = nullptr;
     if (tc_kind < 0 && lookahead_enabled()) {
         wl = workspace_side(stream);
