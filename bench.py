@@ -402,16 +402,19 @@ def our_arm(args, rank: int, world: int) -> None:
 
 
 # (kappa, nrhs, label, precision, solver, max_iter): precision 0 TF32, 1 BF16,
-# 2 FP8 e4m3, 3 FP32-accurate 3xTF32 (all FP32 storage), 4 split (FP64 storage,
-# FP64-accurate split-GEMM trailing updates); solver 0 classical, 1 GMRES-IR,
-# 2 classical switching to GMRES-IR.  The FP8 and the FP32 kappa=1e10 cases
-# are capped: their factors are too inexact a preconditioner at this n, and
-# the lines report where the refinement stands after the cap.
+# 2 FP8 e4m3, 3 FP32-accurate 3xTF32, 5 / 6 FP8 e4m3 with two / three terms
+# per entry (all FP32 storage), 4 split (FP64 storage, FP64-accurate
+# split-GEMM trailing updates); solver 0 classical, 1 GMRES-IR, 2 classical
+# switching to GMRES-IR.  The one- and two-term FP8 and the FP32 kappa=1e10
+# cases are capped: their factors are too inexact a preconditioner at this n,
+# and the lines report where the refinement stands after the cap.
 MIXED_CASES = (
     (1e2, 1, "fp32(3xTF32)", 3, 2, 30),
     (1e2, 1, "tf32", 0, 2, 30),
     (1e2, 1, "bf16", 1, 2, 30),
     (1e2, 1, "fp8", 2, 2, 4),
+    (1e2, 1, "fp8x2", 5, 2, 4),
+    (1e2, 1, "fp8x3", 6, 2, 30),
     (1e2, 1, "split", 4, 2, 30),
     (1e2, 64, "fp32(3xTF32)", 3, 2, 30),
     (1e2, 64, "split", 4, 2, 30),
@@ -652,7 +655,7 @@ def tc_kinds_subbench(torch, fg, dev, n=8192, reps=3):
     TFLOP/s from the library's per-launch CUDA events (the call also converts
     the FP32 operands to the kind's K-major copies, timed separately as aux),
     against the measured dense BF16 peak scaled by the kind's nominal rate
-    (TF32 1/2, FP8 2x; 3xTF32 runs one TF32 product over 3K)."""
+    (TF32 1/2, FP8 2x; 3xTF32 and two-term FP8 run one product over 3K)."""
     import ctypes
     bf16, src = measured_peak("bf16_tflops")
     g = torch.Generator(device=dev)
@@ -668,7 +671,7 @@ def tc_kinds_subbench(torch, fg, dev, n=8192, reps=3):
     out = {"workload": f"sgemm_tc {n}^3, FP32 in/out, tcgen05 kernel only", "kinds": {},
            "bf16_peak_tflops": {"value": bf16, "source": f"{src} (MEASURED_PEAKS.json bf16_tflops)"}}
     for prec, name, rate in ((0, "tf32", 0.5), (1, "bf16", 1.0), (2, "fp8_e4m3", 2.0),
-                             (3, "3xtf32", 0.5)):
+                             (3, "3xtf32", 0.5), (5, "fp8x2_e4m3", 2.0), (6, "fp8x3_e4m3", 2.0)):
         st = f(prec, b"N", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0,
                C.data_ptr(), n, sp)
         if st != 0:

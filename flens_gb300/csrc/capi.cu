@@ -1294,6 +1294,17 @@ FG_API int flens_gb300_dgetrf_split(int m, int n, double *A, int ldA, int *ipiv,
     return dgetrf_split_launch(m, n, A, ldA, ipiv, info, outer_nb, as_stream(stream));
 }
 
+// LU of an FP32 matrix with tensor-core (or, precision -1, CUDA-core)
+// trailing updates: the factorisation of flens_gb300_dgesv_mixed.
+FG_API int flens_gb300_sgetrf_tc(int precision, int m, int n, float *A, int ldA, int *ipiv, int *info,
+                                 void *stream) {
+    if (precision < -1 || precision > 6 || precision == 4) return -1;
+    if (m < 0) return -2;
+    if (n < 0) return -3;
+    if (ldA < std::max(1, m)) return -5;
+    return sgetrf_launch(m, n, A, ldA, ipiv, info, precision, as_stream(stream));
+}
+
 FG_API int flens_gb300_dgetrs(char trans, int n, int nrhs, const double *A, int ldA,
                               const int *ipiv, double *B, int ldB, void *stream) {
     trans = (char)toupper(trans);

@@ -68,8 +68,10 @@ struct SlabLoader {
 };
 
 // ---------------------------------------------------------------- DFMA ----
-// 64x64 CTA tile, 256 threads as 16x16, each thread a 4x4 sub-tile strided by
-// 16 so shared-memory reads are conflict-free broadcasts.  TRI restricts the
+// TM x TN CTA tile (64x64, or 32x32 for launches of few tiles), 256 threads as
+// 16x16, each thread a (TM/16)x(TN/16) sub-tile strided by 16 so shared-memory
+// reads are conflict-free broadcasts.  Every element is summed over k in the
+// same order whatever the tile, so both tiles give the same bits.  TRI restricts the
 // update to one triangle of a square C (syrk): 1 = lower (i >= j), 2 = upper
 // (i <= j); tiles wholly outside it exit at once and diagonal tiles store only
 // their part, so the other triangle of C is never written.
@@ -77,31 +79,32 @@ struct SlabLoader {
 // nonzero (the skipped terms are exact zeros): 1 op(A) upper (k >= row),
 // 2 op(A) lower (k <= row), 3 op(B) upper (k <= column), 4 op(B) lower
 // (k >= column).
-template <typename T, bool TA, bool TB, int TRI = 0, int KR = 0>
+template <typename T, bool TA, bool TB, int TRI = 0, int KR = 0, int TM = BM, int TN = BN>
 __global__ void __launch_bounds__(256)
 dgemm_fma_kernel(int m, int n, int k, T alpha,
                  const T *__restrict__ A, int ldA,
                  const T *__restrict__ B, int ldB,
                  T beta, T *__restrict__ C, int ldC) {
-    __shared__ T As[2][BK][BM + PAD];
-    __shared__ T Bs[2][BK][BN + PAD];
+    constexpr int RI = TM / 16, RJ = TN / 16;
+    __shared__ T As[2][BK][TM + PAD];
+    __shared__ T Bs[2][BK][TN + PAD];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
-    if (TRI == 1 && m0 + BM <= n0) return;       // tile strictly above the diagonal
-    if (TRI == 2 && n0 + BN <= m0) return;       // tile strictly below the diagonal
+    const int m0 = blockIdx.x * TM, n0 = blockIdx.y * TN;
+    if (TRI == 1 && m0 + TM <= n0) return;       // tile strictly above the diagonal
+    if (TRI == 2 && n0 + TN <= m0) return;       // tile strictly below the diagonal
 
-    SlabLoader<T, !TA, BM, 256> la;
-    SlabLoader<T, TB, BN, 256> lb;
-    T acc[4][4];
+    SlabLoader<T, !TA, TM, 256> la;
+    SlabLoader<T, TB, TN, 256> lb;
+    T acc[RI][RJ];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < RI; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+        for (int j = 0; j < RJ; ++j) acc[i][j] = T(0);
 
     int kb0 = 0, nk = (k + BK - 1) / BK;
     if (KR == 1) kb0 = m0 / BK;
-    if (KR == 2) nk = min(nk, (m0 + BM + BK - 1) / BK);
-    if (KR == 3) nk = min(nk, (n0 + BN + BK - 1) / BK);
+    if (KR == 2) nk = min(nk, (m0 + TM + BK - 1) / BK);
+    if (KR == 3) nk = min(nk, (n0 + TN + BK - 1) / BK);
     if (KR == 4) kb0 = n0 / BK;
     if (kb0 < nk) {
         la.fetch(A, ldA, m0, m, kb0 * BK, k);
@@ -118,15 +121,15 @@ dgemm_fma_kernel(int m, int n, int k, T alpha,
         }
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
-            T a[4], b[4];
+            T a[RI], b[RJ];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = As[cur][kk][tx + 16 * i];
+            for (int i = 0; i < RI; ++i) a[i] = As[cur][kk][tx + 16 * i];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = Bs[cur][kk][ty + 16 * j];
+            for (int j = 0; j < RJ; ++j) b[j] = Bs[cur][kk][ty + 16 * j];
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < RI; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+                for (int j = 0; j < RJ; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
         }
         if (kt + 1 < nk) {
             la.store(As[cur ^ 1]);
@@ -139,11 +142,11 @@ dgemm_fma_kernel(int m, int n, int k, T alpha,
     // element on a pipe that bounds the kernel
     const bool beta1 = beta == T(1);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < RJ; ++j) {
         const int gj = n0 + ty + 16 * j;
         if (gj >= n) continue;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < RI; ++i) {
             const int gi = m0 + tx + 16 * i;
             if (gi >= m) continue;
             if (TRI == 1 && gi < gj) continue;
@@ -508,6 +511,18 @@ int gemm_launch_t(char transA, char transB, int m, int n, int k, T alpha, const 
         else if (ta && !tb) dgemm_dmma_kernel<true, false><<<grid, 128, 0, stream>>>(m, n, k, al, Ad, ldA, Bd, ldB, be, Cd, ldC);
         else if (!ta && tb) dgemm_dmma_kernel<false, true><<<grid, 128, 0, stream>>>(m, n, k, al, Ad, ldA, Bd, ldB, be, Cd, ldC);
         else dgemm_dmma_kernel<true, true><<<grid, 128, 0, stream>>>(m, n, k, al, Ad, ldA, Bd, ldB, be, Cd, ldC);
+    } else if ((long long)grid.x * grid.y < 4LL * num_sms()) {
+        // few 64x64 tiles (the look-ahead update of the next panel's columns,
+        // the last trailing updates): a 64x64x64 tile alone on an SM takes
+        // 131k clocks of its FP64 pipe, so 32x32 tiles spread the same work
+        // over four times as many SMs
+        const dim3 g32(ceil_div(m, 32), ceil_div(n, 32));
+#define FG_F32T(TA_, TB_) dgemm_fma_kernel<T, TA_, TB_, 0, 0, 32, 32><<<g32, 256, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC)
+        if (!ta && !tb) FG_F32T(false, false);
+        else if (ta && !tb) FG_F32T(true, false);
+        else if (!ta && tb) FG_F32T(false, true);
+        else FG_F32T(true, true);
+#undef FG_F32T
     } else {
         if (!ta && !tb) dgemm_fma_kernel<T, false, false><<<grid, 256, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
         else if (ta && !tb) dgemm_fma_kernel<T, true, false><<<grid, 256, 0, stream>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);

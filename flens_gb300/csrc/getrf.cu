@@ -149,6 +149,8 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
     const int rb = b * R;
     const int re = min(mp, rb + R);
     const int nr = max(0, re - rb);
+    // lanes per row in the update: 8, 4 or 2 while nr * W fits the CTA
+    const int W = nr <= 32 ? 8 : nr <= 64 ? 4 : nr <= 128 ? 2 : 1;
 
     for (int e = tid; e < nr * jb; e += PANEL_THREADS) {
         const int r = e % nr, c = e / nr;
@@ -256,6 +258,43 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
         // columns > jj, and the pivot key for column jj+1
         nbk = kKeyNone;
         nbi = INT_MAX;
+        if (W > 1) {
+            // W lanes per row (nr * W <= 256: one row per lane group), lane q
+            // of the group taking columns q, q + W, ...: the chain of
+            // dependent shared-memory updates per thread is W times shorter.
+            // The group's first lane reads the multiplier and broadcasts it
+            // (all 32 lanes of every warp take part in the shuffle).
+            const int r = tid / W, q = tid % W;
+            const bool act = r < nr;
+            const int g = rb + r;
+            const bool to_jj = act && swap && g == jj, from_gs = act && swap && g == gs;
+            double l0 = 0.0;
+            if (act && q == 0) l0 = from_gs ? orow[jj] : S[jj * R + r];
+            double l = __shfl_sync(0xffffffffu, l0, lane & ~(W - 1));
+            if (to_jj) {
+                for (int c = q; c < jb; c += W) S[c * R + r] = P[c];
+            } else if (act && g > jj) {
+                if (from_gs)
+                    for (int c = q; c < jj; c += W) S[c * R + r] = orow[c];
+                if (pv != 0.0) l = (rinv != 0.0) ? l * rinv : l / pv;
+                if (q == 0 && (pv != 0.0 || from_gs)) S[jj * R + r] = l;
+                const double *old = from_gs ? orow : nullptr;
+                int c = jj + 1 + q;
+                for (; c + 3 * W < jb; c += 4 * W) {
+                    double v[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) v[u] = old ? old[c + u * W] : S[(c + u * W) * R + r];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) S[(c + u * W) * R + r] = fma(-P[c + u * W], l, v[u]);
+                }
+                for (; c < jb; c += W) S[c * R + r] = fma(-P[c], l, old ? old[c] : S[c * R + r]);
+                if (q == 0 && jj + 1 < jb) {
+                    const unsigned long long key = pivot_key(S[(jj + 1) * R + r]);
+                    nbk = key;
+                    nbi = g;
+                }
+            }
+        } else
         for (int r = tid; r < nr; r += PANEL_THREADS) {
             const int g = rb + r;
             if (swap && g == jj) {
@@ -809,7 +848,7 @@ int sgetrs_launch(char trans, int n, int nrhs, const float *A, int ldA, const in
 //    the GPU (different streams, or different host threads) race on it and
 //    must be serialised by the caller;
 //  * the first call on a device looks the array's device address up
-//    (cudaGetSymbolAddress) -- make that first call before any stream capture.
+//    (cudaGetSymbolAddress); use inside a captured CUDA graph is not tested.
 // The array keeps the last call's contents.  What must start at zero is
 // cleared on the call's stream by each call (cudaMemsetAsync, which does not
 // allocate): the chain flags before every chained solve, and the status

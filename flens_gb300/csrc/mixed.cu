@@ -4,7 +4,9 @@
 //   1. A32 = fp32(A); LU of A32 with partial pivoting (sgetrf_launch): the
 //      panel's pivot search and scaling run in FP64 on FP32 storage, the
 //      trailing updates A22 -= A21*U12 on the tensor cores in TF32, BF16,
-//      FP8 e4m3 (per-row/column scaled) or FP32-accurate 3xTF32.
+//      FP8 e4m3 (per-row/column scaled), FP32-accurate 3xTF32, or FP8 e4m3
+//      with each scaled entry split into two or three e4m3 terms (precision
+//      5 / 6: about 2^-8 / 2^-12 relative products from the FP8 kind).
 //   2. x0 = U^-1 L^-1 P b in FP32 (b scaled per column into FP32 range).
 //   3. Refinement; everything that decides accuracy is FP64:
 //        r = b - A x (FP64 GEMM/GEMV on the original A),
@@ -983,7 +985,7 @@ FG_API int flens_gb300_dgesv_mixed(int n, int nrhs, const double *A, int ldA, co
     if (ldA < (n > 1 ? n : 1)) return -4;
     if (ldB < (n > 1 ? n : 1)) return -6;
     if (ldX < (n > 1 ? n : 1)) return -8;
-    if (precision < 0 || precision > 4) return -9;
+    if (precision < 0 || precision > 6) return -9;
     if (solver < 0 || solver > 2) return -10;
     int it = 0, inf = 0;
     double be = 0.0;

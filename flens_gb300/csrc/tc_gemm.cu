@@ -92,6 +92,28 @@ template <>
 __device__ __forceinline__ void store_lp<kTcFP8>(void *out, size_t idx, float v) {
     ((__nv_fp8_storage_t *)out)[idx] = __nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
 }
+// the terms of the e4m3 splits: t0 = e4m3(v), t1 = e4m3(v - t0),
+// t2 = e4m3(v - t0 - t1).  Each difference is exact in FP32: a term has 4
+// significant bits and is within half an e4m3 step of what it rounds.
+__device__ __forceinline__ float fp8_round(float v, __nv_fp8_storage_t *q) {
+    *q = __nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
+    return __half2float(__half(__nv_cvt_fp8_to_halfraw(*q, __NV_E4M3)));
+}
+template <>
+__device__ __forceinline__ void store_lp<kTcFP8Lo>(void *out, size_t idx, float v) {
+    __nv_fp8_storage_t q;
+    const float t0 = fp8_round(v, &q);
+    fp8_round(v - t0, &q);
+    ((__nv_fp8_storage_t *)out)[idx] = q;
+}
+template <>
+__device__ __forceinline__ void store_lp<kTcFP8Lo2>(void *out, size_t idx, float v) {
+    __nv_fp8_storage_t q;
+    const float t0 = fp8_round(v, &q);
+    const float t1 = fp8_round(v - t0, &q);
+    fp8_round(v - t0 - t1, &q);
+    ((__nv_fp8_storage_t *)out)[idx] = q;
+}
 
 template <int KIND, bool RCONTIG>
 __global__ void __launch_bounds__(256)
@@ -203,7 +225,11 @@ int make_kmajor_map(CUtensorMap *map, int kind, const void *base, int rows, int 
 }  // namespace tc
 
 // K-major leading dimension (elements) for `kind`: K rounded up to 16 bytes.
-static int gemm_kind(int kind) { return (kind == kTcF32x3 || kind == kTcTF32Lo) ? kTcTF32 : kind; }
+static int gemm_kind(int kind) {
+    if (kind == kTcF32x3 || kind == kTcTF32Lo) return kTcTF32;
+    if (kind == kTcFP8x2 || kind == kTcFP8x3 || kind == kTcFP8Lo || kind == kTcFP8Lo2) return kTcFP8;
+    return kind;
+}
 
 int tc_kmajor_ld(int kind, int K) {
     kind = gemm_kind(kind);
@@ -218,7 +244,8 @@ size_t tc_elem_bytes(int kind) {
 
 // Convert op(X) (R x K, FP32, column-major storage, transposed or not) to a
 // K-major low-precision operand: columns 0..width-1 of rows of stride ldo
-// (zero beyond K).  For FP8, also computes per-row scales.
+// (zero beyond K).  For FP8, scales each row by inv_scale; when `scale` is
+// given, first computes the per-row scales (else inv_scale holds them already).
 int tc_convert(int kind, bool trans, int R, int K, const float *X, int ldx, void *out, int ldo,
                float *scale, float *inv_scale, cudaStream_t stream, int width = -1) {
     if (width < 0) width = ldo;
@@ -226,14 +253,15 @@ int tc_convert(int kind, bool trans, int R, int K, const float *X, int ldx, void
     KTimer kt(kFamAux, stream, 0.0, (4.0 + tc_elem_bytes(kind)) * R * (double)K);
     // op(X)(r, k): r-contiguous when X is stored R x K (no transpose)
     const bool rcontig = !trans;
-    if (kind == kTcFP8) {
+    const bool fp8 = kind == kTcFP8 || kind == kTcFP8Lo || kind == kTcFP8Lo2;
+    if (fp8 && scale != nullptr) {
         const dim3 g(ceil_div(R, 8));
         if (rcontig) row_scale_kernel<true><<<g, 256, 0, stream>>>(R, K, X, ldx, scale, inv_scale);
         else row_scale_kernel<false><<<g, 256, 0, stream>>>(R, K, X, ldx, scale, inv_scale);
         FG_CUDA(cudaGetLastError());
     }
     const dim3 grid(ceil_div(R, 32), ceil_div(width, 32));
-    const float *inv = kind == kTcFP8 ? inv_scale : nullptr;
+    const float *inv = fp8 ? inv_scale : nullptr;
 #define FG_CONV(KD)                                                                          \
     do {                                                                                     \
         if (rcontig) to_kmajor_kernel<KD, true><<<grid, 256, 0, stream>>>(R, K, X, ldx, out, ldo, width, inv); \
@@ -242,6 +270,8 @@ int tc_convert(int kind, bool trans, int R, int K, const float *X, int ldx, void
     if (kind == kTcTF32) FG_CONV(kTcTF32);
     else if (kind == kTcTF32Lo) FG_CONV(kTcTF32Lo);
     else if (kind == kTcBF16) FG_CONV(kTcBF16);
+    else if (kind == kTcFP8Lo) FG_CONV(kTcFP8Lo);
+    else if (kind == kTcFP8Lo2) FG_CONV(kTcFP8Lo2);
     else FG_CONV(kTcFP8);
 #undef FG_CONV
     FG_CUDA(cudaGetLastError());
@@ -291,11 +321,13 @@ static size_t round256(size_t b) { return (b + 255) / 256 * 256; }
 
 size_t tc_update_workspace_bytes(int kind, int m, int n, int k) {
     int ld = tc_kmajor_ld(kind, k);
-    if (kind == kTcF32x3) ld *= 3;                 // three K segments, see f32x3_gemm
+    if (kind == kTcF32x3 || kind == kTcFP8x2) ld *= 3;   // three K segments, see f32x3_gemm
+    if (kind == kTcFP8x3) ld *= 6;                       // six, see fp8_terms_gemm
     const size_t eb = tc_elem_bytes(kind);
     const size_t a = round256((size_t)m * ld * eb), b = round256((size_t)n * ld * eb);
     size_t total = a + b;
-    if (kind == kTcFP8) total += round256((size_t)(m + n) * 2 * sizeof(float));
+    if (kind == kTcFP8 || kind == kTcFP8x2 || kind == kTcFP8x3)
+        total += round256((size_t)(m + n) * 2 * sizeof(float));
     return total;
 }
 
@@ -320,6 +352,41 @@ int f32x3_gemm(bool ta_rows, bool tb_rows, int m, int n, int k, float alpha, con
     return tc_gemm_launch(kTcTF32, m, n, ld3, alpha, Ak, ld3, Bk, ld3, beta, C, ldC, nullptr, nullptr, s);
 }
 
+// The same segmented product in e4m3: op(A) row i is scaled by 1/sa_i
+// (sa_i = amax/448 over its K entries) and op(B)^T row j by 1/sb_j; each
+// scaled entry is split into `nterms` e4m3 terms t0 + t1 (+ t2), and the
+// operands are laid out along K' = nseg kp so that segment q multiplies
+// term ta[q] of op(A) by term tb[q] of op(B): for two terms t1*t0, t0*t1,
+// t0*t0; for three terms t2*t0, t0*t2, t1*t1, t1*t0, t0*t1, t0*t0 (small
+// terms first).  One FP32 accumulator sums them and the epilogue multiplies
+// by sa_i sb_j, so C is read and written once.
+int fp8_terms_gemm(int nterms, bool ta_rows, bool tb_rows, int m, int n, int k, float alpha,
+                   const float *A, int ldA, const float *B, int ldB, float beta, float *C, int ldC,
+                   void *buf, cudaStream_t s) {
+    static const int ta2[] = {1, 0, 0}, tb2[] = {0, 1, 0};
+    static const int ta3[] = {2, 0, 1, 1, 0, 0}, tb3[] = {0, 2, 1, 0, 1, 0};
+    static const int conv[] = {kTcFP8, kTcFP8Lo, kTcFP8Lo2};
+    const int nseg = nterms == 3 ? 6 : 3;
+    const int *tA = nterms == 3 ? ta3 : ta2, *tB = nterms == 3 ? tb3 : tb2;
+    const int kp = tc_kmajor_ld(kTcFP8, k), ldw = nseg * kp;
+    const size_t a = round256((size_t)m * ldw), b = round256((size_t)n * ldw);
+    uint8_t *Ak = (uint8_t *)buf, *Bk = (uint8_t *)buf + a;
+    float *sa = (float *)((char *)buf + a + b), *sia = sa + m, *sb = sia + m, *sib = sb + n;
+    int st;
+    // the last segment holds t0 of both operands: its conversion computes the
+    // per-row scales, which every other segment then uses
+    const int q0 = nseg - 1;
+    if ((st = tc_convert(kTcFP8, ta_rows, m, k, A, ldA, Ak + q0 * kp, ldw, sa, sia, s, kp))) return st;
+    if ((st = tc_convert(kTcFP8, tb_rows, n, k, B, ldB, Bk + q0 * kp, ldw, sb, sib, s, kp))) return st;
+    for (int q = 0; q < q0; ++q) {
+        if ((st = tc_convert(conv[tA[q]], ta_rows, m, k, A, ldA, Ak + q * kp, ldw, nullptr, sia, s, kp)))
+            return st;
+        if ((st = tc_convert(conv[tB[q]], tb_rows, n, k, B, ldB, Bk + q * kp, ldw, nullptr, sib, s, kp)))
+            return st;
+    }
+    return tc_gemm_launch(kTcFP8, m, n, ldw, alpha, Ak, ldw, Bk, ldw, beta, C, ldC, sa, sb, s);
+}
+
 }  // namespace
 
 int tc_trailing_update(int kind, int m, int n, int k, const float *A21, int ldA21,
@@ -334,6 +401,9 @@ int tc_trailing_update(int kind, int m, int n, int k, const float *A21, int ldA2
     int st;
     if (kind == kTcF32x3)
         return f32x3_gemm(false, true, m, n, k, -1.0f, A21, ldA21, U12, ldU12, 1.0f, A22, ldA22, buf, stream);
+    if (kind == kTcFP8x2 || kind == kTcFP8x3)
+        return fp8_terms_gemm(kind == kTcFP8x3 ? 3 : 2, false, true, m, n, k, -1.0f, A21, ldA21, U12,
+                              ldU12, 1.0f, A22, ldA22, buf, stream);
     float *sa = nullptr, *sia = nullptr, *sb = nullptr, *sib = nullptr;
     if (kind == kTcFP8) {
         sa = (float *)(p + a + b);
@@ -351,13 +421,14 @@ int tc_trailing_update(int kind, int m, int n, int k, const float *A21, int ldA2
 // ----------------------------------------------------------------- C ABI ----
 // C = alpha*op(A)*op(B) + beta*C with FP32 operands in device memory, the
 // products taken on the tensor cores in `precision` (0 = TF32, 1 = BF16,
-// 2 = FP8 e4m3 with per-row/per-column scaling, 3 = FP32-accurate 3xTF32) and
-// accumulated in FP32.
+// 2 = FP8 e4m3 with per-row/per-column scaling, 3 = FP32-accurate 3xTF32,
+// 5 / 6 = two- / three-term e4m3 with the same scaling) and accumulated in
+// FP32.
 FG_API int flens_gb300_sgemm_tc(int precision, char transA, char transB, int m, int n, int k,
                                 float alpha, const float *A, int ldA, const float *B, int ldB,
                                 float beta, float *C, int ldC, void *stream) {
     using namespace fg;
-    if (precision < 0 || precision > 3) return -1;
+    if (precision < 0 || precision > 6 || precision == 4) return -1;
     const bool ta = !(transA == 'N' || transA == 'n');
     const bool tb = !(transB == 'N' || transB == 'n');
     if (!(transA == 'N' || transA == 'n' || transA == 'T' || transA == 't' || transA == 'C' || transA == 'c')) return -2;
@@ -391,6 +462,9 @@ FG_API int flens_gb300_sgemm_tc(int precision, char transA, char transB, int m, 
     int st;
     if (precision == kTcF32x3)
         return f32x3_gemm(ta, !tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, p, s);
+    if (precision == kTcFP8x2 || precision == kTcFP8x3)
+        return fp8_terms_gemm(precision == kTcFP8x3 ? 3 : 2, ta, !tb, m, n, k, alpha, A, ldA, B, ldB,
+                              beta, C, ldC, p, s);
     void *Alp = p, *Blp = p + a;
     float *sa = nullptr, *sia = nullptr, *sb = nullptr, *sib = nullptr;
     if (precision == kTcFP8) {

@@ -32,9 +32,23 @@ namespace fg {
 
 // Precisions of the tensor-core contraction.  kTcF32x3 is FP32-accurate: each
 // operand is split into a TF32 head and a TF32 tail and three TF32 products
-// (head*head + head*tail + tail*head) are accumulated.  kTcTF32Lo is only a
-// conversion mode (the tail of the split).
-enum TcKind : int { kTcTF32 = 0, kTcBF16 = 1, kTcFP8 = 2, kTcF32x3 = 3, kTcTF32Lo = 4 };
+// (head*head + head*tail + tail*head) are accumulated.  kTcFP8x2 and kTcFP8x3
+// do the same with e4m3: a scaled operand v is stored as t0 = e4m3(v),
+// t1 = e4m3(v - t0) (and t2 = e4m3(v - t0 - t1)), and the products t_i t_j
+// with i + j <= 1 (3 of them) or <= 2 (6 of them) are accumulated: about
+// 2^-8 or 2^-12 relative per operand entry instead of e4m3's 2^-4.
+// kTcTF32Lo, kTcFP8Lo (t1) and kTcFP8Lo2 (t2) are only conversion modes.
+enum TcKind : int {
+    kTcTF32 = 0,
+    kTcBF16 = 1,
+    kTcFP8 = 2,
+    kTcF32x3 = 3,
+    kTcTF32Lo = 4,
+    kTcFP8x2 = 5,
+    kTcFP8x3 = 6,
+    kTcFP8Lo = 7,
+    kTcFP8Lo2 = 8
+};
 
 namespace tc {
 

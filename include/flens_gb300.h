@@ -297,14 +297,28 @@ int flens_gb300_dposv(char uplo, int n, int nrhs, double *A, int ldA,
 
 /* C <- alpha*op(A)*op(B) + beta*C, FP32 operands in device memory, products
  * on the tcgen05 tensor cores in `precision` (0 = TF32, 1 = BF16, 2 = FP8
- * e4m3 with per-row / per-column scaling, 3 = FP32-accurate 3xTF32) with FP32
- * accumulation.  Beta scales C by a multiply, as cxxblas gescal does.  No
+ * e4m3 with per-row / per-column scaling, 3 = FP32-accurate 3xTF32, 5 and 6 =
+ * FP8 e4m3 as above with each scaled entry split into two or three e4m3
+ * terms t0 + t1 (+ t2) and the products t_i t_j with i + j <= 1 or <= 2
+ * taken, about 2^-8 or 2^-12 relative per entry; 4 is not a product
+ * precision and returns -1) with FP32 accumulation.  Beta scales C by a multiply, as cxxblas gescal does.  No
  * reference counterpart: FLENS's float gemm is the generic loop
  * (cxxblas/level3/gemm.tcc:42-190).  Async on stream. */
 int flens_gb300_sgemm_tc(int precision, char transA, char transB, int m, int n,
                          int k, float alpha, const float *A, int ldA,
                          const float *B, int ldB, float beta, float *C, int ldC,
                          void *stream);
+
+/* LU with partial pivoting of an m x n FP32 matrix in device memory (column-
+ * major, 1-based pivots), the factorisation of the precision form: panels
+ * in FP64 arithmetic on the FP32 storage (pivot search and scaling as in
+ * flens_gb300_dgetrf), U12 = L11^-1 A12 in FP32, and the trailing updates
+ * A22 -= L21 U12 on the tensor cores in `precision` (0, 1, 2, 3, 5 or 6 as
+ * for flens_gb300_sgemm_tc) or, for precision -1, on the CUDA cores in
+ * FP32.  *info (device) as dgetrf's.  The counterpart of FLENS's float trf
+ * (flens/lapack/ge/trf.tcc:59-152).  Async on stream. */
+int flens_gb300_sgetrf_tc(int precision, int m, int n, float *A, int ldA,
+                          int *ipiv, int *info, void *stream);
 
 /* FP64-accurate C <- beta*C + alpha*op(A)*op(B) on device memory without FP64
  * arithmetic units: every row of op(A) / column of op(B) is scaled by a power
@@ -327,7 +341,7 @@ int flens_gb300_dgemm_split(char transA, char transB, int m, int n, int k,
 
 /* Solve A X = B (device, column-major FP64; A and B untouched) to FP64
  * accuracy from an LU in FP32 storage whose trailing updates run on the
- * tensor cores in `precision` (as above), or, for precision 4, from the
+ * tensor cores in `precision` (0, 1, 2, 3, 5 or 6 as above), or, for precision 4, from the
  * FP64-accurate flens_gb300_dgetrf_split factors (FP64 storage and solves;
  * for systems too ill-conditioned for FP32 factors, kappa*u32 >> 1),
  * refined in FP64: solver 0 =
@@ -403,8 +417,8 @@ int flens_gb300_batched_panel(void *plan, int bucket);
  * FLENS_GB300_ERR_UNSUPPORTED with a message.  Each call clears the parts
  * that must start at zero on its own stream.  All calls share that array:
  * calls that overlap on the GPU race, so serialise them.  The first call on a
- * device looks up the array's address; make it before any stream capture.
- * Async on stream. */
+ * device looks up the array's address (cudaGetSymbolAddress).  Use inside a
+ * captured CUDA graph is not tested.  Async on stream. */
 int flens_gb300_dgetrs_noalloc(char trans, int n, int nrhs, const double *A,
                                int ldA, const int *ipiv, double *B, int ldB,
                                void *stream);

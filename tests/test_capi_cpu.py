@@ -288,6 +288,38 @@ def test_device_api_argument_errors(flib):
     assert flib.flens_gb300_dgetrf_split(4, 4, None, 4, None, None, -64, None) == -7
 
 
+@pytest.mark.parametrize("prec,want", [(-1, -1), (4, -1), (7, -1)])
+def test_sgemm_tc_precision_codes(flib, prec, want):
+    # 0-3, 5 and 6 (two- and three-term e4m3) are product precisions; 4 names
+    # the split LU of the mixed solve and is rejected here, before any CUDA call
+    f = flib.flens_gb300_sgemm_tc
+    f.argtypes = [ctypes.c_int, ctypes.c_char, ctypes.c_char] + [ctypes.c_int] * 3 + [
+        ctypes.c_float, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+        ctypes.c_float, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    assert f(prec, b"N", b"N", 4, 4, 4, 1.0, None, 4, None, 4, 0.0, None, 4, None) == want
+    assert f(5, b"X", b"N", 4, 4, 4, 1.0, None, 4, None, 4, 0.0, None, 4, None) == -2
+
+
+def test_dgesv_mixed_precision_codes(flib):
+    f = flib.flens_gb300_dgesv_mixed
+    f.argtypes = [ctypes.c_int] * 2 + [ctypes.c_void_p, ctypes.c_int] * 3 + [ctypes.c_int] * 3 + [
+        ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    assert f(4, 1, None, 4, None, 4, None, 4, 7, 2, 0, 0.0, None, None, None, None) == -9
+    assert f(4, 1, None, 4, None, 4, None, 4, -1, 2, 0, 0.0, None, None, None, None) == -9
+    assert f(4, 1, None, 4, None, 4, None, 4, 5, 3, 0, 0.0, None, None, None, None) == -10
+
+
+def test_sgetrf_tc_argument_errors(flib):
+    f = flib.flens_gb300_sgetrf_tc
+    f.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3
+    assert f(4, 4, 4, None, 4, None, None, None) == -1
+    assert f(-2, 4, 4, None, 4, None, None, None) == -1
+    assert f(7, 4, 4, None, 4, None, None, None) == -1
+    assert f(6, -1, 4, None, 4, None, None, None) == -2
+    assert f(6, 4, -1, None, 4, None, None, None) == -3
+    assert f(-1, 4, 4, None, 3, None, None, None) == -5
+
+
 def test_no_gpu_fails_loudly():
     import torch
     if torch.cuda.is_available():

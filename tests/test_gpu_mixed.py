@@ -19,7 +19,7 @@ import flens_gb300 as fg
 pytestmark = pytest.mark.gpu
 
 EPS = np.finfo(np.float64).eps
-PREC = {"tf32": 0, "bf16": 1, "fp8": 2, "fp32": 3, "split": 4}
+PREC = {"tf32": 0, "bf16": 1, "fp8": 2, "fp32": 3, "split": 4, "fp8x2": 5, "fp8x3": 6}
 SOLVER = {"classical": 0, "gmres": 1, "auto": 2}
 
 
@@ -61,7 +61,7 @@ def backward_error(A, X, b):
     return (r.abs().amax(0) / (anorm * X.abs().amax(0) + b.abs().amax(0))).max().item()
 
 
-@pytest.mark.parametrize("prec", ["fp32", "tf32", "bf16", "fp8"])
+@pytest.mark.parametrize("prec", ["fp32", "tf32", "bf16", "fp8", "fp8x2", "fp8x3"])
 @pytest.mark.parametrize("nrhs", [1, 3])
 def test_mixed_well_conditioned(cuda, prec, nrhs):
     n, kappa = 512, 1e2
@@ -162,3 +162,104 @@ def test_mixed_gmres_ill_conditioned_partial_block(cuda):
     st, X, it, be, inf = dgesv_mixed(A, b, "fp32", "gmres", max_iter=10)
     assert st == 0, (st, fg.last_error(), it, be)
     assert backward_error(A, X, b) <= 10 * n * EPS
+
+
+def _emulated_lu_error(A64, prec, nb=64):
+    """||PA - LU||_F / ||A||_F of a torch emulation of the same factorisation
+    (CPU, FP64 arithmetic on FP32 storage): panels in FP64, U12 by an FP64
+    triangular solve, trailing updates from the operands rounded as the
+    tensor-core kind rounds them (e4m3 terms of the per-row / per-column
+    scaled entries)."""
+    import torch
+    pairs = {"fp8x2": [(0, 0), (0, 1), (1, 0)],
+             "fp8x3": [(0, 0), (0, 1), (1, 0), (0, 2), (2, 0), (1, 1)]}[prec]
+    nt = 2 if prec == "fp8x2" else 3
+
+    def terms(x):
+        amax = x.abs().amax(dim=1, keepdim=True)
+        s = torch.where(amax > 0, amax / 448.0, torch.ones_like(amax))
+        r, out = x * (1.0 / s), []
+        for _ in range(nt):
+            t = r.to(torch.float8_e4m3fn).to(torch.float32)
+            out.append(t.double())
+            r = r - t
+        return s.double(), out
+
+    A = A64.to(torch.float32).clone()
+    n = A.shape[0]
+    perm = torch.arange(n)
+    for j in range(0, n, nb):
+        jb = min(nb, n - j)
+        P = A[j:, j:j + jb].double()
+        for c in range(jb):
+            p = int(torch.argmax(P[c:, c].abs())) + c
+            if p != c:
+                P[[c, p]] = P[[p, c]]
+                for sl in (slice(0, j), slice(j + jb, n)):
+                    A[[j + c, j + p], sl] = A[[j + p, j + c], sl]
+                perm[[j + c, j + p]] = perm[[j + p, j + c]]
+            P[c + 1:, c] /= P[c, c]
+            P[c + 1:, c + 1:] -= torch.outer(P[c + 1:, c], P[c, c + 1:])
+        A[j:, j:j + jb] = P.to(torch.float32)
+        if j + jb < n:
+            L11 = torch.tril(A[j:j + jb, j:j + jb].double(), -1) + torch.eye(jb, dtype=torch.float64)
+            A[j:j + jb, j + jb:] = torch.linalg.solve_triangular(
+                L11, A[j:j + jb, j + jb:].double(), upper=False, unitriangular=True).to(torch.float32)
+            sa, ta = terms(A[j + jb:, j:j + jb].contiguous())
+            sb, tb = terms(A[j:j + jb, j + jb:].t().contiguous())
+            upd = sa * sum(ta[i] @ tb[k].t() for i, k in pairs) * sb.t()
+            A[j + jb:, j + jb:] = (A[j + jb:, j + jb:].double() - upd).to(torch.float32)
+    L = torch.tril(A.double(), -1) + torch.eye(n, dtype=torch.float64)
+    return float((A64[perm] - L @ torch.triu(A.double())).norm() / A64.norm())
+
+
+def test_sgetrf_tc_factor_error_per_precision(cuda):
+    """flens_gb300_sgetrf_tc on the mixed-solve matrix family (n = 512,
+    kappa = 1e2): ||PA - LU||_F / ||A||_F per trailing-update precision.  The
+    split e4m3 forms must match a torch emulation of the same factorisation
+    to 25% (the GPU's U12 solve is FP32, the emulation's FP64), and the
+    precisions must order as their unit roundoffs do: FP32 (CUDA cores and
+    3xTF32) << three-term e4m3 (~2^-12) < TF32 (2^-11) < two-term e4m3 and
+    BF16 (~2^-8) < one-term e4m3 (2^-4)."""
+    import torch
+    n = 512
+    A, _, _ = make_system(cuda, n, 1e2, 1, 21)
+    f = fg.lib().flens_gb300_sgetrf_tc
+    f.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3
+    err = {}
+    for name, prec in (("fp32", -1), ("3xtf32", 3), ("tf32", 0), ("bf16", 1), ("fp8", 2),
+                       ("fp8x2", 5), ("fp8x3", 6)):
+        F = A.to(torch.float32).t().contiguous().t()
+        ipiv = torch.zeros(n, dtype=torch.int32, device=cuda)
+        info = torch.zeros(1, dtype=torch.int32, device=cuda)
+        st = f(prec, n, n, F.data_ptr(), n, ipiv.data_ptr(), info.data_ptr(),
+               ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        torch.cuda.synchronize()
+        assert st == 0 and int(info.item()) == 0, (name, st, fg.last_error())
+        perm = list(range(n))
+        for i, p in enumerate(ipiv.cpu().numpy()):
+            perm[i], perm[p - 1] = perm[p - 1], perm[i]
+        Fd = F.double()
+        L = torch.tril(Fd, -1) + torch.eye(n, dtype=torch.float64, device=cuda)
+        err[name] = float((A[perm] - L @ torch.triu(Fd)).norm() / A.norm())
+    A64 = A.cpu()
+    for name in ("fp8x2", "fp8x3"):
+        ref = _emulated_lu_error(A64, name)
+        assert abs(err[name] - ref) <= 0.25 * ref, (name, err[name], ref)
+    assert err["fp32"] < 1e-5 and err["3xtf32"] < 1e-5, err
+    assert err["3xtf32"] < err["fp8x3"] < err["tf32"] < err["fp8x2"] < err["fp8"], err
+    assert err["bf16"] < err["fp8"] and err["fp8x2"] < err["bf16"], err
+
+
+def test_mixed_fp8x3_converges_where_fp8_cannot(cuda):
+    """n = 4096, kappa = 1e2: one-term e4m3 factors are no preconditioner
+    (||I - (LU)^-1 PA|| >> 1 at this size), three-term e4m3 factors reach
+    10 n eps in a few steps."""
+    n = 4096
+    A, b, x = make_system(cuda, n, 1e2, 1, 22)
+    st, X, it, be, inf = dgesv_mixed(A, b, "fp8x3", "auto")
+    assert st == 0 and inf == 0, (st, fg.last_error(), it, be)
+    assert it <= 10, it
+    assert backward_error(A, X, b) <= 10 * n * EPS
+    st1, _, it1, be1, _ = dgesv_mixed(A, b, "fp8", "auto", max_iter=4)
+    assert st1 == fg.ERR_NOT_CONVERGED and be1 > 10 * n * EPS

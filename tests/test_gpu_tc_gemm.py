@@ -19,7 +19,7 @@ import flens_gb300 as fg
 
 pytestmark = pytest.mark.gpu
 
-PREC = {"tf32": 0, "bf16": 1, "fp8": 2}
+PREC = {"tf32": 0, "bf16": 1, "fp8": 2, "fp8x2": 5, "fp8x3": 6}
 
 
 def round_tf32(x):
@@ -117,3 +117,75 @@ def test_sgemm_tc_beta_semantics(cuda):
     An = torch.full_like(A, float("nan"))
     sgemm_tc("bf16", "N", "N", 0.0, An, B, 0.5, C2)
     assert torch.equal(C2, 0.5 * C20)
+
+
+def fp8_terms(x, nterms):
+    """Per-row scale amax/448 and the e4m3 terms of the scaled rows of x
+    (fp32, rows x K): t0 = e4m3(v), t1 = e4m3(v - t0), t2 = e4m3(v - t0 - t1)
+    with v = x * (1/s)."""
+    import torch
+    amax = x.abs().amax(dim=1, keepdim=True)
+    s = torch.where(amax > 0, amax / 448.0, torch.ones_like(amax))
+    r = x * (1.0 / s)
+    terms = []
+    for _ in range(nterms):
+        t = r.to(torch.float8_e4m3fn).to(torch.float32)
+        terms.append(t.to(torch.float64))
+        r = r - t
+    return s.to(torch.float64), terms
+
+
+PAIRS = {"fp8x2": [(1, 0), (0, 1), (0, 0)],
+         "fp8x3": [(2, 0), (0, 2), (1, 1), (1, 0), (0, 1), (0, 0)]}
+
+
+@pytest.mark.parametrize("prec", ["fp8x2", "fp8x3"])
+@pytest.mark.parametrize("m,n,k", [(128, 256, 64), (200, 300, 100), (1000, 600, 256),
+                                   (257, 513, 1000)])
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T")])
+def test_sgemm_tc_fp8_terms_vs_fp64_reference(cuda, prec, m, n, k, ta, tb):
+    """Two- and three-term e4m3 (precisions 5, 6): the tensor cores take the
+    products t_i t_j (i + j <= 1, or <= 2) of the scaled operands' terms; the
+    FP64 reference forms the same products from the same terms.  The tensor
+    core's FP8 sums are not full FP32 (measured up to 2.2e-5 normwise at
+    K' = 3K = 336), so the bar is 1e-4 normwise and 1e-3 elementwise for
+    K' <= 768 and 1e-3 beyond -- still 40x below the 2^-8 operand error two
+    terms leave.  The result must also be much closer to the exact product of
+    the FP32 operands than one-term e4m3 (and three terms than two)."""
+    import torch
+    A = colmajor(torch, m if ta == "N" else k, k if ta == "N" else m, 11 + m, cuda)
+    B = colmajor(torch, k if tb == "N" else n, n if tb == "N" else k, 12 + n, cuda)
+    C0 = colmajor(torch, m, n, 13 + k, cuda)
+    alpha, beta = -1.0, 1.0
+    opA = A if ta == "N" else A.t()
+    opB = B if tb == "N" else B.t()
+    nt = 2 if prec == "fp8x2" else 3
+    sa, ta_ = fp8_terms(opA.contiguous(), nt)
+    sb, tb_ = fp8_terms(opB.t().contiguous(), nt)
+    prod = sa * sum(ta_[i] @ tb_[j].t() for i, j in PAIRS[prec]) * sb.t()
+    ref = alpha * prod + beta * C0.to(torch.float64)
+    absA, absB = sum(t.abs() for t in ta_), sum(t.abs() for t in tb_)
+    bound = abs(alpha) * (sa * (absA @ absB.t()) * sb.t()) + abs(beta) * C0.abs().to(torch.float64)
+    C = C0.clone()
+    sgemm_tc(prec, ta, tb, alpha, A, B, beta, C)
+    err = C.to(torch.float64) - ref
+    rel = (err.norm() / ref.norm()).item()
+    elem = (err.abs() / bound.clamp_min(1e-30)).max().item()
+    kseg = len(PAIRS[prec]) * k
+    tol_rel, tol_elem = (1e-4, 1e-3) if kseg <= 768 else (1e-3, 1e-3)
+    assert rel <= tol_rel and elem <= tol_elem, (rel, elem)
+    # against the exact product of the FP32 operands: one term ~2^-4,
+    # two ~2^-8, three ~2^-12 (down to the FP8 summation error at long K')
+    exact = alpha * (opA.double() @ opB.double()) + beta * C0.double()
+    C1 = C0.clone()
+    sgemm_tc("fp8", ta, tb, alpha, A, B, beta, C1)
+    e_n = ((C.double() - exact).norm() / exact.norm()).item()
+    e_1 = ((C1.double() - exact).norm() / exact.norm()).item()
+    if prec == "fp8x2":
+        assert e_n <= e_1 / 8 and e_n <= 8e-3, (e_n, e_1)
+    else:
+        C2 = C0.clone()
+        sgemm_tc("fp8x2", ta, tb, alpha, A, B, beta, C2)
+        e_2 = ((C2.double() - exact).norm() / exact.norm()).item()
+        # (over long K' the FP8 summation error, ~2e-4, is what is left)
+        assert e_n <= (e_2 / 4 if kseg <= 768 else e_2) and e_n <= max(5e-4, 2 * tol_rel), (e_n, e_2)
