@@ -948,7 +948,7 @@ def batched_subbench(torch, fg, dev, count=20000, reps=3, loop_sample=2000, unif
         return np.array(errs)
 
     sample = rng.choice(count, size=min(1000, count), replace=False)
-    for prec, name in ((0, "fp64"), (1, "fp32_lu+fp64_ir")):
+    for prec, name in ((0, "fp64"), (1, "fp32_lu+fp64_ir"), (2, "auto_per_matrix")):
         plan = ctypes.c_void_p()
         t0 = time.time()
         st = f(count, n.ctypes.data, k.ctypes.data, pa.ctypes.data, lda.ctypes.data, pp.ctypes.data,
@@ -983,7 +983,7 @@ def batched_subbench(torch, fg, dev, count=20000, reps=3, loop_sample=2000, unif
              "backward_error_over_n_eps_p50": float(np.percentile(be, 50)),
              "backward_error_over_n_eps_p99": float(np.percentile(be, 99)),
              "backward_error_sample": f"{len(sample)} matrices"}
-        if prec == 1:
+        if prec >= 1:
             it = iters.cpu().numpy()
             v["refinement_steps_mean"] = float(it[it >= 0].mean()) if (it >= 0).any() else None
             v["fp64_fallback"] = int((it < 0).sum())

@@ -20,7 +20,14 @@
 //     (flens/lapack/ge/rfs.tcc:182-188) or after max_iter steps).  The FP32
 //     factors live in shared memory when they fit, otherwise in the plan's
 //     pool (blocked LU); matrices with more than 32 right-hand sides are
-//     solved in FP64 (iters = -1).
+//     solved in FP64 (iters = -1).  precision 2 = per matrix, precision 1
+//     where it is faster than FP64 -- n >= 256 and nrhs <= n/64: the FP64
+//     residuals of the refinement cost 3 n^2 nrhs FP64 FMAs, which the FP32
+//     LU repays only for large n and few right-hand sides (measured on
+//     homogeneous batches: n = 512, 1 rhs 16.6 against 23.6 ms; n = 300,
+//     4 rhs 18.1 against 21.0 ms; n = 512, 16 rhs 28.7 against 26.1 ms;
+//     n = 200, 4 rhs equal; n <= 100 up to 2.6x slower) -- and FP64
+//     elsewhere (iters = -1).
 #include "common.cuh"
 
 #include <float.h>
@@ -690,8 +697,17 @@ __device__ void refine_fp64(const BatchArgs &a, int idx, const double *A, int ld
     for (int e = lt; e < n * k; e += T) B[e % n + (size_t)(e / n) * ldb] = (double)D[e];
     double anorm = 0.0, worst = 0.0;
     for (int r = lt; r < n; r += T) {
+        // eight loads in flight, summed in column order
         double s = 0.0;
-        for (int c = 0; c < n; ++c) s += fabs(A[r + (size_t)c * lda]);
+        int c = 0;
+        for (; c + 8 <= n; c += 8) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = A[r + (size_t)(c + u) * lda];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s += fabs(v[u]);
+        }
+        for (; c < n; ++c) s += fabs(A[r + (size_t)c * lda]);
         anorm = fmax(anorm, s);
     }
     anorm = team_max(anorm, lt, T, bar, rv);
@@ -701,11 +717,35 @@ __device__ void refine_fp64(const BatchArgs &a, int idx, const double *A, int ld
     for (int c = 0; c < k && c < 32; ++c) prev[c] = INFINITY;
     for (int it = 0; it <= a.max_iter; ++it) {
         team_sync(bar, T);
-        for (int e = lt; e < n * k; e += T) {          // r = b - A x, FP64
-            const int r = e % n, c = e / n;
-            double s = Bs[e];
-            for (int q = 0; q < n; ++q) s = fma(-A[r + (size_t)q * lda], B[q + (size_t)c * ldb], s);
-            Rr[e] = s;
+        // r = b - A x, FP64: a thread takes one row and up to four columns,
+        // so each element of A (from L2) is loaded once for four FMAs, with
+        // eight loads in flight; every sum runs over q in order
+        const int ng = (k + 3) / 4;
+        for (int e = lt; e < n * ng; e += T) {
+            const int r = e % n, c0 = (e / n) * 4, nc = min(4, k - c0);
+            double s[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) s[u] = u < nc ? Bs[r + (size_t)(c0 + u) * n] : 0.0;
+            int q = 0;
+            for (; q + 8 <= n; q += 8) {
+                double av[8];
+#pragma unroll
+                for (int v = 0; v < 8; ++v) av[v] = A[r + (size_t)(q + v) * lda];
+#pragma unroll
+                for (int v = 0; v < 8; ++v)
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (u < nc) s[u] = fma(-av[v], B[(q + v) + (size_t)(c0 + u) * ldb], s[u]);
+            }
+            for (; q < n; ++q) {
+                const double a = A[r + (size_t)q * lda];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (u < nc) s[u] = fma(-a, B[q + (size_t)(c0 + u) * ldb], s[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (u < nc) Rr[r + (size_t)(c0 + u) * n] = s[u];
         }
         team_sync(bar, T);
         bool any = false;
@@ -783,6 +823,9 @@ __device__ __noinline__ void solve_mixed(const BatchArgs &a, int idx, unsigned c
 // of A factored in place in the team's pool slot by the blocked LU (FP32
 // panels in shared memory, FP64 pivot search and scaling), the FP32 solves
 // staged in shared memory, FP64 residuals from the untouched A.
+// precision 2: the matrices for which FP32 LU + FP64 refinement is faster
+__host__ __device__ inline bool mixed_pays(int n, int k) { return n >= 256 && 64 * k <= n; }
+
 __device__ bool mixed_blocked_ok(const BatchArgs &a, int n, int k, int nb, int T, size_t share) {
     return a.mx_pool != nullptr && k <= 32 && BT_THREADS / T <= a.mx_teams &&
            mx_need(n, k) <= a.mx_stride && blocked_need(n, nb, sizeof(float)) <= share;
@@ -862,9 +905,10 @@ batched_gesv_kernel(BatchArgs a) {
             team_sync(bar, T);
             if (item >= end) break;
             const int idx = a.order[item];
-            if (MIXED && a.nrhs[idx] <= 32 && mixed_need(a.n[idx], a.nrhs[idx]) <= share)
+            const bool mix = MIXED && (a.precision != 2 || mixed_pays(a.n[idx], a.nrhs[idx]));
+            if (mix && a.nrhs[idx] <= 32 && mixed_need(a.n[idx], a.nrhs[idx]) <= share)
                 solve_mixed(a, idx, sm, lt, T, bar, red_v[tm], red_i[tm]);
-            else if (MIXED && mixed_blocked_ok(a, a.n[idx], a.nrhs[idx], nb, T, share))
+            else if (mix && mixed_blocked_ok(a, a.n[idx], a.nrhs[idx], nb, T, share))
                 // slots [blockIdx.x * mx_teams, +teams): the same for every
                 // bucket, since CTAs move through the buckets independently
                 solve_mixed_blocked(a, idx, sm, share, nb, blockIdx.x * a.mx_teams + tm, lt, T, bar,
@@ -963,7 +1007,7 @@ int launch(const BatchArgs &a, cudaStream_t s) {
     int st = set_attributes();
     if (st != kOk) return st;
     FG_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(int) * BT_BUCKETS, s));
-    if (a.precision == 1) batched_gesv_kernel<true><<<num_sms(), BT_THREADS, BT_SMEM, s>>>(a);
+    if (a.precision >= 1) batched_gesv_kernel<true><<<num_sms(), BT_THREADS, BT_SMEM, s>>>(a);
     else batched_gesv_kernel<false><<<num_sms(), BT_THREADS, BT_SMEM, s>>>(a);
     FG_CUDA(cudaGetLastError());
     return kOk;
@@ -1190,7 +1234,7 @@ int batched_plan_create(int count, const int *hn, const int *hk, double *const *
     a.queue = d_q;
     a.precision = precision;
     a.max_iter = max_iter > 0 ? max_iter : 10;
-    if (precision == 1) {
+    if (precision >= 1) {
         // pool for the matrices that take the blocked mixed path: a slot per
         // team of the CTAs, as large as the largest such matrix needs (if it
         // cannot be had, those matrices are solved in FP64 instead)
@@ -1202,6 +1246,7 @@ int batched_plan_create(int count, const int *hn, const int *hk, double *const *
             for (int i = a.beg[b]; i < a.end[b]; ++i) {
                 const int ni = hn[order[i]], ki = hk[order[i]];
                 if (ki > 32 || mixed_need(ni, ki) <= share) continue;
+                if (precision == 2 && !mixed_pays(ni, ki)) continue;
                 if (blocked_need(ni, a.panel[b], sizeof(float)) > share) continue;
                 stride = std::max(stride, mx_need(ni, ki));
                 teams = std::max(teams, BT_THREADS / T);
@@ -1277,7 +1322,7 @@ FG_API int flens_gb300_dgesv_batched_plan(int count, const int *n, const int *nr
                                           int precision, int *iters, double *berr, int max_iter,
                                           void *stream, void **plan) {
     if (count < 0) return -1;
-    if (precision < 0 || precision > 1) return -10;
+    if (precision < 0 || precision > 2) return -10;
     if (!plan) return -15;
     for (int i = 0; i < count; ++i) {
         if (n[i] < 0 || nrhs[i] < 0 || lda[i] < (n[i] > 1 ? n[i] : 1) ||

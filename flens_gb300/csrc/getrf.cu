@@ -106,6 +106,15 @@ __device__ __forceinline__ unsigned long long pivot_key(double x) {
     return a > 0x7ff0000000000000ull ? 1ull : a + 2ull;
 }
 
+// Named barrier 1 over `count` threads: the producer warp arrives without
+// waiting, the consumers wait until every participant has arrived.
+__device__ __forceinline__ void named_bar_arrive(int id, int count) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void named_bar_sync(int id, int count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
 __device__ __forceinline__ bool better(unsigned long long k1, int i1, unsigned long long k2, int i2) {
     return k1 > k2 || (k1 == k2 && i1 < i2);
 }
@@ -126,12 +135,22 @@ __device__ __forceinline__ void warp_argmax(unsigned long long &k, int &i) {
 // Panel factorisation, tf2 semantics (flens/lapack/ge/tf2.tcc:56-136).
 // A points at the panel's top-left element A(j,j); the panel is mp x jb.
 // CTA b owns panel rows [b*R, min(mp,(b+1)*R)), kept in shared memory as
-// S[c*R + r]; thread t owns local rows t, t+256, ... for the whole panel:
-// it swaps, scales and updates them and keeps their pivot keys, so a column
-// needs two block barriers: one to collect the warps' candidates, one to
-// hand the pivot to every thread.  Warp 0 does the cross-CTA exchange.
-template <typename T>
-__global__ void __launch_bounds__(PANEL_THREADS)
+// S[c*R + r].  With at most 128 rows a CTA gives each row W = 2, 4 or 8
+// lanes (interleaved columns) and defers most of each column's rank-1 update
+// past the next column's candidate search (see [E2] below); with more rows
+// thread t owns local rows t, t+256, ... and updates them at once.  Block
+// barriers per column: one to collect the warps' candidates, one after the
+// cross-CTA poll, one to hand the pivot to every thread.  Warp 0 does the
+// cross-CTA exchange.
+// Two builds: DEFER (the deferred update below, about 100 registers per
+// thread) for panels that run alone or beside a small update, and the
+// immediate update within 64 registers for panels beside a large look-ahead
+// GEMM (74 registers, 256 threads per CTA): at 102 registers only one GEMM
+// CTA fitted beside the panel instead of two (the n = 8192 LU: 325.9 against
+// 322.8 ms per solve), and capping the deferred build instead slowed the
+// split-update LU's panels by 11%.
+template <typename T, bool DEFER>
+__global__ void __launch_bounds__(PANEL_THREADS, DEFER ? 1 : 4)
 panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
              int *__restrict__ ipiv, int *__restrict__ info, int *__restrict__ status,
              PanelScratch ps, int R, unsigned long long epoch) {
@@ -168,6 +187,21 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
         if (better(key, rb + r, nbk, nbi)) { nbk = key; nbi = rb + r; }
     }
 
+    // Deferred update (DEFER and W > 1): after the pivot of column jj is
+    // known, each
+    // row gets its swap, its multiplier l and the update of column jj + 1
+    // (whose pivot keys the next search needs); the update of columns
+    // >= jj + 2 waits until the next column's candidates are published, so
+    // it runs while the other CTAs publish and this CTA polls.  Warp 0
+    // publishes the candidate rows with those columns computed on the fly,
+    // by the same FMA the deferred update stores: the factors are bitwise
+    // those of the undeferred order.
+    const bool lanes = W > 1, defer = DEFER && lanes;
+    const double *dP = nullptr;          // pivot row of the pending update
+    int d_jj = -1, d_gs = -1;            // its column and pivot row (-1: none)
+    bool d_swap = false;
+    bool pend = false, pend_gs = false;  // this thread's row has a pending update
+    double pend_l = 0.0;
     for (int jj = 0; jj < jb; ++jj) {
         const int par = jj & 1;
         const unsigned long long want = epoch * 128ull + (unsigned long long)jj + 1ull;
@@ -185,16 +219,56 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
             i = lane < NW ? red_i[lane] : INT_MAX;
             warp_argmax(k, i);
             PanelSlot *mine = &ps.slots[par * PANEL_GMAX + b];
-            if (i != INT_MAX)
-                for (int c = lane; c < jb; c += 32) mine->row[c] = S[c * R + (i - rb)];
-            if (jj >= rb && jj < re)
-                for (int c = lane; c < jb; c += 32) mine->rowjj[c] = S[c * R + (jj - rb)];
+            // entry c of local row x, final (the pending update applied)
+            auto fin = [&](int x, int c) -> double {
+                if (d_jj < 0 || c < d_jj + 2) return S[c * R + x];
+                const double src = (d_swap && rb + x == d_gs) ? orow[c] : S[c * R + x];
+                return fma(-dP[c], S[d_jj * R + x], src);
+            };
+            // both rows into registers (jb <= 64: two entries per lane)
+            // before the other warps may store their pending updates
+            const bool has_i = i != INT_MAX, has_jj = jj >= rb && jj < re;
+            double vi[2] = {0.0, 0.0}, vj[2] = {0.0, 0.0};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int c = lane + 32 * h;
+                if (c < jb) {
+                    if (has_i) vi[h] = fin(i - rb, c);
+                    if (has_jj) vj[h] = fin(jj - rb, c);
+                }
+            }
+            if (defer) named_bar_arrive(1, PANEL_THREADS);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int c = lane + 32 * h;
+                if (c < jb) {
+                    if (has_i) mine->row[c] = vi[h];
+                    if (has_jj) mine->rowjj[c] = vj[h];
+                }
+            }
             if (lane == 0) {
                 mine->key = k;
                 mine->idx = i;
             }
             __syncwarp();
             if (lane == 0) st_release(&mine->seq, want);
+        } else if (defer) {
+            named_bar_sync(1, PANEL_THREADS);
+        }
+        // -- [E2] the pending update of column jj - 1: columns >= jj + 1
+        if (pend) {
+            const int r = tid / W, q = tid % W;
+            const double *old = pend_gs ? orow : nullptr;
+            int c = d_jj + 2 + q;
+            for (; c + 3 * W < jb; c += 4 * W) {
+                double v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = old ? old[c + u * W] : S[(c + u * W) * R + r];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) S[(c + u * W) * R + r] = fma(-dP[c + u * W], pend_l, v[u]);
+            }
+            for (; c < jb; c += W) S[c * R + r] = fma(-dP[c], pend_l, old ? old[c] : S[c * R + r]);
+            pend = false;
         }
         // -- [C] thread t < G waits for slot t of this step and reads it
         unsigned long long gk = kKeyNone;
@@ -255,10 +329,11 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
         const double *P = (gs == jj) ? orow : prow;                  // new row jj
 
         // -- [E] per owned row: interchange, scaling, rank-1 update of the
-        // columns > jj, and the pivot key for column jj+1
+        // columns > jj (deferred beyond jj + 1 when W > 1), and the pivot key
+        // for column jj+1
         nbk = kKeyNone;
         nbi = INT_MAX;
-        if (W > 1) {
+        if (lanes) {
             // W lanes per row (nr * W <= 256: one row per lane group), lane q
             // of the group taking columns q, q + W, ...: the chain of
             // dependent shared-memory updates per thread is W times shorter.
@@ -277,22 +352,41 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
                 if (from_gs)
                     for (int c = q; c < jj; c += W) S[c * R + r] = orow[c];
                 if (pv != 0.0) l = (rinv != 0.0) ? l * rinv : l / pv;
-                if (q == 0 && (pv != 0.0 || from_gs)) S[jj * R + r] = l;
+                if (q == 0 && pv != 0.0) S[jj * R + r] = l;
                 const double *old = from_gs ? orow : nullptr;
-                int c = jj + 1 + q;
-                for (; c + 3 * W < jb; c += 4 * W) {
-                    double v[4];
+                if (defer) {
+                    // column jj + 1 and its key now, the rest in [E2]
+                    if (q == 0 && jj + 1 < jb) {
+                        const int c = jj + 1;
+                        const double v = fma(-P[c], l, old ? old[c] : S[c * R + r]);
+                        S[c * R + r] = v;
+                        nbk = pivot_key(v);
+                        nbi = g;
+                    }
+                    pend = jj + 2 + q < jb;
+                    pend_gs = from_gs;
+                    pend_l = l;
+                } else {
+                    int c = jj + 1 + q;
+                    for (; c + 3 * W < jb; c += 4 * W) {
+                        double v[4];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) v[u] = old ? old[c + u * W] : S[(c + u * W) * R + r];
+                        for (int u = 0; u < 4; ++u) v[u] = old ? old[c + u * W] : S[(c + u * W) * R + r];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) S[(c + u * W) * R + r] = fma(-P[c + u * W], l, v[u]);
+                        for (int u = 0; u < 4; ++u) S[(c + u * W) * R + r] = fma(-P[c + u * W], l, v[u]);
+                    }
+                    for (; c < jb; c += W) S[c * R + r] = fma(-P[c], l, old ? old[c] : S[c * R + r]);
+                    if (q == 0 && jj + 1 < jb) {
+                        nbk = pivot_key(S[(jj + 1) * R + r]);
+                        nbi = g;
+                    }
                 }
-                for (; c < jb; c += W) S[c * R + r] = fma(-P[c], l, old ? old[c] : S[c * R + r]);
-                if (q == 0 && jj + 1 < jb) {
-                    const unsigned long long key = pivot_key(S[(jj + 1) * R + r]);
-                    nbk = key;
-                    nbi = g;
-                }
+            }
+            if (defer) {
+                dP = P;
+                d_jj = jj;
+                d_gs = gs;
+                d_swap = swap;
             }
         } else
         for (int r = tid; r < nr; r += PANEL_THREADS) {
@@ -634,7 +728,9 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int 
     unsigned long long epoch = 0;
     static DeviceOnce once;
     {
-        const int st0 = set_smem_once(once, (const void *)panel_kernel<T>, (int)PANEL_SMEM_MAX);
+        static DeviceOnce once_d;
+        int st0 = set_smem_once(once, (const void *)panel_kernel<T, false>, (int)PANEL_SMEM_MAX);
+        if (st0 == kOk) st0 = set_smem_once(once_d, (const void *)panel_kernel<T, true>, (int)PANEL_SMEM_MAX);
         if (st0 != kOk) return st0;
     }
     int sms = num_sms();
@@ -661,7 +757,13 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int 
     int ob_end = (split_nb > 0 && split_nb < mn) ? split_nb : n;
 
     // Launches the panel at column j on stream s; *jb_out = its width.
-    auto panel_at = [&](int j, cudaStream_t s, int *jb_out) -> int {
+    // `defer`: overlap the panel's own rank-1 updates with its exchanges --
+    // asked for when nothing large runs beside the panel.  Beside a big
+    // trailing update it measured slower overall (the n = 8192 LU: 325.3
+    // against 322.8 ms per solve; the GEMM took 3 ms longer, the hidden
+    // panels 6 ms less), since the panel's FP64 work then competes with the
+    // GEMM's on the shared SMs.
+    auto panel_at = [&](int j, cudaStream_t s, int *jb_out, bool defer) -> int {
         int mp = m - j;
         int R = ceil_div(mp, gcap);
         if (R < PANEL_RMIN) R = PANEL_RMIN;
@@ -684,7 +786,8 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int 
         void *args[] = {&Ap, &ldA, &mp, &jb, &j0, &ipiv, &info, &status, &ps, &R, &epoch};
         KTimer ktp(kFamPanel, s, (double)mp * jb * jb - (double)jb * jb * jb / 3.0,
                    2.0 * sizeof(T) * (double)mp * jb);
-        FG_CUDA(cudaLaunchCooperativeKernel((const void *)panel_kernel<T>, dim3(G),
+        const void *fn = defer ? (const void *)panel_kernel<T, true> : (const void *)panel_kernel<T, false>;
+        FG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(G),
                                             dim3(PANEL_THREADS), args, smem, s));
         *jb_out = jb;
         return kOk;
@@ -708,7 +811,7 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int 
             if (ahead) {
                 FG_CUDA(cudaStreamWaitEvent(stream, wl->ev_back, 0));
                 ahead = false;
-            } else if ((st = panel_at(j, stream, &jb)) != kOk) {
+            } else if ((st = panel_at(j, stream, &jb, true)) != kOk) {
                 return st;
             }
             // interchanges on the columns outside the panel
@@ -735,7 +838,10 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int 
                         if ((st = update(j, jb, nx, w2)) != kOk) return st;
                         FG_CUDA(cudaEventRecord(wl->ev_fwd, stream));
                         FG_CUDA(cudaStreamWaitEvent(wl->side, wl->ev_fwd, 0));
-                        if ((st = panel_at(nx, wl->side, &next_jb)) != kOk) return st;
+                        // defer when the update beside the panel is small
+                        // (under ~4M elements: about the panel's own time)
+                        const bool small = (double)(m - j - jb) * (double)(nr - w2) < 4.0e6;
+                        if ((st = panel_at(nx, wl->side, &next_jb, small)) != kOk) return st;
                         FG_CUDA(cudaEventRecord(wl->ev_back, wl->side));
                         ahead = true;
                         if (next_jb > w2) {

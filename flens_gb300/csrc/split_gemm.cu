@@ -318,6 +318,7 @@ struct EpiSplit {
     const int *ea, *eb;                          // row exponents of op(A), column exponents of op(B)
 
     __device__ int groups() const { return geo.ngroups; }
+    __device__ void prefetch(int, int, int, int, int) const {}
     __device__ void group(int g, int &ka, int &kb, int &nk) const {
         int dg, slo, shi, k0, k1;
         geo.decode(g, dg, slo, shi, k0, k1);

@@ -35,8 +35,20 @@ struct EpiF32 {
     int ldc;
     const float *scale_a, *scale_b;
     int nkb;                                     // k-blocks of the whole K
+    int pf;                                      // C 16-byte aligned by column: prefetch it
 
     __device__ int groups() const { return 1; }
+    // column j of the next tile's C into L2 (a contiguous run of its rows),
+    // so that the epilogue's loads of it hit L2 instead of HBM
+    __device__ void prefetch(int m0, int n0, int M, int N, int j) const {
+        if (!pf || beta == 0.0f || j >= min(kBN, N - n0)) return;
+        const int bytes = (min(BM, M - m0) * 4) & ~15;
+        if (bytes <= 0) return;
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
+                         C + (size_t)m0 + (size_t)(n0 + j) * ldc),
+                     "r"(bytes)
+                     : "memory");
+    }
     __device__ void group(int, int &ka, int &kb, int &nk) const {
         ka = 0;
         kb = 0;
@@ -299,7 +311,8 @@ int tc_gemm_launch(int kind, int M, int N, int K, float alpha, const void *A_lp,
     const int sms = num_sms();
     const dim3 grid(ntiles < sms ? ntiles : sms);
     const int bk = 128 / (int)tc_elem_bytes(kind);
-    const EpiF32 epi{alpha, beta, C, ldc, scale_a, scale_b, ceil_div(K, bk)};
+    const int pf = (((uintptr_t)C | ((uintptr_t)ldc * 4)) & 15) == 0 ? 1 : 0;
+    const EpiF32 epi{alpha, beta, C, ldc, scale_a, scale_b, ceil_div(K, bk), pf};
     KTimer kt(kFamTcGemm, stream, 2.0 * M * (double)N * K,
               tc_elem_bytes(kind) * ((double)M * K + (double)N * K) + 8.0 * M * (double)N);
 #define FG_TC(KD)                                                                               \

@@ -210,6 +210,10 @@ __device__ __forceinline__ void tile_origin(int t, int tiles_m, int tiles_n, int
 //        columns col..col+31 of tile row `row` (ncol of them inside C); xt is
 //        the TMEM address of the policy's own kTmemExtra columns for this
 //        warp's lane quarter (tile-local column 0).
+//   void prefetch(int m0, int n0, int M, int N, int j) const
+//        called by epilogue thread j (0..255) when its warps start a tile,
+//        with the origin of the CTA's next tile: may bring column j of that
+//        tile's output into L2 (a no-op for policies that read none)
 //   static constexpr int kBN, kTmemExtra (see Shape)
 template <int KIND, class Epi>
 __global__ void __launch_bounds__(THREADS, 1)
@@ -344,6 +348,12 @@ tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
             int m0, n0;
             tile_origin(t, tiles_m, tiles_n, BN, m0, n0);
             const int row = m0 + quarter * 32 + lane;
+            if (t + (int)gridDim.x < ntiles) {
+                // the next tile's output, one tile ahead of its epilogue
+                int m1, n1;
+                tile_origin(t + (int)gridDim.x, tiles_m, tiles_n, BN, m1, n1);
+                epi.prefetch(m1, n1, M, N, ew * 32 + lane);
+            }
             for (int g = 0; g < ngroups; ++g, ++i) {
                 const int b = i & 1;
                 if (!mbar_wait(&tfull[b], (uint32_t)(i >> 1) & 1u, status)) {

@@ -373,7 +373,9 @@ int flens_gb300_dgesv_mixed(int n, int nrhs, const double *A, int ldA,
  * there, otherwise on FP32 factors of a copy of A_i in a device pool that the
  * plan allocates (one slot per team, sized for the largest such matrix).
  * Matrices with more right-hand sides, or all of them if that pool cannot be
- * allocated, take the FP64 path (iters_i = -1, A_i <- LU factors).  B_i <- X_i
+ * allocated, take the FP64 path (iters_i = -1, A_i <- LU factors).
+ * precision 2 = per matrix: precision 1 where it is the faster of the two
+ * (n_i >= 256 and nrhs_i <= n_i/64), the FP64 path otherwise.  B_i <- X_i
  * when INFO_i == 0, untouched otherwise.  Creating a plan autotunes the team
  * size and panel width of each size bucket (first use per device;
  * FLENS_GB300_BATCH_TUNE=0 disables it, FLENS_GB300_BATCH_TEAM=T and

@@ -355,7 +355,9 @@ def test_batched_plan_argument_errors(flib):
     ld = np.array([4, 4], dtype=np.int32)
     assert f(-1, None, None, None, None, None, None, None, None, 0, None, None, 0, None,
              ctypes.byref(plan)) == -1
-    assert f(0, None, None, None, None, None, None, None, None, 2, None, None, 0, None,
+    assert f(0, None, None, None, None, None, None, None, None, 3, None, None, 0, None,
+             ctypes.byref(plan)) == -10
+    assert f(0, None, None, None, None, None, None, None, None, -1, None, None, 0, None,
              ctypes.byref(plan)) == -10
     assert f(0, None, None, None, None, None, None, None, None, 0, None, None, 0, None, None) == -15
     assert f(2, n.ctypes.data, k.ctypes.data, None, ld.ctypes.data, None, None, ld.ctypes.data,

@@ -256,6 +256,30 @@ def test_batched_mixed_many_buckets_no_slot_sharing(cuda):
         assert be <= 10 * n * EPS, (i, n, ks[i], be, iters[i])
 
 
+def test_batched_auto_precision_per_matrix(cuda, port):
+    # precision 2: FP32 LU + FP64 refinement only where it is faster (n >= 256
+    # and k <= n/64), the FP64 path (iters = -1, A <- LU) for the rest
+    sizes = [16, 100, 200, 256, 300, 512, 512, 300, 64]
+    ks = [4, 1, 4, 4, 4, 1, 16, 5, 1]
+    mats, rhs, host = make_batch(cuda, sizes, ks, 5200)
+    ipivs, info, iters, berr, teams = run_batched(cuda, mats, rhs, 2)
+    assert (info == 0).all(), info
+    for i, (A0, Bh) in enumerate(host):
+        n, k = sizes[i], ks[i]
+        X = rhs[i].cpu().numpy()
+        A1, B1 = A0.copy(order="F"), Bh.copy(order="F")
+        pivr, _ = port.dgesv(A1, B1)
+        assert oracle.normwise_rel(X, B1) <= 1e-12, i
+        if n >= 256 and 64 * k <= n:
+            assert iters[i] >= 0, (i, n, k, iters[i])
+            assert berr[i] <= 10 * n * EPS
+            np.testing.assert_array_equal(mats[i].cpu().numpy(), A0)
+        else:
+            assert iters[i] == -1, (i, n, k, iters[i])
+            assert np.array_equal(ipivs[i].cpu().numpy()[:n], pivr), i
+            assert oracle.lu_backward_error(A0, mats[i].cpu().numpy(), ipivs[i].cpu().numpy()[:n]) <= 10.0
+
+
 def test_batched_unshifted_n512_pivots(cuda, port):
     # eight unshifted 512 x 512 systems (the blocked global-memory path, about
     # 500 interchanges each): pivots entry by entry on every pivot search whose
