@@ -582,21 +582,26 @@ int gemm_tt<float>(char ta, char tb, int m, int n, int k, float alpha, const flo
     return sgemm_launch(ta, tb, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, s);
 }
 
-// A22 -= L21 * U12 through the split GEMM (FP64 storage only).
+// The outer trailing update A22 -= L21 * U12 of the two-level LU: through the
+// split GEMM for FP64 storage, on the tensor cores in `tc_kind` for FP32.
 template <typename T>
-int split_update(int m, int n, int k, const T *L21, int ldL, const T *U12, int ldU, T *A22, int ldA22,
-                 size_t ws0_off, cudaStream_t s);
+int outer_update(int m, int n, int k, const T *L21, int ldL, const T *U12, int ldU, T *A22,
+                 int ldA22, size_t ws0_off, int tc_kind, void *tc_buf, cudaStream_t s);
 template <>
-int split_update<double>(int m, int n, int k, const double *L21, int ldL, const double *U12, int ldU,
-                         double *A22, int ldA22, size_t ws0_off, cudaStream_t s) {
+int outer_update<double>(int m, int n, int k, const double *L21, int ldL, const double *U12,
+                         int ldU, double *A22, int ldA22, size_t ws0_off, int, void *,
+                         cudaStream_t s) {
     return dgemm_split_launch_at('N', 'N', m, n, k, -1.0, L21, ldL, U12, ldU, 1.0, A22, ldA22, 0,
                                  nullptr, ws0_off, s);
 }
 template <>
-int split_update<float>(int, int, int, const float *, int, const float *, int, float *, int, size_t,
-                        cudaStream_t) {
-    set_last_error("split trailing update needs FP64 storage");
-    return kErrUnsupported;
+int outer_update<float>(int m, int n, int k, const float *L21, int ldL, const float *U12, int ldU,
+                        float *A22, int ldA22, size_t, int tc_kind, void *tc_buf, cudaStream_t s) {
+    if (tc_kind < 0) {
+        set_last_error("getrf: an FP32 outer update needs a tensor-core kind");
+        return kErrUnsupported;
+    }
+    return tc_trailing_update(tc_kind, m, n, k, L21, ldL, U12, ldU, A22, ldA22, tc_buf, s);
 }
 
 // Look-ahead in the blocked LU: on unless FLENS_GB300_LOOKAHEAD=0.
@@ -627,6 +632,19 @@ int split_outer_nb() {
         const char *e = getenv("FLENS_GB300_SPLIT_NB");
         const int v = e ? atoi(e) : 0;
         return (v >= 64 && v % 64 == 0) ? v : 512;
+    }();
+    return nb;
+}
+
+// Outer block of the tensor-core LU (FLENS_GB300_TC_NB, a multiple of 64; 64
+// = one level): its trailing updates have this depth, so they read and write
+// the FP32 C once per outer block instead of once per 64 columns.  At
+// n = 16384 the updates took 49.8, 28.0 and 17.3 ms for 64, 128 and 256.
+int tc_outer_nb() {
+    static int nb = [] {
+        const char *e = getenv("FLENS_GB300_TC_NB");
+        const int v = e ? atoi(e) : 0;
+        return (v >= 64 && v % 64 == 0) ? v : 256;
     }();
     return nb;
 }
@@ -692,9 +710,9 @@ int slaswp_launch(int nrows, int ncols, float *A, int ldA, int k1, int k2, const
 
 // Bytes of slot-0 workspace the blocked LU needs: the panel exchange area
 // plus, for a tensor-core trailing update, its operand buffers.
-size_t getrf_workspace_bytes(int m, int n, int tc_kind) {
+size_t getrf_workspace_bytes(int m, int n, int tc_kind, int depth) {
     size_t b = (panel_scratch_bytes() + 255) / 256 * 256;
-    if (tc_kind >= 0) b += tc_update_workspace_bytes(tc_kind, m, n, PANEL_NB);
+    if (tc_kind >= 0) b += tc_update_workspace_bytes(tc_kind, m, n, depth > PANEL_NB ? depth : PANEL_NB);
     return b;
 }
 
@@ -703,24 +721,26 @@ size_t getrf_workspace_bytes(int m, int n, int tc_kind) {
 // CUDA cores (tc_kind < 0) or, for T = float, on the tensor cores in the
 // precision `tc_kind` (see tc_gemm.cu).
 //
-// split_nb > 0 (T = double): two-level blocking.  The 64-column steps of an
-// outer block of split_nb columns update only the columns of that block
-// (their interchanges still reach every column); when the block is done,
-// U12 = L11^-1 A12 for all columns to its right (FP64 trsm) and
-// A22 -= L21 U12 with depth split_nb through the split GEMM.  This is the
-// order of LAPACK's dgetrf with a recursive panel; in exact arithmetic the
-// factors and pivots are those of the right-looking loop.
+// split_nb > 0: two-level blocking.  The 64-column steps of an outer block
+// of split_nb columns update only the columns of that block (their
+// interchanges still reach every column); when the block is done,
+// U12 = L11^-1 A12 for all columns to its right (trsm in T) and
+// A22 -= L21 U12 with depth split_nb, through the split GEMM for T = double
+// and on the tensor cores in `tc_kind` for T = float.  This is the order of
+// LAPACK's dgetrf with a recursive panel; in exact arithmetic the factors
+// and pivots are those of the right-looking loop.
 template <typename T>
 int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int split_nb,
             cudaStream_t stream) {
     FG_CUDA(cudaMemsetAsync(info, 0, sizeof(int), stream));
     if (m == 0 || n == 0) return kOk;
     const int mn = m < n ? m : n;
-    const size_t ws0 = getrf_workspace_bytes(m, n, tc_kind);
+    const size_t ws0 = getrf_workspace_bytes(m, n, tc_kind, split_nb);
     // the split GEMM's slot-0 data goes after ours; sized for the largest
     // update now so that slot 0 never moves under the panel scratch
     const size_t split_off = (ws0 + 255) / 256 * 256;
-    Workspace *w = workspace_for(stream, split_nb > 0 ? split_off + split_ws0_bytes(m, n) : ws0);
+    const bool fp64_split = split_nb > 0 && tc_kind < 0;
+    Workspace *w = workspace_for(stream, fp64_split ? split_off + split_ws0_bytes(m, n) : ws0);
     if (!w) return kErrAlloc;
     PanelScratch ps = carve_panel_scratch(w->buf);
     void *tc_buf = (char *)w->buf + (panel_scratch_bytes() + 255) / 256 * 256;
@@ -865,9 +885,10 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int 
                                     A + ob_start + (size_t)ob_end * ldA, ldA, stream)) != kOk)
                     return st;
                 if (ob_end < m) {
-                    st = split_update(m - ob_end, nr, kb, A + ob_end + (size_t)ob_start * ldA, ldA,
+                    st = outer_update(m - ob_end, nr, kb, A + ob_end + (size_t)ob_start * ldA, ldA,
                                       A + ob_start + (size_t)ob_end * ldA, ldA,
-                                      A + ob_end + (size_t)ob_end * ldA, ldA, split_off, stream);
+                                      A + ob_end + (size_t)ob_end * ldA, ldA, split_off, tc_kind,
+                                      tc_buf, stream);
                     if (st != kOk) return st;
                 }
                 ob_start = ob_end;
@@ -898,7 +919,8 @@ int dgetrf_split_launch(int m, int n, double *A, int ldA, int *ipiv, int *info, 
 
 int sgetrf_launch(int m, int n, float *A, int ldA, int *ipiv, int *info, int tc_kind,
                   cudaStream_t stream) {
-    return getrf_t<float>(m, n, A, ldA, ipiv, info, tc_kind, 0, stream);
+    const int onb = tc_kind >= 0 ? tc_outer_nb() : 0;
+    return getrf_t<float>(m, n, A, ldA, ipiv, info, tc_kind, onb > PANEL_NB ? onb : 0, stream);
 }
 
 template <typename T>
