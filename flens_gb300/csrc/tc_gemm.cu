@@ -183,6 +183,66 @@ row_scale_kernel(int R, int K, const float *__restrict__ in, int ld, float *__re
     }
 }
 
+// The split forms' operands in one pass: each entry of op(X) (R x K) is read
+// once, split into its terms -- TF32: t0 = tf32(v), t1 = tf32(v - t0); e4m3
+// (after the row scale): t0, t1, t2 as store_lp -- and segment q of the
+// K-major output row (columns q*kp .. q*kp + kp - 1, zero beyond K) gets term
+// seg[q].  Bitwise the terms of one tc_convert call per segment.
+struct SegTerms {
+    int nseg;
+    int term[6];
+};
+
+template <bool FP8, bool RCONTIG>
+__global__ void __launch_bounds__(256)
+to_kmajor_terms_kernel(int R, int K, const float *__restrict__ in, int ld, void *__restrict__ out,
+                       int ldo, int kp, SegTerms st, const float *__restrict__ inv_scale) {
+    __shared__ float tile[32][33];
+    const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+    auto emit = [&](int r, int k, float v) {
+        if (FP8 && inv_scale) v *= inv_scale[r];
+        uint32_t w0, w1, w2 = 0u;
+        if (FP8) {
+            __nv_fp8_storage_t q;
+            const float t0 = fp8_round(v, &q);
+            w0 = q;
+            const float t1 = fp8_round(v - t0, &q);
+            w1 = q;
+            fp8_round(v - t0 - t1, &q);
+            w2 = q;
+        } else {
+            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(w0) : "f"(v));
+            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(w1) : "f"(v - __uint_as_float(w0)));
+        }
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            if (q >= st.nseg) break;
+            const int tq = st.term[q];
+            const uint32_t val = tq == 0 ? w0 : tq == 1 ? w1 : w2;
+            const size_t idx = (size_t)r * ldo + (size_t)q * kp + k;
+            if (FP8) ((__nv_fp8_storage_t *)out)[idx] = (__nv_fp8_storage_t)val;
+            else ((uint32_t *)out)[idx] = val;
+        }
+    };
+    if (RCONTIG) {
+        for (int kk = ty; kk < 32; kk += 8) {
+            const int r = r0 + tx, k = k0 + kk;
+            tile[kk][tx] = (r < R && k < K) ? in[(size_t)r + (size_t)k * ld] : 0.0f;
+        }
+        __syncthreads();
+        for (int rr = ty; rr < 32; rr += 8) {
+            const int r = r0 + rr, k = k0 + tx;
+            if (r < R && k < kp) emit(r, k, tile[tx][rr]);
+        }
+    } else {
+        for (int rr = ty; rr < 32; rr += 8) {
+            const int r = r0 + rr, k = k0 + tx;
+            if (r < R && k < kp) emit(r, k, (k < K) ? in[(size_t)k + (size_t)r * ld] : 0.0f);
+        }
+    }
+}
+
 __global__ void sscale_kernel(int m, int n, float beta, float *__restrict__ C, int ldc) {
     const size_t total = (size_t)m * n;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
@@ -290,6 +350,33 @@ int tc_convert(int kind, bool trans, int R, int K, const float *X, int ldx, void
     return kOk;
 }
 
+// The split operand of op(X) (R x K) in one pass: segments st.term[q] at
+// columns q*kp of the K-major rows (see to_kmajor_terms_kernel); for e4m3
+// the per-row scales first (scale, inv_scale).
+int tc_convert_terms(bool fp8, bool trans, int R, int K, const float *X, int ldx, void *out,
+                     int ldo, int kp, const SegTerms &st, float *scale, float *inv_scale,
+                     cudaStream_t stream) {
+    if (R <= 0 || K <= 0) return kOk;
+    KTimer kt(kFamAux, stream, 0.0, (4.0 + (fp8 ? 1.0 : 4.0) * st.nseg) * R * (double)K);
+    const bool rcontig = !trans;
+    if (fp8) {
+        const dim3 g(ceil_div(R, 8));
+        if (rcontig) row_scale_kernel<true><<<g, 256, 0, stream>>>(R, K, X, ldx, scale, inv_scale);
+        else row_scale_kernel<false><<<g, 256, 0, stream>>>(R, K, X, ldx, scale, inv_scale);
+    }
+    const dim3 grid(ceil_div(R, 32), ceil_div(kp, 32));
+    const float *inv = fp8 ? inv_scale : nullptr;
+    if (fp8) {
+        if (rcontig) to_kmajor_terms_kernel<true, true><<<grid, 256, 0, stream>>>(R, K, X, ldx, out, ldo, kp, st, inv);
+        else to_kmajor_terms_kernel<true, false><<<grid, 256, 0, stream>>>(R, K, X, ldx, out, ldo, kp, st, inv);
+    } else {
+        if (rcontig) to_kmajor_terms_kernel<false, true><<<grid, 256, 0, stream>>>(R, K, X, ldx, out, ldo, kp, st, inv);
+        else to_kmajor_terms_kernel<false, false><<<grid, 256, 0, stream>>>(R, K, X, ldx, out, ldo, kp, st, inv);
+    }
+    FG_CUDA(cudaGetLastError());
+    return kOk;
+}
+
 // C (M x N, FP32, col-major) = alpha * A_lp * B_lp^T (* sa_i sb_j) + beta * C
 // A_lp: M x K K-major (lda), B_lp: N x K K-major (ldb), both 16-byte aligned.
 int tc_gemm_launch(int kind, int M, int N, int K, float alpha, const void *A_lp, int lda,
@@ -355,13 +442,10 @@ int f32x3_gemm(bool ta_rows, bool tb_rows, int m, int n, int k, float alpha, con
     const int kp = tc_kmajor_ld(kTcTF32, k), ld3 = 3 * kp;
     float *Ak = (float *)buf;
     float *Bk = (float *)((char *)buf + round256((size_t)m * ld3 * sizeof(float)));
+    const SegTerms sa{3, {1, 0, 0}}, sb{3, {0, 1, 0}};     // [lo | hi | hi], [hi | lo | hi]
     int st;
-    if ((st = tc_convert(kTcTF32Lo, ta_rows, m, k, A, ldA, Ak, ld3, nullptr, nullptr, s, kp))) return st;
-    if ((st = tc_convert(kTcTF32, ta_rows, m, k, A, ldA, Ak + kp, ld3, nullptr, nullptr, s, kp))) return st;
-    if ((st = tc_convert(kTcTF32, ta_rows, m, k, A, ldA, Ak + 2 * kp, ld3, nullptr, nullptr, s, kp))) return st;
-    if ((st = tc_convert(kTcTF32, tb_rows, n, k, B, ldB, Bk, ld3, nullptr, nullptr, s, kp))) return st;
-    if ((st = tc_convert(kTcTF32Lo, tb_rows, n, k, B, ldB, Bk + kp, ld3, nullptr, nullptr, s, kp))) return st;
-    if ((st = tc_convert(kTcTF32, tb_rows, n, k, B, ldB, Bk + 2 * kp, ld3, nullptr, nullptr, s, kp))) return st;
+    if ((st = tc_convert_terms(false, ta_rows, m, k, A, ldA, Ak, ld3, kp, sa, nullptr, nullptr, s))) return st;
+    if ((st = tc_convert_terms(false, tb_rows, n, k, B, ldB, Bk, ld3, kp, sb, nullptr, nullptr, s))) return st;
     return tc_gemm_launch(kTcTF32, m, n, ld3, alpha, Ak, ld3, Bk, ld3, beta, C, ldC, nullptr, nullptr, s);
 }
 
@@ -376,27 +460,17 @@ int f32x3_gemm(bool ta_rows, bool tb_rows, int m, int n, int k, float alpha, con
 int fp8_terms_gemm(int nterms, bool ta_rows, bool tb_rows, int m, int n, int k, float alpha,
                    const float *A, int ldA, const float *B, int ldB, float beta, float *C, int ldC,
                    void *buf, cudaStream_t s) {
-    static const int ta2[] = {1, 0, 0}, tb2[] = {0, 1, 0};
-    static const int ta3[] = {2, 0, 1, 1, 0, 0}, tb3[] = {0, 2, 1, 0, 1, 0};
-    static const int conv[] = {kTcFP8, kTcFP8Lo, kTcFP8Lo2};
-    const int nseg = nterms == 3 ? 6 : 3;
-    const int *tA = nterms == 3 ? ta3 : ta2, *tB = nterms == 3 ? tb3 : tb2;
+    const SegTerms a2{3, {1, 0, 0}}, b2{3, {0, 1, 0}};
+    const SegTerms a3{6, {2, 0, 1, 1, 0, 0}}, b3{6, {0, 2, 1, 0, 1, 0}};
+    const SegTerms &tA = nterms == 3 ? a3 : a2, &tB = nterms == 3 ? b3 : b2;
+    const int nseg = tA.nseg;
     const int kp = tc_kmajor_ld(kTcFP8, k), ldw = nseg * kp;
     const size_t a = round256((size_t)m * ldw), b = round256((size_t)n * ldw);
     uint8_t *Ak = (uint8_t *)buf, *Bk = (uint8_t *)buf + a;
     float *sa = (float *)((char *)buf + a + b), *sia = sa + m, *sb = sia + m, *sib = sb + n;
     int st;
-    // the last segment holds t0 of both operands: its conversion computes the
-    // per-row scales, which every other segment then uses
-    const int q0 = nseg - 1;
-    if ((st = tc_convert(kTcFP8, ta_rows, m, k, A, ldA, Ak + q0 * kp, ldw, sa, sia, s, kp))) return st;
-    if ((st = tc_convert(kTcFP8, tb_rows, n, k, B, ldB, Bk + q0 * kp, ldw, sb, sib, s, kp))) return st;
-    for (int q = 0; q < q0; ++q) {
-        if ((st = tc_convert(conv[tA[q]], ta_rows, m, k, A, ldA, Ak + q * kp, ldw, nullptr, sia, s, kp)))
-            return st;
-        if ((st = tc_convert(conv[tB[q]], tb_rows, n, k, B, ldB, Bk + q * kp, ldw, nullptr, sib, s, kp)))
-            return st;
-    }
+    if ((st = tc_convert_terms(true, ta_rows, m, k, A, ldA, Ak, ldw, kp, tA, sa, sia, s))) return st;
+    if ((st = tc_convert_terms(true, tb_rows, n, k, B, ldB, Bk, ldw, kp, tB, sb, sib, s))) return st;
     return tc_gemm_launch(kTcFP8, m, n, ldw, alpha, Ak, ldw, Bk, ldw, beta, C, ldC, sa, sb, s);
 }
 
