@@ -136,19 +136,18 @@ __device__ __forceinline__ void warp_argmax(unsigned long long &k, int &i) {
 // A points at the panel's top-left element A(j,j); the panel is mp x jb.
 // CTA b owns panel rows [b*R, min(mp,(b+1)*R)), kept in shared memory as
 // S[c*R + r].  With at most 128 rows a CTA gives each row W = 2, 4 or 8
-// lanes (interleaved columns) and defers most of each column's rank-1 update
-// past the next column's candidate search (see [E2] below); with more rows
-// thread t owns local rows t, t+256, ... and updates them at once.  Block
-// barriers per column: one to collect the warps' candidates, one after the
-// cross-CTA poll, one to hand the pivot to every thread.  Warp 0 does the
-// cross-CTA exchange.
-// Two builds: DEFER (the deferred update below, about 100 registers per
-// thread) for panels that run alone or beside a small update, and the
-// immediate update within 64 registers for panels beside a large look-ahead
-// GEMM (74 registers, 256 threads per CTA): at 102 registers only one GEMM
-// CTA fitted beside the panel instead of two (the n = 8192 LU: 325.9 against
-// 322.8 ms per solve), and capping the deferred build instead slowed the
-// split-update LU's panels by 11%.
+// lanes (interleaved columns); with more rows thread t owns local rows t,
+// t+256, ... and updates them at once.  Block barriers per column: one to
+// collect the warps' candidates, one after the cross-CTA poll, one to hand
+// the pivot to every thread.  Warp 0 does the cross-CTA exchange.
+// Two builds: DEFER (lanes per row and most of each column's rank-1 update
+// deferred past the next column's candidate search, see [E2] below; about
+// 120 registers per thread) for panels that run alone or beside a small
+// update, and the immediate update within 64 registers for panels beside a
+// large look-ahead GEMM (74 registers, 256 threads per CTA): at 102
+// registers only one GEMM CTA fitted beside the panel instead of two (the
+// n = 8192 LU: 325.9 against 322.8 ms per solve), and capping the deferred
+// build instead slowed the split-update LU's panels by 11%.
 template <typename T, bool DEFER>
 __global__ void __launch_bounds__(PANEL_THREADS, DEFER ? 1 : 4)
 panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
