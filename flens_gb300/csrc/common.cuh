@@ -355,6 +355,17 @@ int tc_trailing_update(int kind, int m, int n, int k, const float *A21, int ldA2
                        const float *U12, int ldU12, float *A22, int ldA22, void *buf,
                        cudaStream_t stream);
 
+// C = alpha * A * B + beta * C (FP32 storage, no transposes) as one
+// FP32-accurate 3xTF32 tensor-core GEMM; `buf` holds
+// tc_update_workspace_bytes(3, m, n, k) bytes.
+int tc_gemm_f32x3_nn(int m, int n, int k, float alpha, const float *A, int ldA, const float *B,
+                     int ldB, float beta, float *C, int ldC, void *buf, cudaStream_t stream);
+
+// y = A x for an n x n triangular FP64 A whose other triangle holds zeros
+// (uplo 'L' or 'U'): only the triangle is read, y is only written.
+int dtrmv_zeros_launch(char uplo, int n, const double *A, int lda, const double *x, double *y,
+                       cudaStream_t s);
+
 // Reads and clears the workspace status word for `stream` (synchronises).
 int check_device_status(cudaStream_t stream);
 

@@ -398,6 +398,47 @@ gemv_rows_kernel(int m, int n, int k, T alpha, const T *__restrict__ A, int ldA,
     }
 }
 
+// y = A x for a square FP64 A whose other triangle holds zeros (LOWER: the
+// lower triangle): the row-tile GEMV above with each CTA reading only the
+// columns its rows can touch, y stored without being read.  Row blocks are
+// taken longest first (reversed for the lower triangle), so the last wave
+// holds the short ones.  A separate kernel, so that the general one keeps
+// its registers (and residency).
+template <bool LOWER>
+__global__ void __launch_bounds__(256)
+gemv_tri_kernel(int n, const double *__restrict__ A, int ldA, const double *__restrict__ x,
+                double *__restrict__ y) {
+    constexpr int LR = 16;                       // rows per CTA = lanes per column
+    constexpr int G = 256 / LR;                  // column groups
+    __shared__ double red[G][LR];
+    const int r = threadIdx.x % LR, g = threadIdx.x / LR;
+    const int bx = LOWER ? (int)gridDim.x - 1 - (int)blockIdx.x : (int)blockIdx.x;
+    const int i = bx * LR + r;
+    const int kb = LOWER ? 0 : bx * LR;
+    const int ke = LOWER ? min(n, bx * LR + LR) : n;
+    double acc = 0.0;
+    if (i < n) {
+        const double *a = A + i;
+        int p = kb + g;
+        for (; p + (GV_UNROLL - 1) * G < ke; p += GV_UNROLL * G) {
+            double av[GV_UNROLL];
+#pragma unroll
+            for (int u = 0; u < GV_UNROLL; ++u) av[u] = __ldg(&a[(size_t)(p + u * G) * ldA]);
+#pragma unroll
+            for (int u = 0; u < GV_UNROLL; ++u) acc = fma(av[u], __ldg(&x[p + u * G]), acc);
+        }
+        for (; p < ke; p += G) acc = fma(__ldg(&a[(size_t)p * ldA]), __ldg(&x[p]), acc);
+    }
+    red[g][r] = acc;
+    __syncthreads();
+    if (threadIdx.x < LR && i - r + threadIdx.x < n) {
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < G; ++q) s += red[q][threadIdx.x];
+        y[bx * LR + threadIdx.x] = s;
+    }
+}
+
 template <typename T, int NC>
 void launch_gemv_rows(bool tb, int m, int n, int k, T alpha, const T *A, int ldA, const T *B,
                       int ldB, T beta, T *C, int ldC, cudaStream_t s) {
@@ -406,6 +447,25 @@ void launch_gemv_rows(bool tb, int m, int n, int k, T alpha, const T *A, int ldA
     if (tb) gemv_rows_kernel<T, NC, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
     else gemv_rows_kernel<T, NC, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC);
 }
+
+}  // namespace
+
+// y = A x for an n x n triangular FP64 A stored with zeros in its other
+// triangle (uplo 'L' or 'U'); only the triangle is read, y is not.  The
+// explicit-inverse preconditioner of the mixed solve.
+int dtrmv_zeros_launch(char uplo, int n, const double *A, int lda, const double *x, double *y,
+                       cudaStream_t s) {
+    if (n <= 0) return kOk;
+    constexpr int LR = 16;
+    const int grid = ceil_div(n, LR);
+    KTimer kt(kFamPrecond, s, (double)n * n, 4.0 * (double)n * n);
+    if (uplo == 'L') gemv_tri_kernel<true><<<grid, 256, 0, s>>>(n, A, lda, x, y);
+    else gemv_tri_kernel<false><<<grid, 256, 0, s>>>(n, A, lda, x, y);
+    FG_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+namespace {
 
 template <typename T, int NC>
 void launch_skinny(bool ta, bool tb, int m, int n, int k, T alpha, const T *A, int ldA,

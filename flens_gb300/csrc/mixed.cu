@@ -487,6 +487,7 @@ int gmres_restart() {
     }();
     return m;
 }
+constexpr int kPrecBF16 = 1, kPrecFP8 = 2, kPrec3xTF32 = 3, kPrecFP8x2 = 5;   // = the tensor-core kinds
 constexpr int kPrecSplit = 4;     // FP64 storage, split-GEMM trailing updates
 
 struct Solver {
@@ -523,7 +524,71 @@ struct Solver {
     unsigned long long *pcTag = nullptr;   // 2n tagged words: the solved blocks of a call
     unsigned pc_epoch = 0;
     bool pc = false;            // chained block-inverse preconditioner in use
+    // explicit-inverse preconditioner: L^-1 and U^-1 (FP64, n x n, zeros in
+    // the other triangle) and an n-vector between the two products
+    bool pcinv = false;
+    double *Linv = nullptr, *Uinv = nullptr, *pcTmp = nullptr;
 };
+
+// ---------------------------------------------------------------------------
+// Explicit-inverse preconditioner, for factors that need hundreds of GMRES
+// steps (BF16, FP8).  The chained solve above is bound by its 64-row
+// hand-offs (about 4 us each, 1.1 ms per triangle at n = 16384); with L^-1
+// and U^-1 formed once, each application is two triangle-aware FP64 GEMVs
+// (n^2/2 DFMA each, spread over every SM).  The inverses are formed from the
+// stored FP32 factors by 2 x 2 block recursion,
+//   [A 0; B C]^-1 = [A^-1 0; -C^-1 B A^-1  C^-1]  (and likewise for U),
+// with FP32-accurate products (3xTF32 on the tensor cores, FP32 FMAs for
+// small blocks) over 64 x 64 diagonal inverses taken in FP64, and are kept in
+// FP64.  Applying them is again a fixed linear operator -- an FP32-accurate
+// approximation of (LU)^-1, far closer than the factors are to A -- which is
+// what GMRES needs of its preconditioner.
+
+// The inverse of each 64 x 64 diagonal block of the stored triangle (unit
+// lower for LOWER, upper with its diagonal otherwise), in FP64 by
+// substitution, written rounded to FP32 into the same block of Inv.
+template <bool LOWER>
+__global__ void __launch_bounds__(PC_THREADS)
+inv_diag_kernel(int n, const float *__restrict__ F, int ldf, float *__restrict__ Inv, int ldi) {
+    extern __shared__ double pc_sm[];
+    double(*D)[PC_NB + 1] = (double(*)[PC_NB + 1])pc_sm;
+    double(*Y)[PC_NB + 1] = (double(*)[PC_NB + 1])(pc_sm + PC_NB * (PC_NB + 1));
+    const int b = blockIdx.x, tid = threadIdx.x;
+    const int R0 = b * PC_NB, kb = min(PC_NB, n - R0);
+    for (int e = tid; e < PC_NB * PC_NB; e += PC_THREADS) {
+        const int i = e % PC_NB, j = e / PC_NB;
+        double v = (i == j) ? 1.0 : 0.0;
+        if (i < kb && j < kb && (LOWER ? j < i : j >= i))
+            v = (double)F[(size_t)(R0 + i) + (size_t)(R0 + j) * ldf];
+        D[i][j] = v;
+    }
+    __syncthreads();
+    if (tid < PC_NB) {
+        const int c = tid;
+        if (LOWER) {
+            for (int i = 0; i < c; ++i) Y[i][c] = 0.0;
+            Y[c][c] = 1.0;
+            for (int i = c + 1; i < PC_NB; ++i) {
+                double s = 0.0;
+                for (int j = c; j < i; ++j) s = fma(D[i][j], Y[j][c], s);
+                Y[i][c] = -s;
+            }
+        } else {
+            for (int i = c + 1; i < PC_NB; ++i) Y[i][c] = 0.0;
+            Y[c][c] = 1.0 / D[c][c];
+            for (int i = c - 1; i >= 0; --i) {
+                double s = 0.0;
+                for (int j = i + 1; j <= c; ++j) s = fma(D[i][j], Y[j][c], s);
+                Y[i][c] = -s / D[i][i];
+            }
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < kb * kb; e += PC_THREADS) {
+        const int i = e % kb, j = e / kb;
+        Inv[(size_t)(R0 + i) + (size_t)(R0 + j) * ldi] = (float)Y[i][j];
+    }
+}
 
 // Whether the chained block-inverse preconditioner fits (every block of the
 // triangle resident at once for the cooperative launch).
@@ -574,6 +639,103 @@ int pc_solve(Solver &S, const MT *F, int ldf, bool lower, double *x) {
     KTimer kt(kFamPrecond, S.s, (double)n * n, (double)n * n * sizeof(MT) / 2.0 + 16.0 * n * PC_NB);
     const void *fn = lower ? (const void *)pc_chain_kernel<MT, true> : (const void *)pc_chain_kernel<MT, false>;
     FG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(nblk), dim3(PC_THREADS), args, 0, S.s));
+    return kOk;
+}
+
+// ---- explicit-inverse preconditioner: build ---------------------------------
+// Workspace of the build: the two FP32 inverses (ld ldi), the product
+// scratch T, the 3xTF32 operand buffers, the FP64 inverses and an n-vector.
+struct InvPlan {
+    int n, ldi, half;
+    size_t oL32, oU32, oT, oG, oL64, oU64, oTmp, total;
+};
+
+InvPlan inv_plan(int n) {
+    InvPlan p;
+    p.n = n;
+    p.ldi = (n + 3) / 4 * 4;
+    p.half = ((n + 1) / 2 + PC_NB - 1) / PC_NB * PC_NB;   // the largest block a product sees
+    const int th = (p.half + 3) / 4 * 4;
+    size_t o = 0;
+    p.oL32 = o; o += a256((size_t)p.ldi * n * sizeof(float));
+    p.oU32 = o; o += a256((size_t)p.ldi * n * sizeof(float));
+    p.oT = o;   o += a256((size_t)th * p.half * sizeof(float));
+    p.oG = o;   o += a256(tc_update_workspace_bytes(kPrec3xTF32, p.half, p.half, p.half));
+    p.oL64 = o; o += a256((size_t)n * n * sizeof(double));
+    p.oU64 = o; o += a256((size_t)n * n * sizeof(double));
+    p.oTmp = o; o += a256((size_t)n * sizeof(double));
+    p.total = o;
+    return p;
+}
+
+// C (m x n) = alpha * A (m x k) * B (k x n), FP32 storage, FP32-accurate:
+// 3xTF32 on the tensor cores, or FP32 FMAs on the CUDA cores for small blocks
+int inv_product(int m, int n, int k, float alpha, const float *A, int lda, const float *B, int ldb,
+                float *C, int ldc, void *gbuf, cudaStream_t s) {
+    if ((double)m * n * k < 256.0 * 256.0 * 256.0)
+        return sgemm_launch('N', 'N', m, n, k, alpha, A, lda, B, ldb, 0.0f, C, ldc, s);
+    return tc_gemm_f32x3_nn(m, n, k, alpha, A, lda, B, ldb, 0.0f, C, ldc, gbuf, s);
+}
+
+// Inv(r0:r0+sz, r0:r0+sz) = inverse of the stored triangle's diagonal block,
+// given the inverses of its 64 x 64 diagonal blocks already in place.
+int inv_recurse(bool lower, int r0, int sz, const float *F, int ldf, float *Inv, int ldi, float *T,
+                void *gbuf, cudaStream_t s) {
+    if (sz <= PC_NB) return kOk;
+    const int h = ((sz + 1) / 2 + PC_NB - 1) / PC_NB * PC_NB;   // h < sz, a multiple of 64
+    const int h2 = sz - h;
+    int st;
+    if ((st = inv_recurse(lower, r0, h, F, ldf, Inv, ldi, T, gbuf, s)) != kOk) return st;
+    if ((st = inv_recurse(lower, r0 + h, h2, F, ldf, Inv, ldi, T, gbuf, s)) != kOk) return st;
+    float *I11 = Inv + r0 + (size_t)r0 * ldi;
+    float *I22 = Inv + (r0 + h) + (size_t)(r0 + h) * ldi;
+    if (lower) {
+        // L^-1(21) = -L22^-1 L21 L11^-1
+        const int ldt = (h2 + 3) / 4 * 4;
+        const float *L21 = F + (r0 + h) + (size_t)r0 * ldf;
+        if ((st = inv_product(h2, h, h2, 1.0f, I22, ldi, L21, ldf, T, ldt, gbuf, s)) != kOk) return st;
+        return inv_product(h2, h, h, -1.0f, T, ldt, I11, ldi, Inv + (r0 + h) + (size_t)r0 * ldi, ldi,
+                           gbuf, s);
+    }
+    // U^-1(12) = -U11^-1 U12 U22^-1
+    const int ldt = (h + 3) / 4 * 4;
+    const float *U12 = F + r0 + (size_t)(r0 + h) * ldf;
+    if ((st = inv_product(h, h2, h, 1.0f, I11, ldi, U12, ldf, T, ldt, gbuf, s)) != kOk) return st;
+    return inv_product(h, h2, h2, -1.0f, T, ldt, I22, ldi, Inv + r0 + (size_t)(r0 + h) * ldi, ldi,
+                       gbuf, s);
+}
+
+// L^-1 and U^-1 of the FP32 factors into S.Linv / S.Uinv (FP64).
+int pcinv_prepare(Solver &S) {
+    const int n = S.n;
+    const InvPlan p = inv_plan(n);
+    char *base = (char *)workspace_slot(S.s, 3, p.total);
+    if (!base) return kErrAlloc;
+    float *L32 = (float *)(base + p.oL32), *U32 = (float *)(base + p.oU32), *T = (float *)(base + p.oT);
+    void *gbuf = base + p.oG;
+    S.Linv = (double *)(base + p.oL64);
+    S.Uinv = (double *)(base + p.oU64);
+    S.pcTmp = (double *)(base + p.oTmp);
+    static DeviceOnce onceL, onceU;
+    int st = set_smem_once(onceL, (const void *)inv_diag_kernel<true>, PC_PREP_SMEM);
+    if (st != kOk) return st;
+    if ((st = set_smem_once(onceU, (const void *)inv_diag_kernel<false>, PC_PREP_SMEM)) != kOk) return st;
+    const int nblk = ceil_div(n, PC_NB);
+    {
+        KTimer kt(kFamPrecond, S.s, 2.0 * nblk * PC_NB * PC_NB * PC_NB / 3.0, 8.0 * n * (double)p.ldi);
+        FG_CUDA(cudaMemsetAsync(L32, 0, (size_t)p.ldi * n * sizeof(float), S.s));
+        FG_CUDA(cudaMemsetAsync(U32, 0, (size_t)p.ldi * n * sizeof(float), S.s));
+        FG_CUDA(cudaMemsetAsync(T, 0, p.oG - p.oT, S.s));
+        inv_diag_kernel<true><<<nblk, PC_THREADS, PC_PREP_SMEM, S.s>>>(n, S.A32, S.ld32, L32, p.ldi);
+        inv_diag_kernel<false><<<nblk, PC_THREADS, PC_PREP_SMEM, S.s>>>(n, S.A32, S.ld32, U32, p.ldi);
+        FG_CUDA(cudaGetLastError());
+    }
+    if ((st = inv_recurse(true, 0, n, S.A32, S.ld32, L32, p.ldi, T, gbuf, S.s)) != kOk) return st;
+    if ((st = inv_recurse(false, 0, n, S.A32, S.ld32, U32, p.ldi, T, gbuf, S.s)) != kOk) return st;
+    KTimer kt(kFamAux, S.s, 0.0, 24.0 * n * (double)n);
+    s2d_matrix_kernel<<<grid_for((size_t)n * n), 256, 0, S.s>>>(n, L32, p.ldi, S.Linv, n);
+    s2d_matrix_kernel<<<grid_for((size_t)n * n), 256, 0, S.s>>>(n, U32, p.ldi, S.Uinv, n);
+    FG_CUDA(cudaGetLastError());
     return kOk;
 }
 
@@ -636,6 +798,11 @@ int precond64(Solver &S, const double *src, double *dst) {
         KTimer kt(kFamKrylov, S.s, 0.0, 20.0 * S.n);
         gather_perm_kernel<<<grid_for(S.n), 256, 0, S.s>>>(S.n, src, S.perm, dst);
         FG_CUDA(cudaGetLastError());
+    }
+    if (S.pcinv) {
+        int st = dtrmv_zeros_launch('L', S.n, S.Linv, S.n, dst, S.pcTmp, S.s);
+        if (st != kOk) return st;
+        return dtrmv_zeros_launch('U', S.n, S.Uinv, S.n, S.pcTmp, dst, S.s);
     }
     if (S.pc) {
         int st;
@@ -924,7 +1091,11 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
             if (!S.V) {
                 const size_t vB = a256((size_t)n * (M + 1) * sizeof(double));
                 const size_t nB = a256((size_t)n * sizeof(double));
-                S.pc = pc_fits(n, split);
+                // BF16 and FP8 factors: hundreds of GMRES steps, so the
+                // explicit inverses repay their formation (n >= 2048)
+                S.pcinv = !split && n >= 2048 &&
+                          (S.precision == kPrecBF16 || S.precision == kPrecFP8 || S.precision == kPrecFP8x2);
+                S.pc = !S.pcinv && pc_fits(n, split);
                 const size_t pB = S.pc ? pc_block_bytes(n) : 0;
                 const size_t tB = S.pc ? a256(2 * sizeof(unsigned long long) * (size_t)n) : 0;
                 char *p2 = (char *)workspace_slot(s, 2, vB + 2 * nB + 4 * pB + tB);
@@ -942,6 +1113,8 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
                     FG_CUDA(cudaMemsetAsync(S.pcTag, 0, tB, s));
                     st = split ? pc_prepare<double>(S, S.LU64, n) : pc_prepare<float>(S, S.A32, S.ld32);
                     if (st != kOk) return st;
+                } else if (S.pcinv) {
+                    if ((st = pcinv_prepare(S)) != kOk) return st;
                 } else if (!split) {
                     S.LU64 = (double *)workspace_slot(s, 3, (size_t)n * n * sizeof(double));
                     if (!S.LU64) return kErrAlloc;

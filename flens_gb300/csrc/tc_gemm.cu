@@ -476,6 +476,12 @@ int fp8_terms_gemm(int nterms, bool ta_rows, bool tb_rows, int m, int n, int k, 
 
 }  // namespace
 
+int tc_gemm_f32x3_nn(int m, int n, int k, float alpha, const float *A, int ldA, const float *B,
+                     int ldB, float beta, float *C, int ldC, void *buf, cudaStream_t stream) {
+    if (m <= 0 || n <= 0 || k <= 0) return kOk;
+    return f32x3_gemm(false, true, m, n, k, alpha, A, ldA, B, ldB, beta, C, ldC, buf, stream);
+}
+
 int tc_trailing_update(int kind, int m, int n, int k, const float *A21, int ldA21,
                        const float *U12, int ldU12, float *A22, int ldA22, void *buf,
                        cudaStream_t stream) {

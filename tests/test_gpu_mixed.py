@@ -263,3 +263,58 @@ def test_mixed_fp8x3_converges_where_fp8_cannot(cuda):
     assert backward_error(A, X, b) <= 10 * n * EPS
     st1, _, it1, be1, _ = dgesv_mixed(A, b, "fp8", "auto", max_iter=4)
     assert st1 == fg.ERR_NOT_CONVERGED and be1 > 10 * n * EPS
+
+
+@pytest.mark.parametrize("m,n", [(700, 300), (300, 700), (257, 257), (1000, 1000), (64, 64), (65, 130)])
+@pytest.mark.parametrize("prec", [-1, 3, 1])
+def test_sgetrf_tc_shapes(cuda, m, n, prec):
+    """flens_gb300_sgetrf_tc on rectangular and ragged shapes (outer blocks
+    of 256 columns cut short by min(m, n) or by n, panels narrower than 64):
+    P A = L U with a backward error at the precision's level, unit lower L
+    below the diagonal of the first min(m, n) columns, pivots in range."""
+    import torch
+    g = torch.Generator(device=cuda)
+    g.manual_seed(m * 7 + n)
+    A = (torch.rand((m, n), generator=g, dtype=torch.float64, device=cuda) * 2 - 1)
+    ld = m + 3                                   # a leading dimension beyond m
+    buf = torch.zeros((n, ld), dtype=torch.float32, device=cuda)
+    F = buf.t()[:m, :]                           # m x n view, column stride ld
+    F.copy_(A.to(torch.float32))
+    mn = min(m, n)
+    ipiv = torch.zeros(mn, dtype=torch.int32, device=cuda)
+    info = torch.zeros(1, dtype=torch.int32, device=cuda)
+    f = fg.lib().flens_gb300_sgetrf_tc
+    f.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3
+    st = f(prec, m, n, buf.data_ptr(), ld, ipiv.data_ptr(), info.data_ptr(),
+           ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    assert st == 0 and int(info.item()) == 0, (st, fg.last_error())
+    pv = ipiv.cpu().numpy()
+    assert (pv >= np.arange(1, mn + 1)).all() and (pv <= m).all()
+    perm = list(range(m))
+    for i, p in enumerate(pv):
+        perm[i], perm[p - 1] = perm[p - 1], perm[i]
+    Fd = F.double()
+    L = torch.tril(Fd, -1)[:, :mn] + torch.eye(m, mn, dtype=torch.float64, device=cuda)
+    U = torch.triu(Fd)[:mn, :]
+    err = ((A[perm] - L @ U).norm() / A.norm()).item()
+    bound = {-1: 1e-5, 3: 1e-5, 1: 0.25}[prec]     # BF16: gross errors only
+    assert err <= bound, (m, n, prec, err)
+    # the padding rows beyond m are untouched
+    assert (buf.t()[m:, :] == 0).all()
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp8x2"])
+def test_mixed_explicit_inverse_preconditioner(cuda, prec):
+    """BF16 and FP8 factors at n >= 2048 take GMRES with the explicit-inverse
+    preconditioner (L^-1, U^-1 formed once by 3xTF32 block recursion, applied
+    as FP64 products); the solve must reach 10 n eps as with the chained
+    substitution (17 and 22 steps at this size, kappa = 1e2)."""
+    n = 2048
+    A, b, x = make_system(cuda, n, 1e2, 1, 23)
+    st, X, it, be, inf = dgesv_mixed(A, b, prec, "auto")
+    assert st == 0 and inf == 0, (st, fg.last_error(), it, be)
+    assert it <= 60, it
+    assert backward_error(A, X, b) <= 10 * n * EPS
+    fwd = ((X - x).abs().max() / x.abs().max()).item()
+    assert fwd <= 1e2 * 1e3 * EPS, fwd
