@@ -1092,9 +1092,16 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
                 const size_t vB = a256((size_t)n * (M + 1) * sizeof(double));
                 const size_t nB = a256((size_t)n * sizeof(double));
                 // BF16 and FP8 factors: hundreds of GMRES steps, so the
-                // explicit inverses repay their formation (n >= 2048)
+                // explicit inverses repay their formation (n >= 2048); their
+                // workspace is taken first, and without it the chained
+                // preconditioner serves instead
                 S.pcinv = !split && n >= 2048 &&
                           (S.precision == kPrecBF16 || S.precision == kPrecFP8 || S.precision == kPrecFP8x2);
+                if (S.pcinv && !workspace_slot(s, 3, inv_plan(n).total)) {
+                    cudaGetLastError();
+                    trace("dgesv_mixed: no memory for the explicit inverses, chained preconditioner");
+                    S.pcinv = false;
+                }
                 S.pc = !S.pcinv && pc_fits(n, split);
                 const size_t pB = S.pc ? pc_block_bytes(n) : 0;
                 const size_t tB = S.pc ? a256(2 * sizeof(unsigned long long) * (size_t)n) : 0;

@@ -182,3 +182,44 @@ def test_bounded_wait_timeout_then_healthy(cuda):
     fg.sync()
     x = np.linalg.solve(A0, b0)
     assert oracle.normwise_rel(b.cpu().numpy(), x) <= 1e-12
+
+
+def test_mixed_inverse_preconditioner_falls_back_without_memory(cuda):
+    # BF16 factors at n >= 2048 take GMRES with explicit inverses of L and U,
+    # whose workspace is requested first; when that allocation fails the
+    # solve must fall back to the chained preconditioner and still converge.
+    # A GMRES-IR solve with 3xTF32 factors on the same (fresh) stream first
+    # sizes every other workspace, so the next allocation is the inverses'.
+    import torch
+    from test_gpu_mixed import make_system, backward_error, PREC, SOLVER, EPS
+    n = 2048
+    A, b, x = make_system(cuda, n, 1e2, 1, 31)
+    s = torch.cuda.Stream()
+    f = fg.lib().flens_gb300_dgesv_mixed
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
+                  ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
+
+    def solve(prec, solver):
+        X = fg.colmajor_empty(n, 1, device=cuda)
+        it, be, inf = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
+        st = f(n, 1, A.data_ptr(), n, b.data_ptr(), n, X.data_ptr(), n, PREC[prec], SOLVER[solver],
+               30, 0.0, ctypes.byref(it), ctypes.byref(be), ctypes.byref(inf),
+               ctypes.c_void_p(s.cuda_stream))
+        s.synchronize()
+        return st, X, it.value
+
+    st, X, it = solve("fp32", "gmres")
+    assert st == 0, fg.last_error()
+    count = fg.lib().flens_gb300_device_alloc_count
+    count.restype = ctypes.c_longlong
+    before = count()
+    _fail_next(1)
+    try:
+        st, X, it = solve("bf16", "auto")
+    finally:
+        _fail_next(0)
+    assert st == 0, (st, fg.last_error(), it)
+    assert count() == before                    # the one allocation it tried was refused
+    assert backward_error(A, X, b) <= 10 * n * EPS
