@@ -48,6 +48,14 @@ def lu_block_flops(n: int, nblocks: int | None = None) -> float:
     return fl
 
 
+def l2_note(n: int, what: str = "input") -> str:
+    """The L2 line of a config: the size of an n x n FP64 matrix against the
+    129 MB L2 (below it, every step would re-read it from L2)."""
+    mib = 8.0 * n * n / 2 ** 20
+    rel = ">" if 8.0 * n * n > 129e6 else "<"
+    return f"{what} {mib:.0f} MiB {rel} L2"
+
+
 def lu_step_flops(n: int, b: int) -> float:
     """Flops of block step b (nb = 64) of the n x n blocked LU."""
     r = n - NB * b
@@ -180,7 +188,7 @@ def reference_arm(args, rank: int) -> None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (splitmix64 uniform[-1,1] + n/4 diagonal, seeded)",
         "config": {"workload": f"dgetrf+dgetrs n={n} 1 rhs FP64 column-major", "n": n,
-                   "nrhs": 1, "l2": "input 512 MiB > L2"},
+                   "nrhs": 1, "l2": l2_note(n)},
         "cpu_baseline": {
             "value": value, "unit": UNIT, "cores": threads, "kind": kind,
             "sample": (f"step s: {threads} threads each run block step {blocks}[s mod {len(blocks)}] "
@@ -330,7 +338,7 @@ def our_arm(args, rank: int, world: int) -> None:
                  if args.unshifted else "synthetic (torch seeded uniform[-1,1] + n/4 diagonal; b = A x_true)"),
         "config": {"workload": f"dgetrf+dgetrs n={n} 1 rhs FP64 column-major",
                    "n": n, "nrhs": 1, "nb": NB, "parallelism": f"replicas x{world}",
-                   "l2": "input 512 MiB > L2 (no flush)",
+                   "l2": l2_note(n) + " (no flush)",
                    "step": "A,b restored from pristine copies + dgetrf + dgetrs"},
         "gpu_launches": launches,
         "accuracy": {"info": inf, "pivots_identity": pivots_identity,
@@ -593,7 +601,7 @@ def split_subbench(torch, fg, dev, n=8192, Es=(0, 16, 48), reps=5, ref_slices=14
     import numpy as np
     peak, peak_src = measured_peak("bf16_tflops")
     out = {"workload": f"dgemm {n}^3 FP64 in/out, entries u*2^e, e in [-E,E]",
-           "fp64_equivalent_flops": 2.0 * n ** 3, "l2": "inputs 512 MiB each > L2 (no flush)",
+           "fp64_equivalent_flops": 2.0 * n ** 3, "l2": l2_note(n, "inputs, each") + " (no flush)",
            "accuracy_reference": f"same kernel with {ref_slices} slices ({7 * ref_slices} bits)",
            "per_E": {}}
     stream = torch.cuda.current_stream()
