@@ -49,6 +49,7 @@ def test_alloc_failure_device_api_then_recovers(cuda):
     ipiv = torch.zeros(n, dtype=torch.int32, device=cuda)
     info = torch.zeros(1, dtype=torch.int32, device=cuda)
     s = torch.cuda.Stream()                       # a stream without a workspace yet
+    s.wait_stream(torch.cuda.current_stream())    # dA, ipiv, info are made there
     _fail_next(1)
     try:
         with pytest.raises(fg.FlensGB300Error) as e:
@@ -60,6 +61,7 @@ def test_alloc_failure_device_api_then_recovers(cuda):
     fg.dgetrf_dev(dA, ipiv, info, stream=s)
     b0 = oracle.uniform(76, n, 1)
     b = fg.to_colmajor(torch.from_numpy(b0).to(cuda))
+    s.wait_stream(torch.cuda.current_stream())
     fg.dgetrs_dev("N", dA, ipiv, b, stream=s)
     fg.sync(s)
     assert int(info.item()) == 0
@@ -106,6 +108,7 @@ def test_alloc_failure_split_gemm(cuda):
     C = fg.colmajor_empty(m, n, device=cuda)
     C.zero_()
     s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())    # A, B, C are made there
     _fail_next(1)
     try:
         with pytest.raises(fg.FlensGB300Error) as e:
@@ -114,6 +117,7 @@ def test_alloc_failure_split_gemm(cuda):
     finally:
         _fail_next(0)
     fg.dgemm_split_dev("N", "N", 1.0, A, B, 0.0, C, stream=s)
+    fg.sync(s)                                    # C is read on the current stream below
     ref = A @ B
     assert ((C - ref).abs().max() / ref.abs().max()).item() <= 1e-13
 
@@ -195,6 +199,7 @@ def test_mixed_inverse_preconditioner_falls_back_without_memory(cuda):
     n = 2048
     A, b, x = make_system(cuda, n, 1e2, 1, 31)
     s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())    # A and b are made there
     f = fg.lib().flens_gb300_dgesv_mixed
     f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                   ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
