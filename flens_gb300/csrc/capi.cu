@@ -1305,6 +1305,26 @@ FG_API int flens_gb300_sgetrf_tc(int precision, int m, int n, float *A, int ldA,
     return sgetrf_launch(m, n, A, ldA, ipiv, info, precision, as_stream(stream));
 }
 
+// Test hook: the mixed solve's explicit-inverse preconditioner GEMV on its
+// own (y = A x over one triangle of A, the other triangle holding zeros).
+// With part == NULL it only reports the scratch sizes the call needs.
+FG_API int flens_gb300_test_trmv_zeros(char uplo, int n, const double *A, int ldA, const double *x,
+                                       double *y, double *part, unsigned *cnt, size_t *part_elems,
+                                       size_t *cnt_elems, void *stream) {
+    uplo = (char)toupper(uplo);
+    if (uplo != 'L' && uplo != 'U') return -1;
+    if (n < 0) return -2;
+    if (ldA < std::max(1, n)) return -4;
+    if (part_elems) *part_elems = dtrmv_zeros_part_elems(n);
+    if (cnt_elems) *cnt_elems = dtrmv_zeros_cnt_elems(n);
+    if (!part) return kOk;
+    if (num_sms() <= 0) {
+        set_last_error("no CUDA device");
+        return kErrNoDevice;
+    }
+    return dtrmv_zeros_launch(uplo, n, A, ldA, x, y, part, cnt, as_stream(stream));
+}
+
 FG_API int flens_gb300_dgetrs(char trans, int n, int nrhs, const double *A, int ldA,
                               const int *ipiv, double *B, int ldB, void *stream) {
     trans = (char)toupper(trans);

@@ -362,9 +362,14 @@ int tc_gemm_f32x3_nn(int m, int n, int k, float alpha, const float *A, int ldA, 
                      int ldB, float beta, float *C, int ldC, void *buf, cudaStream_t stream);
 
 // y = A x for an n x n triangular FP64 A whose other triangle holds zeros
-// (uplo 'L' or 'U'): only the triangle is read, y is only written.
+// (uplo 'L' or 'U'): only the triangle and the zeros inside its 16 x 16
+// diagonal blocks are read, y is only written.  Scratch:
+// `part` of dtrmv_zeros_part_elems(n) doubles and `cnt` of
+// dtrmv_zeros_cnt_elems(n) counters, zeroed once before the first call.
+size_t dtrmv_zeros_part_elems(int n);
+size_t dtrmv_zeros_cnt_elems(int n);
 int dtrmv_zeros_launch(char uplo, int n, const double *A, int lda, const double *x, double *y,
-                       cudaStream_t s);
+                       double *part, unsigned *cnt, cudaStream_t s);
 
 // Reads and clears the workspace status word for `stream` (synchronises).
 int check_device_status(cudaStream_t stream);

@@ -399,43 +399,77 @@ gemv_rows_kernel(int m, int n, int k, T alpha, const T *__restrict__ A, int ldA,
 }
 
 // y = A x for a square FP64 A whose other triangle holds zeros (LOWER: the
-// lower triangle): the row-tile GEMV above with each CTA reading only the
-// columns its rows can touch, y stored without being read.  Row blocks are
-// taken longest first (reversed for the lower triangle), so the last wave
-// holds the short ones.  A separate kernel, so that the general one keeps
-// its registers (and residency).
+// lower triangle), reading only the triangle and its 16 x 16 diagonal
+// blocks.  The rows go in blocks of 16
+// (one 128-byte line of each column); a row block's columns -- [0, i0 + 16)
+// below the diagonal, [i0, n) above it -- are cut into chunks of `ch`
+// columns, and CTA (row block, chunk) sums its chunk with the row-tile
+// GEMV's thread layout (16 column groups, 8 loads in flight per thread).
+// Every CTA but a row block's last chunk has the same work, so the SMs
+// finish together; with one CTA per whole row block the lengths run from 16
+// to n columns and a quarter of the elapsed time the SMs idled in the
+// ragged last wave.  A row block with one chunk stores y directly; with
+// more, each chunk stores its 16 sums in part[c * n + i] and the CTA that
+// finishes the row block last (a counter per row block, reset by that CTA)
+// adds them in chunk order, so y does not depend on the CTAs' timing.
+// A separate kernel, so that the general one keeps its registers (and
+// residency).
 template <bool LOWER>
 __global__ void __launch_bounds__(256)
-gemv_tri_kernel(int n, const double *__restrict__ A, int ldA, const double *__restrict__ x,
-                double *__restrict__ y) {
+gemv_tri_kernel(int n, int ch, const double *__restrict__ A, int ldA, const double *__restrict__ x,
+                double *__restrict__ y, double *__restrict__ part, unsigned *__restrict__ cnt) {
     constexpr int LR = 16;                       // rows per CTA = lanes per column
     constexpr int G = 256 / LR;                  // column groups
     __shared__ double red[G][LR];
+    __shared__ int s_last;
+    const int rb = blockIdx.x, c = blockIdx.y;
+    const int i0 = rb * LR;
+    const int kb = LOWER ? 0 : i0;
+    const int ke = LOWER ? min(n, i0 + LR) : n;
+    const int nch = (ke - kb + ch - 1) / ch;
+    if (c >= nch) return;                        // uniform over the CTA
+    const int cb = kb + c * ch, ce = min(ke, cb + ch);
     const int r = threadIdx.x % LR, g = threadIdx.x / LR;
-    const int bx = LOWER ? (int)gridDim.x - 1 - (int)blockIdx.x : (int)blockIdx.x;
-    const int i = bx * LR + r;
-    const int kb = LOWER ? 0 : bx * LR;
-    const int ke = LOWER ? min(n, bx * LR + LR) : n;
+    const int i = i0 + r;
     double acc = 0.0;
     if (i < n) {
         const double *a = A + i;
-        int p = kb + g;
-        for (; p + (GV_UNROLL - 1) * G < ke; p += GV_UNROLL * G) {
+        int p = cb + g;
+        for (; p + (GV_UNROLL - 1) * G < ce; p += GV_UNROLL * G) {
             double av[GV_UNROLL];
 #pragma unroll
             for (int u = 0; u < GV_UNROLL; ++u) av[u] = __ldg(&a[(size_t)(p + u * G) * ldA]);
 #pragma unroll
             for (int u = 0; u < GV_UNROLL; ++u) acc = fma(av[u], __ldg(&x[p + u * G]), acc);
         }
-        for (; p < ke; p += G) acc = fma(__ldg(&a[(size_t)p * ldA]), __ldg(&x[p]), acc);
+        for (; p < ce; p += G) acc = fma(__ldg(&a[(size_t)p * ldA]), __ldg(&x[p]), acc);
     }
     red[g][r] = acc;
     __syncthreads();
-    if (threadIdx.x < LR && i - r + threadIdx.x < n) {
+    const int ii = i0 + (int)threadIdx.x;
+    if (threadIdx.x < LR && ii < n) {
         double s = 0.0;
 #pragma unroll
         for (int q = 0; q < G; ++q) s += red[q][threadIdx.x];
-        y[bx * LR + threadIdx.x] = s;
+        if (nch == 1) {
+            y[ii] = s;
+        } else {
+            part[(size_t)c * n + ii] = s;
+            __threadfence();                     // before this chunk is counted
+        }
+    }
+    if (nch == 1) return;
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&cnt[rb], 1u) == (unsigned)(nch - 1);
+    __syncthreads();
+    if (s_last && threadIdx.x < LR) {
+        __threadfence();
+        if (ii < n) {
+            double s = 0.0;
+            for (int cc = 0; cc < nch; ++cc) s += __ldcg(&part[(size_t)cc * n + ii]);
+            y[ii] = s;
+        }
+        if (threadIdx.x == 0) cnt[rb] = 0u;      // ready for the next launch
     }
 }
 
@@ -451,16 +485,32 @@ void launch_gemv_rows(bool tb, int m, int n, int k, T alpha, const T *A, int ldA
 }  // namespace
 
 // y = A x for an n x n triangular FP64 A stored with zeros in its other
-// triangle (uplo 'L' or 'U'); only the triangle is read, y is not.  The
-// explicit-inverse preconditioner of the mixed solve.
+// triangle (uplo 'L' or 'U'); only the triangle and the zeros inside its
+// 16 x 16 diagonal blocks are read, y is not.  The
+// explicit-inverse preconditioner of the mixed solve.  `part` holds
+// dtrmv_zeros_part_elems(n) doubles and `cnt` dtrmv_zeros_cnt_elems(n)
+// counters, zero before the first call (each call leaves them zero).
+static int dtrmv_zeros_chunk(int n) {
+    // about 32 equal CTAs per SM over the n^2/2 triangle, at least 256 columns
+    const int sms = num_sms() > 0 ? num_sms() : 1;
+    const double per = (double)n * n / 2.0 / (16.0 * 32.0 * sms);
+    int ch = ((int)per + 15) / 16 * 16;
+    return ch < 256 ? 256 : ch;
+}
+size_t dtrmv_zeros_part_elems(int n) {
+    return n <= 0 ? 0 : (size_t)ceil_div(n, dtrmv_zeros_chunk(n)) * n;
+}
+size_t dtrmv_zeros_cnt_elems(int n) { return n <= 0 ? 0 : (size_t)ceil_div(n, 16); }
+
 int dtrmv_zeros_launch(char uplo, int n, const double *A, int lda, const double *x, double *y,
-                       cudaStream_t s) {
+                       double *part, unsigned *cnt, cudaStream_t s) {
     if (n <= 0) return kOk;
     constexpr int LR = 16;
-    const int grid = ceil_div(n, LR);
+    const int ch = dtrmv_zeros_chunk(n);
+    const dim3 grid(ceil_div(n, LR), ceil_div(n, ch));
     KTimer kt(kFamPrecond, s, (double)n * n, 4.0 * (double)n * n);
-    if (uplo == 'L') gemv_tri_kernel<true><<<grid, 256, 0, s>>>(n, A, lda, x, y);
-    else gemv_tri_kernel<false><<<grid, 256, 0, s>>>(n, A, lda, x, y);
+    if (uplo == 'L') gemv_tri_kernel<true><<<grid, 256, 0, s>>>(n, ch, A, lda, x, y, part, cnt);
+    else gemv_tri_kernel<false><<<grid, 256, 0, s>>>(n, ch, A, lda, x, y, part, cnt);
     FG_CUDA(cudaGetLastError());
     return kOk;
 }

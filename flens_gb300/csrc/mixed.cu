@@ -528,6 +528,8 @@ struct Solver {
     // the other triangle) and an n-vector between the two products
     bool pcinv = false;
     double *Linv = nullptr, *Uinv = nullptr, *pcTmp = nullptr;
+    double *pcPart = nullptr;                 // triangle GEMV chunk sums
+    unsigned *pcCnt = nullptr;                // and its per-row-block counters
 };
 
 // ---------------------------------------------------------------------------
@@ -644,10 +646,11 @@ int pc_solve(Solver &S, const MT *F, int ldf, bool lower, double *x) {
 
 // ---- explicit-inverse preconditioner: build ---------------------------------
 // Workspace of the build: the two FP32 inverses (ld ldi), the product
-// scratch T, the 3xTF32 operand buffers, the FP64 inverses and an n-vector.
+// scratch T, the 3xTF32 operand buffers, the FP64 inverses, an n-vector and
+// the triangle GEMV's chunk sums and counters.
 struct InvPlan {
     int n, ldi, half;
-    size_t oL32, oU32, oT, oG, oL64, oU64, oTmp, total;
+    size_t oL32, oU32, oT, oG, oL64, oU64, oTmp, oPart, oCnt, total;
 };
 
 InvPlan inv_plan(int n) {
@@ -664,6 +667,8 @@ InvPlan inv_plan(int n) {
     p.oL64 = o; o += a256((size_t)n * n * sizeof(double));
     p.oU64 = o; o += a256((size_t)n * n * sizeof(double));
     p.oTmp = o; o += a256((size_t)n * sizeof(double));
+    p.oPart = o; o += a256(dtrmv_zeros_part_elems(n) * sizeof(double));
+    p.oCnt = o; o += a256(dtrmv_zeros_cnt_elems(n) * sizeof(unsigned));
     p.total = o;
     return p;
 }
@@ -716,6 +721,9 @@ int pcinv_prepare(Solver &S) {
     S.Linv = (double *)(base + p.oL64);
     S.Uinv = (double *)(base + p.oU64);
     S.pcTmp = (double *)(base + p.oTmp);
+    S.pcPart = (double *)(base + p.oPart);
+    S.pcCnt = (unsigned *)(base + p.oCnt);
+    FG_CUDA(cudaMemsetAsync(S.pcCnt, 0, dtrmv_zeros_cnt_elems(n) * sizeof(unsigned), S.s));
     static DeviceOnce onceL, onceU;
     int st = set_smem_once(onceL, (const void *)inv_diag_kernel<true>, PC_PREP_SMEM);
     if (st != kOk) return st;
@@ -800,9 +808,9 @@ int precond64(Solver &S, const double *src, double *dst) {
         FG_CUDA(cudaGetLastError());
     }
     if (S.pcinv) {
-        int st = dtrmv_zeros_launch('L', S.n, S.Linv, S.n, dst, S.pcTmp, S.s);
+        int st = dtrmv_zeros_launch('L', S.n, S.Linv, S.n, dst, S.pcTmp, S.pcPart, S.pcCnt, S.s);
         if (st != kOk) return st;
-        return dtrmv_zeros_launch('U', S.n, S.Uinv, S.n, S.pcTmp, dst, S.s);
+        return dtrmv_zeros_launch('U', S.n, S.Uinv, S.n, S.pcTmp, dst, S.pcPart, S.pcCnt, S.s);
     }
     if (S.pc) {
         int st;

@@ -454,6 +454,18 @@ long long flens_gb300_device_alloc_count(void);
  * count <= 0 clears it. */
 void flens_gb300_test_fail_device_allocs(int count);
 
+/* Test hook: the mixed solve's explicit-inverse preconditioner product on its
+ * own, y = A x for an n x n FP64 A whose other triangle (uplo 'L': above the
+ * diagonal, 'U': below) holds zeros; only the triangle and the zeros inside
+ * its 16 x 16 diagonal blocks are read.  Scratch
+ * `part` (*part_elems doubles) and `cnt` (*cnt_elems counters, zero before
+ * the first call; every call leaves them zero).  With part == NULL the call
+ * only reports the two sizes.  Returns 0, -1/-2/-4 for uplo/n/ldA, or a
+ * FLENS_GB300_ERR_* code.  Async on stream. */
+int flens_gb300_test_trmv_zeros(char uplo, int n, const double *A, int ldA, const double *x,
+                                double *y, double *part, unsigned *cnt, size_t *part_elems,
+                                size_t *cnt_elems, void *stream);
+
 /* Launch accounting: kernel launches issued since load; per-family CUDA-event
  * timing on the launching streams (enable clears the totals; read waits for
  * the recorded events and returns -1 for an unknown family); family names. */

@@ -320,6 +320,29 @@ def test_sgetrf_tc_argument_errors(flib):
     assert f(-1, 4, 4, None, 3, None, None, None) == -5
 
 
+def _trmv_hook(flib):
+    f = flib.flens_gb300_test_trmv_zeros
+    f.argtypes = [ctypes.c_char, ctypes.c_int, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 7
+    return f
+
+
+def test_trmv_zeros_hook_arguments_and_scratch_sizes(flib):
+    f = _trmv_hook(flib)
+    assert f(b"X", 4, None, 4, None, None, None, None, None, None, None) == -1
+    assert f(b"L", -1, None, 4, None, None, None, None, None, None, None) == -2
+    assert f(b"U", 4, None, 3, None, None, None, None, None, None, None) == -4
+    # the size query needs no device: one counter per 16-row block and, per
+    # row, one partial sum for each chunk of the longest row (chunks of at
+    # least 256 columns)
+    pe, ce = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    for n in (1, 16, 17, 256, 257, 2048):
+        assert f(b"l", n, None, n, None, None, None, None, ctypes.byref(pe), ctypes.byref(ce), None) == 0
+        assert ce.value == -(-n // 16)
+        assert n <= pe.value <= n * -(-n // 256)
+    assert f(b"U", 0, None, 1, None, None, None, None, ctypes.byref(pe), ctypes.byref(ce), None) == 0
+    assert pe.value == 0 and ce.value == 0
+
+
 def test_no_gpu_fails_loudly():
     import torch
     if torch.cuda.is_available():

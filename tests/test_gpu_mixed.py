@@ -318,3 +318,43 @@ def test_mixed_explicit_inverse_preconditioner(cuda, prec):
     assert backward_error(A, X, b) <= 10 * n * EPS
     fwd = ((X - x).abs().max() / x.abs().max()).item()
     assert fwd <= 1e2 * 1e3 * EPS, fwd
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+@pytest.mark.parametrize("n", [1, 17, 300, 2048, 5000])
+def test_triangle_gemv_of_the_explicit_inverse(cuda, uplo, n):
+    """The preconditioner's product y = T x over one triangle T (the other
+    holding zeros): equal to the FP64 product to rounding, bitwise the same
+    on a repeated call (the chunk sums of a row block are added in chunk
+    order whatever the CTAs' timing), and the row blocks' counters back at
+    zero after each call.  The kernel reads the triangle and the zeros of its
+    16 x 16 diagonal blocks, nothing else: the rest of the other triangle is
+    NaN here."""
+    import torch
+    g = torch.Generator(device=cuda).manual_seed(n)
+    T = torch.rand((n, n), generator=g, dtype=torch.float64, device=cuda) * 2 - 1
+    T = torch.tril(T) if uplo == "L" else torch.triu(T)
+    i = torch.arange(n, device=cuda).view(-1, 1) // 16
+    j = torch.arange(n, device=cuda).view(1, -1) // 16
+    read = (j <= i) if uplo == "L" else (j >= i)
+    Tp = fg.to_colmajor(torch.where(read, T, torch.full_like(T, float("nan"))))
+    x = torch.rand(n, generator=g, dtype=torch.float64, device=cuda) * 2 - 1
+    f = fg.lib().flens_gb300_test_trmv_zeros
+    f.argtypes = [ctypes.c_char, ctypes.c_int, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 7
+    pe, ce = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    assert f(uplo.encode(), n, None, n, None, None, None, None, ctypes.byref(pe), ctypes.byref(ce), None) == 0
+    part = torch.zeros(max(pe.value, 1), dtype=torch.float64, device=cuda)
+    cnt = torch.zeros(max(ce.value, 1), dtype=torch.int32, device=cuda)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ys = []
+    for _ in range(2):
+        y = torch.full((n,), float("nan"), dtype=torch.float64, device=cuda)
+        assert f(uplo.encode(), n, Tp.data_ptr(), Tp.stride(1), x.data_ptr(), y.data_ptr(),
+                 part.data_ptr(), cnt.data_ptr(), None, None, stream) == 0
+        torch.cuda.synchronize()
+        assert int(cnt.abs().sum()) == 0
+        ys.append(y.cpu().numpy())
+    want = T.cpu().numpy() @ x.cpu().numpy()
+    scale = np.abs(T.cpu().numpy()) @ np.abs(x.cpu().numpy())
+    assert np.all(np.abs(ys[0] - want) <= 4 * n * EPS * scale + 1e-300)
+    np.testing.assert_array_equal(ys[0], ys[1])
