@@ -1305,14 +1305,15 @@ FG_API int flens_gb300_sgetrf_tc(int precision, int m, int n, float *A, int ldA,
     return sgetrf_launch(m, n, A, ldA, ipiv, info, precision, as_stream(stream));
 }
 
-// Test hook: the mixed solve's explicit-inverse preconditioner GEMV on its
-// own (y = A x over one triangle of A, the other triangle holding zeros).
-// With part == NULL it only reports the scratch sizes the call needs.
+// Test hook: the mixed solve's chunked GEMVs on their own: y = A x over one
+// triangle of A, the other triangle holding zeros (uplo 'L' or 'U', the
+// explicit-inverse preconditioner), or over all of A (uplo 'G', the Arnoldi
+// product).  With part == NULL it only reports the scratch sizes.
 FG_API int flens_gb300_test_trmv_zeros(char uplo, int n, const double *A, int ldA, const double *x,
                                        double *y, double *part, unsigned *cnt, size_t *part_elems,
                                        size_t *cnt_elems, void *stream) {
     uplo = (char)toupper(uplo);
-    if (uplo != 'L' && uplo != 'U') return -1;
+    if (uplo != 'L' && uplo != 'U' && uplo != 'G') return -1;
     if (n < 0) return -2;
     if (ldA < std::max(1, n)) return -4;
     if (part_elems) *part_elems = dtrmv_zeros_part_elems(n);
@@ -1322,6 +1323,7 @@ FG_API int flens_gb300_test_trmv_zeros(char uplo, int n, const double *A, int ld
         set_last_error("no CUDA device");
         return kErrNoDevice;
     }
+    if (uplo == 'G') return dgemv_chunk_launch(n, A, ldA, x, y, part, cnt, as_stream(stream));
     return dtrmv_zeros_launch(uplo, n, A, ldA, x, y, part, cnt, as_stream(stream));
 }
 

@@ -370,6 +370,9 @@ size_t dtrmv_zeros_part_elems(int n);
 size_t dtrmv_zeros_cnt_elems(int n);
 int dtrmv_zeros_launch(char uplo, int n, const double *A, int lda, const double *x, double *y,
                        double *part, unsigned *cnt, cudaStream_t s);
+// y = A x for a square n x n FP64 A, same kernel and scratch.
+int dgemv_chunk_launch(int n, const double *A, int lda, const double *x, double *y, double *part,
+                       unsigned *cnt, cudaStream_t s);
 
 // Reads and clears the workspace status word for `stream` (synchronises).
 int check_device_status(cudaStream_t stream);

@@ -398,12 +398,12 @@ gemv_rows_kernel(int m, int n, int k, T alpha, const T *__restrict__ A, int ldA,
     }
 }
 
-// y = A x for a square FP64 A whose other triangle holds zeros (LOWER: the
-// lower triangle), reading only the triangle and its 16 x 16 diagonal
-// blocks.  The rows go in blocks of 16
+// y = A x for a square FP64 A: SHAPE 1 reads the lower triangle (and its
+// 16 x 16 diagonal blocks), the other triangle holding zeros; SHAPE 0 the
+// upper triangle likewise; SHAPE 2 all of A.  The rows go in blocks of 16
 // (one 128-byte line of each column); a row block's columns -- [0, i0 + 16)
 // below the diagonal, [i0, n) above it -- are cut into chunks of `ch`
-// columns, and CTA (row block, chunk) sums its chunk with the row-tile
+// columns (all n for SHAPE 2), and CTA (row block, chunk) sums its chunk with the row-tile
 // GEMV's thread layout (16 column groups, 8 loads in flight per thread).
 // Every CTA but a row block's last chunk has the same work, so the SMs
 // finish together; with one CTA per whole row block the lengths run from 16
@@ -414,7 +414,7 @@ gemv_rows_kernel(int m, int n, int k, T alpha, const T *__restrict__ A, int ldA,
 // adds them in chunk order, so y does not depend on the CTAs' timing.
 // A separate kernel, so that the general one keeps its registers (and
 // residency).
-template <bool LOWER>
+template <int SHAPE>
 __global__ void __launch_bounds__(256)
 gemv_tri_kernel(int n, int ch, const double *__restrict__ A, int ldA, const double *__restrict__ x,
                 double *__restrict__ y, double *__restrict__ part, unsigned *__restrict__ cnt) {
@@ -424,8 +424,8 @@ gemv_tri_kernel(int n, int ch, const double *__restrict__ A, int ldA, const doub
     __shared__ int s_last;
     const int rb = blockIdx.x, c = blockIdx.y;
     const int i0 = rb * LR;
-    const int kb = LOWER ? 0 : i0;
-    const int ke = LOWER ? min(n, i0 + LR) : n;
+    const int kb = SHAPE == 0 ? i0 : 0;
+    const int ke = SHAPE == 1 ? min(n, i0 + LR) : n;
     const int nch = (ke - kb + ch - 1) / ch;
     if (c >= nch) return;                        // uniform over the CTA
     const int cb = kb + c * ch, ce = min(ke, cb + ch);
@@ -490,10 +490,11 @@ void launch_gemv_rows(bool tb, int m, int n, int k, T alpha, const T *A, int ldA
 // explicit-inverse preconditioner of the mixed solve.  `part` holds
 // dtrmv_zeros_part_elems(n) doubles and `cnt` dtrmv_zeros_cnt_elems(n)
 // counters, zero before the first call (each call leaves them zero).
-static int dtrmv_zeros_chunk(int n) {
-    // about 32 equal CTAs per SM over the n^2/2 triangle, at least 256 columns
+static int dtrmv_zeros_chunk(int n, bool full = false) {
+    // about 32 equal CTAs per SM over the n^2/2 triangle (n^2 for all of A),
+    // at least 256 columns
     const int sms = num_sms() > 0 ? num_sms() : 1;
-    const double per = (double)n * n / 2.0 / (16.0 * 32.0 * sms);
+    const double per = (double)n * n / (full ? 1.0 : 2.0) / (16.0 * 32.0 * sms);
     int ch = ((int)per + 15) / 16 * 16;
     return ch < 256 ? 256 : ch;
 }
@@ -509,8 +510,23 @@ int dtrmv_zeros_launch(char uplo, int n, const double *A, int lda, const double 
     const int ch = dtrmv_zeros_chunk(n);
     const dim3 grid(ceil_div(n, LR), ceil_div(n, ch));
     KTimer kt(kFamPrecond, s, (double)n * n, 4.0 * (double)n * n);
-    if (uplo == 'L') gemv_tri_kernel<true><<<grid, 256, 0, s>>>(n, ch, A, lda, x, y, part, cnt);
-    else gemv_tri_kernel<false><<<grid, 256, 0, s>>>(n, ch, A, lda, x, y, part, cnt);
+    if (uplo == 'L') gemv_tri_kernel<1><<<grid, 256, 0, s>>>(n, ch, A, lda, x, y, part, cnt);
+    else gemv_tri_kernel<0><<<grid, 256, 0, s>>>(n, ch, A, lda, x, y, part, cnt);
+    FG_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+// y = A x for a square n x n FP64 A in the same equal chunks (the Arnoldi
+// product of GMRES); the scratch of dtrmv_zeros_launch serves (a row of A
+// has at most as many chunks as the longest row of a triangle).
+int dgemv_chunk_launch(int n, const double *A, int lda, const double *x, double *y, double *part,
+                       unsigned *cnt, cudaStream_t s) {
+    if (n <= 0) return kOk;
+    constexpr int LR = 16;
+    const int ch = dtrmv_zeros_chunk(n, true);
+    const dim3 grid(ceil_div(n, LR), ceil_div(n, ch));
+    KTimer kt(kFamGemm, s, 2.0 * (double)n * n, 8.0 * (double)n * n);
+    gemv_tri_kernel<2><<<grid, 256, 0, s>>>(n, ch, A, lda, x, y, part, cnt);
     FG_CUDA(cudaGetLastError());
     return kOk;
 }

@@ -528,8 +528,10 @@ struct Solver {
     // the other triangle) and an n-vector between the two products
     bool pcinv = false;
     double *Linv = nullptr, *Uinv = nullptr, *pcTmp = nullptr;
-    double *pcPart = nullptr;                 // triangle GEMV chunk sums
-    unsigned *pcCnt = nullptr;                // and its per-row-block counters
+    // chunk sums and per-row-block counters of the chunked GEMVs (the
+    // Arnoldi product A v and the explicit-inverse products)
+    double *gvPart = nullptr;
+    unsigned *gvCnt = nullptr;
 };
 
 // ---------------------------------------------------------------------------
@@ -646,11 +648,10 @@ int pc_solve(Solver &S, const MT *F, int ldf, bool lower, double *x) {
 
 // ---- explicit-inverse preconditioner: build ---------------------------------
 // Workspace of the build: the two FP32 inverses (ld ldi), the product
-// scratch T, the 3xTF32 operand buffers, the FP64 inverses, an n-vector and
-// the triangle GEMV's chunk sums and counters.
+// scratch T, the 3xTF32 operand buffers, the FP64 inverses and an n-vector.
 struct InvPlan {
     int n, ldi, half;
-    size_t oL32, oU32, oT, oG, oL64, oU64, oTmp, oPart, oCnt, total;
+    size_t oL32, oU32, oT, oG, oL64, oU64, oTmp, total;
 };
 
 InvPlan inv_plan(int n) {
@@ -667,8 +668,6 @@ InvPlan inv_plan(int n) {
     p.oL64 = o; o += a256((size_t)n * n * sizeof(double));
     p.oU64 = o; o += a256((size_t)n * n * sizeof(double));
     p.oTmp = o; o += a256((size_t)n * sizeof(double));
-    p.oPart = o; o += a256(dtrmv_zeros_part_elems(n) * sizeof(double));
-    p.oCnt = o; o += a256(dtrmv_zeros_cnt_elems(n) * sizeof(unsigned));
     p.total = o;
     return p;
 }
@@ -721,9 +720,6 @@ int pcinv_prepare(Solver &S) {
     S.Linv = (double *)(base + p.oL64);
     S.Uinv = (double *)(base + p.oU64);
     S.pcTmp = (double *)(base + p.oTmp);
-    S.pcPart = (double *)(base + p.oPart);
-    S.pcCnt = (unsigned *)(base + p.oCnt);
-    FG_CUDA(cudaMemsetAsync(S.pcCnt, 0, dtrmv_zeros_cnt_elems(n) * sizeof(unsigned), S.s));
     static DeviceOnce onceL, onceU;
     int st = set_smem_once(onceL, (const void *)inv_diag_kernel<true>, PC_PREP_SMEM);
     if (st != kOk) return st;
@@ -808,9 +804,9 @@ int precond64(Solver &S, const double *src, double *dst) {
         FG_CUDA(cudaGetLastError());
     }
     if (S.pcinv) {
-        int st = dtrmv_zeros_launch('L', S.n, S.Linv, S.n, dst, S.pcTmp, S.pcPart, S.pcCnt, S.s);
+        int st = dtrmv_zeros_launch('L', S.n, S.Linv, S.n, dst, S.pcTmp, S.gvPart, S.gvCnt, S.s);
         if (st != kOk) return st;
-        return dtrmv_zeros_launch('U', S.n, S.Uinv, S.n, S.pcTmp, dst, S.pcPart, S.pcCnt, S.s);
+        return dtrmv_zeros_launch('U', S.n, S.Uinv, S.n, S.pcTmp, dst, S.gvPart, S.gvCnt, S.s);
     }
     if (S.pc) {
         int st;
@@ -893,9 +889,8 @@ int gmres_cycle(Solver &S, int j, double rtol, int *steps) {
     int k = 0;
     for (; k < M; ++k) {
         double *vk = S.V + (size_t)k * n;
-        // w = (LU)^-1 A v_k, all in FP64
-        FG_CUDA(cudaMemsetAsync(S.t, 0, sizeof(double) * n, S.s));
-        if ((st = dgemm_launch('N', 'N', n, 1, n, 1.0, S.A, S.ldA, vk, n, 0.0, S.t, n, S.s)) != kOk)
+        // w = (LU)^-1 A v_k, all in FP64; A v_k in equal chunks per CTA
+        if ((st = dgemv_chunk_launch(n, S.A, S.ldA, vk, S.t, S.gvPart, S.gvCnt, S.s)) != kOk)
             return st;
         if ((st = precond64(S, S.t, S.w)) != kOk) return st;
         // classical Gram-Schmidt, twice
@@ -1113,11 +1108,16 @@ int dgesv_mixed(int n, int nrhs, const double *A, int ldA, const double *B, int 
                 S.pc = !S.pcinv && pc_fits(n, split);
                 const size_t pB = S.pc ? pc_block_bytes(n) : 0;
                 const size_t tB = S.pc ? a256(2 * sizeof(unsigned long long) * (size_t)n) : 0;
-                char *p2 = (char *)workspace_slot(s, 2, vB + 2 * nB + 4 * pB + tB);
+                const size_t gB = a256(dtrmv_zeros_part_elems(n) * sizeof(double));
+                const size_t cB = a256(dtrmv_zeros_cnt_elems(n) * sizeof(unsigned));
+                char *p2 = (char *)workspace_slot(s, 2, vB + 2 * nB + 4 * pB + tB + gB + cB);
                 if (!p2) return kErrAlloc;
                 S.V = (double *)p2;
                 S.w = (double *)(p2 + vB);
                 S.t = (double *)(p2 + vB + nB);
+                S.gvPart = (double *)(p2 + vB + 2 * nB + 4 * pB + tB);
+                S.gvCnt = (unsigned *)(p2 + vB + 2 * nB + 4 * pB + tB + gB);
+                FG_CUDA(cudaMemsetAsync(S.gvCnt, 0, cB, s));
                 if (S.pc) {
                     char *pp = p2 + vB + 2 * nB;
                     S.pcDL = (double *)pp;

@@ -454,10 +454,11 @@ long long flens_gb300_device_alloc_count(void);
  * count <= 0 clears it. */
 void flens_gb300_test_fail_device_allocs(int count);
 
-/* Test hook: the mixed solve's explicit-inverse preconditioner product on its
- * own, y = A x for an n x n FP64 A whose other triangle (uplo 'L': above the
- * diagonal, 'U': below) holds zeros; only the triangle and the zeros inside
- * its 16 x 16 diagonal blocks are read.  Scratch
+/* Test hook: the mixed solve's chunked GEMVs on their own.  uplo 'L' or 'U':
+ * the explicit-inverse preconditioner product, y = A x for an n x n FP64 A
+ * whose other triangle (above the diagonal for 'L', below for 'U') holds
+ * zeros; only the triangle and the zeros inside its 16 x 16 diagonal blocks
+ * are read.  uplo 'G': the Arnoldi product y = A x over all of A.  Scratch
  * `part` (*part_elems doubles) and `cnt` (*cnt_elems counters, zero before
  * the first call; every call leaves them zero).  With part == NULL the call
  * only reports the two sizes.  Returns 0, -1/-2/-4 for uplo/n/ldA, or a

@@ -320,23 +320,25 @@ def test_mixed_explicit_inverse_preconditioner(cuda, prec):
     assert fwd <= 1e2 * 1e3 * EPS, fwd
 
 
-@pytest.mark.parametrize("uplo", ["L", "U"])
+@pytest.mark.parametrize("uplo", ["L", "U", "G"])
 @pytest.mark.parametrize("n", [1, 17, 300, 2048, 5000])
-def test_triangle_gemv_of_the_explicit_inverse(cuda, uplo, n):
+def test_chunked_gemv_of_the_mixed_solve(cuda, uplo, n):
     """The preconditioner's product y = T x over one triangle T (the other
-    holding zeros): equal to the FP64 product to rounding, bitwise the same
-    on a repeated call (the chunk sums of a row block are added in chunk
-    order whatever the CTAs' timing), and the row blocks' counters back at
-    zero after each call.  The kernel reads the triangle and the zeros of its
-    16 x 16 diagonal blocks, nothing else: the rest of the other triangle is
-    NaN here."""
+    holding zeros; uplo L and U) and the Arnoldi product over all of A
+    (uplo G): equal to the FP64 product to rounding, bitwise the same on a
+    repeated call (the chunk sums of a row block are added in chunk order
+    whatever the CTAs' timing), and the row blocks' counters back at zero
+    after each call.  For a triangle the kernel reads the triangle and the
+    zeros of its 16 x 16 diagonal blocks, nothing else: the rest of the
+    other triangle is NaN here."""
     import torch
     g = torch.Generator(device=cuda).manual_seed(n)
     T = torch.rand((n, n), generator=g, dtype=torch.float64, device=cuda) * 2 - 1
-    T = torch.tril(T) if uplo == "L" else torch.triu(T)
+    if uplo != "G":
+        T = torch.tril(T) if uplo == "L" else torch.triu(T)
     i = torch.arange(n, device=cuda).view(-1, 1) // 16
     j = torch.arange(n, device=cuda).view(1, -1) // 16
-    read = (j <= i) if uplo == "L" else (j >= i)
+    read = (j <= i) if uplo == "L" else (j >= i) if uplo == "U" else (i >= 0) & (j >= 0)
     Tp = fg.to_colmajor(torch.where(read, T, torch.full_like(T, float("nan"))))
     x = torch.rand(n, generator=g, dtype=torch.float64, device=cuda) * 2 - 1
     f = fg.lib().flens_gb300_test_trmv_zeros
