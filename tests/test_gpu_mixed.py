@@ -7,7 +7,8 @@ factors of Householder QR of seeded Gaussian matrices, s geometric from 1 to
 independently recomputed normwise backward error
 ||b - Ax||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= 10 n eps64, and the
 forward error against x_true <= kappa * 1e3 * eps64 (the error a backward
-stable FP64 solve can have).
+stable FP64 solve can have) for n below 1000; beyond, kappa * 10 n eps64,
+since the solver stops once the backward error is below n eps64.
 """
 import ctypes
 
@@ -304,20 +305,25 @@ def test_sgetrf_tc_shapes(cuda, m, n, prec):
     assert (buf.t()[m:, :] == 0).all()
 
 
-@pytest.mark.parametrize("prec", ["bf16", "fp8x2"])
-def test_mixed_explicit_inverse_preconditioner(cuda, prec):
+@pytest.mark.parametrize("prec,n", [("bf16", 2048), ("fp8x2", 2048), ("bf16", 2100)])
+def test_mixed_explicit_inverse_preconditioner(cuda, prec, n):
     """BF16 and FP8 factors at n >= 2048 take GMRES with the explicit-inverse
     preconditioner (L^-1, U^-1 formed once by 3xTF32 block recursion, applied
     as FP64 products); the solve must reach 10 n eps as with the chained
-    substitution (17 and 22 steps at this size, kappa = 1e2)."""
-    n = 2048
+    substitution (17 and 22 steps at n = 2048, kappa = 1e2).  n = 2100 leaves
+    a 52-row last diagonal block, halves of the recursion that are not
+    multiples of 64 and a 4-row last row block in the chunked products.
+    The solver stops once the backward error is below n eps, so the forward
+    error may reach kappa times that: the bar here is kappa * 10 n eps (the
+    module's kappa * 1e3 eps assumes n below 1000 or an earlier stop; at
+    n = 2100 a solve measured 4.3e-11, kappa * n eps = 4.7e-11)."""
     A, b, x = make_system(cuda, n, 1e2, 1, 23)
     st, X, it, be, inf = dgesv_mixed(A, b, prec, "auto")
     assert st == 0 and inf == 0, (st, fg.last_error(), it, be)
     assert it <= 60, it
     assert backward_error(A, X, b) <= 10 * n * EPS
     fwd = ((X - x).abs().max() / x.abs().max()).item()
-    assert fwd <= 1e2 * 1e3 * EPS, fwd
+    assert fwd <= 1e2 * 10 * n * EPS, fwd
 
 
 @pytest.mark.parametrize("uplo", ["L", "U", "G"])
