@@ -20,7 +20,9 @@
 //                       a separate barrier; then every CTA swaps, scales and
 //                       applies the rank-1 update to its own rows.  At the end
 //                       it turns the jb interchanges into a list of
-//                       (destination row, source row) moves.
+//                       (destination row, source row) moves.  FP32 storage
+//                       uses panel32_kernel: FP32 arithmetic, and the key
+//                       published in one word with its sequence number.
 //     laswp_pairs_kernel applies those moves to every column outside the
 //                       panel, one warp per column (loads, then stores).
 //     dtrsm_launch      U12 = L11^-1 A12
@@ -36,6 +38,7 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <mutex>
 
 namespace fg {
@@ -130,6 +133,58 @@ __device__ __forceinline__ void warp_argmax(unsigned long long &k, int &i) {
     const unsigned cand = (hi == mhi && lo == mlo) ? (unsigned)i : 0xffffffffu;
     i = (int)__reduce_min_sync(0xffffffffu, cand);
     k = ((unsigned long long)mhi << 32) | mlo;
+}
+
+// Block 0, warp 0 of a panel (all 32 lanes): the jb interchanges of the
+// panel at column j0 (ipiv, written by this warp's lane 0 during the panel)
+// as a list of (destination row, source row) moves, compacted to the moves
+// that change something, into ps.swap_dst / swap_src / swap_cnt.
+__device__ __forceinline__ void panel_moves(int jb, int j0, const int *ipiv, PanelScratch ps,
+                                            int *s_list_row, int *s_list_src, int lane) {
+    for (int i = lane; i < jb; i += 32) {
+        s_list_row[i] = j0 + i;
+        s_list_src[i] = j0 + i;
+    }
+    __syncwarp();
+    int cnt = jb;
+    for (int i = 0; i < jb; ++i) {
+        const int p = ipiv[j0 + i] - 1;
+        int pos;
+        if (p < j0 + jb) {
+            pos = p - j0;
+        } else {
+            int found = -1;
+            for (int base = jb; base < cnt; base += 32) {
+                const int e = base + lane;
+                const unsigned hit = __ballot_sync(0xffffffffu, e < cnt && s_list_row[e] == p);
+                if (hit) { found = base + __ffs(hit) - 1; break; }
+            }
+            if (found < 0) {
+                found = cnt;
+                if (lane == 0) { s_list_row[cnt] = p; s_list_src[cnt] = p; }
+                ++cnt;
+            }
+            pos = found;
+        }
+        __syncwarp();
+        if (lane == 0 && pos != i) {
+            const int t = s_list_src[i];
+            s_list_src[i] = s_list_src[pos];
+            s_list_src[pos] = t;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        int k = 0;
+        for (int e = 0; e < cnt; ++e) {
+            if (s_list_row[e] != s_list_src[e]) {
+                ps.swap_dst[k] = s_list_row[e];
+                ps.swap_src[k] = s_list_src[e];
+                ++k;
+            }
+        }
+        *ps.swap_cnt = k;
+    }
 }
 
 // Panel factorisation, tf2 semantics (flens/lapack/ge/tf2.tcc:56-136).
@@ -417,53 +472,311 @@ panel_kernel(T *__restrict__ A, int lda, int mp, int jb, int j0,
     }
 
     // -- block 0, warp 0: the jb interchanges as (dst, src) row moves.
-    if (b == 0 && tid < 32) {
-        for (int i = lane; i < jb; i += 32) {
-            s_list_row[i] = j0 + i;
-            s_list_src[i] = j0 + i;
+    if (b == 0 && tid < 32) panel_moves(jb, j0, ipiv, ps, s_list_row, s_list_src, lane);
+}
+
+// ---- the panel of the FP32-storage LU ---------------------------------------
+// Same algorithm and thread layout as panel_kernel, in FP32 arithmetic (the
+// reference's tf2 instantiated for float: slamch's safe minimum is FLT_MIN)
+// and with a shorter exchange.  A float's pivot key fits in 32 bits, so each
+// CTA publishes its candidate as ONE 64-bit word, (sequence << 32) | key,
+// stored as soon as the CTA's argmax is known and before anything else; the
+// load that finds a slot current also returns its key, so the pivot is
+// settled after one round trip through L2 instead of a release store that
+// waits for the rows, a sequence poll and a dependent key load.  The rows
+// (candidate and row jj) and the candidate's index follow under their own
+// release-stored sequence word, and only the two rows the pivot needs are
+// waited for.  Equal keys go to the lower CTA, whose rows come first: with
+// each CTA's own first maximum this is iamax's first-maximum rule.
+struct PanelSlot32 {
+    unsigned long long head;   // (sequence << 32) | pivot key (pivot_key32)
+    unsigned long long rseq;   // sequence, release-stored after row/rowjj/idx
+    int idx;
+    int pad[3];
+    float row[PANEL_NB];
+    float rowjj[PANEL_NB];
+};
+static_assert(2 * PANEL_GMAX * sizeof(PanelSlot32) <= kSlotBytes, "FP32 slots fit the exchange area");
+
+// 0 = no candidate, 1 = NaN, |x| bits + 2 otherwise (at most 0x7f800002)
+__device__ __forceinline__ unsigned long long pivot_key32(float x) {
+    const unsigned a = __float_as_uint(x) & 0x7fffffffu;
+    return a > 0x7f800000u ? 1ull : (unsigned long long)a + 2ull;
+}
+
+__device__ __forceinline__ void st_relaxed(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+template <bool DEFER>
+__global__ void __launch_bounds__(PANEL_THREADS, DEFER ? 1 : 4)
+panel32_kernel(float *__restrict__ A, int lda, int mp, int jb, int j0,
+               int *__restrict__ ipiv, int *__restrict__ info, int *__restrict__ status,
+               PanelScratch ps, int R, unsigned long long epoch) {
+    extern __shared__ double S32_raw[];
+    float *S = reinterpret_cast<float *>(S32_raw);
+    constexpr int NW = PANEL_THREADS / 32;
+    __shared__ float prow[PANEL_NB], orow[PANEL_NB];
+    __shared__ unsigned long long red_k[NW], red_k2[NW];
+    __shared__ int red_i[NW], red_i2[NW];
+    __shared__ int s_gs, s_abort;
+    __shared__ float s_pv, s_rinv;
+    __shared__ int s_list_row[2 * PANEL_NB], s_list_src[2 * PANEL_NB];
+    PanelSlot32 *slots = reinterpret_cast<PanelSlot32 *>(ps.slots);
+
+    const int b = blockIdx.x, G = gridDim.x, tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int rb = b * R;
+    const int re = min(mp, rb + R);
+    const int nr = max(0, re - rb);
+    const int W = nr <= 32 ? 8 : nr <= 64 ? 4 : nr <= 128 ? 2 : 1;
+
+    for (int e = tid; e < nr * jb; e += PANEL_THREADS) {
+        const int r = e % nr, c = e / nr;
+        S[c * R + r] = A[(size_t)(rb + r) + (size_t)c * lda];
+    }
+    if (tid == 0) s_abort = 0;
+    __syncthreads();
+
+    unsigned long long nbk = kKeyNone;
+    int nbi = INT_MAX;
+    for (int r = tid; r < nr; r += PANEL_THREADS) {
+        const unsigned long long key = pivot_key32(S[r]);
+        if (better(key, rb + r, nbk, nbi)) { nbk = key; nbi = rb + r; }
+    }
+
+    const bool lanes = W > 1, defer = DEFER && lanes;
+    const float *dP = nullptr;
+    int d_jj = -1, d_gs = -1;
+    bool d_swap = false;
+    bool pend = false, pend_gs = false;
+    float pend_l = 0.0f;
+    for (int jj = 0; jj < jb; ++jj) {
+        const int par = jj & 1;
+        const unsigned long long want = epoch * 128ull + (unsigned long long)jj + 1ull;
+        const unsigned want32 = (unsigned)want;
+        // -- [A] this CTA's candidate among its rows g >= jj
+        unsigned long long k = nbk;
+        int i = nbi;
+        warp_argmax(k, i);
+        if (lane == 0) { red_k[warp] = k; red_i[warp] = i; }
+        __syncthreads();                                             // B1
+        if (warp == 0) {
+            // -- [B] the key first, in one word with its sequence number;
+            // then the rows under their own sequence word
+            k = lane < NW ? red_k[lane] : kKeyNone;
+            i = lane < NW ? red_i[lane] : INT_MAX;
+            warp_argmax(k, i);
+            PanelSlot32 *mine = &slots[par * PANEL_GMAX + b];
+            if (lane == 0) st_relaxed(&mine->head, ((unsigned long long)want32 << 32) | k);
+            auto fin = [&](int x, int c) -> float {
+                if (d_jj < 0 || c < d_jj + 2) return S[c * R + x];
+                const float src = (d_swap && rb + x == d_gs) ? orow[c] : S[c * R + x];
+                return fmaf(-dP[c], S[d_jj * R + x], src);
+            };
+            const bool has_i = i != INT_MAX, has_jj = jj >= rb && jj < re;
+            float vi[2] = {0.0f, 0.0f}, vj[2] = {0.0f, 0.0f};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int c = lane + 32 * h;
+                if (c < jb) {
+                    if (has_i) vi[h] = fin(i - rb, c);
+                    if (has_jj) vj[h] = fin(jj - rb, c);
+                }
+            }
+            if (defer) named_bar_arrive(1, PANEL_THREADS);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int c = lane + 32 * h;
+                if (c < jb) {
+                    if (has_i) mine->row[c] = vi[h];
+                    if (has_jj) mine->rowjj[c] = vj[h];
+                }
+            }
+            if (lane == 0) mine->idx = i;
+            __syncwarp();
+            if (lane == 0) st_release(&mine->rseq, want);
+        } else if (defer) {
+            named_bar_sync(1, PANEL_THREADS);
         }
-        __syncwarp();
-        int cnt = jb;
-        for (int i = 0; i < jb; ++i) {
-            const int p = ipiv[j0 + i] - 1;       // written by this warp's lane 0 above
-            int pos;
-            if (p < j0 + jb) {
-                pos = p - j0;
+        // -- [E2] the pending update of column jj - 1: columns >= jj + 1
+        if (pend) {
+            const int r = tid / W, q = tid % W;
+            const float *old = pend_gs ? orow : nullptr;
+            int c = d_jj + 2 + q;
+            for (; c + 3 * W < jb; c += 4 * W) {
+                float v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = old ? old[c + u * W] : S[(c + u * W) * R + r];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) S[(c + u * W) * R + r] = fmaf(-dP[c + u * W], pend_l, v[u]);
+            }
+            for (; c < jb; c += W) S[c * R + r] = fmaf(-dP[c], pend_l, old ? old[c] : S[c * R + r]);
+            pend = false;
+        }
+        // -- [C] thread t < G waits for the key word of slot t; the winner is
+        // the largest key, the lower CTA on equal keys
+        unsigned long long gk = kKeyNone;
+        int gc = INT_MAX;
+        if (tid < G) {
+            const PanelSlot32 *sl = &slots[par * PANEL_GMAX + tid];
+            unsigned spins = 0;
+            unsigned long long h;
+            while (((h = ld_acquire(&sl->head)) >> 32) != (unsigned long long)want32) {
+                if (++spins > kSpinLimit) {
+                    atomicOr(status, kDevBarrierTimeout);
+                    s_abort = 1;
+                    break;
+                }
+                if (spins > 32) __nanosleep(32);
+            }
+            gk = h & 0xffffffffull;
+            gc = tid;
+        }
+        if (warp * 32 < G) {                                          // warp-uniform
+            warp_argmax(gk, gc);
+            if (lane == 0) { red_k2[warp] = gk; red_i2[warp] = gc; }
+        }
+        __syncthreads();                                             // B2
+        if (s_abort) return;
+        if (warp == 0) {
+            const int nw = (G + 31) / 32;
+            gk = lane < nw ? red_k2[lane] : kKeyNone;
+            gc = lane < nw ? red_i2[lane] : INT_MAX;
+            warp_argmax(gk, gc);
+            // -- [D] the winner's row and row jj, once their owners have
+            // stored them (bounded waits, every lane)
+            const PanelSlot32 *sj = &slots[par * PANEL_GMAX + jj / R];
+            const PanelSlot32 *sw = &slots[par * PANEL_GMAX + gc];
+            bool ok = true;
+            {
+                unsigned spins = 0;
+                while (ld_acquire(&sw->rseq) != want || ld_acquire(&sj->rseq) != want) {
+                    if (++spins > kSpinLimit) {
+                        ok = false;
+                        break;
+                    }
+                    if (spins > 32) __nanosleep(32);
+                }
+            }
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) {
+                    atomicOr(status, kDevBarrierTimeout);
+                    s_abort = 1;
+                }
             } else {
-                int found = -1;
-                for (int base = jb; base < cnt; base += 32) {
-                    const int e = base + lane;
-                    const unsigned hit = __ballot_sync(0xffffffffu, e < cnt && s_list_row[e] == p);
-                    if (hit) { found = base + __ffs(hit) - 1; break; }
+                for (int c = lane; c < jb; c += 32) {
+                    orow[c] = __ldcg(&sj->rowjj[c]);
+                    prow[c] = __ldcg(&sw->row[c]);
                 }
-                if (found < 0) {
-                    found = cnt;
-                    if (lane == 0) { s_list_row[cnt] = p; s_list_src[cnt] = p; }
-                    ++cnt;
+                const int gi = __ldcg(&sw->idx);
+                __syncwarp();
+                if (lane == 0) {
+                    const float ajj = orow[jj];
+                    const int gs = isnan(ajj) ? jj : gi;
+                    const float pv = (gs == jj) ? ajj : prow[jj];
+                    s_gs = gs;
+                    s_pv = pv;
+                    s_rinv = (pv != 0.0f && fabsf(pv) >= FLT_MIN) ? 1.0f / pv : 0.0f;
+                    if (b == 0) {
+                        ipiv[j0 + jj] = j0 + gs + 1;
+                        if (pv == 0.0f && *info == 0) *info = j0 + jj + 1;
+                    }
                 }
-                pos = found;
             }
-            __syncwarp();
-            if (lane == 0 && pos != i) {
-                const int t = s_list_src[i];
-                s_list_src[i] = s_list_src[pos];
-                s_list_src[pos] = t;
-            }
-            __syncwarp();
         }
-        // compact to the moves that change something
-        if (lane == 0) {
-            int k = 0;
-            for (int e = 0; e < cnt; ++e) {
-                if (s_list_row[e] != s_list_src[e]) {
-                    ps.swap_dst[k] = s_list_row[e];
-                    ps.swap_src[k] = s_list_src[e];
-                    ++k;
+        __syncthreads();                                             // B3
+        if (s_abort) return;
+        const int gs = s_gs;
+        const float pv = s_pv, rinv = s_rinv;
+        const bool swap = (pv != 0.0f) && (gs != jj);
+        const float *P = (gs == jj) ? orow : prow;                   // new row jj
+
+        // -- [E] per owned row: interchange, scaling, rank-1 update of the
+        // columns > jj (deferred beyond jj + 1 when W > 1), and the pivot key
+        // for column jj+1
+        nbk = kKeyNone;
+        nbi = INT_MAX;
+        if (lanes) {
+            const int r = tid / W, q = tid % W;
+            const bool act = r < nr;
+            const int g = rb + r;
+            const bool to_jj = act && swap && g == jj, from_gs = act && swap && g == gs;
+            float l0 = 0.0f;
+            if (act && q == 0) l0 = from_gs ? orow[jj] : S[jj * R + r];
+            float l = __shfl_sync(0xffffffffu, l0, lane & ~(W - 1));
+            if (to_jj) {
+                for (int c = q; c < jb; c += W) S[c * R + r] = P[c];
+            } else if (act && g > jj) {
+                if (from_gs)
+                    for (int c = q; c < jj; c += W) S[c * R + r] = orow[c];
+                if (pv != 0.0f) l = (rinv != 0.0f) ? l * rinv : l / pv;
+                if (q == 0 && pv != 0.0f) S[jj * R + r] = l;
+                const float *old = from_gs ? orow : nullptr;
+                if (defer) {
+                    if (q == 0 && jj + 1 < jb) {
+                        const int c = jj + 1;
+                        const float v = fmaf(-P[c], l, old ? old[c] : S[c * R + r]);
+                        S[c * R + r] = v;
+                        nbk = pivot_key32(v);
+                        nbi = g;
+                    }
+                    pend = jj + 2 + q < jb;
+                    pend_gs = from_gs;
+                    pend_l = l;
+                } else {
+                    int c = jj + 1 + q;
+                    for (; c + 3 * W < jb; c += 4 * W) {
+                        float v[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) v[u] = old ? old[c + u * W] : S[(c + u * W) * R + r];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) S[(c + u * W) * R + r] = fmaf(-P[c + u * W], l, v[u]);
+                    }
+                    for (; c < jb; c += W) S[c * R + r] = fmaf(-P[c], l, old ? old[c] : S[c * R + r]);
+                    if (q == 0 && jj + 1 < jb) {
+                        nbk = pivot_key32(S[(jj + 1) * R + r]);
+                        nbi = g;
+                    }
                 }
             }
-            *ps.swap_cnt = k;
+            if (defer) {
+                dP = P;
+                d_jj = jj;
+                d_gs = gs;
+                d_swap = swap;
+            }
+        } else
+        for (int r = tid; r < nr; r += PANEL_THREADS) {
+            const int g = rb + r;
+            if (swap && g == jj) {
+                for (int c = 0; c < jb; ++c) S[c * R + r] = P[c];
+            } else if (swap && g == gs) {
+                for (int c = 0; c < jb; ++c) S[c * R + r] = orow[c];
+            }
+            if (g > jj) {
+                float l = S[jj * R + r];
+                if (pv != 0.0f) {
+                    l = (rinv != 0.0f) ? l * rinv : l / pv;
+                    S[jj * R + r] = l;
+                }
+                for (int c = jj + 1; c < jb; ++c) S[c * R + r] = fmaf(-P[c], l, S[c * R + r]);
+                if (jj + 1 < jb) {
+                    const unsigned long long key = pivot_key32(S[(jj + 1) * R + r]);
+                    if (better(key, g, nbk, nbi)) { nbk = key; nbi = g; }
+                }
+            }
         }
     }
+    __syncthreads();
+
+    for (int e = tid; e < nr * jb; e += PANEL_THREADS) {
+        const int r = e % nr, c = e / nr;
+        A[(size_t)(rb + r) + (size_t)c * lda] = S[c * R + r];
+    }
+
+    // -- block 0, warp 0: the jb interchanges as (dst, src) row moves.
+    if (b == 0 && tid < 32) panel_moves(jb, j0, ipiv, ps, s_list_row, s_list_src, lane);
 }
 
 // Apply the panel's row moves to columns [0, cSplit) and [cSplit+skip, ...),
@@ -552,8 +865,6 @@ __global__ void copy_back_kernel(int nrows, int ncols, const T *__restrict__ tmp
     }
 }
 
-bool g_panel_attr_set = false;
-
 template <typename T>
 int trsm_t(char side, char uplo, char ta, char diag, int m, int n, T alpha, const T *A, int ldA,
            T *B, int ldB, cudaStream_t s);
@@ -601,6 +912,17 @@ int outer_update<float>(int m, int n, int k, const float *L21, int ldL, const fl
         return kErrUnsupported;
     }
     return tc_trailing_update(tc_kind, m, n, k, L21, ldL, U12, ldU, A22, ldA22, tc_buf, s);
+}
+
+// The FP32 panel (panel32_kernel) for FP32 storage: on unless
+// FLENS_GB300_PANEL32=0, which factors FP32 panels with panel_kernel<float>
+// (FP64 arithmetic on the FP32 values).
+bool panel32_enabled() {
+    static bool on = [] {
+        const char *e = getenv("FLENS_GB300_PANEL32");
+        return !(e && atoi(e) == 0);
+    }();
+    return on;
 }
 
 // Look-ahead in the blocked LU: on unless FLENS_GB300_LOOKAHEAD=0.
@@ -745,11 +1067,15 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int 
     void *tc_buf = (char *)w->buf + (panel_scratch_bytes() + 255) / 256 * 256;
     FG_CUDA(cudaMemsetAsync(ps.slots, 0, kSlotBytes, stream));
     unsigned long long epoch = 0;
-    static DeviceOnce once;
+    // FP32 storage: the FP32 panel (panel32_kernel); FP64: panel_kernel
+    const bool f32 = std::is_same<T, float>::value && panel32_enabled();
+    const void *panel_fn[2] = {
+        f32 ? (const void *)panel32_kernel<false> : (const void *)panel_kernel<T, false>,
+        f32 ? (const void *)panel32_kernel<true> : (const void *)panel_kernel<T, true>};
     {
-        static DeviceOnce once_d;
-        int st0 = set_smem_once(once, (const void *)panel_kernel<T, false>, (int)PANEL_SMEM_MAX);
-        if (st0 == kOk) st0 = set_smem_once(once_d, (const void *)panel_kernel<T, true>, (int)PANEL_SMEM_MAX);
+        static DeviceOnce once, once_d, once_f, once_fd;
+        int st0 = set_smem_once(f32 ? once_f : once, panel_fn[0], (int)PANEL_SMEM_MAX);
+        if (st0 == kOk) st0 = set_smem_once(f32 ? once_fd : once_d, panel_fn[1], (int)PANEL_SMEM_MAX);
         if (st0 != kOk) return st0;
     }
     int sms = num_sms();
@@ -788,9 +1114,11 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int 
         if (R < PANEL_RMIN) R = PANEL_RMIN;
         // panel width: the reference's 64, narrowed only if a CTA's rows
         // would not fit in shared memory (very tall matrices)
+        // (panel_kernel holds the panel in FP64, panel32_kernel in FP32)
+        const size_t es = f32 ? sizeof(float) : sizeof(double);
         int nb = PANEL_NB;
-        while (nb > 1 && (size_t)R * nb * sizeof(double) > PANEL_SMEM_MAX) nb >>= 1;
-        if ((size_t)R * nb * sizeof(double) > PANEL_SMEM_MAX) {
+        while (nb > 1 && (size_t)R * nb * es > PANEL_SMEM_MAX) nb >>= 1;
+        if ((size_t)R * nb * es > PANEL_SMEM_MAX) {
             set_last_error("getrf: m=%d too tall for the shared-memory panel", m);
             return kErrUnsupported;
         }
@@ -800,12 +1128,12 @@ int getrf_t(int m, int n, T *A, int ldA, int *ipiv, int *info, int tc_kind, int 
         T *Ap = A + j + (size_t)j * ldA;
         int *status = w->status;
         int j0 = j;
-        size_t smem = (size_t)R * jb * sizeof(double);
+        size_t smem = (size_t)R * jb * es;
         ++epoch;
         void *args[] = {&Ap, &ldA, &mp, &jb, &j0, &ipiv, &info, &status, &ps, &R, &epoch};
         KTimer ktp(kFamPanel, s, (double)mp * jb * jb - (double)jb * jb * jb / 3.0,
                    2.0 * sizeof(T) * (double)mp * jb);
-        const void *fn = defer ? (const void *)panel_kernel<T, true> : (const void *)panel_kernel<T, false>;
+        const void *fn = panel_fn[defer ? 1 : 0];
         FG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(G),
                                             dim3(PANEL_THREADS), args, smem, s));
         *jb_out = jb;
