@@ -2,7 +2,7 @@
 // cores, FP64 iterative refinement (classical, or GMRES-IR) to FP64 accuracy.
 //
 //   1. A32 = fp32(A); LU of A32 with partial pivoting (sgetrf_launch): the
-//      panel's pivot search and scaling run in FP64 on FP32 storage, the
+//      panels in FP32 arithmetic (the reference's tf2 for float), the
 //      trailing updates A22 -= A21*U12 on the tensor cores in TF32, BF16,
 //      FP8 e4m3 (per-row/column scaled), FP32-accurate 3xTF32, or FP8 e4m3
 //      with each scaled entry split into two or three e4m3 terms (precision

@@ -311,9 +311,11 @@ int flens_gb300_sgemm_tc(int precision, char transA, char transB, int m, int n,
 
 /* LU with partial pivoting of an m x n FP32 matrix in device memory (column-
  * major, 1-based pivots), the factorisation of the precision form: panels
- * in FP64 arithmetic on the FP32 storage (pivot search and scaling as in
- * flens_gb300_dgetrf), U12 = L11^-1 A12 in FP32, and the trailing updates
- * A22 -= L21 U12 on the tensor cores in `precision` (0, 1, 2, 3, 5 or 6 as
+ * in FP32 arithmetic (the reference's tf2 for float: first-maximum pivot
+ * search, scaling by the reciprocal above FLT_MIN; FLENS_GB300_PANEL32=0
+ * runs them in FP64 arithmetic instead), U12 = L11^-1 A12 in FP32, and the
+ * trailing updates A22 -= L21 U12 on the tensor cores in `precision`
+ * (0, 1, 2, 3, 5 or 6 as
  * for flens_gb300_sgemm_tc) or, for precision -1, on the CUDA cores in
  * FP32.  *info (device) as dgetrf's.  The counterpart of FLENS's float trf
  * (flens/lapack/ge/trf.tcc:59-152).  Async on stream. */
