@@ -219,7 +219,8 @@ def test_sgetrf_tc_factor_error_per_precision(cuda):
     """flens_gb300_sgetrf_tc on the mixed-solve matrix family (n = 512,
     kappa = 1e2): ||PA - LU||_F / ||A||_F per trailing-update precision.  The
     split e4m3 forms must match a torch emulation of the same factorisation
-    to 25% (the GPU's U12 solve is FP32, the emulation's FP64), and the
+    to 25% (the GPU's panels and U12 solve are FP32, the emulation's FP64:
+    the e4m3 product errors dominate both), and the
     precisions must order as their unit roundoffs do: FP32 (CUDA cores and
     3xTF32) << three-term e4m3 (~2^-12) < TF32 (2^-11) < two-term e4m3 and
     BF16 (~2^-8) < one-term e4m3 (2^-4)."""
